@@ -1,0 +1,131 @@
+/* CPU oracle for the matrix-free hp-FEM operator path of dohp.
+ *
+ * TEST INFRASTRUCTURE ONLY. This library is the checker: the parity tests, the
+ * smoke check and the CPU-baseline leg of the benchmark call it. The product
+ * library (dohp_gb300) never links, loads or calls it.
+ *
+ * Every routine restates the algorithm of the reference source file:line it
+ * cites (paths relative to the dohp project root). Plain C99, double precision.
+ */
+#ifndef DOHP_ORACLE_H
+#define DOHP_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------- 1-D bases and rules (src/jacobi/impls/tensor/polylib.c, tensor.c) ---- */
+void or_gauss(int n, double *x, double *w);   /* Gauss-Legendre, ascending (polylib zwgj, alpha=beta=0) */
+void or_lobatto(int n, double *x, double *w); /* Gauss-Lobatto-Legendre, ascending (polylib zwglj) */
+/* TensorBasisCreate (src/jacobi/impls/tensor/tensor.c:22-109): P GLL nodes, Q rule points.
+ * interp/deriv are [Q][P] row-major; node/weight are the GLL nodes/weights. */
+int or_tensor_basis(int P, int Q, const double *rcoord, double *interp, double *deriv, double *node, double *weight);
+/* TensorGetRule (src/jacobi/quadrature/impls/tensor/tensorquad.c:51-118).
+ * method: 0 FAST, 1 SPARSE, 2 SELF; family: 0 Gauss-Legendre, 1 Gauss-Lobatto.
+ * Returns the rule size, or -1 on error. x/w need room for the size (<= 100). */
+int or_rule_1d(int method, int family, int order, double *x, double *w);
+/* dRulePatchSetup_Tensor (tensorquad.c:120-169): patch index/weight tables for a 3-D tensor rule
+ * of sizes Q[3]; returns npatches, writes patchsize; ind/weight sized Q0*Q1*Q2. The weight table
+ * keeps the reference's z-weight index (weight[jelem] for z). */
+int or_rule_patches(int method, const int Q[3], const double *w0, const double *w1, const double *w2,
+                    int *patchsize, int *ind, double *weight);
+
+/* ---------------- element kernels (src/jacobi/impls/tensor/efstopo.c, inlinetmulthex.h) ---- */
+#define OR_INTERP 40001
+#define OR_INTERP_TRANSPOSE 40002
+#define OR_GRAD 40003
+#define OR_GRAD_TRANSPOSE 40004
+#define OR_INSERT 1
+#define OR_ADD 2
+/* TensorMult_Hex_nounroll (inlinetmulthex.h:19-100) */
+void or_tensor_mult_hex(int D, const int P[3], const int Q[3], const double *A[3], const double *in, double *out, int imode);
+/* dEFSApply_Tensor_Hex (efstopo.c:368-423) for basis tables b (interp, deriv per direction). */
+int or_efs_apply_hex(const int P[3], const int Q[3], const double *interp[3], const double *deriv[3],
+                     const double *jinv, int D, const double *in, double *out, int amode, int imode);
+/* dGeomInvert3 (include/dohpgeom.h:57-79) */
+void or_invert3(const double a[9], double b[9], double *det);
+/* dEFSGetExplicitSparse_Tensor_Hex (efstopo.c:660-717); cjinv indexed as the reference does. */
+int or_explicit_sparse_hex(int px, int py, int pz, int npatches, int Q, const int *qidx, const double *cjinv,
+                           int eoffset, int *P, int *eidx, double *interp, double *deriv);
+
+/* dEFSGetExplicitSparse for a tensor hex EFS: the Q1 sub-cell path when the patches match the GLL
+ * sub-cells (efstopo.c:668-671), else the dense _Basic fallback (jacobi.c:611-643). */
+int or_explicit_sparse(const int P3[3], const int Q3[3], const double *interp[3], const double *deriv[3],
+                       int npatches, int Q, const int *qidx, const double *cjinv, int eoffset,
+                       int *P, int *eidx, double *ointerp, double *oderiv);
+
+/* ---------------- structured block mesh + function space ---------------- */
+typedef struct or_fs or_fs;
+/* Block mesh with nx*ny*nz vertices on box[6]={x0,x1,y0,y1,z0,z1} following the entity creation order of
+ * dMeshGenerateBlock (src/fs/mesh/interface/genblock.c:206-402). Interior vertices are moved by
+ * U[-perturb*h, perturb*h] per coordinate, drawn from splitmix64(seed) in vertex order.
+ * elem_degree: NULL for uniform `degree`, else one isotropic degree per element (region order).
+ * dirichlet_mask: bit0 = NEUMANN_SET 100 (walls), bit1 = 200 (top), bit2 = 300 (bottom).
+ * Returns NULL on error (message via or_last_error). */
+or_fs *or_fs_create(int nx, int ny, int nz, const double box[6], double perturb, uint64_t seed,
+                    int degree, const int *elem_degree, int bs, int dirichlet_mask);
+void or_fs_destroy(or_fs *fs);
+const char *or_last_error(void);
+/* sizes: [0]=nelem [1]=n explicit nodes [2]=nc closure nodes [3]=nexp expanded nodes [4]=bs
+ *        [5]=nverts [6]=nedges [7]=nfaces */
+void or_fs_sizes(const or_fs *fs, int64_t out[8]);
+const int32_t *or_fs_emap(const or_fs *fs);        /* expanded node -> closure node (one 1.0 per row of E) */
+const int32_t *or_fs_xstart(const or_fs *fs);      /* element offsets in expanded nodes, nelem+1 */
+const int32_t *or_fs_elem_degree(const or_fs *fs); /* per element degree (x,y,z) triples */
+const double *or_fs_coords_expanded(const or_fs *fs); /* [nelem][8][3] in tensor vertex order */
+const double *or_fs_vertex_coords(const or_fs *fs);   /* [nverts][3] */
+/* entity ordering (ordered set), per entity index arrays of length nents */
+void or_fs_entity_info(const or_fs *fs, int32_t *ordered, int32_t *goffset, int32_t *gcoffset, int32_t *inodes);
+
+/* dFSGlobalToExpanded (src/fs/interface/fs.c:543-586): g has n*bs, dcache (nc-n)*bs or NULL (zeros) */
+void or_fs_global_to_expanded(const or_fs *fs, const double *g, const double *dcache, double *x);
+/* dFSExpandedToGlobal (fs.c:592-640): closure = E^T x; g = explicit part (add=0 insert, 1 add) */
+void or_fs_expanded_to_global(const or_fs *fs, const double *x, double *g, int add);
+
+/* Matrix-free operator (EllipShellMatMult src/fs/tests/ellip.c:442-472 with p=2,
+ * ElastShellMatMult src/fs/tests/elast.c:311-341 at F=I).
+ * kind 0: scalar diffusion, dv = w det k du (k per FAST qpt, NULL -> 1)
+ * kind 1: p-Laplacian Jacobian with stash [eta, sqrt_mdeta_Du[3]] per qpt (ellip.c:369-377)
+ * kind 2: linear elasticity, lambda/mu in param[0..1] (elast.c:227-280 at F=I)
+ * nthreads: OpenMP threads over element ranges (the reference runs one MPI rank per core). */
+int or_operator_apply(const or_fs *fs, int kind, const double *qdata, const double *param,
+                      const double *g, double *y, int nthreads);
+/* Number of FAST quadrature points over all elements and per-element offsets (nelem+1). */
+int64_t or_fs_num_qpts(const or_fs *fs, int32_t *qoffset);
+/* Physical coordinates of FAST quadrature points [nq][3] (coordinate-FS INTERP). */
+void or_fs_qpt_coords(const or_fs *fs, double *xq);
+/* p-Laplacian residual stash (ellip.c:333-367) from the global state g (homogeneous Dirichlet):
+ * writes [eta, sqrt_mdeta_Du[3]] per FAST qpt. */
+int or_plap_stash(const or_fs *fs, double p, double eps, const double *g, double *stash);
+
+/* Q1-embedded preconditioner assembly (EllipJacobian ellip.c:474-536 with the SPARSE rule, and the
+ * elasticity analogue elast.c:343-407), into CSR over explicit scalar dofs (n*bs rows).
+ * kcoef_fn: 0 -> k=1, 1 -> k from random Fourier features (or_grf_eval); quirk=1 reproduces
+ * the reference's element-natural cjinv indexing (efstopo.c:700), 0 uses the patch point.
+ * Returns nnz; rowptr has n*bs+1 entries (caller-allocated), col/val are malloc'd (free with or_free). */
+int64_t or_q1_assemble(const or_fs *fs, int kind, const double *param, const double *grf, int quirk,
+                       int32_t *rowptr, int32_t **col, double **val);
+void or_free(void *p);
+
+/* Lognormal coefficient field: g(x) = sqrt(2 var / nf) sum_f cos(w_f . x + b_f) (random Fourier
+ * features of the squared-exponential kernel, Rahimi & Recht 2007). grf = [nf, var, ell, w(3nf), b(nf)] */
+int or_grf_make(int nf, double var, double ell, uint64_t seed, double *grf);
+double or_grf_eval(const double *grf, const double x[3]);
+
+/* CSR helpers and Krylov (PETSc KSP replacements; no reference source) */
+void or_csr_mult(int64_t nrows, const int32_t *rowptr, const int32_t *col, const double *val, const double *x, double *y);
+/* Preconditioned CG on the matrix-free operator with a Chebyshev-Jacobi smoother on the Q1 CSR.
+ * Returns iterations (negative on failure); rnorm receives the final relative residual. */
+int or_cg_solve(const or_fs *fs, int kind, const double *qdata, const double *param,
+                const int32_t *rowptr, const int32_t *col, const double *val, int cheb_degree,
+                const double *b, double *x, double rtol, int maxit, double *rnorm, int nthreads);
+
+uint64_t or_splitmix64(uint64_t *state);
+double or_uniform(uint64_t *state);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,149 @@
+"""Extract golden vectors from the dohp reference's own test outputs (refout files) into small
+fixtures under tests/golden/. Run in a checkout where the dohp source tree is available:
+
+    python tests/golden/make_golden.py /path/to/dohp
+
+The refout files are read as text (they are the reference's expected stdout for its CTest
+targets, see src/*/tests/CMakeLists.txt). Only numbers are extracted; large matrices are
+subsampled to keep the fixtures small. Nothing at test time reads the reference tree.
+"""
+import json
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+NUM = re.compile(r"[-+]?\d+\.\d+(?:e[-+]?\d+)?|[-+]?\d+(?:e[-+]?\d+)?")
+
+
+def read(root, rel):
+    with open(os.path.join(root, rel)) as f:
+        return f.read().splitlines()
+
+
+def explicit_bases(root, name, full_elems=(0, 1), head_rows=16):
+    """jacobi-3-tensor-{gauss,lobatto}: interp (Q,P), grad (Q,3P), mass (P,P) per element."""
+    lines = read(root, f"src/jacobi/tests/refout/{name}.refout")
+    out = {}
+    elem = -1
+    i = 0
+    while i < len(lines):
+        m = re.match(r"(Interpolation|Gradient|Mass) matrix of size \((\d+),(\d+)(\*3)?\)", lines[i])
+        if not m:
+            i += 1
+            continue
+        kind, rows, cols = m.group(1), int(m.group(2)), int(m.group(3)) * (3 if m.group(4) else 1)
+        if kind == "Interpolation":
+            elem += 1
+        mat = np.array([[float(v) for v in lines[i + 1 + r].split()] for r in range(rows)])
+        assert mat.shape == (rows, cols)
+        if elem in full_elems or kind == "Mass":
+            out[f"e{elem}_{kind.lower()}"] = mat
+        else:
+            out[f"e{elem}_{kind.lower()}_head"] = mat[:head_rows]
+        i += 1 + rows
+    return out
+
+
+def sparse_bases(root, name, max_patches=4):
+    lines = read(root, f"src/jacobi/tests/refout/{name}.refout")
+    tabs = {}
+    for ln in lines:
+        m = re.match(r"elem (\d+):? +(?:patch (\d+) +)?(qidx\(patch,q\)|bidx\(patch,b\)|interp|deriv)\[ *(\d+)\]\[ *\d+: *\d+\]\s+(.*)", ln)
+        if not m:
+            continue
+        e, patch, what, row, rest = int(m.group(1)), m.group(2), m.group(3), int(m.group(4)), m.group(5)
+        vals = [float(v) for v in rest.split()]
+        key = (e, what.split("(")[0], None if patch is None else int(patch))
+        tabs.setdefault(key, {})[row] = vals
+    out = {}
+    for (e, what, patch), rows in tabs.items():
+        if patch is not None and patch >= max_patches:
+            continue
+        arr = np.array([rows[r] for r in sorted(rows)])
+        if what in ("qidx", "bidx"):
+            out[f"e{e}_{what}"] = arr.astype(np.int32)
+        else:
+            out[f"e{e}_p{patch}_{what}"] = arr
+    return out
+
+
+def patches(root, name):
+    lines = read(root, f"src/jacobi/tests/refout/{name}.refout")
+    out = {}
+    elem = -1
+    for ln in lines:
+        m = re.match(r"Element (\d+): npatches (\d+)\s+patchsize (\d+)", ln)
+        if m:
+            elem = int(m.group(1))
+            out[f"e{elem}_shape"] = np.array([int(m.group(2)), int(m.group(3))], dtype=np.int32)
+            continue
+        m = re.match(r"\s+(indices|weights)\[ *(\d+)\]\[ *\d+: *\d+\]\s+(.*)", ln)
+        if m:
+            key = f"e{elem}_{m.group(1)}"
+            vals = [float(v) for v in m.group(3).split()]
+            out.setdefault(key, []).append(vals)
+    return {k: (np.array(v, dtype=np.int32 if "indices" in k else np.float64) if isinstance(v, list) else v)
+            for k, v in out.items()}
+
+
+def interp_errors(root, name):
+    lines = read(root, f"src/jacobi/tests/refout/{name}.refout")
+    rows = []
+    for ln in lines:
+        m = re.match(r"L2 error for element +(\d+) \( *(\d+), *\d+, *\d+\) with rule \( *(\d+), *\d+, *\d+\) interp +(\S+), derivative +(\S+)", ln)
+        if m:
+            rows.append([int(m.group(1)), int(m.group(2)), int(m.group(3)), float(m.group(4)), float(m.group(5))])
+    return {"rows": np.array(rows)}
+
+
+def vec_after(lines, header):
+    i = lines.index(header)
+    vals = []
+    for ln in lines[i + 1:]:
+        s = ln.strip()
+        if not s or s.startswith("Vector Object") or s.startswith("type:") or s.startswith("Process"):
+            if vals and (s.startswith("Vector Object") is False and not s.startswith("type") and not s.startswith("Process")):
+                break
+            continue
+        if re.match(r"^[A-Za-z]", s):
+            break
+        vals.append(float(s))
+    return np.array(vals)
+
+
+def bu0(root):
+    lines = read(root, "src/fs/tests/refout/bu-0.refout")
+    return {
+        "closure": vec_after(lines, "Global closure vector, should be a sequence starting with 1000"),
+        "homogeneous": vec_after(lines, "Expanded vector projected into homogeneous space"),
+        "inhomogeneous": vec_after(lines, "Expanded vector projected into inhomogeneous space"),
+        "coords": vec_after(lines, "Global coordinate vector (3 dofs per closure node)"),
+    }
+
+
+def main(root):
+    fixtures = {
+        "jacobi3_gauss": explicit_bases(root, "jacobi-3-tensor-gauss"),
+        "jacobi3_lobatto": explicit_bases(root, "jacobi-3-tensor-lobatto"),
+        "jacobi3_sparsex_r4": sparse_bases(root, "jacobi-3-tensor-sparsex-r4"),
+        "jacobi3_sparsex_r6": sparse_bases(root, "jacobi-3-tensor-sparsex-r6"),
+        "jacobi4_fast": patches(root, "jacobi-4-tensor-fast"),
+        "jacobi4_sparse": patches(root, "jacobi-4-tensor-sparse"),
+        "jacobi1_gauss": interp_errors(root, "jacobi-1"),
+        "jacobi1_lobatto": interp_errors(root, "jacobi-1-lobatto"),
+        "bu0": bu0(root),
+    }
+    meta = {}
+    for name, arrs in fixtures.items():
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)
+        meta[name] = sorted(arrs)
+    with open(os.path.join(HERE, "index.json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+    print("wrote", len(fixtures), "fixtures")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
