@@ -1,0 +1,244 @@
+"""dohp_gb300: GB300-native matrix-free hp-FEM operator path with dohp's C API.
+
+This module is a thin ctypes binding of the C ABI declared in include/dohp_gb300.h (the product is the
+CUDA library libdohp_gb300.so built in-tree by dohp_gb300/build.py). Vectors passed to the library are
+CUDA device pointers; the helpers accept torch tensors (torch is used only for device memory and
+streams). Importing this module never falls back to a CPU implementation: if the library is missing the
+import of `lib()` raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libdohp_gb300.so")
+
+dAPPLY_INTERP, dAPPLY_INTERP_TRANSPOSE, dAPPLY_GRAD, dAPPLY_GRAD_TRANSPOSE = 40001, 40002, 40003, 40004
+INSERT_VALUES, ADD_VALUES = 1, 2
+dFS_HOMOGENEOUS, dFS_INHOMOGENEOUS = 0, 1
+FAST, SPARSE, SELF = 0, 1, 2
+dOP_DIFFUSION, dOP_PLAPLACE_JACOBIAN, dOP_ELASTICITY = 0, 1, 2
+dPREC_FP64, dPREC_FP32 = 0, 1
+dKSP_CG, dKSP_FGMRES = 0, 1
+dPC_NONE, dPC_JACOBI, dPC_CHEBYSHEV_Q1 = 0, 1, 2
+
+_lib = None
+_vp = ctypes.c_void_p
+_i32 = ctypes.c_int32
+_i64 = ctypes.c_int64
+_dbl = ctypes.c_double
+
+
+class DohpError(RuntimeError):
+    pass
+
+
+def lib():
+    """Load the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise DohpError("dohp_gb300 CUDA library not built: run `python dohp_gb300/build.py` (missing %s)" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        L.dGetLastError.restype = ctypes.c_char_p
+        _lib = L
+    return _lib
+
+
+def chk(rc):
+    if rc:
+        raise DohpError(lib().dGetLastError().decode())
+
+
+def ptr(t):
+    """Device (or host) address of a torch tensor or numpy array; None -> NULL."""
+    if t is None:
+        return None
+    if isinstance(t, np.ndarray):
+        return _vp(t.ctypes.data)
+    return _vp(t.data_ptr())
+
+
+def exported_symbols():
+    """Names declared in include/dohp_gb300.h (for the ABI completeness test)."""
+    import re
+    hdr = open(os.path.join(HERE, "..", "include", "dohp_gb300.h")).read()
+    return sorted(set(re.findall(r"^(?:dErr|const char \*)\s*(\w+)\s*\(", hdr, re.M)))
+
+
+class Jacobi:
+    def __init__(self):
+        self.h = _vp()
+        chk(lib().dJacobiCreate(ctypes.byref(self.h)))
+
+    def efs(self, degree, method=FAST, rule_order=None):
+        degree = np.asarray(degree if np.ndim(degree) else [degree] * 3, dtype=np.int32)
+        rule_order = np.asarray(rule_order if rule_order is not None else 2 * degree, dtype=np.int32)
+        h = _vp()
+        chk(lib().dJacobiGetEFS(self.h, ptr(degree), ctypes.c_int(method), ptr(rule_order), ctypes.byref(h)))
+        return EFS(h, self)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.dJacobiDestroy(ctypes.byref(self.h))
+
+
+class EFS:
+    def __init__(self, h, jac):
+        self.h, self._jac = h, jac
+        P = np.zeros(3, np.int32); Q = np.zeros(3, np.int32)
+        chk(lib().dEFSGetTensorNodes(h, ptr(P), ptr(Q), None, None, None))
+        self.P, self.Q = P.tolist(), Q.tolist()
+        nodes = np.zeros(P.sum()); pts = np.zeros(Q.sum()); wts = np.zeros(Q.sum())
+        chk(lib().dEFSGetTensorNodes(h, ptr(P), ptr(Q), ptr(nodes), ptr(pts), ptr(wts)))
+        self.nodes, self.points, self.weights = nodes, pts, wts
+
+    def apply(self, nelem, jinv, D, x, y, amode, imode=INSERT_VALUES, stream=None):
+        chk(lib().dEFSApplyBatched(self.h, _i32(nelem), ptr(jinv), _i32(D), ptr(x), ptr(y), ctypes.c_int(amode),
+                                   ctypes.c_int(imode), _vp(stream)))
+
+
+class FS:
+    """dFS on a seeded perturbed block mesh (dMeshGenerateBlock + dFSBuildSpace)."""
+
+    def __init__(self, npoints, degree=4, box=(0, 1, 0, 1, 0, 1), perturb=0.1, seed=1, bs=1,
+                 dirichlet=(100, 200, 300), elem_degree=None, stream=None):
+        L = lib()
+        self.mesh = _vp()
+        chk(L.dMeshCreateBlock(ptr(np.asarray(npoints, np.int32)), ptr(np.asarray(box, np.float64)), _dbl(perturb),
+                               ctypes.c_uint64(seed), ctypes.byref(self.mesh)))
+        self.jac = Jacobi()
+        self.h = _vp()
+        chk(L.dFSCreate(self.mesh, self.jac.h, ctypes.byref(self.h)))
+        ed = None if elem_degree is None else np.ascontiguousarray(elem_degree, np.int32)
+        chk(L.dFSSetDegree(self.h, _i32(degree), ptr(ed)))
+        chk(L.dFSSetBlockSize(self.h, _i32(bs)))
+        for s in dirichlet:
+            chk(L.dFSRegisterBoundary(self.h, _i32(s), ctypes.c_int(1)))
+        if stream is not None:
+            chk(L.dFSSetStream(self.h, _vp(stream)))
+        chk(L.dFSSetUp(self.h))
+        n, nc, nexp, b, ne = _i32(), _i32(), _i32(), _i32(), _i32()
+        chk(L.dFSGetSizes(self.h, ctypes.byref(n), ctypes.byref(nc), ctypes.byref(nexp), ctypes.byref(b), ctypes.byref(ne)))
+        self.n, self.nc, self.nexp, self.bs, self.nelem = n.value, nc.value, nexp.value, b.value, ne.value
+        nq = _i64()
+        chk(L.dFSGetNumQuadraturePoints(self.h, ctypes.byref(nq)))
+        self.nq = nq.value
+
+    def __del__(self):
+        if _lib is None:
+            return
+        if getattr(self, "h", None):
+            _lib.dFSDestroy(ctypes.byref(self.h))
+        if getattr(self, "mesh", None):
+            _lib.dMeshDestroy(ctypes.byref(self.mesh))
+
+    def set_stream(self, stream):
+        chk(lib().dFSSetStream(self.h, _vp(stream)))
+
+    def emap(self):
+        em = np.zeros(self.nexp, np.int32); xs = np.zeros(self.nelem + 1, np.int32)
+        chk(lib().dFSGetExpandedMap(self.h, ptr(em), ptr(xs)))
+        return em, xs
+
+    def elem_degree(self):
+        d = np.zeros(3 * self.nelem, np.int32)
+        chk(lib().dFSGetElementDegrees(self.h, ptr(d)))
+        return d.reshape(-1, 3)
+
+    def global_to_expanded(self, g, x, inhomogeneous=False, add=False):
+        chk(lib().dFSGlobalToExpanded(self.h, ptr(g), ptr(x), ctypes.c_int(1 if inhomogeneous else 0),
+                                      ctypes.c_int(ADD_VALUES if add else INSERT_VALUES)))
+
+    def expanded_to_global(self, x, g, add=False):
+        chk(lib().dFSExpandedToGlobal(self.h, ptr(x), ptr(g), ctypes.c_int(0), ctypes.c_int(ADD_VALUES if add else INSERT_VALUES)))
+
+    def dirichlet_commit(self, closure):
+        chk(lib().dFSInhomogeneousDirichletCommit(self.h, ptr(closure)))
+
+    def qpt_coords(self, xq):
+        chk(lib().dFSGetQuadratureCoordinates(self.h, ptr(xq)))
+
+    def lognormal(self, grf, kq):
+        chk(lib().dFSEvaluateLognormal(self.h, ptr(np.ascontiguousarray(grf, np.float64)), ptr(kq)))
+
+    def operator(self, kind=dOP_DIFFUSION, param=None):
+        return Operator(self, kind, param)
+
+    def matrix(self):
+        return Mat(self)
+
+
+class Operator:
+    def __init__(self, fs, kind=dOP_DIFFUSION, param=None):
+        self.fs = fs
+        self.h = _vp()
+        pa = None if param is None else np.asarray(param, np.float64)
+        chk(lib().dFSCreateOperator(fs.h, ctypes.c_int(kind), ptr(pa), ctypes.byref(self.h)))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.dOperatorDestroy(ctypes.byref(self.h))
+
+    def set_qdata(self, q):
+        chk(lib().dOperatorSetQuadratureData(self.h, ptr(q)))
+
+    def set_precision(self, prec):
+        chk(lib().dOperatorSetPrecision(self.h, ctypes.c_int(prec)))
+
+    def mult(self, x, y):
+        chk(lib().dOperatorMult(self.h, ptr(x), ptr(y)))
+
+    def mult_host(self, x, y):
+        chk(lib().dOperatorMultHost(self.h, ptr(x), ptr(y)))
+
+
+class Mat:
+    def __init__(self, fs):
+        self.fs = fs
+        self.h = _vp()
+        chk(lib().dFSCreateMatrix(fs.h, ctypes.byref(self.h)))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.dMatDestroy(ctypes.byref(self.h))
+
+    def assemble(self, kind=dOP_DIFFUSION, param=None, grf=None, quirk=1):
+        pa = None if param is None else np.asarray(param, np.float64)
+        g = None if grf is None else np.ascontiguousarray(grf, np.float64)
+        chk(lib().dFSAssembleQ1(self.fs.h, self.h, ctypes.c_int(kind), ptr(pa), ptr(g), ctypes.c_int(quirk)))
+
+    def csr_host(self):
+        nr, nnz = _i32(), _i64()
+        chk(lib().dMatGetCSR(self.h, ctypes.byref(nr), ctypes.byref(nnz), None, None, None))
+        rp = np.zeros(nr.value + 1, np.int32); col = np.zeros(nnz.value, np.int32); val = np.zeros(nnz.value)
+        chk(lib().dMatGetCSRHost(self.h, ptr(rp), ptr(col), ptr(val)))
+        return rp, col, val
+
+    def mult(self, x, y):
+        chk(lib().dMatMult(self.h, ptr(x), ptr(y)))
+
+
+class KSP:
+    def __init__(self, op, pmat=None, ksp_type=dKSP_CG, pc=dPC_CHEBYSHEV_Q1, cheb_degree=3):
+        self.h = _vp()
+        self.op, self.pmat = op, pmat
+        chk(lib().dKSPCreate(op.h, None if pmat is None else pmat.h, ctypes.c_int(ksp_type), ctypes.c_int(pc),
+                             ctypes.byref(self.h)))
+        chk(lib().dKSPSetOptions(self.h, _i32(cheb_degree), ctypes.c_int(0), _i32(30)))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.dKSPDestroy(ctypes.byref(self.h))
+
+    def solve(self, b, x, rtol=1e-8, maxit=1000):
+        its, rn = _i32(), _dbl()
+        chk(lib().dKSPSolve(self.h, ptr(b), ptr(x), _dbl(rtol), _i32(maxit), ctypes.byref(its), ctypes.byref(rn)))
+        return its.value, rn.value
+
+
+def grf_create(nf, var, ell, seed):
+    g = np.zeros(3 + 4 * nf)
+    chk(lib().dGRFCreate(_i32(nf), _dbl(var), _dbl(ell), ctypes.c_uint64(seed), ptr(g)))
+    return g

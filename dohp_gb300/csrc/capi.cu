@@ -1,0 +1,510 @@
+// C ABI entry points for dJacobi/dEFS, dOperator, dMat and the lognormal coefficient, plus the generic
+// batched dEFSApply kernel (dEFSApply_Tensor_Hex, src/jacobi/impls/tensor/efstopo.c:368-423, on the device).
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+
+#include "internal.h"
+
+using namespace dgb;
+
+dErr op_mult(_p_dOperator *op, const double *x, double *y);
+dErr op_compute_geometry(_p_dOperator *op);
+dErr q1_symbolic(_p_dFS *fs, _p_dMat *J);
+dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk);
+dErr mat_mult(_p_dMat *J, const double *x, double *y, cudaStream_t s);
+
+namespace {
+
+// Table layout on the device, per direction d: B[Q][P] then D[Q][P].
+struct EFSDev {
+  int P[3], Q[3];
+  const double *B[3], *D[3];
+};
+
+// out[l,m,n,c] (+)= sum_{ijk} A0[l,i] A1[m,j] A2[n,k] in[i,j,k,c]; A given as [Q][P] (tr=0) or its transpose (tr=1)
+__device__ void tmult(int D, const int P[3], const int Q[3], const double *const A[3], int tr, const double *in, double *t1,
+                      double *t2, double *out, bool add) {
+  // P = input sizes, Q = output sizes. tr=0: A[d] stored [Q][P]; tr=1: A[d] stored [P][Q] (the rule-by-basis
+  // table read transposed, so rule values map back to the basis).
+  const int p0 = P[0], p1 = P[1], p2 = P[2], q0 = Q[0], q1 = Q[1], q2 = Q[2];
+  const int n1 = q0 * p1 * p2 * D;
+  for (int t = threadIdx.x; t < n1; t += blockDim.x) {
+    const int l = t / (p1 * p2 * D), rest = t % (p1 * p2 * D);
+    double s = 0;
+    for (int i = 0; i < p0; i++) s += (tr ? A[0][i * q0 + l] : A[0][l * p0 + i]) * in[i * p1 * p2 * D + rest];
+    t1[t] = s;
+  }
+  __syncthreads();
+  const int n2 = q0 * q1 * p2 * D;
+  for (int t = threadIdx.x; t < n2; t += blockDim.x) {
+    const int l = t / (q1 * p2 * D), m = (t / (p2 * D)) % q1, kc = t % (p2 * D);
+    double s = 0;
+    for (int j = 0; j < p1; j++) s += (tr ? A[1][j * q1 + m] : A[1][m * p1 + j]) * t1[(l * p1 + j) * p2 * D + kc];
+    t2[t] = s;
+  }
+  __syncthreads();
+  const int n3 = q0 * q1 * q2 * D;
+  for (int t = threadIdx.x; t < n3; t += blockDim.x) {
+    const int lm = t / (q2 * D), nn = (t / D) % q2, c = t % D;
+    double s = 0;
+    for (int k = 0; k < p2; k++) s += (tr ? A[2][k * q2 + nn] : A[2][nn * p2 + k]) * t2[(lm * p2 + k) * D + c];
+    out[t] = add ? out[t] + s : s;
+  }
+  __syncthreads();
+}
+
+// one block per element; dynamic shared memory holds the element's input and temporaries
+__global__ void k_efs_apply(EFSDev f, int64_t nelem, const double *jinv, int D, const double *in, double *out, int amode, int imode) {
+  extern __shared__ double sm[];
+  const int64_t e = blockIdx.x;
+  if (e >= nelem) return;
+  const int P[3] = {f.P[0], f.P[1], f.P[2]}, Q[3] = {f.Q[0], f.Q[1], f.Q[2]};
+  const int np = P[0] * P[1] * P[2], nq = Q[0] * Q[1] * Q[2], mx = max(np, nq) * D;
+  // generous scratch: each buffer holds max(P,Q)^3 * D
+  const int m3 = max(max(P[0], Q[0]), max(max(P[1], Q[1]), max(P[2], Q[2])));
+  const int buf = m3 * m3 * m3 * D;
+  double *sin = sm, *t1 = sm + buf, *t2 = sm + 2 * buf, *g = sm + 3 * buf;  // g: 3 gradient buffers
+  (void)mx;
+  const bool add = imode == ADD_VALUES;
+  const double *Jq = jinv ? jinv + e * 9LL * nq : nullptr;
+  if (amode == dAPPLY_INTERP || amode == dAPPLY_GRAD) {
+    for (int t = threadIdx.x; t < np * D; t += blockDim.x) sin[t] = in[e * np * D + t];
+    __syncthreads();
+    if (amode == dAPPLY_INTERP) {
+      double *o = out + e * nq * D;
+      const double *A[3] = {f.B[0], f.B[1], f.B[2]};
+      // write through shared then copy so that ADD semantics apply to global memory
+      tmult(D, P, Q, A, 0, sin, t1, t2, g, false);
+      for (int t = threadIdx.x; t < nq * D; t += blockDim.x) o[t] = add ? o[t] + g[t] : g[t];
+    } else {
+      for (int dir = 0; dir < 3; dir++) {
+        const double *A[3] = {dir == 0 ? f.D[0] : f.B[0], dir == 1 ? f.D[1] : f.B[1], dir == 2 ? f.D[2] : f.B[2]};
+        tmult(D, P, Q, A, 0, sin, t1, t2, g + dir * buf, false);
+      }
+      double *o = out + e * nq * D * 3;
+      for (int t = threadIdx.x; t < nq * D; t += blockDim.x) {
+        const int q = t / D;
+        double gr[3] = {g[t], g[buf + t], g[2 * buf + t]};
+        for (int c = 0; c < 3; c++) {
+          double v = Jq ? gr[0] * Jq[q * 9 + 0 * 3 + c] + gr[1] * Jq[q * 9 + 1 * 3 + c] + gr[2] * Jq[q * 9 + 2 * 3 + c] : gr[c];
+          o[t * 3 + c] = add ? o[t * 3 + c] + v : v;
+        }
+      }
+    }
+  } else {
+    if (amode == dAPPLY_INTERP_TRANSPOSE) {
+      for (int t = threadIdx.x; t < nq * D; t += blockDim.x) sin[t] = in[e * nq * D + t];
+      __syncthreads();
+      const double *A[3] = {f.B[0], f.B[1], f.B[2]};
+      tmult(D, Q, P, A, 1, sin, t1, t2, g, false);
+    } else {  // GRAD_TRANSPOSE: map with jinv^T then three transposed contractions accumulated
+      for (int t = threadIdx.x; t < nq * D; t += blockDim.x) {
+        const int q = t / D;
+        const double *v = in + (e * nq * D + t) * 3;
+        for (int dir = 0; dir < 3; dir++)
+          g[dir * buf + t] = Jq ? v[0] * Jq[q * 9 + dir * 3 + 0] + v[1] * Jq[q * 9 + dir * 3 + 1] + v[2] * Jq[q * 9 + dir * 3 + 2] : v[dir];
+      }
+      __syncthreads();
+      for (int t = threadIdx.x; t < np * D; t += blockDim.x) sin[t] = 0;
+      __syncthreads();
+      for (int dir = 0; dir < 3; dir++) {
+        const double *A[3] = {dir == 0 ? f.D[0] : f.B[0], dir == 1 ? f.D[1] : f.B[1], dir == 2 ? f.D[2] : f.B[2]};
+        tmult(D, Q, P, A, 1, g + dir * buf, t1, t2, sin, true);
+      }
+    }
+    double *o = out + e * np * D;
+    const double *src = amode == dAPPLY_INTERP_TRANSPOSE ? g : sin;
+    for (int t = threadIdx.x; t < np * D; t += blockDim.x) o[t] = add ? o[t] + src[t] : src[t];
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+dErr dJacobiCreate(dJacobi *jac) {
+  if (!jac) return set_error("null argument");
+  *jac = new _p_dJacobi();
+  return 0;
+}
+
+dErr dJacobiDestroy(dJacobi *jac) {
+  if (!jac || !*jac) return 0;
+  for (auto &kv : (*jac)->efs) {
+    cudaFree(kv.second->d_tab);
+    delete kv.second;
+  }
+  delete *jac;
+  *jac = nullptr;
+  return 0;
+}
+
+dErr dJacobiGetEFS(dJacobi jac, const dInt degree[3], dQuadratureMethod method, const dInt rule_order[3], dEFS *efs) {
+  if (!jac || !efs) return set_error("null argument");
+  std::vector<int> key = {degree[0], degree[1], degree[2], (int)method, rule_order[0], rule_order[1], rule_order[2]};
+  auto it = jac->efs.find(key);
+  if (it != jac->efs.end()) {
+    *efs = it->second;
+    return 0;
+  }
+  _p_dEFS *f = new _p_dEFS();
+  f->method = method;
+  std::vector<double> tab;
+  for (int d = 0; d < 3; d++) {
+    Basis1D &b = f->b[d];
+    if (degree[d] < 1 || degree[d] + 1 > MAXP) {
+      delete f;
+      return set_error("basis degree %d out of range", degree[d]);
+    }
+    b.P = degree[d] + 1;
+    b.Q = rule_1d(method, rule_order[d], b.x, b.w);
+    if (b.Q < 1 || b.Q > MAXQ) {
+      delete f;
+      return set_error("rule size %d out of range", b.Q);
+    }
+    double wn[MAXP];
+    lobatto_rule(b.P, b.node, wn);
+    for (int i = 0; i < b.Q; i++) lagrange(b.P, b.node, b.x[i], b.B + i * b.P, b.D + i * b.P);
+    f->P[d] = b.P;
+    f->Q[d] = b.Q;
+    tab.insert(tab.end(), b.B, b.B + b.P * b.Q);
+    tab.insert(tab.end(), b.D, b.D + b.P * b.Q);
+  }
+  CUCHK(cudaMalloc(&f->d_tab, tab.size() * sizeof(double)));
+  CUCHK(cudaMemcpy(f->d_tab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
+  jac->efs[key] = f;
+  *efs = f;
+  return 0;
+}
+
+dErr dEFSGetSizes(dEFS efs, dInt *dim, dInt *inodes, dInt *total) {
+  if (!efs) return set_error("null EFS");
+  if (dim) *dim = 3;
+  if (inodes) *inodes = std::max(0, efs->P[0] - 2) * std::max(0, efs->P[1] - 2) * std::max(0, efs->P[2] - 2);
+  if (total) *total = efs->P[0] * efs->P[1] * efs->P[2];
+  return 0;
+}
+
+dErr dEFSGetTensorNodes(dEFS efs, dInt P[3], dInt Q[3], dReal *basis_nodes, dReal *rule_points, dReal *rule_weights) {
+  if (!efs) return set_error("null EFS");
+  int op = 0, oq = 0;
+  for (int d = 0; d < 3; d++) {
+    if (P) P[d] = efs->P[d];
+    if (Q) Q[d] = efs->Q[d];
+    for (int i = 0; i < efs->P[d]; i++)
+      if (basis_nodes) basis_nodes[op + i] = efs->b[d].node[i];
+    for (int i = 0; i < efs->Q[d]; i++) {
+      if (rule_points) rule_points[oq + i] = efs->b[d].x[i];
+      if (rule_weights) rule_weights[oq + i] = efs->b[d].w[i];
+    }
+    op += efs->P[d];
+    oq += efs->Q[d];
+  }
+  return 0;
+}
+
+dErr dEFSApplyBatched(dEFS efs, dInt nelem, const dReal *jinv, dInt D, const dScalar *in, dScalar *out, dApplyMode amode,
+                      InsertMode imode, void *stream) {
+  if (!efs) return set_error("null EFS");
+  if (amode < dAPPLY_INTERP || amode > dAPPLY_GRAD_TRANSPOSE) return set_error("invalid/unimplemented dApplyMode %d", (int)amode);
+  if (imode != INSERT_VALUES && imode != ADD_VALUES) return set_error("InsertMode %d invalid", (int)imode);
+  if (amode == dAPPLY_GRAD_TRANSPOSE && !jinv) return set_error("No Jinv, need a mapping");
+  if (D < 1 || D > 3) return set_error("D = %d not supported", D);
+  if (nelem <= 0) return 0;
+  EFSDev f;
+  const double *p = efs->d_tab;
+  for (int d = 0; d < 3; d++) {
+    f.P[d] = efs->P[d];
+    f.Q[d] = efs->Q[d];
+    f.B[d] = p;
+    f.D[d] = p + efs->P[d] * efs->Q[d];
+    p += 2 * efs->P[d] * efs->Q[d];
+  }
+  int m3 = 0;
+  for (int d = 0; d < 3; d++) m3 = std::max(m3, std::max(f.P[d], f.Q[d]));
+  const size_t smem = 6ull * m3 * m3 * m3 * D * sizeof(double);
+  if (smem > 220 * 1024) return set_error("element too large for the batched apply (%zu bytes of shared memory)", smem);
+  CUCHK(cudaFuncSetAttribute(k_efs_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_efs_apply<<<nelem, 256, smem, (cudaStream_t)stream>>>(f, nelem, jinv, D, in, out, (int)amode, (int)imode);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+dErr dEFSApply(dEFS efs, const dReal *jinv, dInt D, const dScalar *in, dScalar *out, dApplyMode amode, InsertMode imode) {
+  return dEFSApplyBatched(efs, 1, jinv, D, in, out, amode, imode, nullptr);
+}
+
+// ---------------------------------------------------------------- operator
+dErr dFSCreateOperator(dFS fs, dOperatorKind kind, const dReal *param, dOperator *op) {
+  if (!fs || !op) return set_error("null argument");
+  if (!fs->setup) return set_error("dFS not set up");
+  if ((kind == dOP_ELASTICITY) != (fs->bs == 3)) return set_error("operator kind %d does not match block size %d", (int)kind, fs->bs);
+  _p_dOperator *o = new _p_dOperator();
+  o->fs = fs;
+  o->kind = kind;
+  if (param)
+    for (int i = 0; i < 2; i++) o->param[i] = param[i];
+  if (kind == dOP_ELASTICITY) {  // ElastSetMaterial (src/fs/tests/elast.c:62-69)
+    const double E0 = param ? param[0] : 1.0, nu = param ? param[1] : 0.3;
+    o->lam = E0 * nu / ((1 + nu) * (1 - 2 * nu));
+    o->mu = E0 / (2 * (1 + nu));
+  }
+  *op = o;
+  return 0;
+}
+
+dErr dOperatorDestroy(dOperator *op) {
+  if (!op || !*op) return 0;
+  _p_dOperator *o = *op;
+  cudaFree(o->d_geo);
+  cudaFree(o->d_geo32);
+  cudaFree(o->d_k);
+  cudaFree(o->d_stash);
+  cudaFree(o->d_yexp);
+  cudaFree(o->d_x32);
+  cudaFree(o->d_y32);
+  cudaFree(o->d_hx);
+  cudaFree(o->d_hy);
+  delete o;
+  *op = nullptr;
+  return 0;
+}
+
+dErr dOperatorSetQuadratureData(dOperator op, const dReal *qdata) {
+  if (!op) return set_error("null operator");
+  _p_dFS *fs = op->fs;
+  if (op->kind == dOP_DIFFUSION) {
+    if (!qdata) {
+      cudaFree(op->d_k);
+      op->d_k = nullptr;
+    } else {
+      if (!op->d_k) CUCHK(cudaMalloc(&op->d_k, fs->nq * sizeof(double)));
+      CUCHK(cudaMemcpyAsync(op->d_k, qdata, fs->nq * sizeof(double), cudaMemcpyDeviceToDevice, fs->stream));
+    }
+    op->geo_valid = false;
+    return 0;
+  }
+  if (op->kind == dOP_PLAPLACE_JACOBIAN) {
+    if (!qdata) return set_error("p-Laplacian Jacobian needs its stash");
+    if (!op->d_stash) CUCHK(cudaMalloc(&op->d_stash, fs->nq * 4 * sizeof(double)));
+    CUCHK(cudaMemcpyAsync(op->d_stash, qdata, fs->nq * 4 * sizeof(double), cudaMemcpyDeviceToDevice, fs->stream));
+    return 0;
+  }
+  return set_error("operator kind %d takes no quadrature data", (int)op->kind);
+}
+
+dErr dOperatorSetPrecision(dOperator op, dPrecision prec) {
+  if (!op) return set_error("null operator");
+  if (prec != dPREC_FP64) return set_error("precision %d not built yet", (int)prec);
+  op->prec = prec;
+  return 0;
+}
+
+dErr dOperatorMult(dOperator op, const dScalar *x, dScalar *y) {
+  if (!op) return set_error("null operator");
+  return op_mult(op, x, y);
+}
+
+dErr dOperatorMultHost(dOperator op, const dScalar *x_host, dScalar *y_host) {
+  if (!op) return set_error("null operator");
+  _p_dFS *fs = op->fs;
+  const size_t bytes = fs->n * fs->bs * sizeof(double);
+  if (!op->d_hx) {
+    CUCHK(cudaMalloc(&op->d_hx, std::max<size_t>(bytes, 8)));
+    CUCHK(cudaMalloc(&op->d_hy, std::max<size_t>(bytes, 8)));
+  }
+  CUCHK(cudaMemcpyAsync(op->d_hx, x_host, bytes, cudaMemcpyHostToDevice, fs->stream));
+  DCHK(op_mult(op, op->d_hx, op->d_hy));
+  CUCHK(cudaMemcpyAsync(y_host, op->d_hy, bytes, cudaMemcpyDeviceToHost, fs->stream));
+  CUCHK(cudaStreamSynchronize(fs->stream));
+  return 0;
+}
+
+// ---------------------------------------------------------------- Q1 matrix
+dErr dFSCreateMatrix(dFS fs, dMat *J) {
+  if (!fs || !J) return set_error("null argument");
+  if (!fs->setup) return set_error("dFS not set up");
+  _p_dMat *m = new _p_dMat();
+  m->fs = fs;
+  dErr e = q1_symbolic(fs, m);
+  if (e) {
+    delete m;
+    return e;
+  }
+  *J = m;
+  return 0;
+}
+
+dErr dMatDestroy(dMat *J) {
+  if (!J || !*J) return 0;
+  cudaFree((*J)->d_rowptr);
+  cudaFree((*J)->d_col);
+  cudaFree((*J)->d_val);
+  cudaFree((*J)->d_val32);
+  delete *J;
+  *J = nullptr;
+  return 0;
+}
+
+dErr dFSAssembleQ1(dFS fs, dMat J, dOperatorKind kind, const dReal *param, const dReal *grf, int reference_quirk) {
+  (void)param;
+  if (!fs || !J) return set_error("null argument");
+  if (kind != dOP_DIFFUSION) return set_error("Q1 assembly for operator kind %d not built yet", (int)kind);
+  return q1_numeric(fs, J, grf, reference_quirk);
+}
+
+dErr dMatGetCSR(dMat J, dInt *nrows, int64_t *nnz, const dInt **rowptr, const dInt **col, const dScalar **val) {
+  if (!J) return set_error("null matrix");
+  if (nrows) *nrows = (dInt)J->nrows;
+  if (nnz) *nnz = J->nnz;
+  if (rowptr) *rowptr = J->d_rowptr;
+  if (col) *col = J->d_col;
+  if (val) *val = J->d_val;
+  return 0;
+}
+
+dErr dMatGetCSRHost(dMat J, dInt *rowptr, dInt *col, dScalar *val) {
+  if (!J) return set_error("null matrix");
+  cudaStream_t s = J->fs->stream;
+  if (rowptr) CUCHK(cudaMemcpyAsync(rowptr, J->d_rowptr, (J->nrows + 1) * sizeof(dInt), cudaMemcpyDeviceToHost, s));
+  if (col && J->nnz) CUCHK(cudaMemcpyAsync(col, J->d_col, J->nnz * sizeof(dInt), cudaMemcpyDeviceToHost, s));
+  if (val && J->nnz) CUCHK(cudaMemcpyAsync(val, J->d_val, J->nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CUCHK(cudaStreamSynchronize(s));
+  return 0;
+}
+
+dErr dMatMult(dMat J, const dScalar *x, dScalar *y) {
+  if (!J) return set_error("null matrix");
+  return mat_mult(J, x, y, J->fs->stream);
+}
+
+// ---------------------------------------------------------------- lognormal coefficient
+dErr dGRFCreate(dInt nf, dReal var, dReal ell, uint64_t seed, dReal *grf) {
+  if (nf < 1 || !grf) return set_error("bad GRF arguments");
+  const double twopi = 6.283185307179586476925286766559;
+  uint64_t st = seed;
+  auto next = [&]() {
+    uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+  };
+  grf[0] = nf, grf[1] = var, grf[2] = ell;
+  for (int f = 0; f < nf; f++)
+    for (int d = 0; d < 3; d++) {
+      double u1 = next(), u2 = next();
+      if (u1 < 1e-300) u1 = 1e-300;
+      grf[3 + 3 * f + d] = sqrt(-2.0 * log(u1)) * cos(twopi * u2) / ell;  // Box-Muller
+    }
+  for (int f = 0; f < nf; f++) grf[3 + 3 * nf + f] = twopi * next();
+  return 0;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- quadrature-point fields
+namespace {
+struct GaussTab {
+  double x[MAXP];
+};
+__global__ void k_qpt_coords(int64_t nelem, const int32_t *edeg, const int32_t *qoff, const double *coords, const GaussTab *gt,
+                             const double *grf, double *xq, double *kq) {
+  const int64_t e = blockIdx.x;
+  if (e >= nelem) return;
+  const int pa = edeg[3 * e], pb = edeg[3 * e + 1], pc = edeg[3 * e + 2], Qb = pb + 1, Qc = pc + 1, nq = (pa + 1) * Qb * Qc;
+  const double *X = coords + e * 24;
+  for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+    const int a = q / (Qb * Qc), b = (q / Qc) % Qb, c = q % Qc;
+    const double s = gt[pa].x[a], t = gt[pb].x[b], u = gt[pc].x[c];
+    const double bs[2] = {0.5 * (1 - s), 0.5 * (1 + s)}, bt[2] = {0.5 * (1 - t), 0.5 * (1 + t)}, bu[2] = {0.5 * (1 - u), 0.5 * (1 + u)};
+    double x[3] = {0, 0, 0};
+    for (int v = 0; v < 8; v++) {
+      const double ph = bs[v >> 2] * bt[(v >> 1) & 1] * bu[v & 1];
+      for (int d = 0; d < 3; d++) x[d] += X[v * 3 + d] * ph;
+    }
+    const int64_t o = qoff[e] + q;
+    if (xq)
+      for (int d = 0; d < 3; d++) xq[o * 3 + d] = x[d];
+    if (kq) {
+      const int nf = (int)grf[0];
+      const double *w = grf + 3, *bb = grf + 3 + 3 * nf;
+      double g = 0;
+      for (int f = 0; f < nf; f++) g += cos(w[3 * f] * x[0] + w[3 * f + 1] * x[1] + w[3 * f + 2] * x[2] + bb[f]);
+      kq[o] = exp(sqrt(2.0 * grf[1] / nf) * g);
+    }
+  }
+}
+
+dErr qpt_fields(_p_dFS *fs, const double *grf_host, double *xq, double *kq) {
+  GaussTab h[MAXP];
+  for (int p = 1; p < MAXP; p++) {
+    double w[MAXP];
+    gauss_rule(p + 1, h[p].x, w);
+  }
+  GaussTab *d_gt;
+  double *d_grf = nullptr;
+  CUCHK(cudaMalloc(&d_gt, sizeof h));
+  CUCHK(cudaMemcpyAsync(d_gt, h, sizeof h, cudaMemcpyHostToDevice, fs->stream));
+  if (grf_host) {
+    const int nf = (int)grf_host[0];
+    CUCHK(cudaMalloc(&d_grf, (3 + 4 * nf) * sizeof(double)));
+    CUCHK(cudaMemcpyAsync(d_grf, grf_host, (3 + 4 * nf) * sizeof(double), cudaMemcpyHostToDevice, fs->stream));
+  }
+  k_qpt_coords<<<(unsigned)fs->nelem, 128, 0, fs->stream>>>(fs->nelem, fs->d_edeg, fs->d_qoff, fs->d_coords, d_gt, d_grf, xq, kq);
+  CUCHK(cudaGetLastError());
+  CUCHK(cudaStreamSynchronize(fs->stream));
+  cudaFree(d_gt);
+  cudaFree(d_grf);
+  return 0;
+}
+}  // namespace
+
+extern "C" {
+
+dErr dFSGetQuadratureCoordinates(dFS fs, dReal *xq) {
+  if (!fs || !fs->setup) return set_error("dFS not set up");
+  return qpt_fields(fs, nullptr, xq, nullptr);
+}
+
+dErr dFSEvaluateLognormal(dFS fs, const dReal *grf, dReal *kq) {
+  if (!fs || !fs->setup) return set_error("dFS not set up");
+  if (!grf) return set_error("null GRF");
+  return qpt_fields(fs, grf, nullptr, kq);
+}
+
+dErr dOperatorComputePLaplaceStash(dOperator op, const dScalar *g, dReal p, dReal eps) {
+  (void)g, (void)p, (void)eps;
+  if (!op) return set_error("null operator");
+  return set_error("p-Laplacian stash not built yet");
+}
+
+dErr dRulesetIteratorCreate(dFS fs, dQuadratureMethod method, dRulesetIterator *it) {
+  (void)fs, (void)method, (void)it;
+  return set_error("dRulesetIterator not built yet");
+}
+dErr dRulesetIteratorDestroy(dRulesetIterator *it) {
+  (void)it;
+  return 0;
+}
+dErr dRulesetIteratorStart(dRulesetIterator it, const dScalar *g, dFSHomogeneousMode hmode) {
+  (void)it, (void)g, (void)hmode;
+  return set_error("dRulesetIterator not built yet");
+}
+dErr dRulesetIteratorGetPatchApplied(dRulesetIterator it, int64_t *nq, const dReal **jw, const dScalar **x, const dScalar **dx,
+                                     const dScalar **u, const dScalar **du, dScalar **v, dScalar **dv) {
+  (void)it, (void)nq, (void)jw, (void)x, (void)dx, (void)u, (void)du, (void)v, (void)dv;
+  return set_error("dRulesetIterator not built yet");
+}
+dErr dRulesetIteratorCommitPatchApplied(dRulesetIterator it, InsertMode imode, int use_v, int use_dv) {
+  (void)it, (void)imode, (void)use_v, (void)use_dv;
+  return set_error("dRulesetIterator not built yet");
+}
+dErr dRulesetIteratorFinish(dRulesetIterator it, dScalar *y, InsertMode imode) {
+  (void)it, (void)y, (void)imode;
+  return set_error("dRulesetIterator not built yet");
+}
+
+}  // extern "C"

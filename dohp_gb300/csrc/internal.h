@@ -1,0 +1,118 @@
+// Internal declarations of dohp_gb300 (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/dohp_gb300.h"
+
+namespace dgb {
+
+dErr set_error(const char *fmt, ...);
+#define DCHK(call)                                  \
+  do {                                              \
+    dErr _e = (call);                               \
+    if (_e) return _e;                              \
+  } while (0)
+#define CUCHK(call)                                                                                  \
+  do {                                                                                               \
+    cudaError_t _c = (call);                                                                         \
+    if (_c != cudaSuccess) return ::dgb::set_error("%s:%d CUDA error %s: %s", __FILE__, __LINE__,   \
+                                                   cudaGetErrorName(_c), cudaGetErrorString(_c));    \
+  } while (0)
+
+constexpr int MAXP = 9;   // max nodes per direction (degree 8)
+constexpr int MAXQ = 18;  // max rule points per direction (SPARSE rule of degree 8)
+
+// ---------------------------------------------------------------- 1-D bases (basis.cu)
+void gauss_rule(int n, double *x, double *w);
+void lobatto_rule(int n, double *x, double *w);
+// Lagrange basis on nodes[P] at t: values and derivatives
+void lagrange(int P, const double *nodes, double t, double *val, double *der);
+int rule_1d(dQuadratureMethod method, int order, double *x, double *w);  // Gauss family
+// 1-D tables for one basis degree p (P = p+1 GLL nodes) on a rule
+struct Basis1D {
+  int P = 0, Q = 0;
+  double node[MAXP], x[MAXQ], w[MAXQ];
+  double B[MAXQ * MAXP];   // interp [Q][P]
+  double D[MAXQ * MAXP];   // deriv [Q][P]
+  double Dq[MAXQ * MAXQ];  // collocation derivative at the rule points [Q][Q] (FAST: Q == P)
+  double cB[MAXQ * 2], cD[MAXQ * 2];  // coordinate (P=2) basis on the same rule
+};
+int make_basis(int p, dQuadratureMethod method, Basis1D *b);
+
+}  // namespace dgb
+
+struct _p_dEFS {
+  int P[3], Q[3];
+  dQuadratureMethod method;
+  dgb::Basis1D b[3];
+  double *d_tab = nullptr;  // device: per direction B[Q][P], D[Q][P] packed
+};
+
+struct _p_dJacobi {
+  std::map<std::vector<int>, _p_dEFS *> efs;
+};
+
+struct _p_dMesh {
+  int nx, ny, nz;
+  int64_t nv, ne, nf, nr, nents;
+  std::vector<double> vx;                  // [nv][3]
+  std::vector<int64_t> econn, fconn, hconn;  // [ne][2], [nf][4], [nr][8]
+  std::vector<signed char> fset;           // generator face set per entity (0..5) or -1
+  std::vector<int32_t> adjoff, adjind, adjperm;
+};
+
+struct _p_dFS {
+  dMesh mesh = nullptr;
+  dJacobi jac = nullptr;
+  int bs = 1;
+  int degree = 0;
+  std::vector<int> elem_degree_in;
+  int dirichlet_mask = 0;
+  bool built = false;  // host maps computed (dFSBuildSpace)
+  bool setup = false;  // device arrays uploaded
+  cudaStream_t stream = 0;
+  // host results of the space build
+  int64_t nelem = 0, n = 0, nc = 0, nexp = 0, nq = 0;
+  std::vector<int32_t> xstart, emap, edeg, qoff;
+  bool uniform = true;
+  int p = 0;  // uniform degree
+  // device
+  int32_t *d_emap = nullptr, *d_xstart = nullptr, *d_edeg = nullptr, *d_qoff = nullptr;
+  int32_t *d_et_ptr = nullptr, *d_et_idx = nullptr;  // E^T over closure nodes (ascending expanded index)
+  double *d_coords = nullptr;                        // [nelem][8][3]
+  double *d_dcache = nullptr;                        // Dirichlet values [(nc-n)*bs]
+  // per-degree basis tables on the device for FAST rules: [p] -> B, Dq (Q=P)
+  double *d_fast_tab = nullptr;
+  double *d_scratch_exp = nullptr;  // expanded-size scratch (nexp*bs)
+};
+
+struct _p_dOperator {
+  dFS fs;
+  dOperatorKind kind;
+  dPrecision prec = dPREC_FP64;
+  double param[4] = {0, 0, 0, 0};
+  double lam = 0, mu = 0;
+  double *d_geo = nullptr;       // fp64 geometric factors per qpt
+  float *d_geo32 = nullptr;      // fp32 copy
+  double *d_k = nullptr;         // coefficient per qpt
+  double *d_stash = nullptr;     // p-Laplacian stash [nq][4]
+  double *d_yexp = nullptr;      // expanded output scratch
+  float *d_x32 = nullptr, *d_y32 = nullptr;
+  double *d_hx = nullptr, *d_hy = nullptr;  // device staging for the host-vector form
+  bool geo_valid = false;
+  int geo_kind = -1;
+};
+
+struct _p_dMat {
+  dFS fs;
+  int64_t nrows = 0, nnz = 0;
+  int32_t *d_rowptr = nullptr, *d_col = nullptr;
+  double *d_val = nullptr;
+  float *d_val32 = nullptr;
+};

@@ -1,0 +1,432 @@
+// Block mesh, adjacency and function-space build (host setup; results uploaded to the device).
+//
+//  * entity creation order and boundary sets of dMeshGenerateBlock (src/fs/mesh/interface/genblock.c:206-421)
+//  * canonical downward adjacency + orientation permutations (dMeshGetAdjacency, mesh.c:1039-1191;
+//    dGeomOrientFindPerm_HexQuad/_QuadLine, include/dohpgeom.h:97-150)
+//  * min-rule degree propagation (dJacobiPropagateDown_Tensor, src/jacobi/impls/tensor/tensor.c:199-247)
+//  * partition explicit/Dirichlet and natural ordering (fsbuild.c:55-146, cont.c:93-178, cont.c:293-385)
+//  * the element assembly map E (dJacobiAddConstraints_Tensor, tensor.c:360-468)
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+
+#include "internal.h"
+
+using namespace dgb;
+
+namespace {
+
+struct Ord {
+  int x, y, z;
+};
+
+inline int64_t vidx(const _p_dMesh *m, int i, int j, int k) { return ((int64_t)i * m->ny + j) * m->nz + k; }
+// face/edge families in creation order: z-normal, y-normal, x-normal faces; z-, y-, x-directed edges
+inline int64_t nzf(const _p_dMesh *m) { return (int64_t)(m->nx - 1) * (m->ny - 1) * m->nz; }
+inline int64_t nyf(const _p_dMesh *m) { return (int64_t)(m->nx - 1) * m->ny * (m->nz - 1); }
+inline int64_t fz(const _p_dMesh *m, int i, int j, int k) { return ((int64_t)i * (m->ny - 1) + j) * m->nz + k; }
+inline int64_t fy(const _p_dMesh *m, int i, int j, int k) { return nzf(m) + ((int64_t)i * m->ny + j) * (m->nz - 1) + k; }
+inline int64_t fx(const _p_dMesh *m, int i, int j, int k) { return nzf(m) + nyf(m) + ((int64_t)i * (m->ny - 1) + j) * (m->nz - 1) + k; }
+inline int64_t nze(const _p_dMesh *m) { return (int64_t)m->nx * m->ny * (m->nz - 1); }
+inline int64_t nye(const _p_dMesh *m) { return (int64_t)m->nx * (m->ny - 1) * m->nz; }
+inline int64_t ez(const _p_dMesh *m, int i, int j, int k) { return ((int64_t)i * m->ny + j) * (m->nz - 1) + k; }
+inline int64_t ey(const _p_dMesh *m, int i, int j, int k) { return nze(m) + ((int64_t)i * (m->ny - 1) + j) * m->nz + k; }
+inline int64_t ex(const _p_dMesh *m, int i, int j, int k) { return nze(m) + nye(m) + ((int64_t)i * m->ny + j) * m->nz + k; }
+
+// canonical sides of a hex (faces) and a quad (edges); tables as in include/dohpgeom.h:19,26
+const int kHexFace[6][4] = {{0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}, {0, 3, 2, 1}, {4, 5, 6, 7}};
+const int kQuadEdge[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
+// quad rotations/reflections in the order of dGeomOrientFindPerm_HexQuad (dohpgeom.h:100)
+const int kQuadPerm[8][4] = {{0, 1, 2, 3}, {3, 0, 1, 2}, {2, 3, 0, 1}, {1, 2, 3, 0}, {0, 3, 2, 1}, {1, 0, 3, 2}, {2, 1, 0, 3}, {3, 2, 1, 0}};
+
+uint64_t splitmix(uint64_t *s) {
+  uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+double unif(uint64_t *s) { return (double)(splitmix(s) >> 11) * (1.0 / 9007199254740992.0); }
+
+dErr mesh_build(_p_dMesh *m, const double box[6], double perturb, uint64_t seed) {
+  const int NX = m->nx, NY = m->ny, NZ = m->nz;
+  m->nv = (int64_t)NX * NY * NZ;
+  m->nr = (int64_t)(NX - 1) * (NY - 1) * (NZ - 1);
+  m->nf = nzf(m) + nyf(m) + (int64_t)NX * (NY - 1) * (NZ - 1);
+  m->ne = nze(m) + nye(m) + (int64_t)(NX - 1) * NY * NZ;
+  m->nents = m->nv + m->ne + m->nf + m->nr;
+  m->vx.assign(3 * m->nv, 0.0);
+  m->econn.assign(2 * m->ne, 0);
+  m->fconn.assign(4 * m->nf, 0);
+  m->hconn.assign(8 * m->nr, 0);
+  m->fset.assign(m->nents, -1);
+  const double h[3] = {(box[1] - box[0]) / (NX - 1), (box[3] - box[2]) / (NY - 1), (box[5] - box[4]) / (NZ - 1)};
+  uint64_t st = seed;
+  for (int i = 0; i < NX; i++)
+    for (int j = 0; j < NY; j++)
+      for (int k = 0; k < NZ; k++) {
+        const int64_t v = vidx(m, i, j, k);
+        signed char s = -1;  // genblock vertex set chain (genblock.c:212-218)
+        if (i == 0) s = 3;
+        else if (i == NX - 1) s = 1;
+        else if (j == 0) s = 0;
+        else if (j == NY - 1) s = 2;
+        else if (k == 0) s = 4;
+        else if (k == NZ - 1) s = 5;
+        m->fset[v] = s;
+        double *x = &m->vx[3 * v];
+        x[0] = box[0] + (box[1] - box[0]) * (1. * i / (NX - 1));
+        x[1] = box[2] + (box[3] - box[2]) * (1. * j / (NY - 1));
+        x[2] = box[4] + (box[5] - box[4]) * (1. * k / (NZ - 1));
+        const bool interior = i > 0 && i < NX - 1 && j > 0 && j < NY - 1 && k > 0 && k < NZ - 1;
+        if (perturb != 0 && interior)
+          for (int d = 0; d < 3; d++) x[d] += perturb * h[d] * (2.0 * unif(&st) - 1.0);
+      }
+  for (int i = 0; i < NX - 1; i++)
+    for (int j = 0; j < NY - 1; j++)
+      for (int k = 0; k < NZ - 1; k++) {
+        int64_t *c = &m->hconn[8 * (((int64_t)i * (NY - 1) + j) * (NZ - 1) + k)];
+        const int di[8] = {0, 1, 1, 0, 0, 1, 1, 0}, dj[8] = {0, 0, 1, 1, 0, 0, 1, 1}, dk[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+        for (int t = 0; t < 8; t++) c[t] = vidx(m, i + di[t], j + dj[t], k + dk[t]);
+      }
+  const int64_t F0 = m->nv + m->ne, E0 = m->nv;
+  auto setf = [&](int64_t f, int a0, int a1, int a2, int b0, int b1, int b2, int c0, int c1, int c2, int d0, int d1, int d2) {
+    int64_t *c = &m->fconn[4 * f];
+    c[0] = vidx(m, a0, a1, a2);
+    c[1] = vidx(m, b0, b1, b2);
+    c[2] = vidx(m, c0, c1, c2);
+    c[3] = vidx(m, d0, d1, d2);
+  };
+  for (int i = 0; i < NX - 1; i++)
+    for (int j = 0; j < NY - 1; j++)
+      for (int k = 0; k < NZ; k++) {
+        const int64_t f = fz(m, i, j, k);
+        if (k == 0) m->fset[F0 + f] = 4;
+        if (k == NZ - 1) m->fset[F0 + f] = 5;
+        setf(f, i, j, k, i + 1, j, k, i + 1, j + 1, k, i, j + 1, k);
+      }
+  for (int i = 0; i < NX - 1; i++)
+    for (int j = 0; j < NY; j++)
+      for (int k = 0; k < NZ - 1; k++) {
+        const int64_t f = fy(m, i, j, k);
+        if (j == 0) m->fset[F0 + f] = 0;
+        if (j == NY - 1) m->fset[F0 + f] = 2;
+        setf(f, i, j, k, i + 1, j, k, i + 1, j, k + 1, i, j, k + 1);
+      }
+  for (int i = 0; i < NX; i++)
+    for (int j = 0; j < NY - 1; j++)
+      for (int k = 0; k < NZ - 1; k++) {
+        const int64_t f = fx(m, i, j, k);
+        if (i == 0) m->fset[F0 + f] = 3;
+        if (i == NX - 1) m->fset[F0 + f] = 1;
+        setf(f, i, j, k, i, j + 1, k, i, j + 1, k + 1, i, j, k + 1);
+      }
+  auto sete = [&](int64_t e, int64_t a, int64_t b, signed char s) {
+    m->econn[2 * e] = a;
+    m->econn[2 * e + 1] = b;
+    m->fset[E0 + e] = s;
+  };
+  for (int i = 0; i < NX; i++)  // edge set chains as genblock.c:356-393
+    for (int j = 0; j < NY; j++)
+      for (int k = 0; k < NZ - 1; k++) {
+        signed char s = -1;
+        if (i == 0) s = 0;
+        else if (i == NX - 1) s = 2;
+        else if (j == 0) s = 3;
+        else if (j == NY - 1) s = 1;
+        sete(ez(m, i, j, k), vidx(m, i, j, k), vidx(m, i, j, k + 1), s);
+      }
+  for (int i = 0; i < NX; i++)
+    for (int j = 0; j < NY - 1; j++)
+      for (int k = 0; k < NZ; k++) {
+        signed char s = -1;
+        if (i == 0) s = 0;
+        else if (i == NX - 1) s = 2;
+        else if (k == 0) s = 4;
+        else if (k == NZ - 1) s = 5;
+        sete(ey(m, i, j, k), vidx(m, i, j, k), vidx(m, i, j + 1, k), s);
+      }
+  for (int i = 0; i < NX - 1; i++)
+    for (int j = 0; j < NY; j++)
+      for (int k = 0; k < NZ; k++) {
+        signed char s = -1;
+        if (j == 0) s = 3;
+        else if (j == NY - 1) s = 1;
+        else if (k == 0) s = 4;
+        else if (k == NZ - 1) s = 5;
+        sete(ex(m, i, j, k), vidx(m, i, j, k), vidx(m, i + 1, j, k), s);
+      }
+  return 0;
+}
+
+dErr mesh_adjacency(_p_dMesh *m) {
+  const int NX = m->nx, NY = m->ny, NZ = m->nz;
+  const int64_t E0 = m->nv, F0 = m->nv + m->ne, R0 = F0 + m->nf;
+  m->adjoff.assign(m->nents + 1, 0);
+  m->adjind.assign(2 * m->ne + 4 * m->nf + 6 * m->nr, 0);
+  m->adjperm.assign(m->adjind.size(), 0);
+  int64_t a = 0;
+  for (int64_t e = 0; e < m->ne; e++) {
+    m->adjoff[E0 + e] = (int32_t)a;
+    m->adjind[a++] = (int32_t)m->econn[2 * e];
+    m->adjind[a++] = (int32_t)m->econn[2 * e + 1];
+  }
+  for (int64_t f = 0; f < m->nf; f++) {
+    m->adjoff[F0 + f] = (int32_t)a;
+    int64_t ed[4];
+    if (f < nzf(m)) {
+      const int k = (int)(f % NZ), j = (int)((f / NZ) % (NY - 1)), i = (int)(f / NZ / (NY - 1));
+      ed[0] = ex(m, i, j, k), ed[1] = ey(m, i + 1, j, k), ed[2] = ex(m, i, j + 1, k), ed[3] = ey(m, i, j, k);
+    } else if (f < nzf(m) + nyf(m)) {
+      const int64_t g = f - nzf(m);
+      const int k = (int)(g % (NZ - 1)), j = (int)((g / (NZ - 1)) % NY), i = (int)(g / (NZ - 1) / NY);
+      ed[0] = ex(m, i, j, k), ed[1] = ez(m, i + 1, j, k), ed[2] = ex(m, i, j, k + 1), ed[3] = ez(m, i, j, k);
+    } else {
+      const int64_t g = f - nzf(m) - nyf(m);
+      const int k = (int)(g % (NZ - 1)), j = (int)((g / (NZ - 1)) % (NY - 1)), i = (int)(g / (NZ - 1) / (NY - 1));
+      ed[0] = ey(m, i, j, k), ed[1] = ez(m, i, j + 1, k), ed[2] = ey(m, i, j, k + 1), ed[3] = ez(m, i, j, k);
+    }
+    const int64_t *fv = &m->fconn[4 * f];
+    for (int s = 0; s < 4; s++) {
+      const int64_t *ev = &m->econn[2 * ed[s]];
+      int perm;
+      if (ev[0] == fv[kQuadEdge[s][0]] && ev[1] == fv[kQuadEdge[s][1]]) perm = 0;
+      else if (ev[1] == fv[kQuadEdge[s][0]] && ev[0] == fv[kQuadEdge[s][1]]) perm = 1;
+      else return set_error("edge %lld does not match side %d of face %lld", (long long)ed[s], s, (long long)f);
+      m->adjind[a] = (int32_t)(E0 + ed[s]);
+      m->adjperm[a++] = perm;
+    }
+  }
+  for (int i = 0; i < NX - 1; i++)
+    for (int j = 0; j < NY - 1; j++)
+      for (int k = 0; k < NZ - 1; k++) {
+        const int64_t r = ((int64_t)i * (NY - 1) + j) * (NZ - 1) + k;
+        m->adjoff[R0 + r] = (int32_t)a;
+        const int64_t side[6] = {fy(m, i, j, k), fx(m, i + 1, j, k), fy(m, i, j + 1, k), fx(m, i, j, k), fz(m, i, j, k), fz(m, i, j, k + 1)};
+        const int64_t *rv = &m->hconn[8 * r];
+        for (int s = 0; s < 6; s++) {
+          const int64_t *fv = &m->fconn[4 * side[s]];
+          int perm = -1;
+          for (int t = 0; t < 8 && perm < 0; t++)
+            if (fv[kQuadPerm[t][0]] == rv[kHexFace[s][0]] && fv[kQuadPerm[t][1]] == rv[kHexFace[s][1]]) {
+              if (fv[kQuadPerm[t][2]] != rv[kHexFace[s][2]] || fv[kQuadPerm[t][3]] != rv[kHexFace[s][3]])
+                return set_error("face %lld only partly matches side %d of region %lld", (long long)side[s], s, (long long)r);
+              perm = t;
+            }
+          if (perm < 0) return set_error("face %lld does not match side %d of region %lld", (long long)side[s], s, (long long)r);
+          m->adjind[a] = (int32_t)(F0 + side[s]);
+          m->adjperm[a++] = perm;
+        }
+      }
+  m->adjoff[m->nents] = (int32_t)a;
+  return 0;
+}
+
+inline int dirv(const Ord &o, int d) { return d == 0 ? o.x : d == 1 ? o.y : o.z; }
+
+// index into the interior of a face with orientation perm (dGeomPermQuadIndex, tensor.c:328-345)
+inline int perm_quad_index(int perm, int M, int N, int i, int j) {
+  switch (perm) {
+    case 0: return i * N + j;
+    case 1: return (M - 1 - i) + j * M;
+    case 2: return (M - 1 - i) * N + (N - 1 - j);
+    case 3: return i + (N - 1 - j) * M;
+    case 4: return i + j * M;
+    case 5: return (M - 1 - i) * N + j;
+    case 6: return (M - 1 - i) + (N - 1 - j) * M;
+    default: return i * N + (N - 1 - j);
+  }
+}
+
+}  // namespace
+
+// E rows of one hex (tensor.c:360-468). loff: closure offset of every entity.
+static dErr fill_element_map(const _p_dMesh *m, const std::vector<Ord> &deg, const std::vector<int32_t> &loff,
+                             int64_t r, int32_t xs, int32_t *row) {
+  // which face/edge-of-face pairs meet at each hex edge, with edge orientation (tensor.c:380-383)
+  static const int FE[12][2][3] = {{{0, 0, 0}, {4, 3, 1}}, {{1, 0, 0}, {4, 2, 1}}, {{2, 0, 0}, {4, 1, 1}}, {{3, 0, 0}, {4, 0, 1}},
+                                   {{0, 2, 1}, {5, 0, 0}}, {{1, 2, 1}, {5, 1, 0}}, {{2, 2, 1}, {5, 2, 0}}, {{3, 2, 1}, {5, 3, 0}},
+                                   {{0, 3, 1}, {3, 1, 0}}, {{0, 1, 0}, {1, 3, 1}}, {{1, 1, 0}, {2, 3, 1}}, {{2, 1, 0}, {3, 3, 1}}};
+  static const int IPERM[8][4] = {{0, 1, 2, 3}, {3, 0, 1, 2}, {2, 3, 0, 1}, {1, 2, 3, 0}, {3, 2, 1, 0}, {0, 3, 2, 1}, {1, 0, 3, 2}, {2, 1, 0, 3}};
+  static const int EV[8][3][2] = {{{0, 0}, {3, 1}, {8, 0}}, {{0, 1}, {1, 0}, {9, 0}}, {{1, 1}, {2, 0}, {10, 0}}, {{2, 1}, {3, 0}, {11, 0}},
+                                  {{4, 0}, {7, 1}, {8, 1}}, {{4, 1}, {5, 0}, {9, 1}}, {{5, 1}, {6, 0}, {10, 1}}, {{6, 1}, {7, 0}, {11, 1}}};
+  const int32_t *aI = m->adjind.data(), *aO = m->adjoff.data(), *aP = m->adjperm.data();
+  const int64_t ei = m->nv + m->ne + m->nf + r;
+  const int d0 = deg[ei].x + 1, d1 = deg[ei].y + 1, d2 = deg[ei].z + 1, d[3] = {d0, d1, d2}, scan[3] = {d1 * d2, d2, 1};
+  const int32_t *f = aI + aO[ei], *fP = aP + aO[ei];
+  int e[12], eP[12], v[8];
+  for (int i = 0; i < 12; i++) {
+    int ent[2], ori[2];
+    for (int s = 0; s < 2; s++) {
+      const int fa = FE[i][s][0], slot = aO[f[fa]] + IPERM[fP[fa]][FE[i][s][1]];
+      ent[s] = aI[slot];
+      ori[s] = aP[slot] ^ (((fP[fa] >> 2) & 1) ^ FE[i][s][2]);
+    }
+    if (ent[0] != ent[1]) return set_error("faces disagree about edge %d of region %lld", i, (long long)r);
+    if (ori[0] != ori[1]) return set_error("edge orientations disagree on region %lld", (long long)r);
+    e[i] = ent[0];
+    eP[i] = ori[0];
+  }
+  for (int i = 0; i < 8; i++) {
+    int vv[3];
+    for (int s = 0; s < 3; s++) {
+      const int E = EV[i][s][0], end = EV[i][s][1];
+      vv[s] = aI[aO[e[E]] + (eP[E] ? 1 - end : end)];
+    }
+    if (vv[0] != vv[1] || vv[0] != vv[2]) return set_error("edges disagree about vertex %d of region %lld", i, (long long)r);
+    v[i] = vv[0];
+  }
+  auto at = [&](int a, int b, int c) -> int32_t & { return row[xs + (a * d1 + b) * d2 + c]; };
+  const int T[8][3] = {{0, 0, 0}, {d0 - 1, 0, 0}, {d0 - 1, d1 - 1, 0}, {0, d1 - 1, 0}, {0, 0, d2 - 1}, {d0 - 1, 0, d2 - 1}, {d0 - 1, d1 - 1, d2 - 1}, {0, d1 - 1, d2 - 1}};
+  for (int i = 0; i < 8; i++) at(T[i][0], T[i][1], T[i][2]) = loff[v[i]];
+  // hex edge traversal: start node, varying direction, step, end (tensor.c:413-416)
+  const int ES[12][6] = {{1, 0, 0, 0, 1, d0 - 1},          {d0 - 1, 1, 0, 1, 1, d1 - 1},          {d0 - 2, d1 - 1, 0, 0, -1, 0},
+                         {0, d1 - 2, 0, 1, -1, 0},          {1, 0, d2 - 1, 0, 1, d0 - 1},          {d0 - 1, 1, d2 - 1, 1, 1, d1 - 1},
+                         {d0 - 2, d1 - 1, d2 - 1, 0, -1, 0}, {0, d1 - 2, d2 - 1, 1, -1, 0},        {0, 0, 1, 2, 1, d2 - 1},
+                         {d0 - 1, 0, 1, 2, 1, d2 - 1},      {d0 - 1, d1 - 1, 1, 2, 1, d2 - 1},    {0, d1 - 1, 1, 2, 1, d2 - 1}};
+  for (int i = 0; i < 12; i++) {
+    const int *s = ES[i], dir = s[3], inc = s[4], end = s[5];
+    if (deg[e[i]].x != d[dir] - 1) return set_error("degree does not agree, p-nonconforming (region %lld edge %d)", (long long)r, i);
+    for (int j = s[dir]; j != end; j += inc) {
+      const int t = (j - s[dir]) / inc, ne = d[dir] - 2;
+      const int32_t col = eP[i] == 0 ? loff[e[i]] + t : loff[e[i]] + (ne - 1 - t);
+      row[xs + (s[0] * d1 + s[1]) * d2 + s[2] + (j - s[dir]) * scan[dir]] = col;
+    }
+  }
+  // hex face traversal: start node, two varying directions, steps, ends (tensor.c:432-436)
+  const int FS[6][9] = {{1, 0, 1, 0, 2, 1, 1, d0 - 1, d2 - 1},     {d0 - 1, 1, 1, 1, 2, 1, 1, d1 - 1, d2 - 1},
+                        {d0 - 2, d1 - 1, 1, 0, 2, -1, 1, 0, d2 - 1}, {0, d1 - 2, 1, 1, 2, -1, 1, 0, d2 - 1},
+                        {1, 1, 0, 1, 0, 1, 1, d1 - 1, d0 - 1},     {1, 1, d2 - 1, 0, 1, 1, 1, d0 - 1, d1 - 1}};
+  for (int i = 0; i < 6; i++) {
+    const int *s = FS[i], da = s[3], db = s[4], ia = s[5], ib = s[6];
+    const int M = d[da] - 2, N = d[db] - 2;
+    for (int j = s[da]; j != s[7]; j += ia)
+      for (int k = s[db]; k != s[8]; k += ib) {
+        const int fi = perm_quad_index(fP[i], M, N, (j - s[da]) / ia, (k - s[db]) / ib);
+        row[xs + (s[0] * d1 + s[1]) * d2 + s[2] + (j - s[da]) * scan[da] + (k - s[db]) * scan[db]] = loff[f[i]] + fi;
+      }
+  }
+  for (int a = 1; a < d0 - 1; a++)
+    for (int b = 1; b < d1 - 1; b++)
+      for (int c = 1; c < d2 - 1; c++) at(a, b, c) = loff[ei] + ((a - 1) * (d1 - 2) + (b - 1)) * (d2 - 2) + (c - 1);
+  return 0;
+}
+
+dErr fs_build_space(_p_dFS *fs) {
+  const _p_dMesh *m = fs->mesh;
+  const int64_t E0 = m->nv, F0 = m->nv + m->ne, R0 = F0 + m->nf;
+  int maxdeg = fs->degree;
+  const bool per_elem = !fs->elem_degree_in.empty();
+  if (per_elem) {
+    if ((int64_t)fs->elem_degree_in.size() != m->nr) return set_error("elem_degree has %zu entries, mesh has %lld regions", fs->elem_degree_in.size(), (long long)m->nr);
+    maxdeg = *std::max_element(fs->elem_degree_in.begin(), fs->elem_degree_in.end());
+  }
+  if (maxdeg < 1 || maxdeg > MAXP - 1) return set_error("degree %d out of range [1,%d]", maxdeg, MAXP - 1);
+  // isotropic degree tag then min-rule propagation (tables as tensor.c:201-204)
+  std::vector<Ord> deg(m->nents);
+  for (int64_t v = 0; v < m->nv; v++) deg[v] = {0, 0, 0};
+  for (int64_t e = 0; e < m->ne; e++) deg[E0 + e] = {maxdeg, 0, 0};
+  for (int64_t f = 0; f < m->nf; f++) deg[F0 + f] = {maxdeg, maxdeg, 0};
+  for (int64_t r = 0; r < m->nr; r++) {
+    const int p = per_elem ? fs->elem_degree_in[r] : fs->degree;
+    if (p < 1 || p > MAXP - 1) return set_error("element %lld degree %d out of range", (long long)r, p);
+    deg[R0 + r] = {p, p, p};
+  }
+  static const int HEXAXIS[6][2] = {{0, 2}, {1, 2}, {0, 2}, {1, 2}, {1, 0}, {0, 1}};
+  static const int ORIENT[8][2] = {{0, 1}, {1, 0}, {0, 1}, {1, 0}, {1, 0}, {0, 1}, {1, 0}, {0, 1}};
+  static const int QUADAXIS[4] = {0, 1, 0, 1};
+  for (int64_t r = 0; r < m->nr; r++) {
+    const int64_t e = R0 + r;
+    for (int i = 0; i < 6; i++) {
+      const int ai = m->adjoff[e] + i, f = m->adjind[ai], t = m->adjperm[ai];
+      deg[f] = {std::min(deg[f].x, dirv(deg[e], HEXAXIS[i][ORIENT[t][0]])), std::min(deg[f].y, dirv(deg[e], HEXAXIS[i][ORIENT[t][1]])), 0};
+    }
+  }
+  for (int64_t f = 0; f < m->nf; f++)
+    for (int i = 0; i < 4; i++) {
+      const int ed = m->adjind[m->adjoff[F0 + f] + i];
+      deg[ed] = {std::min(deg[ed].x, dirv(deg[F0 + f], QUADAXIS[i])), 0, 0};
+    }
+  // explicit / Dirichlet partition (sets 0..3 -> 100, 5 -> 200, 4 -> 300) and natural ordering
+  const int setbit[6] = {0, 0, 0, 0, 2, 1};
+  std::vector<int32_t> inodes(m->nents), loff(m->nents);
+  std::vector<char> isdir(m->nents);
+  for (int64_t i = 0; i < m->nents; i++) {
+    const int s = m->fset[i];
+    isdir[i] = s >= 0 && ((fs->dirichlet_mask >> setbit[s]) & 1);
+    const Ord o = deg[i];
+    if (i < E0) inodes[i] = 1;
+    else if (i < F0) inodes[i] = std::max(0, o.x - 1);
+    else if (i < R0) inodes[i] = std::max(0, o.x - 1) * std::max(0, o.y - 1);
+    else inodes[i] = std::max(0, o.x - 1) * std::max(0, o.y - 1) * std::max(0, o.z - 1);
+  }
+  int64_t scan = 0;
+  for (int pass = 0; pass < 2; pass++)
+    for (int64_t i = 0; i < m->nents; i++)
+      if (isdir[i] == pass) {
+        loff[i] = (int32_t)scan;
+        scan += inodes[i];
+      }
+  fs->nc = scan;
+  fs->n = 0;
+  for (int64_t i = 0; i < m->nents; i++)
+    if (!isdir[i]) fs->n += inodes[i];
+  if (fs->nc > INT32_MAX / 4) return set_error("space too large for 32-bit indices");
+  // elements, expanded offsets, E
+  fs->nelem = m->nr;
+  fs->xstart.assign(m->nr + 1, 0);
+  fs->edeg.assign(3 * m->nr, 0);
+  fs->qoff.assign(m->nr + 1, 0);
+  fs->uniform = true;
+  fs->p = deg[R0].x;
+  for (int64_t r = 0; r < m->nr; r++) {
+    const Ord o = deg[R0 + r];
+    fs->edeg[3 * r] = o.x, fs->edeg[3 * r + 1] = o.y, fs->edeg[3 * r + 2] = o.z;
+    if (o.x != fs->p || o.y != fs->p || o.z != fs->p) fs->uniform = false;
+    fs->xstart[r + 1] = fs->xstart[r] + (o.x + 1) * (o.y + 1) * (o.z + 1);
+    fs->qoff[r + 1] = fs->qoff[r] + (o.x + 1) * (o.y + 1) * (o.z + 1);  // FAST rule: p+1 Gauss points per direction
+  }
+  fs->nexp = fs->xstart[m->nr];
+  fs->nq = fs->qoff[m->nr];
+  fs->emap.assign(fs->nexp, -1);
+  for (int64_t r = 0; r < m->nr; r++) DCHK(fill_element_map(m, deg, loff, r, fs->xstart[r], fs->emap.data()));
+  for (int64_t i = 0; i < fs->nexp; i++)
+    if (fs->emap[i] < 0) return set_error("expanded node %lld has no constraint", (long long)i);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------------- C ABI
+extern "C" {
+
+dErr dMeshCreateBlock(const dInt npoints[3], const dReal box[6], dReal perturb, uint64_t seed, dMesh *mesh) {
+  if (!mesh || !npoints || !box) return set_error("dMeshCreateBlock: null argument");
+  *mesh = nullptr;
+  if (npoints[0] < 2 || npoints[1] < 2 || npoints[2] < 2) return set_error("need at least 2 vertices per direction");
+  if ((double)npoints[0] * npoints[1] * npoints[2] > 2e8) return set_error("mesh too large");
+  _p_dMesh *m = new _p_dMesh();
+  m->nx = npoints[0], m->ny = npoints[1], m->nz = npoints[2];
+  dErr e = mesh_build(m, box, perturb, seed);
+  if (!e) e = mesh_adjacency(m);
+  if (e) {
+    delete m;
+    return e;
+  }
+  *mesh = m;
+  return 0;
+}
+
+dErr dMeshDestroy(dMesh *mesh) {
+  if (mesh && *mesh) {
+    delete *mesh;
+    *mesh = nullptr;
+  }
+  return 0;
+}
+
+dErr dMeshGetNumEnts(dMesh m, dInt counts[4]) {
+  if (!m) return set_error("null mesh");
+  counts[0] = (dInt)m->nv, counts[1] = (dInt)m->ne, counts[2] = (dInt)m->nf, counts[3] = (dInt)m->nr;
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,286 @@
+// Fused matrix-free operator apply (the hot path) and per-quadrature-point geometry.
+//
+// One apply = the iterator loop of EllipShellMatMult (src/fs/tests/ellip.c:442-472) / ElastShellMatMult
+// (src/fs/tests/elast.c:311-341): gather the element's nodal values through E, GRAD (dEFSApply,
+// src/jacobi/impls/tensor/efstopo.c:395-402), pointwise q-function, GRAD_TRANSPOSE (efstopo.c:404-418),
+// then E^T. The element work is fused into one kernel that keeps the element in shared memory:
+//   interpolate u to the Gauss points with three 1-D passes (B along x, y, z), take reference gradients
+//   with the collocation derivative at the Gauss points (Dq = derivative of the Lagrange basis on the Gauss
+//   points; exact because u restricted to the points is a degree-p polynomial in each direction), apply the
+//   q-function with precomputed geometric factors, and run the transposes back to the nodes.
+// Geometric factors are computed once per mesh (the reference recomputes them every apply,
+// fsrulesetit.c:548-557): G = k w det(J) J^{-1} J^{-T} (6 values) for diffusion, {J^{-1}, w det J}
+// (10 values) for elasticity, all FP64 (J^{-1} by cofactors and 1/det as dGeomInvert3, dohpgeom.h:57-79).
+#include <stdio.h>
+
+#include "internal.h"
+
+using namespace dgb;
+
+dErr fs_restrict(_p_dFS *fs, const double *x, double *g, int add);
+
+namespace {
+
+__device__ int g_negative_jacobian;
+
+// trilinear Jacobian of the Q1 coordinate map at reference point (s,t,u); X = [8][3] in tensor vertex order
+__device__ __forceinline__ void q1_jacobian(const double *X, double s, double t, double u, double J[9]) {
+  const double bs[2] = {0.5 * (1 - s), 0.5 * (1 + s)}, bt[2] = {0.5 * (1 - t), 0.5 * (1 + t)}, bu[2] = {0.5 * (1 - u), 0.5 * (1 + u)};
+  const double dd[2] = {-0.5, 0.5};
+  for (int i = 0; i < 9; i++) J[i] = 0;
+#pragma unroll
+  for (int v = 0; v < 8; v++) {
+    const int a = v >> 2, b = (v >> 1) & 1, c = v & 1;
+    const double g0 = dd[a] * bt[b] * bu[c], g1 = bs[a] * dd[b] * bu[c], g2 = bs[a] * bt[b] * dd[c];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const double x = X[v * 3 + d];
+      J[d * 3 + 0] += x * g0;
+      J[d * 3 + 1] += x * g1;
+      J[d * 3 + 2] += x * g2;
+    }
+  }
+}
+
+// cofactor inverse (same formula as dGeomInvert3)
+__device__ __forceinline__ double invert3(const double a[9], double b[9]) {
+  const double c0 = a[4] * a[8] - a[7] * a[5];
+  const double c3 = -(a[3] * a[8] - a[6] * a[5]);
+  const double c6 = a[3] * a[7] - a[6] * a[4];
+  const double det = a[0] * c0 + a[1] * c3 + a[2] * c6;
+  const double id = 1.0 / det;
+  b[0] = id * c0;
+  b[1] = -id * (a[1] * a[8] - a[7] * a[2]);
+  b[2] = id * (a[1] * a[5] - a[4] * a[2]);
+  b[3] = id * c3;
+  b[4] = id * (a[0] * a[8] - a[6] * a[2]);
+  b[5] = -id * (a[0] * a[5] - a[3] * a[2]);
+  b[6] = id * c6;
+  b[7] = -id * (a[0] * a[7] - a[6] * a[1]);
+  b[8] = id * (a[0] * a[4] - a[3] * a[1]);
+  return det;
+}
+
+struct RuleTab {
+  double x[MAXP], w[MAXP];
+};
+
+// one thread per FAST quadrature point. mode 0: G (6, SoA per element), mode 1: {jinv(9), jw} (10, SoA)
+__global__ void k_geometry(int64_t nelem, const int32_t *__restrict__ edeg, const int32_t *__restrict__ qoff,
+                           const double *__restrict__ coords, const RuleTab *__restrict__ rules,
+                           const double *__restrict__ kq, int mode, double *__restrict__ geo) {
+  const int64_t e = blockIdx.x;
+  if (e >= nelem) return;
+  const int pa = edeg[3 * e], pb = edeg[3 * e + 1], pc = edeg[3 * e + 2];
+  const int Qa = pa + 1, Qb = pb + 1, Qc = pc + 1, nq = Qa * Qb * Qc;
+  const int64_t q0 = qoff[e];
+  const double *X = coords + e * 24;
+  for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+    const int a = q / (Qb * Qc), b = (q / Qc) % Qb, c = q % Qc;
+    double J[9], Ji[9];
+    q1_jacobian(X, rules[pa].x[a], rules[pb].x[b], rules[pc].x[c], J);
+    const double det = invert3(J, Ji);
+    if (det < 0.) atomicExch(&g_negative_jacobian, 1);
+    const double jw = rules[pa].w[a] * rules[pb].w[b] * rules[pc].w[c] * det;
+    if (mode == 0) {
+      const double s = jw * (kq ? kq[q0 + q] : 1.0);
+      double G[6];
+      G[0] = s * (Ji[0] * Ji[0] + Ji[1] * Ji[1] + Ji[2] * Ji[2]);
+      G[1] = s * (Ji[0] * Ji[3] + Ji[1] * Ji[4] + Ji[2] * Ji[5]);
+      G[2] = s * (Ji[0] * Ji[6] + Ji[1] * Ji[7] + Ji[2] * Ji[8]);
+      G[3] = s * (Ji[3] * Ji[3] + Ji[4] * Ji[4] + Ji[5] * Ji[5]);
+      G[4] = s * (Ji[3] * Ji[6] + Ji[4] * Ji[7] + Ji[5] * Ji[8]);
+      G[5] = s * (Ji[6] * Ji[6] + Ji[7] * Ji[7] + Ji[8] * Ji[8]);
+      for (int i = 0; i < 6; i++) geo[q0 * 6 + (int64_t)i * nq + q] = G[i];
+    } else {
+      for (int i = 0; i < 9; i++) geo[q0 * 10 + (int64_t)i * nq + q] = Ji[i];
+      geo[q0 * 10 + 9LL * nq + q] = jw;
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------ fused diffusion
+// Elements per block chosen so a 256-thread block has a few hundred outputs per pass.
+template <int N>
+struct Tile {
+  static constexpr int N3 = N * N * N;
+  static constexpr int EPB = N <= 2 ? 32 : N == 3 ? 16 : N == 4 ? 8 : N == 5 ? 4 : N <= 7 ? 2 : 1;
+};
+
+// y_exp = (B^T Dq^T) G (Dq B) E x for a uniform-degree scalar space; T = arithmetic type
+template <int N, typename T>
+__global__ void __launch_bounds__(256) k_diffusion(int64_t nelem, const int32_t *__restrict__ emap, int64_t n,
+                                                   const T *__restrict__ x, const T *__restrict__ geo,
+                                                   const double *__restrict__ tab, T *__restrict__ yexp) {
+  constexpr int N3 = Tile<N>::N3, EPB = Tile<N>::EPB, NN = N * N;
+  __shared__ T sB[NN], sD[NN];
+  __shared__ T S[4][EPB * N3];
+  const int tid = threadIdx.x;
+  const int64_t e0 = (int64_t)blockIdx.x * EPB;
+  const int ne = (int)min((int64_t)EPB, nelem - e0);
+  const int tot = ne * N3;
+  for (int i = tid; i < NN; i += blockDim.x) {
+    sB[i] = (T)tab[i];
+    sD[i] = (T)tab[MAXP * MAXP + i];
+  }
+  // gather through E (homogeneous Dirichlet: closure entries beyond n are zero)
+  for (int t = tid; t < tot; t += blockDim.x) {
+    const int32_t c = emap[e0 * N3 + t];
+    S[0][t] = c < n ? x[c] : (T)0;
+  }
+  __syncthreads();
+  // interpolate to Gauss points: x pass, y pass, z pass
+  for (int t = tid; t < tot; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3, a = r / NN, jk = r - a * NN;
+    const T *in = &S[0][el * N3 + jk];
+    T s = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++) s += sB[a * N + i] * in[i * NN];
+    S[1][t] = s;
+  }
+  __syncthreads();
+  for (int t = tid; t < tot; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3, a = r / NN, b = (r / N) % N, k = r % N;
+    const T *in = &S[1][el * N3 + a * NN + k];
+    T s = 0;
+#pragma unroll
+    for (int j = 0; j < N; j++) s += sB[b * N + j] * in[j * N];
+    S[0][t] = s;
+  }
+  __syncthreads();
+  for (int t = tid; t < tot; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3, ab = r / N, c = r % N;
+    const T *in = &S[0][el * N3 + ab * N];
+    T s = 0;
+#pragma unroll
+    for (int k = 0; k < N; k++) s += sB[c * N + k] * in[k];
+    S[1][t] = s;
+  }
+  __syncthreads();
+  // reference gradient at the points, pointwise q-function dv = G grad u, stored in S0 (x), S2 (y), S3 (z)
+  for (int t = tid; t < tot; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3, a = r / NN, b = (r / N) % N, c = r % N;
+    const T *U = &S[1][el * N3];
+    T g0 = 0, g1 = 0, g2 = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+      g0 += sD[a * N + i] * U[i * NN + b * N + c];
+      g1 += sD[b * N + i] * U[a * NN + i * N + c];
+      g2 += sD[c * N + i] * U[a * NN + b * N + i];
+    }
+    const T *G = geo + (e0 + el) * 6 * N3 + r;
+    const T G0 = G[0], G1 = G[N3], G2 = G[2 * N3], G3 = G[3 * N3], G4 = G[4 * N3], G5 = G[5 * N3];
+    S[0][t] = G0 * g0 + G1 * g1 + G2 * g2;
+    S[2][t] = G1 * g0 + G3 * g1 + G4 * g2;
+    S[3][t] = G2 * g0 + G4 * g1 + G5 * g2;
+  }
+  __syncthreads();
+  // transposed gradient back to Gauss-point values
+  for (int t = tid; t < tot; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3, a = r / NN, b = (r / N) % N, c = r % N;
+    const T *V0 = &S[0][el * N3], *V1 = &S[2][el * N3], *V2 = &S[3][el * N3];
+    T s = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++)
+      s += sD[i * N + a] * V0[i * NN + b * N + c] + sD[i * N + b] * V1[a * NN + i * N + c] + sD[i * N + c] * V2[a * NN + b * N + i];
+    S[1][t] = s;
+  }
+  __syncthreads();
+  // B^T along z, y, x
+  for (int t = tid; t < tot; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3, ab = r / N, k = r % N;
+    const T *in = &S[1][el * N3 + ab * N];
+    T s = 0;
+#pragma unroll
+    for (int c = 0; c < N; c++) s += sB[c * N + k] * in[c];
+    S[0][t] = s;
+  }
+  __syncthreads();
+  for (int t = tid; t < tot; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3, a = r / NN, j = (r / N) % N, k = r % N;
+    const T *in = &S[0][el * N3 + a * NN + k];
+    T s = 0;
+#pragma unroll
+    for (int b = 0; b < N; b++) s += sB[b * N + j] * in[b * N];
+    S[1][t] = s;
+  }
+  __syncthreads();
+  for (int t = tid; t < tot; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3, i = r / NN, jk = r - i * NN;
+    const T *in = &S[1][el * N3 + jk];
+    T s = 0;
+#pragma unroll
+    for (int a = 0; a < N; a++) s += sB[a * N + i] * in[a * NN];
+    yexp[e0 * N3 + t] = s;
+  }
+}
+
+template <int N, typename T>
+dErr launch_diffusion(_p_dFS *fs, const T *x, const T *geo, T *yexp) {
+  constexpr int EPB = Tile<N>::EPB;
+  const unsigned grid = (unsigned)((fs->nelem + EPB - 1) / EPB);
+  const double *tab = fs->d_fast_tab + (size_t)2 * (N - 2) * MAXP * MAXP;
+  k_diffusion<N, T><<<grid, 256, 0, fs->stream>>>(fs->nelem, fs->d_emap, fs->n, x, geo, tab, yexp);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------------------------------------------
+dErr op_compute_geometry(_p_dOperator *op) {
+  _p_dFS *fs = op->fs;
+  const int mode = op->kind == dOP_ELASTICITY ? 1 : 0;
+  const int ncomp = mode ? 10 : 6;
+  if (op->geo_valid && op->geo_kind == mode) return 0;
+  cudaFree(op->d_geo);
+  op->d_geo = nullptr;
+  CUCHK(cudaMalloc(&op->d_geo, (size_t)fs->nq * ncomp * sizeof(double)));
+  RuleTab h[MAXP];
+  for (int p = 1; p < MAXP; p++) gauss_rule(p + 1, h[p].x, h[p].w);
+  RuleTab *d_rules;
+  CUCHK(cudaMalloc(&d_rules, sizeof h));
+  CUCHK(cudaMemcpyAsync(d_rules, h, sizeof h, cudaMemcpyHostToDevice, fs->stream));
+  int zero = 0;
+  CUCHK(cudaMemcpyToSymbolAsync(g_negative_jacobian, &zero, sizeof zero, 0, cudaMemcpyHostToDevice, fs->stream));
+  k_geometry<<<(unsigned)fs->nelem, 128, 0, fs->stream>>>(fs->nelem, fs->d_edeg, fs->d_qoff, fs->d_coords, d_rules,
+                                                          op->kind == dOP_DIFFUSION ? op->d_k : nullptr, mode, op->d_geo);
+  CUCHK(cudaGetLastError());
+  int neg = 0;
+  CUCHK(cudaMemcpyFromSymbolAsync(&neg, g_negative_jacobian, sizeof neg, 0, cudaMemcpyDeviceToHost, fs->stream));
+  CUCHK(cudaStreamSynchronize(fs->stream));
+  cudaFree(d_rules);
+  if (neg) return set_error("Negative Jacobian in the element geometry");
+  if (op->d_geo32) {
+    cudaFree(op->d_geo32);
+    op->d_geo32 = nullptr;
+  }
+  op->geo_valid = true;
+  op->geo_kind = mode;
+  return 0;
+}
+
+template <typename T>
+static dErr diffusion_apply_t(_p_dFS *fs, const T *x, const T *geo, T *yexp) {
+  if (!fs->uniform) return set_error("fused diffusion apply needs a uniform-degree space (hp path not built yet)");
+  switch (fs->p + 1) {
+    case 2: return launch_diffusion<2, T>(fs, x, geo, yexp);
+    case 3: return launch_diffusion<3, T>(fs, x, geo, yexp);
+    case 4: return launch_diffusion<4, T>(fs, x, geo, yexp);
+    case 5: return launch_diffusion<5, T>(fs, x, geo, yexp);
+    case 6: return launch_diffusion<6, T>(fs, x, geo, yexp);
+    case 7: return launch_diffusion<7, T>(fs, x, geo, yexp);
+    case 8: return launch_diffusion<8, T>(fs, x, geo, yexp);
+    case 9: return launch_diffusion<9, T>(fs, x, geo, yexp);
+  }
+  return set_error("degree %d not supported", fs->p);
+}
+
+dErr op_mult(_p_dOperator *op, const double *x, double *y) {
+  _p_dFS *fs = op->fs;
+  if (op->kind != dOP_DIFFUSION) return set_error("operator kind %d not built yet", (int)op->kind);
+  DCHK(op_compute_geometry(op));
+  if (!op->d_yexp) CUCHK(cudaMalloc(&op->d_yexp, fs->nexp * fs->bs * sizeof(double)));
+  DCHK(diffusion_apply_t<double>(fs, x, op->d_geo, op->d_yexp));
+  return fs_restrict(fs, op->d_yexp, y, 0);
+}

@@ -1,0 +1,303 @@
+// Q1-embedded preconditioning matrix on the device: symbolic CSR, numeric assembly, SpMV.
+//
+// The matrix is the one EllipJacobian (src/fs/tests/ellip.c:474-536) assembles: SPARSE quadrature (two
+// Gauss points per GLL sub-interval, tensorquad.c:32-49) tiled into 2x2x2-point patches, Q1 basis on every
+// GLL sub-cell (dEFSGetExplicitSparse_Tensor_Hex, efstopo.c:660-717: derivative with respect to the unit
+// sub-cell coordinate), rows/columns mapped through E with Dirichlet rows/columns dropped
+// (dFSMatSetValuesBlockedExpanded, fs.c:826-930 with negative global indices for Dirichlet nodes).
+//
+// Device layout: CSR over explicit scalar dofs with sorted columns. Assembly is owner-computes: each
+// patch matrix is formed once (phase 1), then every row sums the patches that touch it in ascending
+// (element, patch) order (phase 2) -- the same order in which MatSetValues(ADD) receives them, with no
+// atomics, so the result is deterministic.
+#include <algorithm>
+
+#include "internal.h"
+
+using namespace dgb;
+
+dErr device_exclusive_scan(const int32_t *in, int32_t *out, int64_t n, cudaStream_t s, int64_t *total);
+
+namespace {
+
+constexpr int MAXCOLS = 64;
+
+__device__ __forceinline__ int64_t find_elem(const int32_t *xstart, int64_t nelem, int64_t x) {
+  int64_t lo = 0, hi = nelem;  // largest e with xstart[e] <= x
+  while (hi - lo > 1) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (xstart[mid] <= x) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// visit the patches touching row r in ascending (element, patch) order:
+// f(e, pidx, corner, px, py, pz, local node (a,b,c) of the patch origin)
+template <typename F>
+__device__ __forceinline__ void for_row_patches(int64_t r, const int32_t *et_ptr, const int32_t *et_idx, const int32_t *xstart,
+                                                const int32_t *edeg, int64_t nelem, F f) {
+  for (int32_t k = et_ptr[r]; k < et_ptr[r + 1]; k++) {
+    const int64_t x = et_idx[k];
+    const int64_t e = find_elem(xstart, nelem, x);
+    const int px = edeg[3 * e], py = edeg[3 * e + 1], pz = edeg[3 * e + 2];
+    const int loc = (int)(x - xstart[e]);
+    const int a = loc / ((py + 1) * (pz + 1)), b = (loc / (pz + 1)) % (py + 1), c = loc % (pz + 1);
+    for (int i = a - 1; i <= a; i++) {
+      if (i < 0 || i >= px) continue;
+      for (int j = b - 1; j <= b; j++) {
+        if (j < 0 || j >= py) continue;
+        for (int l = c - 1; l <= c; l++) {
+          if (l < 0 || l >= pz) continue;
+          const int corner = ((a - i) * 2 + (b - j)) * 2 + (c - l);
+          f(e, (i * py + j) * pz + l, corner, px, py, pz, i, j, l);
+        }
+      }
+    }
+  }
+}
+
+__global__ void k_q1_symbolic(int64_t n, const int32_t *et_ptr, const int32_t *et_idx, const int32_t *xstart, const int32_t *edeg,
+                              int64_t nelem, const int32_t *emap, const int32_t *rowptr, int32_t *counts, int32_t *cols,
+                              int *overflow) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  int32_t set[MAXCOLS];
+  int cnt = 0;
+  for_row_patches(r, et_ptr, et_idx, xstart, edeg, nelem, [&](int64_t e, int, int, int, int py, int pz, int i, int j, int l) {
+    for (int b = 0; b < 8; b++) {
+      const int bi = b >> 2, bj = (b >> 1) & 1, bk = b & 1;
+      const int32_t col = emap[xstart[e] + ((i + bi) * (py + 1) + j + bj) * (pz + 1) + l + bk];
+      if (col >= n) continue;
+      int pos = cnt;
+      while (pos > 0 && set[pos - 1] > col) pos--;
+      if (pos > 0 && set[pos - 1] == col) continue;
+      if (cnt == MAXCOLS) {
+        *overflow = 1;
+        continue;
+      }
+      for (int t = cnt; t > pos; t--) set[t] = set[t - 1];
+      set[pos] = col;
+      cnt++;
+    }
+  });
+  if (!rowptr) {
+    counts[r] = cnt;
+  } else {
+    for (int t = 0; t < cnt; t++) cols[rowptr[r] + t] = set[t];
+  }
+}
+
+__device__ __forceinline__ double grf_eval_dev(const double *grf, const double x[3]) {
+  const int nf = (int)grf[0];
+  const double *w = grf + 3, *b = grf + 3 + 3 * nf;
+  double s = 0;
+  for (int f = 0; f < nf; f++) s += cos(w[3 * f] * x[0] + w[3 * f + 1] * x[1] + w[3 * f + 2] * x[2] + b[f]);
+  return sqrt(2.0 * grf[1] / nf) * s;
+}
+
+__device__ __forceinline__ double inv3(const double a[9], double b[9]) {
+  const double c0 = a[4] * a[8] - a[7] * a[5], c3 = -(a[3] * a[8] - a[6] * a[5]), c6 = a[3] * a[7] - a[6] * a[4];
+  const double det = a[0] * c0 + a[1] * c3 + a[2] * c6, id = 1.0 / det;
+  b[0] = id * c0;
+  b[1] = -id * (a[1] * a[8] - a[7] * a[2]);
+  b[2] = id * (a[1] * a[5] - a[4] * a[2]);
+  b[3] = id * c3;
+  b[4] = id * (a[0] * a[8] - a[6] * a[2]);
+  b[5] = -id * (a[0] * a[5] - a[3] * a[2]);
+  b[6] = id * c6;
+  b[7] = -id * (a[0] * a[7] - a[6] * a[1]);
+  b[8] = id * (a[0] * a[4] - a[3] * a[1]);
+  return det;
+}
+
+// coordinates and Jacobian of the Q1 map at (s,t,u)
+__device__ __forceinline__ void q1_map(const double *X, double s, double t, double u, double xo[3], double J[9]) {
+  const double bs[2] = {0.5 * (1 - s), 0.5 * (1 + s)}, bt[2] = {0.5 * (1 - t), 0.5 * (1 + t)}, bu[2] = {0.5 * (1 - u), 0.5 * (1 + u)};
+  for (int i = 0; i < 9; i++) J[i] = 0;
+  xo[0] = xo[1] = xo[2] = 0;
+  for (int v = 0; v < 8; v++) {
+    const int a = v >> 2, b = (v >> 1) & 1, c = v & 1;
+    const double da = a ? 0.5 : -0.5, db = b ? 0.5 : -0.5, dc = c ? 0.5 : -0.5;
+    const double g0 = da * bt[b] * bu[c], g1 = bs[a] * db * bu[c], g2 = bs[a] * bt[b] * dc, ph = bs[a] * bt[b] * bu[c];
+    for (int d = 0; d < 3; d++) {
+      const double x = X[v * 3 + d];
+      xo[d] += x * ph;
+      J[d * 3 + 0] += x * g0;
+      J[d * 3 + 1] += x * g1;
+      J[d * 3 + 2] += x * g2;
+    }
+  }
+}
+
+struct SparseRules {
+  double x[MAXP][2 * (MAXP - 1)], w[MAXP][2 * (MAXP - 1)];  // [p][2p points]
+};
+
+// phase 1: one 64-thread group per patch computes the 8x8 patch matrix K[i][j] = sum_q w k dphi_i . dphi_j
+__global__ void __launch_bounds__(256) k_q1_patch(int64_t nelem, const int32_t *edeg, const int64_t *pstart, const double *coords,
+                                                  const SparseRules *rules, const double *grf, int quirk, int64_t npatch_total,
+                                                  double *K) {
+  __shared__ double sJ[4][8][9], sW[4][8], sDer[4][8][8][3];
+  const int g = threadIdx.x >> 6, lt = threadIdx.x & 63;
+  const int64_t gp = (int64_t)blockIdx.x * 4 + g;
+  const bool active = gp < npatch_total;
+  int64_t e = 0;
+  int px = 1, py = 1, pz = 1, pidx = 0;
+  if (active) {
+    int64_t lo = 0, hi = nelem;
+    while (hi - lo > 1) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (pstart[mid] <= gp) lo = mid;
+      else hi = mid;
+    }
+    e = lo;
+    px = edeg[3 * e], py = edeg[3 * e + 1], pz = edeg[3 * e + 2];
+    pidx = (int)(gp - pstart[e]);
+  }
+  const int pi = pidx / (py * pz), pj = (pidx / pz) % py, pk = pidx % pz;
+  // Q1 sub-cell basis values at the two Gauss points and unit-coordinate derivatives (efstopo.c:665-666)
+  const double I1[2][2] = {{0.78867513459481287, 0.21132486540518713}, {0.21132486540518713, 0.78867513459481287}};
+  const double D1[2][2] = {{-1., 1.}, {-1., 1.}};
+  if (active && lt < 8) {
+    const int q = lt, qi = q >> 2, qj = (q >> 1) & 1, qk = q & 1;
+    const double *X = coords + e * 24;
+    // weight and coefficient at the patch point (element-natural point index of this patch point)
+    const int ai = 2 * pi + qi, aj = 2 * pj + qj, ak = 2 * pk + qk;
+    double xo[3], J[9], Ji[9];
+    q1_map(X, rules->x[px][ai], rules->x[py][aj], rules->x[pz][ak], xo, J);
+    double det = inv3(J, Ji);
+    double w = rules->w[px][ai] * rules->w[py][aj] * rules->w[pz][ak] * det;
+    if (grf) w *= exp(grf_eval_dev(grf, xo));
+    sW[g][q] = w;
+    if (quirk) {  // inverse Jacobian read at element-natural index pidx*8+q (efstopo.c:700)
+      const int t = pidx * 8 + q, Qy = 2 * py, Qz = 2 * pz;
+      const int ti = t / (Qy * Qz), tj = (t / Qz) % Qy, tk = t % Qz;
+      q1_map(X, rules->x[px][ti], rules->x[py][tj], rules->x[pz][tk], xo, J);
+      inv3(J, Ji);
+    }
+    for (int i = 0; i < 9; i++) sJ[g][q][i] = Ji[i];
+  }
+  __syncthreads();
+  if (active) {
+    const int q = lt >> 3, b = lt & 7, qi = q >> 2, qj = (q >> 1) & 1, qk = q & 1, bi = b >> 2, bj = (b >> 1) & 1, bk = b & 1;
+    const double dX = D1[qi][bi] * I1[qj][bj] * I1[qk][bk], dY = I1[qi][bi] * D1[qj][bj] * I1[qk][bk], dZ = I1[qi][bi] * I1[qj][bj] * D1[qk][bk];
+    const double *Ji = sJ[g][q];
+    for (int d = 0; d < 3; d++) sDer[g][q][b][d] = dX * Ji[0 * 3 + d] + dY * Ji[1 * 3 + d] + dZ * Ji[2 * 3 + d];
+  }
+  __syncthreads();
+  if (active) {
+    const int i = lt >> 3, j = lt & 7;
+    double s = 0;
+    for (int q = 0; q < 8; q++) {
+      const double w = sW[g][q];
+      const double dv0 = w * sDer[g][q][j][0], dv1 = w * sDer[g][q][j][1], dv2 = w * sDer[g][q][j][2];
+      s += sDer[g][q][i][0] * dv0 + sDer[g][q][i][1] * dv1 + sDer[g][q][i][2] * dv2;
+    }
+    K[gp * 64 + lt] = s;
+  }
+}
+
+// phase 2: each explicit row sums its patches in ascending (element, patch) order
+__global__ void k_q1_rows(int64_t n, const int32_t *et_ptr, const int32_t *et_idx, const int32_t *xstart, const int32_t *edeg,
+                          int64_t nelem, const int64_t *pstart, const int32_t *emap, const double *K, const int32_t *rowptr,
+                          const int32_t *cols, double *vals) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int32_t r0 = rowptr[r], r1 = rowptr[r + 1];
+  for (int32_t t = r0; t < r1; t++) vals[t] = 0;
+  for_row_patches(r, et_ptr, et_idx, xstart, edeg, nelem, [&](int64_t e, int pidx, int corner, int, int py, int pz, int i, int j, int l) {
+    const double *Kp = K + (pstart[e] + pidx) * 64 + corner * 8;
+    for (int b = 0; b < 8; b++) {
+      const int bi = b >> 2, bj = (b >> 1) & 1, bk = b & 1;
+      const int32_t col = emap[xstart[e] + ((i + bi) * (py + 1) + j + bj) * (pz + 1) + l + bk];
+      if (col >= n) continue;
+      int lo = r0, hi = r1 - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (cols[mid] < col) lo = mid + 1;
+        else hi = mid;
+      }
+      vals[lo] += Kp[b];
+    }
+  });
+}
+
+}  // namespace
+
+dErr q1_symbolic(_p_dFS *fs, _p_dMat *J) {
+  if (fs->bs != 1) return set_error("Q1 matrix for block size %d not built yet", fs->bs);
+  const int64_t n = fs->n;
+  J->nrows = n;
+  CUCHK(cudaMalloc(&J->d_rowptr, (n + 1) * sizeof(int32_t)));
+  int32_t *counts;
+  int *d_over;
+  CUCHK(cudaMalloc(&counts, std::max<int64_t>(n, 1) * sizeof(int32_t)));
+  CUCHK(cudaMalloc(&d_over, sizeof(int)));
+  CUCHK(cudaMemsetAsync(d_over, 0, sizeof(int), fs->stream));
+  const unsigned grid = (unsigned)((n + 127) / 128);
+  if (n) {
+    k_q1_symbolic<<<grid, 128, 0, fs->stream>>>(n, fs->d_et_ptr, fs->d_et_idx, fs->d_xstart, fs->d_edeg, fs->nelem, fs->d_emap,
+                                                nullptr, counts, nullptr, d_over);
+    CUCHK(cudaGetLastError());
+  }
+  int64_t nnz = 0;
+  DCHK(device_exclusive_scan(counts, J->d_rowptr, n, fs->stream, &nnz));
+  if (nnz > INT32_MAX) return set_error("Q1 matrix has %lld nonzeros, beyond 32-bit CSR", (long long)nnz);
+  J->nnz = nnz;
+  CUCHK(cudaMalloc(&J->d_col, std::max<int64_t>(nnz, 1) * sizeof(int32_t)));
+  CUCHK(cudaMalloc(&J->d_val, std::max<int64_t>(nnz, 1) * sizeof(double)));
+  if (n) {
+    k_q1_symbolic<<<grid, 128, 0, fs->stream>>>(n, fs->d_et_ptr, fs->d_et_idx, fs->d_xstart, fs->d_edeg, fs->nelem, fs->d_emap,
+                                                J->d_rowptr, counts, J->d_col, d_over);
+    CUCHK(cudaGetLastError());
+  }
+  int over = 0;
+  CUCHK(cudaMemcpyAsync(&over, d_over, sizeof(int), cudaMemcpyDeviceToHost, fs->stream));
+  CUCHK(cudaStreamSynchronize(fs->stream));
+  cudaFree(counts);
+  cudaFree(d_over);
+  if (over) return set_error("Q1 row with more than %d columns", MAXCOLS);
+  return 0;
+}
+
+dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk) {
+  std::vector<int64_t> pstart(fs->nelem + 1, 0);
+  for (int64_t e = 0; e < fs->nelem; e++)
+    pstart[e + 1] = pstart[e] + (int64_t)fs->edeg[3 * e] * fs->edeg[3 * e + 1] * fs->edeg[3 * e + 2];
+  const int64_t np = pstart[fs->nelem];
+  SparseRules h;
+  for (int p = 1; p < MAXP; p++) rule_1d(dQUADRATURE_METHOD_SPARSE, 2 * p, h.x[p], h.w[p]);
+  int64_t *d_pstart;
+  SparseRules *d_rules;
+  double *d_K, *d_grf = nullptr;
+  CUCHK(cudaMalloc(&d_pstart, pstart.size() * sizeof(int64_t)));
+  CUCHK(cudaMalloc(&d_rules, sizeof h));
+  CUCHK(cudaMalloc(&d_K, std::max<int64_t>(np, 1) * 64 * sizeof(double)));
+  CUCHK(cudaMemcpyAsync(d_pstart, pstart.data(), pstart.size() * sizeof(int64_t), cudaMemcpyHostToDevice, fs->stream));
+  CUCHK(cudaMemcpyAsync(d_rules, &h, sizeof h, cudaMemcpyHostToDevice, fs->stream));
+  if (grf_host) {
+    const int nf = (int)grf_host[0];
+    CUCHK(cudaMalloc(&d_grf, (3 + 4 * nf) * sizeof(double)));
+    CUCHK(cudaMemcpyAsync(d_grf, grf_host, (3 + 4 * nf) * sizeof(double), cudaMemcpyHostToDevice, fs->stream));
+  }
+  if (np) {
+    k_q1_patch<<<(unsigned)((np + 3) / 4), 256, 0, fs->stream>>>(fs->nelem, fs->d_edeg, d_pstart, fs->d_coords, d_rules, d_grf, quirk, np, d_K);
+    CUCHK(cudaGetLastError());
+  }
+  if (fs->n) {
+    k_q1_rows<<<(unsigned)((fs->n + 127) / 128), 128, 0, fs->stream>>>(fs->n, fs->d_et_ptr, fs->d_et_idx, fs->d_xstart, fs->d_edeg,
+                                                                       fs->nelem, d_pstart, fs->d_emap, d_K, J->d_rowptr, J->d_col, J->d_val);
+    CUCHK(cudaGetLastError());
+  }
+  CUCHK(cudaStreamSynchronize(fs->stream));
+  cudaFree(d_pstart);
+  cudaFree(d_rules);
+  cudaFree(d_K);
+  cudaFree(d_grf);
+  if (J->d_val32) {
+    cudaFree(J->d_val32);
+    J->d_val32 = nullptr;
+  }
+  return 0;
+}

@@ -1,0 +1,193 @@
+/* dohp_gb300: GB300-native matrix-free hp-FEM operator path with dohp's C API.
+ *
+ * Drop-in boundary for dohp callers (PETSc SNES/KSP shell operators and the dRulesetIterator element
+ * loop). Every entry point returns dErr (0 = success); on failure dGetLastError() describes the error.
+ * Vectors are plain device pointers (CUDA global memory) unless the name says Host. Each dFS owns one
+ * CUDA stream (default: the legacy default stream); all work of a call is ordered on that stream.
+ *
+ * Layouts (as in dohp):
+ *   global vector   : n explicit nodes x bs, node-major, components interleaved
+ *   closure vector  : [global | Dirichlet nodes] x bs (VecDohp closure, src/vec/vecd.c:28-159)
+ *   expanded vector : per element, (P0*P1*P2) nodes x bs, element-natural node order
+ *                     ((i*P1 + j)*P2 + k, i along x slowest, k along z fastest)
+ *
+ * Reference locations are relative to the dohp project root.
+ */
+#ifndef DOHP_GB300_H
+#define DOHP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int dErr;
+typedef int32_t dInt;
+typedef double dReal;
+typedef double dScalar;
+
+/* include/dohpjacobi.h:101-108 */
+typedef enum {
+  dAPPLY_INTERP = 40001,
+  dAPPLY_INTERP_TRANSPOSE,
+  dAPPLY_GRAD,
+  dAPPLY_GRAD_TRANSPOSE,
+  dAPPLY_SYMGRAD,
+  dAPPLY_SYMGRAD_TRANSPOSE
+} dApplyMode;
+/* PETSc InsertMode values */
+typedef enum { NOT_SET_VALUES = 0, INSERT_VALUES = 1, ADD_VALUES = 2 } InsertMode;
+/* include/dohpfs.h:49 */
+typedef enum { dFS_HOMOGENEOUS, dFS_INHOMOGENEOUS } dFSHomogeneousMode;
+/* include/dohpjacobi.h:141-148 */
+typedef enum { dQUADRATURE_METHOD_FAST, dQUADRATURE_METHOD_SPARSE, dQUADRATURE_METHOD_SELF } dQuadratureMethod;
+/* include/dohpfs.h:41-47 (only Dirichlet is supported on this path) */
+typedef enum { dFSBSTATUS_INTERIOR = 0, dFSBSTATUS_DIRICHLET = 1 } dFSBStatus;
+
+typedef struct _p_dJacobi *dJacobi;
+typedef struct _p_dEFS *dEFS;
+typedef struct _p_dMesh *dMesh;
+typedef struct _p_dFS *dFS;
+typedef struct _p_dOperator *dOperator;
+typedef struct _p_dMat *dMat;
+typedef struct _p_dRulesetIterator *dRulesetIterator;
+typedef struct _p_dKSP *dKSP;
+
+/* Operator (pointwise q-function) kinds of the fused matrix-free apply */
+typedef enum {
+  dOP_DIFFUSION = 0,      /* EllipPointwiseJacobian with p=2 (src/fs/tests/ellip.c:369-377): dv = k w det(J) grad u */
+  dOP_PLAPLACE_JACOBIAN = 1, /* EllipPointwiseJacobian with the residual stash (ellip.c:333-377) */
+  dOP_ELASTICITY = 2      /* ElastPointwiseJacobian at F = I (src/fs/tests/elast.c:256-280), bs = 3 */
+} dOperatorKind;
+/* Arithmetic of an operator apply */
+typedef enum { dPREC_FP64 = 0, dPREC_FP32 = 1 } dPrecision;
+
+const char *dGetLastError(void);
+
+/* ---------------------------------------------------------------- dJacobi / dEFS (src/jacobi) */
+/* dJacobiCreate (src/jacobi/interface/jacobi.c) with the tensor (GLL nodal) type */
+dErr dJacobiCreate(dJacobi *jac);
+dErr dJacobiDestroy(dJacobi *jac);
+/* dJacobiGetEFS (include/dohpjacobi.h:169) for one hex topology: basis degree per direction and a
+ * tensor rule (method, rule order per direction as produced by dFSGetPreferredQuadratureRuleSet).
+ * The EFS is cached and owned by the dJacobi. */
+dErr dJacobiGetEFS(dJacobi jac, const dInt degree[3], dQuadratureMethod method, const dInt rule_order[3], dEFS *efs);
+/* dEFSGetSizes (include/dohpjacobi.h:172): dim, interior nodes, total nodes */
+dErr dEFSGetSizes(dEFS efs, dInt *dim, dInt *inodes, dInt *total);
+/* dEFSGetTensorNodes / dRuleGetTensorNodeWeight: host copies of basis nodes, rule points, weights */
+dErr dEFSGetTensorNodes(dEFS efs, dInt P[3], dInt Q[3], dReal *basis_nodes, dReal *rule_points, dReal *rule_weights);
+/* dEFSApply (include/dohpjacobi.h:177, src/jacobi/impls/tensor/efstopo.c:368-423) for ONE element:
+ * device pointers; jinv NULL means reference coordinates (efstopo.c:565-568). */
+dErr dEFSApply(dEFS efs, const dReal *jinv, dInt D, const dScalar *in, dScalar *out, dApplyMode amode, InsertMode imode);
+/* Batched dEFSApply over nelem elements stored back to back (element stride = the mode's in/out size),
+ * jinv strided by 9*Q per element (or NULL). stream: cudaStream_t or NULL. */
+dErr dEFSApplyBatched(dEFS efs, dInt nelem, const dReal *jinv, dInt D, const dScalar *in, dScalar *out,
+                      dApplyMode amode, InsertMode imode, void *stream);
+
+/* ---------------------------------------------------------------- dMesh (src/fs/mesh) */
+/* dMeshGenerateBlock (src/fs/mesh/interface/genblock.c:145-521) with npoints vertices per direction on
+ * box = {x0,x1,y0,y1,z0,z1}, followed by a seeded perturbation of interior vertices by
+ * U[-perturb h, perturb h] per coordinate (splitmix64(seed), vertex order) in place of dMeshMorph. */
+dErr dMeshCreateBlock(const dInt npoints[3], const dReal box[6], dReal perturb, uint64_t seed, dMesh *mesh);
+dErr dMeshDestroy(dMesh *mesh);
+dErr dMeshGetNumEnts(dMesh mesh, dInt counts[4]); /* vertices, edges, faces, regions */
+
+/* ---------------------------------------------------------------- dFS (src/fs/interface) */
+dErr dFSCreate(dMesh mesh, dJacobi jac, dFS *fs);
+dErr dFSDestroy(dFS *fs);
+/* dFSSetDegree with an isotropic degree tag (dMeshCreateRuleTagIsotropic, mesh.c:978-1023); elem_degree
+ * (host, one per region, may be NULL) gives per-element orders for hp spaces. */
+dErr dFSSetDegree(dFS fs, dInt degree, const dInt *elem_degree);
+dErr dFSSetBlockSize(dFS fs, dInt bs);
+/* dFSRegisterBoundary (include/dohpfs.h): boundary set 100 (walls), 200 (top), 300 (bottom) */
+dErr dFSRegisterBoundary(dFS fs, dInt setid, dFSBStatus status);
+dErr dFSSetStream(dFS fs, void *stream);
+/* dFSBuildSpace (src/fs/impls/cont/cont.c:258-385) with natural ordering: host maps only (no device) */
+dErr dFSBuildSpace(dFS fs);
+/* dFSSetFromOptions analogue: builds the space if needed and uploads maps and geometry to the device */
+dErr dFSSetUp(dFS fs);
+/* n explicit nodes, nc closure nodes, nexp expanded nodes, bs, nelem */
+dErr dFSGetSizes(dFS fs, dInt *n, dInt *nc, dInt *nexp, dInt *bs, dInt *nelem);
+/* host copies of the bit-exact maps: E (expanded node -> closure node) and element offsets */
+dErr dFSGetExpandedMap(dFS fs, dInt *emap, dInt *xstart);
+/* host copy of per-element degrees (3 per element after propagation) */
+dErr dFSGetElementDegrees(dFS fs, dInt *deg);
+/* dFSGetGeometryVectorExpanded (src/fs/interface/fsgeom.c:216-227): device [nelem][8][3] */
+dErr dFSGetGeometryVectorExpanded(dFS fs, const dReal **coords);
+/* dFSInhomogeneousDirichletCommit (src/fs/interface/fs.c:527-541): cache the Dirichlet part of a closure vector */
+dErr dFSInhomogeneousDirichletCommit(dFS fs, const dScalar *closure);
+/* dFSGlobalToExpanded (fs.c:543-586) / dFSExpandedToGlobal (fs.c:592-640) on device vectors */
+dErr dFSGlobalToExpanded(dFS fs, const dScalar *g, dScalar *x, dFSHomogeneousMode hmode, InsertMode imode);
+dErr dFSExpandedToGlobal(dFS fs, const dScalar *x, dScalar *g, dFSHomogeneousMode hmode, InsertMode imode);
+/* number of FAST quadrature points over all elements (rule order 2p, fsruleset.c:32-37) */
+dErr dFSGetNumQuadraturePoints(dFS fs, int64_t *nq);
+/* physical coordinates of the FAST quadrature points, device [nq][3] (caller-allocated) */
+dErr dFSGetQuadratureCoordinates(dFS fs, dReal *xq);
+
+/* ---------------------------------------------------------------- matrix-free operator (MatShell) */
+/* The matrix-free Jacobian of EllipShellMatMult (src/fs/tests/ellip.c:442-472) or ElastShellMatMult
+ * (src/fs/tests/elast.c:311-341) on global vectors with homogeneous Dirichlet conditions.
+ * param: elasticity {E, nu} (Lame parameters as ElastSetMaterial, elast.c:62-69); unused otherwise. */
+dErr dFSCreateOperator(dFS fs, dOperatorKind kind, const dReal *param, dOperator *op);
+dErr dOperatorDestroy(dOperator *op);
+/* per-quadrature-point data: dOP_DIFFUSION coefficient k [nq] (NULL: k = 1); dOP_PLAPLACE_JACOBIAN stash
+ * [nq][4] = {eta, sqrt(-eta') du} (ellip.c:119-123). Device pointer, copied into the operator. */
+dErr dOperatorSetQuadratureData(dOperator op, const dReal *qdata);
+/* p-Laplacian stash from the state g (EllipPointwiseComputeStore, ellip.c:333-342), exponent p, eps */
+dErr dOperatorComputePLaplaceStash(dOperator op, const dScalar *g, dReal p, dReal eps);
+dErr dOperatorSetPrecision(dOperator op, dPrecision prec);
+/* MatMult: y = A x, device vectors of n*bs entries */
+dErr dOperatorMult(dOperator op, const dScalar *x, dScalar *y);
+/* MatMult with host vectors: copies in, applies, copies out, synchronizes (end-to-end form) */
+dErr dOperatorMultHost(dOperator op, const dScalar *x_host, dScalar *y_host);
+
+/* ---------------------------------------------------------------- dRulesetIterator (batched device form) */
+/* dRulesetIterator* (include/dohpfs.h:106-128, src/fs/interface/fsrulesetit.c): one Start / GetPatchApplied /
+ * CommitPatchApplied / Finish cycle covers all elements at once on the device. Arrays are element-natural
+ * per element, elements back to back (patch order = element order for FAST rules). */
+dErr dRulesetIteratorCreate(dFS fs, dQuadratureMethod method, dRulesetIterator *it);
+dErr dRulesetIteratorDestroy(dRulesetIterator *it);
+dErr dRulesetIteratorStart(dRulesetIterator it, const dScalar *g, dFSHomogeneousMode hmode);
+/* device pointers: jw[nq], x[nq][3], dx[nq][3][3], u[nq][bs], du[nq][bs][3]; v/dv are writable test arrays */
+dErr dRulesetIteratorGetPatchApplied(dRulesetIterator it, int64_t *nq, const dReal **jw, const dScalar **x,
+                                     const dScalar **dx, const dScalar **u, const dScalar **du, dScalar **v, dScalar **dv);
+/* integrate v (INTERP_TRANSPOSE) and dv (GRAD_TRANSPOSE) back into the expanded test vector */
+dErr dRulesetIteratorCommitPatchApplied(dRulesetIterator it, InsertMode imode, int use_v, int use_dv);
+/* dRulesetIteratorFinish: restrict the expanded test vector into the global vector y */
+dErr dRulesetIteratorFinish(dRulesetIterator it, dScalar *y, InsertMode imode);
+
+/* ---------------------------------------------------------------- Q1-embedded preconditioning matrix */
+/* dFSCreateMatrix (src/fs/interface/fs.c:770-813) as a device CSR over explicit scalar dofs; the sparsity is
+ * that of the Q1 sub-element grid (symbolic pass on the device). */
+dErr dFSCreateMatrix(dFS fs, dMat *J);
+dErr dMatDestroy(dMat *J);
+/* EllipJacobian (src/fs/tests/ellip.c:474-536): SPARSE rule, Q1 sub-cell bases (efstopo.c:660-717),
+ * dFSMatSetValuesBlockedExpanded (fs.c:826-930). kind/param as dFSCreateOperator; coefficient: k at the
+ * SPARSE points (NULL: k = 1), reference_quirk = 1 reproduces the reference's inverse-Jacobian indexing. */
+dErr dFSAssembleQ1(dFS fs, dMat J, dOperatorKind kind, const dReal *param, const dReal *grf, int reference_quirk);
+dErr dMatGetCSR(dMat J, dInt *nrows, int64_t *nnz, const dInt **rowptr, const dInt **col, const dScalar **val);
+dErr dMatMult(dMat J, const dScalar *x, dScalar *y);
+/* host copies of the CSR arrays (rowptr nrows+1, col nnz, val nnz) */
+dErr dMatGetCSRHost(dMat J, dInt *rowptr, dInt *col, dScalar *val);
+
+/* ---------------------------------------------------------------- Krylov (PETSc KSP replacement) */
+typedef enum { dKSP_CG = 0, dKSP_FGMRES = 1 } dKSPType;
+typedef enum { dPC_NONE = 0, dPC_JACOBI = 1, dPC_CHEBYSHEV_Q1 = 2 } dPCType;
+dErr dKSPCreate(dOperator op, dMat pmat, dKSPType type, dPCType pc, dKSP *ksp);
+dErr dKSPDestroy(dKSP *ksp);
+/* Chebyshev-Jacobi degree on the Q1 matrix, inner precision, restart length */
+dErr dKSPSetOptions(dKSP ksp, dInt cheb_degree, dPrecision pc_precision, dInt restart);
+dErr dKSPSolve(dKSP ksp, const dScalar *b, dScalar *x, dReal rtol, dInt maxit, dInt *its, dReal *rnorm);
+
+/* ---------------------------------------------------------------- lognormal coefficient */
+/* g(x) = sqrt(2 var / nf) sum_f cos(w_f . x + b_f), random Fourier features of the squared-exponential
+ * covariance (Rahimi & Recht 2007), w ~ N(0, I / ell^2), b ~ U[0, 2 pi), splitmix64(seed). grf is a host
+ * array of 3 + 4 nf doubles; k = exp(g) is evaluated at the FAST points into kq (device [nq]). */
+dErr dGRFCreate(dInt nf, dReal var, dReal ell, uint64_t seed, dReal *grf);
+dErr dFSEvaluateLognormal(dFS fs, const dReal *grf, dReal *kq);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

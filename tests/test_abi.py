@@ -1,0 +1,94 @@
+"""CPU-side checks of the product library: it loads, exports every entry point include/dohp_gb300.h
+declares, and its host-side space build (block mesh, adjacency, numbering, E map) is bit-exact with the
+oracle. No GPU is touched."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import dohp_gb300 as dg
+import pyoracle as po
+
+
+@pytest.fixture(scope="module")
+def L():
+    import subprocess, sys, os
+    if not os.path.exists(dg.LIB_PATH):
+        subprocess.run([sys.executable, os.path.join(os.path.dirname(dg.__file__), "build.py")], check=True)
+    return dg.lib()
+
+
+def test_exports_every_declared_symbol(L):
+    names = dg.exported_symbols()
+    assert len(names) > 40
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def host_fs(npoints, degree, box=(0, 1, 0, 1, 0, 1), perturb=0.1, seed=1, bs=1, dirichlet=(100, 200, 300), elem_degree=None):
+    L = dg.lib()
+    mesh = ctypes.c_void_p()
+    dg.chk(L.dMeshCreateBlock(dg.ptr(np.asarray(npoints, np.int32)), dg.ptr(np.asarray(box, np.float64)),
+                              ctypes.c_double(perturb), ctypes.c_uint64(seed), ctypes.byref(mesh)))
+    fs = ctypes.c_void_p()
+    dg.chk(L.dFSCreate(mesh, None, ctypes.byref(fs)))
+    ed = None if elem_degree is None else np.ascontiguousarray(elem_degree, np.int32)
+    dg.chk(L.dFSSetDegree(fs, ctypes.c_int32(degree), dg.ptr(ed)))
+    dg.chk(L.dFSSetBlockSize(fs, ctypes.c_int32(bs)))
+    for s in dirichlet:
+        dg.chk(L.dFSRegisterBoundary(fs, ctypes.c_int32(s), ctypes.c_int(1)))
+    rc = L.dFSBuildSpace(fs)
+    if rc:
+        msg = L.dGetLastError().decode()
+        L.dFSDestroy(ctypes.byref(fs)); L.dMeshDestroy(ctypes.byref(mesh))
+        raise dg.DohpError(msg)
+    sz = [ctypes.c_int32() for _ in range(5)]
+    dg.chk(L.dFSGetSizes(fs, *[ctypes.byref(s) for s in sz]))
+    n, nc, nexp, b, ne = [s.value for s in sz]
+    em = np.zeros(nexp, np.int32); xs = np.zeros(ne + 1, np.int32)
+    dg.chk(L.dFSGetExpandedMap(fs, dg.ptr(em), dg.ptr(xs)))
+    L.dFSDestroy(ctypes.byref(fs)); L.dMeshDestroy(ctypes.byref(mesh))
+    return dict(n=n, nc=nc, nexp=nexp, nelem=ne, emap=em, xstart=xs)
+
+
+MASKS = {(100, 200, 300): 7, (100,): 1, (200, 300): 6, (): 0}
+
+
+@pytest.mark.parametrize("npoints,degree", [((3, 2, 2), 2), ((4, 3, 5), 1), ((4, 4, 4), 3), ((3, 4, 3), 5), ((3, 3, 3), 8)])
+@pytest.mark.parametrize("dirichlet", list(MASKS))
+def test_host_space_bit_exact_with_oracle(L, npoints, degree, dirichlet):
+    h = host_fs(npoints, degree, dirichlet=dirichlet)
+    o = po.FS(*npoints, degree=degree, perturb=0.1, seed=1, dirichlet_mask=MASKS[dirichlet])
+    assert (h["n"], h["nc"], h["nexp"], h["nelem"]) == (o.n, o.nc, o.nexp, o.nelem)
+    np.testing.assert_array_equal(h["emap"], o.emap())
+    np.testing.assert_array_equal(h["xstart"], o.xstart())
+
+
+def test_bu0_numbering_from_product(L):
+    """bu-0 golden (src/fs/tests/refout/bu-0.refout) reproduced by the product's host build."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "bu0.npz"))
+    h = host_fs((3, 2, 2), 2, box=(-1, 1, -1, 1, -1, 1), perturb=0.0, dirichlet=(100,))
+    closure = g["closure"]
+    x = np.where(h["emap"] < h["n"], closure[np.minimum(h["emap"], h["n"] - 1)], 0.0)
+    np.testing.assert_array_equal(x, g["homogeneous"])
+
+
+def test_nonconforming_orders_rejected_like_the_reference(L):
+    """dJacobiAddConstraints_Tensor errors on p-nonconforming edges (tensor.c:417)."""
+    ed = np.array([2, 3, 2, 3, 2, 3, 2, 3], np.int32)
+    with pytest.raises(dg.DohpError, match="nonconforming"):
+        host_fs((3, 3, 3), 3, elem_degree=ed)
+
+
+def test_grf_parameters_match_oracle(L):
+    g = dg.grf_create(64, 2.0, 0.1, 42)
+    o = po.grf_make(64, 2.0, 0.1, 42)
+    np.testing.assert_array_equal(g, o)
+
+
+def test_errors_are_reported_not_aborted(L):
+    mesh = ctypes.c_void_p()
+    rc = L.dMeshCreateBlock(dg.ptr(np.asarray([1, 2, 2], np.int32)), dg.ptr(np.zeros(6)), ctypes.c_double(0),
+                            ctypes.c_uint64(0), ctypes.byref(mesh))
+    assert rc != 0 and b"vertices" in L.dGetLastError()
