@@ -242,3 +242,10 @@ def grf_create(nf, var, ell, seed):
     g = np.zeros(3 + 4 * nf)
     chk(lib().dGRFCreate(_i32(nf), _dbl(var), _dbl(ell), ctypes.c_uint64(seed), ptr(g)))
     return g
+
+
+def _op_mult_expanded(self, x, yexp):
+    chk(lib().dOperatorMultExpanded(self.h, ptr(x), ptr(yexp)))
+
+
+Operator.mult_expanded = _op_mult_expanded

@@ -276,11 +276,21 @@ static dErr diffusion_apply_t(_p_dFS *fs, const T *x, const T *geo, T *yexp) {
   return set_error("degree %d not supported", fs->p);
 }
 
-dErr op_mult(_p_dOperator *op, const double *x, double *y) {
+dErr op_mult_expanded(_p_dOperator *op, const double *x, double *yexp) {
   _p_dFS *fs = op->fs;
   if (op->kind != dOP_DIFFUSION) return set_error("operator kind %d not built yet", (int)op->kind);
   DCHK(op_compute_geometry(op));
+  return diffusion_apply_t<double>(fs, x, op->d_geo, yexp);
+}
+
+dErr op_mult(_p_dOperator *op, const double *x, double *y) {
+  _p_dFS *fs = op->fs;
   if (!op->d_yexp) CUCHK(cudaMalloc(&op->d_yexp, fs->nexp * fs->bs * sizeof(double)));
-  DCHK(diffusion_apply_t<double>(fs, x, op->d_geo, op->d_yexp));
+  DCHK(op_mult_expanded(op, x, op->d_yexp));
   return fs_restrict(fs, op->d_yexp, y, 0);
+}
+
+extern "C" dErr dOperatorMultExpanded(dOperator op, const dScalar *x, dScalar *yexp) {
+  if (!op) return set_error("null operator");
+  return op_mult_expanded(op, x, yexp);
 }

@@ -139,6 +139,9 @@ dErr dOperatorComputePLaplaceStash(dOperator op, const dScalar *g, dReal p, dRea
 dErr dOperatorSetPrecision(dOperator op, dPrecision prec);
 /* MatMult: y = A x, device vectors of n*bs entries */
 dErr dOperatorMult(dOperator op, const dScalar *x, dScalar *y);
+/* element part of MatMult: yexp = (per-element q-function apply) E x, expanded device vector of nexp*bs;
+ * dFSExpandedToGlobal(yexp) then completes y = A x (the dRulesetIteratorCommitPatchApplied/Finish split) */
+dErr dOperatorMultExpanded(dOperator op, const dScalar *x, dScalar *yexp);
 /* MatMult with host vectors: copies in, applies, copies out, synchronizes (end-to-end form) */
 dErr dOperatorMultHost(dOperator op, const dScalar *x_host, dScalar *y_host);
 

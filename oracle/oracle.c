@@ -208,8 +208,9 @@ int or_rule_patches(int method, const int Q[3], const double *w0, const double *
 void or_tensor_mult_hex(int D, const int P[3], const int Q[3], const double *A[3], const double *in, double *out, int imode)
 {
   const int JKD = P[1] * P[2] * D, KD = P[2] * D;
-  double *a = calloc((size_t)Q[0] * JKD, sizeof(double));
-  double *b = calloc((size_t)Q[0] * Q[1] * KD, sizeof(double));
+  double a[Q[0] * JKD], b[Q[0] * Q[1] * KD]; /* stack work arrays, as the reference (inlinetmulthex.h:21) */
+  memset(a, 0, sizeof a);
+  memset(b, 0, sizeof b);
   if (imode == OR_INSERT) memset(out, 0, sizeof(double) * Q[0] * Q[1] * Q[2] * D);
   for (int l = 0; l < Q[0]; l++)
     for (int i = 0; i < P[0]; i++) {
@@ -229,8 +230,6 @@ void or_tensor_mult_hex(int D, const int P[3], const int Q[3], const double *A[3
         for (int k = 0; k < P[2]; k++) s += A[2][l * P[2] + k] * b[(ij * P[2] + k) * D + d];
         out[(ij * Q[2] + l) * D + d] += s;
       }
-  free(a);
-  free(b);
 }
 
 /* TensorRuleMapping / TensorRuleMappingTranspose / TensorRuleNoMapping (efstopo.c:518-623). */
@@ -259,12 +258,10 @@ static void rule_mapping_transpose(int Q, const double *jinv, int D, const doubl
 int or_efs_apply_hex(const int P[3], const int Q[3], const double *interp[3], const double *deriv[3],
                      const double *jinv, int D, const double *in, double *out, int amode, int imode)
 {
-  double *it[3], *dt[3];
+  double itb[3][32 * 32], dtb[3][32 * 32], *it[3] = {itb[0], itb[1], itb[2]}, *dt[3] = {dtb[0], dtb[1], dtb[2]};
   const double *A[3];
   const int nq = Q[0] * Q[1] * Q[2];
   for (int d = 0; d < 3; d++) {
-    it[d] = malloc(sizeof(double) * P[d] * Q[d]);
-    dt[d] = malloc(sizeof(double) * P[d] * Q[d]);
     for (int i = 0; i < Q[d]; i++)
       for (int j = 0; j < P[d]; j++) {
         it[d][j * Q[d] + i] = interp[d][i * P[d] + j];
@@ -282,28 +279,25 @@ int or_efs_apply_hex(const int P[3], const int Q[3], const double *interp[3], co
     or_tensor_mult_hex(D, Q, P, A, in, out, imode);
     break;
   case OR_GRAD: {
-    double *df = malloc(sizeof(double) * 3 * nq * D);
+    double df[3 * nq * D];
     for (int g = 0; g < 3; g++) {
       for (int d = 0; d < 3; d++) A[d] = (d == g) ? deriv[d] : interp[d];
       or_tensor_mult_hex(D, P, Q, A, in, df + g * nq * D, OR_INSERT);
     }
     rule_mapping(nq, jinv, D, df, out, imode);
-    free(df);
   } break;
   case OR_GRAD_TRANSPOSE: {
-    double *df = malloc(sizeof(double) * 3 * nq * D);
-    if (!jinv) { rc = or_fail("No Jinv, need a mapping"); free(df); break; }
+    double df[3 * nq * D];
+    if (!jinv) { rc = or_fail("No Jinv, need a mapping"); break; }
     rule_mapping_transpose(nq, jinv, D, in, df);
     if (imode == OR_INSERT) memset(out, 0, sizeof(double) * P[0] * P[1] * P[2] * D);
     for (int g = 0; g < 3; g++) {
       for (int d = 0; d < 3; d++) A[d] = (d == g) ? dt[d] : it[d];
       or_tensor_mult_hex(D, Q, P, A, df + g * nq * D, out, OR_ADD);
     }
-    free(df);
   } break;
   default: rc = or_fail("invalid dApplyMode %d", amode);
   }
-  for (int d = 0; d < 3; d++) { free(it[d]); free(dt[d]); }
   return rc;
 }
 
