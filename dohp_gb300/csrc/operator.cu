@@ -13,6 +13,8 @@
 // (10 values) for elasticity, all FP64 (J^{-1} by cofactors and 1/det as dGeomInvert3, dohpgeom.h:57-79).
 #include <stdio.h>
 
+#include <mutex>
+
 #include "internal.h"
 
 using namespace dgb;
@@ -293,4 +295,55 @@ dErr op_mult(_p_dOperator *op, const double *x, double *y) {
 extern "C" dErr dOperatorMultExpanded(dOperator op, const dScalar *x, dScalar *yexp) {
   if (!op) return set_error("null operator");
   return op_mult_expanded(op, x, yexp);
+}
+
+// ----------------------------------------------------------------------------------------------------------
+// Operator apply that allocates nothing.
+//
+// Some callers cannot let a library call cudaMalloc or cudaFree while they run: applications that hand
+// all device memory to their own pool or arena at start-up and account for every byte, and solver
+// callbacks (a PETSc MatShell multiply inside a Krylov iteration) that run next to work on other
+// streams, where a cudaMalloc or cudaFree may synchronize the whole device. dOperatorMultNoAlloc serves
+// them. Its one temporary, the expanded element output (nexp*bs doubles), lives in the fixed-size
+// file-scope device array below, which every GPU that loads this library holds until the process exits.
+// In host code the array's name is only a host-side stand-in; its device address is looked up once per
+// device with cudaGetSymbolAddress (with that device current) and passed to the kernels.
+// Every call shares the array and overwrites all of the part it uses before reading it, so nothing has
+// to be cleared between calls; calls that overlap on the GPU (different streams, or several host
+// threads) race on it.
+static constexpr int64_t kNoAllocScratchDoubles = 1 << 20;  // 8 MiB per device
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+static std::mutex g_noalloc_mutex;
+static double *g_noalloc_addr[128];  // device address of g_noalloc_scratch per device ordinal
+
+static dErr noalloc_scratch(double **out) {
+  int dev = -1;
+  CUCHK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 128) return set_error("dOperatorMultNoAlloc: device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[dev]) {
+    void *p = nullptr;
+    CUCHK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_addr[dev] = (double *)p;
+  }
+  *out = g_noalloc_addr[dev];
+  return 0;
+}
+
+extern "C" dErr dOperatorMultNoAlloc(dOperator op, const dScalar *x, dScalar *y) {
+  if (!op) return set_error("null operator");
+  _p_dFS *fs = op->fs;
+  if (op->kind != dOP_DIFFUSION) return set_error("dOperatorMultNoAlloc: operator kind %d not supported", (int)op->kind);
+  if (!op->geo_valid || op->geo_kind != 0)
+    return set_error("dOperatorMultNoAlloc: the operator's geometric factors do not exist yet; make one dOperatorMult "
+                     "call at set-up time (where allocation is allowed) after the last dOperatorSetQuadratureData");
+  const int64_t need = fs->nexp * fs->bs;
+  if (need > kNoAllocScratchDoubles)
+    return set_error("dOperatorMultNoAlloc: the space has %lld expanded values, more than the fixed scratch of %lld "
+                     "doubles (8 MiB); use dOperatorMult for this space",
+                     (long long)need, (long long)kNoAllocScratchDoubles);
+  double *scratch = nullptr;
+  DCHK(noalloc_scratch(&scratch));
+  DCHK(diffusion_apply_t<double>(fs, x, op->d_geo, scratch));
+  return fs_restrict(fs, scratch, y, 0);
 }

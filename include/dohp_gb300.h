@@ -142,6 +142,15 @@ dErr dOperatorMult(dOperator op, const dScalar *x, dScalar *y);
 /* element part of MatMult: yexp = (per-element q-function apply) E x, expanded device vector of nexp*bs;
  * dFSExpandedToGlobal(yexp) then completes y = A x (the dRulesetIteratorCommitPatchApplied/Finish split) */
 dErr dOperatorMultExpanded(dOperator op, const dScalar *x, dScalar *yexp);
+/* MatMult that allocates nothing (no counterpart in the reference). For callers that cannot let a library
+ * call cudaMalloc/cudaFree while they run: applications that give all device memory to their own pool or
+ * arena, and solver callbacks running beside other streams, where cudaMalloc/cudaFree may synchronize
+ * the device. Its temporary lives in a fixed 8 MiB device array per GPU (at most 1,048,576 expanded
+ * values, nexp*bs); larger spaces are rejected with an error. dOP_DIFFUSION only. Requires one ordinary
+ * dOperatorMult call first (after the last dOperatorSetQuadratureData), which builds the geometric factors.
+ * The first call on a device looks up the array's device address; make it before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race. */
+dErr dOperatorMultNoAlloc(dOperator op, const dScalar *x, dScalar *y);
 /* MatMult with host vectors: copies in, applies, copies out, synchronizes (end-to-end form) */
 dErr dOperatorMultHost(dOperator op, const dScalar *x_host, dScalar *y_host);
 
