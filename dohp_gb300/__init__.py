@@ -221,12 +221,13 @@ class Mat:
 
 
 class KSP:
-    def __init__(self, op, pmat=None, ksp_type=dKSP_CG, pc=dPC_CHEBYSHEV_Q1, cheb_degree=3):
+    def __init__(self, op, pmat=None, ksp_type=dKSP_CG, pc=dPC_CHEBYSHEV_Q1, cheb_degree=3, inner_prec=dPREC_FP64,
+                 restart=30):
         self.h = _vp()
         self.op, self.pmat = op, pmat
         chk(lib().dKSPCreate(op.h, None if pmat is None else pmat.h, ctypes.c_int(ksp_type), ctypes.c_int(pc),
                              ctypes.byref(self.h)))
-        chk(lib().dKSPSetOptions(self.h, _i32(cheb_degree), ctypes.c_int(0), _i32(30)))
+        chk(lib().dKSPSetOptions(self.h, _i32(cheb_degree), ctypes.c_int(inner_prec), _i32(restart)))
 
     def __del__(self):
         if getattr(self, "h", None) and _lib is not None:

@@ -297,7 +297,7 @@ dErr dOperatorSetQuadratureData(dOperator op, const dReal *qdata) {
 
 dErr dOperatorSetPrecision(dOperator op, dPrecision prec) {
   if (!op) return set_error("null operator");
-  if (prec != dPREC_FP64) return set_error("precision %d not built yet", (int)prec);
+  if (prec != dPREC_FP64 && prec != dPREC_FP32) return set_error("precision %d not supported", (int)prec);
   op->prec = prec;
   return 0;
 }

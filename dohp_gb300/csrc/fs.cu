@@ -29,15 +29,16 @@ __global__ void k_expand(int64_t nexp, int bs, const int32_t *__restrict__ emap,
   x[t] = add ? x[t] + v : v;
 }
 
-// one thread per explicit scalar dof: sum over its expanded copies in ascending order
+// one thread per explicit scalar dof: sum (in FP64) over its expanded copies in ascending order
+template <typename TI>
 __global__ void k_restrict(int64_t n, int bs, const int32_t *__restrict__ et_ptr, const int32_t *__restrict__ et_idx,
-                           const double *__restrict__ x, double *__restrict__ g, int add) {
+                           const TI *__restrict__ x, double *__restrict__ g, int add) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= n * bs) return;
   const int64_t c = t / bs;
   const int b = (int)(t - c * bs);
   double s = 0;
-  for (int32_t k = et_ptr[c]; k < et_ptr[c + 1]; k++) s += x[(int64_t)et_idx[k] * bs + b];
+  for (int32_t k = et_ptr[c]; k < et_ptr[c + 1]; k++) s += (double)x[(int64_t)et_idx[k] * bs + b];
   g[t] = add ? g[t] + s : s;
 }
 
@@ -46,7 +47,15 @@ __global__ void k_restrict(int64_t n, int bs, const int32_t *__restrict__ et_ptr
 dErr fs_restrict(_p_dFS *fs, const double *x, double *g, int add) {
   const int64_t N = fs->n * fs->bs;
   if (N == 0) return 0;
-  k_restrict<<<(unsigned)((N + 255) / 256), 256, 0, fs->stream>>>(fs->n, fs->bs, fs->d_et_ptr, fs->d_et_idx, x, g, add);
+  k_restrict<double><<<(unsigned)((N + 255) / 256), 256, 0, fs->stream>>>(fs->n, fs->bs, fs->d_et_ptr, fs->d_et_idx, x, g, add);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+dErr fs_restrict32(_p_dFS *fs, const float *x, double *g, int add) {
+  const int64_t N = fs->n * fs->bs;
+  if (N == 0) return 0;
+  k_restrict<float><<<(unsigned)((N + 255) / 256), 256, 0, fs->stream>>>(fs->n, fs->bs, fs->d_et_ptr, fs->d_et_idx, x, g, add);
   CUCHK(cudaGetLastError());
   return 0;
 }

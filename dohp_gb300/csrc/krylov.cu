@@ -116,6 +116,75 @@ __global__ void k_cheb_step(int64_t n, const double *dinv, const double *r, cons
   z[i] += v;
 }
 
+template <typename A, typename B>
+__global__ void k_convert(int64_t n, const A *__restrict__ a, B *__restrict__ b) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (B)a[i];
+}
+
+template <typename T>
+__global__ void k_cheb_first_t(int64_t n, const T *dinv, const T *r, T inv_theta, T *d, T *z) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const T v = dinv[i] * r[i] * inv_theta;
+  d[i] = v;
+  z[i] = v;
+}
+
+template <typename T>
+__global__ void k_cheb_step_t(int64_t n, const T *dinv, const T *r, const T *w, T c1, T c2, T *d, T *z) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const T v = c1 * d[i] + c2 * dinv[i] * (r[i] - w[i]);
+  d[i] = v;
+  z[i] += v;
+}
+
+// out[v] = <V_v, w> for v < nv (V row-major [nv][n]), fixed-order partials then a fixed-order tree
+__global__ void k_mdot_partial(int64_t n, int nv, const double *__restrict__ V, const double *__restrict__ w, double *__restrict__ part) {
+  __shared__ double s[RED_THREADS];
+  const int v = blockIdx.y;
+  const double *a = V + (int64_t)v * n;
+  double acc = 0;
+  for (int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; i < n; i += (int64_t)RED_BLOCKS * RED_THREADS) acc += a[i] * w[i];
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int off = RED_THREADS / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) s[threadIdx.x] += s[threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[(int64_t)v * RED_BLOCKS + blockIdx.x] = s[0];
+}
+
+__global__ void k_mdot_final(const double *__restrict__ part, double *__restrict__ out, double *__restrict__ acc) {
+  __shared__ double s[RED_BLOCKS];
+  const int v = blockIdx.x;
+  for (int i = threadIdx.x; i < RED_BLOCKS; i += blockDim.x) s[i] = part[(int64_t)v * RED_BLOCKS + i];
+  __syncthreads();
+  for (int off = RED_BLOCKS / 2; off > 0; off >>= 1) {
+    for (int i = threadIdx.x; i < off; i += blockDim.x) s[i] += s[i + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[v] = s[0];
+    if (acc) acc[v] += s[0];
+  }
+}
+
+// w += sign * sum_v c[v] V_v
+__global__ void k_maxpy(int64_t n, int nv, double sign, const double *__restrict__ c, const double *__restrict__ V, double *__restrict__ w) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0;
+  for (int v = 0; v < nv; v++) s += c[v] * V[(int64_t)v * n + i];
+  w[i] += sign * s;
+}
+
+__global__ void k_scale_into(int64_t n, const double *__restrict__ a, const double *__restrict__ num, double inv, double *__restrict__ y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = a[i] * inv;
+}
+
 __global__ void k_pointwise_mult(int64_t n, const double *a, const double *b, double *y) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) y[i] = a[i] * b[i];
@@ -179,7 +248,13 @@ struct _p_dKSP {
   double emin = 0, emax = 0;
   bool pc_ready = false;
   double *d_dinv = nullptr, *d_work = nullptr, *d_part = nullptr, *d_s = nullptr;
-  std::vector<double *> V, Z;  // FGMRES bases
+  dPrecision inner_prec = dPREC_FP64;  // precision of the operator applies inside an FGMRES cycle
+  double *d_V = nullptr, *d_Z = nullptr, *d_h = nullptr;  // FGMRES bases [(m+1) x n], [m x n], coefficients
+  float *d_w32 = nullptr, *d_dinv32 = nullptr, *d_val32 = nullptr;  // FP32 Chebyshev workspace
+  // optional preconditioner correction applied after the Chebyshev step: z += corr(r) (learned correction)
+  dErr (*correction)(void *ctx, const double *r, double *z) = nullptr;
+  void *correction_ctx = nullptr;
+  int64_t pc_applies = 0, correction_rejects = 0;
 };
 
 static dErr ksp_alloc(_p_dKSP *k) {
@@ -231,9 +306,38 @@ static dErr pc_setup(_p_dKSP *k) {
 }
 
 // z = M^{-1} r
+// Chebyshev-Jacobi on the Q1 matrix in FP32 (values, vectors and arithmetic), FP64 in/out
+static dErr pc_apply_fp32(_p_dKSP *k, const double *r, double *z) {
+  const int64_t n = k->n, nnz = k->pmat->nnz;
+  cudaStream_t s = k->op->fs->stream;
+  if (!k->d_w32) {
+    CUCHK(cudaMalloc(&k->d_w32, 5 * std::max<int64_t>(n, 1) * sizeof(float)));
+    CUCHK(cudaMalloc(&k->d_dinv32, std::max<int64_t>(n, 1) * sizeof(float)));
+    CUCHK(cudaMalloc(&k->d_val32, std::max<int64_t>(nnz, 1) * sizeof(float)));
+    k_convert<double, float><<<nb(n), 256, 0, s>>>(n, k->d_dinv, k->d_dinv32);
+    k_convert<double, float><<<nb(nnz), 256, 0, s>>>(nnz, k->pmat->d_val, k->d_val32);
+  }
+  float *r32 = k->d_w32, *z32 = r32 + n, *d32 = z32 + n, *w32 = d32 + n;
+  k_convert<double, float><<<nb(n), 256, 0, s>>>(n, r, r32);
+  const double theta = 0.5 * (k->emax + k->emin), delta = 0.5 * (k->emax - k->emin), sigma = theta / delta;
+  double rho = 1.0 / sigma;
+  k_cheb_first_t<float><<<nb(n), 256, 0, s>>>(n, k->d_dinv32, r32, (float)(1.0 / theta), d32, z32);
+  for (int it = 1; it < k->cheb_degree; it++) {
+    k_spmv<float><<<nb(n), 256, 0, s>>>(n, k->pmat->d_rowptr, k->pmat->d_col, k->d_val32, z32, w32);
+    const double rho1 = 1.0 / (2.0 * sigma - rho);
+    k_cheb_step_t<float><<<nb(n), 256, 0, s>>>(n, k->d_dinv32, r32, w32, (float)(rho1 * rho), (float)(2.0 * rho1 / delta), d32, z32);
+    rho = rho1;
+  }
+  k_convert<float, double><<<nb(n), 256, 0, s>>>(n, z32, z);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
 static dErr pc_apply(_p_dKSP *k, const double *r, double *z) {
   const int64_t n = k->n;
   cudaStream_t s = k->op->fs->stream;
+  k->pc_applies++;
+  if (k->pc == dPC_CHEBYSHEV_Q1 && k->pc_prec == dPREC_FP32) return pc_apply_fp32(k, r, z);
   if (k->pc == dPC_NONE) {
     CUCHK(cudaMemcpyAsync(z, r, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
     return 0;
@@ -305,11 +409,95 @@ static dErr cg_solve(_p_dKSP *k, const double *b, double *x, double rtol, int ma
   return 0;
 }
 
+dErr op_mult_prec(_p_dOperator *op, const double *x, double *y, dPrecision prec);
+
+// Right-preconditioned FGMRES(m) (Saad Alg. 9.6) with classical Gram-Schmidt applied twice (CGS2) in FP64.
+// Each cycle starts from the true residual b - A x computed with the FP64 operator; the operator applies
+// inside a cycle and the preconditioner run in k->pc_prec (FP32 for the mixed-precision solver). The
+// flexible (Z) basis makes the varying inner precision and a learned correction admissible.
+static dErr fgmres_solve(_p_dKSP *k, const double *b, double *x, double rtol, int maxit, int *its, double *rnorm) {
+  const int64_t n = k->n;
+  const int m = std::max(1, k->restart);
+  cudaStream_t s = k->op->fs->stream;
+  if (!k->d_V) {
+    CUCHK(cudaMalloc(&k->d_V, (size_t)(m + 1) * n * sizeof(double)));
+    CUCHK(cudaMalloc(&k->d_Z, (size_t)m * n * sizeof(double)));
+    CUCHK(cudaMalloc(&k->d_h, (size_t)(2 * (m + 2) + (m + 1) * RED_BLOCKS) * sizeof(double)));
+  }
+  double *V = k->d_V, *Z = k->d_Z, *h1 = k->d_h, *h2 = k->d_h + (m + 2), *mpart = k->d_h + 2 * (m + 2);
+  std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), yv(m), hcol(m + 2);
+  double bb;
+  DCHK(device_dot(n, b, b, k->d_part, k->d_s, s));
+  DCHK(read_scalar(k->d_s, &bb, s));
+  const double bn = sqrt(bb) > 0 ? sqrt(bb) : 1.0;
+  int total = 0;
+  double res = 0;
+  for (;;) {
+    DCHK(op_mult_prec(k->op, x, V, dPREC_FP64));
+    k_axpby<<<nb(n), 256, 0, s>>>(n, 1.0, nullptr, nullptr, b, -1.0, V);  // V0 = b - A x
+    double rr;
+    DCHK(device_dot(n, V, V, k->d_part, k->d_s, s));
+    DCHK(read_scalar(k->d_s, &rr, s));
+    const double beta = sqrt(rr);
+    res = beta / bn;
+    if (!(beta > rtol * bn) || total >= maxit) break;
+    k_scale_into<<<nb(n), 256, 0, s>>>(n, V, nullptr, 1.0 / beta, V);
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int j = 0;
+    for (; j < m && total < maxit;) {
+      double *w = V + (size_t)(j + 1) * n;
+      DCHK(pc_apply(k, V + (size_t)j * n, Z + (size_t)j * n));
+      DCHK(op_mult_prec(k->op, Z + (size_t)j * n, w, k->pc_prec));
+      const int nv = j + 1;
+      k_mdot_partial<<<dim3(RED_BLOCKS, nv), RED_THREADS, 0, s>>>(n, nv, V, w, mpart);
+      k_mdot_final<<<nv, 1024, 0, s>>>(mpart, h1, nullptr);
+      k_maxpy<<<nb(n), 256, 0, s>>>(n, nv, -1.0, h1, V, w);
+      k_mdot_partial<<<dim3(RED_BLOCKS, nv), RED_THREADS, 0, s>>>(n, nv, V, w, mpart);
+      k_mdot_final<<<nv, 1024, 0, s>>>(mpart, h2, h1);
+      k_maxpy<<<nb(n), 256, 0, s>>>(n, nv, -1.0, h2, V, w);
+      DCHK(device_dot(n, w, w, k->d_part, h1 + nv, s));
+      CUCHK(cudaMemcpyAsync(hcol.data(), h1, (nv + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
+      CUCHK(cudaStreamSynchronize(s));
+      const double hn = sqrt(hcol[nv]);
+      if (hn > 0) k_scale_into<<<nb(n), 256, 0, s>>>(n, w, nullptr, 1.0 / hn, w);
+      for (int i = 0; i < nv; i++) H[(size_t)i * m + j] = hcol[i];
+      for (int i = 0; i < j; i++) {  // previous Givens rotations
+        const double a = H[(size_t)i * m + j], c = H[(size_t)(i + 1) * m + j];
+        H[(size_t)i * m + j] = cs[i] * a + sn[i] * c;
+        H[(size_t)(i + 1) * m + j] = -sn[i] * a + cs[i] * c;
+      }
+      const double a = H[(size_t)j * m + j], r = hypot(a, hn);
+      cs[j] = r > 0 ? a / r : 1.0;
+      sn[j] = r > 0 ? hn / r : 0.0;
+      H[(size_t)j * m + j] = r;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = cs[j] * g[j];
+      total++;
+      j++;
+      if (!(fabs(g[j]) > rtol * bn) || hn == 0) break;
+    }
+    for (int i = j - 1; i >= 0; i--) {  // H y = g, upper triangular
+      double t = g[i];
+      for (int l = i + 1; l < j; l++) t -= H[(size_t)i * m + l] * yv[l];
+      yv[i] = H[(size_t)i * m + i] != 0 ? t / H[(size_t)i * m + i] : 0.0;
+    }
+    CUCHK(cudaMemcpyAsync(h1, yv.data(), j * sizeof(double), cudaMemcpyHostToDevice, s));
+    k_maxpy<<<nb(n), 256, 0, s>>>(n, j, 1.0, h1, Z, x);
+    CUCHK(cudaStreamSynchronize(s));
+    CUCHK(cudaGetLastError());
+  }
+  *its = total;
+  *rnorm = res;
+  if (res > rtol) return set_error("FGMRES did not converge in %d iterations (relative residual %g)", maxit, res);
+  return 0;
+}
+
 extern "C" {
 
 dErr dKSPCreate(dOperator op, dMat pmat, dKSPType type, dPCType pc, dKSP *ksp) {
   if (!op || !ksp) return set_error("dKSPCreate: null argument");
-  if (type != dKSP_CG) return set_error("KSP type %d not built yet", (int)type);
+  if (type != dKSP_CG && type != dKSP_FGMRES) return set_error("KSP type %d not supported", (int)type);
   _p_dKSP *k = new _p_dKSP();
   k->op = op;
   k->pmat = pmat;
@@ -327,6 +515,12 @@ dErr dKSPDestroy(dKSP *ksp) {
   cudaFree(k->d_work);
   cudaFree(k->d_part);
   cudaFree(k->d_s);
+  cudaFree(k->d_V);
+  cudaFree(k->d_Z);
+  cudaFree(k->d_h);
+  cudaFree(k->d_w32);
+  cudaFree(k->d_dinv32);
+  cudaFree(k->d_val32);
   delete k;
   *ksp = nullptr;
   return 0;
@@ -337,8 +531,19 @@ dErr dKSPSetOptions(dKSP ksp, dInt cheb_degree, dPrecision pc_precision, dInt re
   if (cheb_degree < 1) return set_error("Chebyshev degree must be >= 1");
   ksp->cheb_degree = cheb_degree;
   ksp->pc_prec = pc_precision;
+  if (restart < 1 || restart > 200) return set_error("restart %d out of range [1,200]", restart);
+  if (ksp->restart != restart) {
+    cudaFree(ksp->d_V);
+    cudaFree(ksp->d_Z);
+    cudaFree(ksp->d_h);
+    ksp->d_V = ksp->d_Z = ksp->d_h = nullptr;
+  }
   ksp->restart = restart;
   ksp->pc_ready = false;
+  cudaFree(ksp->d_w32);
+  cudaFree(ksp->d_dinv32);
+  cudaFree(ksp->d_val32);
+  ksp->d_w32 = nullptr, ksp->d_dinv32 = nullptr, ksp->d_val32 = nullptr;
   return 0;
 }
 
@@ -348,7 +553,7 @@ dErr dKSPSolve(dKSP ksp, const dScalar *b, dScalar *x, dReal rtol, dInt maxit, d
   DCHK(pc_setup(ksp));
   int it = 0;
   double rn = 0;
-  dErr e = cg_solve(ksp, b, x, rtol, maxit, &it, &rn);
+  dErr e = ksp->type == dKSP_FGMRES ? fgmres_solve(ksp, b, x, rtol, maxit, &it, &rn) : cg_solve(ksp, b, x, rtol, maxit, &it, &rn);
   if (its) *its = it;
   if (rnorm) *rnorm = rn;
   return e;

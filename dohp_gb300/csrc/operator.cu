@@ -20,6 +20,7 @@
 using namespace dgb;
 
 dErr fs_restrict(_p_dFS *fs, const double *x, double *g, int add);
+dErr fs_restrict32(_p_dFS *fs, const float *x, double *g, int add);
 
 namespace {
 
@@ -112,7 +113,7 @@ struct Tile {
 // y_exp = (B^T Dq^T) G (Dq B) E x for a uniform-degree scalar space; T = arithmetic type
 template <int N, typename T>
 __global__ void __launch_bounds__(256) k_diffusion(int64_t nelem, const int32_t *__restrict__ emap, int64_t n,
-                                                   const T *__restrict__ x, const T *__restrict__ geo,
+                                                   const double *__restrict__ x, const T *__restrict__ geo,
                                                    const double *__restrict__ tab, T *__restrict__ yexp) {
   constexpr int N3 = Tile<N>::N3, EPB = Tile<N>::EPB, NN = N * N;
   __shared__ T sB[NN], sD[NN];
@@ -128,7 +129,7 @@ __global__ void __launch_bounds__(256) k_diffusion(int64_t nelem, const int32_t 
   // gather through E (homogeneous Dirichlet: closure entries beyond n are zero)
   for (int t = tid; t < tot; t += blockDim.x) {
     const int32_t c = emap[e0 * N3 + t];
-    S[0][t] = c < n ? x[c] : (T)0;
+    S[0][t] = c < n ? (T)x[c] : (T)0;
   }
   __syncthreads();
   // interpolate to Gauss points: x pass, y pass, z pass
@@ -218,11 +219,169 @@ __global__ void __launch_bounds__(256) k_diffusion(int64_t nelem, const int32_t 
 }
 
 template <int N, typename T>
-dErr launch_diffusion(_p_dFS *fs, const T *x, const T *geo, T *yexp) {
+dErr launch_diffusion(_p_dFS *fs, const double *x, const T *geo, T *yexp) {
   constexpr int EPB = Tile<N>::EPB;
   const unsigned grid = (unsigned)((fs->nelem + EPB - 1) / EPB);
   const double *tab = fs->d_fast_tab + (size_t)2 * (N - 2) * MAXP * MAXP;
   k_diffusion<N, T><<<grid, 256, 0, fs->stream>>>(fs->nelem, fs->d_emap, fs->n, x, geo, tab, yexp);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+// ------------------------------------------------------------------------------------------ fused elasticity
+// ElastPointwiseJacobian at F = I (src/fs/tests/elast.c:269-280): eps = sym(grad u),
+// dv = w (lambda tr(eps) I + 2 mu eps). Three components (bs = 3, interleaved), geometry {J^-1, w det J}.
+template <int N>
+struct ETile {
+  static constexpr int EPB = N <= 3 ? 8 : N == 4 ? 4 : N == 5 ? 2 : 1;
+};
+
+template <int N, typename T>
+__global__ void __launch_bounds__(256) k_elasticity(int64_t nelem, const int32_t *__restrict__ emap, int64_t n,
+                                                    const double *__restrict__ x, const T *__restrict__ geo,
+                                                    const double *__restrict__ tab, T lam, T mu, T *__restrict__ yexp) {
+  constexpr int N3 = N * N * N, EPB = ETile<N>::EPB, NN = N * N, L = EPB * N3;
+  __shared__ T sB[NN], sD[NN];
+  extern __shared__ unsigned char smraw[];
+  T *A = reinterpret_cast<T *>(smraw), *Bf = A + L, *G = Bf + L;  // ping, pong, 9 gradient buffers [d][k][L]
+  const int tid = threadIdx.x;
+  const int64_t e0 = (int64_t)blockIdx.x * EPB;
+  const int ne = (int)min((int64_t)EPB, nelem - e0);
+  const int tot = ne * N3;
+  for (int i = tid; i < NN; i += blockDim.x) {
+    sB[i] = (T)tab[i];
+    sD[i] = (T)tab[MAXP * MAXP + i];
+  }
+  __syncthreads();
+  for (int d = 0; d < 3; d++) {
+    for (int t = tid; t < tot; t += blockDim.x) {
+      const int32_t c = emap[e0 * N3 + t];
+      A[t] = c < n ? (T)x[(int64_t)c * 3 + d] : (T)0;
+    }
+    __syncthreads();
+    for (int t = tid; t < tot; t += blockDim.x) {
+      const int el = t / N3, r = t - el * N3, a = r / NN, jk = r - a * NN;
+      const T *in = &A[el * N3 + jk];
+      T s = 0;
+#pragma unroll
+      for (int i = 0; i < N; i++) s += sB[a * N + i] * in[i * NN];
+      Bf[t] = s;
+    }
+    __syncthreads();
+    for (int t = tid; t < tot; t += blockDim.x) {
+      const int el = t / N3, r = t - el * N3, a = r / NN, b = (r / N) % N, k = r % N;
+      const T *in = &Bf[el * N3 + a * NN + k];
+      T s = 0;
+#pragma unroll
+      for (int j = 0; j < N; j++) s += sB[b * N + j] * in[j * N];
+      A[t] = s;
+    }
+    __syncthreads();
+    for (int t = tid; t < tot; t += blockDim.x) {
+      const int el = t / N3, r = t - el * N3, ab = r / N, c = r % N;
+      const T *in = &A[el * N3 + ab * N];
+      T s = 0;
+#pragma unroll
+      for (int k = 0; k < N; k++) s += sB[c * N + k] * in[k];
+      Bf[t] = s;
+    }
+    __syncthreads();
+    for (int t = tid; t < tot; t += blockDim.x) {
+      const int el = t / N3, r = t - el * N3, a = r / NN, b = (r / N) % N, c = r % N;
+      const T *U = &Bf[el * N3];
+      T g0 = 0, g1 = 0, g2 = 0;
+#pragma unroll
+      for (int i = 0; i < N; i++) {
+        g0 += sD[a * N + i] * U[i * NN + b * N + c];
+        g1 += sD[b * N + i] * U[a * NN + i * N + c];
+        g2 += sD[c * N + i] * U[a * NN + b * N + i];
+      }
+      G[(d * 3 + 0) * L + t] = g0;
+      G[(d * 3 + 1) * L + t] = g1;
+      G[(d * 3 + 2) * L + t] = g2;
+    }
+    __syncthreads();
+  }
+  // pointwise: physical gradient, strain, stress, back to reference directions
+  for (int t = tid; t < tot; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3;
+    const T *gq = geo + (e0 + el) * 10 * N3 + r;
+    T Ji[9];
+#pragma unroll
+    for (int i = 0; i < 9; i++) Ji[i] = gq[i * N3];
+    const T w = gq[9 * N3];
+    T Du[9];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const T a0 = G[(d * 3 + 0) * L + t], a1 = G[(d * 3 + 1) * L + t], a2 = G[(d * 3 + 2) * L + t];
+#pragma unroll
+      for (int e = 0; e < 3; e++) Du[d * 3 + e] = a0 * Ji[0 * 3 + e] + a1 * Ji[1 * 3 + e] + a2 * Ji[2 * 3 + e];
+    }
+    const T e00 = Du[0], e11 = Du[4], e22 = Du[8];
+    const T e01 = (T)0.5 * (Du[1] + Du[3]), e02 = (T)0.5 * (Du[2] + Du[6]), e12 = (T)0.5 * (Du[5] + Du[7]);
+    const T tr = e00 + e11 + e22;
+    T S[9];
+    S[0] = w * (lam * tr + 2 * mu * e00);
+    S[4] = w * (lam * tr + 2 * mu * e11);
+    S[8] = w * (lam * tr + 2 * mu * e22);
+    S[1] = S[3] = w * (2 * mu * e01);
+    S[2] = S[6] = w * (2 * mu * e02);
+    S[5] = S[7] = w * (2 * mu * e12);
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+      for (int k = 0; k < 3; k++) G[(d * 3 + k) * L + t] = S[d * 3 + 0] * Ji[k * 3 + 0] + S[d * 3 + 1] * Ji[k * 3 + 1] + S[d * 3 + 2] * Ji[k * 3 + 2];
+  }
+  __syncthreads();
+  for (int d = 0; d < 3; d++) {
+    for (int t = tid; t < tot; t += blockDim.x) {
+      const int el = t / N3, r = t - el * N3, a = r / NN, b = (r / N) % N, c = r % N;
+      const T *V0 = &G[(d * 3 + 0) * L + el * N3], *V1 = &G[(d * 3 + 1) * L + el * N3], *V2 = &G[(d * 3 + 2) * L + el * N3];
+      T s = 0;
+#pragma unroll
+      for (int i = 0; i < N; i++)
+        s += sD[i * N + a] * V0[i * NN + b * N + c] + sD[i * N + b] * V1[a * NN + i * N + c] + sD[i * N + c] * V2[a * NN + b * N + i];
+      A[t] = s;
+    }
+    __syncthreads();
+    for (int t = tid; t < tot; t += blockDim.x) {
+      const int el = t / N3, r = t - el * N3, ab = r / N, k = r % N;
+      const T *in = &A[el * N3 + ab * N];
+      T s = 0;
+#pragma unroll
+      for (int c = 0; c < N; c++) s += sB[c * N + k] * in[c];
+      Bf[t] = s;
+    }
+    __syncthreads();
+    for (int t = tid; t < tot; t += blockDim.x) {
+      const int el = t / N3, r = t - el * N3, a = r / NN, j = (r / N) % N, k = r % N;
+      const T *in = &Bf[el * N3 + a * NN + k];
+      T s = 0;
+#pragma unroll
+      for (int b = 0; b < N; b++) s += sB[b * N + j] * in[b * N];
+      A[t] = s;
+    }
+    __syncthreads();
+    for (int t = tid; t < tot; t += blockDim.x) {
+      const int el = t / N3, r = t - el * N3, i = r / NN, jk = r - i * NN;
+      const T *in = &A[el * N3 + jk];
+      T s = 0;
+#pragma unroll
+      for (int a = 0; a < N; a++) s += sB[a * N + i] * in[a * NN];
+      yexp[(e0 * N3 + t) * 3 + d] = s;
+    }
+    __syncthreads();
+  }
+}
+
+template <int N, typename T>
+dErr launch_elasticity(_p_dFS *fs, const double *x, const T *geo, T lam, T mu, T *yexp) {
+  constexpr int EPB = ETile<N>::EPB;
+  const unsigned grid = (unsigned)((fs->nelem + EPB - 1) / EPB);
+  const double *tab = fs->d_fast_tab + (size_t)2 * (N - 2) * MAXP * MAXP;
+  const size_t smem = (size_t)11 * EPB * N * N * N * sizeof(T);
+  CUCHK(cudaFuncSetAttribute(k_elasticity<N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_elasticity<N, T><<<grid, 256, smem, fs->stream>>>(fs->nelem, fs->d_emap, fs->n, x, geo, tab, lam, mu, yexp);
   CUCHK(cudaGetLastError());
   return 0;
 }
@@ -263,7 +422,7 @@ dErr op_compute_geometry(_p_dOperator *op) {
 }
 
 template <typename T>
-static dErr diffusion_apply_t(_p_dFS *fs, const T *x, const T *geo, T *yexp) {
+static dErr diffusion_apply_t(_p_dFS *fs, const double *x, const T *geo, T *yexp) {
   if (!fs->uniform) return set_error("fused diffusion apply needs a uniform-degree space (hp path not built yet)");
   switch (fs->p + 1) {
     case 2: return launch_diffusion<2, T>(fs, x, geo, yexp);
@@ -278,18 +437,70 @@ static dErr diffusion_apply_t(_p_dFS *fs, const T *x, const T *geo, T *yexp) {
   return set_error("degree %d not supported", fs->p);
 }
 
+template <typename T>
+static dErr elasticity_apply_t(_p_dFS *fs, const double *x, const T *geo, T lam, T mu, T *yexp) {
+  if (!fs->uniform) return set_error("fused elasticity apply needs a uniform-degree space (use the hp path)");
+  switch (fs->p + 1) {
+    case 2: return launch_elasticity<2, T>(fs, x, geo, lam, mu, yexp);
+    case 3: return launch_elasticity<3, T>(fs, x, geo, lam, mu, yexp);
+    case 4: return launch_elasticity<4, T>(fs, x, geo, lam, mu, yexp);
+    case 5: return launch_elasticity<5, T>(fs, x, geo, lam, mu, yexp);
+    case 6: return launch_elasticity<6, T>(fs, x, geo, lam, mu, yexp);
+    case 7: return launch_elasticity<7, T>(fs, x, geo, lam, mu, yexp);
+    case 8: return launch_elasticity<8, T>(fs, x, geo, lam, mu, yexp);
+    case 9: return launch_elasticity<9, T>(fs, x, geo, lam, mu, yexp);
+  }
+  return set_error("degree %d not supported", fs->p);
+}
+
 dErr op_mult_expanded(_p_dOperator *op, const double *x, double *yexp) {
   _p_dFS *fs = op->fs;
-  if (op->kind != dOP_DIFFUSION) return set_error("operator kind %d not built yet", (int)op->kind);
   DCHK(op_compute_geometry(op));
-  return diffusion_apply_t<double>(fs, x, op->d_geo, yexp);
+  if (op->kind == dOP_DIFFUSION) return diffusion_apply_t<double>(fs, x, op->d_geo, yexp);
+  if (op->kind == dOP_ELASTICITY) return elasticity_apply_t<double>(fs, x, op->d_geo, op->lam, op->mu, yexp);
+  return set_error("operator kind %d not built yet", (int)op->kind);
+}
+
+__global__ void k_to_float(int64_t n, const double *__restrict__ a, float *__restrict__ b) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+
+// FP32 element arithmetic (geometric factors rounded to FP32 once), FP64 input and FP64 restriction
+static dErr op_mult_fp32(_p_dOperator *op, const double *x, double *y) {
+  _p_dFS *fs = op->fs;
+  if (op->kind != dOP_DIFFUSION && op->kind != dOP_ELASTICITY)
+    return set_error("FP32 apply for operator kind %d not built yet", (int)op->kind);
+  DCHK(op_compute_geometry(op));
+  const int64_t ng = fs->nq * (op->kind == dOP_ELASTICITY ? 10 : 6);
+  if (!op->d_geo32) {
+    CUCHK(cudaMalloc(&op->d_geo32, ng * sizeof(float)));
+    k_to_float<<<(unsigned)((ng + 255) / 256), 256, 0, fs->stream>>>(ng, op->d_geo, op->d_geo32);
+    CUCHK(cudaGetLastError());
+  }
+  if (!op->d_y32) CUCHK(cudaMalloc(&op->d_y32, fs->nexp * fs->bs * sizeof(float)));
+  if (op->kind == dOP_ELASTICITY)
+    DCHK(elasticity_apply_t<float>(fs, x, op->d_geo32, (float)op->lam, (float)op->mu, op->d_y32));
+  else
+    DCHK(diffusion_apply_t<float>(fs, x, op->d_geo32, op->d_y32));
+  return fs_restrict32(fs, op->d_y32, y, 0);
 }
 
 dErr op_mult(_p_dOperator *op, const double *x, double *y) {
   _p_dFS *fs = op->fs;
+  if (op->prec == dPREC_FP32) return op_mult_fp32(op, x, y);
   if (!op->d_yexp) CUCHK(cudaMalloc(&op->d_yexp, fs->nexp * fs->bs * sizeof(double)));
   DCHK(op_mult_expanded(op, x, op->d_yexp));
   return fs_restrict(fs, op->d_yexp, y, 0);
+}
+
+// apply in a given precision regardless of the operator's default (used by the mixed-precision solvers)
+dErr op_mult_prec(_p_dOperator *op, const double *x, double *y, dPrecision prec) {
+  const dPrecision save = op->prec;
+  op->prec = prec;
+  const dErr e = op_mult(op, x, y);
+  op->prec = save;
+  return e;
 }
 
 extern "C" dErr dOperatorMultExpanded(dOperator op, const dScalar *x, dScalar *yexp) {

@@ -182,3 +182,46 @@ def test_negative_jacobian_is_an_error():
     x = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
     with pytest.raises(dg.DohpError, match="Negative Jacobian"):
         op.mult(x, torch.zeros_like(x))
+
+
+def _poisson_setup(npoints=(6, 6, 6), degree=4, seed=1):
+    fs = dg.FS(npoints, degree=degree, perturb=0.1, seed=seed)
+    o = po.FS(*npoints, degree=degree, perturb=0.1, seed=seed)
+    op = fs.operator()
+    J = fs.matrix()
+    J.assemble()
+    b = np.random.default_rng(seed).uniform(-1, 1, fs.n)
+    return fs, o, op, J, b
+
+
+def test_fp32_apply_accuracy():
+    fs, o, op, _, b = _poisson_setup()
+    op.set_precision(dg.dPREC_FP32)
+    y = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
+    op.mult(dev(b), y)
+    err = rel_err(host(y), o.apply(b))
+    assert 1e-9 < err < 1e-5, err  # FP32 element arithmetic, FP64 restriction
+
+
+@pytest.mark.parametrize("inner", [0, 1])
+def test_fgmres_reaches_rtol(inner):
+    """FGMRES(30) with Q1 Chebyshev-Jacobi; inner=1: FP32 operator applies and FP32 preconditioner inside
+    each cycle, FP64 residual at every restart and FP64 orthogonalisation (mixed precision)."""
+    fs, o, op, J, b = _poisson_setup()
+    ksp = dg.KSP(op, J, ksp_type=dg.dKSP_FGMRES, pc=dg.dPC_CHEBYSHEV_Q1, cheb_degree=3, inner_prec=inner, restart=30)
+    x = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
+    its, rn = ksp.solve(dev(b), x, rtol=1e-8, maxit=400)
+    assert rn <= 1e-8
+    r = b - o.apply(host(x))
+    assert np.linalg.norm(r) <= 1.05e-8 * np.linalg.norm(b)
+
+
+def test_fgmres_deterministic():
+    fs, o, op, J, b = _poisson_setup((5, 5, 5), 3)
+    xs = []
+    for _ in range(2):
+        ksp = dg.KSP(op, J, ksp_type=dg.dKSP_FGMRES, inner_prec=1)
+        x = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
+        ksp.solve(dev(b), x, rtol=1e-8)
+        xs.append(host(x))
+    np.testing.assert_array_equal(xs[0], xs[1])
