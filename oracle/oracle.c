@@ -435,7 +435,40 @@ struct or_fs {
   int64_t n, nc, nexp;
   int32_t *xstart, *emap, *edeg;
   double *xexp;            /* expanded coordinates [nr][8][3] */
+  int hp;                  /* 1: interpolation constraints on p-nonconforming entities (extension) */
+  double gll[16][16];      /* GLL nodes per degree (index p) */
+  /* constrained rows (hp): emap[r] = -2 - k refers to entries cptr[k]..cptr[k+1] */
+  int64_t ncrow, ccap, nent, entcap;
+  int64_t *cptr;
+  int32_t *ccol;
+  double *cval;
+  /* E as CSR over expanded rows (built after the constraints) */
+  int64_t *eptr;
+  int32_t *ecol;
+  double *eval;
 };
+
+/* Lagrange basis on the degree-p GLL nodes at t */
+static void gll_lagrange(const or_fs *m, int p, double t, double *L)
+{
+  const double *x = m->gll[p];
+  for (int j = 0; j <= p; j++) {
+    long double v = 1;
+    for (int k = 0; k <= p; k++)
+      if (k != j) v *= ((long double)t - x[k]) / ((long double)x[j] - x[k]);
+    L[j] = (double)v;
+  }
+}
+
+typedef struct { int n; int32_t col[2048]; double w[2048]; } rowacc;
+static void acc_add(rowacc *a, int32_t col, double w)
+{
+  for (int i = 0; i < a->n; i++)
+    if (a->col[i] == col) { a->w[i] += w; return; }
+  a->col[a->n] = col;
+  a->w[a->n] = w;
+  a->n++;
+}
 
 static int64_t VI(const or_fs *m, int i, int j, int k) { return ((int64_t)i * m->ny + j) * m->nz + k; }
 
@@ -691,6 +724,92 @@ static int dGeomPermQuadIndex(int perm, const int dim[2], const int ij[2], int *
 
 /* dJacobiAddConstraints_Tensor for a HEX (tensor.c:360-468): one row of E per expanded node of the
  * element; the edge/face extraction and traversal tables are the reference's (table as reference). */
+/* ---- interpolation constraints for p-nonconforming entities (extension; the reference errors,
+ * src/jacobi/impls/tensor/tensor.c:417). An edge of degree q carries the polynomial through its GLL nodes
+ * (vertex, q-1 interior dofs in the edge direction, vertex); a face of degree q carries the tensor
+ * polynomial through its (q+1)^2 GLL grid in its own frame (u along fv0->fv1, v along fv0->fv3) whose
+ * corner values are the vertices, boundary values the edge polynomials and interior values its dofs. */
+static void edge_poly(const or_fs *m, int32_t edge, double t, double scale, rowacc *a)
+{
+  const int q = m->deg[edge].x;
+  const int64_t *ev = m->econn + 2 * (edge - m->nv);
+  double L[16];
+  gll_lagrange(m, q, t, L);
+  for (int k = 0; k <= q; k++) {
+    const int32_t col = k == 0 ? m->gcoff[ev[0]] : k == q ? m->gcoff[ev[1]] : m->gcoff[edge] + (k - 1);
+    acc_add(a, col, scale * L[k]);
+  }
+}
+
+static void face_poly(const or_fs *m, int32_t face, double u, double v, rowacc *a)
+{
+  const int qu = m->deg[face].x, qv = m->deg[face].y;
+  const int64_t *fv = m->fconn + 4 * (face - m->nv - m->ne);
+  double Lu[16], Lv[16];
+  gll_lagrange(m, qu, u, Lu);
+  gll_lagrange(m, qv, v, Lv);
+  for (int r = 0; r <= qu; r++)
+    for (int c = 0; c <= qv; c++) {
+      const double w = Lu[r] * Lv[c];
+      const int bu = r == 0 || r == qu, bv = c == 0 || c == qv;
+      if (bu && bv) {
+        const int corner = r == 0 ? (c == 0 ? 0 : 3) : (c == 0 ? 1 : 2);
+        acc_add(a, m->gcoff[fv[corner]], w);
+      } else if (!bu && !bv) {
+        acc_add(a, m->gcoff[face] + (r - 1) * (qv - 1) + (c - 1), w);
+      } else {
+        int side;
+        double tau;
+        if (c == 0) side = 0, tau = m->gll[qu][r];
+        else if (r == qu) side = 1, tau = m->gll[qv][c];
+        else if (c == qv) side = 2, tau = -m->gll[qu][r];
+        else side = 3, tau = -m->gll[qv][c];
+        const int32_t slot = m->adjoff[face] + side;
+        edge_poly(m, m->adjind[slot], m->adjperm[slot] == 0 ? tau : -tau, w, a);
+      }
+    }
+}
+
+/* element-face traversal coordinates (s,t) -> face frame (u,v) for the 8 orientations of
+ * dGeomPermQuadIndex (tensor.c:328-345) */
+static void face_frame(int perm, double s, double t, double *u, double *v)
+{
+  switch (perm) {
+  case 0: *u = s, *v = t; break;
+  case 1: *u = t, *v = -s; break;
+  case 2: *u = -s, *v = -t; break;
+  case 3: *u = -t, *v = s; break;
+  case 4: *u = t, *v = s; break;
+  case 5: *u = -s, *v = t; break;
+  case 6: *u = -t, *v = -s; break;
+  default: *u = s, *v = -t; break;
+  }
+}
+
+static int push_row(or_fs *m, int rw, const rowacc *a)
+{
+  if (m->ncrow + 1 >= m->ccap) {
+    m->ccap = m->ccap ? 2 * m->ccap : 1024;
+    m->cptr = realloc(m->cptr, sizeof(int64_t) * (m->ccap + 1));
+  }
+  if (m->ncrow == 0) m->cptr[0] = 0;
+  for (int i = 0; i < a->n; i++) {
+    if (fabs(a->w[i]) < 1e-14) continue; /* exact zeros of the Lagrange weights (node coincidences) */
+    if (m->nent == m->entcap) {
+      m->entcap = m->entcap ? 2 * m->entcap : 4096;
+      m->ccol = realloc(m->ccol, sizeof(int32_t) * m->entcap);
+      m->cval = realloc(m->cval, sizeof(double) * m->entcap);
+    }
+    m->ccol[m->nent] = a->col[i];
+    m->cval[m->nent] = a->w[i];
+    m->nent++;
+  }
+  m->cptr[m->ncrow + 1] = m->nent;
+  m->emap[rw] = (int32_t)(-2 - m->ncrow);
+  m->ncrow++;
+  return 0;
+}
+
 static int add_constraints_hex(or_fs *m, int64_t r, int xs)
 {
   static const struct { int f, e, o; } fe[12][2] = {
@@ -736,7 +855,19 @@ static int add_constraints_hex(or_fs *m, int64_t r, int xs)
         {{0, 0, 1}, 2, 1, d2 - 1}, {{d0 - 1, 0, 1}, 2, 1, d2 - 1}, {{d0 - 1, d1 - 1, 1}, 2, 1, d2 - 1}, {{0, d1 - 1, 1}, 2, 1, d2 - 1}};
     for (int i = 0; i < 12; i++) {
       const int *st = E[i].start, incd = E[i].incd, inci = E[i].inci, end = E[i].end;
-      if (m->deg[e[i]].x != d[incd] - 1) return or_fail("degree does not agree, p-nonconforming");
+      if (m->deg[e[i]].x != d[incd] - 1) {
+        if (!m->hp) return or_fail("degree does not agree, p-nonconforming");
+        /* extension: element edge nodes interpolate the lower-degree edge polynomial */
+        for (int j = st[incd]; j != end; j += inci) {
+          const int rw = xs + (st[0] * d1 + st[1]) * d2 + st[2] + (j - st[incd]) * scan[incd];
+          const double tau = inci * m->gll[d[incd] - 1][j];
+          rowacc *a = calloc(1, sizeof(rowacc));
+          edge_poly(m, e[i], eP[i] == 0 ? tau : -tau, 1.0, a);
+          if (push_row(m, rw, a)) { free(a); return -1; }
+          free(a);
+        }
+        continue;
+      }
       for (int j = st[incd]; j != end; j += inci) {
         int rw = xs + (st[0] * d1 + st[1]) * d2 + st[2] + (j - st[incd]) * scan[incd], col;
         if (eP[i] == 0) col = is[e[i]] + (j - st[incd]) / inci;
@@ -753,6 +884,22 @@ static int add_constraints_hex(or_fs *m, int64_t r, int xs)
         {{1, 1, 0}, {1, 0}, {1, 1}, {d1 - 1, d0 - 1}}, {{1, 1, d2 - 1}, {0, 1}, {1, 1}, {d0 - 1, d1 - 1}}};
     for (int i = 0; i < 6; i++) {
       const int *st = F[i].start, *incd = F[i].incd, *inc = F[i].inc, *end = F[i].end;
+      if (m->deg[f[i]].x != d[incd[0]] - 1 || m->deg[f[i]].y != d[incd[1]] - 1) {
+        if (!m->hp) return or_fail("degree does not agree, p-nonconforming");
+        /* extension: element face nodes interpolate the lower-degree face polynomial in the face's frame */
+        for (int j = st[incd[0]]; j != end[0]; j += inc[0])
+          for (int k = st[incd[1]]; k != end[1]; k += inc[1]) {
+            const int rw = xs + (st[0] * d1 + st[1]) * d2 + st[2] + (j - st[incd[0]]) * scan[incd[0]] + (k - st[incd[1]]) * scan[incd[1]];
+            const double s = inc[0] * m->gll[d[incd[0]] - 1][j], t = inc[1] * m->gll[d[incd[1]] - 1][k];
+            double u, w;
+            face_frame(fP[i], s, t, &u, &w);
+            rowacc *a = calloc(1, sizeof(rowacc));
+            face_poly(m, f[i], u, w, a);
+            if (push_row(m, rw, a)) { free(a); return -1; }
+            free(a);
+          }
+        continue;
+      }
       for (int j = st[incd[0]]; j != end[0]; j += inc[0])
         for (int k = st[incd[1]]; k != end[1]; k += inc[1]) {
           const int dim[2] = {d[incd[0]], d[incd[1]]};
@@ -777,6 +924,8 @@ or_fs *or_fs_create(int nx, int ny, int nz, const double box[6], double perturb,
   if (nx < 2 || ny < 2 || nz < 2) { or_fail("need at least 2 vertices per direction"); return NULL; }
   or_fs *m = calloc(1, sizeof(or_fs));
   m->nx = nx; m->ny = ny; m->nz = nz; m->bs = bs;
+  m->hp = elem_degree != NULL;
+  for (int p = 1; p < 16; p++) { double w[16]; or_lobatto(p + 1, m->gll[p], w); }
   if (build_mesh(m, box, perturb, seed) || build_adjacency(m) || propagate_degree(m, degree, elem_degree)) { or_fs_destroy(m); return NULL; }
   /* boundary face sets 0..3 -> 100 (walls), 5 -> 200 (top), 4 -> 300 (bottom) (genblock.c:409-421) */
   const int set_of_face[6] = {0, 0, 0, 0, 2, 1};
@@ -818,7 +967,29 @@ or_fs *or_fs_create(int nx, int ny, int nz, const double box[6], double perturb,
   for (int64_t r = 0; r < m->nr; r++)
     if (add_constraints_hex(m, r, m->xstart[r])) { or_fs_destroy(m); return NULL; }
   for (int64_t i = 0; i < m->nexp; i++)
-    if (m->emap[i] < 0) { or_fail("expanded node %lld has no constraint", (long long)i); or_fs_destroy(m); return NULL; }
+    if (m->emap[i] == -1) { or_fail("expanded node %lld has no constraint", (long long)i); or_fs_destroy(m); return NULL; }
+  /* E as CSR: Boolean rows (1.0 at emap) and interpolation rows (columns ascending) */
+  m->eptr = malloc(sizeof(int64_t) * (m->nexp + 1));
+  {
+    int64_t cnt = 0;
+    for (int64_t i = 0; i < m->nexp; i++) cnt += m->emap[i] >= 0 ? 1 : m->cptr[-2 - m->emap[i] + 1] - m->cptr[-2 - m->emap[i]];
+    m->ecol = malloc(sizeof(int32_t) * (cnt ? cnt : 1));
+    m->eval = malloc(sizeof(double) * (cnt ? cnt : 1));
+    int64_t o = 0;
+    for (int64_t i = 0; i < m->nexp; i++) {
+      m->eptr[i] = o;
+      if (m->emap[i] >= 0) { m->ecol[o] = m->emap[i]; m->eval[o] = 1.0; o++; continue; }
+      const int64_t k = -2 - m->emap[i], b = m->cptr[k], e2 = m->cptr[k + 1];
+      for (int64_t t = b; t < e2; t++) { /* insertion by column */
+        int64_t pos = o;
+        while (pos > m->eptr[i] && m->ecol[pos - 1] > m->ccol[t]) { m->ecol[pos] = m->ecol[pos - 1]; m->eval[pos] = m->eval[pos - 1]; pos--; }
+        m->ecol[pos] = m->ccol[t];
+        m->eval[pos] = m->cval[t];
+        o++;
+      }
+    }
+    m->eptr[m->nexp] = o;
+  }
   /* expanded coordinates, tensor vertex order (dFSCreateGeometryFromMesh_Private fsgeom.c:146-156) */
   static const int connidx[8] = {0, 4, 3, 7, 1, 5, 2, 6};
   m->xexp = malloc(sizeof(double) * 24 * m->nr);
@@ -835,6 +1006,7 @@ void or_fs_destroy(or_fs *m)
   free(m->adjoff); free(m->adjind); free(m->adjperm); free(m->deg);
   free(m->ordered); free(m->goff); free(m->gcoff); free(m->inodes);
   free(m->xstart); free(m->emap); free(m->edeg); free(m->xexp);
+  free(m->cptr); free(m->ccol); free(m->cval); free(m->eptr); free(m->ecol); free(m->eval);
   free(m);
 }
 
@@ -844,6 +1016,11 @@ void or_fs_sizes(const or_fs *m, int64_t out[8])
   out[5] = m->nv; out[6] = m->ne; out[7] = m->nf;
 }
 const int32_t *or_fs_emap(const or_fs *m) { return m->emap; }
+int64_t or_fs_ecsr(const or_fs *m, const int64_t **eptr, const int32_t **ecol, const double **eval)
+{
+  *eptr = m->eptr; *ecol = m->ecol; *eval = m->eval;
+  return m->eptr[m->nexp];
+}
 const int32_t *or_fs_xstart(const or_fs *m) { return m->xstart; }
 const int32_t *or_fs_elem_degree(const or_fs *m) { return m->edeg; }
 const double *or_fs_coords_expanded(const or_fs *m) { return m->xexp; }
@@ -860,10 +1037,16 @@ void or_fs_entity_info(const or_fs *m, int32_t *ordered, int32_t *goffset, int32
 void or_fs_global_to_expanded(const or_fs *m, const double *g, const double *dcache, double *x)
 {
   const int bs = m->bs;
-  for (int64_t r = 0; r < m->nexp; r++) {
-    const int64_t c = m->emap[r];
-    for (int b = 0; b < bs; b++) x[r * bs + b] = c < m->n ? g[c * bs + b] : (dcache ? dcache[(c - m->n) * bs + b] : 0.0);
-  }
+  for (int64_t r = 0; r < m->nexp; r++)
+    for (int b = 0; b < bs; b++) {
+      double v = 0;
+      for (int64_t k = m->eptr[r]; k < m->eptr[r + 1]; k++) {
+        const int64_t c = m->ecol[k];
+        const double cv = c < m->n ? g[c * bs + b] : (dcache ? dcache[(c - m->n) * bs + b] : 0.0);
+        v = (k == m->eptr[r]) ? m->eval[k] * cv : v + m->eval[k] * cv;
+      }
+      x[r * bs + b] = v;
+    }
 }
 
 /* dFSExpandedToGlobal (fs.c:592-640): closure = E^T x (MatMultTranspose sums rows in order) */
@@ -872,7 +1055,8 @@ void or_fs_expanded_to_global(const or_fs *m, const double *x, double *g, int ad
   const int bs = m->bs;
   double *cl = calloc((size_t)m->nc * bs, sizeof(double));
   for (int64_t r = 0; r < m->nexp; r++)
-    for (int b = 0; b < bs; b++) cl[(int64_t)m->emap[r] * bs + b] += x[r * bs + b];
+    for (int64_t k = m->eptr[r]; k < m->eptr[r + 1]; k++)
+      for (int b = 0; b < bs; b++) cl[(int64_t)m->ecol[k] * bs + b] += m->eval[k] * x[r * bs + b];
   for (int64_t i = 0; i < m->n * bs; i++) g[i] = add ? g[i] + cl[i] : cl[i];
   free(cl);
 }

@@ -71,7 +71,10 @@ const char *or_last_error(void);
 /* sizes: [0]=nelem [1]=n explicit nodes [2]=nc closure nodes [3]=nexp expanded nodes [4]=bs
  *        [5]=nverts [6]=nedges [7]=nfaces */
 void or_fs_sizes(const or_fs *fs, int64_t out[8]);
-const int32_t *or_fs_emap(const or_fs *fs);        /* expanded node -> closure node (one 1.0 per row of E) */
+const int32_t *or_fs_emap(const or_fs *fs);        /* expanded node -> closure node (one 1.0 per row of E); < -1 marks an interpolated row */
+/* E as CSR (rows = expanded nodes, columns ascending); returns nnz. With per-element degrees, rows of element
+ * nodes on lower-degree faces/edges interpolate that entity's polynomial (extension; the reference errors). */
+int64_t or_fs_ecsr(const or_fs *fs, const int64_t **eptr, const int32_t **ecol, const double **eval);
 const int32_t *or_fs_xstart(const or_fs *fs);      /* element offsets in expanded nodes, nelem+1 */
 const int32_t *or_fs_elem_degree(const or_fs *fs); /* per element degree (x,y,z) triples */
 const double *or_fs_coords_expanded(const or_fs *fs); /* [nelem][8][3] in tensor vertex order */

@@ -62,6 +62,9 @@ def lib():
         for name in ("or_fs_coords_expanded", "or_fs_vertex_coords"):
             getattr(L, name).restype = ctypes.POINTER(ctypes.c_double)
             getattr(L, name).argtypes = [ctypes.c_void_p]
+        L.or_fs_ecsr.restype = ctypes.c_int64
+        L.or_fs_ecsr.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.POINTER(ctypes.c_int64)),
+                                 ctypes.POINTER(ctypes.POINTER(ctypes.c_int32)), ctypes.POINTER(ctypes.POINTER(ctypes.c_double))]
         L.or_fs_entity_info.argtypes = [ctypes.c_void_p, _i32p, _i32p, _i32p, _i32p]
         L.or_fs_global_to_expanded.argtypes = [ctypes.c_void_p, _f64p, ctypes.c_void_p, _f64p]
         L.or_fs_expanded_to_global.argtypes = [ctypes.c_void_p, _f64p, _f64p, ctypes.c_int]
@@ -208,6 +211,12 @@ class FS:
 
     def emap(self):
         return np.ctypeslib.as_array(lib().or_fs_emap(self.h), shape=(self.nexp,)).copy()
+
+    def ecsr(self):
+        p = ctypes.POINTER(ctypes.c_int64)(); c = ctypes.POINTER(ctypes.c_int32)(); v = ctypes.POINTER(ctypes.c_double)()
+        nnz = lib().or_fs_ecsr(self.h, ctypes.byref(p), ctypes.byref(c), ctypes.byref(v))
+        return (np.ctypeslib.as_array(p, shape=(self.nexp + 1,)).copy(), np.ctypeslib.as_array(c, shape=(nnz,)).copy(),
+                np.ctypeslib.as_array(v, shape=(nnz,)).copy())
 
     def xstart(self):
         return np.ctypeslib.as_array(lib().or_fs_xstart(self.h), shape=(self.nelem + 1,)).copy()
