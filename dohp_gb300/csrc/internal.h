@@ -80,6 +80,9 @@ struct _p_dFS {
   // host results of the space build
   int64_t nelem = 0, n = 0, nc = 0, nexp = 0, nq = 0;
   std::vector<int32_t> xstart, emap, edeg, qoff;
+  std::vector<int32_t> eptr, ecol;  // E as CSR (rows = expanded nodes); Boolean rows have one 1.0
+  std::vector<double> eval;
+  bool boolean_e = true;            // every row of E is a single 1.0 (emap holds it)
   bool uniform = true;
   int p = 0;  // uniform degree
   // device

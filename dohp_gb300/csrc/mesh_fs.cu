@@ -6,6 +6,7 @@
 //  * min-rule degree propagation (dJacobiPropagateDown_Tensor, src/jacobi/impls/tensor/tensor.c:199-247)
 //  * partition explicit/Dirichlet and natural ordering (fsbuild.c:55-146, cont.c:93-178, cont.c:293-385)
 //  * the element assembly map E (dJacobiAddConstraints_Tensor, tensor.c:360-468)
+#include <math.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -240,9 +241,118 @@ inline int perm_quad_index(int perm, int M, int N, int i, int j) {
 
 }  // namespace
 
-// E rows of one hex (tensor.c:360-468). loff: closure offset of every entity.
+// Interpolation rows for p-nonconforming entities (extension of dJacobiAddConstraints_Tensor, which
+// errors at tensor.c:417). An edge of degree q carries the polynomial through its q+1 GLL nodes (vertex,
+// q-1 interior dofs in the edge direction, vertex); a face of degree q the tensor polynomial through its
+// (q+1)^2 GLL grid in its own frame (u along fv0->fv1, v along fv0->fv3): corners are the vertices, the
+// boundary the edge polynomials, the interior its dofs. An element node on a lower-degree edge or face
+// takes that polynomial's value at the node; rows keep their columns ascending, weights |w| < 1e-14 (exact
+// zeros of the Lagrange weights at coinciding nodes) are dropped.
+struct HpRows {
+  double gll[MAXP + 1][MAXP + 1];
+  std::vector<int64_t> row;                 // expanded row of each constrained row
+  std::vector<int64_t> ptr{0};              // entries of constrained row k: ptr[k]..ptr[k+1]
+  std::vector<int32_t> col;
+  std::vector<double> w;
+};
+
+struct Acc {
+  int n = 0;
+  int32_t c[2048];
+  double w[2048];
+  void add(int32_t col, double v) {
+    for (int i = 0; i < n; i++)
+      if (c[i] == col) {
+        w[i] += v;
+        return;
+      }
+    c[n] = col;
+    w[n] = v;
+    n++;
+  }
+};
+
+static void gll_weights(const HpRows &h, int q, double t, double *L) {
+  for (int j = 0; j <= q; j++) {
+    long double v = 1;
+    for (int k = 0; k <= q; k++)
+      if (k != j) v *= ((long double)t - h.gll[q][k]) / ((long double)h.gll[q][j] - h.gll[q][k]);
+    L[j] = (double)v;
+  }
+}
+
+static void edge_value(const _p_dMesh *m, const std::vector<Ord> &deg, const std::vector<int32_t> &loff, const HpRows &h,
+                       int32_t edge, double t, double scale, Acc &a) {
+  const int q = deg[edge].x;
+  const int64_t *ev = &m->econn[2 * (edge - m->nv)];
+  double L[MAXP + 1];
+  gll_weights(h, q, t, L);
+  for (int k = 0; k <= q; k++) a.add(k == 0 ? loff[ev[0]] : k == q ? loff[ev[1]] : loff[edge] + (k - 1), scale * L[k]);
+}
+
+static void face_value(const _p_dMesh *m, const std::vector<Ord> &deg, const std::vector<int32_t> &loff, const HpRows &h,
+                       int32_t face, double u, double v, Acc &a) {
+  const int qu = deg[face].x, qv = deg[face].y;
+  const int64_t *fv = &m->fconn[4 * (face - m->nv - m->ne)];
+  double Lu[MAXP + 1], Lv[MAXP + 1];
+  gll_weights(h, qu, u, Lu);
+  gll_weights(h, qv, v, Lv);
+  for (int r = 0; r <= qu; r++)
+    for (int c = 0; c <= qv; c++) {
+      const double w = Lu[r] * Lv[c];
+      const bool bu = r == 0 || r == qu, bv = c == 0 || c == qv;
+      if (bu && bv) {
+        a.add(loff[fv[r == 0 ? (c == 0 ? 0 : 3) : (c == 0 ? 1 : 2)]], w);
+      } else if (!bu && !bv) {
+        a.add(loff[face] + (r - 1) * (qv - 1) + (c - 1), w);
+      } else {
+        int side;
+        double tau;
+        if (c == 0) side = 0, tau = h.gll[qu][r];
+        else if (r == qu) side = 1, tau = h.gll[qv][c];
+        else if (c == qv) side = 2, tau = -h.gll[qu][r];
+        else side = 3, tau = -h.gll[qv][c];
+        const int32_t slot = m->adjoff[face] + side;
+        edge_value(m, deg, loff, h, m->adjind[slot], m->adjperm[slot] == 0 ? tau : -tau, w, a);
+      }
+    }
+}
+
+static void push_hp_row(HpRows &h, int64_t row, Acc &a) {
+  // ascending columns
+  for (int i = 1; i < a.n; i++)
+    for (int j = i; j > 0 && a.c[j - 1] > a.c[j]; j--) {
+      std::swap(a.c[j - 1], a.c[j]);
+      std::swap(a.w[j - 1], a.w[j]);
+    }
+  h.row.push_back(row);
+  for (int i = 0; i < a.n; i++)
+    if (fabs(a.w[i]) >= 1e-14) {
+      h.col.push_back(a.c[i]);
+      h.w.push_back(a.w[i]);
+    }
+  h.ptr.push_back((int64_t)h.col.size());
+}
+
+// element-face traversal coordinates (s,t) to the face frame (u,v) for the 8 orientations of
+// dGeomPermQuadIndex (tensor.c:328-345)
+static void face_frame(int perm, double s, double t, double &u, double &v) {
+  switch (perm) {
+    case 0: u = s, v = t; break;
+    case 1: u = t, v = -s; break;
+    case 2: u = -s, v = -t; break;
+    case 3: u = -t, v = s; break;
+    case 4: u = t, v = s; break;
+    case 5: u = -s, v = t; break;
+    case 6: u = -t, v = -s; break;
+    default: u = s, v = -t; break;
+  }
+}
+
+// E rows of one hex (tensor.c:360-468). loff: closure offset of every entity. hp: interpolation rows for
+// lower-degree edges/faces (NULL: error as the reference).
 static dErr fill_element_map(const _p_dMesh *m, const std::vector<Ord> &deg, const std::vector<int32_t> &loff,
-                             int64_t r, int32_t xs, int32_t *row) {
+                             int64_t r, int32_t xs, int32_t *row, HpRows *hp) {
   // which face/edge-of-face pairs meet at each hex edge, with edge orientation (tensor.c:380-383)
   static const int FE[12][2][3] = {{{0, 0, 0}, {4, 3, 1}}, {{1, 0, 0}, {4, 2, 1}}, {{2, 0, 0}, {4, 1, 1}}, {{3, 0, 0}, {4, 0, 1}},
                                    {{0, 2, 1}, {5, 0, 0}}, {{1, 2, 1}, {5, 1, 0}}, {{2, 2, 1}, {5, 2, 0}}, {{3, 2, 1}, {5, 3, 0}},
@@ -286,7 +396,18 @@ static dErr fill_element_map(const _p_dMesh *m, const std::vector<Ord> &deg, con
                          {d0 - 1, 0, 1, 2, 1, d2 - 1},      {d0 - 1, d1 - 1, 1, 2, 1, d2 - 1},    {0, d1 - 1, 1, 2, 1, d2 - 1}};
   for (int i = 0; i < 12; i++) {
     const int *s = ES[i], dir = s[3], inc = s[4], end = s[5];
-    if (deg[e[i]].x != d[dir] - 1) return set_error("degree does not agree, p-nonconforming (region %lld edge %d)", (long long)r, i);
+    if (deg[e[i]].x != d[dir] - 1) {
+      if (!hp) return set_error("degree does not agree, p-nonconforming (region %lld edge %d)", (long long)r, i);
+      for (int j = s[dir]; j != end; j += inc) {
+        const int64_t rw = xs + (s[0] * d1 + s[1]) * d2 + s[2] + (j - s[dir]) * scan[dir];
+        const double tau = inc * hp->gll[d[dir] - 1][j];
+        Acc a;
+        edge_value(m, deg, loff, *hp, e[i], eP[i] == 0 ? tau : -tau, 1.0, a);
+        row[rw] = -2;
+        push_hp_row(*hp, rw, a);
+      }
+      continue;
+    }
     for (int j = s[dir]; j != end; j += inc) {
       const int t = (j - s[dir]) / inc, ne = d[dir] - 2;
       const int32_t col = eP[i] == 0 ? loff[e[i]] + t : loff[e[i]] + (ne - 1 - t);
@@ -300,6 +421,20 @@ static dErr fill_element_map(const _p_dMesh *m, const std::vector<Ord> &deg, con
   for (int i = 0; i < 6; i++) {
     const int *s = FS[i], da = s[3], db = s[4], ia = s[5], ib = s[6];
     const int M = d[da] - 2, N = d[db] - 2;
+    if (deg[f[i]].x != d[da] - 1 || deg[f[i]].y != d[db] - 1) {
+      if (!hp) return set_error("degree does not agree, p-nonconforming (region %lld face %d)", (long long)r, i);
+      for (int j = s[da]; j != s[7]; j += ia)
+        for (int k = s[db]; k != s[8]; k += ib) {
+          const int64_t rw = xs + (s[0] * d1 + s[1]) * d2 + s[2] + (j - s[da]) * scan[da] + (k - s[db]) * scan[db];
+          double u, v;
+          face_frame(fP[i], ia * hp->gll[d[da] - 1][j], ib * hp->gll[d[db] - 1][k], u, v);
+          Acc a;
+          face_value(m, deg, loff, *hp, f[i], u, v, a);
+          row[rw] = -2;
+          push_hp_row(*hp, rw, a);
+        }
+      continue;
+    }
     for (int j = s[da]; j != s[7]; j += ia)
       for (int k = s[db]; k != s[8]; k += ib) {
         const int fi = perm_quad_index(fP[i], M, N, (j - s[da]) / ia, (k - s[db]) / ib);
@@ -389,9 +524,38 @@ dErr fs_build_space(_p_dFS *fs) {
   fs->nexp = fs->xstart[m->nr];
   fs->nq = fs->qoff[m->nr];
   fs->emap.assign(fs->nexp, -1);
-  for (int64_t r = 0; r < m->nr; r++) DCHK(fill_element_map(m, deg, loff, r, fs->xstart[r], fs->emap.data()));
+  HpRows hp;
+  for (int q = 1; q <= MAXP; q++) {
+    double w[MAXP + 1];
+    lobatto_rule(q + 1, hp.gll[q], w);
+  }
+  for (int64_t r = 0; r < m->nr; r++) DCHK(fill_element_map(m, deg, loff, r, fs->xstart[r], fs->emap.data(), per_elem ? &hp : nullptr));
   for (int64_t i = 0; i < fs->nexp; i++)
-    if (fs->emap[i] < 0) return set_error("expanded node %lld has no constraint", (long long)i);
+    if (fs->emap[i] == -1) return set_error("expanded node %lld has no constraint", (long long)i);
+  // E as CSR over expanded rows
+  fs->boolean_e = hp.row.empty();
+  fs->eptr.assign(fs->nexp + 1, 0);
+  {
+    std::vector<int64_t> which(fs->nexp, -1);
+    for (size_t k = 0; k < hp.row.size(); k++) which[hp.row[k]] = (int64_t)k;
+    int64_t nnz = 0;
+    for (int64_t i = 0; i < fs->nexp; i++) nnz += which[i] < 0 ? 1 : hp.ptr[which[i] + 1] - hp.ptr[which[i]];
+    if (nnz > INT32_MAX) return set_error("E has too many entries");
+    fs->ecol.resize(nnz);
+    fs->eval.resize(nnz);
+    int64_t o = 0;
+    for (int64_t i = 0; i < fs->nexp; i++) {
+      fs->eptr[i] = (int32_t)o;
+      if (which[i] < 0) {
+        fs->ecol[o] = fs->emap[i];
+        fs->eval[o] = 1.0;
+        o++;
+      } else {
+        for (int64_t t = hp.ptr[which[i]]; t < hp.ptr[which[i] + 1]; t++, o++) fs->ecol[o] = hp.col[t], fs->eval[o] = hp.w[t];
+      }
+    }
+    fs->eptr[fs->nexp] = (int32_t)o;
+  }
   return 0;
 }
 
@@ -430,3 +594,12 @@ dErr dMeshGetNumEnts(dMesh m, dInt counts[4]) {
 }
 
 }  // extern "C"
+
+extern "C" dErr dFSGetElementAssemblyMatrix(dFS fs, int64_t *nnz, dInt *rowptr, dInt *col, dReal *val) {
+  if (!fs || !fs->built) return set_error("dFS space not built");
+  if (nnz) *nnz = (int64_t)fs->ecol.size();
+  if (rowptr) memcpy(rowptr, fs->eptr.data(), fs->eptr.size() * sizeof(dInt));
+  if (col) memcpy(col, fs->ecol.data(), fs->ecol.size() * sizeof(dInt));
+  if (val) memcpy(val, fs->eval.data(), fs->eval.size() * sizeof(double));
+  return 0;
+}

@@ -111,6 +111,11 @@ dErr dFSSetUp(dFS fs);
 dErr dFSGetSizes(dFS fs, dInt *n, dInt *nc, dInt *nexp, dInt *bs, dInt *nelem);
 /* host copies of the bit-exact maps: E (expanded node -> closure node) and element offsets */
 dErr dFSGetExpandedMap(dFS fs, dInt *emap, dInt *xstart);
+/* host copy of E as CSR (rows = expanded nodes, columns = closure nodes ascending, values); any output may
+ * be NULL. With uniform degree every row is one 1.0 (the reference's Boolean E, cont.c:200-249). With
+ * per-element degrees (dFSSetDegree elem_degree), element nodes on lower-degree faces/edges interpolate
+ * that entity's polynomial (an extension: the reference errors on p-nonconforming entities, tensor.c:417). */
+dErr dFSGetElementAssemblyMatrix(dFS fs, int64_t *nnz, dInt *rowptr, dInt *col, dReal *val);
 /* host copy of per-element degrees (3 per element after propagation) */
 dErr dFSGetElementDegrees(dFS fs, dInt *deg);
 /* dFSGetGeometryVectorExpanded (src/fs/interface/fsgeom.c:216-227): device [nelem][8][3] */

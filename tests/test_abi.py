@@ -74,11 +74,40 @@ def test_bu0_numbering_from_product(L):
     np.testing.assert_array_equal(x, g["homogeneous"])
 
 
-def test_nonconforming_orders_rejected_like_the_reference(L):
-    """dJacobiAddConstraints_Tensor errors on p-nonconforming edges (tensor.c:417)."""
-    ed = np.array([2, 3, 2, 3, 2, 3, 2, 3], np.int32)
-    with pytest.raises(dg.DohpError, match="nonconforming"):
-        host_fs((3, 3, 3), 3, elem_degree=ed)
+def host_ecsr(npoints, degree, elem_degree, dirichlet=(100, 200, 300)):
+    L = dg.lib()
+    mesh = ctypes.c_void_p()
+    dg.chk(L.dMeshCreateBlock(dg.ptr(np.asarray(npoints, np.int32)), dg.ptr(np.asarray((0, 1, 0, 1, 0, 1), np.float64)),
+                              ctypes.c_double(0.1), ctypes.c_uint64(1), ctypes.byref(mesh)))
+    fs = ctypes.c_void_p()
+    dg.chk(L.dFSCreate(mesh, None, ctypes.byref(fs)))
+    dg.chk(L.dFSSetDegree(fs, ctypes.c_int32(degree), dg.ptr(np.ascontiguousarray(elem_degree, np.int32))))
+    for s in dirichlet:
+        dg.chk(L.dFSRegisterBoundary(fs, ctypes.c_int32(s), ctypes.c_int(1)))
+    dg.chk(L.dFSBuildSpace(fs))
+    sz = [ctypes.c_int32() for _ in range(5)]
+    dg.chk(L.dFSGetSizes(fs, *[ctypes.byref(s) for s in sz]))
+    nnz = ctypes.c_int64()
+    dg.chk(L.dFSGetElementAssemblyMatrix(fs, ctypes.byref(nnz), None, None, None))
+    p = np.zeros(sz[2].value + 1, np.int32); c = np.zeros(nnz.value, np.int32); v = np.zeros(nnz.value)
+    dg.chk(L.dFSGetElementAssemblyMatrix(fs, None, dg.ptr(p), dg.ptr(c), dg.ptr(v)))
+    L.dFSDestroy(ctypes.byref(fs)); L.dMeshDestroy(ctypes.byref(mesh))
+    return sz[0].value, sz[1].value, p, c, v
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_hp_element_assembly_matrix_matches_oracle(L, seed):
+    """per-element orders 2..8 (config-2 style): interpolation-constrained E, sparsity bit-exact with the
+    oracle's extension, weights within 1e-14."""
+    npoints = (4, 4, 3)
+    ed = np.random.default_rng(seed).integers(2, 9, size=3 * 3 * 2).astype(np.int32)
+    n, nc, p, c, v = host_ecsr(npoints, 4, ed)
+    o = po.FS(*npoints, degree=4, perturb=0.1, seed=1, elem_degree=ed)
+    op_, oc, ov = o.ecsr()
+    assert (n, nc) == (o.n, o.nc)
+    np.testing.assert_array_equal(p, op_)
+    np.testing.assert_array_equal(c, oc)
+    np.testing.assert_allclose(v, ov, rtol=0, atol=1e-14)
 
 
 def test_grf_parameters_match_oracle(L):
