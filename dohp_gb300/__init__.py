@@ -249,4 +249,26 @@ def _op_mult_expanded(self, x, yexp):
     chk(lib().dOperatorMultExpanded(self.h, ptr(x), ptr(yexp)))
 
 
+dLAUNCH_DEFAULT, dLAUNCH_PER_ORDER, dLAUNCH_PERSISTENT, dLAUNCH_GRAPH = 0, 1, 2, 3
+
+
+def _op_set_launch(self, mode):
+    chk(lib().dOperatorSetLaunchMode(self.h, ctypes.c_int(mode)))
+
+
+def _op_autotune(self, cache_path=None):
+    chk(lib().dOperatorAutotune(self.h, None if cache_path is None else ctypes.c_char_p(cache_path.encode())))
+
+
+def _op_tiles(self):
+    nb = _i32()
+    chk(lib().dOperatorGetTiles(self.h, ctypes.byref(nb), None, None, None))
+    o = np.zeros(max(nb.value, 1), np.int32); c = np.zeros_like(o); t = np.zeros_like(o)
+    chk(lib().dOperatorGetTiles(self.h, ctypes.byref(nb), ptr(o), ptr(c), ptr(t)))
+    return [(int(o[i]), int(c[i]), int(t[i])) for i in range(nb.value)]
+
+
 Operator.mult_expanded = _op_mult_expanded
+Operator.set_launch = _op_set_launch
+Operator.autotune = _op_autotune
+Operator.tiles = _op_tiles

@@ -14,6 +14,7 @@ dErr op_compute_geometry(_p_dOperator *op);
 dErr q1_symbolic(_p_dFS *fs, _p_dMat *J);
 dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk);
 dErr mat_mult(_p_dMat *J, const double *x, double *y, cudaStream_t s);
+void hp_plan_destroy(void *p);
 
 namespace {
 
@@ -267,6 +268,7 @@ dErr dOperatorDestroy(dOperator *op) {
   cudaFree(o->d_y32);
   cudaFree(o->d_hx);
   cudaFree(o->d_hy);
+  hp_plan_destroy(o->hp_plan);
   delete o;
   *op = nullptr;
   return 0;

@@ -42,11 +42,45 @@ __global__ void k_restrict(int64_t n, int bs, const int32_t *__restrict__ et_ptr
   g[t] = add ? g[t] + s : s;
 }
 
+// weighted forms for hp spaces (E with interpolation rows)
+__global__ void k_expand_w(int64_t nexp, int bs, const int32_t *__restrict__ eptr, const int32_t *__restrict__ ecol,
+                           const double *__restrict__ eval, int64_t n, const double *__restrict__ g,
+                           const double *__restrict__ dcache, double *__restrict__ x, int add) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nexp * bs) return;
+  const int64_t r = t / bs;
+  const int b = (int)(t - r * bs);
+  double v = 0;
+  for (int32_t k = eptr[r]; k < eptr[r + 1]; k++) {
+    const int64_t c = ecol[k];
+    const double cv = c < n ? g[c * bs + b] : (dcache ? dcache[(c - n) * bs + b] : 0.0);
+    v += eval[k] * cv;
+  }
+  x[t] = add ? x[t] + v : v;
+}
+
+template <typename TI>
+__global__ void k_restrict_w(int64_t n, int bs, const int32_t *__restrict__ et_ptr, const int32_t *__restrict__ et_idx,
+                             const double *__restrict__ et_w, const TI *__restrict__ x, double *__restrict__ g, int add) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= n * bs) return;
+  const int64_t c = t / bs;
+  const int b = (int)(t - c * bs);
+  double s = 0;
+  for (int32_t k = et_ptr[c]; k < et_ptr[c + 1]; k++) s += et_w[k] * (double)x[(int64_t)et_idx[k] * bs + b];
+  g[t] = add ? g[t] + s : s;
+}
+
 }  // namespace
 
 dErr fs_restrict(_p_dFS *fs, const double *x, double *g, int add) {
   const int64_t N = fs->n * fs->bs;
   if (N == 0) return 0;
+  if (!fs->boolean_e) {
+    k_restrict_w<double><<<(unsigned)((N + 255) / 256), 256, 0, fs->stream>>>(fs->n, fs->bs, fs->d_et_ptr, fs->d_et_idx, fs->d_et_w, x, g, add);
+    CUCHK(cudaGetLastError());
+    return 0;
+  }
   k_restrict<double><<<(unsigned)((N + 255) / 256), 256, 0, fs->stream>>>(fs->n, fs->bs, fs->d_et_ptr, fs->d_et_idx, x, g, add);
   CUCHK(cudaGetLastError());
   return 0;
@@ -55,6 +89,11 @@ dErr fs_restrict(_p_dFS *fs, const double *x, double *g, int add) {
 dErr fs_restrict32(_p_dFS *fs, const float *x, double *g, int add) {
   const int64_t N = fs->n * fs->bs;
   if (N == 0) return 0;
+  if (!fs->boolean_e) {
+    k_restrict_w<float><<<(unsigned)((N + 255) / 256), 256, 0, fs->stream>>>(fs->n, fs->bs, fs->d_et_ptr, fs->d_et_idx, fs->d_et_w, x, g, add);
+    CUCHK(cudaGetLastError());
+    return 0;
+  }
   k_restrict<float><<<(unsigned)((N + 255) / 256), 256, 0, fs->stream>>>(fs->n, fs->bs, fs->d_et_ptr, fs->d_et_idx, x, g, add);
   CUCHK(cudaGetLastError());
   return 0;
@@ -62,6 +101,12 @@ dErr fs_restrict32(_p_dFS *fs, const float *x, double *g, int add) {
 
 dErr fs_expand(_p_dFS *fs, const double *g, double *x, bool inhomogeneous, int add) {
   const int64_t N = fs->nexp * fs->bs;
+  if (!fs->boolean_e) {
+    k_expand_w<<<(unsigned)((N + 255) / 256), 256, 0, fs->stream>>>(fs->nexp, fs->bs, fs->d_eptr, fs->d_ecol, fs->d_eval, fs->n, g,
+                                                                    inhomogeneous ? fs->d_dcache : nullptr, x, add);
+    CUCHK(cudaGetLastError());
+    return 0;
+  }
   k_expand<<<(unsigned)((N + 255) / 256), 256, 0, fs->stream>>>(fs->nexp, fs->bs, fs->d_emap, fs->n, g,
                                                                 inhomogeneous ? fs->d_dcache : nullptr, x, add);
   CUCHK(cudaGetLastError());
@@ -79,6 +124,12 @@ static void fs_free_device(_p_dFS *fs) {
   cudaFree(fs->d_dcache);
   cudaFree(fs->d_fast_tab);
   cudaFree(fs->d_scratch_exp);
+  cudaFree(fs->d_eptr);
+  cudaFree(fs->d_ecol);
+  cudaFree(fs->d_eval);
+  cudaFree(fs->d_et_w);
+  fs->d_eptr = fs->d_ecol = nullptr;
+  fs->d_eval = fs->d_et_w = nullptr;
   fs->d_emap = fs->d_xstart = fs->d_edeg = fs->d_qoff = fs->d_et_ptr = fs->d_et_idx = nullptr;
   fs->d_coords = fs->d_dcache = fs->d_fast_tab = fs->d_scratch_exp = nullptr;
 }
@@ -153,13 +204,27 @@ dErr dFSSetUp(dFS fs) {
   if (fs->setup) return 0;
   DCHK(dFSBuildSpace(fs));
   const _p_dMesh *m = fs->mesh;
-  // E^T over closure nodes, ascending expanded index (counting sort over the row-ordered E)
-  std::vector<int32_t> ptr(fs->nc + 1, 0), idx(fs->nexp);
-  for (int64_t r = 0; r < fs->nexp; r++) ptr[fs->emap[r] + 1]++;
+  // E^T over closure nodes, ascending expanded index (counting sort over the row-ordered E): each closure
+  // node sums its contributions in MatMultTranspose order
+  const int64_t enz = (int64_t)fs->ecol.size();
+  std::vector<int32_t> ptr(fs->nc + 1, 0), idx(enz);
+  std::vector<double> wts(enz);
+  for (int64_t k = 0; k < enz; k++) ptr[fs->ecol[k] + 1]++;
   for (int64_t c = 0; c < fs->nc; c++) ptr[c + 1] += ptr[c];
   {
     std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
-    for (int64_t r = 0; r < fs->nexp; r++) idx[fill[fs->emap[r]]++] = (int32_t)r;
+    for (int64_t r = 0; r < fs->nexp; r++)
+      for (int32_t k = fs->eptr[r]; k < fs->eptr[r + 1]; k++) {
+        const int32_t pos = fill[fs->ecol[k]]++;
+        idx[pos] = (int32_t)r;
+        wts[pos] = fs->eval[k];
+      }
+  }
+  if (!fs->boolean_e) {
+    DCHK(upload(&fs->d_eptr, fs->eptr.data(), fs->eptr.size()));
+    DCHK(upload(&fs->d_ecol, fs->ecol.data(), fs->ecol.size()));
+    DCHK(upload(&fs->d_eval, fs->eval.data(), fs->eval.size()));
+    DCHK(upload(&fs->d_et_w, wts.data(), wts.size()));
   }
   // expanded coordinates in tensor vertex order (dFSCreateGeometryFromMesh_Private, fsgeom.c:146-156)
   static const int kConn[8] = {0, 4, 3, 7, 1, 5, 2, 6};

@@ -1,0 +1,688 @@
+// hp (mixed-order) operator apply.
+//
+// Elements are bucketed by order (p = 1..8, isotropic). Each element gathers its nodal values through the
+// interpolation-constrained E (CSR rows of weights; Boolean rows for conforming nodes), runs the same
+// sum-factorized element kernel as the uniform path for its order (interpolate to Gauss points, collocation
+// gradient, q-function, transposes; see operator.cu), and writes its expanded output; the weighted E^T
+// restriction sums contributions per closure node in ascending expanded order (deterministic).
+// Launch forms:
+//   dLAUNCH_PER_ORDER : one launch per order bucket (plain)
+//   dLAUNCH_PERSISTENT: one launch over all buckets; blocks take (bucket, element group) work items from a
+//                       device counter in descending order cost; each item is processed by exactly one block,
+//                       so results are bitwise identical to the per-order form
+//   dLAUNCH_GRAPH     : the persistent launch and the restriction replayed from a CUDA graph; x and y are
+//                       passed through a small device pointer table so one graph serves every call
+// Tile sizes (elements per block, threads per block) come from a measured autotuner per (kind, order,
+// precision), optionally persisted as JSON.
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <fstream>
+#include <sstream>
+
+#include "internal.h"
+
+using namespace dgb;
+
+dErr op_compute_geometry(_p_dOperator *op);
+dErr fs_restrict(_p_dFS *fs, const double *x, double *g, int add);
+dErr fs_restrict32(_p_dFS *fs, const float *x, double *g, int add);
+
+namespace {
+
+struct HpArgs {
+  const int32_t *xstart, *qoff, *eptr, *ecol;
+  const double *eval;
+  int64_t n;
+  const double *x;
+  const double *const *px;  // graph form: x read through this table when non-null
+  const void *geo;
+  const double *tab_all;
+  void *yexp;
+  double lam, mu;
+};
+
+template <int N, typename T>
+__device__ __forceinline__ void load_tables(const double *tab_all, T *sB, T *sD) {
+  const double *tab = tab_all + (size_t)2 * (N - 2) * MAXP * MAXP;
+  for (int i = threadIdx.x; i < N * N; i += blockDim.x) {
+    sB[i] = (T)tab[i];
+    sD[i] = (T)tab[MAXP * MAXP + i];
+  }
+}
+
+// gather one component of the element's nodes through E (homogeneous Dirichlet: closure beyond n is 0)
+template <int N, typename T, int BS>
+__device__ __forceinline__ void gather(const HpArgs &A, const double *x, const int32_t *els, int ne, int d, T *dst) {
+  constexpr int N3 = N * N * N;
+  for (int t = threadIdx.x; t < ne * N3; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3;
+    const int64_t row = A.xstart[els[el]] + r;
+    double v = 0;
+    for (int32_t k = A.eptr[row]; k < A.eptr[row + 1]; k++) {
+      const int32_t c = A.ecol[k];
+      if (c < A.n) v += A.eval[k] * x[(int64_t)c * BS + d];
+    }
+    dst[t] = (T)v;
+  }
+}
+
+// three interpolation passes: in (S0) -> out (S1), using S0 as scratch
+template <int N, typename T>
+__device__ __forceinline__ void interp3(const T *sB, T *S0, T *S1, int tot, int cap) {
+  constexpr int N3 = N * N * N, NN = N * N;
+  (void)cap;
+  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3, a = r / NN, jk = r - a * NN;
+    const T *in = &S0[el * N3 + jk];
+    T s = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++) s += sB[a * N + i] * in[i * NN];
+    S1[t] = s;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3, a = r / NN, b = (r / N) % N, k = r % N;
+    const T *in = &S1[el * N3 + a * NN + k];
+    T s = 0;
+#pragma unroll
+    for (int j = 0; j < N; j++) s += sB[b * N + j] * in[j * N];
+    S0[t] = s;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3, ab = r / N, c = r % N;
+    const T *in = &S0[el * N3 + ab * N];
+    T s = 0;
+#pragma unroll
+    for (int k = 0; k < N; k++) s += sB[c * N + k] * in[k];
+    S1[t] = s;
+  }
+  __syncthreads();
+}
+
+// transposed gradient (V0,V1,V2 -> S1) then three transposed interpolation passes to out (via S0)
+template <int N, typename T, int BS>
+__device__ __forceinline__ void back(const T *sB, const T *sD, const T *V0, const T *V1, const T *V2, T *S0, T *S1, int tot,
+                                     const HpArgs &A, const int32_t *els, int d, T *yexp) {
+  constexpr int N3 = N * N * N, NN = N * N;
+  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3, a = r / NN, b = (r / N) % N, c = r % N;
+    const T *v0 = &V0[el * N3], *v1 = &V1[el * N3], *v2 = &V2[el * N3];
+    T s = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++) s += sD[i * N + a] * v0[i * NN + b * N + c] + sD[i * N + b] * v1[a * NN + i * N + c] + sD[i * N + c] * v2[a * NN + b * N + i];
+    S1[t] = s;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3, ab = r / N, k = r % N;
+    const T *in = &S1[el * N3 + ab * N];
+    T s = 0;
+#pragma unroll
+    for (int c = 0; c < N; c++) s += sB[c * N + k] * in[c];
+    S0[t] = s;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3, a = r / NN, j = (r / N) % N, k = r % N;
+    const T *in = &S0[el * N3 + a * NN + k];
+    T s = 0;
+#pragma unroll
+    for (int b = 0; b < N; b++) s += sB[b * N + j] * in[b * N];
+    S1[t] = s;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3, i = r / NN, jk = r - i * NN;
+    const T *in = &S1[el * N3 + jk];
+    T s = 0;
+#pragma unroll
+    for (int a = 0; a < N; a++) s += sB[a * N + i] * in[a * NN];
+    yexp[((int64_t)A.xstart[els[el]] + r) * BS + d] = s;
+  }
+  __syncthreads();
+}
+
+// gradient at Gauss points of U (in S1) -> G0, G1, G2
+template <int N, typename T>
+__device__ __forceinline__ void grad(const T *sD, const T *S1, T *G0, T *G1, T *G2, int tot) {
+  constexpr int N3 = N * N * N, NN = N * N;
+  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3, a = r / NN, b = (r / N) % N, c = r % N;
+    const T *U = &S1[el * N3];
+    T g0 = 0, g1 = 0, g2 = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+      g0 += sD[a * N + i] * U[i * NN + b * N + c];
+      g1 += sD[b * N + i] * U[a * NN + i * N + c];
+      g2 += sD[c * N + i] * U[a * NN + b * N + i];
+    }
+    G0[t] = g0;
+    G1[t] = g1;
+    G2[t] = g2;
+  }
+  __syncthreads();
+}
+
+// shared memory (in T) of one group: two basis tables + buffers
+__host__ __device__ constexpr int group_smem_elems(int N, int kind, int cap) {
+  return 2 * MAXP * MAXP + (kind == dOP_ELASTICITY ? 11 : 5) * cap * N * N * N;
+}
+
+template <int N, typename T, int KIND>
+__device__ void group_apply(const HpArgs &A, const int32_t *els, int ne, int cap, T *sm) {
+  constexpr int N3 = N * N * N;
+  T *sB = sm, *sD = sm + MAXP * MAXP, *buf = sm + 2 * MAXP * MAXP;
+  const int L = cap * N3, tot = ne * N3;
+  const double *x = A.px ? *A.px : A.x;
+  T *yexp = (T *)A.yexp;
+  load_tables<N, T>(A.tab_all, sB, sD);
+  if (KIND == dOP_DIFFUSION) {
+    T *S0 = buf, *S1 = buf + L, *G0 = buf + 2 * L, *G1 = buf + 3 * L, *G2 = buf + 4 * L;
+    gather<N, T, 1>(A, x, els, ne, 0, S0);
+    __syncthreads();
+    interp3<N, T>(sB, S0, S1, tot, cap);
+    grad<N, T>(sD, S1, G0, G1, G2, tot);
+    const T *geo = (const T *)A.geo;
+    for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+      const int el = t / N3, r = t - el * N3;
+      const T *G = geo + (int64_t)A.qoff[els[el]] * 6 + r;
+      const T g0 = G0[t], g1 = G1[t], g2 = G2[t];
+      const T a0 = G[0], a1 = G[N3], a2 = G[2 * N3], a3 = G[3 * N3], a4 = G[4 * N3], a5 = G[5 * N3];
+      G0[t] = a0 * g0 + a1 * g1 + a2 * g2;
+      G1[t] = a1 * g0 + a3 * g1 + a4 * g2;
+      G2[t] = a2 * g0 + a4 * g1 + a5 * g2;
+    }
+    __syncthreads();
+    back<N, T, 1>(sB, sD, G0, G1, G2, S0, S1, tot, A, els, 0, yexp);
+  } else {
+    T *S0 = buf, *S1 = buf + L, *G = buf + 2 * L;  // G: [d][k][L]
+    for (int d = 0; d < 3; d++) {
+      gather<N, T, 3>(A, x, els, ne, d, S0);
+      __syncthreads();
+      interp3<N, T>(sB, S0, S1, tot, cap);
+      grad<N, T>(sD, S1, G + (d * 3 + 0) * L, G + (d * 3 + 1) * L, G + (d * 3 + 2) * L, tot);
+    }
+    const T *geo = (const T *)A.geo;
+    const T lam = (T)A.lam, mu = (T)A.mu;
+    for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+      const int el = t / N3, r = t - el * N3;
+      const T *gq = geo + (int64_t)A.qoff[els[el]] * 10 + r;
+      T Ji[9];
+#pragma unroll
+      for (int i = 0; i < 9; i++) Ji[i] = gq[i * N3];
+      const T w = gq[9 * N3];
+      T Du[9];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        const T a0 = G[(d * 3 + 0) * L + t], a1 = G[(d * 3 + 1) * L + t], a2 = G[(d * 3 + 2) * L + t];
+#pragma unroll
+        for (int e = 0; e < 3; e++) Du[d * 3 + e] = a0 * Ji[0 * 3 + e] + a1 * Ji[1 * 3 + e] + a2 * Ji[2 * 3 + e];
+      }
+      const T e01 = (T)0.5 * (Du[1] + Du[3]), e02 = (T)0.5 * (Du[2] + Du[6]), e12 = (T)0.5 * (Du[5] + Du[7]);
+      const T tr = Du[0] + Du[4] + Du[8];
+      T S[9];
+      S[0] = w * (lam * tr + 2 * mu * Du[0]);
+      S[4] = w * (lam * tr + 2 * mu * Du[4]);
+      S[8] = w * (lam * tr + 2 * mu * Du[8]);
+      S[1] = S[3] = w * (2 * mu * e01);
+      S[2] = S[6] = w * (2 * mu * e02);
+      S[5] = S[7] = w * (2 * mu * e12);
+#pragma unroll
+      for (int d = 0; d < 3; d++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) G[(d * 3 + k) * L + t] = S[d * 3 + 0] * Ji[k * 3 + 0] + S[d * 3 + 1] * Ji[k * 3 + 1] + S[d * 3 + 2] * Ji[k * 3 + 2];
+    }
+    __syncthreads();
+    for (int d = 0; d < 3; d++) back<N, T, 3>(sB, sD, G + (d * 3 + 0) * L, G + (d * 3 + 1) * L, G + (d * 3 + 2) * L, S0, S1, tot, A, els, d, yexp);
+  }
+}
+
+template <int N, typename T, int KIND>
+__global__ void __launch_bounds__(256) k_hp_bucket(HpArgs A, const int32_t *__restrict__ elist, int64_t count, int cap) {
+  extern __shared__ unsigned char raw[];
+  const int64_t g0 = (int64_t)blockIdx.x * cap;
+  const int ne = (int)min((int64_t)cap, count - g0);
+  group_apply<N, T, KIND>(A, elist + g0, ne, cap, reinterpret_cast<T *>(raw));
+}
+
+// work item: x = nodes per direction, y = first element in elist, z = elements, w = group capacity
+template <typename T, int KIND>
+__global__ void __launch_bounds__(256) k_hp_persistent(HpArgs A, const int32_t *__restrict__ elist, const int4 *__restrict__ work,
+                                                       int nwork, int *counter) {
+  extern __shared__ unsigned char raw[];
+  __shared__ int item;
+  T *sm = reinterpret_cast<T *>(raw);
+  for (;;) {
+    if (threadIdx.x == 0) item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int it = item;
+    __syncthreads();
+    if (it >= nwork) break;
+    const int4 w = work[it];
+    switch (w.x) {
+      case 2: group_apply<2, T, KIND>(A, elist + w.y, w.z, w.w, sm); break;
+      case 3: group_apply<3, T, KIND>(A, elist + w.y, w.z, w.w, sm); break;
+      case 4: group_apply<4, T, KIND>(A, elist + w.y, w.z, w.w, sm); break;
+      case 5: group_apply<5, T, KIND>(A, elist + w.y, w.z, w.w, sm); break;
+      case 6: group_apply<6, T, KIND>(A, elist + w.y, w.z, w.w, sm); break;
+      case 7: group_apply<7, T, KIND>(A, elist + w.y, w.z, w.w, sm); break;
+      case 8: group_apply<8, T, KIND>(A, elist + w.y, w.z, w.w, sm); break;
+      case 9: group_apply<9, T, KIND>(A, elist + w.y, w.z, w.w, sm); break;
+    }
+    __syncthreads();
+  }
+}
+
+// weighted E^T restriction reading the output pointer through the table (graph form)
+template <typename TI>
+__global__ void k_restrict_table(int64_t n, int bs, const int32_t *__restrict__ et_ptr, const int32_t *__restrict__ et_idx,
+                                 const double *__restrict__ et_w, const TI *__restrict__ x, double *const *py) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= n * bs) return;
+  const int64_t c = t / bs;
+  const int b = (int)(t - c * bs);
+  double s = 0;
+  for (int32_t k = et_ptr[c]; k < et_ptr[c + 1]; k++) s += (et_w ? et_w[k] : 1.0) * (double)x[(int64_t)et_idx[k] * bs + b];
+  (*py)[t] = s;
+}
+
+int default_cap(int N, int kind) {
+  if (kind == dOP_ELASTICITY) return N <= 3 ? 8 : N == 4 ? 4 : N == 5 ? 2 : 1;
+  return N <= 2 ? 32 : N == 3 ? 16 : N == 4 ? 8 : N == 5 ? 4 : N <= 7 ? 2 : 1;
+}
+
+template <int N, typename T, int KIND>
+dErr launch_bucket(const HpArgs &A, const int32_t *elist, int64_t count, int cap, int threads, cudaStream_t s) {
+  if (count == 0) return 0;
+  const size_t smem = (size_t)group_smem_elems(N, KIND, cap) * sizeof(T);
+  CUCHK(cudaFuncSetAttribute(k_hp_bucket<N, T, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_hp_bucket<N, T, KIND><<<(unsigned)((count + cap - 1) / cap), threads, smem, s>>>(A, elist, count, cap);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+template <typename T, int KIND>
+dErr launch_bucket_n(int N, const HpArgs &A, const int32_t *elist, int64_t count, int cap, int threads, cudaStream_t s) {
+  switch (N) {
+    case 2: return launch_bucket<2, T, KIND>(A, elist, count, cap, threads, s);
+    case 3: return launch_bucket<3, T, KIND>(A, elist, count, cap, threads, s);
+    case 4: return launch_bucket<4, T, KIND>(A, elist, count, cap, threads, s);
+    case 5: return launch_bucket<5, T, KIND>(A, elist, count, cap, threads, s);
+    case 6: return launch_bucket<6, T, KIND>(A, elist, count, cap, threads, s);
+    case 7: return launch_bucket<7, T, KIND>(A, elist, count, cap, threads, s);
+    case 8: return launch_bucket<8, T, KIND>(A, elist, count, cap, threads, s);
+    case 9: return launch_bucket<9, T, KIND>(A, elist, count, cap, threads, s);
+  }
+  return set_error("order %d out of range", N - 1);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------------- plan
+struct HpPlan {
+  int nb = 0;
+  int N[MAXP], cap[MAXP], threads[MAXP];
+  int64_t first[MAXP], count[MAXP];
+  int32_t *d_elist = nullptr;
+  int4 *d_work = nullptr;
+  int nwork = 0;
+  int *d_counter = nullptr;
+  size_t persistent_smem[2] = {0, 0};  // per precision (0: fp64, 1: fp32)
+  int persistent_blocks = 0;
+  bool tuned = false;
+  // graph form
+  const double **d_ptrs = nullptr;  // [x, y]
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+};
+
+static void plan_free(HpPlan *p) {
+  if (!p) return;
+  cudaFree(p->d_elist);
+  cudaFree(p->d_work);
+  cudaFree(p->d_counter);
+  cudaFree((void *)p->d_ptrs);
+  for (int i = 0; i < 2; i++)
+    if (p->exec[i]) cudaGraphExecDestroy(p->exec[i]);
+  delete p;
+}
+
+void hp_plan_destroy(void *p) { plan_free((HpPlan *)p); }
+
+static dErr plan_work(HpPlan *P, int kind, cudaStream_t s) {
+  std::vector<int4> work;
+  for (int b = 0; b < P->nb; b++)
+    for (int64_t g = 0; g < P->count[b]; g += P->cap[b])
+      work.push_back(make_int4(P->N[b], (int)(P->first[b] + g), (int)std::min<int64_t>(P->cap[b], P->count[b] - g), P->cap[b]));
+  P->nwork = (int)work.size();
+  cudaFree(P->d_work);
+  CUCHK(cudaMalloc(&P->d_work, std::max<size_t>(work.size(), 1) * sizeof(int4)));
+  CUCHK(cudaMemcpyAsync(P->d_work, work.data(), work.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+  for (int pr = 0; pr < 2; pr++) {
+    size_t mx = 0;
+    for (int b = 0; b < P->nb; b++) mx = std::max(mx, (size_t)group_smem_elems(P->N[b], kind, P->cap[b]) * (pr ? 4 : 8));
+    P->persistent_smem[pr] = mx;
+  }
+  CUCHK(cudaStreamSynchronize(s));
+  return 0;
+}
+
+static dErr plan_build(_p_dOperator *op) {
+  _p_dFS *fs = op->fs;
+  HpPlan *P = new HpPlan();
+  std::vector<std::vector<int32_t>> by(MAXP + 1);
+  for (int64_t e = 0; e < fs->nelem; e++) {
+    const int px = fs->edeg[3 * e];
+    if (fs->edeg[3 * e + 1] != px || fs->edeg[3 * e + 2] != px) {
+      delete P;
+      return set_error("hp apply needs isotropic element orders");
+    }
+    by[px + 1].push_back((int32_t)e);
+  }
+  std::vector<int32_t> elist;
+  for (int N = MAXP; N >= 2; N--)  // descending cost first (load balance of the persistent form)
+    if (!by[N].empty()) {
+      const int b = P->nb++;
+      P->N[b] = N;
+      P->first[b] = (int64_t)elist.size();
+      P->count[b] = (int64_t)by[N].size();
+      P->cap[b] = default_cap(N, op->kind);
+      P->threads[b] = 256;
+      elist.insert(elist.end(), by[N].begin(), by[N].end());
+    }
+  CUCHK(cudaMalloc(&P->d_elist, std::max<size_t>(elist.size(), 1) * sizeof(int32_t)));
+  CUCHK(cudaMemcpy(P->d_elist, elist.data(), elist.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  CUCHK(cudaMalloc(&P->d_counter, sizeof(int)));
+  CUCHK(cudaMalloc((void **)&P->d_ptrs, 2 * sizeof(double *)));
+  int dev, sms;
+  CUCHK(cudaGetDevice(&dev));
+  CUCHK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  P->persistent_blocks = sms;
+  DCHK(plan_work(P, op->kind, fs->stream));
+  op->hp_plan = P;
+  return 0;
+}
+
+static HpArgs make_args(_p_dOperator *op, const double *x, bool fp32, void *yexp, const double *const *px) {
+  _p_dFS *fs = op->fs;
+  HpArgs A;
+  A.xstart = fs->d_xstart;
+  A.qoff = fs->d_qoff;
+  A.eptr = fs->d_eptr;
+  A.ecol = fs->d_ecol;
+  A.eval = fs->d_eval;
+  A.n = fs->n;
+  A.x = x;
+  A.px = px;
+  A.geo = fp32 ? (const void *)op->d_geo32 : (const void *)op->d_geo;
+  A.tab_all = fs->d_fast_tab;
+  A.yexp = yexp;
+  A.lam = op->lam;
+  A.mu = op->mu;
+  return A;
+}
+
+template <typename T>
+static dErr run_per_order(_p_dOperator *op, const HpArgs &A) {
+  HpPlan *P = (HpPlan *)op->hp_plan;
+  for (int b = 0; b < P->nb; b++) {
+    const int32_t *el = P->d_elist + P->first[b];
+    if (op->kind == dOP_ELASTICITY) DCHK((launch_bucket_n<T, dOP_ELASTICITY>(P->N[b], A, el, P->count[b], P->cap[b], P->threads[b], op->fs->stream)));
+    else DCHK((launch_bucket_n<T, dOP_DIFFUSION>(P->N[b], A, el, P->count[b], P->cap[b], P->threads[b], op->fs->stream)));
+  }
+  return 0;
+}
+
+template <typename T>
+static dErr run_persistent(_p_dOperator *op, const HpArgs &A) {
+  HpPlan *P = (HpPlan *)op->hp_plan;
+  cudaStream_t s = op->fs->stream;
+  const size_t smem = P->persistent_smem[sizeof(T) == 4];
+  CUCHK(cudaMemsetAsync(P->d_counter, 0, sizeof(int), s));
+  if (op->kind == dOP_ELASTICITY) {
+    CUCHK(cudaFuncSetAttribute(k_hp_persistent<T, dOP_ELASTICITY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per = 1;
+    CUCHK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_hp_persistent<T, dOP_ELASTICITY>, 256, smem));
+    k_hp_persistent<T, dOP_ELASTICITY><<<P->persistent_blocks * std::max(per, 1), 256, smem, s>>>(A, P->d_elist, P->d_work, P->nwork, P->d_counter);
+  } else {
+    CUCHK(cudaFuncSetAttribute(k_hp_persistent<T, dOP_DIFFUSION>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per = 1;
+    CUCHK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_hp_persistent<T, dOP_DIFFUSION>, 256, smem));
+    k_hp_persistent<T, dOP_DIFFUSION><<<P->persistent_blocks * std::max(per, 1), 256, smem, s>>>(A, P->d_elist, P->d_work, P->nwork, P->d_counter);
+  }
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+// Measured tile choice per bucket: capacity in {c/2, c, 2c} x threads {128, 256}, 3 timed launches each.
+template <typename T>
+static dErr autotune(_p_dOperator *op, const HpArgs &A) {
+  HpPlan *P = (HpPlan *)op->hp_plan;
+  cudaStream_t s = op->fs->stream;
+  cudaEvent_t e0, e1;
+  CUCHK(cudaEventCreate(&e0));
+  CUCHK(cudaEventCreate(&e1));
+  for (int b = 0; b < P->nb; b++) {
+    const int base = default_cap(P->N[b], op->kind);
+    int best_cap = base, best_thr = 256;
+    float best = 1e30f;
+    const int caps[3] = {std::max(1, base / 2), base, base * 2};
+    for (int ci = 0; ci < 3; ci++)
+      for (int thr : {128, 256}) {
+        const int cap = caps[ci];
+        if ((size_t)group_smem_elems(P->N[b], op->kind, cap) * sizeof(T) > 160 * 1024) continue;
+        const int32_t *el = P->d_elist + P->first[b];
+        auto go = [&]() -> dErr {
+          if (op->kind == dOP_ELASTICITY) return launch_bucket_n<T, dOP_ELASTICITY>(P->N[b], A, el, P->count[b], cap, thr, s);
+          return launch_bucket_n<T, dOP_DIFFUSION>(P->N[b], A, el, P->count[b], cap, thr, s);
+        };
+        DCHK(go());
+        CUCHK(cudaEventRecord(e0, s));
+        for (int r = 0; r < 3; r++) DCHK(go());
+        CUCHK(cudaEventRecord(e1, s));
+        CUCHK(cudaEventSynchronize(e1));
+        float ms;
+        CUCHK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) best = ms, best_cap = cap, best_thr = thr;
+      }
+    P->cap[b] = best_cap;
+    P->threads[b] = best_thr;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  P->tuned = true;
+  for (int i = 0; i < 2; i++)
+    if (P->exec[i]) cudaGraphExecDestroy(P->exec[i]), P->exec[i] = nullptr;
+  return plan_work(P, op->kind, s);
+}
+
+static std::string tune_key(_p_dOperator *op, int N, bool fp32) {
+  char name[256] = "gpu";
+  int dev;
+  cudaDeviceProp prop;
+  if (cudaGetDevice(&dev) == cudaSuccess && cudaGetDeviceProperties(&prop, dev) == cudaSuccess) snprintf(name, sizeof name, "%s", prop.name);
+  for (char *c = name; *c; c++)
+    if (*c == ' ' || *c == '"') *c = '_';
+  std::ostringstream k;
+  k << name << ":kind" << (int)op->kind << ":N" << N << ":" << (fp32 ? "fp32" : "fp64");
+  return k.str();
+}
+
+// JSON cache: {"key": [cap, threads], ...}
+static void tune_load(_p_dOperator *op, const char *path, bool fp32) {
+  std::ifstream f(path);
+  if (!f) return;
+  std::stringstream ss;
+  ss << f.rdbuf();
+  const std::string js = ss.str();
+  HpPlan *P = (HpPlan *)op->hp_plan;
+  int found = 0;
+  for (int b = 0; b < P->nb; b++) {
+    const std::string key = "\"" + tune_key(op, P->N[b], fp32) + "\"";
+    const size_t at = js.find(key);
+    if (at == std::string::npos) continue;
+    int cap, thr;
+    if (sscanf(js.c_str() + at + key.size(), " : [%d , %d]", &cap, &thr) == 2 || sscanf(js.c_str() + at + key.size(), ": [%d, %d]", &cap, &thr) == 2) {
+      if (cap >= 1 && cap <= 64 && (thr == 128 || thr == 256)) P->cap[b] = cap, P->threads[b] = thr, found++;
+    }
+  }
+  if (found == P->nb) P->tuned = true;
+}
+
+static void tune_save(_p_dOperator *op, const char *path, bool fp32) {
+  HpPlan *P = (HpPlan *)op->hp_plan;
+  std::string js;
+  {
+    std::ifstream f(path);
+    if (f) {
+      std::stringstream ss;
+      ss << f.rdbuf();
+      js = ss.str();
+    }
+  }
+  std::ostringstream o;
+  o << "{\n";
+  bool firstk = true;
+  // keep other keys from the existing file
+  size_t pos = 0;
+  while ((pos = js.find('"', pos)) != std::string::npos) {
+    const size_t end = js.find('"', pos + 1);
+    if (end == std::string::npos) break;
+    const std::string key = js.substr(pos + 1, end - pos - 1);
+    const size_t lb = js.find('[', end), rb = js.find(']', end);
+    if (lb == std::string::npos || rb == std::string::npos) break;
+    bool ours = false;
+    for (int b = 0; b < P->nb; b++) ours |= key == tune_key(op, P->N[b], fp32);
+    if (!ours) {
+      o << (firstk ? "" : ",\n") << " \"" << key << "\": " << js.substr(lb, rb - lb + 1);
+      firstk = false;
+    }
+    pos = rb + 1;
+  }
+  for (int b = 0; b < P->nb; b++) {
+    o << (firstk ? "" : ",\n") << " \"" << tune_key(op, P->N[b], fp32) << "\": [" << P->cap[b] << ", " << P->threads[b] << "]";
+    firstk = false;
+  }
+  o << "\n}\n";
+  std::ofstream f(path);
+  f << o.str();
+}
+
+// y = A x for hp spaces (any E) in the operator's launch form and precision
+dErr hp_mult(_p_dOperator *op, const double *x, double *y) {
+  _p_dFS *fs = op->fs;
+  if (op->kind == dOP_PLAPLACE_JACOBIAN) return set_error("hp apply for the p-Laplacian Jacobian not built yet");
+  if (fs->boolean_e) {  // uniform-order spaces also run here when the caller asks for the hp forms
+    if (!fs->d_eptr) {
+      std::vector<int32_t> p(fs->nexp + 1);
+      for (int64_t i = 0; i <= fs->nexp; i++) p[i] = (int32_t)i;
+      std::vector<double> w(fs->nexp, 1.0);
+      CUCHK(cudaMalloc(&fs->d_eptr, p.size() * sizeof(int32_t)));
+      CUCHK(cudaMalloc(&fs->d_eval, w.size() * sizeof(double)));
+      CUCHK(cudaMalloc(&fs->d_ecol, fs->nexp * sizeof(int32_t)));
+      CUCHK(cudaMemcpy(fs->d_eptr, p.data(), p.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+      CUCHK(cudaMemcpy(fs->d_eval, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice));
+      CUCHK(cudaMemcpy(fs->d_ecol, fs->d_emap, fs->nexp * sizeof(int32_t), cudaMemcpyDeviceToDevice));
+    }
+  }
+  DCHK(op_compute_geometry(op));
+  const bool fp32 = op->prec == dPREC_FP32;
+  if (fp32 && !op->d_geo32) {
+    const int64_t ng = fs->nq * (op->kind == dOP_ELASTICITY ? 10 : 6);
+    std::vector<double> h(ng);
+    CUCHK(cudaMemcpy(h.data(), op->d_geo, ng * sizeof(double), cudaMemcpyDeviceToHost));
+    std::vector<float> f(h.begin(), h.end());
+    CUCHK(cudaMalloc(&op->d_geo32, ng * sizeof(float)));
+    CUCHK(cudaMemcpy(op->d_geo32, f.data(), ng * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  if (!op->hp_plan) {
+    DCHK(plan_build(op));
+    if (op->tune_path[0]) tune_load(op, op->tune_path, fp32);
+  }
+  HpPlan *P = (HpPlan *)op->hp_plan;
+  void *yexp;
+  if (fp32) {
+    if (!op->d_y32) CUCHK(cudaMalloc(&op->d_y32, fs->nexp * fs->bs * sizeof(float)));
+    yexp = op->d_y32;
+  } else {
+    if (!op->d_yexp) CUCHK(cudaMalloc(&op->d_yexp, fs->nexp * fs->bs * sizeof(double)));
+    yexp = op->d_yexp;
+  }
+  if (op->autotune && !P->tuned) {
+    const HpArgs A = make_args(op, x, fp32, yexp, nullptr);
+    if (fp32) DCHK(autotune<float>(op, A));
+    else DCHK(autotune<double>(op, A));
+    if (op->tune_path[0]) tune_save(op, op->tune_path, fp32);
+  }
+  cudaStream_t s = fs->stream;
+  if (op->launch == dLAUNCH_GRAPH) {
+    const double *ptrs[2] = {x, y};
+    CUCHK(cudaMemcpyAsync((void *)P->d_ptrs, ptrs, sizeof ptrs, cudaMemcpyHostToDevice, s));
+    cudaGraphExec_t &ex = P->exec[fp32 ? 1 : 0];
+    if (!ex) {
+      cudaGraph_t g;
+      CUCHK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      const HpArgs A = make_args(op, nullptr, fp32, yexp, P->d_ptrs);
+      dErr e = fp32 ? run_persistent<float>(op, A) : run_persistent<double>(op, A);
+      const int64_t N = fs->n * fs->bs;
+      if (!e && N) {
+        const int32_t *eti = fs->d_et_idx;
+        const double *etw = fs->boolean_e ? nullptr : fs->d_et_w;
+        if (fp32) k_restrict_table<float><<<(unsigned)((N + 255) / 256), 256, 0, s>>>(fs->n, fs->bs, fs->d_et_ptr, eti, etw, (const float *)yexp, (double *const *)(P->d_ptrs + 1));
+        else k_restrict_table<double><<<(unsigned)((N + 255) / 256), 256, 0, s>>>(fs->n, fs->bs, fs->d_et_ptr, eti, etw, (const double *)yexp, (double *const *)(P->d_ptrs + 1));
+      }
+      cudaError_t ce = cudaStreamEndCapture(s, &g);
+      if (e) return e;
+      CUCHK(ce);
+      CUCHK(cudaGraphInstantiate(&ex, g, 0));
+      CUCHK(cudaGraphDestroy(g));
+    }
+    CUCHK(cudaGraphLaunch(ex, s));
+    return 0;
+  }
+  const HpArgs A = make_args(op, x, fp32, yexp, nullptr);
+  if (op->launch == dLAUNCH_PERSISTENT) DCHK(fp32 ? run_persistent<float>(op, A) : run_persistent<double>(op, A));
+  else DCHK(fp32 ? run_per_order<float>(op, A) : run_per_order<double>(op, A));
+  return fp32 ? fs_restrict32(fs, (const float *)yexp, y, 0) : fs_restrict(fs, (const double *)yexp, y, 0);
+}
+
+extern "C" {
+
+dErr dOperatorSetLaunchMode(dOperator op, dLaunchMode mode) {
+  if (!op) return set_error("null operator");
+  if (mode < dLAUNCH_DEFAULT || mode > dLAUNCH_GRAPH) return set_error("launch mode %d invalid", (int)mode);
+  op->launch = mode;
+  return 0;
+}
+
+dErr dOperatorAutotune(dOperator op, const char *cache_path) {
+  if (!op) return set_error("null operator");
+  op->autotune = true;
+  op->tune_path[0] = 0;
+  if (cache_path) snprintf(op->tune_path, sizeof op->tune_path, "%s", cache_path);
+  if (op->hp_plan) {
+    ((HpPlan *)op->hp_plan)->tuned = false;
+    if (op->tune_path[0]) tune_load(op, op->tune_path, op->prec == dPREC_FP32);
+  }
+  return 0;
+}
+
+dErr dOperatorGetTiles(dOperator op, dInt *nbuckets, dInt *order, dInt *cap, dInt *threads) {
+  if (!op) return set_error("null operator");
+  HpPlan *P = (HpPlan *)op->hp_plan;
+  if (!P) {
+    if (nbuckets) *nbuckets = 0;
+    return 0;
+  }
+  if (nbuckets) *nbuckets = P->nb;
+  for (int b = 0; b < P->nb; b++) {
+    if (order) order[b] = P->N[b] - 1;
+    if (cap) cap[b] = P->cap[b];
+    if (threads) threads[b] = P->threads[b];
+  }
+  return 0;
+}
+
+}  // extern "C"

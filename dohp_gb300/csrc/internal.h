@@ -88,6 +88,8 @@ struct _p_dFS {
   // device
   int32_t *d_emap = nullptr, *d_xstart = nullptr, *d_edeg = nullptr, *d_qoff = nullptr;
   int32_t *d_et_ptr = nullptr, *d_et_idx = nullptr;  // E^T over closure nodes (ascending expanded index)
+  int32_t *d_eptr = nullptr, *d_ecol = nullptr;       // E as CSR (hp spaces only)
+  double *d_eval = nullptr, *d_et_w = nullptr;        // E values and E^T weights (hp spaces only)
   double *d_coords = nullptr;                        // [nelem][8][3]
   double *d_dcache = nullptr;                        // Dirichlet values [(nc-n)*bs]
   // per-degree basis tables on the device for FAST rules: [p] -> B, Dq (Q=P)
@@ -110,6 +112,10 @@ struct _p_dOperator {
   double *d_hx = nullptr, *d_hy = nullptr;  // device staging for the host-vector form
   bool geo_valid = false;
   int geo_kind = -1;
+  void *hp_plan = nullptr;  // order buckets, tiles, work list, graphs (hp.cu)
+  dLaunchMode launch = dLAUNCH_DEFAULT;
+  bool autotune = false;
+  char tune_path[512] = "";
 };
 
 struct _p_dMat {

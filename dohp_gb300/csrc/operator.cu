@@ -486,8 +486,11 @@ static dErr op_mult_fp32(_p_dOperator *op, const double *x, double *y) {
   return fs_restrict32(fs, op->d_y32, y, 0);
 }
 
+dErr hp_mult(_p_dOperator *op, const double *x, double *y);
+
 dErr op_mult(_p_dOperator *op, const double *x, double *y) {
   _p_dFS *fs = op->fs;
+  if (!fs->uniform || op->launch != dLAUNCH_DEFAULT) return hp_mult(op, x, y);
   if (op->prec == dPREC_FP32) return op_mult_fp32(op, x, y);
   if (!op->d_yexp) CUCHK(cudaMalloc(&op->d_yexp, fs->nexp * fs->bs * sizeof(double)));
   DCHK(op_mult_expanded(op, x, op->d_yexp));

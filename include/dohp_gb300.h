@@ -62,6 +62,10 @@ typedef enum {
 } dOperatorKind;
 /* Arithmetic of an operator apply */
 typedef enum { dPREC_FP64 = 0, dPREC_FP32 = 1 } dPrecision;
+/* Launch form of an operator apply: DEFAULT = one fused kernel for uniform-order spaces (per-order form for
+ * hp spaces); PER_ORDER = one launch per order bucket; PERSISTENT = one launch over all buckets with a device
+ * work counter; GRAPH = the persistent launch and the restriction replayed from a CUDA graph. */
+typedef enum { dLAUNCH_DEFAULT = 0, dLAUNCH_PER_ORDER = 1, dLAUNCH_PERSISTENT = 2, dLAUNCH_GRAPH = 3 } dLaunchMode;
 
 const char *dGetLastError(void);
 
@@ -142,6 +146,12 @@ dErr dOperatorSetQuadratureData(dOperator op, const dReal *qdata);
 /* p-Laplacian stash from the state g (EllipPointwiseComputeStore, ellip.c:333-342), exponent p, eps */
 dErr dOperatorComputePLaplaceStash(dOperator op, const dScalar *g, dReal p, dReal eps);
 dErr dOperatorSetPrecision(dOperator op, dPrecision prec);
+dErr dOperatorSetLaunchMode(dOperator op, dLaunchMode mode);
+/* measure tile shapes (elements per block x threads) per order bucket on the next apply; cache_path (may be
+ * NULL) is a JSON file read before and written after tuning, keyed by device, kind, order and precision */
+dErr dOperatorAutotune(dOperator op, const char *cache_path);
+/* current tiles per order bucket (after the first apply): order, elements per block, threads per block */
+dErr dOperatorGetTiles(dOperator op, dInt *nbuckets, dInt *order, dInt *cap, dInt *threads);
 /* MatMult: y = A x, device vectors of n*bs entries */
 dErr dOperatorMult(dOperator op, const dScalar *x, dScalar *y);
 /* element part of MatMult: yexp = (per-element q-function apply) E x, expanded device vector of nexp*bs;
