@@ -436,22 +436,32 @@ static dErr run_per_order(_p_dOperator *op, const HpArgs &A) {
 }
 
 template <typename T>
-static dErr run_persistent(_p_dOperator *op, const HpArgs &A) {
+// shared-memory attribute and grid of the persistent kernel (outside any stream capture)
+template <typename T>
+static dErr prepare_persistent(_p_dOperator *op, int *grid) {
   HpPlan *P = (HpPlan *)op->hp_plan;
-  cudaStream_t s = op->fs->stream;
   const size_t smem = P->persistent_smem[sizeof(T) == 4];
-  CUCHK(cudaMemsetAsync(P->d_counter, 0, sizeof(int), s));
+  int per = 1;
   if (op->kind == dOP_ELASTICITY) {
     CUCHK(cudaFuncSetAttribute(k_hp_persistent<T, dOP_ELASTICITY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per = 1;
     CUCHK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_hp_persistent<T, dOP_ELASTICITY>, 256, smem));
-    k_hp_persistent<T, dOP_ELASTICITY><<<P->persistent_blocks * std::max(per, 1), 256, smem, s>>>(A, P->d_elist, P->d_work, P->nwork, P->d_counter);
   } else {
     CUCHK(cudaFuncSetAttribute(k_hp_persistent<T, dOP_DIFFUSION>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per = 1;
     CUCHK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_hp_persistent<T, dOP_DIFFUSION>, 256, smem));
-    k_hp_persistent<T, dOP_DIFFUSION><<<P->persistent_blocks * std::max(per, 1), 256, smem, s>>>(A, P->d_elist, P->d_work, P->nwork, P->d_counter);
   }
+  *grid = P->persistent_blocks * std::max(per, 1);
+  return 0;
+}
+
+template <typename T>
+static dErr run_persistent(_p_dOperator *op, const HpArgs &A, cudaStream_t s, int grid) {
+  HpPlan *P = (HpPlan *)op->hp_plan;
+  const size_t smem = P->persistent_smem[sizeof(T) == 4];
+  CUCHK(cudaMemsetAsync(P->d_counter, 0, sizeof(int), s));
+  if (op->kind == dOP_ELASTICITY)
+    k_hp_persistent<T, dOP_ELASTICITY><<<grid, 256, smem, s>>>(A, P->d_elist, P->d_work, P->nwork, P->d_counter);
+  else
+    k_hp_persistent<T, dOP_DIFFUSION><<<grid, 256, smem, s>>>(A, P->d_elist, P->d_work, P->nwork, P->d_counter);
   CUCHK(cudaGetLastError());
   return 0;
 }
@@ -617,23 +627,30 @@ dErr hp_mult(_p_dOperator *op, const double *x, double *y) {
     if (op->tune_path[0]) tune_save(op, op->tune_path, fp32);
   }
   cudaStream_t s = fs->stream;
+  int grid = 0;
+  if (op->launch == dLAUNCH_PERSISTENT || op->launch == dLAUNCH_GRAPH) DCHK(fp32 ? prepare_persistent<float>(op, &grid) : prepare_persistent<double>(op, &grid));
   if (op->launch == dLAUNCH_GRAPH) {
     const double *ptrs[2] = {x, y};
     CUCHK(cudaMemcpyAsync((void *)P->d_ptrs, ptrs, sizeof ptrs, cudaMemcpyHostToDevice, s));
     cudaGraphExec_t &ex = P->exec[fp32 ? 1 : 0];
     if (!ex) {
+      // capture on a private stream (the legacy default stream cannot be captured); the graph is then
+      // launched on the operator's stream, ordered after the pointer-table copy above
+      cudaStream_t cs;
+      CUCHK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
       cudaGraph_t g;
-      CUCHK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      CUCHK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
       const HpArgs A = make_args(op, nullptr, fp32, yexp, P->d_ptrs);
-      dErr e = fp32 ? run_persistent<float>(op, A) : run_persistent<double>(op, A);
+      dErr e = fp32 ? run_persistent<float>(op, A, cs, grid) : run_persistent<double>(op, A, cs, grid);
       const int64_t N = fs->n * fs->bs;
       if (!e && N) {
         const int32_t *eti = fs->d_et_idx;
         const double *etw = fs->boolean_e ? nullptr : fs->d_et_w;
-        if (fp32) k_restrict_table<float><<<(unsigned)((N + 255) / 256), 256, 0, s>>>(fs->n, fs->bs, fs->d_et_ptr, eti, etw, (const float *)yexp, (double *const *)(P->d_ptrs + 1));
-        else k_restrict_table<double><<<(unsigned)((N + 255) / 256), 256, 0, s>>>(fs->n, fs->bs, fs->d_et_ptr, eti, etw, (const double *)yexp, (double *const *)(P->d_ptrs + 1));
+        if (fp32) k_restrict_table<float><<<(unsigned)((N + 255) / 256), 256, 0, cs>>>(fs->n, fs->bs, fs->d_et_ptr, eti, etw, (const float *)yexp, (double *const *)(P->d_ptrs + 1));
+        else k_restrict_table<double><<<(unsigned)((N + 255) / 256), 256, 0, cs>>>(fs->n, fs->bs, fs->d_et_ptr, eti, etw, (const double *)yexp, (double *const *)(P->d_ptrs + 1));
       }
-      cudaError_t ce = cudaStreamEndCapture(s, &g);
+      cudaError_t ce = cudaStreamEndCapture(cs, &g);
+      cudaStreamDestroy(cs);
       if (e) return e;
       CUCHK(ce);
       CUCHK(cudaGraphInstantiate(&ex, g, 0));
@@ -643,7 +660,7 @@ dErr hp_mult(_p_dOperator *op, const double *x, double *y) {
     return 0;
   }
   const HpArgs A = make_args(op, x, fp32, yexp, nullptr);
-  if (op->launch == dLAUNCH_PERSISTENT) DCHK(fp32 ? run_persistent<float>(op, A) : run_persistent<double>(op, A));
+  if (op->launch == dLAUNCH_PERSISTENT) DCHK(fp32 ? run_persistent<float>(op, A, s, grid) : run_persistent<double>(op, A, s, grid));
   else DCHK(fp32 ? run_per_order<float>(op, A) : run_per_order<double>(op, A));
   return fp32 ? fs_restrict32(fs, (const float *)yexp, y, 0) : fs_restrict(fs, (const double *)yexp, y, 0);
 }
