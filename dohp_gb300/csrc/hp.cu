@@ -435,7 +435,6 @@ static dErr run_per_order(_p_dOperator *op, const HpArgs &A) {
   return 0;
 }
 
-template <typename T>
 // shared-memory attribute and grid of the persistent kernel (outside any stream capture)
 template <typename T>
 static dErr prepare_persistent(_p_dOperator *op, int *grid) {
