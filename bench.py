@@ -1,36 +1,40 @@
-"""Benchmark: GDoF/s of the matrix-free hp-FEM operator apply (dohp's EllipShellMatMult) on one GB300.
+"""Benchmark: GDoF/s of the matrix-free hp-FEM operator apply (dohp's ElastShellMatMult / EllipShellMatMult)
+on one GB300.
 
-Workload (default, --config cfg4): variable-coefficient Poisson -div(k grad u) on a 64^3 structured hex
-mesh of the unit cube, interior vertices perturbed U[-0.1h, 0.1h] (seed 1), uniform p=4 on GLL nodes with
-Gauss (p+1)^3 quadrature, k = exp(g) with g a lognormal random field (variance 2, correlation length 0.1,
-random Fourier features, seed 2), homogeneous Dirichlet on all walls, FP64. 16,581,375 explicit dofs.
-A step is one operator apply y = A x (gather through E, element kernel, deterministic E^T restrict) on a
-seeded x ~ U[-1,1]. Inputs (x 133 MB, geometric factors 1.57 GB, E map 131 MB) exceed the 129 MB L2, so
-no flush is needed between steps.
+Default workload (--config cfg2, the hp-batching configuration): 3-D linear elasticity (E=1, nu=0.3,
+ElastPointwiseJacobian at F=I) on a 32^3 structured hex mesh of the unit cube, interior vertices perturbed
+U[-0.1h, 0.1h] (seed 1), per-element order drawn i.i.d. uniform from {2..8} (seed 2), min-order shared
+faces/edges with interpolation constraints, Gauss (p+1)^3 quadrature, Dirichlet walls, FP64. A step is one
+operator apply y = A x on a seeded x ~ U[-1,1]: one persistent kernel over all order buckets plus the
+deterministic E^T restriction, replayed from a CUDA graph. The per-order-launch and persistent forms are timed
+beside it. Inputs (geometric factors ~3 GB, E ~1 GB) exceed the 129 MB L2: no flush between steps.
+A secondary entry times the uniform FP64 Poisson apply (lognormal k, 64^3, p=4; --config cfg4 makes it the
+headline).
 
-Prints one JSON line (see the contract in the repository docs): value = explicit dofs / seconds per apply,
-device-timed with CUDA events on the launching stream; e2e = the same apply through dOperatorMultHost
-(host buffers, H2D and D2H copies inside the timed region); roofline of the dominant (element) kernel;
-cpu_baseline = the oracle's CPU restatement of the reference apply on the host cores.
+Prints one JSON line: value = explicit scalar dofs / device seconds per apply (CUDA events on the launching
+stream); e2e = dOperatorMultHost (host vectors, copies inside the timed region); roofline of the dominant
+element kernel; cpu_baseline = the oracle's CPU restatement of the reference apply on the host cores.
 """
 import argparse
 import json
 import os
 import subprocess
 import sys
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 CONFIGS = {
-    # name: (elements per direction, degree, lognormal coefficient)
-    "cfg4": dict(ne=64, p=4, grf=True, label="poisson-lognormal-64^3-p4"),
-    "cfg1": dict(ne=8, p=4, grf=False, label="poisson-8^3-p4"),
-    # reduced case of the same kernel for full ncu captures (geometric factors 196 MB, above L2)
-    "cfg4_32": dict(ne=32, p=4, grf=True, label="poisson-lognormal-32^3-p4"),
+    "cfg2": dict(ne=32, kind="elasticity", hp=True, p=4, grf=False, label="hp-elasticity-32^3-p2..8 (configs[1])"),
+    "cfg4": dict(ne=64, kind="diffusion", hp=False, p=4, grf=True, label="poisson-lognormal-64^3-p4 (configs[3])"),
+    "cfg1": dict(ne=8, kind="diffusion", hp=False, p=4, grf=False, label="poisson-8^3-p4 (configs[0])"),
+    # reduced cases of the same kernels for full ncu captures (inputs still above L2)
+    "cfg2_16": dict(ne=16, kind="elasticity", hp=True, p=4, grf=False, label="hp-elasticity-16^3-p2..8"),
+    "cfg4_32": dict(ne=32, kind="diffusion", hp=False, p=4, grf=True, label="poisson-lognormal-32^3-p4"),
 }
+E0, NU = 1.0, 0.3
+FP64_PEAK_GFLOPS = 1203.0  # FP64 FMA issue rate measured on this GB300 (FMA-chain probe)
 
 
 def parse():
@@ -39,8 +43,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="cfg4", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="cfg2", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true")
     return ap.parse_args()
 
 
@@ -55,11 +60,11 @@ def peaks():
 
 class ClockSampler:
     """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
-    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index):
-        self.index = index
-        self.proc = None
+        self.index, self.proc, self.lines = index, None, []
 
     def __enter__(self):
         try:
@@ -72,7 +77,6 @@ class ClockSampler:
         return self
 
     def __exit__(self, *a):
-        self.lines = []
         if self.proc:
             time.sleep(0.25)
             self.proc.terminate()
@@ -82,7 +86,7 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for l in getattr(self, "lines", []):
+        for l in self.lines:
             f = [x.strip() for x in l.split(",")]
             if len(f) < 9:
                 continue
@@ -95,8 +99,14 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(n)
         sm.sort()
-        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def elem_orders(cfg, ne):
+    import numpy as np
+    if not cfg["hp"]:
+        return None
+    return np.random.default_rng(2).integers(2, 9, size=ne ** 3).astype(np.int32)
 
 
 def grf_numpy(grf, X):
@@ -112,48 +122,120 @@ def grf_numpy(grf, X):
 
 
 def cpu_baseline(cfg, threads, budget_s=20.0):
-    """Oracle (CPU restatement of the reference apply: per-element geometry recompute, INTERP+GRAD,
-    q-function, INTERP_T+GRAD_T, E/E^T) timed on a bounded sample of the workload: a 32^3-element block
-    of the same order and coefficient kind, all host threads (OpenMP)."""
+    """Oracle (CPU restatement of the reference apply: per-element geometry recompute, INTERP+GRAD, q-function,
+    INTERP_T+GRAD_T, E/E^T) timed on a bounded sample of the workload (a smaller block of the same kind, order
+    distribution and coefficient), all host threads (OpenMP; the reference runs one MPI rank per core)."""
     import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as po
     po.build()
-    ne = min(cfg["ne"], 32)
-    fs = po.FS(ne + 1, ne + 1, ne + 1, degree=cfg["p"], perturb=0.1, seed=1)
-    qd = None
+    ne = min(cfg["ne"], 12 if cfg["hp"] else 32)
+    bs = 3 if cfg["kind"] == "elasticity" else 1
+    fs = po.FS(ne + 1, ne + 1, ne + 1, degree=cfg["p"], perturb=0.1, seed=1, bs=bs, elem_degree=elem_orders(cfg, ne))
+    qd, kind, param = None, 0, None
+    if cfg["kind"] == "elasticity":
+        kind = 2
+        param = np.array([E0 * NU / ((1 + NU) * (1 - 2 * NU)), E0 / (2 * (1 + NU))])
     if cfg["grf"]:
         grf = po.grf_make(64, 2.0, 0.1, 2)
         qd = grf_numpy(grf, fs.qpt_coords())
-    x = np.random.default_rng(0).uniform(-1, 1, fs.n)
-    fs.apply(x, qdata=qd, nthreads=threads)  # warm-up
+    x = np.random.default_rng(0).uniform(-1, 1, fs.n * bs)
+    fs.apply(x, kind=kind, qdata=qd, param=param, nthreads=threads)  # warm-up
     times = []
     t_start = time.perf_counter()
     while len(times) < 3 or (time.perf_counter() - t_start < budget_s and len(times) < 10):
         t0 = time.perf_counter()
-        fs.apply(x, qdata=qd, nthreads=threads)
+        fs.apply(x, kind=kind, qdata=qd, param=param, nthreads=threads)
         times.append(time.perf_counter() - t0)
         if time.perf_counter() - t_start > budget_s:
             break
     times.sort()
     t = times[len(times) // 2]
-    return {"value": fs.n / t / 1e9, "unit": "GDoF/s", "cores": threads, "kind": "port",
-            "sample": "%d^3 elements p=%d (%d dofs), median of %d applies, oracle C restatement, %d OpenMP threads"
-                      % (ne, cfg["p"], fs.n, len(times), threads)}
+    return {"value": fs.n * bs / t / 1e9, "unit": "GDoF/s", "cores": threads, "kind": "port",
+            "sample": "%d^3 elements of the same workload (%d dofs), median of %d applies, oracle C restatement, %d OpenMP threads"
+                      % (ne, fs.n * bs, len(times), threads)}
 
 
 def run_reference(args, cfg, rank):
-    threads = os.cpu_count() or 1
     if rank != 0:
         return
+    threads = os.cpu_count() or 1
     cb = cpu_baseline(cfg, threads, budget_s=max(10.0, min(60.0, 3.0 * args.steps)))
     line = {"impl": "reference", "metric": "GDoF/s operator apply", "value": cb["value"], "unit": "GDoF/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": cfg["label"] + " (bounded CPU sample)", "parallelism": "host threads"},
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "GDoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def setup(cfg, stream):
+    import numpy as np
+    import torch
+    import dohp_gb300 as dg
+    ne = cfg["ne"]
+    bs = 3 if cfg["kind"] == "elasticity" else 1
+    fs = dg.FS((ne + 1,) * 3, degree=cfg["p"], perturb=0.1, seed=1, bs=bs, elem_degree=elem_orders(cfg, ne),
+               stream=stream.cuda_stream)
+    if cfg["kind"] == "elasticity":
+        op = fs.operator(dg.dOP_ELASTICITY, param=(E0, NU))
+    else:
+        op = fs.operator(dg.dOP_DIFFUSION)
+        if cfg["grf"]:
+            kq = torch.empty(fs.nq, dtype=torch.float64, device="cuda")
+            fs.lognormal(dg.grf_create(64, 2.0, 0.1, 2), kq)
+            op.set_qdata(kq)
+    x = torch.as_tensor(np.random.default_rng(0).uniform(-1, 1, fs.n * bs), device="cuda")
+    return fs, op, x, bs
+
+
+def time_loop(fn, steps, stream):
+    import torch
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0.record(stream)
+    for a, b in evs:
+        a.record(stream)
+        fn()
+        b.record(stream)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    per = sorted(a.elapsed_time(b) for a, b in evs)
+    return t0.elapsed_time(t1) / steps, per[len(per) // 2]
+
+
+def work_per_apply(fs, cfg, bs):
+    """SURVEY 8(d) algorithmic bytes and flops per apply, and the flops the element kernels issue."""
+    import numpy as np
+    deg = fs.elem_degree()[:, 0].astype(np.float64)
+    n1 = deg + 1
+    alg_bytes = 16.0 * bs * fs.nc + float(np.sum(4.0 * n1 ** 3 + 192.0))
+    alg_flops = float(np.sum(36.0 * n1 ** 4 * bs + 30.0 * n1 ** 3 * bs))
+    pw = 150.0 if bs == 3 else 18.0
+    issued = float(np.sum(24.0 * n1 ** 4 * bs + pw * n1 ** 3))
+    return alg_bytes, alg_flops, issued
+
+
+def secondary_cfg4(args):
+    """uniform FP64 Poisson apply (lognormal k, 64^3, p=4): element kernel + restrict, device-timed."""
+    import torch
+    cfg = CONFIGS["cfg4"]
+    stream = torch.cuda.current_stream()
+    fs, op, x, bs = setup(cfg, stream)
+    y = torch.empty(fs.n, dtype=torch.float64, device="cuda")
+    yexp = torch.empty(fs.nexp, dtype=torch.float64, device="cuda")
+    for _ in range(3):
+        op.mult_expanded(x, yexp)
+        fs.expanded_to_global(yexp, y)
+    ms, _ = time_loop(lambda: (op.mult_expanded(x, yexp), fs.expanded_to_global(yexp, y)), max(args.steps // 2, 5), stream)
+    _, kms = time_loop(lambda: op.mult_expanded(x, yexp), max(args.steps // 2, 5), stream)
+    _, _, issued = work_per_apply(fs, cfg, bs)
+    return {"workload": cfg["label"], "dofs": fs.n, "value": fs.n / (ms * 1e-3) / 1e9, "unit": "GDoF/s", "ms_per_apply": ms,
+            "element_kernel_ms": kms, "fp64_gflops": issued / (kms * 1e-3) / 1e9,
+            "fp64_frac_of_peak": issued / (kms * 1e-3) / 1e9 / FP64_PEAK_GFLOPS, "dtype": "f64"}
 
 
 def main():
@@ -165,7 +247,6 @@ def main():
     if args.impl == "reference":
         return run_reference(args, cfg, rank)
 
-    import numpy as np
     import torch
     dist = None
     if world > 1:
@@ -179,46 +260,38 @@ def main():
     _b.build()
 
     stream = torch.cuda.current_stream()
-    ne, p = cfg["ne"], cfg["p"]
-    fs = dg.FS((ne + 1,) * 3, degree=p, perturb=0.1, seed=1, stream=stream.cuda_stream)
-    op = fs.operator(dg.dOP_DIFFUSION)
-    if cfg["grf"]:
-        grf = dg.grf_create(64, 2.0, 0.1, 2)
-        kq = torch.empty(fs.nq, dtype=torch.float64, device="cuda")
-        fs.lognormal(grf, kq)
-        op.set_qdata(kq)
-    x = torch.as_tensor(np.random.default_rng(0).uniform(-1, 1, fs.n), device="cuda")
-    y = torch.empty(fs.n, dtype=torch.float64, device="cuda")
-    yexp = torch.empty(fs.nexp, dtype=torch.float64, device="cuda")
-
-    def step():
-        op.mult_expanded(x, yexp)
-        fs.expanded_to_global(yexp, y)
-
+    fs, op, x, bs = setup(cfg, stream)
+    N = fs.n * bs
+    y = torch.empty(N, dtype=torch.float64, device="cuda")
+    yexp = torch.empty(fs.nexp * bs, dtype=torch.float64, device="cuda")
+    forms = {}
+    if cfg["hp"]:
+        op.autotune(os.path.join(ROOT, "dohp_gb300", "_lib", "autotune.json"))
+        op.set_launch(dg.dLAUNCH_PER_ORDER)
+        for _ in range(3):
+            op.mult(x, y)
+        forms["per_order_ms"], _ = time_loop(lambda: op.mult(x, y), max(args.steps // 2, 3), stream)
+        op.set_launch(dg.dLAUNCH_PERSISTENT)
+        for _ in range(3):
+            op.mult(x, y)
+        forms["persistent_ms"], _ = time_loop(lambda: op.mult(x, y), max(args.steps // 2, 3), stream)
+        _, kms = time_loop(lambda: op.mult_expanded(x, yexp), max(args.steps // 2, 3), stream)
+        op.set_launch(dg.dLAUNCH_GRAPH)
+        kernel_name = "k_hp_persistent<double,elasticity> (all order buckets)"
+    else:
+        for _ in range(3):
+            op.mult_expanded(x, yexp)
+        _, kms = time_loop(lambda: op.mult_expanded(x, yexp), max(args.steps // 2, 3), stream)
+        kernel_name = "k_diffusion<%d,double> (element apply)" % (cfg["p"] + 1)
     for _ in range(max(args.warmup, 3)):
-        step()
+        op.mult(x, y)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
     with ClockSampler(local) as clk:
-        torch.cuda.synchronize()
-        t0 = torch.cuda.Event(enable_timing=True); t1 = torch.cuda.Event(enable_timing=True)
-        t0.record(stream)
-        for a, b, c in ev:
-            a.record(stream)
-            op.mult_expanded(x, yexp)
-            b.record(stream)
-            fs.expanded_to_global(yexp, y)
-            c.record(stream)
-        t1.record(stream)
-        torch.cuda.synchronize()
-        # keep the sampler alive over a comparable window for the e2e loop below
-    total_ms = t0.elapsed_time(t1)
-    kern_ms = sorted(a.elapsed_time(b) for a, b, _ in ev)
-    rest_ms = sorted(b.elapsed_time(c) for _, b, c in ev)
-    ms_step = total_ms / args.steps
+        ms_step, _ = time_loop(lambda: op.mult(x, y), args.steps, stream)
+    if cfg["hp"]:
+        forms["graph_ms"] = ms_step
     if dist:
         t = torch.tensor([ms_step], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -226,13 +299,12 @@ def main():
         dist.barrier()
 
     # end to end through the host-vector entry point (pinned buffers, copies inside the timed region)
-    xh = torch.empty(fs.n, dtype=torch.float64).pin_memory()
-    yh = torch.empty(fs.n, dtype=torch.float64).pin_memory()
+    xh = torch.empty(N, dtype=torch.float64).pin_memory()
+    yh = torch.empty(N, dtype=torch.float64).pin_memory()
     xh.copy_(x.cpu())
     xn, yn = xh.numpy(), yh.numpy()
     for _ in range(3):
         op.mult_host(xn, yn)
-    torch.cuda.synchronize()
     e2e_steps = max(3, args.steps // 2)
     t_e = time.perf_counter()
     for _ in range(e2e_steps):
@@ -242,43 +314,40 @@ def main():
         t = torch.tensor([e2e_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
-
     if rank != 0:
         dist.destroy_process_group()
         return
+
     hbm, src = peaks()
-    nelem = fs.nelem
-    closure_dofs = fs.nc  # (64*4+1)^3 nodes incl. Dirichlet
-    alg_bytes = 16.0 * closure_dofs + nelem * (4.0 * (p + 1) ** 3 + 192.0)  # survey algorithmic figure per apply
-    n1 = p + 1
-    alg_flops = nelem * (36.0 * n1 ** 4 + 30.0 * n1 ** 3)
-    kmed = kern_ms[len(kern_ms) // 2]
-    achieved = alg_bytes / (kmed * 1e-3) / 1e9
-    fp64_peak = 1203.0  # GFLOP/s: FP64 FMA issue rate measured on this GB300 by an FMA-chain probe
-    actual_flops = nelem * (2 * 12.0 * n1 ** 4 + 2 * 9.0 * n1 ** 3)  # FLOPs the kernel issues (collocation form)
-    clocks = clk.summary()
-    value = world * fs.n / (ms_step * 1e-3) / 1e9
+    alg_bytes, alg_flops, issued = work_per_apply(fs, cfg, bs)
+    achieved = alg_bytes / (kms * 1e-3) / 1e9
+    value = world * N / (ms_step * 1e-3) / 1e9
     line = {
         "metric": "GDoF/s operator apply", "value": value, "unit": "GDoF/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded mesh perturbation, seeded field and input)",
-        "config": {"workload": cfg["label"], "elements": nelem, "degree": p, "dofs": fs.n, "closure_dofs": closure_dofs,
-                   "quadrature": "Gauss (p+1)^3", "l2": "inputs larger than L2 (1.8 GB per apply), no flush",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)",
-                     "kernel": "k_diffusion<5,double> (element apply)", "kernel_ms_median": kmed,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded mesh perturbation, orders, field and input)",
+        "config": {"workload": cfg["label"], "elements": fs.nelem, "dofs": N, "block_size": bs,
+                   "orders": "i.i.d. U{2..8}, seed 2" if cfg["hp"] else "p=%d" % cfg["p"], "quadrature": "Gauss (p+1)^3",
+                   "launch": "persistent kernel + restriction in a CUDA graph" if cfg["hp"] else "fused element kernel + restriction",
+                   "l2": "inputs larger than L2, no flush", "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                     "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)", "kernel": kernel_name, "kernel_ms_median": kms,
                      "alg_bytes_per_launch": alg_bytes},
-        "fp64_roofline": {"bound": "fp64 pipe", "achieved": actual_flops / (kmed * 1e-3) / 1e9, "peak": fp64_peak,
-                          "unit": "GFLOP/s", "frac": actual_flops / (kmed * 1e-3) / 1e9 / fp64_peak,
-                          "alg_flops_per_launch": alg_flops, "issued_flops_per_launch": actual_flops,
-                          "alg_gflops_per_s": alg_flops / (kmed * 1e-3) / 1e9},
-        "restrict_ms_median": rest_ms[len(rest_ms) // 2],
-        "e2e": {"value": world * fs.n / e2e_s / 1e9, "unit": "GDoF/s", "h2d_bytes_per_step": 8 * fs.n,
-                "d2h_bytes_per_step": 8 * fs.n, "entry_point": "dOperatorMultHost"},
+        "fp64_roofline": {"bound": "fp64 pipe", "achieved": issued / (kms * 1e-3) / 1e9, "peak": FP64_PEAK_GFLOPS,
+                          "unit": "GFLOP/s", "frac": issued / (kms * 1e-3) / 1e9 / FP64_PEAK_GFLOPS,
+                          "issued_flops_per_launch": issued, "alg_flops_per_launch": alg_flops},
+        "e2e": {"value": world * N / e2e_s / 1e9, "unit": "GDoF/s", "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N,
+                "entry_point": "dOperatorMultHost"},
         "gpu_launches": 2 * args.steps,
-        "clocks": clocks,
+        "clocks": clk.summary(),
     }
+    if cfg["hp"]:
+        line["launch_forms"] = forms
+        line["tiles"] = op.tiles()
+    if not args.no_secondary and args.config == "cfg2":
+        del fs, op, x, y, yexp
+        torch.cuda.empty_cache()
+        line["secondary"] = secondary_cfg4(args)
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(cfg, os.cpu_count() or 1)
     print(json.dumps(line))

@@ -580,6 +580,29 @@ static void tune_save(_p_dOperator *op, const char *path, bool fp32) {
 }
 
 // y = A x for hp spaces (any E) in the operator's launch form and precision
+dErr hp_mult(_p_dOperator *op, const double *x, double *y);
+
+// element part only (FP64): yexp = element kernels in the per-order or persistent form, no restriction
+dErr hp_mult_expanded(_p_dOperator *op, const double *x, double *yexp) {
+  if (op->prec != dPREC_FP64) return set_error("expanded-output form is FP64 only");
+  if (!op->hp_plan) {  // run one full apply to build the plan, geometry and tiles
+    double *tmp;
+    CUCHK(cudaMalloc(&tmp, std::max<int64_t>(op->fs->n * op->fs->bs, 1) * sizeof(double)));
+    const dLaunchMode save = op->launch;
+    if (op->launch == dLAUNCH_GRAPH) op->launch = dLAUNCH_PERSISTENT;
+    const dErr e = hp_mult(op, x, tmp);
+    op->launch = save;
+    CUCHK(cudaStreamSynchronize(op->fs->stream));
+    cudaFree(tmp);
+    if (e) return e;
+  }
+  const HpArgs A = make_args(op, x, false, yexp, nullptr);
+  if (op->launch == dLAUNCH_PER_ORDER || op->launch == dLAUNCH_DEFAULT) return run_per_order<double>(op, A);
+  int grid = 0;
+  DCHK(prepare_persistent<double>(op, &grid));
+  return run_persistent<double>(op, A, op->fs->stream, grid);
+}
+
 dErr hp_mult(_p_dOperator *op, const double *x, double *y) {
   _p_dFS *fs = op->fs;
   if (op->kind == dOP_PLAPLACE_JACOBIAN) return set_error("hp apply for the p-Laplacian Jacobian not built yet");

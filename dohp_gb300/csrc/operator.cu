@@ -453,8 +453,11 @@ static dErr elasticity_apply_t(_p_dFS *fs, const double *x, const T *geo, T lam,
   return set_error("degree %d not supported", fs->p);
 }
 
+dErr hp_mult_expanded(_p_dOperator *op, const double *x, double *yexp);
+
 dErr op_mult_expanded(_p_dOperator *op, const double *x, double *yexp) {
   _p_dFS *fs = op->fs;
+  if (!fs->uniform || op->launch != dLAUNCH_DEFAULT) return hp_mult_expanded(op, x, yexp);
   DCHK(op_compute_geometry(op));
   if (op->kind == dOP_DIFFUSION) return diffusion_apply_t<double>(fs, x, op->d_geo, yexp);
   if (op->kind == dOP_ELASTICITY) return elasticity_apply_t<double>(fs, x, op->d_geo, op->lam, op->mu, yexp);
