@@ -272,3 +272,47 @@ Operator.mult_expanded = _op_mult_expanded
 Operator.set_launch = _op_set_launch
 Operator.autotune = _op_autotune
 Operator.tiles = _op_tiles
+
+
+class _DeviceArray:
+    """Exposes a library-owned device array to torch through __cuda_array_interface__ (no copy)."""
+
+    def __init__(self, addr, shape):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": "<f8", "data": (addr, False),
+                                         "version": 3, "strides": None}
+
+
+class RulesetIterator:
+    """dRulesetIterator over all elements at once (FAST rule, uniform order). get() returns torch views of the
+    library's quadrature arrays: jw[nq], x[nq,3], dx[nq,3,3], u[nq,bs], du[nq,bs,3], v[nq,bs], dv[nq,bs,3].
+    Only v and dv are meant to be written (torch has no read-only device tensors)."""
+
+    def __init__(self, fs, method=FAST):
+        self.fs = fs
+        self.h = _vp()
+        chk(lib().dRulesetIteratorCreate(fs.h, ctypes.c_int(method), ctypes.byref(self.h)))
+
+    def __del__(self):
+        if _lib is not None and getattr(self, "h", None):
+            _lib.dRulesetIteratorDestroy(ctypes.byref(self.h))
+
+    def start(self, g=None, hmode=dFS_HOMOGENEOUS):
+        chk(lib().dRulesetIteratorStart(self.h, ptr(g), ctypes.c_int(hmode)))
+
+    def get(self):
+        import torch
+        nq = _i64()
+        p = [_vp() for _ in range(7)]
+        chk(lib().dRulesetIteratorGetPatchApplied(self.h, ctypes.byref(nq), *[ctypes.byref(q) for q in p]))
+        n, bs = nq.value, self.fs.bs
+        shapes = [(n,), (n, 3), (n, 3, 3), (n, bs), (n, bs, 3), (n, bs), (n, bs, 3)]
+        names = ["jw", "x", "dx", "u", "du", "v", "dv"]
+        return {k: torch.as_tensor(_DeviceArray(q.value, s), device="cuda")
+                for k, q, s in zip(names, p, shapes)}
+
+    def commit(self, imode=INSERT_VALUES, use_v=True, use_dv=True):
+        chk(lib().dRulesetIteratorCommitPatchApplied(self.h, ctypes.c_int(imode), ctypes.c_int(int(use_v)),
+                                                     ctypes.c_int(int(use_dv))))
+
+    def finish(self, y=None, imode=INSERT_VALUES):
+        chk(lib().dRulesetIteratorFinish(self.h, ptr(y), ctypes.c_int(imode)))

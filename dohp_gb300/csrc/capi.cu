@@ -483,30 +483,4 @@ dErr dOperatorComputePLaplaceStash(dOperator op, const dScalar *g, dReal p, dRea
   return set_error("p-Laplacian stash not built yet");
 }
 
-dErr dRulesetIteratorCreate(dFS fs, dQuadratureMethod method, dRulesetIterator *it) {
-  (void)fs, (void)method, (void)it;
-  return set_error("dRulesetIterator not built yet");
-}
-dErr dRulesetIteratorDestroy(dRulesetIterator *it) {
-  (void)it;
-  return 0;
-}
-dErr dRulesetIteratorStart(dRulesetIterator it, const dScalar *g, dFSHomogeneousMode hmode) {
-  (void)it, (void)g, (void)hmode;
-  return set_error("dRulesetIterator not built yet");
-}
-dErr dRulesetIteratorGetPatchApplied(dRulesetIterator it, int64_t *nq, const dReal **jw, const dScalar **x, const dScalar **dx,
-                                     const dScalar **u, const dScalar **du, dScalar **v, dScalar **dv) {
-  (void)it, (void)nq, (void)jw, (void)x, (void)dx, (void)u, (void)du, (void)v, (void)dv;
-  return set_error("dRulesetIterator not built yet");
-}
-dErr dRulesetIteratorCommitPatchApplied(dRulesetIterator it, InsertMode imode, int use_v, int use_dv) {
-  (void)it, (void)imode, (void)use_v, (void)use_dv;
-  return set_error("dRulesetIterator not built yet");
-}
-dErr dRulesetIteratorFinish(dRulesetIterator it, dScalar *y, InsertMode imode) {
-  (void)it, (void)y, (void)imode;
-  return set_error("dRulesetIterator not built yet");
-}
-
 }  // extern "C"

@@ -1,0 +1,173 @@
+// dRulesetIterator, batched device form (src/fs/interface/fsrulesetit.c:234-643).
+//
+// The reference walks elements one at a time: GetPatchApplied evaluates coordinates (link 0: INTERP and
+// GRAD of the Q1 coordinate space, dRuleComputePhysical) and the field (INTERP, GRAD mapped by J^-1) at the
+// element's quadrature points, the caller's q-function fills v/dv, CommitPatchApplied integrates them back
+// (INTERP_TRANSPOSE, GRAD_TRANSPOSE) into the expanded test vector, and Finish restricts it. Here one call of
+// each step covers all elements: quadrature arrays are element-natural per element, elements back to back,
+// and every evaluation is one batched dEFSApply launch. FAST rules (one patch per element) on uniform-order
+// spaces.
+#include "internal.h"
+
+using namespace dgb;
+
+dErr fs_expand(_p_dFS *fs, const double *g, double *x, bool inhomogeneous, int add);
+dErr fs_restrict(_p_dFS *fs, const double *x, double *g, int add);
+
+struct _p_dRulesetIterator {
+  dFS fs;
+  dEFS efs = nullptr, cefs = nullptr;  // field and coordinate element spaces on the same rule
+  int64_t nq = 0, nel = 0;
+  double *xexp = nullptr, *yexp = nullptr;
+  double *jw = nullptr, *x = nullptr, *dx = nullptr, *jinv = nullptr, *u = nullptr, *du = nullptr, *v = nullptr, *dv = nullptr;
+  double *d_w = nullptr;  // rule weights per element-natural point
+  bool started = false, applied = false;
+};
+
+namespace {
+
+// dRuleComputePhysical (src/jacobi/interface/jacobi.c:383-414): J^-1 by cofactors, jw = w det J, det < 0 is an error
+__global__ void k_physical(int64_t nel, int nq, const double *__restrict__ w, const double *__restrict__ dx,
+                           double *__restrict__ jinv, double *__restrict__ jw, int *neg) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nel * nq) return;
+  const double *a = dx + t * 9;
+  double *b = jinv + t * 9;
+  const double c0 = a[4] * a[8] - a[7] * a[5], c3 = -(a[3] * a[8] - a[6] * a[5]), c6 = a[3] * a[7] - a[6] * a[4];
+  const double det = a[0] * c0 + a[1] * c3 + a[2] * c6, id = 1.0 / det;
+  b[0] = id * c0;
+  b[1] = -id * (a[1] * a[8] - a[7] * a[2]);
+  b[2] = id * (a[1] * a[5] - a[4] * a[2]);
+  b[3] = id * c3;
+  b[4] = id * (a[0] * a[8] - a[6] * a[2]);
+  b[5] = -id * (a[0] * a[5] - a[3] * a[2]);
+  b[6] = id * c6;
+  b[7] = -id * (a[0] * a[7] - a[6] * a[1]);
+  b[8] = id * (a[0] * a[4] - a[3] * a[1]);
+  if (det < 0) atomicExch(neg, 1);
+  jw[t] = w[t % nq] * det;
+}
+
+}  // namespace
+
+extern "C" {
+
+dErr dRulesetIteratorCreate(dFS fs, dQuadratureMethod method, dRulesetIterator *it) {
+  if (!fs || !it) return set_error("null argument");
+  if (!fs->setup) return set_error("dFS not set up");
+  if (method != dQUADRATURE_METHOD_FAST) return set_error("batched iterator supports FAST rules (one patch per element)");
+  if (!fs->uniform) return set_error("batched iterator needs a uniform-order space");
+  if (!fs->jac) return set_error("dFS was created without a dJacobi");
+  _p_dRulesetIterator *I = new _p_dRulesetIterator();
+  I->fs = fs;
+  const dInt deg[3] = {fs->p, fs->p, fs->p}, one[3] = {1, 1, 1}, ro[3] = {2 * fs->p, 2 * fs->p, 2 * fs->p};
+  dErr e = dJacobiGetEFS(fs->jac, deg, method, ro, &I->efs);
+  if (!e) e = dJacobiGetEFS(fs->jac, one, method, ro, &I->cefs);
+  if (e) {
+    delete I;
+    return e;
+  }
+  const int Q = I->efs->Q[0] * I->efs->Q[1] * I->efs->Q[2];
+  I->nel = fs->nelem;
+  I->nq = fs->nelem * Q;
+  const int bs = fs->bs;
+  CUCHK(cudaMalloc(&I->xexp, fs->nexp * bs * sizeof(double)));
+  CUCHK(cudaMalloc(&I->yexp, fs->nexp * bs * sizeof(double)));
+  CUCHK(cudaMalloc(&I->jw, I->nq * sizeof(double)));
+  CUCHK(cudaMalloc(&I->x, I->nq * 3 * sizeof(double)));
+  CUCHK(cudaMalloc(&I->dx, I->nq * 9 * sizeof(double)));
+  CUCHK(cudaMalloc(&I->jinv, I->nq * 9 * sizeof(double)));
+  CUCHK(cudaMalloc(&I->u, I->nq * bs * sizeof(double)));
+  CUCHK(cudaMalloc(&I->du, I->nq * bs * 3 * sizeof(double)));
+  CUCHK(cudaMalloc(&I->v, I->nq * bs * sizeof(double)));
+  CUCHK(cudaMalloc(&I->dv, I->nq * bs * 3 * sizeof(double)));
+  std::vector<double> w(Q);
+  const Basis1D *b = I->efs->b;
+  for (int i = 0; i < b[0].Q; i++)
+    for (int j = 0; j < b[1].Q; j++)
+      for (int k = 0; k < b[2].Q; k++) w[(i * b[1].Q + j) * b[2].Q + k] = b[0].w[i] * b[1].w[j] * b[2].w[k];
+  CUCHK(cudaMalloc(&I->d_w, Q * sizeof(double)));
+  CUCHK(cudaMemcpy(I->d_w, w.data(), Q * sizeof(double), cudaMemcpyHostToDevice));
+  *it = I;
+  return 0;
+}
+
+dErr dRulesetIteratorDestroy(dRulesetIterator *it) {
+  if (!it || !*it) return 0;
+  _p_dRulesetIterator *I = *it;
+  for (double *p : {I->xexp, I->yexp, I->jw, I->x, I->dx, I->jinv, I->u, I->du, I->v, I->dv, I->d_w}) cudaFree(p);
+  delete I;
+  *it = nullptr;
+  return 0;
+}
+
+dErr dRulesetIteratorStart(dRulesetIterator it, const dScalar *g, dFSHomogeneousMode hmode) {
+  if (!it) return set_error("null iterator");
+  _p_dFS *fs = it->fs;
+  if (g) DCHK(fs_expand(fs, g, it->xexp, hmode == dFS_INHOMOGENEOUS, 0));
+  else CUCHK(cudaMemsetAsync(it->xexp, 0, fs->nexp * fs->bs * sizeof(double), fs->stream));
+  CUCHK(cudaMemsetAsync(it->yexp, 0, fs->nexp * fs->bs * sizeof(double), fs->stream));
+  it->started = true;
+  it->applied = false;
+  return 0;
+}
+
+dErr dRulesetIteratorGetPatchApplied(dRulesetIterator it, int64_t *nq, const dReal **jw, const dScalar **x, const dScalar **dx,
+                                     const dScalar **u, const dScalar **du, dScalar **v, dScalar **dv) {
+  if (!it || !it->started) return set_error("dRulesetIteratorStart first");
+  _p_dFS *fs = it->fs;
+  cudaStream_t s = fs->stream;
+  const int bs = fs->bs;
+  const int Q = (int)(it->nq / it->nel);
+  if (!it->applied) {
+    // link 0 (coordinates): INTERP and GRAD without mapping, then the physical map
+    DCHK(dEFSApplyBatched(it->cefs, (dInt)it->nel, nullptr, 3, fs->d_coords, it->x, dAPPLY_INTERP, INSERT_VALUES, s));
+    DCHK(dEFSApplyBatched(it->cefs, (dInt)it->nel, nullptr, 3, fs->d_coords, it->dx, dAPPLY_GRAD, INSERT_VALUES, s));
+    int *neg;
+    CUCHK(cudaMalloc(&neg, sizeof(int)));
+    CUCHK(cudaMemsetAsync(neg, 0, sizeof(int), s));
+    k_physical<<<(unsigned)((it->nq + 255) / 256), 256, 0, s>>>(it->nel, Q, it->d_w, it->dx, it->jinv, it->jw, neg);
+    CUCHK(cudaGetLastError());
+    int hneg = 0;
+    CUCHK(cudaMemcpyAsync(&hneg, neg, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUCHK(cudaStreamSynchronize(s));
+    cudaFree(neg);
+    if (hneg) return set_error("Negative Jacobian in the element geometry");
+    // link 1 (field): INTERP and GRAD mapped to physical coordinates
+    DCHK(dEFSApplyBatched(it->efs, (dInt)it->nel, nullptr, bs, it->xexp, it->u, dAPPLY_INTERP, INSERT_VALUES, s));
+    DCHK(dEFSApplyBatched(it->efs, (dInt)it->nel, it->jinv, bs, it->xexp, it->du, dAPPLY_GRAD, INSERT_VALUES, s));
+    CUCHK(cudaMemsetAsync(it->v, 0, it->nq * bs * sizeof(double), s));
+    CUCHK(cudaMemsetAsync(it->dv, 0, it->nq * bs * 3 * sizeof(double), s));
+    it->applied = true;
+  }
+  if (nq) *nq = it->nq;
+  if (jw) *jw = it->jw;
+  if (x) *x = it->x;
+  if (dx) *dx = it->dx;
+  if (u) *u = it->u;
+  if (du) *du = it->du;
+  if (v) *v = it->v;
+  if (dv) *dv = it->dv;
+  return 0;
+}
+
+dErr dRulesetIteratorCommitPatchApplied(dRulesetIterator it, InsertMode imode, int use_v, int use_dv) {
+  if (!it || !it->applied) return set_error("dRulesetIteratorGetPatchApplied first");
+  _p_dFS *fs = it->fs;
+  InsertMode m = imode;
+  if (use_v) {
+    DCHK(dEFSApplyBatched(it->efs, (dInt)it->nel, it->jinv, fs->bs, it->v, it->yexp, dAPPLY_INTERP_TRANSPOSE, m, fs->stream));
+    m = ADD_VALUES;
+  }
+  if (use_dv) DCHK(dEFSApplyBatched(it->efs, (dInt)it->nel, it->jinv, fs->bs, it->dv, it->yexp, dAPPLY_GRAD_TRANSPOSE, m, fs->stream));
+  return 0;
+}
+
+dErr dRulesetIteratorFinish(dRulesetIterator it, dScalar *y, InsertMode imode) {
+  if (!it || !it->started) return set_error("dRulesetIteratorStart first");
+  it->started = false;
+  if (!y) return 0;
+  return fs_restrict(it->fs, it->yexp, y, imode == ADD_VALUES);
+}
+
+}  // extern "C"

@@ -1,0 +1,122 @@
+"""Batched dRulesetIterator: a q-function written in torch between GetPatchApplied and CommitPatchApplied
+reproduces the fused operator applies and the oracle (src/fs/interface/fsrulesetit.c, the Start /
+GetPatchApplied / CommitPatchApplied / Finish cycle used by src/fs/tests/elast.c and src/fs/tests/ellip.c)."""
+import os
+
+import numpy as np
+import pytest
+
+import dohp_gb300 as dg
+import pyoracle as po
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+E0, NU = 1.0, 0.3
+LAM, MU = E0 * NU / ((1 + NU) * (1 - 2 * NU)), E0 / (2 * (1 + NU))
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import subprocess, sys
+    subprocess.run([sys.executable, os.path.join(os.path.dirname(dg.__file__), "build.py")], check=True)
+    dg.lib()
+
+
+def cycle(fs, g, qfun, use_v=False, use_dv=True):
+    it = dg.RulesetIterator(fs)
+    it.start(torch.as_tensor(g, device="cuda"))
+    a = it.get()
+    qfun(a)
+    it.commit(dg.INSERT_VALUES, use_v, use_dv)
+    y = torch.zeros(fs.n * fs.bs, dtype=torch.float64, device="cuda")
+    it.finish(y)
+    torch.cuda.synchronize()
+    return y.cpu().numpy(), it, a
+
+
+def poisson(a):
+    a["dv"].copy_(a["jw"][:, None, None] * a["du"])
+
+
+@pytest.mark.parametrize("p", [1, 2, 4, 7])
+def test_poisson_qfunction_matches_operator_and_oracle(p):
+    npoints = (4, 5, 4)
+    fs = dg.FS(npoints, degree=p, perturb=0.1, seed=p)
+    o = po.FS(*npoints, degree=p, perturb=0.1, seed=p)
+    g = np.random.default_rng(p).uniform(-1, 1, fs.n)
+    y, _, _ = cycle(fs, g, poisson)
+    yo = o.apply(g)
+    assert np.linalg.norm(y - yo) / np.linalg.norm(yo) < 1e-12
+    yf = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
+    fs.operator().mult(torch.as_tensor(g, device="cuda"), yf)
+    torch.cuda.synchronize()
+    assert np.linalg.norm(y - yf.cpu().numpy()) / np.linalg.norm(yo) < 1e-13
+
+
+def test_elasticity_qfunction_matches_operator():
+    npoints = (4, 4, 3)
+    fs = dg.FS(npoints, degree=3, perturb=0.1, seed=3, bs=3)
+    o = po.FS(*npoints, degree=3, perturb=0.1, seed=3, bs=3)
+    g = np.random.default_rng(0).uniform(-1, 1, fs.n * 3)
+
+    def elast(a):  # ElastPointwiseFunction (src/fs/tests/elast.c): sigma = lam tr(eps) I + 2 mu eps
+        du = a["du"]
+        eps = 0.5 * (du + du.transpose(1, 2))
+        tr = eps.diagonal(dim1=1, dim2=2).sum(-1)
+        sig = LAM * tr[:, None, None] * torch.eye(3, dtype=du.dtype, device=du.device) + 2 * MU * eps
+        a["dv"].copy_(a["jw"][:, None, None] * sig)
+
+    y, _, _ = cycle(fs, g, elast)
+    yo = o.apply(g, kind=2, param=np.array([LAM, MU]))
+    assert np.linalg.norm(y - yo) / np.linalg.norm(yo) < 1e-12
+
+
+def test_energy_identities_mass_and_stiffness():
+    """g^T M g = sum jw u^2 and g^T A g = sum jw |grad u|^2 (restriction is E^T, homogeneous Dirichlet)."""
+    fs = dg.FS((5, 4, 4), degree=4, perturb=0.15, seed=9)
+    g = np.random.default_rng(3).standard_normal(fs.n)
+    mass = lambda a: a["v"].copy_(a["jw"][:, None] * a["u"])
+    y, _, a = cycle(fs, g, mass, use_v=True, use_dv=False)
+    e = float((a["jw"][:, None] * a["u"] ** 2).sum())
+    assert abs(g @ y - e) < 1e-12 * abs(e)
+    y, _, a = cycle(fs, g, poisson)
+    e = float((a["jw"][:, None, None] * a["du"] ** 2).sum())
+    assert abs(g @ y - e) < 1e-12 * abs(e)
+
+
+def test_coordinates_and_jacobian():
+    """x matches dFSGetQuadratureCoordinates; jw sums to the mesh volume (the box [0,1]^3)."""
+    fs = dg.FS((4, 4, 5), degree=3, perturb=0.1, seed=2)
+    _, _, a = cycle(fs, np.zeros(fs.n), poisson)
+    xq = torch.zeros(fs.nq * 3, dtype=torch.float64, device="cuda")
+    fs.qpt_coords(xq)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(a["x"].cpu().numpy().ravel(), xq.cpu().numpy(), rtol=0, atol=1e-14)
+    assert abs(float(a["jw"].sum()) - 1.0) < 1e-13
+    assert float(a["jw"].min()) > 0
+
+
+def test_restart_and_add_mode():
+    fs = dg.FS((4, 4, 4), degree=2, perturb=0.1, seed=4)
+    g = np.random.default_rng(4).uniform(-1, 1, fs.n)
+    y1, it, _ = cycle(fs, g, poisson)
+    y = torch.as_tensor(y1, device="cuda").clone()
+    it.start(torch.as_tensor(g, device="cuda"))
+    poisson(it.get())
+    it.commit()
+    it.finish(y, dg.ADD_VALUES)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(y.cpu().numpy(), 2 * y1, rtol=1e-15, atol=1e-15)
+
+
+def test_errors():
+    fs = dg.FS((3, 3, 3), degree=2, seed=1)
+    with pytest.raises(dg.DohpError):
+        dg.RulesetIterator(fs, method=dg.SPARSE)
+    it = dg.RulesetIterator(fs)
+    with pytest.raises(dg.DohpError):
+        it.get()
+    ed = np.random.default_rng(0).integers(2, 5, size=fs.nelem).astype(np.int32)
+    with pytest.raises(dg.DohpError):
+        dg.RulesetIterator(dg.FS((3, 3, 3), degree=2, seed=1, elem_degree=ed))
