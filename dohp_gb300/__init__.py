@@ -193,6 +193,17 @@ class Operator:
     def mult_host(self, x, y):
         chk(lib().dOperatorMultHost(self.h, ptr(x), ptr(y)))
 
+    def plap_stash(self, g, p, eps):
+        """dOperatorComputePLaplaceStash: the Jacobian at state g (device vector)."""
+        chk(lib().dOperatorComputePLaplaceStash(self.h, ptr(g), _dbl(p), _dbl(eps)))
+
+    def plap_function(self, g, p, eps, y):
+        """dOperatorPLaplaceFunction: y = N(g) (no forcing); the stash of g stays for the Jacobian."""
+        chk(lib().dOperatorPLaplaceFunction(self.h, ptr(g), _dbl(p), _dbl(eps), ptr(y)))
+
+    def get_qdata(self, out):
+        chk(lib().dOperatorGetQuadratureData(self.h, ptr(out)))
+
 
 class Mat:
     def __init__(self, fs):
@@ -208,6 +219,9 @@ class Mat:
         pa = None if param is None else np.asarray(param, np.float64)
         g = None if grf is None else np.ascontiguousarray(grf, np.float64)
         chk(lib().dFSAssembleQ1(self.fs.h, self.h, ctypes.c_int(kind), ptr(pa), ptr(g), ctypes.c_int(quirk)))
+
+    def assemble_plap(self, g, p, eps, quirk=1):
+        chk(lib().dFSAssembleQ1PLaplace(self.fs.h, self.h, ptr(g), _dbl(p), _dbl(eps), ctypes.c_int(quirk)))
 
     def csr_host(self):
         nr, nnz = _i32(), _i64()
@@ -232,6 +246,13 @@ class KSP:
     def __del__(self):
         if getattr(self, "h", None) and _lib is not None:
             _lib.dKSPDestroy(ctypes.byref(self.h))
+
+    def set_operators(self, op=None, pmat=None):
+        chk(lib().dKSPSetOperators(self.h, None if op is None else op.h, None if pmat is None else pmat.h))
+        if op is not None:
+            self.op = op
+        if pmat is not None:
+            self.pmat = pmat
 
     def solve(self, b, x, rtol=1e-8, maxit=1000):
         its, rn = _i32(), _dbl()
@@ -316,3 +337,20 @@ class RulesetIterator:
 
     def finish(self, y=None, imode=INSERT_VALUES):
         chk(lib().dRulesetIteratorFinish(self.h, ptr(y), ctypes.c_int(imode)))
+
+
+class dNewtonOptions(ctypes.Structure):
+    _fields_ = [("max_it", _i32), ("rtol", _dbl), ("atol", _dbl), ("lin_rtol", _dbl), ("lin_maxit", _i32),
+                ("reference_quirk", ctypes.c_int)]
+
+
+def plap_newton(op, pmat, ksp, b, u, p, eps, rtol=1e-8, atol=0.0, lin_rtol=1e-3, lin_maxit=500, max_it=30, quirk=1):
+    """dPLaplaceNewtonSolve: returns (steps, residual norms [steps+1], linear iterations [steps])."""
+    opt = dNewtonOptions(max_it, rtol, atol, lin_rtol, lin_maxit, quirk)
+    its = _i32()
+    fn = np.zeros(max_it + 1)
+    li = np.zeros(max_it, np.int32)
+    chk(lib().dPLaplaceNewtonSolve(op.h, pmat.h, ksp.h, ptr(b), ptr(u), _dbl(p), _dbl(eps), ctypes.byref(opt),
+                                   ctypes.byref(its), ptr(fn), ptr(li)))
+    k = its.value
+    return k, fn[:k + 1], li[:k]

@@ -12,7 +12,8 @@ using namespace dgb;
 dErr op_mult(_p_dOperator *op, const double *x, double *y);
 dErr op_compute_geometry(_p_dOperator *op);
 dErr q1_symbolic(_p_dFS *fs, _p_dMat *J);
-dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk);
+dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk, const double *dref, double pe, double eps);
+dErr plap_set_stash(_p_dOperator *op, const double *stash);
 dErr mat_mult(_p_dMat *J, const double *x, double *y, cudaStream_t s);
 void hp_plan_destroy(void *p);
 
@@ -268,6 +269,7 @@ dErr dOperatorDestroy(dOperator *op) {
   cudaFree(o->d_y32);
   cudaFree(o->d_hx);
   cudaFree(o->d_hy);
+  cudaFree(o->d_gbase);
   hp_plan_destroy(o->hp_plan);
   delete o;
   *op = nullptr;
@@ -288,12 +290,7 @@ dErr dOperatorSetQuadratureData(dOperator op, const dReal *qdata) {
     op->geo_valid = false;
     return 0;
   }
-  if (op->kind == dOP_PLAPLACE_JACOBIAN) {
-    if (!qdata) return set_error("p-Laplacian Jacobian needs its stash");
-    if (!op->d_stash) CUCHK(cudaMalloc(&op->d_stash, fs->nq * 4 * sizeof(double)));
-    CUCHK(cudaMemcpyAsync(op->d_stash, qdata, fs->nq * 4 * sizeof(double), cudaMemcpyDeviceToDevice, fs->stream));
-    return 0;
-  }
+  if (op->kind == dOP_PLAPLACE_JACOBIAN) return plap_set_stash(op, qdata);
   return set_error("operator kind %d takes no quadrature data", (int)op->kind);
 }
 
@@ -353,8 +350,9 @@ dErr dMatDestroy(dMat *J) {
 dErr dFSAssembleQ1(dFS fs, dMat J, dOperatorKind kind, const dReal *param, const dReal *grf, int reference_quirk) {
   (void)param;
   if (!fs || !J) return set_error("null argument");
+  if (kind == dOP_PLAPLACE_JACOBIAN) return set_error("the p-Laplacian Q1 matrix depends on the state: use dFSAssembleQ1PLaplace");
   if (kind != dOP_DIFFUSION) return set_error("Q1 assembly for operator kind %d not built yet", (int)kind);
-  return q1_numeric(fs, J, grf, reference_quirk);
+  return q1_numeric(fs, J, grf, reference_quirk, nullptr, 0, 0);
 }
 
 dErr dMatGetCSR(dMat J, dInt *nrows, int64_t *nnz, const dInt **rowptr, const dInt **col, const dScalar **val) {
@@ -475,12 +473,6 @@ dErr dFSEvaluateLognormal(dFS fs, const dReal *grf, dReal *kq) {
   if (!fs || !fs->setup) return set_error("dFS not set up");
   if (!grf) return set_error("null GRF");
   return qpt_fields(fs, grf, nullptr, kq);
-}
-
-dErr dOperatorComputePLaplaceStash(dOperator op, const dScalar *g, dReal p, dReal eps) {
-  (void)g, (void)p, (void)eps;
-  if (!op) return set_error("null operator");
-  return set_error("p-Laplacian stash not built yet");
 }
 
 }  // extern "C"

@@ -107,6 +107,7 @@ struct _p_dOperator {
   float *d_geo32 = nullptr;      // fp32 copy
   double *d_k = nullptr;         // coefficient per qpt
   double *d_stash = nullptr;     // p-Laplacian stash [nq][4]
+  double *d_gbase = nullptr;     // p-Laplacian: {J^-1, w det J} per qpt (10, SoA per element)
   double *d_yexp = nullptr;      // expanded output scratch
   float *d_x32 = nullptr, *d_y32 = nullptr;
   double *d_hx = nullptr, *d_hy = nullptr;  // device staging for the host-vector form

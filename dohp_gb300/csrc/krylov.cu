@@ -547,6 +547,24 @@ dErr dKSPSetOptions(dKSP ksp, dInt cheb_degree, dPrecision pc_precision, dInt re
   return 0;
 }
 
+dErr dKSPSetOperators(dKSP ksp, dOperator op, dMat pmat) {
+  if (!ksp) return set_error("null KSP");
+  if (op) {
+    if (op->fs->n * op->fs->bs != ksp->n) return set_error("operator size differs from the KSP's");
+    ksp->op = op;
+  }
+  if (pmat) {
+    if (pmat->nrows != ksp->n) return set_error("matrix size differs from the KSP's");
+    ksp->pmat = pmat;
+  }
+  ksp->pc_ready = false;
+  cudaFree(ksp->d_w32);
+  cudaFree(ksp->d_dinv32);
+  cudaFree(ksp->d_val32);
+  ksp->d_w32 = nullptr, ksp->d_dinv32 = nullptr, ksp->d_val32 = nullptr;
+  return 0;
+}
+
 dErr dKSPSolve(dKSP ksp, const dScalar *b, dScalar *x, dReal rtol, dInt maxit, dInt *its, dReal *rnorm) {
   if (!ksp) return set_error("null KSP");
   DCHK(ksp_alloc(ksp));

@@ -389,14 +389,9 @@ dErr launch_elasticity(_p_dFS *fs, const double *x, const T *geo, T lam, T mu, T
 }  // namespace
 
 // ----------------------------------------------------------------------------------------------------------
-dErr op_compute_geometry(_p_dOperator *op) {
-  _p_dFS *fs = op->fs;
-  const int mode = op->kind == dOP_ELASTICITY ? 1 : 0;
-  const int ncomp = mode ? 10 : 6;
-  if (op->geo_valid && op->geo_kind == mode) return 0;
-  cudaFree(op->d_geo);
-  op->d_geo = nullptr;
-  CUCHK(cudaMalloc(&op->d_geo, (size_t)fs->nq * ncomp * sizeof(double)));
+// geometric factors at the FAST points of every element into out (mode 0: 6 per point with coefficient kq,
+// mode 1: {J^-1, w det J}, 10 per point); a negative Jacobian anywhere is an error
+dErr geometry_fill(_p_dFS *fs, int mode, const double *kq, double *out) {
   RuleTab h[MAXP];
   for (int p = 1; p < MAXP; p++) gauss_rule(p + 1, h[p].x, h[p].w);
   RuleTab *d_rules;
@@ -404,14 +399,30 @@ dErr op_compute_geometry(_p_dOperator *op) {
   CUCHK(cudaMemcpyAsync(d_rules, h, sizeof h, cudaMemcpyHostToDevice, fs->stream));
   int zero = 0;
   CUCHK(cudaMemcpyToSymbolAsync(g_negative_jacobian, &zero, sizeof zero, 0, cudaMemcpyHostToDevice, fs->stream));
-  k_geometry<<<(unsigned)fs->nelem, 128, 0, fs->stream>>>(fs->nelem, fs->d_edeg, fs->d_qoff, fs->d_coords, d_rules,
-                                                          op->kind == dOP_DIFFUSION ? op->d_k : nullptr, mode, op->d_geo);
+  k_geometry<<<(unsigned)fs->nelem, 128, 0, fs->stream>>>(fs->nelem, fs->d_edeg, fs->d_qoff, fs->d_coords, d_rules, kq, mode, out);
   CUCHK(cudaGetLastError());
   int neg = 0;
   CUCHK(cudaMemcpyFromSymbolAsync(&neg, g_negative_jacobian, sizeof neg, 0, cudaMemcpyDeviceToHost, fs->stream));
   CUCHK(cudaStreamSynchronize(fs->stream));
   cudaFree(d_rules);
   if (neg) return set_error("Negative Jacobian in the element geometry");
+  return 0;
+}
+
+dErr op_compute_geometry(_p_dOperator *op) {
+  _p_dFS *fs = op->fs;
+  if (op->kind == dOP_PLAPLACE_JACOBIAN) {  // factors come from the stash (plap.cu)
+    if (op->geo_valid) return 0;
+    return set_error("p-Laplacian Jacobian has no stash: call dOperatorComputePLaplaceStash, dOperatorPLaplaceFunction "
+                     "or dOperatorSetQuadratureData first");
+  }
+  const int mode = op->kind == dOP_ELASTICITY ? 1 : 0;
+  const int ncomp = mode ? 10 : 6;
+  if (op->geo_valid && op->geo_kind == mode) return 0;
+  cudaFree(op->d_geo);
+  op->d_geo = nullptr;
+  CUCHK(cudaMalloc(&op->d_geo, (size_t)fs->nq * ncomp * sizeof(double)));
+  DCHK(geometry_fill(fs, mode, op->kind == dOP_DIFFUSION ? op->d_k : nullptr, op->d_geo));
   if (op->d_geo32) {
     cudaFree(op->d_geo32);
     op->d_geo32 = nullptr;
@@ -422,7 +433,7 @@ dErr op_compute_geometry(_p_dOperator *op) {
 }
 
 template <typename T>
-static dErr diffusion_apply_t(_p_dFS *fs, const double *x, const T *geo, T *yexp) {
+dErr diffusion_apply_t(_p_dFS *fs, const double *x, const T *geo, T *yexp) {
   if (!fs->uniform) return set_error("fused diffusion apply needs a uniform-degree space (hp path not built yet)");
   switch (fs->p + 1) {
     case 2: return launch_diffusion<2, T>(fs, x, geo, yexp);
@@ -461,6 +472,7 @@ dErr op_mult_expanded(_p_dOperator *op, const double *x, double *yexp) {
   DCHK(op_compute_geometry(op));
   if (op->kind == dOP_DIFFUSION) return diffusion_apply_t<double>(fs, x, op->d_geo, yexp);
   if (op->kind == dOP_ELASTICITY) return elasticity_apply_t<double>(fs, x, op->d_geo, op->lam, op->mu, yexp);
+  if (op->kind == dOP_PLAPLACE_JACOBIAN) return diffusion_apply_t<double>(fs, x, op->d_geo, yexp);  // G from the stash
   return set_error("operator kind %d not built yet", (int)op->kind);
 }
 
@@ -472,7 +484,7 @@ __global__ void k_to_float(int64_t n, const double *__restrict__ a, float *__res
 // FP32 element arithmetic (geometric factors rounded to FP32 once), FP64 input and FP64 restriction
 static dErr op_mult_fp32(_p_dOperator *op, const double *x, double *y) {
   _p_dFS *fs = op->fs;
-  if (op->kind != dOP_DIFFUSION && op->kind != dOP_ELASTICITY)
+  if (op->kind != dOP_DIFFUSION && op->kind != dOP_ELASTICITY && op->kind != dOP_PLAPLACE_JACOBIAN)
     return set_error("FP32 apply for operator kind %d not built yet", (int)op->kind);
   DCHK(op_compute_geometry(op));
   const int64_t ng = fs->nq * (op->kind == dOP_ELASTICITY ? 10 : 6);

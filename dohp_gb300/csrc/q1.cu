@@ -135,10 +135,14 @@ struct SparseRules {
 };
 
 // phase 1: one 64-thread group per patch computes the 8x8 patch matrix K[i][j] = sum_q w k dphi_i . dphi_j
+// p-Laplacian Jacobian (dref != NULL): the state's reference gradient at every SPARSE point, element-natural
+// per element (8 points per patch, elements back to back), gives the store of EllipPointwiseComputeStore
+// (ellip.c:333-342) at the patch point and K[i][j] = sum_q dphi_i . (w eta dphi_j - w (s . dphi_j) s)
+// (EllipPointwiseJacobian, ellip.c:369-377).
 __global__ void __launch_bounds__(256) k_q1_patch(int64_t nelem, const int32_t *edeg, const int64_t *pstart, const double *coords,
                                                   const SparseRules *rules, const double *grf, int quirk, int64_t npatch_total,
-                                                  double *K) {
-  __shared__ double sJ[4][8][9], sW[4][8], sDer[4][8][8][3];
+                                                  const double *dref, double pe, double eps, double *K) {
+  __shared__ double sJ[4][8][9], sW[4][8], sDer[4][8][8][3], sSt[4][8][4];
   const int g = threadIdx.x >> 6, lt = threadIdx.x & 63;
   const int64_t gp = (int64_t)blockIdx.x * 4 + g;
   const bool active = gp < npatch_total;
@@ -170,6 +174,16 @@ __global__ void __launch_bounds__(256) k_q1_patch(int64_t nelem, const int32_t *
     double w = rules->w[px][ai] * rules->w[py][aj] * rules->w[pz][ak] * det;
     if (grf) w *= exp(grf_eval_dev(grf, xo));
     sW[g][q] = w;
+    if (dref) {  // state gradient mapped by the inverse Jacobian of this point
+      const double *dr = dref + (pstart[e] * 8 + (int64_t)(ai * (2 * py) + aj) * (2 * pz) + ak) * 3;
+      double Du[3];
+      for (int c = 0; c < 3; c++) Du[c] = dr[0] * Ji[0 * 3 + c] + dr[1] * Ji[1 * 3 + c] + dr[2] * Ji[2 * 3 + c];
+      const double gamma = 0.5 * (Du[0] * Du[0] + Du[1] * Du[1] + Du[2] * Du[2]);
+      const double espg = eps * eps + gamma, eta = pow(espg, (pe - 2) / 2);
+      const double sm = sqrt(-((pe - 2) / 2) * eta / espg);
+      sSt[g][q][0] = eta;
+      for (int c = 0; c < 3; c++) sSt[g][q][1 + c] = sm * Du[c];
+    }
     if (quirk) {  // inverse Jacobian read at element-natural index pidx*8+q (efstopo.c:700)
       const int t = pidx * 8 + q, Qy = 2 * py, Qz = 2 * pz;
       const int ti = t / (Qy * Qz), tj = (t / Qz) % Qy, tk = t % Qz;
@@ -191,7 +205,16 @@ __global__ void __launch_bounds__(256) k_q1_patch(int64_t nelem, const int32_t *
     double s = 0;
     for (int q = 0; q < 8; q++) {
       const double w = sW[g][q];
-      const double dv0 = w * sDer[g][q][j][0], dv1 = w * sDer[g][q][j][1], dv2 = w * sDer[g][q][j][2];
+      double dv0, dv1, dv2;
+      if (dref) {
+        const double *st = sSt[g][q], *dj = sDer[g][q][j];
+        const double dotw = (st[1] * dj[0] + st[2] * dj[1] + st[3] * dj[2]) * w, etaw = st[0] * w;
+        dv0 = etaw * dj[0] - dotw * st[1];
+        dv1 = etaw * dj[1] - dotw * st[2];
+        dv2 = etaw * dj[2] - dotw * st[3];
+      } else {
+        dv0 = w * sDer[g][q][j][0], dv1 = w * sDer[g][q][j][1], dv2 = w * sDer[g][q][j][2];
+      }
       s += sDer[g][q][i][0] * dv0 + sDer[g][q][i][1] * dv1 + sDer[g][q][i][2] * dv2;
     }
     K[gp * 64 + lt] = s;
@@ -261,7 +284,7 @@ dErr q1_symbolic(_p_dFS *fs, _p_dMat *J) {
   return 0;
 }
 
-dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk) {
+dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk, const double *dref, double pe, double eps) {
   std::vector<int64_t> pstart(fs->nelem + 1, 0);
   for (int64_t e = 0; e < fs->nelem; e++)
     pstart[e + 1] = pstart[e] + (int64_t)fs->edeg[3 * e] * fs->edeg[3 * e + 1] * fs->edeg[3 * e + 2];
@@ -282,7 +305,7 @@ dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk) {
     CUCHK(cudaMemcpyAsync(d_grf, grf_host, (3 + 4 * nf) * sizeof(double), cudaMemcpyHostToDevice, fs->stream));
   }
   if (np) {
-    k_q1_patch<<<(unsigned)((np + 3) / 4), 256, 0, fs->stream>>>(fs->nelem, fs->d_edeg, d_pstart, fs->d_coords, d_rules, d_grf, quirk, np, d_K);
+    k_q1_patch<<<(unsigned)((np + 3) / 4), 256, 0, fs->stream>>>(fs->nelem, fs->d_edeg, d_pstart, fs->d_coords, d_rules, d_grf, quirk, np, dref, pe, eps, d_K);
     CUCHK(cudaGetLastError());
   }
   if (fs->n) {

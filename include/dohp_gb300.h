@@ -143,8 +143,15 @@ dErr dOperatorDestroy(dOperator *op);
 /* per-quadrature-point data: dOP_DIFFUSION coefficient k [nq] (NULL: k = 1); dOP_PLAPLACE_JACOBIAN stash
  * [nq][4] = {eta, sqrt(-eta') du} (ellip.c:119-123). Device pointer, copied into the operator. */
 dErr dOperatorSetQuadratureData(dOperator op, const dReal *qdata);
-/* p-Laplacian stash from the state g (EllipPointwiseComputeStore, ellip.c:333-342), exponent p, eps */
+/* p-Laplacian stash from the state g (EllipPointwiseComputeStore, ellip.c:333-342), exponent p, eps: the store
+ * [nq][4] at every FAST point and the Jacobian's coefficients, so that dOperatorMult then applies
+ * EllipShellMatMult (ellip.c:442-472) at g. g is expanded dFS_INHOMOGENEOUS (as EllipFunction does). */
 dErr dOperatorComputePLaplaceStash(dOperator op, const dScalar *g, dReal p, dReal eps);
+/* EllipFunction (ellip.c:407-440) without the forcing term, lambda = 0: y = sum_e E^T B^T (w eta Du) at the
+ * state g; also leaves the stash of g in place (the next dOperatorMult is the Jacobian at g). */
+dErr dOperatorPLaplaceFunction(dOperator op, const dScalar *g, dReal p, dReal eps, dScalar *y);
+/* copy out the per-point data: dOP_DIFFUSION coefficient [nq], dOP_PLAPLACE_JACOBIAN stash [nq][4] (device) */
+dErr dOperatorGetQuadratureData(dOperator op, dReal *qdata);
 dErr dOperatorSetPrecision(dOperator op, dPrecision prec);
 dErr dOperatorSetLaunchMode(dOperator op, dLaunchMode mode);
 /* measure tile shapes (elements per block x threads) per order bucket on the next apply; cache_path (may be
@@ -193,6 +200,9 @@ dErr dMatDestroy(dMat *J);
  * dFSMatSetValuesBlockedExpanded (fs.c:826-930). kind/param as dFSCreateOperator; coefficient: k at the
  * SPARSE points (NULL: k = 1), reference_quirk = 1 reproduces the reference's inverse-Jacobian indexing. */
 dErr dFSAssembleQ1(dFS fs, dMat J, dOperatorKind kind, const dReal *param, const dReal *grf, int reference_quirk);
+/* EllipJacobian (ellip.c:474-536): the Q1-embedded p-Laplacian Jacobian at the state g (device vector),
+ * store at every SPARSE point from the state's gradient there; scalar uniform-order spaces */
+dErr dFSAssembleQ1PLaplace(dFS fs, dMat J, const dScalar *g, dReal p, dReal eps, int reference_quirk);
 dErr dMatGetCSR(dMat J, dInt *nrows, int64_t *nnz, const dInt **rowptr, const dInt **col, const dScalar **val);
 dErr dMatMult(dMat J, const dScalar *x, dScalar *y);
 /* host copies of the CSR arrays (rowptr nrows+1, col nnz, val nnz) */
@@ -206,6 +216,24 @@ dErr dKSPDestroy(dKSP *ksp);
 /* Chebyshev-Jacobi degree on the Q1 matrix, inner precision, restart length */
 dErr dKSPSetOptions(dKSP ksp, dInt cheb_degree, dPrecision pc_precision, dInt restart);
 dErr dKSPSolve(dKSP ksp, const dScalar *b, dScalar *x, dReal rtol, dInt maxit, dInt *its, dReal *rnorm);
+/* ---------------------------------------------------------------- Newton (p-Laplacian) */
+/* Newton-Krylov for N(u) = b with N the p-Laplacian function (dOperatorPLaplaceFunction): the SNES side of
+ * ellip.c (SNESSetFunction/SNESSetJacobian, ellip.c:697-704; PETSc SNES is not part of this library).
+ * Each step re-assembles the Q1 Jacobian into Jp at u (dFSAssembleQ1PLaplace), solves with ksp (operator
+ * op = the matrix-free Jacobian at u; FGMRES with FP32 inner applies gives the mixed-precision form),
+ * and backtracks on ||F||. fnorm receives max_it+1 residual norms, lin_its max_it iteration counts. */
+typedef struct {
+  dInt max_it;
+  dReal rtol, atol;   /* stop when ||F|| <= rtol ||F0|| or ||F|| <= atol */
+  dReal lin_rtol;     /* linear solve tolerance per Newton step */
+  dInt lin_maxit;
+  int reference_quirk; /* Q1 assembly quirk (dFSAssembleQ1) */
+} dNewtonOptions;
+dErr dPLaplaceNewtonSolve(dOperator op, dMat Jp, dKSP ksp, const dScalar *b, dScalar *u, dReal p, dReal eps,
+                          const dNewtonOptions *opt, dInt *its, dReal *fnorm, dInt *lin_its);
+/* KSPSetOperators: new operator and/or preconditioning matrix (NULL keeps the current one); the
+ * preconditioner is set up again on the next solve (a Newton step that re-assembled the Q1 matrix) */
+dErr dKSPSetOperators(dKSP ksp, dOperator op, dMat pmat);
 
 /* ---------------------------------------------------------------- lognormal coefficient */
 /* g(x) = sqrt(2 var / nf) sum_f cos(w_f . x + b_f), random Fourier features of the squared-exponential

@@ -1286,20 +1286,35 @@ static int cmp_pair(const void *a, const void *b)
   return (x > y) - (x < y);
 }
 
-int64_t or_q1_assemble(const or_fs *m, int kind, const double *param, const double *grf, int quirk,
-                       int32_t *rowptr, int32_t **colp, double **valp)
+/* EllipJacobian (ellip.c:474-536) on the SPARSE ruleset: the state's gradient at every SPARSE point comes from
+ * GetPatchApplied (element GRAD with the point's own inverse Jacobian, then patch order), the store from
+ * EllipPointwiseComputeStore, and the patch matrix from EllipPointwiseJacobian with the Q1 patch bases. */
+static int64_t q1_assemble(const or_fs *m, int kind, const double *param, const double *grf, int quirk,
+                           const double *state, int32_t *rowptr, int32_t **colp, double **valp)
 {
   const int bs = m->bs;
-  if (kind == 1) return or_fail("p-Laplacian Q1 assembly needs the state; not provided");
+  if (kind == 1 && (!state || bs != 1)) return or_fail("p-Laplacian Q1 assembly needs a scalar space and the state");
   const int64_t nrows = m->n * bs;
   rowlist *rows = calloc(nrows, sizeof(rowlist));
   basis1d B[11];
   for (int p = 1; p <= 10; p++) if (basis_for(1, p, &B[p])) return -1;
+  double *sexp = NULL;
+  if (kind == 1) {
+    sexp = malloc(sizeof(double) * m->nexp);
+    or_fs_global_to_expanded(m, state, NULL, sexp);
+  }
   for (int64_t r = 0; r < m->nr; r++) {
     const basis1d *b[3] = {&B[m->edeg[3 * r]], &B[m->edeg[3 * r + 1]], &B[m->edeg[3 * r + 2]]};
     const int Q[3] = {b[0]->Q, b[1]->Q, b[2]->Q}, nq = Q[0] * Q[1] * Q[2];
     double *xq = malloc(sizeof(double) * 3 * nq), *cjinv = malloc(sizeof(double) * 9 * nq), *jwe = malloc(sizeof(double) * nq);
     if (element_geometry(m, r, b, xq, cjinv, jwe)) return -1;
+    double *sdu = NULL;
+    if (kind == 1) {
+      const int P[3] = {b[0]->P, b[1]->P, b[2]->P};
+      const double *bi[3] = {b[0]->interp, b[1]->interp, b[2]->interp}, *bd[3] = {b[0]->deriv, b[1]->deriv, b[2]->deriv};
+      sdu = malloc(sizeof(double) * 3 * nq);
+      or_efs_apply_hex(P, Q, bi, bd, cjinv, 1, sexp + m->xstart[r], sdu, OR_GRAD, OR_INSERT);
+    }
     int *ind = malloc(sizeof(int) * nq), psz;
     double *pw = malloc(sizeof(double) * nq);
     const int np = or_rule_patches(1, Q, b[0]->w, b[1]->w, b[2]->w, &psz, ind, pw);
@@ -1318,7 +1333,18 @@ int64_t or_q1_assemble(const or_fs *m, int kind, const double *param, const doub
         const int eq = ind[pt * 8 + q];
         const double w = jwe[eq];
         const double *I = interp + (pt * 8 + q) * 8, *Dd = deriv + (pt * 8 + q) * 24;
-        if (bs == 1) {
+        if (kind == 1) {
+          const double *Du = sdu + 3 * eq, pe = param[0], eps = param[1];
+          const double gamma = 0.5 * (Du[0] * Du[0] + Du[1] * Du[1] + Du[2] * Du[2]);
+          const double espg = eps * eps + gamma, eta = pow(espg, (pe - 2) / 2);
+          const double sm = sqrt(-((pe - 2) / 2) * eta / espg);
+          const double st[4] = {eta, sm * Du[0], sm * Du[1], sm * Du[2]};
+          for (int j = 0; j < 8; j++) {
+            double v, dv[3], uu = I[j];
+            qfunction(1, 1, st, param, w, &uu, Dd + 3 * j, &v, dv);
+            for (int i = 0; i < 8; i++) K[i][j] += I[i] * v + Dd[3 * i] * dv[0] + Dd[3 * i + 1] * dv[1] + Dd[3 * i + 2] * dv[2];
+          }
+        } else if (bs == 1) {
           double qd = grf ? exp(or_grf_eval(grf, xq + 3 * eq)) : 1.0;
           for (int j = 0; j < 8; j++) {
             double v, dv[3], uu = I[j];
@@ -1349,8 +1375,9 @@ int64_t or_q1_assemble(const or_fs *m, int kind, const double *param, const doub
           }
       }
     }
-    free(xq); free(cjinv); free(jwe); free(ind); free(pw); free(eidx); free(interp); free(deriv); free(pjinv);
+    free(xq); free(cjinv); free(jwe); free(ind); free(pw); free(eidx); free(interp); free(deriv); free(pjinv); free(sdu);
   }
+  free(sexp);
   int64_t nnz = 0;
   for (int64_t i = 0; i < nrows; i++) nnz += rows[i].n;
   int32_t *col = malloc(sizeof(int32_t) * (nnz ? nnz : 1));
@@ -1369,6 +1396,20 @@ int64_t or_q1_assemble(const or_fs *m, int kind, const double *param, const doub
   *colp = col;
   *valp = val;
   return nnz;
+}
+
+int64_t or_q1_assemble(const or_fs *m, int kind, const double *param, const double *grf, int quirk,
+                       int32_t *rowptr, int32_t **colp, double **valp)
+{
+  if (kind == 1) return or_fail("p-Laplacian Q1 assembly needs the state: use or_q1_assemble_plap");
+  return q1_assemble(m, kind, param, grf, quirk, NULL, rowptr, colp, valp);
+}
+
+int64_t or_q1_assemble_plap(const or_fs *m, double p, double eps, const double *g, int quirk,
+                            int32_t *rowptr, int32_t **colp, double **valp)
+{
+  const double param[2] = {p, eps};
+  return q1_assemble(m, 1, param, NULL, quirk, g, rowptr, colp, valp);
 }
 
 /* ----------------------------------------------------------------------------------------------

@@ -110,6 +110,10 @@ int or_plap_stash(const or_fs *fs, double p, double eps, const double *g, double
  * Returns nnz; rowptr has n*bs+1 entries (caller-allocated), col/val are malloc'd (free with or_free). */
 int64_t or_q1_assemble(const or_fs *fs, int kind, const double *param, const double *grf, int quirk,
                        int32_t *rowptr, int32_t **col, double **val);
+/* p-Laplacian Jacobian at the state g (homogeneous Dirichlet), exponent p, regularisation eps:
+ * EllipJacobian (ellip.c:474-536), store at every SPARSE point (ellip.c:333-342). */
+int64_t or_q1_assemble_plap(const or_fs *fs, double p, double eps, const double *g, int quirk,
+                            int32_t *rowptr, int32_t **col, double **val);
 void or_free(void *p);
 
 /* Lognormal coefficient field: g(x) = sqrt(2 var / nf) sum_f cos(w_f . x + b_f) (random Fourier
