@@ -37,6 +37,11 @@ E0, NU = 1.0, 0.3
 FP64_PEAK_GFLOPS = 1203.0  # FP64 FMA issue rate measured on this GB300 (FMA-chain probe)
 
 
+def _plain(o):
+    """JSON fallback for numpy scalars."""
+    return o.item() if hasattr(o, "item") else str(o)
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -46,6 +51,8 @@ def parse():
     ap.add_argument("--config", default="cfg2", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--secondary", default="all", help="comma list of apply,solve,newton (or all)")
+    ap.add_argument("--newton-ne", type=int, default=24, help="elements per side of the p-Laplacian Newton run")
     return ap.parse_args()
 
 
@@ -238,6 +245,98 @@ def secondary_cfg4(args):
             "fp64_frac_of_peak": issued / (kms * 1e-3) / 1e9 / FP64_PEAK_GFLOPS, "dtype": "f64"}
 
 
+def secondary_newton(args):
+    """p-Laplacian Newton-Krylov (exponent 1.5, eps 1e-6, 48^3, p=6, f ~ U[-1,1] per dof): FP64 inner applies vs
+    FP32 inner applies inside FGMRES (FP64 residuals and orthogonalisation). Per Newton step: ||F||, FGMRES
+    iterations, and the relative error of the mixed run's iterate and of its FP32 Jacobian apply against the
+    FP64 run (the FP64 path is the one pinned to the oracle)."""
+    import numpy as np
+    import torch
+    import dohp_gb300 as dg
+    ne, p, pe, eps = args.newton_ne, 6, 1.5, 1e-6
+    fs = dg.FS((ne + 1,) * 3, degree=p, perturb=0.1, seed=1)
+    b = torch.as_tensor(np.random.default_rng(0).uniform(-1, 1, fs.n), device="cuda")
+    out = {"workload": "plaplace-newton-%d^3-p6: exponent 1.5, eps 1e-6 (the 48^3 shape with --newton-ne 48)" % ne,
+           "dofs": fs.n, "rtol": 1e-8, "lin_rtol": 1e-3, "lin_maxit": 300,
+           "ksp": "FGMRES(30) + Chebyshev(3)-Jacobi on the Q1-embedded Jacobian, inexact steps at lin_maxit"}
+    runs = {}
+    for name, prec in (("fp64", dg.dPREC_FP64), ("fp32", dg.dPREC_FP32)):
+        op = fs.operator(dg.dOP_PLAPLACE_JACOBIAN)
+        m = fs.matrix()
+        ksp = dg.KSP(op, m, ksp_type=dg.dKSP_FGMRES, inner_prec=prec, restart=30)
+        u = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
+        runs[name] = dict(op=op, m=m, ksp=ksp, u=u, wall=0.0, fnorm=[], its=[], done=False)
+    # both runs advance one Newton step at a time so that every iterate can be compared
+    per = []
+    for k in range(30):
+        for name, r in runs.items():
+            if r["done"]:
+                continue
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            _, fn, li = dg.plap_newton(r["op"], r["m"], r["ksp"], b, r["u"], pe, eps, rtol=0.0, lin_rtol=1e-3, lin_maxit=300,
+                                       max_it=1)
+            torch.cuda.synchronize()
+            r["wall"] += time.perf_counter() - t0
+            if not r["fnorm"]:
+                r["fnorm"].append(float(fn[0]))
+            r["fnorm"].append(float(fn[1]))
+            r["its"].append(int(li[0]))
+            r["done"] = bool(fn[1] <= 1e-8 * r["fnorm"][0])
+        r64, r32 = runs["fp64"], runs["fp32"]
+        if len(r64["its"]) == len(r32["its"]) == k + 1:
+            op = r32["op"]
+            op.plap_stash(r32["u"], pe, eps)
+            d = torch.as_tensor(np.random.default_rng(k).uniform(-1, 1, fs.n), device="cuda")
+            y64, y32 = torch.empty_like(d), torch.empty_like(d)
+            op.set_precision(dg.dPREC_FP64)
+            op.mult(d, y64)
+            op.set_precision(dg.dPREC_FP32)
+            op.mult(d, y32)
+            op.set_precision(dg.dPREC_FP64)
+            per.append({"step": k + 1,
+                        "iterate_rel_err": float(torch.linalg.norm(r32["u"] - r64["u"]) / torch.linalg.norm(r64["u"])),
+                        "fp32_jacobian_apply_rel_err": float(torch.linalg.norm(y32 - y64) / torch.linalg.norm(y64))})
+        if r64["done"] and r32["done"]:
+            break
+    for name, r in runs.items():
+        out[name] = {"newton_steps": len(r["its"]), "fnorm": r["fnorm"], "fgmres_its": r["its"], "wall_s": r["wall"],
+                     "converged": r["done"]}
+    out["per_step_vs_fp64"] = per
+    return out
+
+
+def secondary_solve_cfg4(args):
+    """time to rtol 1e-8 on the lognormal Poisson problem (64^3, p=4): FGMRES with FP64 inner applies vs FP32
+    inner applies (operator and Chebyshev-Jacobi on the Q1 matrix), same right-hand side U[-1,1]."""
+    import numpy as np
+    import torch
+    import dohp_gb300 as dg
+    cfg = CONFIGS["cfg4"]
+    stream = torch.cuda.current_stream()
+    fs, op, _, _ = setup(cfg, stream)
+    m = fs.matrix()
+    m.assemble(grf=dg.grf_create(64, 2.0, 0.1, 2))
+    b = torch.as_tensor(np.random.default_rng(1).uniform(-1, 1, fs.n), device="cuda")
+    out = {"workload": cfg["label"] + ", FGMRES(30), Chebyshev(3)-Jacobi Q1", "rtol": 1e-8}
+    for name, prec in (("fp64", dg.dPREC_FP64), ("fp32_inner", dg.dPREC_FP32)):
+        ksp = dg.KSP(op, m, ksp_type=dg.dKSP_FGMRES, inner_prec=prec, restart=30)
+        x = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
+        ksp.solve(b, x, rtol=1e-1, maxit=200)  # set-up (power iteration, FP32 copies) outside the timed solve
+        x.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        its, rn = ksp.solve(b, x, rtol=1e-8, maxit=2000)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        r = torch.empty_like(x)
+        op.mult(x, r)
+        true_rel = float(torch.linalg.norm(b - r) / torch.linalg.norm(b))
+        out[name] = {"its": its, "wall_s": wall, "true_rel_residual": true_rel}
+    out["speedup_fp32_inner"] = out["fp64"]["wall_s"] / out["fp32_inner"]["wall_s"]
+    return out
+
+
 def main():
     args = parse()
     cfg = CONFIGS[args.config]
@@ -347,10 +446,18 @@ def main():
     if not args.no_secondary and args.config == "cfg2":
         del fs, op, x, y, yexp
         torch.cuda.empty_cache()
-        line["secondary"] = secondary_cfg4(args)
+        which = {"apply", "solve", "newton"} if args.secondary == "all" else set(args.secondary.split(","))
+        if "apply" in which:
+            line["secondary"] = secondary_cfg4(args)
+        if "solve" in which:
+            line["solve_time_to_rtol"] = secondary_solve_cfg4(args)
+            torch.cuda.empty_cache()
+        if "newton" in which:
+            line["newton_mixed_precision"] = secondary_newton(args)
+            torch.cuda.empty_cache()
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(cfg, os.cpu_count() or 1)
-    print(json.dumps(line))
+    print(json.dumps(line, default=_plain))
     if dist:
         dist.destroy_process_group()
 

@@ -405,7 +405,6 @@ static dErr cg_solve(_p_dKSP *k, const double *b, double *x, double rtol, int ma
   }
   CUCHK(cudaGetLastError());
   *rnorm = sqrt(rr) / bn;
-  if (!(sqrt(rr) <= rtol * bn)) return set_error("CG did not converge in %d iterations (relative residual %g)", maxit, *rnorm);
   return 0;
 }
 
@@ -489,7 +488,6 @@ static dErr fgmres_solve(_p_dKSP *k, const double *b, double *x, double rtol, in
   }
   *its = total;
   *rnorm = res;
-  if (res > rtol) return set_error("FGMRES did not converge in %d iterations (relative residual %g)", maxit, res);
   return 0;
 }
 
@@ -565,7 +563,10 @@ dErr dKSPSetOperators(dKSP ksp, dOperator op, dMat pmat) {
   return 0;
 }
 
-dErr dKSPSolve(dKSP ksp, const dScalar *b, dScalar *x, dReal rtol, dInt maxit, dInt *its, dReal *rnorm) {
+}  // extern "C"
+
+// solve without treating the iteration limit as an error (inexact Newton steps); rnorm = ||b - A x|| / ||b||
+dErr ksp_solve(dKSP ksp, const double *b, double *x, double rtol, int maxit, int *its, double *rnorm) {
   if (!ksp) return set_error("null KSP");
   DCHK(ksp_alloc(ksp));
   DCHK(pc_setup(ksp));
@@ -575,6 +576,19 @@ dErr dKSPSolve(dKSP ksp, const dScalar *b, dScalar *x, dReal rtol, dInt maxit, d
   if (its) *its = it;
   if (rnorm) *rnorm = rn;
   return e;
+}
+
+extern "C" {
+
+dErr dKSPSolve(dKSP ksp, const dScalar *b, dScalar *x, dReal rtol, dInt maxit, dInt *its, dReal *rnorm) {
+  int it = 0;
+  double rn = 0;
+  DCHK(ksp_solve(ksp, b, x, rtol, maxit, &it, &rn));
+  if (its) *its = it;
+  if (rnorm) *rnorm = rn;
+  if (!(rn <= rtol))
+    return set_error("%s did not converge in %d iterations (relative residual %g)", ksp->type == dKSP_FGMRES ? "FGMRES" : "CG", it, rn);
+  return 0;
 }
 
 }  // extern "C"
