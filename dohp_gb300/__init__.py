@@ -354,3 +354,91 @@ def plap_newton(op, pmat, ksp, b, u, p, eps, rtol=1e-8, atol=0.0, lin_rtol=1e-3,
                                    ctypes.byref(its), ptr(fn), ptr(li)))
     k = its.value
     return k, fn[:k + 1], li[:k]
+
+
+class Learned:
+    """dLearned: learned coarse correction (U-Net on the vertex lattice) for FGMRES."""
+
+    def __init__(self, fs, seed=0):
+        self.fs = fs
+        self.h = _vp()
+        chk(lib().dLearnedCreate(fs.h, ctypes.c_uint64(seed), ctypes.byref(self.h)))
+        d = np.zeros(3, np.int32)
+        npar, npairs = _i64(), _i64()
+        chk(lib().dLearnedGetSizes(self.h, ptr(d), ctypes.byref(npar), ctypes.byref(npairs)))
+        self.dims, self.nparam = tuple(int(v) for v in d), npar.value
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.dLearnedDestroy(ctypes.byref(self.h))
+
+    @property
+    def npairs(self):
+        npairs = _i64()
+        chk(lib().dLearnedGetSizes(self.h, None, None, ctypes.byref(npairs)))
+        return npairs.value
+
+    def set_field(self, grf=None):
+        g = None if grf is None else np.ascontiguousarray(grf, np.float64)
+        chk(lib().dLearnedSetField(self.h, ptr(g)))
+
+    def collect(self, ksp, b, rtol=1e-10, maxit=5000, every=1, max_pairs=100):
+        n = _i32()
+        chk(lib().dLearnedCollectPairs(self.h, ksp.h, ptr(b), _dbl(rtol), _i32(maxit), _i32(every), _i32(max_pairs),
+                                       ctypes.byref(n)))
+        return n.value
+
+    def train(self, epochs, batch=8, lr=1e-3, seed=0):
+        losses = np.zeros(epochs)
+        chk(lib().dLearnedTrain(self.h, _i32(epochs), _i32(batch), _dbl(lr), ctypes.c_uint64(seed), ptr(losses)))
+        return losses
+
+    def apply(self, r, z):
+        chk(lib().dLearnedApply(self.h, ptr(r), ptr(z)))
+
+    def forward(self, x, y):
+        chk(lib().dLearnedForward(self.h, _i32(x.shape[0]), ptr(x), ptr(y)))
+
+    def loss_grad(self, x, t, grad):
+        lv = _dbl()
+        chk(lib().dLearnedLossGrad(self.h, _i32(x.shape[0]), ptr(x), ptr(t), ctypes.byref(lv), ptr(grad)))
+        return lv.value
+
+    def get_weights(self):
+        w = np.zeros(self.nparam, np.float32)
+        chk(lib().dLearnedGetWeights(self.h, ptr(w)))
+        return w
+
+    def set_weights(self, w, target_scale=0.0):
+        chk(lib().dLearnedSetWeights(self.h, ptr(np.ascontiguousarray(w, np.float32)), _dbl(target_scale)))
+
+    def scale(self):
+        v = _dbl()
+        chk(lib().dLearnedGetScale(self.h, ctypes.byref(v)))
+        return v.value
+
+    def restrict(self, r, rc):
+        chk(lib().dLearnedRestrict(self.h, ptr(r), ptr(rc)))
+
+    def prolong(self, c, z):
+        chk(lib().dLearnedProlong(self.h, ptr(c), ptr(z)))
+
+    def stats(self):
+        a, d = _i64(), _i64()
+        chk(lib().dLearnedGetStats(self.h, ctypes.byref(a), ctypes.byref(d)))
+        return a.value, d.value
+
+
+def _ksp_set_learned(self, net):
+    chk(lib().dKSPSetLearnedCorrection(self.h, None if net is None else net.h))
+    self.net = net
+
+
+def _ksp_stats(self):
+    a, r, on = _i64(), _i64(), ctypes.c_int()
+    chk(lib().dKSPGetStats(self.h, ctypes.byref(a), ctypes.byref(r), ctypes.byref(on)))
+    return a.value, r.value, bool(on.value)
+
+
+KSP.set_learned = _ksp_set_learned
+KSP.stats = _ksp_stats

@@ -251,11 +251,31 @@ struct _p_dKSP {
   dPrecision inner_prec = dPREC_FP64;  // precision of the operator applies inside an FGMRES cycle
   double *d_V = nullptr, *d_Z = nullptr, *d_h = nullptr;  // FGMRES bases [(m+1) x n], [m x n], coefficients
   float *d_w32 = nullptr, *d_dinv32 = nullptr, *d_val32 = nullptr;  // FP32 Chebyshev workspace
-  // optional preconditioner correction applied after the Chebyshev step: z += corr(r) (learned correction)
+  // optional preconditioner correction applied after the Chebyshev step: z += corr(r) (learned correction,
+  // FGMRES only); dropped for the rest of a solve when a restart cycle with it fails to reduce the residual
   dErr (*correction)(void *ctx, const double *r, double *z) = nullptr;
   void *correction_ctx = nullptr;
+  bool correction_on = false;
   int64_t pc_applies = 0, correction_rejects = 0;
+  // optional per-iteration monitor (CG: after every iterate, with x and r)
+  dErr (*monitor)(void *ctx, int it, const double *x, const double *r) = nullptr;
+  void *monitor_ctx = nullptr;
 };
+
+dErr ksp_set_monitor(dKSP ksp, dErr (*fn)(void *, int, const double *, const double *), void *ctx) {
+  if (!ksp) return set_error("null KSP");
+  ksp->monitor = fn;
+  ksp->monitor_ctx = ctx;
+  return 0;
+}
+
+dErr ksp_set_correction(dKSP ksp, dErr (*fn)(void *, const double *, double *), void *ctx) {
+  if (!ksp) return set_error("null KSP");
+  if (fn && ksp->type != dKSP_FGMRES) return set_error("a learned correction needs FGMRES (it is not a fixed linear operator)");
+  ksp->correction = fn;
+  ksp->correction_ctx = ctx;
+  return 0;
+}
 
 static dErr ksp_alloc(_p_dKSP *k) {
   if (k->d_work) return 0;
@@ -333,10 +353,18 @@ static dErr pc_apply_fp32(_p_dKSP *k, const double *r, double *z) {
   return 0;
 }
 
+static dErr pc_apply_plain(_p_dKSP *k, const double *r, double *z);
+
 static dErr pc_apply(_p_dKSP *k, const double *r, double *z) {
+  k->pc_applies++;
+  DCHK(pc_apply_plain(k, r, z));
+  if (k->correction && k->correction_on) DCHK(k->correction(k->correction_ctx, r, z));
+  return 0;
+}
+
+static dErr pc_apply_plain(_p_dKSP *k, const double *r, double *z) {
   const int64_t n = k->n;
   cudaStream_t s = k->op->fs->stream;
-  k->pc_applies++;
   if (k->pc == dPC_CHEBYSHEV_Q1 && k->pc_prec == dPREC_FP32) return pc_apply_fp32(k, r, z);
   if (k->pc == dPC_NONE) {
     CUCHK(cudaMemcpyAsync(z, r, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -386,6 +414,7 @@ static dErr cg_solve(_p_dKSP *k, const double *b, double *x, double rtol, int ma
     *rnorm = sqrt(rr) / bn;
     return 0;
   }
+  if (k->monitor) DCHK(k->monitor(k->monitor_ctx, 0, x, r));
   DCHK(pc_apply(k, r, z));
   CUCHK(cudaMemcpyAsync(p, z, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
   DCHK(device_dot(n, r, z, k->d_part, S, s));
@@ -394,6 +423,7 @@ static dErr cg_solve(_p_dKSP *k, const double *b, double *x, double rtol, int ma
     DCHK(device_dot(n, p, q, k->d_part, S + 1, s));
     k_axpby<<<nb(n), 256, 0, s>>>(n, 1.0, S, S + 1, p, 1.0, x);
     k_axpby<<<nb(n), 256, 0, s>>>(n, -1.0, S, S + 1, q, 1.0, r);
+    if (k->monitor) DCHK(k->monitor(k->monitor_ctx, it + 1, x, r));
     DCHK(device_dot(n, r, r, k->d_part, S + 2, s));
     DCHK(read_scalar(S + 2, &rr, s));
     *its = it + 1;
@@ -430,7 +460,8 @@ static dErr fgmres_solve(_p_dKSP *k, const double *b, double *x, double rtol, in
   DCHK(read_scalar(k->d_s, &bb, s));
   const double bn = sqrt(bb) > 0 ? sqrt(bb) : 1.0;
   int total = 0;
-  double res = 0;
+  double res = 0, prev = -1;
+  k->correction_on = k->correction != nullptr;
   for (;;) {
     DCHK(op_mult_prec(k->op, x, V, dPREC_FP64));
     k_axpby<<<nb(n), 256, 0, s>>>(n, 1.0, nullptr, nullptr, b, -1.0, V);  // V0 = b - A x
@@ -440,6 +471,13 @@ static dErr fgmres_solve(_p_dKSP *k, const double *b, double *x, double rtol, in
     const double beta = sqrt(rr);
     res = beta / bn;
     if (!(beta > rtol * bn) || total >= maxit) break;
+    // the plain preconditioner judges the correction: a restart cycle that did not reduce the true
+    // residual by 10 % drops the correction for the rest of this solve
+    if (k->correction_on && prev > 0 && !(beta < 0.9 * prev)) {
+      k->correction_on = false;
+      k->correction_rejects++;
+    }
+    prev = beta;
     k_scale_into<<<nb(n), 256, 0, s>>>(n, V, nullptr, 1.0 / beta, V);
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
@@ -542,6 +580,14 @@ dErr dKSPSetOptions(dKSP ksp, dInt cheb_degree, dPrecision pc_precision, dInt re
   cudaFree(ksp->d_dinv32);
   cudaFree(ksp->d_val32);
   ksp->d_w32 = nullptr, ksp->d_dinv32 = nullptr, ksp->d_val32 = nullptr;
+  return 0;
+}
+
+dErr dKSPGetStats(dKSP ksp, int64_t *pc_applies, int64_t *correction_rejects, int *correction_active) {
+  if (!ksp) return set_error("null KSP");
+  if (pc_applies) *pc_applies = ksp->pc_applies;
+  if (correction_rejects) *correction_rejects = ksp->correction_rejects;
+  if (correction_active) *correction_active = ksp->correction_on;
   return 0;
 }
 

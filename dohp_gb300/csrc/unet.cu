@@ -1,0 +1,1114 @@
+// Learned coarse correction for the Q1-embedded Chebyshev-Jacobi preconditioner (no counterpart in the
+// reference; the preconditioner it augments is the one EllipJacobian assembles, ellip.c:474-536).
+//
+// A 3-level 3-D convolutional U-Net (16/32/64 channels, 3x3x3 kernels, BF16 weights, FP32 accumulation)
+// runs on the Q1 lattice of the mesh vertices, the coarsest level of the embedded Q1 hierarchy. Input
+// channels: the restricted residual R r (R = P^T, normalised by its RMS over interior vertices) and log k at
+// the vertices. Output: the error at the vertices, which P (trilinear interpolation of the vertex lattice
+// onto every GLL node, element by element) carries back to the global dofs: FGMRES uses
+// z = Chebyshev(r) + P N(R r). The smoother handles the high frequencies; the network supplies the coarse
+// correction that Chebyshev-Jacobi lacks.
+//
+// Training pairs (residual, error) come from the plain solver: a CG monitor records R r_k and x_k at the
+// vertices; once the solve has converged, the targets are x* - x_k at the vertices. Training is plain
+// minibatch Adam on the mean squared error over interior vertices, with hand-written forward and backward
+// kernels (direct convolutions, FP32 activations, deterministic two-stage weight-gradient sums).
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <random>
+
+#include "internal.h"
+
+using namespace dgb;
+
+dErr device_dot(int64_t n, const double *a, const double *b, double *part, double *out, cudaStream_t s);
+dErr ksp_set_monitor(dKSP ksp, dErr (*fn)(void *, int, const double *, const double *), void *ctx);
+dErr ksp_set_correction(dKSP ksp, dErr (*fn)(void *, const double *, double *), void *ctx);
+dErr ksp_solve(dKSP ksp, const double *b, double *x, double rtol, int maxit, int *its, double *rnorm);
+
+namespace {
+
+struct Dims {
+  int x, y, z;
+  __host__ __device__ int64_t n() const { return (int64_t)x * y * z; }
+};
+Dims coarsen(Dims d) { return {(d.x - 1) / 2 + 1, (d.y - 1) / 2 + 1, (d.z - 1) / 2 + 1}; }
+
+struct LayerDef {
+  int ci, co, stride, level_in;  // level of the layer's input grid
+};
+enum { C1A, C1B, D1, C2A, D2, C3A, C3B, U2, C2B, U1, C1C, OUT, NLAYER };
+// up blocks convolve on the coarse grid and then interpolate (U2: level 2 -> 1, U1: level 1 -> 0)
+constexpr LayerDef kLayer[NLAYER] = {{2, 16, 1, 0},  {16, 16, 1, 0}, {16, 32, 2, 0}, {32, 32, 1, 1},
+                                     {32, 64, 2, 1}, {64, 64, 1, 2}, {64, 64, 1, 2}, {64, 32, 1, 2},
+                                     {32, 32, 1, 1}, {32, 16, 1, 1}, {16, 16, 1, 0}, {16, 1, 1, 0}};
+
+// ------------------------------------------------------------------------------------------ kernels
+__device__ __forceinline__ void vox(int64_t r, Dims d, int &i, int &j, int &k) {
+  k = (int)(r % d.z);
+  const int64_t q = r / d.z;
+  j = (int)(q % d.y);
+  i = (int)(q / d.y);
+}
+
+// y = act(conv(x) + bias) [+ skip]; x [B][Ci][di], W [Co][Ci][27] (bf16), y [B][Co][dout]
+template <int CO_T>
+__global__ void __launch_bounds__(128) k_conv_fwd(int B, int Ci, int Co, Dims di, Dims dout, int stride, const float *__restrict__ x,
+                                                  const __nv_bfloat16 *__restrict__ W, const float *__restrict__ bias, int relu,
+                                                  float *__restrict__ y) {
+  constexpr int CK = 8;
+  __shared__ float sW[CO_T][CK][27];
+  const int64_t nvo = dout.n(), nvi = di.n();
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool active = t < (int64_t)B * nvo;
+  const int co0 = blockIdx.y * CO_T;
+  const int64_t b = active ? t / nvo : 0, r = active ? t % nvo : 0;
+  int ox, oy, oz;
+  vox(r, dout, ox, oy, oz);
+  float acc[CO_T];
+#pragma unroll
+  for (int c = 0; c < CO_T; c++) acc[c] = (co0 + c < Co) ? bias[co0 + c] : 0.f;
+  for (int ci0 = 0; ci0 < Ci; ci0 += CK) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < CO_T * CK * 27; i += blockDim.x) {
+      const int c = i / (CK * 27), rr = i % (CK * 27), k = rr / 27, tap = rr % 27;
+      sW[c][k][tap] = (co0 + c < Co && ci0 + k < Ci) ? __bfloat162float(W[((size_t)(co0 + c) * Ci + ci0 + k) * 27 + tap]) : 0.f;
+    }
+    __syncthreads();
+    if (!active) continue;
+    const int kmax = min(CK, Ci - ci0);
+    for (int k = 0; k < kmax; k++) {
+      const float *xc = x + ((size_t)b * Ci + ci0 + k) * nvi;
+      float xv[27];
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        const int ix = ox * stride + a - 1;
+#pragma unroll
+        for (int bb = 0; bb < 3; bb++) {
+          const int iy = oy * stride + bb - 1;
+#pragma unroll
+          for (int cc = 0; cc < 3; cc++) {
+            const int iz = oz * stride + cc - 1;
+            const bool in = ix >= 0 && ix < di.x && iy >= 0 && iy < di.y && iz >= 0 && iz < di.z;
+            xv[(a * 3 + bb) * 3 + cc] = in ? xc[((int64_t)ix * di.y + iy) * di.z + iz] : 0.f;
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < CO_T; c++) {
+        float s = acc[c];
+#pragma unroll
+        for (int tap = 0; tap < 27; tap++) s = fmaf(sW[c][k][tap], xv[tap], s);
+        acc[c] = s;
+      }
+    }
+  }
+  if (!active) return;
+#pragma unroll
+  for (int c = 0; c < CO_T; c++) {
+    if (co0 + c >= Co) break;
+    const float v = relu ? fmaxf(acc[c], 0.f) : acc[c];
+    y[((size_t)b * Co + co0 + c) * nvo + r] = v;
+  }
+}
+
+// gx (=, or += with accumulate) = conv^T(gy): gx[ci][u] = sum_{co, taps with s v + t - 1 = u} W[co][ci][t] gy[co][v]
+template <int CI_T>
+__global__ void __launch_bounds__(128) k_conv_bwd_data(int B, int Ci, int Co, Dims di, Dims dout, int stride,
+                                                       const float *__restrict__ gy, const __nv_bfloat16 *__restrict__ W,
+                                                       float *__restrict__ gx, int accumulate) {
+  constexpr int CK = 8;
+  __shared__ float sW[CK][CI_T][27];
+  const int64_t nvo = dout.n(), nvi = di.n();
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool active = t < (int64_t)B * nvi;
+  const int ci0 = blockIdx.y * CI_T;
+  const int64_t b = active ? t / nvi : 0, r = active ? t % nvi : 0;
+  int ix, iy, iz;
+  vox(r, di, ix, iy, iz);
+  float acc[CI_T];
+#pragma unroll
+  for (int c = 0; c < CI_T; c++) acc[c] = 0.f;
+  for (int co0 = 0; co0 < Co; co0 += CK) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < CK * CI_T * 27; i += blockDim.x) {
+      const int k = i / (CI_T * 27), rr = i % (CI_T * 27), c = rr / 27, tap = rr % 27;
+      sW[k][c][tap] = (co0 + k < Co && ci0 + c < Ci) ? __bfloat162float(W[((size_t)(co0 + k) * Ci + ci0 + c) * 27 + tap]) : 0.f;
+    }
+    __syncthreads();
+    if (!active) continue;
+    const int kmax = min(CK, Co - co0);
+    for (int k = 0; k < kmax; k++) {
+      const float *gc = gy + ((size_t)b * Co + co0 + k) * nvo;
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        const int nx = ix + 1 - a;
+        if (nx < 0 || nx % stride) continue;
+        const int vx = nx / stride;
+        if (vx >= dout.x) continue;
+#pragma unroll
+        for (int bb = 0; bb < 3; bb++) {
+          const int ny = iy + 1 - bb;
+          if (ny < 0 || ny % stride) continue;
+          const int vy = ny / stride;
+          if (vy >= dout.y) continue;
+#pragma unroll
+          for (int cc = 0; cc < 3; cc++) {
+            const int nz = iz + 1 - cc;
+            if (nz < 0 || nz % stride) continue;
+            const int vz = nz / stride;
+            if (vz >= dout.z) continue;
+            const float g = gc[((int64_t)vx * dout.y + vy) * dout.z + vz];
+            const int tap = (a * 3 + bb) * 3 + cc;
+#pragma unroll
+            for (int c = 0; c < CI_T; c++) acc[c] = fmaf(sW[k][c][tap], g, acc[c]);
+          }
+        }
+      }
+    }
+  }
+  if (!active) return;
+#pragma unroll
+  for (int c = 0; c < CI_T; c++) {
+    if (ci0 + c >= Ci) break;
+    float *o = gx + ((size_t)b * Ci + ci0 + c) * nvi + r;
+    *o = accumulate ? *o + acc[c] : acc[c];
+  }
+}
+
+// weight and bias gradient partial sums over a chunk of output voxels: one (co, ci) pair per block.
+// partial layout [chunk][Co*Ci*27 + Co]
+__global__ void __launch_bounds__(256) k_conv_bwd_weight(int B, int Ci, int Co, Dims di, Dims dout, int stride,
+                                                         const float *__restrict__ x, const float *__restrict__ gy, int64_t chunk,
+                                                         float *__restrict__ partial) {
+  __shared__ float red[28][257];
+  const int pair = blockIdx.x, co = pair / Ci, ci = pair % Ci;
+  const int64_t nvo = dout.n(), nvi = di.n(), total = (int64_t)B * nvo;
+  const int64_t v0 = blockIdx.y * chunk, v1 = min(total, v0 + chunk);
+  float acc[28];
+#pragma unroll
+  for (int i = 0; i < 28; i++) acc[i] = 0.f;
+  for (int64_t v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
+    const int64_t b = v / nvo, r = v % nvo;
+    const float g = gy[((size_t)b * Co + co) * nvo + r];
+    if (g == 0.f) continue;
+    int ox, oy, oz;
+    vox(r, dout, ox, oy, oz);
+    const float *xc = x + ((size_t)b * Ci + ci) * nvi;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      const int ix = ox * stride + a - 1;
+#pragma unroll
+      for (int bb = 0; bb < 3; bb++) {
+        const int iy = oy * stride + bb - 1;
+#pragma unroll
+        for (int cc = 0; cc < 3; cc++) {
+          const int iz = oz * stride + cc - 1;
+          const bool in = ix >= 0 && ix < di.x && iy >= 0 && iy < di.y && iz >= 0 && iz < di.z;
+          if (in) acc[(a * 3 + bb) * 3 + cc] = fmaf(g, xc[((int64_t)ix * di.y + iy) * di.z + iz], acc[(a * 3 + bb) * 3 + cc]);
+        }
+      }
+    }
+    acc[27] += g;
+  }
+#pragma unroll
+  for (int i = 0; i < 28; i++) red[i][threadIdx.x] = acc[i];
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int i = 0; i < 28; i++) red[i][threadIdx.x] += red[i][threadIdx.x + s];
+    __syncthreads();
+  }
+  const int64_t np = (int64_t)Co * Ci * 27 + Co;
+  float *pp = partial + blockIdx.y * np;
+  if (threadIdx.x < 27) pp[(int64_t)pair * 27 + threadIdx.x] = red[threadIdx.x][0];
+  if (threadIdx.x == 27 && ci == 0) pp[(int64_t)Co * Ci * 27 + co] = red[27][0];
+}
+
+// grad[p] = sum over chunks in order (deterministic)
+__global__ void k_sum_chunks(int64_t np, int nchunk, const float *__restrict__ partial, float *__restrict__ grad) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  float s = 0.f;
+  for (int c = 0; c < nchunk; c++) s += partial[(int64_t)c * np + p];
+  grad[p] = s;
+}
+
+// trilinear interpolation between vertex-centred grids (align corners): weight of coarse i at fine f
+__device__ __forceinline__ float tent(int f, int Lf, int i, int Lc) {
+  if (Lc == 1) return 1.f;
+  const double pos = (double)f * (Lc - 1) / (Lf - 1);
+  const double w = 1.0 - fabs(pos - i);
+  return w > 0 ? (float)w : 0.f;
+}
+
+__device__ __forceinline__ void lohi(int f, int Lf, int Lc, int &lo, float &fr) {
+  if (Lc == 1) {
+    lo = 0, fr = 0.f;
+    return;
+  }
+  const double pos = (double)f * (Lc - 1) / (Lf - 1);
+  lo = min((int)floor(pos), Lc - 2);
+  fr = (float)(pos - lo);
+}
+
+// out[B][C][df] = interp(in[B][C][dc]); add: out += skip
+__global__ void k_up_fwd(int BC, Dims dc, Dims df, const float *__restrict__ in, const float *__restrict__ skip, float *__restrict__ out) {
+  const int64_t nf = df.n(), t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)BC * nf) return;
+  const int64_t bc = t / nf, r = t % nf;
+  int fx, fy, fz, lx, ly, lz;
+  float ax, ay, az;
+  vox(r, df, fx, fy, fz);
+  lohi(fx, df.x, dc.x, lx, ax);
+  lohi(fy, df.y, dc.y, ly, ay);
+  lohi(fz, df.z, dc.z, lz, az);
+  const float *c = in + bc * dc.n();
+  float s = 0.f;
+  for (int a = 0; a < 2; a++) {
+    const float wa = a ? ax : 1.f - ax;
+    const int ix = min(lx + a, dc.x - 1);
+    for (int b = 0; b < 2; b++) {
+      const float wb = b ? ay : 1.f - ay;
+      const int iy = min(ly + b, dc.y - 1);
+      for (int cc = 0; cc < 2; cc++) {
+        const float wc = cc ? az : 1.f - az;
+        const int iz = min(lz + cc, dc.z - 1);
+        s += wa * wb * wc * c[((int64_t)ix * dc.y + iy) * dc.z + iz];
+      }
+    }
+  }
+  out[t] = skip ? s + skip[t] : s;
+}
+
+// adjoint of the interpolation, as a gather over the fine points in each coarse point's support
+__global__ void k_up_bwd(int BC, Dims dc, Dims df, const float *__restrict__ gf, float *__restrict__ gc) {
+  const int64_t nc = dc.n(), t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)BC * nc) return;
+  const int64_t bc = t / nc, r = t % nc;
+  int cx, cy, cz;
+  vox(r, dc, cx, cy, cz);
+  auto range = [](int i, int Lc, int Lf, int &f0, int &f1) {
+    if (Lc == 1) {
+      f0 = 0, f1 = Lf - 1;
+      return;
+    }
+    const double rr = (double)(Lf - 1) / (Lc - 1);
+    f0 = max(0, (int)floor((i - 1) * rr));
+    f1 = min(Lf - 1, (int)ceil((i + 1) * rr));
+  };
+  int x0, x1, y0, y1, z0, z1;
+  range(cx, dc.x, df.x, x0, x1);
+  range(cy, dc.y, df.y, y0, y1);
+  range(cz, dc.z, df.z, z0, z1);
+  const float *g = gf + bc * df.n();
+  float s = 0.f;
+  for (int fx = x0; fx <= x1; fx++) {
+    const float wx = tent(fx, df.x, cx, dc.x);
+    if (wx == 0.f) continue;
+    for (int fy = y0; fy <= y1; fy++) {
+      const float wy = tent(fy, df.y, cy, dc.y);
+      if (wy == 0.f) continue;
+      for (int fz = z0; fz <= z1; fz++) {
+        const float wz = tent(fz, df.z, cz, dc.z);
+        if (wz == 0.f) continue;
+        s += wx * wy * wz * g[((int64_t)fx * df.y + fy) * df.z + fz];
+      }
+    }
+  }
+  gc[t] = s;
+}
+
+__global__ void k_mask(int64_t n, const float *__restrict__ g, const float *__restrict__ act, float *__restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = act[i] > 0.f ? g[i] : 0.f;
+}
+
+__global__ void k_copy_f(int64_t n, const float *__restrict__ a, float *__restrict__ b) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = a[i];
+}
+
+// MSE over interior vertices: grad = 2 (y - t) / count, block partial sums of (y - t)^2
+__global__ void k_mse(int B, int64_t nv, const float *__restrict__ y, const float *__restrict__ tg, const uint8_t *__restrict__ mask,
+                      float inv_count, float *__restrict__ grad, double *__restrict__ part) {
+  __shared__ double red[256];
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double l = 0;
+  if (i < (int64_t)B * nv) {
+    const bool in = mask[i % nv];
+    const float d = in ? y[i] - tg[i] : 0.f;
+    grad[i] = 2.f * d * inv_count;
+    l = (double)d * d;
+  }
+  red[threadIdx.x] = l;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// partial sums of squares of the targets over interior vertices
+__global__ void k_masked_sumsq(int64_t total, int64_t nv, const float *__restrict__ t, const uint8_t *__restrict__ mask,
+                               double *__restrict__ part) {
+  __shared__ double red[256];
+  double l = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+    if (mask[i % nv]) l += (double)t[i] * t[i];
+  red[threadIdx.x] = l;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void k_adam(int64_t n, float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m, float *__restrict__ v,
+                       float lr, float b1, float b2, float eps, float bc1, float bc2, __nv_bfloat16 *__restrict__ wb) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi, vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi, v[i] = vi;
+  const float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+  w[i] = wi;
+  wb[i] = __float2bfloat16_rn(wi);
+}
+
+__global__ void k_to_bf16(int64_t n, const float *__restrict__ w, __nv_bfloat16 *__restrict__ wb) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) wb[i] = __float2bfloat16_rn(w[i]);
+}
+
+// y = A x for a CSR matrix in FP64 (P: dofs x lattice, R = P^T: lattice x dofs)
+__global__ void k_csr_mv(int64_t nrows, const int32_t *__restrict__ rp, const int32_t *__restrict__ col, const double *__restrict__ val,
+                         const double *__restrict__ x, double *__restrict__ y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nrows) return;
+  double s = 0;
+  for (int32_t k = rp[i]; k < rp[i + 1]; k++) s += val[k] * x[col[k]];
+  y[i] = s;
+}
+
+// network input channel 0 = rc / rms(rc) (interior), channel 1 = log k; scale[0] = rms
+__global__ void k_make_input(int64_t nv, const double *__restrict__ rc, const double *__restrict__ ss, double nint,
+                             const uint8_t *__restrict__ mask, const float *__restrict__ logk, float *__restrict__ in,
+                             double *__restrict__ scale) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const double s = sqrt(*ss / nint), inv = s > 0 ? 1.0 / s : 0.0;
+  if (i == 0) *scale = s;
+  if (i >= nv) return;
+  in[i] = mask[i] ? (float)(rc[i] * inv) : 0.f;
+  if (logk) in[nv + i] = logk[i];
+}
+
+// z += P (y * scale * ysc), non-finite values dropped and counted
+__global__ void k_prolong_add(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ col, const double *__restrict__ val,
+                              const float *__restrict__ y, const double *__restrict__ scale, double ysc, double *__restrict__ z,
+                              int *__restrict__ bad) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0;
+  for (int32_t k = rp[i]; k < rp[i + 1]; k++) s += val[k] * (double)y[col[k]];
+  s *= *scale * ysc;
+  if (!isfinite(s)) {
+    atomicAdd(bad, 1);
+    return;
+  }
+  z[i] += s;
+}
+
+// x at the lattice vertices (0 where the vertex is not an explicit dof)
+__global__ void k_gather_vertices(int64_t nv, const int32_t *__restrict__ vdof, const double *__restrict__ x, double *__restrict__ xv) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < nv) xv[i] = vdof[i] >= 0 ? x[vdof[i]] : 0.0;
+}
+
+// target = (x* - x_k) / scale_k at the vertices
+__global__ void k_targets(int64_t nv, int npairs, const double *__restrict__ xstar, const double *__restrict__ xk,
+                          const double *__restrict__ scale, float *__restrict__ tg) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nv * npairs) return;
+  const int64_t p = t / nv, i = t % nv;
+  const double s = scale[p];
+  tg[t] = s > 0 ? (float)((xstar[i] - xk[t]) / s) : 0.f;
+}
+
+// minibatch: in[b][0] = pair input, in[b][1] = log k of the pair's field; tb[b] = target / ysc
+__global__ void k_batch(int B, int64_t nv, const int32_t *__restrict__ idx, const int32_t *__restrict__ pfield,
+                        const float *__restrict__ pin, const float *__restrict__ ptg, const float *__restrict__ flogk, float inv_ysc,
+                        float *__restrict__ in, float *__restrict__ tb) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)B * nv) return;
+  const int64_t b = t / nv, i = t % nv;
+  const int p = idx[b];
+  in[(b * 2) * nv + i] = pin[(int64_t)p * nv + i];
+  in[(b * 2 + 1) * nv + i] = flogk[(int64_t)pfield[p] * nv + i];
+  tb[t] = ptg[(int64_t)p * nv + i] * inv_ysc;
+}
+
+// log k = g(x) at the vertex coordinates (random Fourier features, as dFSEvaluateLognormal)
+__global__ void k_logk(int64_t nv, const double *__restrict__ xyz, const double *__restrict__ grf, float *__restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  if (!grf) {
+    out[i] = 0.f;
+    return;
+  }
+  const int nf = (int)grf[0];
+  const double *w = grf + 3, *b = grf + 3 + 3 * nf, *x = xyz + 3 * i;
+  double s = 0;
+  for (int f = 0; f < nf; f++) s += cos(w[3 * f] * x[0] + w[3 * f + 1] * x[1] + w[3 * f + 2] * x[2] + b[f]);
+  out[i] = (float)(sqrt(2.0 * grf[1] / nf) * s);
+}
+
+inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------ object
+struct _p_dLearned {
+  _p_dFS *fs = nullptr;
+  Dims d[3];
+  int64_t nint = 0;
+  // transfer between the global dofs and the vertex lattice
+  int32_t *Pp = nullptr, *Pc = nullptr, *Rp = nullptr, *Rc = nullptr, *vdof = nullptr;
+  double *Pv = nullptr, *Rv = nullptr, *vxyz = nullptr;
+  uint8_t *mask = nullptr;
+  float *logk = nullptr;  // current field
+  // parameters: per layer W [co][ci][27] then bias [co]
+  int64_t woff[NLAYER], boff[NLAYER], nparam = 0;
+  float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
+  __nv_bfloat16 *wb = nullptr;
+  int64_t adam_t = 0;
+  double ysc = 1.0;
+  bool trained = false;
+  // activations and gradients for a batch of up to cap samples
+  int cap = 0;
+  float *act[16] = {};
+  float *G1 = nullptr, *G2 = nullptr, *GZ = nullptr, *ga1 = nullptr, *ga2 = nullptr, *tb = nullptr, *partial = nullptr;
+  int64_t partial_len = 0;
+  double *lpart = nullptr;
+  // correction workspace
+  double *rc = nullptr, *ss = nullptr, *scale = nullptr, *dpart = nullptr;
+  int *bad = nullptr;
+  int64_t applies = 0, dropped = 0;
+  // training pairs
+  int maxpairs = 0, npairs = 0, nfields = 0, maxfields = 0;
+  float *pin = nullptr, *ptg = nullptr, *flogk = nullptr;
+  int32_t *pfield = nullptr;
+  std::vector<int32_t> h_pfield;
+  // collection in progress
+  double *cxk = nullptr, *cscale = nullptr, *cxstar = nullptr;
+  int cfirst = 0, ccount = 0, cevery = 1, cmax = 0;
+};
+
+namespace {
+
+// activation slots
+enum { X0, H1, A1, H2, A2, H3, H3B, A3, W2, S2, B2, W1, S1, B1, Y, NACT };
+
+struct Shape {
+  int c, level;
+};
+constexpr Shape kAct[NACT] = {{2, 0},  {16, 0}, {16, 0}, {32, 1}, {32, 1}, {64, 2}, {64, 2}, {64, 2},
+                              {32, 2}, {32, 1}, {32, 1}, {16, 1}, {16, 0}, {16, 0}, {1, 0}};
+
+dErr ensure_cap(_p_dLearned *L, int B) {
+  if (B <= L->cap) return 0;
+  for (int i = 0; i < NACT; i++) {
+    cudaFree(L->act[i]);
+    L->act[i] = nullptr;
+  }
+  for (float **p : {&L->G1, &L->G2, &L->GZ, &L->ga1, &L->ga2, &L->tb, &L->partial}) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
+  cudaFree(L->lpart);
+  L->lpart = nullptr;
+  for (int i = 0; i < NACT; i++) CUCHK(cudaMalloc(&L->act[i], (size_t)B * kAct[i].c * L->d[kAct[i].level].n() * sizeof(float)));
+  int64_t gmax = 0;
+  for (int i = 0; i < NACT; i++) gmax = std::max<int64_t>(gmax, (int64_t)kAct[i].c * L->d[kAct[i].level].n());
+  for (float **p : {&L->G1, &L->G2, &L->GZ}) CUCHK(cudaMalloc(p, (size_t)B * gmax * sizeof(float)));
+  CUCHK(cudaMalloc(&L->ga1, (size_t)B * 16 * L->d[0].n() * sizeof(float)));
+  CUCHK(cudaMalloc(&L->ga2, (size_t)B * 32 * L->d[1].n() * sizeof(float)));
+  CUCHK(cudaMalloc(&L->tb, (size_t)B * L->d[0].n() * sizeof(float)));
+  CUCHK(cudaMalloc(&L->lpart, (size_t)nblk((int64_t)B * L->d[0].n()) * sizeof(double)));
+  // weight-gradient partials: the largest chunk count times parameters over the layers
+  int64_t need = 0;
+  for (int l = 0; l < NLAYER; l++) {
+    const LayerDef &ld = kLayer[l];
+    const Dims dout = ld.stride == 2 ? L->d[ld.level_in + 1] : L->d[ld.level_in];
+    const int64_t nch = ((int64_t)B * dout.n() + 16383) / 16384;
+    need = std::max<int64_t>(need, nch * ((int64_t)ld.co * ld.ci * 27 + ld.co));
+  }
+  CUCHK(cudaMalloc(&L->partial, need * sizeof(float)));
+  L->partial_len = need;
+  L->cap = B;
+  return 0;
+}
+
+dErr conv_fwd(_p_dLearned *L, int l, int B, const float *x, float *y, int relu, cudaStream_t s) {
+  const LayerDef &ld = kLayer[l];
+  const Dims di = L->d[ld.level_in], dout = ld.stride == 2 ? L->d[ld.level_in + 1] : di;
+  const __nv_bfloat16 *W = L->wb + L->woff[l];
+  const float *bias = L->w + L->boff[l];
+  if (ld.co >= 16) {
+    dim3 grid(nblk((int64_t)B * dout.n(), 128), (ld.co + 15) / 16);
+    k_conv_fwd<16><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, dout, ld.stride, x, W, bias, relu, y);
+  } else {
+    dim3 grid(nblk((int64_t)B * dout.n(), 128), ld.co);
+    k_conv_fwd<1><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, dout, ld.stride, x, W, bias, relu, y);
+  }
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+dErr conv_bwd(_p_dLearned *L, int l, int B, const float *x, const float *gz, float *gx, int accumulate, cudaStream_t s) {
+  const LayerDef &ld = kLayer[l];
+  const Dims di = L->d[ld.level_in], dout = ld.stride == 2 ? L->d[ld.level_in + 1] : di;
+  const int64_t total = (int64_t)B * dout.n();
+  const int nch = (int)((total + 16383) / 16384);
+  const int64_t np = (int64_t)ld.co * ld.ci * 27 + ld.co;
+  if ((int64_t)nch * np > L->partial_len) return set_error("learned correction: gradient workspace too small");
+  k_conv_bwd_weight<<<dim3(ld.co * ld.ci, nch), 256, 0, s>>>(B, ld.ci, ld.co, di, dout, ld.stride, x, gz, 16384, L->partial);
+  k_sum_chunks<<<nblk(np), 256, 0, s>>>(np, nch, L->partial, L->g + L->woff[l]);
+  CUCHK(cudaGetLastError());
+  if (gx) {
+    dim3 grid(nblk((int64_t)B * di.n(), 128), (ld.ci + 15) / 16);
+    k_conv_bwd_data<16><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, dout, ld.stride, gz, L->wb + L->woff[l], gx, accumulate);
+    CUCHK(cudaGetLastError());
+  }
+  return 0;
+}
+
+dErr up_fwd(_p_dLearned *L, int B, int C, int lc, const float *in, const float *skip, float *out, cudaStream_t s) {
+  const Dims dc = L->d[lc], df = L->d[lc - 1];
+  k_up_fwd<<<nblk((int64_t)B * C * df.n()), 256, 0, s>>>(B * C, dc, df, in, skip, out);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+dErr up_bwd(_p_dLearned *L, int B, int C, int lc, const float *gf, float *gc, cudaStream_t s) {
+  const Dims dc = L->d[lc], df = L->d[lc - 1];
+  k_up_bwd<<<nblk((int64_t)B * C * dc.n()), 256, 0, s>>>(B * C, dc, df, gf, gc);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+dErr mask(int64_t n, const float *g, const float *act, float *out, cudaStream_t s) {
+  k_mask<<<nblk(n), 256, 0, s>>>(n, g, act, out);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+// forward of a batch whose input is in act[X0]; output in act[Y]
+dErr forward(_p_dLearned *L, int B, cudaStream_t s) {
+  float **a = L->act;
+  DCHK(conv_fwd(L, C1A, B, a[X0], a[H1], 1, s));
+  DCHK(conv_fwd(L, C1B, B, a[H1], a[A1], 1, s));
+  DCHK(conv_fwd(L, D1, B, a[A1], a[H2], 1, s));
+  DCHK(conv_fwd(L, C2A, B, a[H2], a[A2], 1, s));
+  DCHK(conv_fwd(L, D2, B, a[A2], a[H3], 1, s));
+  DCHK(conv_fwd(L, C3A, B, a[H3], a[H3B], 1, s));
+  DCHK(conv_fwd(L, C3B, B, a[H3B], a[A3], 1, s));
+  DCHK(conv_fwd(L, U2, B, a[A3], a[W2], 1, s));
+  DCHK(up_fwd(L, B, 32, 2, a[W2], a[A2], a[S2], s));  // s2 = up(w2) + a2
+  DCHK(conv_fwd(L, C2B, B, a[S2], a[B2], 1, s));
+  DCHK(conv_fwd(L, U1, B, a[B2], a[W1], 1, s));
+  DCHK(up_fwd(L, B, 16, 1, a[W1], a[A1], a[S1], s));  // s1 = up(w1) + a1
+  DCHK(conv_fwd(L, C1C, B, a[S1], a[B1], 1, s));
+  DCHK(conv_fwd(L, OUT, B, a[B1], a[Y], 0, s));
+  return 0;
+}
+
+// backward from dL/dy in G1 [B][1][n0]; parameter gradients into L->g
+dErr backward(_p_dLearned *L, int B, cudaStream_t s) {
+  float **a = L->act;
+  const int64_t n0 = L->d[0].n(), n1 = L->d[1].n(), n2 = L->d[2].n();
+  float *G1 = L->G1, *G2 = L->G2, *GZ = L->GZ;
+  DCHK(conv_bwd(L, OUT, B, a[B1], G1, G2, 0, s));  // dL/db1
+  DCHK(mask((int64_t)B * 16 * n0, G2, a[B1], GZ, s));
+  DCHK(conv_bwd(L, C1C, B, a[S1], GZ, G1, 0, s));  // dL/ds1 = dL/dv1 = dL/da1 (skip)
+  k_copy_f<<<nblk((int64_t)B * 16 * n0), 256, 0, s>>>((int64_t)B * 16 * n0, G1, L->ga1);
+  DCHK(up_bwd(L, B, 16, 1, G1, G2, s));  // dL/dw1 [16][n1]
+  DCHK(mask((int64_t)B * 16 * n1, G2, a[W1], GZ, s));
+  DCHK(conv_bwd(L, U1, B, a[B2], GZ, G1, 0, s));  // dL/db2
+  DCHK(mask((int64_t)B * 32 * n1, G1, a[B2], GZ, s));
+  DCHK(conv_bwd(L, C2B, B, a[S2], GZ, G1, 0, s));  // dL/ds2
+  k_copy_f<<<nblk((int64_t)B * 32 * n1), 256, 0, s>>>((int64_t)B * 32 * n1, G1, L->ga2);
+  DCHK(up_bwd(L, B, 32, 2, G1, G2, s));  // dL/dw2 [32][n2]
+  DCHK(mask((int64_t)B * 32 * n2, G2, a[W2], GZ, s));
+  DCHK(conv_bwd(L, U2, B, a[A3], GZ, G1, 0, s));  // dL/da3
+  DCHK(mask((int64_t)B * 64 * n2, G1, a[A3], GZ, s));
+  DCHK(conv_bwd(L, C3B, B, a[H3B], GZ, G1, 0, s));  // dL/dh3b
+  DCHK(mask((int64_t)B * 64 * n2, G1, a[H3B], GZ, s));
+  DCHK(conv_bwd(L, C3A, B, a[H3], GZ, G1, 0, s));  // dL/dh3
+  DCHK(mask((int64_t)B * 64 * n2, G1, a[H3], GZ, s));
+  DCHK(conv_bwd(L, D2, B, a[A2], GZ, L->ga2, 1, s));  // dL/da2 += down path
+  DCHK(mask((int64_t)B * 32 * n1, L->ga2, a[A2], GZ, s));
+  DCHK(conv_bwd(L, C2A, B, a[H2], GZ, G1, 0, s));  // dL/dh2
+  DCHK(mask((int64_t)B * 32 * n1, G1, a[H2], GZ, s));
+  DCHK(conv_bwd(L, D1, B, a[A1], GZ, L->ga1, 1, s));  // dL/da1 += down path
+  DCHK(mask((int64_t)B * 16 * n0, L->ga1, a[A1], GZ, s));
+  DCHK(conv_bwd(L, C1B, B, a[H1], GZ, G1, 0, s));  // dL/dh1
+  DCHK(mask((int64_t)B * 16 * n0, G1, a[H1], GZ, s));
+  DCHK(conv_bwd(L, C1A, B, a[X0], GZ, nullptr, 0, s));
+  return 0;
+}
+
+// loss of act[Y] against L->tb; gradient into G1
+dErr loss(_p_dLearned *L, int B, double *out, cudaStream_t s) {
+  const int64_t n0 = L->d[0].n(), tot = (int64_t)B * n0;
+  const unsigned nb = nblk(tot);
+  k_mse<<<nb, 256, 0, s>>>(B, n0, L->act[Y], L->tb, L->mask, (float)(1.0 / ((double)B * L->nint)), L->G1, L->lpart);
+  CUCHK(cudaGetLastError());
+  if (out) {
+    std::vector<double> h(nb);
+    CUCHK(cudaMemcpyAsync(h.data(), L->lpart, nb * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CUCHK(cudaStreamSynchronize(s));
+    double t = 0;
+    for (double v : h) t += v;
+    *out = t / ((double)B * L->nint);
+  }
+  return 0;
+}
+
+dErr adam_step(_p_dLearned *L, double lr, cudaStream_t s) {
+  L->adam_t++;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float bc1 = 1.f - powf(b1, (float)L->adam_t), bc2 = 1.f - powf(b2, (float)L->adam_t);
+  k_adam<<<nblk(L->nparam), 256, 0, s>>>(L->nparam, L->w, L->g, L->m, L->v, (float)lr, b1, b2, 1e-8f, bc1, bc2, L->wb);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+// the correction z += P N(R r); called by FGMRES after the Chebyshev step
+dErr apply_correction(void *ctx, const double *r, double *z) {
+  _p_dLearned *L = (_p_dLearned *)ctx;
+  _p_dFS *fs = L->fs;
+  cudaStream_t s = fs->stream;
+  const int64_t n0 = L->d[0].n();
+  DCHK(ensure_cap(L, 1));
+  k_csr_mv<<<nblk(n0), 256, 0, s>>>(n0, L->Rp, L->Rc, L->Rv, r, L->rc);
+  DCHK(device_dot(n0, L->rc, L->rc, L->dpart, L->ss, s));
+  k_make_input<<<nblk(n0), 256, 0, s>>>(n0, L->rc, L->ss, (double)L->nint, L->mask, L->logk, L->act[X0], L->scale);
+  CUCHK(cudaGetLastError());
+  DCHK(forward(L, 1, s));
+  k_prolong_add<<<nblk(fs->n), 256, 0, s>>>(fs->n, L->Pp, L->Pc, L->Pv, L->act[Y], L->scale, L->ysc, z, L->bad);
+  CUCHK(cudaGetLastError());
+  L->applies++;
+  return 0;
+}
+
+// CG monitor during pair collection: every cevery-th iterate, R r_k (normalised) and x_k at the vertices
+dErr collect_monitor(void *ctx, int it, const double *x, const double *r) {
+  _p_dLearned *L = (_p_dLearned *)ctx;
+  if (it % L->cevery || L->ccount >= L->cmax) return 0;
+  cudaStream_t s = L->fs->stream;
+  const int64_t n0 = L->d[0].n();
+  const int p = L->cfirst + L->ccount;
+  k_csr_mv<<<nblk(n0), 256, 0, s>>>(n0, L->Rp, L->Rc, L->Rv, r, L->rc);
+  DCHK(device_dot(n0, L->rc, L->rc, L->dpart, L->ss, s));
+  k_make_input<<<nblk(n0), 256, 0, s>>>(n0, L->rc, L->ss, (double)L->nint, L->mask, nullptr, L->pin + (int64_t)p * n0,
+                                        L->cscale + L->ccount);
+  k_gather_vertices<<<nblk(n0), 256, 0, s>>>(n0, L->vdof, x, L->cxk + (int64_t)L->ccount * n0);
+  CUCHK(cudaGetLastError());
+  L->ccount++;
+  return 0;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------ C ABI
+extern "C" {
+
+dErr dLearnedCreate(dFS fs, uint64_t seed, dLearned *out) {
+  if (!fs || !out) return set_error("null argument");
+  if (!fs->setup) return set_error("dFS not set up");
+  if (!fs->uniform || fs->bs != 1) return set_error("learned correction needs a scalar uniform-order space");
+  _p_dMesh *mesh = fs->mesh;
+  const int p = fs->p, N = p + 1, N3 = N * N * N;
+  _p_dLearned *L = new _p_dLearned();
+  L->fs = fs;
+  L->d[0] = {mesh->nx, mesh->ny, mesh->nz};
+  L->d[1] = coarsen(L->d[0]);
+  L->d[2] = coarsen(L->d[1]);
+  if (std::min({L->d[2].x, L->d[2].y, L->d[2].z}) < 2) {
+    delete L;
+    return set_error("learned correction needs at least 4 elements per direction");
+  }
+  const Dims d0 = L->d[0];
+  const int64_t n0 = d0.n(), n = fs->n;
+  // lattice index of every mesh vertex from its position (interior vertices move by less than half a cell)
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int64_t i = 0; i < mesh->nv; i++)
+    for (int c = 0; c < 3; c++) lo[c] = std::min(lo[c], mesh->vx[3 * i + c]), hi[c] = std::max(hi[c], mesh->vx[3 * i + c]);
+  const int Ld[3] = {d0.x, d0.y, d0.z};
+  auto lat = [&](const double *X, int c) { return (int)std::lround((X[c] - lo[c]) / (hi[c] - lo[c]) * (Ld[c] - 1)); };
+  std::vector<double> coords((size_t)fs->nelem * 24), vxyz((size_t)n0 * 3, 0.0);
+  CUCHK(cudaMemcpy(coords.data(), fs->d_coords, coords.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int64_t i = 0; i < mesh->nv; i++) {
+    const double *X = &mesh->vx[3 * i];
+    const int64_t li = ((int64_t)lat(X, 0) * d0.y + lat(X, 1)) * d0.z + lat(X, 2);
+    for (int c = 0; c < 3; c++) vxyz[3 * li + c] = X[c];
+  }
+  // P: every explicit dof from its first occurrence in the expanded ordering; trilinear weights of the
+  // element's corner vertices at the dof's GLL reference coordinates; Dirichlet vertices carry no value
+  double gll[MAXP], wgll[MAXP];
+  lobatto_rule(N, gll, wgll);
+  std::vector<int64_t> first(n, -1);
+  for (int64_t x = 0; x < fs->nexp; x++) {
+    const int32_t c = fs->emap[x];
+    if (c < n && first[c] < 0) first[c] = x;
+  }
+  std::vector<int32_t> vdof(n0, -1);
+  std::vector<int64_t> corner_lat((size_t)fs->nelem * 8);
+  for (int64_t e = 0; e < fs->nelem; e++)
+    for (int v = 0; v < 8; v++) {
+      const double *X = &coords[(size_t)e * 24 + 3 * v];
+      corner_lat[e * 8 + v] = ((int64_t)lat(X, 0) * d0.y + lat(X, 1)) * d0.z + lat(X, 2);
+      const int i = v >> 2, j = (v >> 1) & 1, k = v & 1;
+      const int32_t c = fs->emap[e * N3 + ((i * p) * N + j * p) * N + k * p];
+      if (c < n) vdof[corner_lat[e * 8 + v]] = c;
+    }
+  std::vector<int32_t> Pp(n + 1, 0), Pc;
+  std::vector<double> Pv;
+  Pc.reserve(n * 8), Pv.reserve(n * 8);
+  for (int64_t d = 0; d < n; d++) {
+    const int64_t x = first[d], e = x / N3;
+    const int loc = (int)(x - e * N3), a = loc / (N * N), b = (loc / N) % N, c = loc % N;
+    std::vector<std::pair<int64_t, double>> row;
+    for (int v = 0; v < 8; v++) {
+      const int i = v >> 2, j = (v >> 1) & 1, k = v & 1;
+      const double w = (i ? 1 + gll[a] : 1 - gll[a]) * (j ? 1 + gll[b] : 1 - gll[b]) * (k ? 1 + gll[c] : 1 - gll[c]) / 8;
+      const int64_t lt = corner_lat[e * 8 + v];
+      if (w != 0 && vdof[lt] >= 0) row.push_back({lt, w});
+    }
+    std::sort(row.begin(), row.end());
+    for (auto &q : row) Pc.push_back((int32_t)q.first), Pv.push_back(q.second);
+    Pp[d + 1] = (int32_t)Pc.size();
+  }
+  // R = P^T with ascending dof order per lattice row
+  std::vector<int32_t> Rp(n0 + 1, 0), Rc(Pc.size());
+  std::vector<double> Rv(Pc.size());
+  for (int32_t c : Pc) Rp[c + 1]++;
+  for (int64_t i = 0; i < n0; i++) Rp[i + 1] += Rp[i];
+  {
+    std::vector<int32_t> pos(Rp.begin(), Rp.end() - 1);
+    for (int64_t d = 0; d < n; d++)
+      for (int32_t k = Pp[d]; k < Pp[d + 1]; k++) {
+        Rc[pos[Pc[k]]] = (int32_t)d;
+        Rv[pos[Pc[k]]++] = Pv[k];
+      }
+  }
+  std::vector<uint8_t> msk(n0);
+  for (int64_t i = 0; i < n0; i++) msk[i] = vdof[i] >= 0, L->nint += msk[i];
+  auto up = [](auto **dst, const auto &src) -> dErr {
+    CUCHK(cudaMalloc(dst, std::max<size_t>(src.size(), 1) * sizeof(src[0])));
+    if (src.size()) CUCHK(cudaMemcpy(*dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice));
+    return 0;
+  };
+  DCHK(up(&L->Pp, Pp));
+  DCHK(up(&L->Pc, Pc));
+  DCHK(up(&L->Pv, Pv));
+  DCHK(up(&L->Rp, Rp));
+  DCHK(up(&L->Rc, Rc));
+  DCHK(up(&L->Rv, Rv));
+  DCHK(up(&L->vdof, vdof));
+  DCHK(up(&L->mask, msk));
+  DCHK(up(&L->vxyz, vxyz));
+  CUCHK(cudaMalloc(&L->logk, n0 * sizeof(float)));
+  CUCHK(cudaMemset(L->logk, 0, n0 * sizeof(float)));
+  CUCHK(cudaMalloc(&L->rc, n0 * sizeof(double)));
+  CUCHK(cudaMalloc(&L->ss, 2 * sizeof(double)));
+  CUCHK(cudaMalloc(&L->scale, sizeof(double)));
+  CUCHK(cudaMalloc(&L->dpart, 1024 * sizeof(double)));
+  CUCHK(cudaMalloc(&L->bad, sizeof(int)));
+  CUCHK(cudaMemset(L->bad, 0, sizeof(int)));
+  // parameters: He-uniform initialisation from a seeded generator, zero biases
+  int64_t off = 0;
+  for (int l = 0; l < NLAYER; l++) {
+    L->woff[l] = off;
+    off += (int64_t)kLayer[l].co * kLayer[l].ci * 27;
+    L->boff[l] = off;
+    off += kLayer[l].co;
+  }
+  L->nparam = off;
+  std::vector<float> w(off, 0.f);
+  std::mt19937_64 gen(seed);
+  for (int l = 0; l < NLAYER; l++) {
+    const double bound = std::sqrt(6.0 / (kLayer[l].ci * 27.0)) * (l == OUT ? 0.1 : 1.0);
+    std::uniform_real_distribution<double> U(-bound, bound);
+    for (int64_t i = L->woff[l]; i < L->boff[l]; i++) w[i] = (float)U(gen);
+  }
+  DCHK(up(&L->w, w));
+  for (float **q : {&L->g, &L->m, &L->v}) {
+    CUCHK(cudaMalloc(q, off * sizeof(float)));
+    CUCHK(cudaMemset(*q, 0, off * sizeof(float)));
+  }
+  CUCHK(cudaMalloc(&L->wb, off * sizeof(__nv_bfloat16)));
+  k_to_bf16<<<nblk(off), 256>>>(off, L->w, L->wb);
+  CUCHK(cudaGetLastError());
+  CUCHK(cudaDeviceSynchronize());
+  *out = L;
+  return 0;
+}
+
+dErr dLearnedDestroy(dLearned *net) {
+  if (!net || !*net) return 0;
+  _p_dLearned *L = *net;
+  for (int i = 0; i < NACT; i++) cudaFree(L->act[i]);
+  for (void *p : {(void *)L->Pp, (void *)L->Pc, (void *)L->Rp, (void *)L->Rc, (void *)L->vdof, (void *)L->Pv, (void *)L->Rv,
+                  (void *)L->vxyz, (void *)L->mask, (void *)L->logk, (void *)L->w, (void *)L->g, (void *)L->m, (void *)L->v,
+                  (void *)L->wb, (void *)L->G1, (void *)L->G2, (void *)L->GZ, (void *)L->ga1, (void *)L->ga2, (void *)L->tb,
+                  (void *)L->partial, (void *)L->lpart, (void *)L->rc, (void *)L->ss, (void *)L->scale, (void *)L->dpart,
+                  (void *)L->bad, (void *)L->pin, (void *)L->ptg, (void *)L->flogk, (void *)L->pfield, (void *)L->cxk,
+                  (void *)L->cscale, (void *)L->cxstar})
+    cudaFree(p);
+  delete L;
+  *net = nullptr;
+  return 0;
+}
+
+dErr dLearnedGetSizes(dLearned L, dInt dims[3], int64_t *nparam, int64_t *npairs) {
+  if (!L) return set_error("null network");
+  if (dims) dims[0] = L->d[0].x, dims[1] = L->d[0].y, dims[2] = L->d[0].z;
+  if (nparam) *nparam = L->nparam;
+  if (npairs) *npairs = L->npairs;
+  return 0;
+}
+
+dErr dLearnedSetField(dLearned L, const dReal *grf) {
+  if (!L) return set_error("null network");
+  const int64_t n0 = L->d[0].n();
+  double *dg = nullptr;
+  if (grf) {
+    const int nf = (int)grf[0];
+    CUCHK(cudaMalloc(&dg, (3 + 4 * nf) * sizeof(double)));
+    CUCHK(cudaMemcpy(dg, grf, (3 + 4 * nf) * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  k_logk<<<nblk(n0), 256, 0, L->fs->stream>>>(n0, L->vxyz, dg, L->logk);
+  CUCHK(cudaGetLastError());
+  CUCHK(cudaStreamSynchronize(L->fs->stream));
+  cudaFree(dg);
+  return 0;
+}
+
+dErr dLearnedGetWeights(dLearned L, float *w_host) {
+  if (!L || !w_host) return set_error("null argument");
+  CUCHK(cudaMemcpy(w_host, L->w, L->nparam * sizeof(float), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+dErr dLearnedSetWeights(dLearned L, const float *w_host, dReal ysc) {
+  if (!L || !w_host) return set_error("null argument");
+  CUCHK(cudaMemcpy(L->w, w_host, L->nparam * sizeof(float), cudaMemcpyHostToDevice));
+  k_to_bf16<<<nblk(L->nparam), 256>>>(L->nparam, L->w, L->wb);
+  CUCHK(cudaGetLastError());
+  CUCHK(cudaDeviceSynchronize());
+  if (ysc > 0) L->ysc = ysc, L->trained = true;
+  return 0;
+}
+
+// raw network on device arrays: in [B][2][lattice], out [B][1][lattice] (FP32)
+dErr dLearnedForward(dLearned L, dInt B, const float *in, float *out) {
+  if (!L || !in || !out || B < 1) return set_error("bad argument");
+  cudaStream_t s = L->fs->stream;
+  DCHK(ensure_cap(L, B));
+  const int64_t n0 = L->d[0].n();
+  CUCHK(cudaMemcpyAsync(L->act[X0], in, (size_t)B * 2 * n0 * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  DCHK(forward(L, B, s));
+  CUCHK(cudaMemcpyAsync(out, L->act[Y], (size_t)B * n0 * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  CUCHK(cudaStreamSynchronize(s));
+  return 0;
+}
+
+// loss (mean squared error over interior vertices) and its parameter gradient (device array [nparam])
+dErr dLearnedLossGrad(dLearned L, dInt B, const float *in, const float *target, dReal *lossv, float *grad) {
+  if (!L || !in || !target || B < 1) return set_error("bad argument");
+  cudaStream_t s = L->fs->stream;
+  DCHK(ensure_cap(L, B));
+  const int64_t n0 = L->d[0].n();
+  CUCHK(cudaMemcpyAsync(L->act[X0], in, (size_t)B * 2 * n0 * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  CUCHK(cudaMemcpyAsync(L->tb, target, (size_t)B * n0 * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  DCHK(forward(L, B, s));
+  double lv = 0;
+  DCHK(loss(L, B, &lv, s));
+  DCHK(backward(L, B, s));
+  if (grad) CUCHK(cudaMemcpyAsync(grad, L->g, L->nparam * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  CUCHK(cudaStreamSynchronize(s));
+  if (lossv) *lossv = lv;
+  return 0;
+}
+
+// run the plain solver (CG, its preconditioner as configured) on b and record up to max_pairs
+// (residual, error) pairs from every `every`-th iterate; the current field (dLearnedSetField) is the
+// pairs' log k channel
+dErr dLearnedCollectPairs(dLearned L, dKSP ksp, const dScalar *b, dReal rtol, dInt maxit, dInt every, dInt max_pairs,
+                          dInt *collected) {
+  if (!L || !ksp || !b) return set_error("null argument");
+  if (every < 1 || max_pairs < 1) return set_error("every and max_pairs must be positive");
+  _p_dFS *fs = L->fs;
+  cudaStream_t s = fs->stream;
+  const int64_t n0 = L->d[0].n();
+  // grow the pair store and the field store
+  const int newmax = L->npairs + max_pairs;
+  if (newmax > L->maxpairs) {
+    float *pin, *ptg;
+    int32_t *pf;
+    CUCHK(cudaMalloc(&pin, (size_t)newmax * n0 * sizeof(float)));
+    CUCHK(cudaMalloc(&ptg, (size_t)newmax * n0 * sizeof(float)));
+    CUCHK(cudaMalloc(&pf, (size_t)newmax * sizeof(int32_t)));
+    if (L->npairs) {
+      CUCHK(cudaMemcpy(pin, L->pin, (size_t)L->npairs * n0 * sizeof(float), cudaMemcpyDeviceToDevice));
+      CUCHK(cudaMemcpy(ptg, L->ptg, (size_t)L->npairs * n0 * sizeof(float), cudaMemcpyDeviceToDevice));
+    }
+    cudaFree(L->pin), cudaFree(L->ptg), cudaFree(L->pfield);
+    L->pin = pin, L->ptg = ptg, L->pfield = pf, L->maxpairs = newmax;
+  }
+  if (L->nfields + 1 > L->maxfields) {
+    const int nm = std::max(8, 2 * L->maxfields);
+    float *fl;
+    CUCHK(cudaMalloc(&fl, (size_t)nm * n0 * sizeof(float)));
+    if (L->nfields) CUCHK(cudaMemcpy(fl, L->flogk, (size_t)L->nfields * n0 * sizeof(float), cudaMemcpyDeviceToDevice));
+    cudaFree(L->flogk);
+    L->flogk = fl, L->maxfields = nm;
+  }
+  CUCHK(cudaMemcpy(L->flogk + (int64_t)L->nfields * n0, L->logk, n0 * sizeof(float), cudaMemcpyDeviceToDevice));
+  CUCHK(cudaMalloc(&L->cxk, (size_t)max_pairs * n0 * sizeof(double)));
+  CUCHK(cudaMalloc(&L->cscale, (size_t)max_pairs * sizeof(double)));
+  CUCHK(cudaMalloc(&L->cxstar, (size_t)n0 * sizeof(double)));
+  L->cfirst = L->npairs, L->ccount = 0, L->cevery = every, L->cmax = max_pairs;
+  double *x;
+  CUCHK(cudaMalloc(&x, std::max<int64_t>(fs->n, 1) * sizeof(double)));
+  CUCHK(cudaMemsetAsync(x, 0, fs->n * sizeof(double), s));
+  int its = 0;
+  double rn = 0;
+  dErr err = ksp_set_monitor(ksp, collect_monitor, L);
+  if (!err) err = ksp_solve(ksp, b, x, rtol, maxit, &its, &rn);
+  ksp_set_monitor(ksp, nullptr, nullptr);
+  if (!err && !(rn <= rtol)) err = set_error("plain solve reached only %g of %g while collecting pairs", rn, rtol);
+  if (!err) {
+    const int np = L->ccount;
+    k_gather_vertices<<<nblk(n0), 256, 0, s>>>(n0, L->vdof, x, L->cxstar);
+    if (np) k_targets<<<nblk((int64_t)np * n0), 256, 0, s>>>(n0, np, L->cxstar, L->cxk, L->cscale, L->ptg + (int64_t)L->cfirst * n0);
+    L->h_pfield.resize(L->cfirst + np, L->nfields);
+    if (L->cfirst + np)
+      CUCHK(cudaMemcpyAsync(L->pfield, L->h_pfield.data(), (L->cfirst + np) * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    CUCHK(cudaStreamSynchronize(s));
+    CUCHK(cudaGetLastError());
+    L->npairs += np;
+    L->nfields++;
+    if (collected) *collected = np;
+  }
+  cudaFree(x);
+  cudaFree(L->cxk), cudaFree(L->cscale), cudaFree(L->cxstar);
+  L->cxk = L->cscale = L->cxstar = nullptr;
+  return err;
+}
+
+// minibatch Adam on the collected pairs; losses[epochs] receives the mean loss of every epoch
+dErr dLearnedTrain(dLearned L, dInt epochs, dInt batch, dReal lr, uint64_t seed, dReal *losses) {
+  if (!L) return set_error("null network");
+  if (L->npairs < 1) return set_error("no training pairs collected");
+  if (epochs < 1 || batch < 1) return set_error("epochs and batch must be positive");
+  _p_dFS *fs = L->fs;
+  cudaStream_t s = fs->stream;
+  const int64_t n0 = L->d[0].n();
+  const int B = std::min<int>(batch, L->npairs);
+  DCHK(ensure_cap(L, B));
+  // target scale: RMS of all targets over interior vertices (fixed once, kept with the network)
+  if (!L->trained) {
+    k_masked_sumsq<<<1024, 256, 0, s>>>((int64_t)L->npairs * n0, n0, L->ptg, L->mask, L->dpart);
+    CUCHK(cudaGetLastError());
+    std::vector<double> h(1024);
+    CUCHK(cudaMemcpyAsync(h.data(), L->dpart, 1024 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CUCHK(cudaStreamSynchronize(s));
+    double ss = 0;
+    for (double v : h) ss += v;
+    L->ysc = std::sqrt(ss / ((double)L->npairs * L->nint));
+    if (!(L->ysc > 0)) L->ysc = 1;
+  }
+  int32_t *didx;
+  CUCHK(cudaMalloc(&didx, B * sizeof(int32_t)));
+  std::mt19937_64 gen(seed);
+  std::vector<int32_t> perm(L->npairs);
+  dErr err = 0;
+  for (int ep = 0; ep < epochs && !err; ep++) {
+    for (int i = 0; i < L->npairs; i++) perm[i] = i;
+    std::shuffle(perm.begin(), perm.end(), gen);
+    double tot = 0;
+    int nb = 0;
+    for (int i0 = 0; i0 + B <= L->npairs && !err; i0 += B, nb++) {
+      CUCHK(cudaMemcpyAsync(didx, perm.data() + i0, B * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+      k_batch<<<nblk((int64_t)B * n0), 256, 0, s>>>(B, n0, didx, L->pfield, L->pin, L->ptg, L->flogk, (float)(1.0 / L->ysc),
+                                                    L->act[X0], L->tb);
+      CUCHK(cudaGetLastError());
+      DCHK(forward(L, B, s));
+      double lv = 0;
+      DCHK(loss(L, B, &lv, s));
+      DCHK(backward(L, B, s));
+      DCHK(adam_step(L, lr, s));
+      tot += lv;
+    }
+    if (losses) losses[ep] = nb ? tot / nb : 0;
+  }
+  CUCHK(cudaStreamSynchronize(s));
+  cudaFree(didx);
+  L->trained = true;
+  return err;
+}
+
+dErr dLearnedGetScale(dLearned L, dReal *ysc) {
+  if (!L || !ysc) return set_error("null argument");
+  *ysc = L->ysc;
+  return 0;
+}
+
+// z += P N(R r) for a global residual r (device vectors)
+dErr dLearnedApply(dLearned L, const dScalar *r, dScalar *z) {
+  if (!L || !r || !z) return set_error("null argument");
+  DCHK(apply_correction(L, r, z));
+  CUCHK(cudaStreamSynchronize(L->fs->stream));
+  return 0;
+}
+
+// restriction and prolongation on their own (device vectors): rc = R r [lattice], z += P c
+dErr dLearnedRestrict(dLearned L, const dScalar *r, dScalar *rc) {
+  if (!L || !r || !rc) return set_error("null argument");
+  const int64_t n0 = L->d[0].n();
+  k_csr_mv<<<nblk(n0), 256, 0, L->fs->stream>>>(n0, L->Rp, L->Rc, L->Rv, r, rc);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+dErr dLearnedProlong(dLearned L, const dScalar *c, dScalar *z) {
+  if (!L || !c || !z) return set_error("null argument");
+  k_csr_mv<<<nblk(L->fs->n), 256, 0, L->fs->stream>>>(L->fs->n, L->Pp, L->Pc, L->Pv, c, z);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+// FGMRES preconditioner z = Chebyshev(r) + P N(R r); NULL removes the correction
+dErr dKSPSetLearnedCorrection(dKSP ksp, dLearned L) {
+  if (!ksp) return set_error("null KSP");
+  if (L && !L->trained) return set_error("the network has not been trained or loaded");
+  return L ? ksp_set_correction(ksp, apply_correction, L) : ksp_set_correction(ksp, nullptr, nullptr);
+}
+
+dErr dLearnedGetStats(dLearned L, int64_t *applies, int64_t *dropped_values) {
+  if (!L) return set_error("null network");
+  int bad = 0;
+  CUCHK(cudaMemcpy(&bad, L->bad, sizeof(int), cudaMemcpyDeviceToHost));
+  if (applies) *applies = L->applies;
+  if (dropped_values) *dropped_values = bad;
+  return 0;
+}
+
+}  // extern "C"

@@ -216,12 +216,52 @@ dErr dKSPDestroy(dKSP *ksp);
 /* Chebyshev-Jacobi degree on the Q1 matrix, inner precision, restart length */
 dErr dKSPSetOptions(dKSP ksp, dInt cheb_degree, dPrecision pc_precision, dInt restart);
 dErr dKSPSolve(dKSP ksp, const dScalar *b, dScalar *x, dReal rtol, dInt maxit, dInt *its, dReal *rnorm);
+/* statistics: preconditioner applications, learned corrections dropped by the fallback, whether the
+ * correction was still in use at the end of the last solve */
+dErr dKSPGetStats(dKSP ksp, int64_t *pc_applies, int64_t *correction_rejects, int *correction_active);
+
+/* ---------------------------------------------------------------- learned coarse correction */
+/* No counterpart in the reference. A 3-level 3-D convolutional U-Net (16/32/64 channels, 3x3x3 kernels,
+ * BF16 weights, FP32 accumulation) on the lattice of mesh vertices: z = Chebyshev(r) + P N(R r) inside
+ * FGMRES, where R = P^T restricts the residual to the vertices, N maps [R r / rms, log k] to the error at
+ * the vertices, and P interpolates trilinearly onto the GLL nodes. Scalar uniform-order spaces on block
+ * meshes with at least 4 elements per direction. */
+typedef struct _p_dLearned *dLearned;
+dErr dLearnedCreate(dFS fs, uint64_t seed, dLearned *net);
+dErr dLearnedDestroy(dLearned *net);
+/* vertex lattice dims, parameter count, collected pairs */
+dErr dLearnedGetSizes(dLearned net, dInt dims[3], int64_t *nparam, int64_t *npairs);
+/* coefficient field of the next pairs / corrections: log k at the vertices from dGRFCreate data (NULL: k = 1) */
+dErr dLearnedSetField(dLearned net, const dReal *grf);
+/* run the plain solver (CG on ksp) on b to rtol and record every `every`-th (residual, error) pair */
+dErr dLearnedCollectPairs(dLearned net, dKSP ksp, const dScalar *b, dReal rtol, dInt maxit, dInt every, dInt max_pairs,
+                          dInt *collected);
+/* Adam on the collected pairs (mean squared error over interior vertices); losses[epochs] (may be NULL) */
+dErr dLearnedTrain(dLearned net, dInt epochs, dInt batch, dReal lr, uint64_t seed, dReal *losses);
+/* z += P N(R r) */
+dErr dLearnedApply(dLearned net, const dScalar *r, dScalar *z);
+/* FGMRES preconditioner z = Chebyshev(r) + P N(R r) with the plain preconditioner as fallback; NULL removes it */
+dErr dKSPSetLearnedCorrection(dKSP ksp, dLearned net);
+/* raw network (device FP32 arrays): in [B][2][lattice] -> out [B][1][lattice]; loss and parameter gradient */
+dErr dLearnedForward(dLearned net, dInt B, const float *in, float *out);
+dErr dLearnedLossGrad(dLearned net, dInt B, const float *in, const float *target, dReal *loss, float *grad);
+/* parameters (host FP32 [nparam], layer by layer: W[co][ci][27] then bias[co]); target scale */
+dErr dLearnedGetWeights(dLearned net, float *w);
+dErr dLearnedSetWeights(dLearned net, const float *w, dReal target_scale);
+dErr dLearnedGetScale(dLearned net, dReal *target_scale);
+/* transfer operators on their own: rc = R r (lattice), z = P c (global) */
+dErr dLearnedRestrict(dLearned net, const dScalar *r, dScalar *rc);
+dErr dLearnedProlong(dLearned net, const dScalar *c, dScalar *z);
+/* corrections applied and non-finite values dropped */
+dErr dLearnedGetStats(dLearned net, int64_t *applies, int64_t *dropped_values);
+
 /* ---------------------------------------------------------------- Newton (p-Laplacian) */
 /* Newton-Krylov for N(u) = b with N the p-Laplacian function (dOperatorPLaplaceFunction): the SNES side of
  * ellip.c (SNESSetFunction/SNESSetJacobian, ellip.c:697-704; PETSc SNES is not part of this library).
  * Each step re-assembles the Q1 Jacobian into Jp at u (dFSAssembleQ1PLaplace), solves with ksp (operator
  * op = the matrix-free Jacobian at u; FGMRES with FP32 inner applies gives the mixed-precision form),
- * and backtracks on ||F||. fnorm receives max_it+1 residual norms, lin_its max_it iteration counts. */
+ * and backtracks on ||F||. fnorm receives max_it+1 residual norms, lin_its max_it iteration counts.
+ * Reaching max_it is not an error (as SNES, the caller reads its and fnorm); a failed line search is. */
 typedef struct {
   dInt max_it;
   dReal rtol, atol;   /* stop when ||F|| <= rtol ||F0|| or ||F|| <= atol */

@@ -1,0 +1,192 @@
+"""Learned coarse correction: the U-Net kernels against the numpy oracle (forward, loss, full parameter
+gradient), the vertex-lattice transfer operators, training on (residual, error) pairs from the plain solver,
+the gain it gives FGMRES on a fresh lognormal field, and the fallback to the plain preconditioner."""
+import os
+
+import numpy as np
+import pytest
+
+import dohp_gb300 as dg
+import pyoracle as po
+import unet_oracle as uo
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import subprocess, sys
+    subprocess.run([sys.executable, os.path.join(os.path.dirname(dg.__file__), "build.py")], check=True)
+    dg.lib()
+
+
+def dev(a, dtype=None):
+    return torch.as_tensor(np.ascontiguousarray(a if dtype is None else a.astype(dtype)), device="cuda")
+
+
+def rounded(w):
+    """the weights the kernels use: W entries rounded to bf16, biases kept"""
+    out, o = np.asarray(w, np.float64).copy(), 0
+    for _, ci, co, _, _ in uo.LAYERS:
+        out[o:o + co * ci * 27] = uo.bf16_round(w[o:o + co * ci * 27])
+        o += co * ci * 27 + co
+    return out
+
+
+def interior(dims):
+    m = np.zeros(dims, bool)
+    m[1:-1, 1:-1, 1:-1] = True
+    return m
+
+
+def test_forward_matches_oracle():
+    fs = dg.FS((7, 6, 7), degree=2, seed=1)
+    net = dg.Learned(fs, seed=3)
+    assert net.dims == (7, 6, 7) and net.nparam == uo.nparams()
+    w = net.get_weights()
+    x = np.random.default_rng(0).standard_normal((2, 2) + net.dims).astype(np.float32)
+    y = torch.zeros((2, 1) + net.dims, dtype=torch.float32, device="cuda")
+    net.forward(dev(x), y)
+    yo, _ = uo.forward(rounded(w), x.astype(np.float64), net.dims)
+    yg = y.cpu().numpy()
+    assert np.linalg.norm(yg - yo) / np.linalg.norm(yo) < 2e-5
+
+
+def test_loss_and_gradient_match_oracle():
+    fs = dg.FS((7, 7, 6), degree=2, seed=2)
+    net = dg.Learned(fs, seed=5)
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((3, 2) + net.dims).astype(np.float32)
+    t = rng.standard_normal((3, 1) + net.dims).astype(np.float32)
+    g = torch.zeros(net.nparam, dtype=torch.float32, device="cuda")
+    lv = net.loss_grad(dev(x), dev(t), g)
+    lo, go, _ = uo.loss_grad(rounded(net.get_weights()), x.astype(np.float64), t.astype(np.float64), interior(net.dims))
+    assert abs(lv - lo) / lo < 1e-5
+    gg = g.cpu().numpy()
+    assert np.linalg.norm(gg - go) / np.linalg.norm(go) < 1e-4
+    # every layer's block of the gradient, not just the norm
+    o = 0
+    for name, ci, co, _, _ in uo.LAYERS:
+        n = co * ci * 27 + co
+        assert np.linalg.norm(gg[o:o + n] - go[o:o + n]) <= 1e-3 * np.linalg.norm(go[o:o + n]) + 1e-12, name
+        o += n
+
+
+def test_transfer_operators():
+    """R = P^T; P interpolates the vertex lattice trilinearly onto the GLL nodes of each element."""
+    M, p = 5, 3
+    fs = dg.FS((M + 1,) * 3, degree=p, perturb=0.1, seed=4)
+    o = po.FS(M + 1, M + 1, M + 1, degree=p, perturb=0.1, seed=4)
+    net = dg.Learned(fs)
+    L = M + 1
+    rng = np.random.default_rng(2)
+    c = rng.standard_normal(L ** 3)
+    c.reshape(L, L, L)[~interior((L, L, L))] = 0
+    r = rng.standard_normal(fs.n)
+    z = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
+    rc = torch.zeros(L ** 3, dtype=torch.float64, device="cuda")
+    net.prolong(dev(c), z)
+    net.restrict(dev(r), rc)
+    torch.cuda.synchronize()
+    zc, rcc = z.cpu().numpy(), rc.cpu().numpy()
+    assert abs(rcc @ c - r @ zc) < 1e-12 * abs(r @ zc)
+    # independent construction from the oracle's E map and element coordinates
+    em, xs, ce = o.emap(), o.xstart(), o.coords_expanded()
+    gll = po.lobatto(p + 1)[0]
+    ref = np.full(fs.n, np.nan)
+    for e in range(o.nelem):
+        lat = np.rint(ce[e] * M).astype(int)  # unit box: lattice index of each corner
+        for loc in range(xs[e + 1] - xs[e]):
+            d = em[xs[e] + loc]
+            if d >= fs.n:
+                continue
+            a, b, cc = loc // (p + 1) ** 2, (loc // (p + 1)) % (p + 1), loc % (p + 1)
+            v = 0.0
+            for k in range(8):
+                i, j, l = k >> 2, (k >> 1) & 1, k & 1
+                wgt = ((1 + gll[a]) if i else (1 - gll[a])) * ((1 + gll[b]) if j else (1 - gll[b])) * \
+                      ((1 + gll[cc]) if l else (1 - gll[cc])) / 8
+                v += wgt * c[(lat[k, 0] * L + lat[k, 1]) * L + lat[k, 2]]
+            ref[d] = v
+    np.testing.assert_allclose(zc, ref, rtol=0, atol=1e-13)
+
+
+def lognormal(ne, field_seed, p=4):
+    fs = dg.FS((ne + 1,) * 3, degree=p, perturb=0.1, seed=1)
+    grf = dg.grf_create(64, 2.0, 0.1, field_seed)
+    kq = torch.empty(fs.nq, dtype=torch.float64, device="cuda")
+    fs.lognormal(grf, kq)
+    op = fs.operator()
+    op.set_qdata(kq)
+    m = fs.matrix()
+    m.assemble(grf=grf)
+    return fs, op, m, grf
+
+
+def fgmres(op, m, b, net=None, prec=dg.dPREC_FP64):
+    ksp = dg.KSP(op, m, ksp_type=dg.dKSP_FGMRES, inner_prec=prec, restart=30)
+    if net is not None:
+        ksp.set_learned(net)
+    x = torch.zeros_like(b)
+    its, rn = ksp.solve(b, x, rtol=1e-8, maxit=3000)
+    r = torch.empty_like(x)
+    op.mult(x, r)
+    true = float(torch.linalg.norm(b - r) / torch.linalg.norm(b))
+    return its, true, ksp.stats()
+
+
+@pytest.fixture(scope="module")
+def trained():
+    ne = 10
+    fs0, _, _, _ = lognormal(ne, 11)
+    net = dg.Learned(fs0, seed=7)
+    for seed in (11, 12, 13, 14, 15):
+        fs, op, m, grf = lognormal(ne, seed)
+        net.set_field(grf)
+        ksp = dg.KSP(op, m, ksp_type=dg.dKSP_CG)
+        b = dev(np.random.default_rng(seed).uniform(-1, 1, fs.n))
+        net.collect(ksp, b, rtol=1e-10, every=1, max_pairs=120)
+    losses = net.train(epochs=40, batch=8, lr=1e-3, seed=1)
+    return net, losses, ne
+
+
+def test_training_reduces_the_loss(trained):
+    net, losses, _ = trained
+    assert net.npairs >= 300
+    assert losses[-1] < 0.5 * losses[0]
+
+
+def test_learned_correction_reduces_fgmres_iterations(trained):
+    net, _, ne = trained
+    fs, op, m, grf = lognormal(ne, 99)
+    net.set_field(grf)
+    b = dev(np.random.default_rng(99).uniform(-1, 1, fs.n))
+    its_plain, true_plain, _ = fgmres(op, m, b)
+    its_l, true_l, (_, rejects, active) = fgmres(op, m, b, net=net)
+    assert true_plain <= 1.01e-8 and true_l <= 1.01e-8
+    assert rejects == 0 and active
+    assert its_l <= 0.75 * its_plain, (its_l, its_plain)
+    # mixed precision with the correction also reaches the FP64 tolerance
+    its_m, true_m, _ = fgmres(op, m, b, net=net, prec=dg.dPREC_FP32)
+    assert true_m <= 1.01e-8 and its_m <= 0.8 * its_plain
+
+
+def test_fallback_to_plain_preconditioner(trained):
+    """a network that makes things worse is dropped by the restart judge; non-finite values are dropped"""
+    net, _, ne = trained
+    fs, op, m, grf = lognormal(ne, 98)
+    b = dev(np.random.default_rng(98).uniform(-1, 1, fs.n))
+    its_plain, _, _ = fgmres(op, m, b)
+    bad = dg.Learned(fs, seed=1)
+    bad.set_field(grf)
+    bad.set_weights(bad.get_weights() * 3.0, target_scale=1e3)
+    its_b, true_b, (_, rejects, _) = fgmres(op, m, b, net=bad)
+    assert true_b <= 1.01e-8
+    assert rejects >= 1 or its_b <= its_plain
+    w = bad.get_weights()
+    w[-1] = np.nan  # bias of the output layer
+    bad.set_weights(w, target_scale=1.0)
+    its_n, true_n, _ = fgmres(op, m, b, net=bad)
+    assert true_n <= 1.01e-8
+    assert bad.stats()[1] > 0
