@@ -17,7 +17,7 @@ FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std
 def _compile(src):
     obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
     path = os.path.join(CSRC, src)
-    deps = [path, os.path.join(CSRC, "internal.h"), os.path.join(HERE, "..", "include", "dohp_gb300.h")]
+    deps = [path, os.path.join(CSRC, "internal.h"), os.path.join(CSRC, "element.cuh"), os.path.join(HERE, "..", "include", "dohp_gb300.h")]
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj, ""
     cmd = [NVCC] + FLAGS + ["-c", path, "-o", obj]

@@ -21,7 +21,7 @@
 #include <fstream>
 #include <sstream>
 
-#include "internal.h"
+#include "element.cuh"
 
 using namespace dgb;
 
@@ -31,221 +31,14 @@ dErr fs_restrict32(_p_dFS *fs, const float *x, double *g, int add);
 
 namespace {
 
-struct HpArgs {
-  const int32_t *xstart, *qoff, *eptr, *ecol;
-  const double *eval;
-  int64_t n;
-  const double *x;
-  const double *const *px;  // graph form: x read through this table when non-null
-  const void *geo;
-  const double *tab_all;
-  void *yexp;
-  double lam, mu;
-};
-
-template <int N, typename T>
-__device__ __forceinline__ void load_tables(const double *tab_all, T *sB, T *sD) {
-  const double *tab = tab_all + (size_t)2 * (N - 2) * MAXP * MAXP;
-  for (int i = threadIdx.x; i < N * N; i += blockDim.x) {
-    sB[i] = (T)tab[i];
-    sD[i] = (T)tab[MAXP * MAXP + i];
-  }
-}
-
-// gather one component of the element's nodes through E (homogeneous Dirichlet: closure beyond n is 0)
-template <int N, typename T, int BS>
-__device__ __forceinline__ void gather(const HpArgs &A, const double *x, const int32_t *els, int ne, int d, T *dst) {
-  constexpr int N3 = N * N * N;
-  for (int t = threadIdx.x; t < ne * N3; t += blockDim.x) {
-    const int el = t / N3, r = t - el * N3;
-    const int64_t row = A.xstart[els[el]] + r;
-    double v = 0;
-    for (int32_t k = A.eptr[row]; k < A.eptr[row + 1]; k++) {
-      const int32_t c = A.ecol[k];
-      if (c < A.n) v += A.eval[k] * x[(int64_t)c * BS + d];
-    }
-    dst[t] = (T)v;
-  }
-}
-
-// three interpolation passes: in (S0) -> out (S1), using S0 as scratch
-template <int N, typename T>
-__device__ __forceinline__ void interp3(const T *sB, T *S0, T *S1, int tot, int cap) {
-  constexpr int N3 = N * N * N, NN = N * N;
-  (void)cap;
-  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-    const int el = t / N3, r = t - el * N3, a = r / NN, jk = r - a * NN;
-    const T *in = &S0[el * N3 + jk];
-    T s = 0;
-#pragma unroll
-    for (int i = 0; i < N; i++) s += sB[a * N + i] * in[i * NN];
-    S1[t] = s;
-  }
-  __syncthreads();
-  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-    const int el = t / N3, r = t - el * N3, a = r / NN, b = (r / N) % N, k = r % N;
-    const T *in = &S1[el * N3 + a * NN + k];
-    T s = 0;
-#pragma unroll
-    for (int j = 0; j < N; j++) s += sB[b * N + j] * in[j * N];
-    S0[t] = s;
-  }
-  __syncthreads();
-  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-    const int el = t / N3, r = t - el * N3, ab = r / N, c = r % N;
-    const T *in = &S0[el * N3 + ab * N];
-    T s = 0;
-#pragma unroll
-    for (int k = 0; k < N; k++) s += sB[c * N + k] * in[k];
-    S1[t] = s;
-  }
-  __syncthreads();
-}
-
-// transposed gradient (V0,V1,V2 -> S1) then three transposed interpolation passes to out (via S0)
-template <int N, typename T, int BS>
-__device__ __forceinline__ void back(const T *sB, const T *sD, const T *V0, const T *V1, const T *V2, T *S0, T *S1, int tot,
-                                     const HpArgs &A, const int32_t *els, int d, T *yexp) {
-  constexpr int N3 = N * N * N, NN = N * N;
-  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-    const int el = t / N3, r = t - el * N3, a = r / NN, b = (r / N) % N, c = r % N;
-    const T *v0 = &V0[el * N3], *v1 = &V1[el * N3], *v2 = &V2[el * N3];
-    T s = 0;
-#pragma unroll
-    for (int i = 0; i < N; i++) s += sD[i * N + a] * v0[i * NN + b * N + c] + sD[i * N + b] * v1[a * NN + i * N + c] + sD[i * N + c] * v2[a * NN + b * N + i];
-    S1[t] = s;
-  }
-  __syncthreads();
-  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-    const int el = t / N3, r = t - el * N3, ab = r / N, k = r % N;
-    const T *in = &S1[el * N3 + ab * N];
-    T s = 0;
-#pragma unroll
-    for (int c = 0; c < N; c++) s += sB[c * N + k] * in[c];
-    S0[t] = s;
-  }
-  __syncthreads();
-  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-    const int el = t / N3, r = t - el * N3, a = r / NN, j = (r / N) % N, k = r % N;
-    const T *in = &S0[el * N3 + a * NN + k];
-    T s = 0;
-#pragma unroll
-    for (int b = 0; b < N; b++) s += sB[b * N + j] * in[b * N];
-    S1[t] = s;
-  }
-  __syncthreads();
-  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-    const int el = t / N3, r = t - el * N3, i = r / NN, jk = r - i * NN;
-    const T *in = &S1[el * N3 + jk];
-    T s = 0;
-#pragma unroll
-    for (int a = 0; a < N; a++) s += sB[a * N + i] * in[a * NN];
-    yexp[((int64_t)A.xstart[els[el]] + r) * BS + d] = s;
-  }
-  __syncthreads();
-}
-
-// gradient at Gauss points of U (in S1) -> G0, G1, G2
-template <int N, typename T>
-__device__ __forceinline__ void grad(const T *sD, const T *S1, T *G0, T *G1, T *G2, int tot) {
-  constexpr int N3 = N * N * N, NN = N * N;
-  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-    const int el = t / N3, r = t - el * N3, a = r / NN, b = (r / N) % N, c = r % N;
-    const T *U = &S1[el * N3];
-    T g0 = 0, g1 = 0, g2 = 0;
-#pragma unroll
-    for (int i = 0; i < N; i++) {
-      g0 += sD[a * N + i] * U[i * NN + b * N + c];
-      g1 += sD[b * N + i] * U[a * NN + i * N + c];
-      g2 += sD[c * N + i] * U[a * NN + b * N + i];
-    }
-    G0[t] = g0;
-    G1[t] = g1;
-    G2[t] = g2;
-  }
-  __syncthreads();
-}
-
-// shared memory (in T) of one group: two basis tables + buffers
-__host__ __device__ constexpr int group_smem_elems(int N, int kind, int cap) {
-  return 2 * MAXP * MAXP + (kind == dOP_ELASTICITY ? 11 : 5) * cap * N * N * N;
-}
-
-template <int N, typename T, int KIND>
-__device__ void group_apply(const HpArgs &A, const int32_t *els, int ne, int cap, T *sm) {
-  constexpr int N3 = N * N * N;
-  T *sB = sm, *sD = sm + MAXP * MAXP, *buf = sm + 2 * MAXP * MAXP;
-  const int L = cap * N3, tot = ne * N3;
-  const double *x = A.px ? *A.px : A.x;
-  T *yexp = (T *)A.yexp;
-  load_tables<N, T>(A.tab_all, sB, sD);
-  if (KIND == dOP_DIFFUSION) {
-    T *S0 = buf, *S1 = buf + L, *G0 = buf + 2 * L, *G1 = buf + 3 * L, *G2 = buf + 4 * L;
-    gather<N, T, 1>(A, x, els, ne, 0, S0);
-    __syncthreads();
-    interp3<N, T>(sB, S0, S1, tot, cap);
-    grad<N, T>(sD, S1, G0, G1, G2, tot);
-    const T *geo = (const T *)A.geo;
-    for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-      const int el = t / N3, r = t - el * N3;
-      const T *G = geo + (int64_t)A.qoff[els[el]] * 6 + r;
-      const T g0 = G0[t], g1 = G1[t], g2 = G2[t];
-      const T a0 = G[0], a1 = G[N3], a2 = G[2 * N3], a3 = G[3 * N3], a4 = G[4 * N3], a5 = G[5 * N3];
-      G0[t] = a0 * g0 + a1 * g1 + a2 * g2;
-      G1[t] = a1 * g0 + a3 * g1 + a4 * g2;
-      G2[t] = a2 * g0 + a4 * g1 + a5 * g2;
-    }
-    __syncthreads();
-    back<N, T, 1>(sB, sD, G0, G1, G2, S0, S1, tot, A, els, 0, yexp);
-  } else {
-    T *S0 = buf, *S1 = buf + L, *G = buf + 2 * L;  // G: [d][k][L]
-    for (int d = 0; d < 3; d++) {
-      gather<N, T, 3>(A, x, els, ne, d, S0);
-      __syncthreads();
-      interp3<N, T>(sB, S0, S1, tot, cap);
-      grad<N, T>(sD, S1, G + (d * 3 + 0) * L, G + (d * 3 + 1) * L, G + (d * 3 + 2) * L, tot);
-    }
-    const T *geo = (const T *)A.geo;
-    const T lam = (T)A.lam, mu = (T)A.mu;
-    for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-      const int el = t / N3, r = t - el * N3;
-      const T *gq = geo + (int64_t)A.qoff[els[el]] * 10 + r;
-      T Ji[9];
-#pragma unroll
-      for (int i = 0; i < 9; i++) Ji[i] = gq[i * N3];
-      const T w = gq[9 * N3];
-      T Du[9];
-#pragma unroll
-      for (int d = 0; d < 3; d++) {
-        const T a0 = G[(d * 3 + 0) * L + t], a1 = G[(d * 3 + 1) * L + t], a2 = G[(d * 3 + 2) * L + t];
-#pragma unroll
-        for (int e = 0; e < 3; e++) Du[d * 3 + e] = a0 * Ji[0 * 3 + e] + a1 * Ji[1 * 3 + e] + a2 * Ji[2 * 3 + e];
-      }
-      const T e01 = (T)0.5 * (Du[1] + Du[3]), e02 = (T)0.5 * (Du[2] + Du[6]), e12 = (T)0.5 * (Du[5] + Du[7]);
-      const T tr = Du[0] + Du[4] + Du[8];
-      T S[9];
-      S[0] = w * (lam * tr + 2 * mu * Du[0]);
-      S[4] = w * (lam * tr + 2 * mu * Du[4]);
-      S[8] = w * (lam * tr + 2 * mu * Du[8]);
-      S[1] = S[3] = w * (2 * mu * e01);
-      S[2] = S[6] = w * (2 * mu * e02);
-      S[5] = S[7] = w * (2 * mu * e12);
-#pragma unroll
-      for (int d = 0; d < 3; d++)
-#pragma unroll
-        for (int k = 0; k < 3; k++) G[(d * 3 + k) * L + t] = S[d * 3 + 0] * Ji[k * 3 + 0] + S[d * 3 + 1] * Ji[k * 3 + 1] + S[d * 3 + 2] * Ji[k * 3 + 2];
-    }
-    __syncthreads();
-    for (int d = 0; d < 3; d++) back<N, T, 3>(sB, sD, G + (d * 3 + 0) * L, G + (d * 3 + 1) * L, G + (d * 3 + 2) * L, S0, S1, tot, A, els, d, yexp);
-  }
-}
+using HpArgs = ElemArgs;
 
 template <int N, typename T, int KIND>
 __global__ void __launch_bounds__(256) k_hp_bucket(HpArgs A, const int32_t *__restrict__ elist, int64_t count, int cap) {
   extern __shared__ unsigned char raw[];
   const int64_t g0 = (int64_t)blockIdx.x * cap;
   const int ne = (int)min((int64_t)cap, count - g0);
-  group_apply<N, T, KIND>(A, elist + g0, ne, cap, reinterpret_cast<T *>(raw));
+  group_apply<N, T, KIND>(A, elist + g0, 0, ne, cap, reinterpret_cast<T *>(raw));
 }
 
 // work item: x = nodes per direction, y = first element in elist, z = elements, w = group capacity
@@ -263,14 +56,14 @@ __global__ void __launch_bounds__(256) k_hp_persistent(HpArgs A, const int32_t *
     if (it >= nwork) break;
     const int4 w = work[it];
     switch (w.x) {
-      case 2: group_apply<2, T, KIND>(A, elist + w.y, w.z, w.w, sm); break;
-      case 3: group_apply<3, T, KIND>(A, elist + w.y, w.z, w.w, sm); break;
-      case 4: group_apply<4, T, KIND>(A, elist + w.y, w.z, w.w, sm); break;
-      case 5: group_apply<5, T, KIND>(A, elist + w.y, w.z, w.w, sm); break;
-      case 6: group_apply<6, T, KIND>(A, elist + w.y, w.z, w.w, sm); break;
-      case 7: group_apply<7, T, KIND>(A, elist + w.y, w.z, w.w, sm); break;
-      case 8: group_apply<8, T, KIND>(A, elist + w.y, w.z, w.w, sm); break;
-      case 9: group_apply<9, T, KIND>(A, elist + w.y, w.z, w.w, sm); break;
+      case 2: group_apply<2, T, KIND>(A, elist + w.y, 0, w.z, w.w, sm); break;
+      case 3: group_apply<3, T, KIND>(A, elist + w.y, 0, w.z, w.w, sm); break;
+      case 4: group_apply<4, T, KIND>(A, elist + w.y, 0, w.z, w.w, sm); break;
+      case 5: group_apply<5, T, KIND>(A, elist + w.y, 0, w.z, w.w, sm); break;
+      case 6: group_apply<6, T, KIND>(A, elist + w.y, 0, w.z, w.w, sm); break;
+      case 7: group_apply<7, T, KIND>(A, elist + w.y, 0, w.z, w.w, sm); break;
+      case 8: group_apply<8, T, KIND>(A, elist + w.y, 0, w.z, w.w, sm); break;
+      case 9: group_apply<9, T, KIND>(A, elist + w.y, 0, w.z, w.w, sm); break;
     }
     __syncthreads();
   }
@@ -413,6 +206,7 @@ static HpArgs make_args(_p_dOperator *op, const double *x, bool fp32, void *yexp
   A.eptr = fs->d_eptr;
   A.ecol = fs->d_ecol;
   A.eval = fs->d_eval;
+  A.emap = fs->d_emap;
   A.n = fs->n;
   A.x = x;
   A.px = px;

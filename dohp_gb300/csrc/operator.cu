@@ -15,7 +15,7 @@
 
 #include <mutex>
 
-#include "internal.h"
+#include "element.cuh"
 
 using namespace dgb;
 
@@ -102,288 +102,55 @@ __global__ void k_geometry(int64_t nelem, const int32_t *__restrict__ edeg, cons
   }
 }
 
-// ------------------------------------------------------------------------------------------ fused diffusion
+// ------------------------------------------------------------------------------------------ fused element apply
 // Elements per block chosen so a 256-thread block has a few hundred outputs per pass.
 template <int N>
 struct Tile {
-  static constexpr int N3 = N * N * N;
   static constexpr int EPB = N <= 2 ? 32 : N == 3 ? 16 : N == 4 ? 8 : N == 5 ? 4 : N <= 7 ? 2 : 1;
 };
-
-// y_exp = (B^T Dq^T) G (Dq B) E x for a uniform-degree scalar space; T = arithmetic type
-template <int N, typename T>
-__global__ void __launch_bounds__(256) k_diffusion(int64_t nelem, const int32_t *__restrict__ emap, int64_t n,
-                                                   const double *__restrict__ x, const T *__restrict__ geo,
-                                                   const double *__restrict__ tab, T *__restrict__ yexp) {
-  constexpr int N3 = Tile<N>::N3, EPB = Tile<N>::EPB, NN = N * N;
-  __shared__ T sB[NN], sD[NN];
-  __shared__ T S[4][EPB * N3];
-  const int tid = threadIdx.x;
-  const int64_t e0 = (int64_t)blockIdx.x * EPB;
-  const int ne = (int)min((int64_t)EPB, nelem - e0);
-  const int tot = ne * N3;
-  for (int i = tid; i < NN; i += blockDim.x) {
-    sB[i] = (T)tab[i];
-    sD[i] = (T)tab[MAXP * MAXP + i];
-  }
-  // gather through E (homogeneous Dirichlet: closure entries beyond n are zero)
-  for (int t = tid; t < tot; t += blockDim.x) {
-    const int32_t c = emap[e0 * N3 + t];
-    S[0][t] = c < n ? (T)x[c] : (T)0;
-  }
-  __syncthreads();
-  // interpolate to Gauss points: x pass, y pass, z pass
-  for (int t = tid; t < tot; t += blockDim.x) {
-    const int el = t / N3, r = t - el * N3, a = r / NN, jk = r - a * NN;
-    const T *in = &S[0][el * N3 + jk];
-    T s = 0;
-#pragma unroll
-    for (int i = 0; i < N; i++) s += sB[a * N + i] * in[i * NN];
-    S[1][t] = s;
-  }
-  __syncthreads();
-  for (int t = tid; t < tot; t += blockDim.x) {
-    const int el = t / N3, r = t - el * N3, a = r / NN, b = (r / N) % N, k = r % N;
-    const T *in = &S[1][el * N3 + a * NN + k];
-    T s = 0;
-#pragma unroll
-    for (int j = 0; j < N; j++) s += sB[b * N + j] * in[j * N];
-    S[0][t] = s;
-  }
-  __syncthreads();
-  for (int t = tid; t < tot; t += blockDim.x) {
-    const int el = t / N3, r = t - el * N3, ab = r / N, c = r % N;
-    const T *in = &S[0][el * N3 + ab * N];
-    T s = 0;
-#pragma unroll
-    for (int k = 0; k < N; k++) s += sB[c * N + k] * in[k];
-    S[1][t] = s;
-  }
-  __syncthreads();
-  // reference gradient at the points, pointwise q-function dv = G grad u, stored in S0 (x), S2 (y), S3 (z)
-  for (int t = tid; t < tot; t += blockDim.x) {
-    const int el = t / N3, r = t - el * N3, a = r / NN, b = (r / N) % N, c = r % N;
-    const T *U = &S[1][el * N3];
-    T g0 = 0, g1 = 0, g2 = 0;
-#pragma unroll
-    for (int i = 0; i < N; i++) {
-      g0 += sD[a * N + i] * U[i * NN + b * N + c];
-      g1 += sD[b * N + i] * U[a * NN + i * N + c];
-      g2 += sD[c * N + i] * U[a * NN + b * N + i];
-    }
-    const T *G = geo + (e0 + el) * 6 * N3 + r;
-    const T G0 = G[0], G1 = G[N3], G2 = G[2 * N3], G3 = G[3 * N3], G4 = G[4 * N3], G5 = G[5 * N3];
-    S[0][t] = G0 * g0 + G1 * g1 + G2 * g2;
-    S[2][t] = G1 * g0 + G3 * g1 + G4 * g2;
-    S[3][t] = G2 * g0 + G4 * g1 + G5 * g2;
-  }
-  __syncthreads();
-  // transposed gradient back to Gauss-point values
-  for (int t = tid; t < tot; t += blockDim.x) {
-    const int el = t / N3, r = t - el * N3, a = r / NN, b = (r / N) % N, c = r % N;
-    const T *V0 = &S[0][el * N3], *V1 = &S[2][el * N3], *V2 = &S[3][el * N3];
-    T s = 0;
-#pragma unroll
-    for (int i = 0; i < N; i++)
-      s += sD[i * N + a] * V0[i * NN + b * N + c] + sD[i * N + b] * V1[a * NN + i * N + c] + sD[i * N + c] * V2[a * NN + b * N + i];
-    S[1][t] = s;
-  }
-  __syncthreads();
-  // B^T along z, y, x
-  for (int t = tid; t < tot; t += blockDim.x) {
-    const int el = t / N3, r = t - el * N3, ab = r / N, k = r % N;
-    const T *in = &S[1][el * N3 + ab * N];
-    T s = 0;
-#pragma unroll
-    for (int c = 0; c < N; c++) s += sB[c * N + k] * in[c];
-    S[0][t] = s;
-  }
-  __syncthreads();
-  for (int t = tid; t < tot; t += blockDim.x) {
-    const int el = t / N3, r = t - el * N3, a = r / NN, j = (r / N) % N, k = r % N;
-    const T *in = &S[0][el * N3 + a * NN + k];
-    T s = 0;
-#pragma unroll
-    for (int b = 0; b < N; b++) s += sB[b * N + j] * in[b * N];
-    S[1][t] = s;
-  }
-  __syncthreads();
-  for (int t = tid; t < tot; t += blockDim.x) {
-    const int el = t / N3, r = t - el * N3, i = r / NN, jk = r - i * NN;
-    const T *in = &S[1][el * N3 + jk];
-    T s = 0;
-#pragma unroll
-    for (int a = 0; a < N; a++) s += sB[a * N + i] * in[a * NN];
-    yexp[e0 * N3 + t] = s;
-  }
-}
-
-template <int N, typename T>
-dErr launch_diffusion(_p_dFS *fs, const double *x, const T *geo, T *yexp) {
-  constexpr int EPB = Tile<N>::EPB;
-  const unsigned grid = (unsigned)((fs->nelem + EPB - 1) / EPB);
-  const double *tab = fs->d_fast_tab + (size_t)2 * (N - 2) * MAXP * MAXP;
-  k_diffusion<N, T><<<grid, 256, 0, fs->stream>>>(fs->nelem, fs->d_emap, fs->n, x, geo, tab, yexp);
-  CUCHK(cudaGetLastError());
-  return 0;
-}
-
-// ------------------------------------------------------------------------------------------ fused elasticity
-// ElastPointwiseJacobian at F = I (src/fs/tests/elast.c:269-280): eps = sym(grad u),
-// dv = w (lambda tr(eps) I + 2 mu eps). Three components (bs = 3, interleaved), geometry {J^-1, w det J}.
 template <int N>
 struct ETile {
   static constexpr int EPB = N <= 3 ? 8 : N == 4 ? 4 : N == 5 ? 2 : 1;
 };
 
+// y_exp = (B^T Dq^T) G (Dq B) E x for cap consecutive elements per block (uniform order, Boolean E)
+template <int N, typename T, int KIND>
+__global__ void __launch_bounds__(256) k_uniform(ElemArgs A, int64_t nelem, int cap) {
+  extern __shared__ unsigned char raw[];
+  const int64_t e0 = (int64_t)blockIdx.x * cap;
+  const int ne = (int)min((int64_t)cap, nelem - e0);
+  group_apply<N, T, KIND>(A, nullptr, e0, ne, cap, reinterpret_cast<T *>(raw));
+}
+
+template <int N, typename T, int KIND>
+dErr launch_uniform(_p_dFS *fs, const double *x, const T *geo, double lam, double mu, T *yexp) {
+  constexpr int cap = KIND == dOP_ELASTICITY ? ETile<N>::EPB : Tile<N>::EPB;
+  ElemArgs A{};
+  A.xstart = fs->d_xstart;
+  A.qoff = fs->d_qoff;
+  A.emap = fs->d_emap;
+  A.n = fs->n;
+  A.x = x;
+  A.geo = geo;
+  A.tab_all = fs->d_fast_tab;
+  A.yexp = yexp;
+  A.lam = lam;
+  A.mu = mu;
+  const size_t smem = (size_t)group_smem_elems(N, KIND, cap) * sizeof(T);
+  CUCHK(cudaFuncSetAttribute(k_uniform<N, T, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_uniform<N, T, KIND><<<(unsigned)((fs->nelem + cap - 1) / cap), 256, smem, fs->stream>>>(A, fs->nelem, cap);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
 template <int N, typename T>
-__global__ void __launch_bounds__(256) k_elasticity(int64_t nelem, const int32_t *__restrict__ emap, int64_t n,
-                                                    const double *__restrict__ x, const T *__restrict__ geo,
-                                                    const double *__restrict__ tab, T lam, T mu, T *__restrict__ yexp) {
-  constexpr int N3 = N * N * N, EPB = ETile<N>::EPB, NN = N * N, L = EPB * N3;
-  __shared__ T sB[NN], sD[NN];
-  extern __shared__ unsigned char smraw[];
-  T *A = reinterpret_cast<T *>(smraw), *Bf = A + L, *G = Bf + L;  // ping, pong, 9 gradient buffers [d][k][L]
-  const int tid = threadIdx.x;
-  const int64_t e0 = (int64_t)blockIdx.x * EPB;
-  const int ne = (int)min((int64_t)EPB, nelem - e0);
-  const int tot = ne * N3;
-  for (int i = tid; i < NN; i += blockDim.x) {
-    sB[i] = (T)tab[i];
-    sD[i] = (T)tab[MAXP * MAXP + i];
-  }
-  __syncthreads();
-  for (int d = 0; d < 3; d++) {
-    for (int t = tid; t < tot; t += blockDim.x) {
-      const int32_t c = emap[e0 * N3 + t];
-      A[t] = c < n ? (T)x[(int64_t)c * 3 + d] : (T)0;
-    }
-    __syncthreads();
-    for (int t = tid; t < tot; t += blockDim.x) {
-      const int el = t / N3, r = t - el * N3, a = r / NN, jk = r - a * NN;
-      const T *in = &A[el * N3 + jk];
-      T s = 0;
-#pragma unroll
-      for (int i = 0; i < N; i++) s += sB[a * N + i] * in[i * NN];
-      Bf[t] = s;
-    }
-    __syncthreads();
-    for (int t = tid; t < tot; t += blockDim.x) {
-      const int el = t / N3, r = t - el * N3, a = r / NN, b = (r / N) % N, k = r % N;
-      const T *in = &Bf[el * N3 + a * NN + k];
-      T s = 0;
-#pragma unroll
-      for (int j = 0; j < N; j++) s += sB[b * N + j] * in[j * N];
-      A[t] = s;
-    }
-    __syncthreads();
-    for (int t = tid; t < tot; t += blockDim.x) {
-      const int el = t / N3, r = t - el * N3, ab = r / N, c = r % N;
-      const T *in = &A[el * N3 + ab * N];
-      T s = 0;
-#pragma unroll
-      for (int k = 0; k < N; k++) s += sB[c * N + k] * in[k];
-      Bf[t] = s;
-    }
-    __syncthreads();
-    for (int t = tid; t < tot; t += blockDim.x) {
-      const int el = t / N3, r = t - el * N3, a = r / NN, b = (r / N) % N, c = r % N;
-      const T *U = &Bf[el * N3];
-      T g0 = 0, g1 = 0, g2 = 0;
-#pragma unroll
-      for (int i = 0; i < N; i++) {
-        g0 += sD[a * N + i] * U[i * NN + b * N + c];
-        g1 += sD[b * N + i] * U[a * NN + i * N + c];
-        g2 += sD[c * N + i] * U[a * NN + b * N + i];
-      }
-      G[(d * 3 + 0) * L + t] = g0;
-      G[(d * 3 + 1) * L + t] = g1;
-      G[(d * 3 + 2) * L + t] = g2;
-    }
-    __syncthreads();
-  }
-  // pointwise: physical gradient, strain, stress, back to reference directions
-  for (int t = tid; t < tot; t += blockDim.x) {
-    const int el = t / N3, r = t - el * N3;
-    const T *gq = geo + (e0 + el) * 10 * N3 + r;
-    T Ji[9];
-#pragma unroll
-    for (int i = 0; i < 9; i++) Ji[i] = gq[i * N3];
-    const T w = gq[9 * N3];
-    T Du[9];
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-      const T a0 = G[(d * 3 + 0) * L + t], a1 = G[(d * 3 + 1) * L + t], a2 = G[(d * 3 + 2) * L + t];
-#pragma unroll
-      for (int e = 0; e < 3; e++) Du[d * 3 + e] = a0 * Ji[0 * 3 + e] + a1 * Ji[1 * 3 + e] + a2 * Ji[2 * 3 + e];
-    }
-    const T e00 = Du[0], e11 = Du[4], e22 = Du[8];
-    const T e01 = (T)0.5 * (Du[1] + Du[3]), e02 = (T)0.5 * (Du[2] + Du[6]), e12 = (T)0.5 * (Du[5] + Du[7]);
-    const T tr = e00 + e11 + e22;
-    T S[9];
-    S[0] = w * (lam * tr + 2 * mu * e00);
-    S[4] = w * (lam * tr + 2 * mu * e11);
-    S[8] = w * (lam * tr + 2 * mu * e22);
-    S[1] = S[3] = w * (2 * mu * e01);
-    S[2] = S[6] = w * (2 * mu * e02);
-    S[5] = S[7] = w * (2 * mu * e12);
-#pragma unroll
-    for (int d = 0; d < 3; d++)
-#pragma unroll
-      for (int k = 0; k < 3; k++) G[(d * 3 + k) * L + t] = S[d * 3 + 0] * Ji[k * 3 + 0] + S[d * 3 + 1] * Ji[k * 3 + 1] + S[d * 3 + 2] * Ji[k * 3 + 2];
-  }
-  __syncthreads();
-  for (int d = 0; d < 3; d++) {
-    for (int t = tid; t < tot; t += blockDim.x) {
-      const int el = t / N3, r = t - el * N3, a = r / NN, b = (r / N) % N, c = r % N;
-      const T *V0 = &G[(d * 3 + 0) * L + el * N3], *V1 = &G[(d * 3 + 1) * L + el * N3], *V2 = &G[(d * 3 + 2) * L + el * N3];
-      T s = 0;
-#pragma unroll
-      for (int i = 0; i < N; i++)
-        s += sD[i * N + a] * V0[i * NN + b * N + c] + sD[i * N + b] * V1[a * NN + i * N + c] + sD[i * N + c] * V2[a * NN + b * N + i];
-      A[t] = s;
-    }
-    __syncthreads();
-    for (int t = tid; t < tot; t += blockDim.x) {
-      const int el = t / N3, r = t - el * N3, ab = r / N, k = r % N;
-      const T *in = &A[el * N3 + ab * N];
-      T s = 0;
-#pragma unroll
-      for (int c = 0; c < N; c++) s += sB[c * N + k] * in[c];
-      Bf[t] = s;
-    }
-    __syncthreads();
-    for (int t = tid; t < tot; t += blockDim.x) {
-      const int el = t / N3, r = t - el * N3, a = r / NN, j = (r / N) % N, k = r % N;
-      const T *in = &Bf[el * N3 + a * NN + k];
-      T s = 0;
-#pragma unroll
-      for (int b = 0; b < N; b++) s += sB[b * N + j] * in[b * N];
-      A[t] = s;
-    }
-    __syncthreads();
-    for (int t = tid; t < tot; t += blockDim.x) {
-      const int el = t / N3, r = t - el * N3, i = r / NN, jk = r - i * NN;
-      const T *in = &A[el * N3 + jk];
-      T s = 0;
-#pragma unroll
-      for (int a = 0; a < N; a++) s += sB[a * N + i] * in[a * NN];
-      yexp[(e0 * N3 + t) * 3 + d] = s;
-    }
-    __syncthreads();
-  }
+dErr launch_diffusion(_p_dFS *fs, const double *x, const T *geo, T *yexp) {
+  return launch_uniform<N, T, dOP_DIFFUSION>(fs, x, geo, 0, 0, yexp);
 }
 
 template <int N, typename T>
 dErr launch_elasticity(_p_dFS *fs, const double *x, const T *geo, T lam, T mu, T *yexp) {
-  constexpr int EPB = ETile<N>::EPB;
-  const unsigned grid = (unsigned)((fs->nelem + EPB - 1) / EPB);
-  const double *tab = fs->d_fast_tab + (size_t)2 * (N - 2) * MAXP * MAXP;
-  const size_t smem = (size_t)11 * EPB * N * N * N * sizeof(T);
-  CUCHK(cudaFuncSetAttribute(k_elasticity<N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_elasticity<N, T><<<grid, 256, smem, fs->stream>>>(fs->nelem, fs->d_emap, fs->n, x, geo, tab, lam, mu, yexp);
-  CUCHK(cudaGetLastError());
-  return 0;
+  return launch_uniform<N, T, dOP_ELASTICITY>(fs, x, geo, lam, mu, yexp);
 }
 
 }  // namespace
