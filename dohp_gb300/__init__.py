@@ -429,8 +429,10 @@ class Learned:
         return a.value, d.value
 
 
-def _ksp_set_learned(self, net):
+def _ksp_set_learned(self, net, policy=2):
+    """policy: 0 every preconditioner application, 1 first vector of each restart cycle, 2 adaptive"""
     chk(lib().dKSPSetLearnedCorrection(self.h, None if net is None else net.h))
+    chk(lib().dKSPSetCorrectionPolicy(self.h, ctypes.c_int(policy)))
     self.net = net
 
 

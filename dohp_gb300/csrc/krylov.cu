@@ -256,6 +256,10 @@ struct _p_dKSP {
   dErr (*correction)(void *ctx, const double *r, double *z) = nullptr;
   void *correction_ctx = nullptr;
   bool correction_on = false;
+  // 0: every preconditioner application; 1: first vector of each restart cycle (the true residual);
+  // 2: adaptive -- one cycle of each, then the one that reduced the residual more
+  int correction_policy = 2, active_policy = 0;
+  int cycle_pos = 0;  // position of the vector being preconditioned within the FGMRES cycle
   int64_t pc_applies = 0, correction_rejects = 0;
   // optional per-iteration monitor (CG: after every iterate, with x and r)
   dErr (*monitor)(void *ctx, int it, const double *x, const double *r) = nullptr;
@@ -358,7 +362,8 @@ static dErr pc_apply_plain(_p_dKSP *k, const double *r, double *z);
 static dErr pc_apply(_p_dKSP *k, const double *r, double *z) {
   k->pc_applies++;
   DCHK(pc_apply_plain(k, r, z));
-  if (k->correction && k->correction_on) DCHK(k->correction(k->correction_ctx, r, z));
+  if (k->correction && k->correction_on && (k->active_policy == 0 || k->cycle_pos == 0))
+    DCHK(k->correction(k->correction_ctx, r, z));
   return 0;
 }
 
@@ -459,8 +464,8 @@ static dErr fgmres_solve(_p_dKSP *k, const double *b, double *x, double rtol, in
   DCHK(device_dot(n, b, b, k->d_part, k->d_s, s));
   DCHK(read_scalar(k->d_s, &bb, s));
   const double bn = sqrt(bb) > 0 ? sqrt(bb) : 1.0;
-  int total = 0;
-  double res = 0, prev = -1;
+  int total = 0, cycle = 0;
+  double res = 0, prev = -1, rho[2] = {-1, -1};
   k->correction_on = k->correction != nullptr;
   for (;;) {
     DCHK(op_mult_prec(k->op, x, V, dPREC_FP64));
@@ -477,6 +482,12 @@ static dErr fgmres_solve(_p_dKSP *k, const double *b, double *x, double rtol, in
       k->correction_on = false;
       k->correction_rejects++;
     }
+    if (k->correction_on && prev > 0 && rho[k->active_policy] < 0) rho[k->active_policy] = beta / prev;
+    if (k->correction_policy == 2)
+      k->active_policy = cycle == 0 ? 0 : cycle == 1 ? 1 : (rho[0] >= 0 && (rho[1] < 0 || rho[0] <= rho[1]) ? 0 : 1);
+    else
+      k->active_policy = k->correction_policy;
+    cycle++;
     prev = beta;
     k_scale_into<<<nb(n), 256, 0, s>>>(n, V, nullptr, 1.0 / beta, V);
     std::fill(g.begin(), g.end(), 0.0);
@@ -484,6 +495,7 @@ static dErr fgmres_solve(_p_dKSP *k, const double *b, double *x, double rtol, in
     int j = 0;
     for (; j < m && total < maxit;) {
       double *w = V + (size_t)(j + 1) * n;
+      k->cycle_pos = j;
       DCHK(pc_apply(k, V + (size_t)j * n, Z + (size_t)j * n));
       DCHK(op_mult_prec(k->op, Z + (size_t)j * n, w, k->pc_prec));
       const int nv = j + 1;
@@ -580,6 +592,13 @@ dErr dKSPSetOptions(dKSP ksp, dInt cheb_degree, dPrecision pc_precision, dInt re
   cudaFree(ksp->d_dinv32);
   cudaFree(ksp->d_val32);
   ksp->d_w32 = nullptr, ksp->d_dinv32 = nullptr, ksp->d_val32 = nullptr;
+  return 0;
+}
+
+dErr dKSPSetCorrectionPolicy(dKSP ksp, int policy) {
+  if (!ksp) return set_error("null KSP");
+  if (policy < 0 || policy > 2) return set_error("correction policy %d not in {0, 1, 2}", policy);
+  ksp->correction_policy = policy;
   return 0;
 }
 

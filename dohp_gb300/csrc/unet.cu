@@ -178,53 +178,226 @@ __global__ void __launch_bounds__(128) k_conv_bwd_data(int B, int Ci, int Co, Di
   }
 }
 
-// weight and bias gradient partial sums over a chunk of output voxels: one (co, ci) pair per block.
-// partial layout [chunk][Co*Ci*27 + Co]
-__global__ void __launch_bounds__(256) k_conv_bwd_weight(int B, int Ci, int Co, Dims di, Dims dout, int stride,
-                                                         const float *__restrict__ x, const float *__restrict__ gy, int64_t chunk,
-                                                         float *__restrict__ partial) {
-  __shared__ float red[28][257];
-  const int pair = blockIdx.x, co = pair / Ci, ci = pair % Ci;
-  const int64_t nvo = dout.n(), nvi = di.n(), total = (int64_t)B * nvo;
-  const int64_t v0 = blockIdx.y * chunk, v1 = min(total, v0 + chunk);
-  float acc[28];
+// Register-blocked forms: a thread computes VZ consecutive outputs along z, so every weight read from
+// shared memory feeds VZ multiply-adds and the 3 x 3 x ZW input window is shared by the VZ outputs.
+constexpr int VZ = 4;
+constexpr int64_t kQuadChunk = 4096;  // z-quads of output voxels per weight-gradient block
+
+__device__ __forceinline__ void quad(int64_t r, Dims d, int nzq, int &ox, int &oy, int &oz0) {
+  oz0 = (int)(r % nzq) * VZ;
+  r /= nzq;
+  oy = (int)(r % d.y);
+  ox = (int)(r / d.y);
+}
+
+template <int S>
+__device__ __forceinline__ void load_window(const float *__restrict__ xc, Dims di, int ox, int oy, int oz0,
+                                            float (&w)[3][3][(VZ - 1) * S + 3]) {
+  constexpr int ZW = (VZ - 1) * S + 3;
 #pragma unroll
-  for (int i = 0; i < 28; i++) acc[i] = 0.f;
-  for (int64_t v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
-    const int64_t b = v / nvo, r = v % nvo;
-    const float g = gy[((size_t)b * Co + co) * nvo + r];
-    if (g == 0.f) continue;
-    int ox, oy, oz;
-    vox(r, dout, ox, oy, oz);
-    const float *xc = x + ((size_t)b * Ci + ci) * nvi;
+  for (int a = 0; a < 3; a++) {
+    const int ix = ox * S + a - 1;
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-      const int ix = ox * stride + a - 1;
+    for (int b = 0; b < 3; b++) {
+      const int iy = oy * S + b - 1;
+      const bool row = ix >= 0 && ix < di.x && iy >= 0 && iy < di.y;
+      const float *xr = xc + ((int64_t)ix * di.y + iy) * di.z;
 #pragma unroll
-      for (int bb = 0; bb < 3; bb++) {
-        const int iy = oy * stride + bb - 1;
-#pragma unroll
-        for (int cc = 0; cc < 3; cc++) {
-          const int iz = oz * stride + cc - 1;
-          const bool in = ix >= 0 && ix < di.x && iy >= 0 && iy < di.y && iz >= 0 && iz < di.z;
-          if (in) acc[(a * 3 + bb) * 3 + cc] = fmaf(g, xc[((int64_t)ix * di.y + iy) * di.z + iz], acc[(a * 3 + bb) * 3 + cc]);
-        }
+      for (int z = 0; z < ZW; z++) {
+        const int iz = oz0 * S - 1 + z;
+        w[a][b][z] = row && iz >= 0 && iz < di.z ? xr[iz] : 0.f;
       }
     }
-    acc[27] += g;
   }
+}
+
+template <int CO_T, int S>
+__global__ void __launch_bounds__(128) k_conv_fwd_rb(int B, int Ci, int Co, Dims di, Dims dout, const float *__restrict__ x,
+                                                     const __nv_bfloat16 *__restrict__ W, const float *__restrict__ bias, int relu,
+                                                     float *__restrict__ y) {
+  constexpr int CK = 8, ZW = (VZ - 1) * S + 3;
+  __shared__ float sW[CO_T][CK][27];
+  const int nzq = (dout.z + VZ - 1) / VZ;
+  const int64_t nq = (int64_t)dout.x * dout.y * nzq, nvo = dout.n(), nvi = di.n();
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool active = t < (int64_t)B * nq;
+  const int co0 = blockIdx.y * CO_T;
+  const int64_t b = active ? t / nq : 0;
+  int ox, oy, oz0;
+  quad(active ? t % nq : 0, dout, nzq, ox, oy, oz0);
+  float acc[CO_T][VZ];
 #pragma unroll
-  for (int i = 0; i < 28; i++) red[i][threadIdx.x] = acc[i];
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s)
-      for (int i = 0; i < 28; i++) red[i][threadIdx.x] += red[i][threadIdx.x + s];
+  for (int c = 0; c < CO_T; c++)
+#pragma unroll
+    for (int v = 0; v < VZ; v++) acc[c][v] = (co0 + c < Co) ? bias[co0 + c] : 0.f;
+  for (int ci0 = 0; ci0 < Ci; ci0 += CK) {
     __syncthreads();
+    for (int i = threadIdx.x; i < CO_T * CK * 27; i += blockDim.x) {
+      const int c = i / (CK * 27), rr = i % (CK * 27), k = rr / 27, tap = rr % 27;
+      sW[c][k][tap] = (co0 + c < Co && ci0 + k < Ci) ? __bfloat162float(W[((size_t)(co0 + c) * Ci + ci0 + k) * 27 + tap]) : 0.f;
+    }
+    __syncthreads();
+    if (!active) continue;
+    const int kmax = min(CK, Ci - ci0);
+    for (int k = 0; k < kmax; k++) {
+      float xw[3][3][ZW];
+      load_window<S>(x + ((size_t)b * Ci + ci0 + k) * nvi, di, ox, oy, oz0, xw);
+#pragma unroll
+      for (int c = 0; c < CO_T; c++)
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+          for (int bb = 0; bb < 3; bb++)
+#pragma unroll
+            for (int cc = 0; cc < 3; cc++) {
+              const float w = sW[c][k][(a * 3 + bb) * 3 + cc];
+#pragma unroll
+              for (int v = 0; v < VZ; v++) acc[c][v] = fmaf(w, xw[a][bb][v * S + cc], acc[c][v]);
+            }
+    }
   }
-  const int64_t np = (int64_t)Co * Ci * 27 + Co;
-  float *pp = partial + blockIdx.y * np;
-  if (threadIdx.x < 27) pp[(int64_t)pair * 27 + threadIdx.x] = red[threadIdx.x][0];
-  if (threadIdx.x == 27 && ci == 0) pp[(int64_t)Co * Ci * 27 + co] = red[27][0];
+  if (!active) return;
+  float *yo = y + (size_t)b * Co * nvo + ((int64_t)ox * dout.y + oy) * dout.z + oz0;
+#pragma unroll
+  for (int c = 0; c < CO_T; c++) {
+    if (co0 + c >= Co) break;
+#pragma unroll
+    for (int v = 0; v < VZ; v++)
+      if (oz0 + v < dout.z) yo[(size_t)(co0 + c) * nvo + v] = relu ? fmaxf(acc[c][v], 0.f) : acc[c][v];
+  }
+}
+
+// stride-1 data gradient: gx[ci][u] = sum_co sum_taps W[co][ci][t] gy[co][u + 1 - t] (flipped window of gy)
+template <int CI_T>
+__global__ void __launch_bounds__(128) k_conv_bwd_data_rb(int B, int Ci, int Co, Dims d, const float *__restrict__ gy,
+                                                          const __nv_bfloat16 *__restrict__ W, float *__restrict__ gx, int accumulate) {
+  constexpr int CK = 8, ZW = VZ + 2;
+  __shared__ float sW[CK][CI_T][27];
+  const int nzq = (d.z + VZ - 1) / VZ;
+  const int64_t nq = (int64_t)d.x * d.y * nzq, nv = d.n();
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool active = t < (int64_t)B * nq;
+  const int ci0 = blockIdx.y * CI_T;
+  const int64_t b = active ? t / nq : 0;
+  int ix, iy, iz0;
+  quad(active ? t % nq : 0, d, nzq, ix, iy, iz0);
+  float acc[CI_T][VZ];
+#pragma unroll
+  for (int c = 0; c < CI_T; c++)
+#pragma unroll
+    for (int v = 0; v < VZ; v++) acc[c][v] = 0.f;
+  for (int co0 = 0; co0 < Co; co0 += CK) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < CK * CI_T * 27; i += blockDim.x) {
+      const int k = i / (CI_T * 27), rr = i % (CI_T * 27), c = rr / 27, tap = rr % 27;
+      sW[k][c][tap] = (co0 + k < Co && ci0 + c < Ci) ? __bfloat162float(W[((size_t)(co0 + k) * Ci + ci0 + c) * 27 + tap]) : 0.f;
+    }
+    __syncthreads();
+    if (!active) continue;
+    const int kmax = min(CK, Co - co0);
+    for (int k = 0; k < kmax; k++) {
+      float gw[3][3][ZW];  // gy at (ix - 1 + a', iy - 1 + b', iz0 - 1 + z')
+      load_window<1>(gy + ((size_t)b * Co + co0 + k) * nv, d, ix, iy, iz0, gw);
+#pragma unroll
+      for (int c = 0; c < CI_T; c++)
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+          for (int bb = 0; bb < 3; bb++)
+#pragma unroll
+            for (int cc = 0; cc < 3; cc++) {
+              const float w = sW[k][c][(a * 3 + bb) * 3 + cc];
+#pragma unroll
+              for (int v = 0; v < VZ; v++) acc[c][v] = fmaf(w, gw[2 - a][2 - bb][v + 2 - cc], acc[c][v]);
+            }
+    }
+  }
+  if (!active) return;
+  float *go = gx + (size_t)b * Ci * nv + ((int64_t)ix * d.y + iy) * d.z + iz0;
+#pragma unroll
+  for (int c = 0; c < CI_T; c++) {
+    if (ci0 + c >= Ci) break;
+#pragma unroll
+    for (int v = 0; v < VZ; v++)
+      if (iz0 + v < d.z) {
+        float *o = go + (size_t)(ci0 + c) * nv + v;
+        *o = accumulate ? *o + acc[c][v] : acc[c][v];
+      }
+  }
+}
+
+// weight and bias gradient partial sums: CG output channels and one input channel per block, a chunk of
+// output z-quads; partial layout [chunk][Co*Ci*27 + Co]
+template <int CG, int S>
+__global__ void __launch_bounds__(256) k_conv_bwd_weight_rb(int B, int Ci, int Co, Dims di, Dims dout, const float *__restrict__ x,
+                                                            const float *__restrict__ gy, float *__restrict__ partial) {
+  constexpr int ZW = (VZ - 1) * S + 3, NV = CG * 28;
+  __shared__ float red[8][NV];
+  const int pair = blockIdx.x, cg = pair / Ci, ci = pair % Ci, co0 = cg * CG;
+  const int nzq = (dout.z + VZ - 1) / VZ;
+  const int64_t nq = (int64_t)dout.x * dout.y * nzq, nvo = dout.n(), nvi = di.n(), total = (int64_t)B * nq;
+  const int64_t q0 = blockIdx.y * kQuadChunk, q1 = min(total, q0 + kQuadChunk);
+  float acc[CG][28];
+#pragma unroll
+  for (int c = 0; c < CG; c++)
+#pragma unroll
+    for (int i = 0; i < 28; i++) acc[c][i] = 0.f;
+  for (int64_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
+    const int64_t b = q / nq;
+    int ox, oy, oz0;
+    quad(q % nq, dout, nzq, ox, oy, oz0);
+    float g[CG][VZ];
+    bool any = false;
+#pragma unroll
+    for (int c = 0; c < CG; c++) {
+      const float *gr = gy + ((size_t)b * Co + co0 + c) * nvo + ((int64_t)ox * dout.y + oy) * dout.z + oz0;
+#pragma unroll
+      for (int v = 0; v < VZ; v++) {
+        g[c][v] = oz0 + v < dout.z ? gr[v] : 0.f;
+        any |= g[c][v] != 0.f;
+      }
+    }
+    if (!any) continue;
+    float xw[3][3][ZW];
+    load_window<S>(x + ((size_t)b * Ci + ci) * nvi, di, ox, oy, oz0, xw);
+#pragma unroll
+    for (int c = 0; c < CG; c++) {
+#pragma unroll
+      for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int bb = 0; bb < 3; bb++)
+#pragma unroll
+          for (int cc = 0; cc < 3; cc++) {
+            float s = acc[c][(a * 3 + bb) * 3 + cc];
+#pragma unroll
+            for (int v = 0; v < VZ; v++) s = fmaf(g[c][v], xw[a][bb][v * S + cc], s);
+            acc[c][(a * 3 + bb) * 3 + cc] = s;
+          }
+#pragma unroll
+      for (int v = 0; v < VZ; v++) acc[c][27] += g[c][v];
+    }
+  }
+  // warp sums, then the 8 warp partials in order
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < CG; c++)
+#pragma unroll
+    for (int i = 0; i < 28; i++) {
+      float v = acc[c][i];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) red[wp][c * 28 + i] = v;
+    }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    float s = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[w][threadIdx.x];
+    const int c = threadIdx.x / 28, i = threadIdx.x % 28;
+    const int64_t np = (int64_t)Co * Ci * 27 + Co;
+    float *pp = partial + blockIdx.y * np;
+    if (i < 27) pp[((int64_t)(co0 + c) * Ci + ci) * 27 + i] = s;
+    else if (ci == 0) pp[(int64_t)Co * Ci * 27 + co0 + c] = s;
+  }
 }
 
 // grad[p] = sum over chunks in order (deterministic)
@@ -544,7 +717,7 @@ dErr ensure_cap(_p_dLearned *L, int B) {
   for (int l = 0; l < NLAYER; l++) {
     const LayerDef &ld = kLayer[l];
     const Dims dout = ld.stride == 2 ? L->d[ld.level_in + 1] : L->d[ld.level_in];
-    const int64_t nch = ((int64_t)B * dout.n() + 16383) / 16384;
+    const int64_t nch = ((int64_t)B * dout.x * dout.y * ((dout.z + VZ - 1) / VZ) + kQuadChunk - 1) / kQuadChunk;
     need = std::max<int64_t>(need, nch * ((int64_t)ld.co * ld.ci * 27 + ld.co));
   }
   CUCHK(cudaMalloc(&L->partial, need * sizeof(float)));
@@ -559,8 +732,10 @@ dErr conv_fwd(_p_dLearned *L, int l, int B, const float *x, float *y, int relu, 
   const __nv_bfloat16 *W = L->wb + L->woff[l];
   const float *bias = L->w + L->boff[l];
   if (ld.co >= 16) {
-    dim3 grid(nblk((int64_t)B * dout.n(), 128), (ld.co + 15) / 16);
-    k_conv_fwd<16><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, dout, ld.stride, x, W, bias, relu, y);
+    const int64_t nq = (int64_t)dout.x * dout.y * ((dout.z + VZ - 1) / VZ);
+    dim3 grid(nblk((int64_t)B * nq, 128), (ld.co + 15) / 16);
+    if (ld.stride == 1) k_conv_fwd_rb<16, 1><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, dout, x, W, bias, relu, y);
+    else k_conv_fwd_rb<16, 2><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, dout, x, W, bias, relu, y);
   } else {
     dim3 grid(nblk((int64_t)B * dout.n(), 128), ld.co);
     k_conv_fwd<1><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, dout, ld.stride, x, W, bias, relu, y);
@@ -572,16 +747,30 @@ dErr conv_fwd(_p_dLearned *L, int l, int B, const float *x, float *y, int relu, 
 dErr conv_bwd(_p_dLearned *L, int l, int B, const float *x, const float *gz, float *gx, int accumulate, cudaStream_t s) {
   const LayerDef &ld = kLayer[l];
   const Dims di = L->d[ld.level_in], dout = ld.stride == 2 ? L->d[ld.level_in + 1] : di;
-  const int64_t total = (int64_t)B * dout.n();
-  const int nch = (int)((total + 16383) / 16384);
+  const int64_t total = (int64_t)B * dout.x * dout.y * ((dout.z + VZ - 1) / VZ);
+  const int nch = (int)((total + kQuadChunk - 1) / kQuadChunk);
   const int64_t np = (int64_t)ld.co * ld.ci * 27 + ld.co;
   if ((int64_t)nch * np > L->partial_len) return set_error("learned correction: gradient workspace too small");
-  k_conv_bwd_weight<<<dim3(ld.co * ld.ci, nch), 256, 0, s>>>(B, ld.ci, ld.co, di, dout, ld.stride, x, gz, 16384, L->partial);
+  if (ld.co % 2 == 0) {
+    const dim3 grid(ld.co / 2 * ld.ci, nch);
+    if (ld.stride == 1) k_conv_bwd_weight_rb<2, 1><<<grid, 256, 0, s>>>(B, ld.ci, ld.co, di, dout, x, gz, L->partial);
+    else k_conv_bwd_weight_rb<2, 2><<<grid, 256, 0, s>>>(B, ld.ci, ld.co, di, dout, x, gz, L->partial);
+  } else {
+    const dim3 grid(ld.co * ld.ci, nch);
+    if (ld.stride == 1) k_conv_bwd_weight_rb<1, 1><<<grid, 256, 0, s>>>(B, ld.ci, ld.co, di, dout, x, gz, L->partial);
+    else k_conv_bwd_weight_rb<1, 2><<<grid, 256, 0, s>>>(B, ld.ci, ld.co, di, dout, x, gz, L->partial);
+  }
   k_sum_chunks<<<nblk(np), 256, 0, s>>>(np, nch, L->partial, L->g + L->woff[l]);
   CUCHK(cudaGetLastError());
   if (gx) {
-    dim3 grid(nblk((int64_t)B * di.n(), 128), (ld.ci + 15) / 16);
-    k_conv_bwd_data<16><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, dout, ld.stride, gz, L->wb + L->woff[l], gx, accumulate);
+    if (ld.stride == 1) {
+      const int64_t nq = (int64_t)di.x * di.y * ((di.z + VZ - 1) / VZ);
+      dim3 grid(nblk((int64_t)B * nq, 128), (ld.ci + 15) / 16);
+      k_conv_bwd_data_rb<16><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, gz, L->wb + L->woff[l], gx, accumulate);
+    } else {
+      dim3 grid(nblk((int64_t)B * di.n(), 128), (ld.ci + 15) / 16);
+      k_conv_bwd_data<16><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, dout, ld.stride, gz, L->wb + L->woff[l], gx, accumulate);
+    }
     CUCHK(cudaGetLastError());
   }
   return 0;

@@ -242,6 +242,10 @@ dErr dLearnedTrain(dLearned net, dInt epochs, dInt batch, dReal lr, uint64_t see
 dErr dLearnedApply(dLearned net, const dScalar *r, dScalar *z);
 /* FGMRES preconditioner z = Chebyshev(r) + P N(R r) with the plain preconditioner as fallback; NULL removes it */
 dErr dKSPSetLearnedCorrection(dKSP ksp, dLearned net);
+/* where the correction is applied: 0 = every preconditioner application, 1 = only to the first vector of
+ * each restart cycle (the true residual, the kind of input the network was trained on), 2 = adaptive
+ * (default): one cycle with each, then the one whose cycle reduced the residual more */
+dErr dKSPSetCorrectionPolicy(dKSP ksp, int policy);
 /* raw network (device FP32 arrays): in [B][2][lattice] -> out [B][1][lattice]; loss and parameter gradient */
 dErr dLearnedForward(dLearned net, dInt B, const float *in, float *out);
 dErr dLearnedLossGrad(dLearned net, dInt B, const float *in, const float *target, dReal *loss, float *grad);
