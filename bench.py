@@ -248,10 +248,10 @@ def secondary_cfg4(args):
 
 
 def secondary_newton(args):
-    """p-Laplacian Newton-Krylov (exponent 1.5, eps 1e-6, 48^3, p=6, f ~ U[-1,1] per dof): FP64 inner applies vs
-    FP32 inner applies inside FGMRES (FP64 residuals and orthogonalisation). Per Newton step: ||F||, FGMRES
-    iterations, and the relative error of the mixed run's iterate and of its FP32 Jacobian apply against the
-    FP64 run (the FP64 path is the one pinned to the oracle)."""
+    """p-Laplacian Newton-Krylov (exponent 1.5, eps 1e-6, p=6, f ~ U[-1,1] per dof): FP64, FP32 and BF16 inner
+    applies (Jacobian and Chebyshev-Jacobi) inside FGMRES with FP64 residuals and orthogonalisation. Per Newton
+    step: ||F||, FGMRES iterations, and the relative error of each reduced-precision run's iterate and of its
+    Jacobian apply against the FP64 run (the FP64 path is the one pinned to the oracle)."""
     import numpy as np
     import torch
     import dohp_gb300 as dg
@@ -262,7 +262,7 @@ def secondary_newton(args):
            "dofs": fs.n, "rtol": 1e-8, "lin_rtol": 1e-3, "lin_maxit": 300,
            "ksp": "FGMRES(30) + Chebyshev(3)-Jacobi on the Q1-embedded Jacobian, inexact steps at lin_maxit"}
     runs = {}
-    for name, prec in (("fp64", dg.dPREC_FP64), ("fp32", dg.dPREC_FP32)):
+    for name, prec in (("fp64", dg.dPREC_FP64), ("fp32", dg.dPREC_FP32), ("bf16", dg.dPREC_BF16)):
         op = fs.operator(dg.dOP_PLAPLACE_JACOBIAN)
         m = fs.matrix()
         ksp = dg.KSP(op, m, ksp_type=dg.dKSP_FGMRES, inner_prec=prec, restart=30)
@@ -285,21 +285,24 @@ def secondary_newton(args):
             r["fnorm"].append(float(fn[1]))
             r["its"].append(int(li[0]))
             r["done"] = bool(fn[1] <= 1e-8 * r["fnorm"][0])
-        r64, r32 = runs["fp64"], runs["fp32"]
-        if len(r64["its"]) == len(r32["its"]) == k + 1:
-            op = r32["op"]
-            op.plap_stash(r32["u"], pe, eps)
+        r64 = runs["fp64"]
+        if all(len(r["its"]) == k + 1 for r in runs.values()):
+            row = {"step": k + 1}
             d = torch.as_tensor(np.random.default_rng(k).uniform(-1, 1, fs.n), device="cuda")
-            y64, y32 = torch.empty_like(d), torch.empty_like(d)
-            op.set_precision(dg.dPREC_FP64)
-            op.mult(d, y64)
-            op.set_precision(dg.dPREC_FP32)
-            op.mult(d, y32)
-            op.set_precision(dg.dPREC_FP64)
-            per.append({"step": k + 1,
-                        "iterate_rel_err": float(torch.linalg.norm(r32["u"] - r64["u"]) / torch.linalg.norm(r64["u"])),
-                        "fp32_jacobian_apply_rel_err": float(torch.linalg.norm(y32 - y64) / torch.linalg.norm(y64))})
-        if r64["done"] and r32["done"]:
+            for name, prec in (("fp32", dg.dPREC_FP32), ("bf16", dg.dPREC_BF16)):
+                r = runs[name]
+                op = r["op"]
+                op.plap_stash(r["u"], pe, eps)
+                y64, yl = torch.empty_like(d), torch.empty_like(d)
+                op.set_precision(dg.dPREC_FP64)
+                op.mult(d, y64)
+                op.set_precision(prec)
+                op.mult(d, yl)
+                op.set_precision(dg.dPREC_FP64)
+                row[name + "_iterate_rel_err"] = float(torch.linalg.norm(r["u"] - r64["u"]) / torch.linalg.norm(r64["u"]))
+                row[name + "_jacobian_apply_rel_err"] = float(torch.linalg.norm(yl - y64) / torch.linalg.norm(y64))
+            per.append(row)
+        if all(r["done"] for r in runs.values()):
             break
     for name, r in runs.items():
         out[name] = {"newton_steps": len(r["its"]), "fnorm": r["fnorm"], "fgmres_its": r["its"], "wall_s": r["wall"],
@@ -358,7 +361,8 @@ def secondary_learned(args):
     b = torch.as_tensor(np.random.default_rng(5000).uniform(-1, 1, fs.n), device="cuda")
     out["dofs"] = fs.n
     for name, prec, learned in (("plain_fp64", dg.dPREC_FP64, False), ("mixed_fp32", dg.dPREC_FP32, False),
-                                ("learned_mixed", dg.dPREC_FP32, True), ("learned_fp64", dg.dPREC_FP64, True)):
+                                ("mixed_bf16", dg.dPREC_BF16, False), ("learned_mixed", dg.dPREC_FP32, True),
+                                ("learned_bf16", dg.dPREC_BF16, True), ("learned_fp64", dg.dPREC_FP64, True)):
         ksp = dg.KSP(op, m, ksp_type=dg.dKSP_FGMRES, inner_prec=prec, restart=30)
         if learned:
             ksp.set_learned(net)
@@ -379,7 +383,7 @@ def secondary_learned(args):
         out[name] = {"its": its, "wall_s": wall, "true_rel_residual": float(torch.linalg.norm(b - r) / torch.linalg.norm(b)),
                      "correction_dropped": bool(rejects), "correction_active_at_end": active}
     out["speedup_vs_plain_fp64"] = {k: out["plain_fp64"]["wall_s"] / out[k]["wall_s"]
-                                    for k in ("mixed_fp32", "learned_mixed", "learned_fp64")}
+                                    for k in ("mixed_fp32", "mixed_bf16", "learned_mixed", "learned_bf16", "learned_fp64")}
     return out
 
 

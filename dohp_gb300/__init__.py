@@ -19,7 +19,7 @@ INSERT_VALUES, ADD_VALUES = 1, 2
 dFS_HOMOGENEOUS, dFS_INHOMOGENEOUS = 0, 1
 FAST, SPARSE, SELF = 0, 1, 2
 dOP_DIFFUSION, dOP_PLAPLACE_JACOBIAN, dOP_ELASTICITY = 0, 1, 2
-dPREC_FP64, dPREC_FP32 = 0, 1
+dPREC_FP64, dPREC_FP32, dPREC_BF16 = 0, 1, 2
 dKSP_CG, dKSP_FGMRES = 0, 1
 dPC_NONE, dPC_JACOBI, dPC_CHEBYSHEV_Q1 = 0, 1, 2
 

@@ -262,6 +262,7 @@ dErr dOperatorDestroy(dOperator *op) {
   _p_dOperator *o = *op;
   cudaFree(o->d_geo);
   cudaFree(o->d_geo32);
+  cudaFree(o->d_geo16);
   cudaFree(o->d_k);
   cudaFree(o->d_stash);
   cudaFree(o->d_yexp);
@@ -296,7 +297,7 @@ dErr dOperatorSetQuadratureData(dOperator op, const dReal *qdata) {
 
 dErr dOperatorSetPrecision(dOperator op, dPrecision prec) {
   if (!op) return set_error("null operator");
-  if (prec != dPREC_FP64 && prec != dPREC_FP32) return set_error("precision %d not supported", (int)prec);
+  if (prec != dPREC_FP64 && prec != dPREC_FP32 && prec != dPREC_BF16) return set_error("precision %d not supported", (int)prec);
   op->prec = prec;
   return 0;
 }

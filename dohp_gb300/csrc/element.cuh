@@ -11,6 +11,8 @@
 // measured slower on GB300: one thread per line leaves too few warps to hide the FP64 latency.
 #pragma once
 
+#include <cuda_bf16.h>
+
 #include "internal.h"
 
 namespace dgb {
@@ -33,12 +35,18 @@ struct ElemArgs {
 constexpr int kTabElems = 2 * MAXP * MAXP;
 enum { M_B = 0, M_BT = 1, M_D = 2, M_DT = 3 };
 
-template <int N, typename T>
+// value rounded to BF16 and widened back (the BF16 apply stores inputs, tables and factors in BF16)
+template <typename T>
+__device__ __forceinline__ T bf16_round(double v) {
+  return (T)__bfloat162float(__float2bfloat16_rn((float)v));
+}
+
+template <int N, typename T, bool BF = false>
 __device__ __forceinline__ void load_tables(const double *tab_all, T *sm) {
   const double *tab = tab_all + (size_t)2 * (N - 2) * MAXP * MAXP;
   for (int i = threadIdx.x; i < N * N; i += blockDim.x) {
-    sm[i] = (T)tab[i];
-    sm[MAXP * MAXP + i] = (T)tab[MAXP * MAXP + i];
+    sm[i] = BF ? bf16_round<T>(tab[i]) : (T)tab[i];
+    sm[MAXP * MAXP + i] = BF ? bf16_round<T>(tab[MAXP * MAXP + i]) : (T)tab[MAXP * MAXP + i];
   }
   __syncthreads();
 }
@@ -63,7 +71,7 @@ __device__ __forceinline__ void pass(const T *sm, const T *in, T *out, int ne) {
 __device__ __forceinline__ int64_t elem_id(const int32_t *els, int64_t first, int el) { return els ? els[el] : first + el; }
 
 // gather one component of the element's nodes through E (homogeneous Dirichlet: closure beyond n is 0)
-template <int N, typename T, int BS>
+template <int N, typename T, int BS, bool BF = false>
 __device__ __forceinline__ void gather(const ElemArgs &A, const double *x, const int32_t *els, int64_t first, int ne, int d, T *dst) {
   constexpr int N3 = N * N * N;
   for (int t = threadIdx.x; t < ne * N3; t += blockDim.x) {
@@ -79,7 +87,7 @@ __device__ __forceinline__ void gather(const ElemArgs &A, const double *x, const
       const int32_t c = A.emap[row];
       if (c < A.n) v = x[(int64_t)c * BS + d];
     }
-    dst[t] = (T)v;
+    dst[t] = BF ? bf16_round<T>(v) : (T)v;
   }
 }
 
@@ -152,27 +160,29 @@ __host__ __device__ constexpr int group_smem_elems(int N, int kind, int cap) {
   return kTabElems + (kind == dOP_ELASTICITY ? 11 : 5) * cap * N * N * N;
 }
 
-// apply the operator to ne (<= cap) elements: ids els[0..ne) or first..first+ne
-template <int N, typename T, int KIND>
+// apply the operator to ne (<= cap) elements: ids els[0..ne) or first..first+ne. T: arithmetic type;
+// GT: storage type of the geometric factors; BF: inputs and basis tables rounded to BF16 (the BF16 apply:
+// BF16 storage, FP32 arithmetic and accumulation)
+template <int N, typename T, int KIND, typename GT = T, bool BF = false>
 __device__ void group_apply(const ElemArgs &A, const int32_t *els, int64_t first, int ne, int cap, T *sm) {
   constexpr int N3 = N * N * N;
   T *buf = sm + kTabElems;
   const int L = cap * N3, tot = ne * N3;
   const double *x = A.px ? *A.px : A.x;
   T *yexp = (T *)A.yexp;
-  load_tables<N, T>(A.tab_all, sm);
+  load_tables<N, T, BF>(A.tab_all, sm);
   if (KIND != dOP_ELASTICITY) {  // diffusion and the p-Laplacian Jacobian: G (6 per point)
     T *S0 = buf, *S1 = buf + L, *G0 = buf + 2 * L, *G1 = buf + 3 * L, *G2 = buf + 4 * L;
-    gather<N, T, 1>(A, x, els, first, ne, 0, S0);
+    gather<N, T, 1, BF>(A, x, els, first, ne, 0, S0);
     __syncthreads();
     interp3<N, T>(sm, S0, S1, ne);
     grad<N, T>(sm, S1, G0, G1, G2, ne);
-    const T *geo = (const T *)A.geo;
+    const GT *geo = (const GT *)A.geo;
     for (int t = threadIdx.x; t < tot; t += blockDim.x) {
       const int el = t / N3, r = t - el * N3;
-      const T *G = geo + (int64_t)A.qoff[elem_id(els, first, el)] * 6 + r;
+      const GT *G = geo + (int64_t)A.qoff[elem_id(els, first, el)] * 6 + r;
       const T g0 = G0[t], g1 = G1[t], g2 = G2[t];
-      const T a0 = G[0], a1 = G[N3], a2 = G[2 * N3], a3 = G[3 * N3], a4 = G[4 * N3], a5 = G[5 * N3];
+      const T a0 = (T)G[0], a1 = (T)G[N3], a2 = (T)G[2 * N3], a3 = (T)G[3 * N3], a4 = (T)G[4 * N3], a5 = (T)G[5 * N3];
       G0[t] = a0 * g0 + a1 * g1 + a2 * g2;
       G1[t] = a1 * g0 + a3 * g1 + a4 * g2;
       G2[t] = a2 * g0 + a4 * g1 + a5 * g2;

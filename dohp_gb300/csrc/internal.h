@@ -105,6 +105,7 @@ struct _p_dOperator {
   double lam = 0, mu = 0;
   double *d_geo = nullptr;       // fp64 geometric factors per qpt
   float *d_geo32 = nullptr;      // fp32 copy
+  void *d_geo16 = nullptr;       // bf16 copy (scalar kinds)
   double *d_k = nullptr;         // coefficient per qpt
   double *d_stash = nullptr;     // p-Laplacian stash [nq][4]
   double *d_gbase = nullptr;     // p-Laplacian: {J^-1, w det J} per qpt (10, SoA per element)

@@ -10,6 +10,8 @@
 #include <algorithm>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "internal.h"
 
 using namespace dgb;
@@ -40,6 +42,21 @@ __global__ void k_scan_add(int32_t *out, int64_t n, const int64_t *block_offsets
   const int64_t i = blockIdx.x * 1024LL + threadIdx.x;
   if (i < n) out[i] += (int32_t)block_offsets[blockIdx.x];
   if (i == 0) out[n] = (int32_t)total;
+}
+
+// FP32 vectors, BF16 values, FP32 accumulation
+__global__ void k_spmv_bf16(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ col,
+                            const __nv_bfloat16 *__restrict__ val, const float *__restrict__ x, float *__restrict__ y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float s = 0;
+  for (int32_t k = rp[i]; k < rp[i + 1]; k++) s = fmaf(__bfloat162float(val[k]), x[col[k]], s);
+  y[i] = s;
+}
+
+__global__ void k_val_to_bf16(int64_t n, const double *__restrict__ a, __nv_bfloat16 *__restrict__ b) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = __float2bfloat16_rn((float)a[i]);
 }
 
 template <typename T>
@@ -251,6 +268,7 @@ struct _p_dKSP {
   dPrecision inner_prec = dPREC_FP64;  // precision of the operator applies inside an FGMRES cycle
   double *d_V = nullptr, *d_Z = nullptr, *d_h = nullptr;  // FGMRES bases [(m+1) x n], [m x n], coefficients
   float *d_w32 = nullptr, *d_dinv32 = nullptr, *d_val32 = nullptr;  // FP32 Chebyshev workspace
+  __nv_bfloat16 *d_val16 = nullptr;                                // BF16 Q1 values
   // optional preconditioner correction applied after the Chebyshev step: z += corr(r) (learned correction,
   // FGMRES only); dropped for the rest of a solve when a restart cycle with it fails to reduce the residual
   dErr (*correction)(void *ctx, const double *r, double *z) = nullptr;
@@ -334,12 +352,19 @@ static dErr pc_setup(_p_dKSP *k) {
 static dErr pc_apply_fp32(_p_dKSP *k, const double *r, double *z) {
   const int64_t n = k->n, nnz = k->pmat->nnz;
   cudaStream_t s = k->op->fs->stream;
+  const bool bf = k->pc_prec == dPREC_BF16;
   if (!k->d_w32) {
     CUCHK(cudaMalloc(&k->d_w32, 5 * std::max<int64_t>(n, 1) * sizeof(float)));
     CUCHK(cudaMalloc(&k->d_dinv32, std::max<int64_t>(n, 1) * sizeof(float)));
-    CUCHK(cudaMalloc(&k->d_val32, std::max<int64_t>(nnz, 1) * sizeof(float)));
     k_convert<double, float><<<nb(n), 256, 0, s>>>(n, k->d_dinv, k->d_dinv32);
+  }
+  if (!bf && !k->d_val32) {
+    CUCHK(cudaMalloc(&k->d_val32, std::max<int64_t>(nnz, 1) * sizeof(float)));
     k_convert<double, float><<<nb(nnz), 256, 0, s>>>(nnz, k->pmat->d_val, k->d_val32);
+  }
+  if (bf && !k->d_val16) {
+    CUCHK(cudaMalloc(&k->d_val16, std::max<int64_t>(nnz, 1) * sizeof(__nv_bfloat16)));
+    k_val_to_bf16<<<nb(nnz), 256, 0, s>>>(nnz, k->pmat->d_val, k->d_val16);
   }
   float *r32 = k->d_w32, *z32 = r32 + n, *d32 = z32 + n, *w32 = d32 + n;
   k_convert<double, float><<<nb(n), 256, 0, s>>>(n, r, r32);
@@ -347,7 +372,8 @@ static dErr pc_apply_fp32(_p_dKSP *k, const double *r, double *z) {
   double rho = 1.0 / sigma;
   k_cheb_first_t<float><<<nb(n), 256, 0, s>>>(n, k->d_dinv32, r32, (float)(1.0 / theta), d32, z32);
   for (int it = 1; it < k->cheb_degree; it++) {
-    k_spmv<float><<<nb(n), 256, 0, s>>>(n, k->pmat->d_rowptr, k->pmat->d_col, k->d_val32, z32, w32);
+    if (bf) k_spmv_bf16<<<nb(n), 256, 0, s>>>(n, k->pmat->d_rowptr, k->pmat->d_col, k->d_val16, z32, w32);
+    else k_spmv<float><<<nb(n), 256, 0, s>>>(n, k->pmat->d_rowptr, k->pmat->d_col, k->d_val32, z32, w32);
     const double rho1 = 1.0 / (2.0 * sigma - rho);
     k_cheb_step_t<float><<<nb(n), 256, 0, s>>>(n, k->d_dinv32, r32, w32, (float)(rho1 * rho), (float)(2.0 * rho1 / delta), d32, z32);
     rho = rho1;
@@ -370,7 +396,7 @@ static dErr pc_apply(_p_dKSP *k, const double *r, double *z) {
 static dErr pc_apply_plain(_p_dKSP *k, const double *r, double *z) {
   const int64_t n = k->n;
   cudaStream_t s = k->op->fs->stream;
-  if (k->pc == dPC_CHEBYSHEV_Q1 && k->pc_prec == dPREC_FP32) return pc_apply_fp32(k, r, z);
+  if (k->pc == dPC_CHEBYSHEV_Q1 && k->pc_prec != dPREC_FP64) return pc_apply_fp32(k, r, z);
   if (k->pc == dPC_NONE) {
     CUCHK(cudaMemcpyAsync(z, r, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
     return 0;
@@ -569,6 +595,7 @@ dErr dKSPDestroy(dKSP *ksp) {
   cudaFree(k->d_w32);
   cudaFree(k->d_dinv32);
   cudaFree(k->d_val32);
+  cudaFree(k->d_val16);
   delete k;
   *ksp = nullptr;
   return 0;
@@ -591,7 +618,8 @@ dErr dKSPSetOptions(dKSP ksp, dInt cheb_degree, dPrecision pc_precision, dInt re
   cudaFree(ksp->d_w32);
   cudaFree(ksp->d_dinv32);
   cudaFree(ksp->d_val32);
-  ksp->d_w32 = nullptr, ksp->d_dinv32 = nullptr, ksp->d_val32 = nullptr;
+  cudaFree(ksp->d_val16);
+  ksp->d_w32 = nullptr, ksp->d_dinv32 = nullptr, ksp->d_val32 = nullptr, ksp->d_val16 = nullptr;
   return 0;
 }
 
@@ -624,7 +652,8 @@ dErr dKSPSetOperators(dKSP ksp, dOperator op, dMat pmat) {
   cudaFree(ksp->d_w32);
   cudaFree(ksp->d_dinv32);
   cudaFree(ksp->d_val32);
-  ksp->d_w32 = nullptr, ksp->d_dinv32 = nullptr, ksp->d_val32 = nullptr;
+  cudaFree(ksp->d_val16);
+  ksp->d_w32 = nullptr, ksp->d_dinv32 = nullptr, ksp->d_val32 = nullptr, ksp->d_val16 = nullptr;
   return 0;
 }
 

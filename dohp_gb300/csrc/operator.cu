@@ -114,16 +114,16 @@ struct ETile {
 };
 
 // y_exp = (B^T Dq^T) G (Dq B) E x for cap consecutive elements per block (uniform order, Boolean E)
-template <int N, typename T, int KIND>
+template <int N, typename T, int KIND, typename GT = T, bool BF = false>
 __global__ void __launch_bounds__(256) k_uniform(ElemArgs A, int64_t nelem, int cap) {
   extern __shared__ unsigned char raw[];
   const int64_t e0 = (int64_t)blockIdx.x * cap;
   const int ne = (int)min((int64_t)cap, nelem - e0);
-  group_apply<N, T, KIND>(A, nullptr, e0, ne, cap, reinterpret_cast<T *>(raw));
+  group_apply<N, T, KIND, GT, BF>(A, nullptr, e0, ne, cap, reinterpret_cast<T *>(raw));
 }
 
-template <int N, typename T, int KIND>
-dErr launch_uniform(_p_dFS *fs, const double *x, const T *geo, double lam, double mu, T *yexp) {
+template <int N, typename T, int KIND, typename GT = T, bool BF = false>
+dErr launch_uniform(_p_dFS *fs, const double *x, const GT *geo, double lam, double mu, T *yexp) {
   constexpr int cap = KIND == dOP_ELASTICITY ? ETile<N>::EPB : Tile<N>::EPB;
   ElemArgs A{};
   A.xstart = fs->d_xstart;
@@ -137,8 +137,8 @@ dErr launch_uniform(_p_dFS *fs, const double *x, const T *geo, double lam, doubl
   A.lam = lam;
   A.mu = mu;
   const size_t smem = (size_t)group_smem_elems(N, KIND, cap) * sizeof(T);
-  CUCHK(cudaFuncSetAttribute(k_uniform<N, T, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_uniform<N, T, KIND><<<(unsigned)((fs->nelem + cap - 1) / cap), 256, smem, fs->stream>>>(A, fs->nelem, cap);
+  CUCHK(cudaFuncSetAttribute(k_uniform<N, T, KIND, GT, BF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_uniform<N, T, KIND, GT, BF><<<(unsigned)((fs->nelem + cap - 1) / cap), 256, smem, fs->stream>>>(A, fs->nelem, cap);
   CUCHK(cudaGetLastError());
   return 0;
 }
@@ -146,6 +146,11 @@ dErr launch_uniform(_p_dFS *fs, const double *x, const T *geo, double lam, doubl
 template <int N, typename T>
 dErr launch_diffusion(_p_dFS *fs, const double *x, const T *geo, T *yexp) {
   return launch_uniform<N, T, dOP_DIFFUSION>(fs, x, geo, 0, 0, yexp);
+}
+
+template <int N>
+dErr launch_diffusion_bf16(_p_dFS *fs, const double *x, const __nv_bfloat16 *geo, float *yexp) {
+  return launch_uniform<N, float, dOP_DIFFUSION, __nv_bfloat16, true>(fs, x, geo, 0, 0, yexp);
 }
 
 template <int N, typename T>
@@ -193,6 +198,10 @@ dErr op_compute_geometry(_p_dOperator *op) {
   if (op->d_geo32) {
     cudaFree(op->d_geo32);
     op->d_geo32 = nullptr;
+  }
+  if (op->d_geo16) {
+    cudaFree(op->d_geo16);
+    op->d_geo16 = nullptr;
   }
   op->geo_valid = true;
   op->geo_kind = mode;
@@ -268,12 +277,50 @@ static dErr op_mult_fp32(_p_dOperator *op, const double *x, double *y) {
   return fs_restrict32(fs, op->d_y32, y, 0);
 }
 
+__global__ void k_to_bf16_geo(int64_t n, const double *__restrict__ a, __nv_bfloat16 *__restrict__ b) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = __float2bfloat16_rn((float)a[i]);
+}
+
+// BF16 storage (factors, inputs, basis tables), FP32 arithmetic; FP64 restriction
+static dErr op_mult_bf16(_p_dOperator *op, const double *x, double *y) {
+  _p_dFS *fs = op->fs;
+  if (op->kind != dOP_DIFFUSION && op->kind != dOP_PLAPLACE_JACOBIAN)
+    return set_error("BF16 apply for operator kind %d not built (scalar kinds only)", (int)op->kind);
+  DCHK(op_compute_geometry(op));
+  const int64_t ng = fs->nq * 6;
+  if (!op->d_geo16) {
+    CUCHK(cudaMalloc(&op->d_geo16, ng * sizeof(__nv_bfloat16)));
+    k_to_bf16_geo<<<(unsigned)((ng + 255) / 256), 256, 0, fs->stream>>>(ng, op->d_geo, (__nv_bfloat16 *)op->d_geo16);
+    CUCHK(cudaGetLastError());
+  }
+  if (!op->d_y32) CUCHK(cudaMalloc(&op->d_y32, fs->nexp * fs->bs * sizeof(float)));
+  const __nv_bfloat16 *g = (const __nv_bfloat16 *)op->d_geo16;
+  dErr e = 0;
+  switch (fs->p + 1) {
+    case 2: e = launch_diffusion_bf16<2>(fs, x, g, op->d_y32); break;
+    case 3: e = launch_diffusion_bf16<3>(fs, x, g, op->d_y32); break;
+    case 4: e = launch_diffusion_bf16<4>(fs, x, g, op->d_y32); break;
+    case 5: e = launch_diffusion_bf16<5>(fs, x, g, op->d_y32); break;
+    case 6: e = launch_diffusion_bf16<6>(fs, x, g, op->d_y32); break;
+    case 7: e = launch_diffusion_bf16<7>(fs, x, g, op->d_y32); break;
+    case 8: e = launch_diffusion_bf16<8>(fs, x, g, op->d_y32); break;
+    case 9: e = launch_diffusion_bf16<9>(fs, x, g, op->d_y32); break;
+    default: return set_error("degree %d not supported", fs->p);
+  }
+  if (e) return e;
+  return fs_restrict32(fs, op->d_y32, y, 0);
+}
+
 dErr hp_mult(_p_dOperator *op, const double *x, double *y);
 
 dErr op_mult(_p_dOperator *op, const double *x, double *y) {
   _p_dFS *fs = op->fs;
+  if (op->prec == dPREC_BF16 && (!fs->uniform || op->launch != dLAUNCH_DEFAULT))
+    return set_error("BF16 apply needs a uniform-order space and the default launch");
   if (!fs->uniform || op->launch != dLAUNCH_DEFAULT) return hp_mult(op, x, y);
   if (op->prec == dPREC_FP32) return op_mult_fp32(op, x, y);
+  if (op->prec == dPREC_BF16) return op_mult_bf16(op, x, y);
   if (!op->d_yexp) CUCHK(cudaMalloc(&op->d_yexp, fs->nexp * fs->bs * sizeof(double)));
   DCHK(op_mult_expanded(op, x, op->d_yexp));
   return fs_restrict(fs, op->d_yexp, y, 0);

@@ -220,6 +220,10 @@ dErr plap_prepare(_p_dOperator *op) {
     cudaFree(op->d_geo32);
     op->d_geo32 = nullptr;
   }
+  if (op->d_geo16) {
+    cudaFree(op->d_geo16);
+    op->d_geo16 = nullptr;
+  }
   return 0;
 }
 

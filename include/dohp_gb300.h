@@ -61,7 +61,10 @@ typedef enum {
   dOP_ELASTICITY = 2      /* ElastPointwiseJacobian at F = I (src/fs/tests/elast.c:256-280), bs = 3 */
 } dOperatorKind;
 /* Arithmetic of an operator apply */
-typedef enum { dPREC_FP64 = 0, dPREC_FP32 = 1 } dPrecision;
+/* arithmetic of operator applies and of the Chebyshev-Jacobi preconditioner: FP64; FP32 (factors, inputs and
+ * arithmetic in FP32); BF16 (geometric factors, inputs, basis tables and Q1 values stored in BF16, FP32
+ * arithmetic and accumulation; scalar uniform-order operators) */
+typedef enum { dPREC_FP64 = 0, dPREC_FP32 = 1, dPREC_BF16 = 2 } dPrecision;
 /* Launch form of an operator apply: DEFAULT = one fused kernel for uniform-order spaces (per-order form for
  * hp spaces); PER_ORDER = one launch per order bucket; PERSISTENT = one launch over all buckets with a device
  * work counter; GRAPH = the persistent launch and the restriction replayed from a CUDA graph. */
