@@ -431,7 +431,7 @@ def main():
         for _ in range(3):
             op.mult_expanded(x, yexp)
         _, kms = time_loop(lambda: op.mult_expanded(x, yexp), max(args.steps // 2, 3), stream)
-        kernel_name = "k_diffusion<%d,double> (element apply)" % (cfg["p"] + 1)
+        kernel_name = "k_uniform<%d,double,diffusion> (element apply)" % (cfg["p"] + 1)
     for _ in range(max(args.warmup, 3)):
         op.mult(x, y)
     torch.cuda.synchronize()
