@@ -382,10 +382,10 @@ class Learned:
         g = None if grf is None else np.ascontiguousarray(grf, np.float64)
         chk(lib().dLearnedSetField(self.h, ptr(g)))
 
-    def collect(self, ksp, b, rtol=1e-10, maxit=5000, every=1, max_pairs=100):
+    def collect(self, ksp, b, rtol=1e-10, maxit=5000, every=1, max_pairs=100, rough_start=False):
         n = _i32()
         chk(lib().dLearnedCollectPairs(self.h, ksp.h, ptr(b), _dbl(rtol), _i32(maxit), _i32(every), _i32(max_pairs),
-                                       ctypes.byref(n)))
+                                       ctypes.c_int(int(rough_start)), ctypes.byref(n)))
         return n.value
 
     def train(self, epochs, batch=8, lr=1e-3, seed=0):

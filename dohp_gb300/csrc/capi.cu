@@ -13,6 +13,7 @@ dErr op_mult(_p_dOperator *op, const double *x, double *y);
 dErr op_compute_geometry(_p_dOperator *op);
 dErr q1_symbolic(_p_dFS *fs, _p_dMat *J);
 dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk, const double *dref, double pe, double eps);
+dErr q1_numeric_elast(_p_dFS *fs, _p_dMat *J, double lam, double mu, int quirk);
 dErr plap_set_stash(_p_dOperator *op, const double *stash);
 dErr mat_mult(_p_dMat *J, const double *x, double *y, cudaStream_t s);
 void hp_plan_destroy(void *p);
@@ -343,6 +344,8 @@ dErr dMatDestroy(dMat *J) {
   cudaFree((*J)->d_col);
   cudaFree((*J)->d_val);
   cudaFree((*J)->d_val32);
+  cudaFree((*J)->d_srowptr);
+  cudaFree((*J)->d_scol);
   delete *J;
   *J = nullptr;
   return 0;
@@ -352,7 +355,13 @@ dErr dFSAssembleQ1(dFS fs, dMat J, dOperatorKind kind, const dReal *param, const
   (void)param;
   if (!fs || !J) return set_error("null argument");
   if (kind == dOP_PLAPLACE_JACOBIAN) return set_error("the p-Laplacian Q1 matrix depends on the state: use dFSAssembleQ1PLaplace");
+  if (kind == dOP_ELASTICITY) {  // ElastJacobian (elast.c:343-407) at F = I, Lame parameters as ElastSetMaterial
+    if (fs->bs != 3 || J->bs != 3) return set_error("elasticity Q1 assembly needs block size 3");
+    const double E0 = param ? param[0] : 1.0, nu = param ? param[1] : 0.3;
+    return q1_numeric_elast(fs, J, E0 * nu / ((1 + nu) * (1 - 2 * nu)), E0 / (2 * (1 + nu)), reference_quirk);
+  }
   if (kind != dOP_DIFFUSION) return set_error("Q1 assembly for operator kind %d not built yet", (int)kind);
+  if (fs->bs != 1) return set_error("diffusion Q1 assembly needs block size 1");
   return q1_numeric(fs, J, grf, reference_quirk, nullptr, 0, 0);
 }
 

@@ -122,8 +122,12 @@ struct _p_dOperator {
 
 struct _p_dMat {
   dFS fs;
+  int bs = 1;
   int64_t nrows = 0, nnz = 0;
   int32_t *d_rowptr = nullptr, *d_col = nullptr;
   double *d_val = nullptr;
   float *d_val32 = nullptr;
+  // bs > 1: the node (scalar) pattern the blocked CSR expands
+  int64_t snnz = 0;
+  int32_t *d_srowptr = nullptr, *d_scol = nullptr;
 };

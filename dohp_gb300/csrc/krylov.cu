@@ -284,6 +284,12 @@ struct _p_dKSP {
   void *monitor_ctx = nullptr;
 };
 
+dErr ksp_get_operator(dKSP ksp, dOperator *op) {
+  if (!ksp || !op) return set_error("null argument");
+  *op = ksp->op;
+  return 0;
+}
+
 dErr ksp_set_monitor(dKSP ksp, dErr (*fn)(void *, int, const double *, const double *), void *ctx) {
   if (!ksp) return set_error("null KSP");
   ksp->monitor = fn;

@@ -246,10 +246,128 @@ __global__ void k_q1_rows(int64_t n, const int32_t *et_ptr, const int32_t *et_id
   });
 }
 
+// ElastJacobian patch matrices (elast.c:343-407 with ElastPointwiseJacobian at F = I, elast.c:269-280):
+// K[i*3+fi][j*3+fj] = sum_q dphi_i . dv(fi), dv = w (lambda tr(eps) I + 2 mu eps), eps = sym(e_fj dphi_j^T).
+// One 64-thread group per patch, thread (i, j) forms the 3 x 3 block; patches [p0, p0 + np) of the chunk.
+__global__ void __launch_bounds__(256) k_q1_patch_elast(int64_t nelem, const int32_t *edeg, const int64_t *pstart, const double *coords,
+                                                        const SparseRules *rules, int quirk, int64_t p0, int64_t np, double lam,
+                                                        double mu, double *K) {
+  __shared__ double sJ[4][8][9], sW[4][8], sDer[4][8][8][3];
+  const int g = threadIdx.x >> 6, lt = threadIdx.x & 63;
+  const int64_t gp = p0 + (int64_t)blockIdx.x * 4 + g;
+  const bool active = gp < p0 + np;
+  int64_t e = 0;
+  int px = 1, py = 1, pz = 1, pidx = 0;
+  if (active) {
+    int64_t lo = 0, hi = nelem;
+    while (hi - lo > 1) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (pstart[mid] <= gp) lo = mid;
+      else hi = mid;
+    }
+    e = lo;
+    px = edeg[3 * e], py = edeg[3 * e + 1], pz = edeg[3 * e + 2];
+    pidx = (int)(gp - pstart[e]);
+  }
+  const int pi = pidx / (py * pz), pj = (pidx / pz) % py, pk = pidx % pz;
+  const double I1[2][2] = {{0.78867513459481287, 0.21132486540518713}, {0.21132486540518713, 0.78867513459481287}};
+  const double D1[2][2] = {{-1., 1.}, {-1., 1.}};
+  if (active && lt < 8) {
+    const int q = lt, qi = q >> 2, qj = (q >> 1) & 1, qk = q & 1;
+    const double *X = coords + e * 24;
+    const int ai = 2 * pi + qi, aj = 2 * pj + qj, ak = 2 * pk + qk;
+    double xo[3], J[9], Ji[9];
+    q1_map(X, rules->x[px][ai], rules->x[py][aj], rules->x[pz][ak], xo, J);
+    const double det = inv3(J, Ji);
+    sW[g][q] = rules->w[px][ai] * rules->w[py][aj] * rules->w[pz][ak] * det;
+    if (quirk) {  // inverse Jacobian read at element-natural index pidx*8+q (efstopo.c:700)
+      const int t = pidx * 8 + q, Qy = 2 * py, Qz = 2 * pz;
+      const int ti = t / (Qy * Qz), tj = (t / Qz) % Qy, tk = t % Qz;
+      q1_map(X, rules->x[px][ti], rules->x[py][tj], rules->x[pz][tk], xo, J);
+      inv3(J, Ji);
+    }
+    for (int i = 0; i < 9; i++) sJ[g][q][i] = Ji[i];
+  }
+  __syncthreads();
+  if (active) {
+    const int q = lt >> 3, b = lt & 7, qi = q >> 2, qj = (q >> 1) & 1, qk = q & 1, bi = b >> 2, bj = (b >> 1) & 1, bk = b & 1;
+    const double dX = D1[qi][bi] * I1[qj][bj] * I1[qk][bk], dY = I1[qi][bi] * D1[qj][bj] * I1[qk][bk], dZ = I1[qi][bi] * I1[qj][bj] * D1[qk][bk];
+    const double *Ji = sJ[g][q];
+    for (int d = 0; d < 3; d++) sDer[g][q][b][d] = dX * Ji[0 * 3 + d] + dY * Ji[1 * 3 + d] + dZ * Ji[2 * 3 + d];
+  }
+  __syncthreads();
+  if (!active) return;
+  const int i = lt >> 3, j = lt & 7;
+  double blk[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int q = 0; q < 8; q++) {
+    const double w = sW[g][q], *Di = sDer[g][q][i], *Dj = sDer[g][q][j];
+    for (int fj = 0; fj < 3; fj++) {
+      double du[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      for (int c = 0; c < 3; c++) du[fj * 3 + c] = Dj[c];
+      const double dE[6] = {du[0], du[4], du[8], 0.5 * (du[1] + du[3]), 0.5 * (du[2] + du[6]), 0.5 * (du[5] + du[7])};
+      const double tr = dE[0] + dE[1] + dE[2];
+      double dS[6];
+      for (int k = 0; k < 6; k++) dS[k] = lam * tr * (k < 3) + 2 * mu * dE[k];
+      const double dv[9] = {dS[0] * w, dS[3] * w, dS[4] * w, dS[3] * w, dS[1] * w, dS[5] * w, dS[4] * w, dS[5] * w, dS[2] * w};
+      for (int fi = 0; fi < 3; fi++) blk[fi][fj] += Di[0] * dv[fi * 3] + Di[1] * dv[fi * 3 + 1] + Di[2] * dv[fi * 3 + 2];
+    }
+  }
+  double *Kp = K + (gp - p0) * 576;
+  for (int fi = 0; fi < 3; fi++)
+    for (int fj = 0; fj < 3; fj++) Kp[(i * 3 + fi) * 24 + j * 3 + fj] = blk[fi][fj];
+}
+
+// each node row adds the 3 x 3 blocks of its patches in [p0, p0 + np), in ascending (element, patch) order
+__global__ void k_q1_rows_elast(int64_t n, const int32_t *et_ptr, const int32_t *et_idx, const int32_t *xstart, const int32_t *edeg,
+                                int64_t nelem, const int64_t *pstart, const int32_t *emap, const double *K, int64_t p0, int64_t np,
+                                const int32_t *srp, const int32_t *scol, const int32_t *rowptr, double *vals) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int32_t s0 = srp[r], s1 = srp[r + 1], cnt = s1 - s0;
+  for_row_patches(r, et_ptr, et_idx, xstart, edeg, nelem, [&](int64_t e, int pidx, int corner, int, int py, int pz, int i, int j, int l) {
+    const int64_t gp = pstart[e] + pidx;
+    if (gp < p0 || gp >= p0 + np) return;
+    const double *Kp = K + (gp - p0) * 576;
+    for (int b = 0; b < 8; b++) {
+      const int bi = b >> 2, bj = (b >> 1) & 1, bk = b & 1;
+      const int32_t col = emap[xstart[e] + ((i + bi) * (py + 1) + j + bj) * (pz + 1) + l + bk];
+      if (col >= n) continue;
+      int lo = s0, hi = s1 - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (scol[mid] < col) lo = mid + 1;
+        else hi = mid;
+      }
+      const int k = lo - s0;
+      for (int fi = 0; fi < 3; fi++)
+        for (int fj = 0; fj < 3; fj++) vals[rowptr[3 * r + fi] + 3 * k + fj] += Kp[(corner * 3 + fi) * 24 + b * 3 + fj];
+    }
+  });
+  (void)cnt;
+}
+
 }  // namespace
 
+// blocked pattern (bs = 3): node row r, component fi -> columns 3 c + fj for the node columns c of r
+__global__ void k_expand_pattern(int64_t n, const int32_t *__restrict__ srp, const int32_t *__restrict__ scol,
+                                 int32_t *__restrict__ rp, int32_t *__restrict__ col) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int32_t s0 = srp[r], cnt = srp[r + 1] - s0;
+  for (int fi = 0; fi < 3; fi++) {
+    const int32_t base = 9 * s0 + fi * 3 * cnt;
+    rp[3 * r + fi] = base;
+    for (int k = 0; k < cnt; k++)
+      for (int fj = 0; fj < 3; fj++) col[base + 3 * k + fj] = 3 * scol[s0 + k] + fj;
+  }
+  if (r == n - 1) rp[3 * n] = 9 * srp[n];
+}
+
 dErr q1_symbolic(_p_dFS *fs, _p_dMat *J) {
-  if (fs->bs != 1) return set_error("Q1 matrix for block size %d not built yet", fs->bs);
+  if (fs->bs != 1 && fs->bs != 3) return set_error("Q1 matrix for block size %d not built", fs->bs);
+  // rows and columns go through E as a node map (dFSMatSetValuesBlockedExpanded, fs.c:826-930), which needs
+  // one closure node per expanded node: conforming spaces (the reference errors on p-nonconforming ones)
+  if (!fs->boolean_e) return set_error("Q1-embedded matrix needs a conforming space (Boolean E)");
   const int64_t n = fs->n;
   J->nrows = n;
   CUCHK(cudaMalloc(&J->d_rowptr, (n + 1) * sizeof(int32_t)));
@@ -281,6 +399,23 @@ dErr q1_symbolic(_p_dFS *fs, _p_dMat *J) {
   cudaFree(counts);
   cudaFree(d_over);
   if (over) return set_error("Q1 row with more than %d columns", MAXCOLS);
+  if (fs->bs == 3) {  // keep the node pattern, expand to the interleaved 3 x 3 blocked CSR
+    J->bs = 3;
+    J->snnz = J->nnz;
+    J->d_srowptr = J->d_rowptr, J->d_scol = J->d_col;
+    cudaFree(J->d_val);
+    J->nrows = 3 * n;
+    J->nnz = 9 * J->snnz;
+    if (J->nnz > INT32_MAX) return set_error("blocked Q1 matrix has %lld nonzeros, beyond 32-bit CSR", (long long)J->nnz);
+    CUCHK(cudaMalloc(&J->d_rowptr, (3 * n + 1) * sizeof(int32_t)));
+    CUCHK(cudaMalloc(&J->d_col, std::max<int64_t>(J->nnz, 1) * sizeof(int32_t)));
+    CUCHK(cudaMalloc(&J->d_val, std::max<int64_t>(J->nnz, 1) * sizeof(double)));
+    if (n) {
+      k_expand_pattern<<<(unsigned)((n + 127) / 128), 128, 0, fs->stream>>>(n, J->d_srowptr, J->d_scol, J->d_rowptr, J->d_col);
+      CUCHK(cudaGetLastError());
+    }
+    CUCHK(cudaStreamSynchronize(fs->stream));
+  }
   return 0;
 }
 
@@ -318,6 +453,46 @@ dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk, const
   cudaFree(d_rules);
   cudaFree(d_K);
   cudaFree(d_grf);
+  if (J->d_val32) {
+    cudaFree(J->d_val32);
+    J->d_val32 = nullptr;
+  }
+  return 0;
+}
+
+// blocked (bs = 3) elasticity assembly, in chunks of patches so the patch matrices stay within a few GB
+dErr q1_numeric_elast(_p_dFS *fs, _p_dMat *J, double lam, double mu, int quirk) {
+  std::vector<int64_t> pstart(fs->nelem + 1, 0);
+  for (int64_t e = 0; e < fs->nelem; e++)
+    pstart[e + 1] = pstart[e] + (int64_t)fs->edeg[3 * e] * fs->edeg[3 * e + 1] * fs->edeg[3 * e + 2];
+  const int64_t np = pstart[fs->nelem], chunk = std::min<int64_t>(std::max<int64_t>(np, 1), 1 << 20);
+  SparseRules h;
+  for (int p = 1; p < MAXP; p++) rule_1d(dQUADRATURE_METHOD_SPARSE, 2 * p, h.x[p], h.w[p]);
+  int64_t *d_pstart;
+  SparseRules *d_rules;
+  double *d_K;
+  CUCHK(cudaMalloc(&d_pstart, pstart.size() * sizeof(int64_t)));
+  CUCHK(cudaMalloc(&d_rules, sizeof h));
+  CUCHK(cudaMalloc(&d_K, chunk * 576 * sizeof(double)));
+  CUCHK(cudaMemcpyAsync(d_pstart, pstart.data(), pstart.size() * sizeof(int64_t), cudaMemcpyHostToDevice, fs->stream));
+  CUCHK(cudaMemcpyAsync(d_rules, &h, sizeof h, cudaMemcpyHostToDevice, fs->stream));
+  CUCHK(cudaMemsetAsync(J->d_val, 0, std::max<int64_t>(J->nnz, 1) * sizeof(double), fs->stream));
+  for (int64_t p0 = 0; p0 < np; p0 += chunk) {
+    const int64_t cnp = std::min(chunk, np - p0);
+    k_q1_patch_elast<<<(unsigned)((cnp + 3) / 4), 256, 0, fs->stream>>>(fs->nelem, fs->d_edeg, d_pstart, fs->d_coords, d_rules, quirk,
+                                                                        p0, cnp, lam, mu, d_K);
+    CUCHK(cudaGetLastError());
+    if (fs->n) {
+      k_q1_rows_elast<<<(unsigned)((fs->n + 127) / 128), 128, 0, fs->stream>>>(fs->n, fs->d_et_ptr, fs->d_et_idx, fs->d_xstart, fs->d_edeg,
+                                                                               fs->nelem, d_pstart, fs->d_emap, d_K, p0, cnp, J->d_srowptr,
+                                                                               J->d_scol, J->d_rowptr, J->d_val);
+      CUCHK(cudaGetLastError());
+    }
+  }
+  CUCHK(cudaStreamSynchronize(fs->stream));
+  cudaFree(d_pstart);
+  cudaFree(d_rules);
+  cudaFree(d_K);
   if (J->d_val32) {
     cudaFree(J->d_val32);
     J->d_val32 = nullptr;

@@ -27,6 +27,8 @@ dErr device_dot(int64_t n, const double *a, const double *b, double *part, doubl
 dErr ksp_set_monitor(dKSP ksp, dErr (*fn)(void *, int, const double *, const double *), void *ctx);
 dErr ksp_set_correction(dKSP ksp, dErr (*fn)(void *, const double *, double *), void *ctx);
 dErr ksp_solve(dKSP ksp, const double *b, double *x, double rtol, int maxit, int *its, double *rnorm);
+dErr op_mult(_p_dOperator *op, const double *x, double *y);
+dErr ksp_get_operator(dKSP ksp, dOperator *op);
 
 namespace {
 
@@ -625,6 +627,22 @@ __global__ void k_batch(int B, int64_t nv, const int32_t *__restrict__ idx, cons
   tb[t] = ptg[(int64_t)p * nv + i] * inv_ysc;
 }
 
+// seeded uniform values in [-1, 1) (splitmix64 of the index)
+__global__ void k_uniform_noise(int64_t n, uint64_t seed, double *__restrict__ x) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(i + 1);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  x[i] = (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+}
+
+__global__ void k_scale_d(int64_t n, const double *__restrict__ num, const double *__restrict__ den, double *__restrict__ x) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) x[i] *= sqrt(*num / *den);
+}
+
 // log k = g(x) at the vertex coordinates (random Fourier features, as dFSEvaluateLognormal)
 __global__ void k_logk(int64_t nv, const double *__restrict__ xyz, const double *__restrict__ grf, float *__restrict__ out) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -1140,7 +1158,7 @@ dErr dLearnedLossGrad(dLearned L, dInt B, const float *in, const float *target, 
 // (residual, error) pairs from every `every`-th iterate; the current field (dLearnedSetField) is the
 // pairs' log k channel
 dErr dLearnedCollectPairs(dLearned L, dKSP ksp, const dScalar *b, dReal rtol, dInt maxit, dInt every, dInt max_pairs,
-                          dInt *collected) {
+                          int rough_start, dInt *collected) {
   if (!L || !ksp || !b) return set_error("null argument");
   if (every < 1 || max_pairs < 1) return set_error("every and max_pairs must be positive");
   _p_dFS *fs = L->fs;
@@ -1177,6 +1195,22 @@ dErr dLearnedCollectPairs(dLearned L, dKSP ksp, const dScalar *b, dReal rtol, dI
   double *x;
   CUCHK(cudaMalloc(&x, std::max<int64_t>(fs->n, 1) * sizeof(double)));
   CUCHK(cudaMemsetAsync(x, 0, fs->n * sizeof(double), s));
+  if (rough_start) {  // x0 = a xi, xi seeded noise, a such that ||A x0|| = ||b||: rough early residuals
+    dOperator op;
+    double *ax, *nrm;
+    DCHK(ksp_get_operator(ksp, &op));
+    CUCHK(cudaMalloc(&ax, std::max<int64_t>(fs->n, 1) * sizeof(double)));
+    CUCHK(cudaMalloc(&nrm, 2 * sizeof(double)));
+    k_uniform_noise<<<nblk(fs->n), 256, 0, s>>>(fs->n, 0x5EEDull + 7919ull * (uint64_t)L->nfields, x);
+    DCHK(op_mult(op, x, ax));
+    DCHK(device_dot(fs->n, b, b, L->dpart, nrm, s));
+    DCHK(device_dot(fs->n, ax, ax, L->dpart, nrm + 1, s));
+    k_scale_d<<<nblk(fs->n), 256, 0, s>>>(fs->n, nrm, nrm + 1, x);
+    CUCHK(cudaGetLastError());
+    CUCHK(cudaStreamSynchronize(s));
+    cudaFree(ax);
+    cudaFree(nrm);
+  }
   int its = 0;
   double rn = 0;
   dErr err = ksp_set_monitor(ksp, collect_monitor, L);

@@ -236,9 +236,11 @@ dErr dLearnedDestroy(dLearned *net);
 dErr dLearnedGetSizes(dLearned net, dInt dims[3], int64_t *nparam, int64_t *npairs);
 /* coefficient field of the next pairs / corrections: log k at the vertices from dGRFCreate data (NULL: k = 1) */
 dErr dLearnedSetField(dLearned net, const dReal *grf);
-/* run the plain solver (CG on ksp) on b to rtol and record every `every`-th (residual, error) pair */
+/* run the plain solver (CG on ksp) on b to rtol and record every `every`-th (residual, error) pair; with
+ * rough_start the solve starts from seeded noise scaled so that ||A x0|| = ||b|| (early residuals then carry
+ * the rough components that FGMRES's Arnoldi vectors have), otherwise from zero */
 dErr dLearnedCollectPairs(dLearned net, dKSP ksp, const dScalar *b, dReal rtol, dInt maxit, dInt every, dInt max_pairs,
-                          dInt *collected);
+                          int rough_start, dInt *collected);
 /* Adam on the collected pairs (mean squared error over interior vertices); losses[epochs] (may be NULL) */
 dErr dLearnedTrain(dLearned net, dInt epochs, dInt batch, dReal lr, uint64_t seed, dReal *losses);
 /* z += P N(R r) */
