@@ -165,6 +165,56 @@ def cpu_baseline(cfg, threads, budget_s=20.0):
                       % (ne, fs.n * bs, len(times), threads)}
 
 
+def cpu_time_to_rtol_cfg1(threads):
+    """The CPU-runnable configuration (Poisson 8^3, p=4, mass right-hand side of f ~ U[-1,1], CG + Q1
+    Chebyshev(3)-Jacobi to rtol 1e-8) solved by the oracle on the host cores: wall seconds."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    o = po.FS(9, 9, 9, degree=4, perturb=0.1, seed=1)
+    b = o.apply(np.random.default_rng(0).uniform(-1, 1, o.n), kind=3, nthreads=threads)
+    t0 = time.perf_counter()
+    csr = o.q1_assemble()
+    t1 = time.perf_counter()
+    _, its, rn = o.cg_solve(b, csr, rtol=1e-8, maxit=1000, nthreads=threads)
+    t2 = time.perf_counter()
+    return {"its": its, "solve_s": t2 - t1, "q1_assembly_s": t1 - t0, "rel_residual": rn, "threads": threads}
+
+
+def gpu_time_to_rtol_cfg1():
+    """Same problem on the GPU: mass right-hand side through the batched dRulesetIterator, Q1 assembly on the
+    device, CG with Chebyshev(3)-Jacobi, FP64."""
+    import numpy as np
+    import torch
+    import dohp_gb300 as dg
+    fs = dg.FS((9, 9, 9), degree=4, perturb=0.1, seed=1)
+    f = torch.as_tensor(np.random.default_rng(0).uniform(-1, 1, fs.n), device="cuda")
+    it = dg.RulesetIterator(fs)
+    it.start(f)
+    a = it.get()
+    a["v"].copy_(a["jw"][:, None] * a["u"])
+    it.commit(dg.INSERT_VALUES, use_v=True, use_dv=False)
+    b = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
+    it.finish(b)
+    op = fs.operator()
+    m = fs.matrix()
+    m.assemble()
+    for _ in range(2):  # warm-up (geometry, kernels); the timed run below includes assembly and set-up
+        x = torch.zeros_like(b)
+        dg.KSP(op, m, ksp_type=dg.dKSP_CG).solve(b, x, rtol=1e-8, maxit=1000)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    m.assemble()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    ksp = dg.KSP(op, m, ksp_type=dg.dKSP_CG)
+    x = torch.zeros_like(b)
+    its, rn = ksp.solve(b, x, rtol=1e-8, maxit=1000)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    return {"its": its, "solve_s": t2 - t1, "q1_assembly_s": t1 - t0, "rel_residual": rn}
+
+
 def run_reference(args, cfg, rank):
     if rank != 0:
         return
@@ -505,8 +555,13 @@ def main():
         if "newton" in which:
             line["newton_mixed_precision"] = secondary_newton(args)
             torch.cuda.empty_cache()
+    if not args.no_secondary and args.config == "cfg2":
+        line["time_to_rtol_cfg1"] = {"workload": "poisson-8^3-p4 (configs[0]), mass right-hand side, CG + Q1 Chebyshev(3)-Jacobi, rtol 1e-8",
+                                     "gpu": gpu_time_to_rtol_cfg1()}
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(cfg, os.cpu_count() or 1)
+        if "time_to_rtol_cfg1" in line:
+            line["time_to_rtol_cfg1"]["cpu_oracle"] = cpu_time_to_rtol_cfg1(os.cpu_count() or 1)
     print(json.dumps(line, default=_plain))
     if dist:
         dist.destroy_process_group()

@@ -1132,6 +1132,9 @@ static void qfunction(int kind, int D, const double *qd, const double *param, do
     const double etaw = k * w;
     v[0] = -w * 0.0 * u[0];
     for (int i = 0; i < 3; i++) dv[i] = etaw * du[i];
+  } else if (kind == 3) { /* mass: the right-hand side b = int v f_h of src/fs/tests/ex1.c:399-430 */
+    v[0] = w * u[0];
+    dv[0] = dv[1] = dv[2] = 0;
   } else if (kind == 1) {
     const double eta = qd[0], *s = qd + 1;
     const double dotw = (s[0] * du[0] + s[1] * du[1] + s[2] * du[2]) * w, etaw = eta * w;

@@ -92,6 +92,7 @@ void or_fs_expanded_to_global(const or_fs *fs, const double *x, double *g, int a
  * kind 0: scalar diffusion, dv = w det k du (k per FAST qpt, NULL -> 1)
  * kind 1: p-Laplacian Jacobian with stash [eta, sqrt_mdeta_Du[3]] per qpt (ellip.c:369-377)
  * kind 2: linear elasticity, lambda/mu in param[0..1] (elast.c:227-280 at F=I)
+ * kind 3: mass, v = w u (the right-hand side of ex1.c:399-430 and of configuration 1)
  * nthreads: OpenMP threads over element ranges (the reference runs one MPI rank per core). */
 int or_operator_apply(const or_fs *fs, int kind, const double *qdata, const double *param,
                       const double *g, double *y, int nthreads);
