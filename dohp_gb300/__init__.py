@@ -201,6 +201,13 @@ class Operator:
         """dOperatorPLaplaceFunction: y = N(g) (no forcing); the stash of g stays for the Jacobian."""
         chk(lib().dOperatorPLaplaceFunction(self.h, ptr(g), _dbl(p), _dbl(eps), ptr(y)))
 
+    def elasticity_state(self, g):
+        """dOperatorElasticityState: St. Venant-Kirchhoff Jacobian at g from now on (None: linear)"""
+        chk(lib().dOperatorElasticityState(self.h, ptr(g)))
+
+    def elasticity_function(self, g, y):
+        chk(lib().dOperatorElasticityFunction(self.h, ptr(g), ptr(y)))
+
     def get_qdata(self, out):
         chk(lib().dOperatorGetQuadratureData(self.h, ptr(out)))
 

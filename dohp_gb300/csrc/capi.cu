@@ -272,6 +272,7 @@ dErr dOperatorDestroy(dOperator *op) {
   cudaFree(o->d_hx);
   cudaFree(o->d_hy);
   cudaFree(o->d_gbase);
+  cudaFree(o->d_svk);
   hp_plan_destroy(o->hp_plan);
   delete o;
   *op = nullptr;

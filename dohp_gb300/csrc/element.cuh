@@ -31,7 +31,12 @@ struct ElemArgs {
   const double *tab_all;
   void *yexp;
   double lam, mu;
+  double *stash;  // St. Venant-Kirchhoff: {F (9), S (6)} per point, SoA per element
 };
+
+// element kinds beyond the ABI's operator kinds: St. Venant-Kirchhoff function (writes the stash) and
+// Jacobian at the stashed state (elast.c:224-280)
+constexpr int K_SVK_FUNC = 100, K_SVK_JAC = 101;
 
 // shared-memory table region: B and Dq (MAXP x MAXP each)
 constexpr int kTabElems = 2 * MAXP * MAXP;
@@ -158,8 +163,9 @@ __device__ __forceinline__ void back(const T *sm, const T *V0, const T *V1, cons
 }
 
 // shared memory (in T) of one group of cap elements: tables + buffers
+__host__ __device__ constexpr bool elastic_kind(int kind) { return kind == dOP_ELASTICITY || kind == K_SVK_FUNC || kind == K_SVK_JAC; }
 __host__ __device__ constexpr int group_smem_elems(int N, int kind, int cap) {
-  return kTabElems + (kind == dOP_ELASTICITY ? 11 : 5) * cap * N * N * N;
+  return kTabElems + (elastic_kind(kind) ? 11 : 5) * cap * N * N * N;
 }
 
 // apply the operator to ne (<= cap) elements: ids els[0..ne) or first..first+ne. T: arithmetic type;
@@ -173,7 +179,7 @@ __device__ void group_apply(const ElemArgs &A, const int32_t *els, int64_t first
   const double *x = A.px ? *A.px : A.x;
   T *yexp = (T *)A.yexp;
   load_tables<N, T, BF>(A.tab_all, sm);
-  if (KIND != dOP_ELASTICITY) {  // diffusion and the p-Laplacian Jacobian: G (6 per point)
+  if constexpr (!elastic_kind(KIND)) {  // diffusion and the p-Laplacian Jacobian: G (6 per point)
     T *S0 = buf, *S1 = buf + L, *G0 = buf + 2 * L, *G1 = buf + 3 * L, *G2 = buf + 4 * L;
     gather<N, T, 1, BF>(A, x, els, first, ne, 0, S0);
     __syncthreads();
@@ -215,16 +221,69 @@ __device__ void group_apply(const ElemArgs &A, const int32_t *els, int64_t first
 #pragma unroll
         for (int e = 0; e < 3; e++) Du[d * 3 + e] = a0 * Ji[0 * 3 + e] + a1 * Ji[1 * 3 + e] + a2 * Ji[2 * 3 + e];
       }
-      // ElastPointwiseJacobian at F = I (elast.c:269-280): eps = sym(grad u), dv = w (lambda tr(eps) I + 2 mu eps)
-      const T e01 = (T)0.5 * (Du[1] + Du[3]), e02 = (T)0.5 * (Du[2] + Du[6]), e12 = (T)0.5 * (Du[5] + Du[7]);
-      const T tr = Du[0] + Du[4] + Du[8];
       T S[9];
-      S[0] = w * (lam * tr + 2 * mu * Du[0]);
-      S[4] = w * (lam * tr + 2 * mu * Du[4]);
-      S[8] = w * (lam * tr + 2 * mu * Du[8]);
-      S[1] = S[3] = w * (2 * mu * e01);
-      S[2] = S[6] = w * (2 * mu * e02);
-      S[5] = S[7] = w * (2 * mu * e12);
+      if constexpr (KIND == dOP_ELASTICITY) {
+        // ElastPointwiseJacobian at F = I (elast.c:269-280): eps = sym(grad u), dv = w (lambda tr(eps) I + 2 mu eps)
+        const T e01 = (T)0.5 * (Du[1] + Du[3]), e02 = (T)0.5 * (Du[2] + Du[6]), e12 = (T)0.5 * (Du[5] + Du[7]);
+        const T tr = Du[0] + Du[4] + Du[8];
+        S[0] = w * (lam * tr + 2 * mu * Du[0]);
+        S[4] = w * (lam * tr + 2 * mu * Du[4]);
+        S[8] = w * (lam * tr + 2 * mu * Du[8]);
+        S[1] = S[3] = w * (2 * mu * e01);
+        S[2] = S[6] = w * (2 * mu * e02);
+        S[5] = S[7] = w * (2 * mu * e12);
+      } else {
+        // St. Venant-Kirchhoff (elast.c:224-280): E = (F^T F - I)/2, S = lambda tr(E) I + 2 mu E (storage
+        // [00, 11, 22, 01, 02, 12]); function Dv = w F S with F = I + Du, Jacobian Dv = w (F dS + dF S)
+        double *st = A.stash + (int64_t)A.qoff[elem_id(els, first, el)] * 15 + r;
+        T F[9], P6[6];
+        auto dotcol = [](const T *a, const T *b, int i, int j) { return a[i] * b[j] + a[3 + i] * b[3 + j] + a[6 + i] * b[6 + j]; };
+        auto pk2 = [&](const T *Fm, const T *dF, T *out) {  // dF == nullptr: S(F); else dS(F; dF)
+          T E[6];
+          const int ij[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+#pragma unroll
+          for (int k = 0; k < 6; k++)
+            E[k] = dF ? (T)0.5 * (dotcol(Fm, dF, ij[k][0], ij[k][1]) + dotcol(dF, Fm, ij[k][0], ij[k][1]))
+                      : (T)0.5 * (dotcol(Fm, Fm, ij[k][0], ij[k][1]) - (k < 3 ? (T)1 : (T)0));
+          const T trE = E[0] + E[1] + E[2];
+#pragma unroll
+          for (int k = 0; k < 6; k++) out[k] = lam * trE * (k < 3 ? (T)1 : (T)0) + 2 * mu * E[k];
+        };
+        auto gesy = [](T *C, const T *Am, const T *Sy, bool add) {
+#pragma unroll
+          for (int i = 0; i < 3; i++) {
+            const T c0 = Am[i * 3 + 0] * Sy[0] + Am[i * 3 + 1] * Sy[3] + Am[i * 3 + 2] * Sy[4];
+            const T c1 = Am[i * 3 + 0] * Sy[3] + Am[i * 3 + 1] * Sy[1] + Am[i * 3 + 2] * Sy[5];
+            const T c2 = Am[i * 3 + 0] * Sy[4] + Am[i * 3 + 1] * Sy[5] + Am[i * 3 + 2] * Sy[2];
+            C[i * 3 + 0] = add ? C[i * 3 + 0] + c0 : c0;
+            C[i * 3 + 1] = add ? C[i * 3 + 1] + c1 : c1;
+            C[i * 3 + 2] = add ? C[i * 3 + 2] + c2 : c2;
+          }
+        };
+        if constexpr (KIND == K_SVK_FUNC) {
+#pragma unroll
+          for (int i = 0; i < 9; i++) F[i] = Du[i] + ((i % 4 == 0) ? (T)1 : (T)0);
+          pk2(F, nullptr, P6);
+          gesy(S, F, P6, false);
+          if (A.stash) {
+#pragma unroll
+            for (int i = 0; i < 9; i++) st[i * N3] = F[i];
+#pragma unroll
+            for (int i = 0; i < 6; i++) st[(9 + i) * N3] = P6[i];
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < 9; i++) F[i] = st[i * N3];
+#pragma unroll
+          for (int i = 0; i < 6; i++) P6[i] = st[(9 + i) * N3];
+          T dS[6];
+          pk2(F, Du, dS);
+          gesy(S, F, dS, false);
+          gesy(S, Du, P6, true);
+        }
+#pragma unroll
+        for (int i = 0; i < 9; i++) S[i] *= w;
+      }
 #pragma unroll
       for (int d = 0; d < 3; d++)
 #pragma unroll

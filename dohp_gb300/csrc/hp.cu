@@ -207,6 +207,7 @@ static HpArgs make_args(_p_dOperator *op, const double *x, bool fp32, void *yexp
   A.ecol = fs->d_ecol;
   A.eval = fs->d_eval;
   A.emap = fs->d_emap;
+  A.stash = nullptr;
   A.n = fs->n;
   A.x = x;
   A.px = px;

@@ -109,6 +109,8 @@ struct _p_dOperator {
   double *d_k = nullptr;         // coefficient per qpt
   double *d_stash = nullptr;     // p-Laplacian stash [nq][4]
   double *d_gbase = nullptr;     // p-Laplacian: {J^-1, w det J} per qpt (10, SoA per element)
+  double *d_svk = nullptr;       // St. Venant-Kirchhoff state: {F, S} per qpt (15, SoA per element)
+  bool svk_state = false;        // elasticity Jacobian at that state instead of F = I
   double *d_yexp = nullptr;      // expanded output scratch
   float *d_x32 = nullptr, *d_y32 = nullptr;
   double *d_hx = nullptr, *d_hy = nullptr;  // device staging for the host-vector form

@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(256) k_uniform(ElemArgs A, int64_t nelem, int 
 }
 
 template <int N, typename T, int KIND, typename GT = T, bool BF = false>
-dErr launch_uniform(_p_dFS *fs, const double *x, const GT *geo, double lam, double mu, T *yexp) {
+dErr launch_uniform(_p_dFS *fs, const double *x, const GT *geo, double lam, double mu, T *yexp, double *stash = nullptr) {
   constexpr int cap = KIND == dOP_ELASTICITY ? ETile<N>::EPB : Tile<N>::EPB;
   ElemArgs A{};
   A.xstart = fs->d_xstart;
@@ -136,6 +136,7 @@ dErr launch_uniform(_p_dFS *fs, const double *x, const GT *geo, double lam, doub
   A.yexp = yexp;
   A.lam = lam;
   A.mu = mu;
+  A.stash = stash;
   const size_t smem = (size_t)group_smem_elems(N, KIND, cap) * sizeof(T);
   CUCHK(cudaFuncSetAttribute(k_uniform<N, T, KIND, GT, BF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   k_uniform<N, T, KIND, GT, BF><<<(unsigned)((fs->nelem + cap - 1) / cap), 256, smem, fs->stream>>>(A, fs->nelem, cap);
@@ -146,6 +147,21 @@ dErr launch_uniform(_p_dFS *fs, const double *x, const GT *geo, double lam, doub
 template <int N, typename T>
 dErr launch_diffusion(_p_dFS *fs, const double *x, const T *geo, T *yexp) {
   return launch_uniform<N, T, dOP_DIFFUSION>(fs, x, geo, 0, 0, yexp);
+}
+
+template <int KIND>
+dErr svk_launch(_p_dFS *fs, const double *x, const double *geo, double lam, double mu, double *yexp, double *stash) {
+  switch (fs->p + 1) {
+    case 2: return launch_uniform<2, double, KIND>(fs, x, geo, lam, mu, yexp, stash);
+    case 3: return launch_uniform<3, double, KIND>(fs, x, geo, lam, mu, yexp, stash);
+    case 4: return launch_uniform<4, double, KIND>(fs, x, geo, lam, mu, yexp, stash);
+    case 5: return launch_uniform<5, double, KIND>(fs, x, geo, lam, mu, yexp, stash);
+    case 6: return launch_uniform<6, double, KIND>(fs, x, geo, lam, mu, yexp, stash);
+    case 7: return launch_uniform<7, double, KIND>(fs, x, geo, lam, mu, yexp, stash);
+    case 8: return launch_uniform<8, double, KIND>(fs, x, geo, lam, mu, yexp, stash);
+    case 9: return launch_uniform<9, double, KIND>(fs, x, geo, lam, mu, yexp, stash);
+  }
+  return ::dgb::set_error("degree %d not supported", fs->p);
 }
 
 template <int N>
@@ -247,6 +263,7 @@ dErr op_mult_expanded(_p_dOperator *op, const double *x, double *yexp) {
   if (!fs->uniform || op->launch != dLAUNCH_DEFAULT) return hp_mult_expanded(op, x, yexp);
   DCHK(op_compute_geometry(op));
   if (op->kind == dOP_DIFFUSION) return diffusion_apply_t<double>(fs, x, op->d_geo, yexp);
+  if (op->kind == dOP_ELASTICITY && op->svk_state) return svk_launch<K_SVK_JAC>(fs, x, op->d_geo, op->lam, op->mu, yexp, op->d_svk);
   if (op->kind == dOP_ELASTICITY) return elasticity_apply_t<double>(fs, x, op->d_geo, op->lam, op->mu, yexp);
   if (op->kind == dOP_PLAPLACE_JACOBIAN) return diffusion_apply_t<double>(fs, x, op->d_geo, yexp);  // G from the stash
   return set_error("operator kind %d not built yet", (int)op->kind);
@@ -262,6 +279,7 @@ static dErr op_mult_fp32(_p_dOperator *op, const double *x, double *y) {
   _p_dFS *fs = op->fs;
   if (op->kind != dOP_DIFFUSION && op->kind != dOP_ELASTICITY && op->kind != dOP_PLAPLACE_JACOBIAN)
     return set_error("FP32 apply for operator kind %d not built yet", (int)op->kind);
+  if (op->svk_state) return set_error("FP32 St. Venant-Kirchhoff Jacobian not built (use FP64)");
   DCHK(op_compute_geometry(op));
   const int64_t ng = fs->nq * (op->kind == dOP_ELASTICITY ? 10 : 6);
   if (!op->d_geo32) {
@@ -318,6 +336,8 @@ dErr op_mult(_p_dOperator *op, const double *x, double *y) {
   _p_dFS *fs = op->fs;
   if (op->prec == dPREC_BF16 && (!fs->uniform || op->launch != dLAUNCH_DEFAULT))
     return set_error("BF16 apply needs a uniform-order space and the default launch");
+  if (op->svk_state && (!fs->uniform || op->launch != dLAUNCH_DEFAULT))
+    return set_error("St. Venant-Kirchhoff Jacobian needs a uniform-order space and the default launch");
   if (!fs->uniform || op->launch != dLAUNCH_DEFAULT) return hp_mult(op, x, y);
   if (op->prec == dPREC_FP32) return op_mult_fp32(op, x, y);
   if (op->prec == dPREC_BF16) return op_mult_bf16(op, x, y);
@@ -333,6 +353,35 @@ dErr op_mult_prec(_p_dOperator *op, const double *x, double *y, dPrecision prec)
   const dErr e = op_mult(op, x, y);
   op->prec = save;
   return e;
+}
+
+// St. Venant-Kirchhoff state at g (ElastPointwiseComputeStore, elast.c:224-225) and, with y, the function
+// (ElastFunction without body force, elast.c:282-309); g = NULL returns to F = I
+static dErr svk_state(_p_dOperator *op, const double *g, double *y) {
+  _p_dFS *fs = op->fs;
+  if (op->kind != dOP_ELASTICITY) return set_error("St. Venant-Kirchhoff needs an elasticity operator");
+  if (!g) {
+    op->svk_state = false;
+    return 0;
+  }
+  if (!fs->uniform) return set_error("St. Venant-Kirchhoff needs a uniform-order space");
+  DCHK(op_compute_geometry(op));
+  if (!op->d_svk) CUCHK(cudaMalloc(&op->d_svk, (size_t)fs->nq * 15 * sizeof(double)));
+  if (!op->d_yexp) CUCHK(cudaMalloc(&op->d_yexp, fs->nexp * fs->bs * sizeof(double)));
+  DCHK(svk_launch<K_SVK_FUNC>(fs, g, op->d_geo, op->lam, op->mu, op->d_yexp, op->d_svk));
+  op->svk_state = true;
+  if (y) DCHK(fs_restrict(fs, op->d_yexp, y, 0));
+  return 0;
+}
+
+extern "C" dErr dOperatorElasticityState(dOperator op, const dScalar *g) {
+  if (!op) return set_error("null operator");
+  return svk_state(op, g, nullptr);
+}
+
+extern "C" dErr dOperatorElasticityFunction(dOperator op, const dScalar *g, dScalar *y) {
+  if (!op || !g || !y) return set_error("null argument");
+  return svk_state(op, g, y);
 }
 
 extern "C" dErr dOperatorMultExpanded(dOperator op, const dScalar *x, dScalar *yexp) {

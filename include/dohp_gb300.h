@@ -153,6 +153,13 @@ dErr dOperatorComputePLaplaceStash(dOperator op, const dScalar *g, dReal p, dRea
 /* EllipFunction (ellip.c:407-440) without the forcing term, lambda = 0: y = sum_e E^T B^T (w eta Du) at the
  * state g; also leaves the stash of g in place (the next dOperatorMult is the Jacobian at g). */
 dErr dOperatorPLaplaceFunction(dOperator op, const dScalar *g, dReal p, dReal eps, dScalar *y);
+/* St. Venant-Kirchhoff elasticity (dOP_ELASTICITY operators, uniform-order spaces, FP64): the state at g
+ * (deformation gradient F = I + Du and second Piola-Kirchhoff stress S at every FAST point,
+ * ElastPointwiseComputeStore elast.c:224-225), after which dOperatorMult applies ElastShellMatMult at that
+ * state (ElastPointwiseJacobian, elast.c:268-280); g = NULL returns to F = I (linear elasticity) */
+dErr dOperatorElasticityState(dOperator op, const dScalar *g);
+/* ElastFunction without body force (elast.c:282-309): y = sum_e E^T B^T (w F S) at g; also sets the state */
+dErr dOperatorElasticityFunction(dOperator op, const dScalar *g, dScalar *y);
 /* copy out the per-point data: dOP_DIFFUSION coefficient [nq], dOP_PLAPLACE_JACOBIAN stash [nq][4] (device) */
 dErr dOperatorGetQuadratureData(dOperator op, dReal *qdata);
 dErr dOperatorSetPrecision(dOperator op, dPrecision prec);

@@ -1125,6 +1125,47 @@ void or_fs_qpt_coords(const or_fs *m, double *xq)
 
 /* Pointwise q-functions: EllipPointwiseJacobian (ellip.c:369-377; p=2 gives eta=1, s=0) and
  * ElastPointwiseJacobian at F=I (elast.c:269-280: dS = lambda tr(dE) I + 2 mu dE, Dv = F dS + dF S). */
+/* St. Venant-Kirchhoff pieces (elast.c:224-254): column dot, S = lambda tr(E) I + 2 mu E with the Green-Lagrange
+ * strain E = (F^T F - I)/2 in compressed symmetric storage [00, 11, 22, 01, 02, 12], and C = A S */
+static double dotcol(const double a[9], const double b[9], int i, int j)
+{
+  return a[0 * 3 + i] * b[0 * 3 + j] + a[1 * 3 + i] * b[1 * 3 + j] + a[2 * 3 + i] * b[2 * 3 + j];
+}
+static void svk_pk2(double lam, double mu, const double F[9], double S[6])
+{
+  double E[6], tr;
+  E[0] = 0.5 * (dotcol(F, F, 0, 0) - 1);
+  E[1] = 0.5 * (dotcol(F, F, 1, 1) - 1);
+  E[2] = 0.5 * (dotcol(F, F, 2, 2) - 1);
+  E[3] = 0.5 * dotcol(F, F, 0, 1);
+  E[4] = 0.5 * dotcol(F, F, 0, 2);
+  E[5] = 0.5 * dotcol(F, F, 1, 2);
+  tr = E[0] + E[1] + E[2];
+  for (int i = 0; i < 6; i++) S[i] = lam * tr * (i < 3) + 2 * mu * E[i];
+}
+static void svk_pk2_jac(double lam, double mu, const double F[9], const double dF[9], double dS[6])
+{
+  double dE[6], tr;
+  dE[0] = 0.5 * (dotcol(F, dF, 0, 0) + dotcol(dF, F, 0, 0));
+  dE[1] = 0.5 * (dotcol(F, dF, 1, 1) + dotcol(dF, F, 1, 1));
+  dE[2] = 0.5 * (dotcol(F, dF, 2, 2) + dotcol(dF, F, 2, 2));
+  dE[3] = 0.5 * (dotcol(F, dF, 0, 1) + dotcol(dF, F, 0, 1));
+  dE[4] = 0.5 * (dotcol(F, dF, 0, 2) + dotcol(dF, F, 0, 2));
+  dE[5] = 0.5 * (dotcol(F, dF, 1, 2) + dotcol(dF, F, 1, 2));
+  tr = dE[0] + dE[1] + dE[2];
+  for (int i = 0; i < 6; i++) dS[i] = lam * tr * (i < 3) + 2 * mu * dE[i];
+}
+static void mult_gesy3(double C[9], const double A[9], const double S[6], int add)
+{
+  for (int i = 0; i < 3; i++) {
+    const double c0 = A[i * 3 + 0] * S[0] + A[i * 3 + 1] * S[3] + A[i * 3 + 2] * S[4];
+    const double c1 = A[i * 3 + 0] * S[3] + A[i * 3 + 1] * S[1] + A[i * 3 + 2] * S[5];
+    const double c2 = A[i * 3 + 0] * S[4] + A[i * 3 + 1] * S[5] + A[i * 3 + 2] * S[2];
+    if (add) { C[i * 3 + 0] += c0; C[i * 3 + 1] += c1; C[i * 3 + 2] += c2; }
+    else { C[i * 3 + 0] = c0; C[i * 3 + 1] = c1; C[i * 3 + 2] = c2; }
+  }
+}
+
 static void qfunction(int kind, int D, const double *qd, const double *param, double w, const double *u, const double *du, double *v, double *dv)
 {
   if (kind == 0) {
@@ -1132,6 +1173,22 @@ static void qfunction(int kind, int D, const double *qd, const double *param, do
     const double etaw = k * w;
     v[0] = -w * 0.0 * u[0];
     for (int i = 0; i < 3; i++) dv[i] = etaw * du[i];
+  } else if (kind == 4) { /* ElastPointwiseFunction without body force (elast.c:256-266): Dv = w F S, F = I + Du */
+    double F[9], S[6];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) F[i * 3 + j] = (i == j) + du[i * 3 + j];
+    svk_pk2(param[0], param[1], F, S);
+    mult_gesy3(dv, F, S, 0);
+    for (int i = 0; i < 9; i++) dv[i] *= w;
+    v[0] = v[1] = v[2] = 0;
+  } else if (kind == 5) { /* ElastPointwiseJacobian at the stashed F (elast.c:268-280): Dv = w (F dS + dF S) */
+    double S[6], dS[6];
+    svk_pk2(param[0], param[1], qd, S);
+    svk_pk2_jac(param[0], param[1], qd, du, dS);
+    mult_gesy3(dv, qd, dS, 0);
+    mult_gesy3(dv, du, S, 1);
+    for (int i = 0; i < 9; i++) dv[i] *= w;
+    v[0] = v[1] = v[2] = 0;
   } else if (kind == 3) { /* mass: the right-hand side b = int v f_h of src/fs/tests/ex1.c:399-430 */
     v[0] = w * u[0];
     dv[0] = dv[1] = dv[2] = 0;
@@ -1160,7 +1217,8 @@ int or_operator_apply(const or_fs *m, int kind, const double *qdata, const doubl
                       const double *g, double *y, int nthreads)
 {
   const int bs = m->bs, D = bs;
-  if ((kind == 2) != (bs == 3)) return or_fail("kind %d needs block size %d", kind, kind == 2 ? 3 : 1);
+  const int elastic = kind == 2 || kind == 4 || kind == 5;
+  if (elastic != (bs == 3)) return or_fail("kind %d needs block size %d", kind, elastic ? 3 : 1);
   basis1d B[11];
   for (int p = 1; p <= 10; p++) if (basis_for(0, p, &B[p])) return -1;
   double *xexp = malloc(sizeof(double) * m->nexp * bs), *yexp = malloc(sizeof(double) * m->nexp * bs);
@@ -1193,6 +1251,7 @@ int or_operator_apply(const or_fs *m, int kind, const double *qdata, const doubl
         const double *qd = NULL;
         if (kind == 0 && qdata) qd = qdata + qoff[r] + q;
         if (kind == 1) qd = qdata + 4 * (int64_t)(qoff[r] + q);
+        if (kind == 5) qd = qdata + 9 * (int64_t)(qoff[r] + q);
         qfunction(kind, D, qd, param, jw[q], u + q * D, du + q * 3 * D, v + q * D, dv + q * 3 * D);
       }
       or_efs_apply_hex(P, Q, bi, bd, jinv, D, v, ye, OR_INTERP_TRANSPOSE, OR_INSERT);
@@ -1230,6 +1289,30 @@ int or_plap_stash(const or_fs *m, double p, double eps, const double *g, double 
       st[0] = eta;
       for (int i = 0; i < 3; i++) st[1 + i] = sm * Du[i];
     }
+    off += nq;
+  }
+  free(xexp); free(jinv); free(jw); free(du);
+  return 0;
+}
+
+int or_elast_state(const or_fs *m, const double *g, double *Fq)
+{
+  if (m->bs != 3) return or_fail("elasticity needs block size 3");
+  basis1d B[11];
+  for (int k = 1; k <= 10; k++) if (basis_for(0, k, &B[k])) return -1;
+  double *xexp = malloc(sizeof(double) * m->nexp * 3);
+  or_fs_global_to_expanded(m, g, NULL, xexp);
+  double *jinv = malloc(sizeof(double) * 9 * 1000), *jw = malloc(sizeof(double) * 1000), *du = malloc(sizeof(double) * 9000);
+  int64_t off = 0;
+  for (int64_t r = 0; r < m->nr; r++) {
+    const basis1d *b[3] = {&B[m->edeg[3 * r]], &B[m->edeg[3 * r + 1]], &B[m->edeg[3 * r + 2]]};
+    const int P[3] = {b[0]->P, b[1]->P, b[2]->P}, Q[3] = {b[0]->Q, b[1]->Q, b[2]->Q}, nq = Q[0] * Q[1] * Q[2];
+    const double *bi[3] = {b[0]->interp, b[1]->interp, b[2]->interp}, *bd[3] = {b[0]->deriv, b[1]->deriv, b[2]->deriv};
+    if (element_geometry(m, r, b, NULL, jinv, jw)) { free(xexp); free(jinv); free(jw); free(du); return -1; }
+    or_efs_apply_hex(P, Q, bi, bd, jinv, 3, xexp + (int64_t)m->xstart[r] * 3, du, OR_GRAD, OR_INSERT);
+    for (int q = 0; q < nq; q++)
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) Fq[9 * (off + q) + i * 3 + j] = (i == j) + du[q * 9 + i * 3 + j];
     off += nq;
   }
   free(xexp); free(jinv); free(jw); free(du);

@@ -93,6 +93,8 @@ void or_fs_expanded_to_global(const or_fs *fs, const double *x, double *g, int a
  * kind 1: p-Laplacian Jacobian with stash [eta, sqrt_mdeta_Du[3]] per qpt (ellip.c:369-377)
  * kind 2: linear elasticity, lambda/mu in param[0..1] (elast.c:227-280 at F=I)
  * kind 3: mass, v = w u (the right-hand side of ex1.c:399-430 and of configuration 1)
+ * kind 4: St. Venant-Kirchhoff function at the state g (ElastPointwiseFunction, elast.c:256-266, no body force)
+ * kind 5: St. Venant-Kirchhoff Jacobian at the stashed deformation gradients qdata [nq][9] (elast.c:268-280)
  * nthreads: OpenMP threads over element ranges (the reference runs one MPI rank per core). */
 int or_operator_apply(const or_fs *fs, int kind, const double *qdata, const double *param,
                       const double *g, double *y, int nthreads);
@@ -116,6 +118,10 @@ int64_t or_q1_assemble(const or_fs *fs, int kind, const double *param, const dou
 int64_t or_q1_assemble_plap(const or_fs *fs, double p, double eps, const double *g, int quirk,
                             int32_t *rowptr, int32_t **col, double **val);
 void or_free(void *p);
+
+/* deformation gradient F = I + Du [nq][9] at every FAST point of the state g (bs = 3, homogeneous Dirichlet;
+ * ElastPointwiseComputeStore, elast.c:224-225) */
+int or_elast_state(const or_fs *fs, const double *g, double *Fq);
 
 /* Lognormal coefficient field: g(x) = sqrt(2 var / nf) sum_f cos(w_f . x + b_f) (random Fourier
  * features of the squared-exponential kernel, Rahimi & Recht 2007). grf = [nf, var, ell, w(3nf), b(nf)] */

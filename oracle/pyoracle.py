@@ -83,6 +83,7 @@ def lib():
                                           _i32p, ctypes.POINTER(ctypes.POINTER(ctypes.c_int32)),
                                           ctypes.POINTER(ctypes.POINTER(ctypes.c_double))]
         L.or_free.argtypes = [ctypes.c_void_p]
+        L.or_elast_state.argtypes = [ctypes.c_void_p, _f64p, _f64p]
         L.or_grf_make.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_uint64, _f64p]
         L.or_grf_eval.restype = ctypes.c_double
         L.or_grf_eval.argtypes = [_f64p, _f64p]
@@ -272,6 +273,14 @@ class FS:
         if rc:
             raise RuntimeError(lib().or_last_error().decode())
         return y
+
+    def elast_state(self, g):
+        nq, _ = self.num_qpts()
+        F = np.zeros(nq * 9)
+        rc = lib().or_elast_state(self.h, np.ascontiguousarray(g, dtype=np.float64), F)
+        if rc:
+            raise RuntimeError(lib().or_last_error().decode())
+        return F
 
     def plap_stash(self, g, p, eps):
         nq, _ = self.num_qpts()
