@@ -345,6 +345,12 @@ class RulesetIterator:
     def finish(self, y=None, imode=INSERT_VALUES):
         chk(lib().dRulesetIteratorFinish(self.h, ptr(y), ctypes.c_int(imode)))
 
+    def error_norms(self, exact_u=None, exact_du=None):
+        """dRulesetIteratorErrorNorms: ({L1, L2, Linf} of u - exact_u, the same of |grad u - exact_du|)"""
+        ue, ge = np.zeros(3), np.zeros(3)
+        chk(lib().dRulesetIteratorErrorNorms(self.h, ptr(exact_u), ptr(exact_du), ptr(ue), ptr(ge)))
+        return ue, ge
+
 
 class dNewtonOptions(ctypes.Structure):
     _fields_ = [("max_it", _i32), ("rtol", _dbl), ("atol", _dbl), ("lin_rtol", _dbl), ("lin_maxit", _i32),

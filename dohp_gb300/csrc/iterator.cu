@@ -7,6 +7,9 @@
 // each step covers all elements: quadrature arrays are element-natural per element, elements back to back,
 // and every evaluation is one batched dEFSApply launch. FAST rules (one patch per element) on uniform-order
 // spaces.
+#include <algorithm>
+#include <cmath>
+
 #include "internal.h"
 
 using namespace dgb;
@@ -46,6 +49,42 @@ __global__ void k_physical(int64_t nel, int nq, const double *__restrict__ w, co
   b[8] = id * (a[0] * a[4] - a[3] * a[1]);
   if (det < 0) atomicExch(neg, 1);
   jw[t] = w[t % nq] * det;
+}
+
+// dNormsUpdate (src/util/util.c:121-144) over all points: per block partial sums of |r| jw, r^2 jw, max |r| and
+// of |grad r| jw, |grad r|^2 jw, max |grad r|
+__global__ void k_norms(int64_t nq, int bs, const double *__restrict__ jw, const double *__restrict__ u, const double *__restrict__ du,
+                        const double *__restrict__ uu, const double *__restrict__ duu, double *__restrict__ part) {
+  __shared__ double red[6][256];
+  double a[6] = {0, 0, 0, 0, 0, 0};
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nq; q += (int64_t)gridDim.x * blockDim.x) {
+    const double w = jw[q];
+    for (int i = 0; i < bs; i++) {
+      if (uu) {
+        const double r = uu[q * bs + i] - u[q * bs + i];
+        a[0] += fabs(r) * w;
+        a[1] += r * r * w;
+        a[2] = fmax(a[2], fabs(r));
+      }
+      if (duu) {
+        const double *e = duu + (q * bs + i) * 3, *g = du + (q * bs + i) * 3;
+        const double d0 = e[0] - g[0], d1 = e[1] - g[1], d2 = e[2] - g[2];
+        const double gr2 = d0 * d0 + d1 * d1 + d2 * d2, ga = sqrt(gr2);
+        a[3] += ga * w;
+        a[4] += gr2 * w;
+        a[5] = fmax(a[5], ga);
+      }
+    }
+  }
+  for (int k = 0; k < 6; k++) red[k][threadIdx.x] = a[k];
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int k = 0; k < 6; k++)
+        red[k][threadIdx.x] = (k == 2 || k == 5) ? fmax(red[k][threadIdx.x], red[k][threadIdx.x + st]) : red[k][threadIdx.x] + red[k][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x < 6) part[blockIdx.x * 6 + threadIdx.x] = red[threadIdx.x][0];
 }
 
 }  // namespace
@@ -168,6 +207,29 @@ dErr dRulesetIteratorFinish(dRulesetIterator it, dScalar *y, InsertMode imode) {
   it->started = false;
   if (!y) return 0;
   return fs_restrict(it->fs, it->yexp, y, imode == ADD_VALUES);
+}
+
+// dNormsStart/Update/Finish (src/util/util.c:110-153) over all points of the last GetPatchApplied: errors of
+// the field against exact values at the same points, uerr = {L1, L2, Linf} of u - exact_u and gerr = the same
+// of |grad u - exact_du| (exact arrays on the device, [nq][bs] and [nq][bs][3]; either may be NULL)
+dErr dRulesetIteratorErrorNorms(dRulesetIterator it, const dScalar *exact_u, const dScalar *exact_du, dReal uerr[3], dReal gerr[3]) {
+  if (!it || !it->applied) return set_error("dRulesetIteratorGetPatchApplied first");
+  cudaStream_t s = it->fs->stream;
+  constexpr int NB = 512;
+  double *part;
+  CUCHK(cudaMalloc(&part, NB * 6 * sizeof(double)));
+  k_norms<<<NB, 256, 0, s>>>(it->nq, it->fs->bs, it->jw, it->u, it->du, exact_u, exact_du, part);
+  CUCHK(cudaGetLastError());
+  std::vector<double> h(NB * 6);
+  CUCHK(cudaMemcpyAsync(h.data(), part, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CUCHK(cudaStreamSynchronize(s));
+  cudaFree(part);
+  double a[6] = {0, 0, 0, 0, 0, 0};
+  for (int b = 0; b < NB; b++)
+    for (int k = 0; k < 6; k++) a[k] = (k == 2 || k == 5) ? std::max(a[k], h[b * 6 + k]) : a[k] + h[b * 6 + k];
+  if (uerr) uerr[0] = a[0], uerr[1] = std::sqrt(a[1]), uerr[2] = a[2];
+  if (gerr) gerr[0] = a[3], gerr[1] = std::sqrt(a[4]), gerr[2] = a[5];
+  return 0;
 }
 
 }  // extern "C"

@@ -200,6 +200,11 @@ dErr dRulesetIteratorGetPatchApplied(dRulesetIterator it, int64_t *nq, const dRe
 dErr dRulesetIteratorCommitPatchApplied(dRulesetIterator it, InsertMode imode, int use_v, int use_dv);
 /* dRulesetIteratorFinish: restrict the expanded test vector into the global vector y */
 dErr dRulesetIteratorFinish(dRulesetIterator it, dScalar *y, InsertMode imode);
+/* dNormsStart/Update/Finish (src/util/util.c:110-153) over every point of the last GetPatchApplied: uerr =
+ * {L1, L2, Linf} of u - exact_u, gerr = the same of |grad u - exact_du| (device arrays [nq][bs], [nq][bs][3],
+ * either may be NULL, e.g. exact values computed from the x that GetPatchApplied returned) */
+dErr dRulesetIteratorErrorNorms(dRulesetIterator it, const dScalar *exact_u, const dScalar *exact_du, dReal uerr[3],
+                                dReal gerr[3]);
 
 /* ---------------------------------------------------------------- Q1-embedded preconditioning matrix */
 /* dFSCreateMatrix (src/fs/interface/fs.c:770-813) as a device CSR over explicit scalar dofs; the sparsity is

@@ -120,3 +120,50 @@ def test_errors():
     ed = np.random.default_rng(0).integers(2, 5, size=fs.nelem).astype(np.int32)
     with pytest.raises(dg.DohpError):
         dg.RulesetIterator(dg.FS((3, 3, 3), degree=2, seed=1, elem_degree=ed))
+
+
+def test_error_norms_match_numpy():
+    """dRulesetIteratorErrorNorms = dNormsUpdate (src/util/util.c:121-144) summed over the points"""
+    fs = dg.FS((4, 5, 4), degree=3, perturb=0.1, seed=2)
+    g = np.random.default_rng(8).uniform(-1, 1, fs.n)
+    it = dg.RulesetIterator(fs)
+    it.start(torch.as_tensor(g, device="cuda"))
+    a = it.get()
+    rng = np.random.default_rng(9)
+    eu = rng.standard_normal(a["u"].shape)
+    edu = rng.standard_normal(a["du"].shape)
+    ue, ge = it.error_norms(torch.as_tensor(eu, device="cuda"), torch.as_tensor(edu, device="cuda"))
+    jw, u, du = a["jw"].cpu().numpy(), a["u"].cpu().numpy(), a["du"].cpu().numpy()
+    r = eu - u
+    gr = np.sqrt(((edu - du) ** 2).sum(-1))
+    np.testing.assert_allclose(ue, [(np.abs(r) * jw[:, None]).sum(), np.sqrt((r ** 2 * jw[:, None]).sum()), np.abs(r).max()],
+                               rtol=1e-12)
+    np.testing.assert_allclose(ge, [(gr * jw[:, None]).sum(), np.sqrt((gr ** 2 * jw[:, None]).sum()), gr.max()], rtol=1e-12)
+
+
+def test_error_norms_of_an_exactly_represented_solution():
+    """u = x(1-x) y(1-y) z(1-z) lies in the p=2 space on an unperturbed mesh: errors at rounding level"""
+    npoints = (4, 4, 5)
+    fs = dg.FS(npoints, degree=2, perturb=0.0, seed=1)
+    o = po.FS(*npoints, degree=2, perturb=0.0, seed=1)
+    em, xs, ce = o.emap(), o.xstart(), o.coords_expanded()
+    gll = po.lobatto(3)[0]
+    f = lambda X: X[0] * (1 - X[0]) * X[1] * (1 - X[1]) * X[2] * (1 - X[2])
+    g = np.zeros(fs.n)
+    for e in range(o.nelem):
+        lo, hi = ce[e].min(0), ce[e].max(0)
+        for loc in range(27):
+            d = em[xs[e] + loc]
+            if d < fs.n:
+                ijk = (loc // 9, (loc // 3) % 3, loc % 3)
+                g[d] = f([lo[k] + (1 + gll[ijk[k]]) / 2 * (hi[k] - lo[k]) for k in range(3)])
+    it = dg.RulesetIterator(fs)
+    it.start(torch.as_tensor(g, device="cuda"))
+    a = it.get()
+    X = a["x"].cpu().numpy()
+    eu = f(X.T)[:, None]
+    edu = np.stack([(1 - 2 * X[:, 0]) * X[:, 1] * (1 - X[:, 1]) * X[:, 2] * (1 - X[:, 2]),
+                    X[:, 0] * (1 - X[:, 0]) * (1 - 2 * X[:, 1]) * X[:, 2] * (1 - X[:, 2]),
+                    X[:, 0] * (1 - X[:, 0]) * X[:, 1] * (1 - X[:, 1]) * (1 - 2 * X[:, 2])], -1)[:, None, :]
+    ue, ge = it.error_norms(torch.as_tensor(eu, device="cuda"), torch.as_tensor(edu, device="cuda"))
+    assert ue[2] < 1e-15 and ge[2] < 1e-13 and ue[1] < 1e-15
