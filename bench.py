@@ -37,6 +37,21 @@ E0, NU = 1.0, 0.3
 FP64_PEAK_GFLOPS = 1203.0  # FP64 FMA issue rate measured on this GB300 (FMA-chain probe)
 
 
+def max_over_ranks(v, dist, device="cuda"):
+    """Max of a per-rank time over all ranks: the replicas' only collective (no data-path exchange)."""
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_gdofs(world, dofs_per_rank, seconds):
+    """value: dofs of all replicas over the slowest rank's time"""
+    return world * dofs_per_rank / seconds / 1e9
+
+
 def _plain(o):
     """JSON fallback for numpy scalars."""
     return o.item() if hasattr(o, "item") else str(o)
@@ -492,9 +507,7 @@ def main():
     if cfg["hp"]:
         forms["graph_ms"] = ms_step
     if dist:
-        t = torch.tensor([ms_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
+        ms_step = max_over_ranks(ms_step, dist)
         dist.barrier()
 
     # end to end through the host-vector entry point (pinned buffers, copies inside the timed region)
@@ -510,9 +523,7 @@ def main():
         op.mult_host(xn, yn)
     e2e_s = (time.perf_counter() - t_e) / e2e_steps
     if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+        e2e_s = max_over_ranks(e2e_s, dist)
     if rank != 0:
         dist.destroy_process_group()
         return
@@ -520,7 +531,7 @@ def main():
     hbm, src = peaks()
     alg_bytes, alg_flops, issued = work_per_apply(fs, cfg, bs)
     achieved = alg_bytes / (kms * 1e-3) / 1e9
-    value = world * N / (ms_step * 1e-3) / 1e9
+    value = whole_job_gdofs(world, N, ms_step * 1e-3)
     line = {
         "metric": "GDoF/s operator apply", "value": value, "unit": "GDoF/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -535,7 +546,7 @@ def main():
         "fp64_roofline": {"bound": "fp64 pipe", "achieved": issued / (kms * 1e-3) / 1e9, "peak": FP64_PEAK_GFLOPS,
                           "unit": "GFLOP/s", "frac": issued / (kms * 1e-3) / 1e9 / FP64_PEAK_GFLOPS,
                           "issued_flops_per_launch": issued, "alg_flops_per_launch": alg_flops},
-        "e2e": {"value": world * N / e2e_s / 1e9, "unit": "GDoF/s", "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N,
+        "e2e": {"value": whole_job_gdofs(world, N, e2e_s), "unit": "GDoF/s", "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N,
                 "entry_point": "dOperatorMultHost"},
         "gpu_launches": 2 * args.steps,
         "clocks": clk.summary(),
