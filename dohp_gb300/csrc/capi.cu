@@ -344,9 +344,11 @@ dErr dMatDestroy(dMat *J) {
   cudaFree((*J)->d_rowptr);
   cudaFree((*J)->d_col);
   cudaFree((*J)->d_val);
-  cudaFree((*J)->d_val32);
   cudaFree((*J)->d_srowptr);
   cudaFree((*J)->d_scol);
+  cudaFree((*J)->d_sell_off);
+  cudaFree((*J)->d_sell_col);
+  cudaFree((*J)->d_sell_val);
   delete *J;
   *J = nullptr;
   return 0;

@@ -128,8 +128,17 @@ struct _p_dMat {
   int64_t nrows = 0, nnz = 0;
   int32_t *d_rowptr = nullptr, *d_col = nullptr;
   double *d_val = nullptr;
-  float *d_val32 = nullptr;
   // bs > 1: the node (scalar) pattern the blocked CSR expands
   int64_t snnz = 0;
   int32_t *d_srowptr = nullptr, *d_scol = nullptr;
+  // sliced-ELL copy the SpMV runs on (32-row slices, column-major, padded to the slice's longest row):
+  // slice s holds entries [d_sell_off[s], d_sell_off[s+1]); built from the CSR on first use, values refreshed
+  // after each numeric assembly (sell_valid false)
+  int64_t sell_len = 0;
+  int64_t *d_sell_off = nullptr;
+  int32_t *d_sell_col = nullptr;
+  double *d_sell_val = nullptr;
+  bool sell_valid = false;
 };
+
+dErr mat_sell(_p_dMat *J, cudaStream_t s);

@@ -1,4 +1,4 @@
-// Device linear algebra for the solvers: exclusive scan, CSR SpMV, deterministic dot products,
+// Device linear algebra for the solvers: exclusive scan, sliced-ELL SpMV, deterministic dot products,
 // Chebyshev-Jacobi smoothing on the Q1 matrix, preconditioned CG and FGMRES.
 //
 // PETSc KSPCG / KSPFGMRES / KSPCHEBYSHEV+PCJACOBI are the reference's solvers (not vendored); these are
@@ -44,29 +44,54 @@ __global__ void k_scan_add(int32_t *out, int64_t n, const int64_t *block_offsets
   if (i == 0) out[n] = (int32_t)total;
 }
 
-// FP32 vectors, BF16 values, FP32 accumulation
-__global__ void k_spmv_bf16(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ col,
-                            const __nv_bfloat16 *__restrict__ val, const float *__restrict__ x, float *__restrict__ y) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float s = 0;
-  for (int32_t k = rp[i]; k < rp[i + 1]; k++) s = fmaf(__bfloat162float(val[k]), x[col[k]], s);
-  y[i] = s;
-}
-
 __global__ void k_val_to_bf16(int64_t n, const double *__restrict__ a, __nv_bfloat16 *__restrict__ b) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) b[i] = __float2bfloat16_rn((float)a[i]);
 }
 
-template <typename T>
-__global__ void k_spmv(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ col, const T *__restrict__ val,
+// Sliced ELL (SELL-32): rows in slices of 32, each slice stored column-major and padded to its longest row, so
+// at step k the 32 lanes of a warp read 32 consecutive values and column indices. With the row-per-thread CSR
+// loop each lane walks its own row and a warp touches 32 cache lines per step; on the 27-point Q1 rows that
+// ran at 2.7 TB/s against 5.1-5.7 TB/s for this layout. Padding points at the row itself with value 0, so a
+// row's sum runs over its CSR entries in CSR order plus exact zeros: the result equals the CSR loop's.
+__device__ __forceinline__ double sell_val(double v) { return v; }
+__device__ __forceinline__ float sell_val(float v) { return v; }
+__device__ __forceinline__ float sell_val(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+template <typename V, typename T>
+__global__ void k_sell(int64_t n, const int64_t *__restrict__ off, const int32_t *__restrict__ col, const V *__restrict__ val,
                        const T *__restrict__ x, T *__restrict__ y) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const int64_t b = off[i >> 5] + (i & 31), w = (off[(i >> 5) + 1] - off[i >> 5]) >> 5;
   T s = 0;
-  for (int32_t k = rp[i]; k < rp[i + 1]; k++) s += val[k] * x[col[k]];
+  for (int64_t k = 0; k < w; k++) s += sell_val(val[b + 32 * k]) * x[col[b + 32 * k]];
   y[i] = s;
+}
+
+// one thread per row of the padded slices (32 * nslices threads): the slice width is the warp's max row length
+__global__ void k_sell_width(int64_t n, const int32_t *__restrict__ rp, int64_t nslices, int32_t *__restrict__ w) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= 32 * nslices) return;  // whole warps only: 32 * nslices is a multiple of 32
+  const int32_t len = i < n ? rp[i + 1] - rp[i] : 0;
+  const int32_t m = __reduce_max_sync(0xffffffffu, len);
+  if ((i & 31) == 0) w[i >> 5] = m;
+}
+
+// scatter CSR values (and, when scol is given, column indices) into the slices
+__global__ void k_sell_fill(int64_t n, int64_t nslices, const int32_t *__restrict__ rp, const int32_t *__restrict__ col,
+                            const double *__restrict__ val, const int64_t *__restrict__ off, int32_t *__restrict__ scol,
+                            double *__restrict__ sval) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= 32 * nslices) return;
+  const int64_t b = off[i >> 5] + (i & 31), w = (off[(i >> 5) + 1] - off[i >> 5]) >> 5;
+  const int32_t r0 = i < n ? rp[i] : 0, len = i < n ? rp[i + 1] - r0 : 0;
+  const int32_t self = (int32_t)(i < n ? i : n - 1);
+  for (int64_t k = 0; k < w; k++) {
+    const bool in = k < len;
+    if (scol) scol[b + 32 * k] = in ? col[r0 + k] : self;
+    sval[b + 32 * k] = in ? val[r0 + k] : 0.0;
+  }
 }
 
 __global__ void k_dot_partial(int64_t n, const double *__restrict__ a, const double *__restrict__ b, double *__restrict__ part) {
@@ -237,9 +262,40 @@ dErr device_exclusive_scan(const int32_t *in, int32_t *out, int64_t n, cudaStrea
   return 0;
 }
 
+// build the sliced-ELL copy of J's CSR (pattern once, values whenever an assembly has changed them)
+dErr mat_sell(_p_dMat *J, cudaStream_t s) {
+  if (J->sell_valid || J->nrows == 0) return 0;
+  const int64_t n = J->nrows, ns = (n + 31) / 32;
+  const bool pattern = !J->d_sell_off;
+  if (pattern) {
+    int32_t *d_w;
+    CUCHK(cudaMalloc(&d_w, ns * sizeof(int32_t)));
+    k_sell_width<<<nb(32 * ns), 256, 0, s>>>(n, J->d_rowptr, ns, d_w);
+    CUCHK(cudaGetLastError());
+    std::vector<int32_t> w(ns);
+    CUCHK(cudaMemcpyAsync(w.data(), d_w, ns * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CUCHK(cudaStreamSynchronize(s));
+    cudaFree(d_w);
+    std::vector<int64_t> off(ns + 1, 0);
+    for (int64_t i = 0; i < ns; i++) off[i + 1] = off[i] + 32 * (int64_t)w[i];
+    J->sell_len = off[ns];
+    CUCHK(cudaMalloc(&J->d_sell_off, (ns + 1) * sizeof(int64_t)));
+    CUCHK(cudaMalloc(&J->d_sell_col, std::max<int64_t>(J->sell_len, 1) * sizeof(int32_t)));
+    CUCHK(cudaMalloc(&J->d_sell_val, std::max<int64_t>(J->sell_len, 1) * sizeof(double)));
+    CUCHK(cudaMemcpyAsync(J->d_sell_off, off.data(), (ns + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+  }
+  k_sell_fill<<<nb(32 * ns), 256, 0, s>>>(n, ns, J->d_rowptr, J->d_col, J->d_val, J->d_sell_off, pattern ? J->d_sell_col : nullptr,
+                                          J->d_sell_val);
+  CUCHK(cudaGetLastError());
+  CUCHK(cudaStreamSynchronize(s));  // the host vector above must outlive its copy
+  J->sell_valid = true;
+  return 0;
+}
+
 dErr mat_mult(_p_dMat *J, const double *x, double *y, cudaStream_t s) {
   if (J->nrows == 0) return 0;
-  k_spmv<double><<<nb(J->nrows), 256, 0, s>>>(J->nrows, J->d_rowptr, J->d_col, J->d_val, x, y);
+  DCHK(mat_sell(J, s));
+  k_sell<double, double><<<nb(J->nrows), 256, 0, s>>>(J->nrows, J->d_sell_off, J->d_sell_col, J->d_sell_val, x, y);
   CUCHK(cudaGetLastError());
   return 0;
 }
@@ -356,8 +412,10 @@ static dErr pc_setup(_p_dKSP *k) {
 // z = M^{-1} r
 // Chebyshev-Jacobi on the Q1 matrix in FP32 (values, vectors and arithmetic), FP64 in/out
 static dErr pc_apply_fp32(_p_dKSP *k, const double *r, double *z) {
-  const int64_t n = k->n, nnz = k->pmat->nnz;
+  _p_dMat *J = k->pmat;
   cudaStream_t s = k->op->fs->stream;
+  DCHK(mat_sell(J, s));
+  const int64_t n = k->n, nnz = J->sell_len;  // values converted in the sliced layout, padding included
   const bool bf = k->pc_prec == dPREC_BF16;
   if (!k->d_w32) {
     CUCHK(cudaMalloc(&k->d_w32, 5 * std::max<int64_t>(n, 1) * sizeof(float)));
@@ -366,11 +424,11 @@ static dErr pc_apply_fp32(_p_dKSP *k, const double *r, double *z) {
   }
   if (!bf && !k->d_val32) {
     CUCHK(cudaMalloc(&k->d_val32, std::max<int64_t>(nnz, 1) * sizeof(float)));
-    k_convert<double, float><<<nb(nnz), 256, 0, s>>>(nnz, k->pmat->d_val, k->d_val32);
+    k_convert<double, float><<<nb(nnz), 256, 0, s>>>(nnz, J->d_sell_val, k->d_val32);
   }
   if (bf && !k->d_val16) {
     CUCHK(cudaMalloc(&k->d_val16, std::max<int64_t>(nnz, 1) * sizeof(__nv_bfloat16)));
-    k_val_to_bf16<<<nb(nnz), 256, 0, s>>>(nnz, k->pmat->d_val, k->d_val16);
+    k_val_to_bf16<<<nb(nnz), 256, 0, s>>>(nnz, J->d_sell_val, k->d_val16);
   }
   float *r32 = k->d_w32, *z32 = r32 + n, *d32 = z32 + n, *w32 = d32 + n;
   k_convert<double, float><<<nb(n), 256, 0, s>>>(n, r, r32);
@@ -378,8 +436,8 @@ static dErr pc_apply_fp32(_p_dKSP *k, const double *r, double *z) {
   double rho = 1.0 / sigma;
   k_cheb_first_t<float><<<nb(n), 256, 0, s>>>(n, k->d_dinv32, r32, (float)(1.0 / theta), d32, z32);
   for (int it = 1; it < k->cheb_degree; it++) {
-    if (bf) k_spmv_bf16<<<nb(n), 256, 0, s>>>(n, k->pmat->d_rowptr, k->pmat->d_col, k->d_val16, z32, w32);
-    else k_spmv<float><<<nb(n), 256, 0, s>>>(n, k->pmat->d_rowptr, k->pmat->d_col, k->d_val32, z32, w32);
+    if (bf) k_sell<__nv_bfloat16, float><<<nb(n), 256, 0, s>>>(n, J->d_sell_off, J->d_sell_col, k->d_val16, z32, w32);
+    else k_sell<float, float><<<nb(n), 256, 0, s>>>(n, J->d_sell_off, J->d_sell_col, k->d_val32, z32, w32);
     const double rho1 = 1.0 / (2.0 * sigma - rho);
     k_cheb_step_t<float><<<nb(n), 256, 0, s>>>(n, k->d_dinv32, r32, w32, (float)(rho1 * rho), (float)(2.0 * rho1 / delta), d32, z32);
     rho = rho1;

@@ -453,10 +453,7 @@ dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk, const
   cudaFree(d_rules);
   cudaFree(d_K);
   cudaFree(d_grf);
-  if (J->d_val32) {
-    cudaFree(J->d_val32);
-    J->d_val32 = nullptr;
-  }
+  J->sell_valid = false;
   return 0;
 }
 
@@ -493,9 +490,6 @@ dErr q1_numeric_elast(_p_dFS *fs, _p_dMat *J, double lam, double mu, int quirk) 
   cudaFree(d_pstart);
   cudaFree(d_rules);
   cudaFree(d_K);
-  if (J->d_val32) {
-    cudaFree(J->d_val32);
-    J->d_val32 = nullptr;
-  }
+  J->sell_valid = false;
   return 0;
 }
