@@ -18,6 +18,7 @@ dAPPLY_INTERP, dAPPLY_INTERP_TRANSPOSE, dAPPLY_GRAD, dAPPLY_GRAD_TRANSPOSE = 400
 INSERT_VALUES, ADD_VALUES = 1, 2
 dFS_HOMOGENEOUS, dFS_INHOMOGENEOUS = 0, 1
 FAST, SPARSE, SELF = 0, 1, 2
+dFSBSTATUS_DIRICHLET, dFSBSTATUS_WEAK = 1 << 16, 1 << 17
 dOP_DIFFUSION, dOP_PLAPLACE_JACOBIAN, dOP_ELASTICITY = 0, 1, 2
 dPREC_FP64, dPREC_FP32, dPREC_BF16 = 0, 1, 2
 dKSP_CG, dKSP_FGMRES = 0, 1
@@ -103,7 +104,7 @@ class FS:
     """dFS on a seeded perturbed block mesh (dMeshGenerateBlock + dFSBuildSpace)."""
 
     def __init__(self, npoints, degree=4, box=(0, 1, 0, 1, 0, 1), perturb=0.1, seed=1, bs=1,
-                 dirichlet=(100, 200, 300), elem_degree=None, stream=None):
+                 dirichlet=(100, 200, 300), elem_degree=None, stream=None, weak=()):
         L = lib()
         self.mesh = _vp()
         chk(L.dMeshCreateBlock(ptr(np.asarray(npoints, np.int32)), ptr(np.asarray(box, np.float64)), _dbl(perturb),
@@ -114,8 +115,9 @@ class FS:
         ed = None if elem_degree is None else np.ascontiguousarray(elem_degree, np.int32)
         chk(L.dFSSetDegree(self.h, _i32(degree), ptr(ed)))
         chk(L.dFSSetBlockSize(self.h, _i32(bs)))
-        for s in dirichlet:
-            chk(L.dFSRegisterBoundary(self.h, _i32(s), ctypes.c_int(1)))
+        for s in set(dirichlet) | set(weak):
+            st = (dFSBSTATUS_DIRICHLET if s in dirichlet else 0) | (dFSBSTATUS_WEAK if s in weak else 0)
+            chk(L.dFSRegisterBoundary(self.h, _i32(s), ctypes.c_int(st)))
         if stream is not None:
             chk(L.dFSSetStream(self.h, _vp(stream)))
         chk(L.dFSSetUp(self.h))
@@ -350,6 +352,59 @@ class RulesetIterator:
         ue, ge = np.zeros(3), np.zeros(3)
         chk(lib().dRulesetIteratorErrorNorms(self.h, ptr(exact_u), ptr(exact_du), ptr(ue), ptr(ge)))
         return ue, ge
+
+
+class FacetIterator:
+    """dFacetIterator over the faces of the weak sets (FAST rules). get() returns torch views of the library's
+    facet-point arrays: jw[nq] (area weight), x[nq,3], normal[nq,3], u[nq,bs], v[nq,bs] (writable, zeroed)."""
+
+    def __init__(self, fs, method=FAST):
+        self.fs = fs
+        self.h = _vp()
+        chk(lib().dFacetIteratorCreate(fs.h, ctypes.c_int(method), ctypes.byref(self.h)))
+
+    def __del__(self):
+        if _lib is not None and getattr(self, "h", None):
+            _lib.dFacetIteratorDestroy(ctypes.byref(self.h))
+
+    def facets(self):
+        """(element, side, point offsets) as numpy arrays"""
+        nf = _i64()
+        p = [ctypes.POINTER(ctypes.c_int32)() for _ in range(3)]
+        chk(lib().dFacetIteratorGetFacets(self.h, ctypes.byref(nf), *[ctypes.byref(q) for q in p]))
+        n = nf.value
+        if n == 0:
+            return np.zeros(0, np.int32), np.zeros(0, np.int32), np.zeros(1, np.int32)
+        return tuple(np.ctypeslib.as_array(q, shape=(m,)).copy() for q, m in zip(p, (n, n, n + 1)))
+
+    def start(self, g=None, hmode=dFS_HOMOGENEOUS):
+        chk(lib().dFacetIteratorStart(self.h, ptr(g), ctypes.c_int(hmode)))
+
+    def get(self):
+        import torch
+        nq = _i64()
+        p = [_vp() for _ in range(5)]
+        chk(lib().dFacetIteratorGetApplied(self.h, ctypes.byref(nq), *[ctypes.byref(q) for q in p]))
+        n, bs = nq.value, self.fs.bs
+        if n == 0:
+            return {k: torch.zeros(s, dtype=torch.float64, device="cuda") for k, s in
+                    zip(["jw", "x", "normal", "u", "v"], [(0,), (0, 3), (0, 3), (0, bs), (0, bs)])}
+        shapes = [(n,), (n, 3), (n, 3), (n, bs), (n, bs)]
+        names = ["jw", "x", "normal", "u", "v"]
+        return {k: torch.as_tensor(_DeviceArray(q.value, s), device="cuda") for k, q, s in zip(names, p, shapes)}
+
+    def commit(self, imode=ADD_VALUES):
+        chk(lib().dFacetIteratorCommit(self.h, ctypes.c_int(imode)))
+
+    def finish(self, y=None, imode=INSERT_VALUES):
+        chk(lib().dFacetIteratorFinish(self.h, ptr(y), ctypes.c_int(imode)))
+
+
+def facet_rule(side, order, method=FAST):
+    """dFSGetFacetRule: nodes [n,3] in hex reference coordinates and weights [n]"""
+    nodes, w, n = np.zeros(3 * 81), np.zeros(81), _i32()
+    chk(lib().dFSGetFacetRule(_i32(side), ctypes.c_int(method), _i32(order), ctypes.byref(n), ptr(nodes), ptr(w)))
+    return nodes[:3 * n.value].reshape(-1, 3), w[:n.value]
 
 
 class dNewtonOptions(ctypes.Structure):

@@ -180,8 +180,11 @@ dErr dFSRegisterBoundary(dFS fs, dInt setid, dFSBStatus status) {
   if (!fs) return set_error("null dFS");
   const int bit = setid == 100 ? 0 : setid == 200 ? 1 : setid == 300 ? 2 : -1;
   if (bit < 0) return set_error("unknown boundary set %d (block meshes have 100, 200, 300)", setid);
-  if (status == dFSBSTATUS_DIRICHLET) fs->dirichlet_mask |= 1 << bit;
+  if (status & ~(dFSBSTATUS_DIRICHLET | dFSBSTATUS_WEAK | 0xffff)) return set_error("unknown boundary status %#x", (unsigned)status);
+  if (status & dFSBSTATUS_DIRICHLET) fs->dirichlet_mask |= 1 << bit;
   else fs->dirichlet_mask &= ~(1 << bit);
+  if (status & dFSBSTATUS_WEAK) fs->weak_mask |= 1 << bit;
+  else fs->weak_mask &= ~(1 << bit);
   return 0;
 }
 

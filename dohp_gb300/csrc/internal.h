@@ -73,7 +73,8 @@ struct _p_dFS {
   int bs = 1;
   int degree = 0;
   std::vector<int> elem_degree_in;
-  int dirichlet_mask = 0;
+  int dirichlet_mask = 0;  // bit0 set 100 (walls), bit1 200 (top), bit2 300 (bottom)
+  int weak_mask = 0;       // sets registered with dFSBSTATUS_WEAK, same bits
   bool built = false;  // host maps computed (dFSBuildSpace)
   bool setup = false;  // device arrays uploaded
   cudaStream_t stream = 0;

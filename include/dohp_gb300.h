@@ -42,8 +42,13 @@ typedef enum { NOT_SET_VALUES = 0, INSERT_VALUES = 1, ADD_VALUES = 2 } InsertMod
 typedef enum { dFS_HOMOGENEOUS, dFS_INHOMOGENEOUS } dFSHomogeneousMode;
 /* include/dohpjacobi.h:141-148 */
 typedef enum { dQUADRATURE_METHOD_FAST, dQUADRATURE_METHOD_SPARSE, dQUADRATURE_METHOD_SELF } dQuadratureMethod;
-/* include/dohpfs.h:41-47 (only Dirichlet is supported on this path) */
-typedef enum { dFSBSTATUS_INTERIOR = 0, dFSBSTATUS_DIRICHLET = 1 } dFSBStatus;
+/* include/dohpfs.h:41-47: the reference's values (the low 16 bits hold a count of strongly enforced dofs, unused
+ * here). DIRICHLET removes the set's nodes from the global space; WEAK puts its faces in the facet iterator. */
+typedef enum {
+  dFSBSTATUS_INTERIOR = 0,
+  dFSBSTATUS_DIRICHLET = (0xffff + 1) << 0,
+  dFSBSTATUS_WEAK = (0xffff + 1) << 1
+} dFSBStatus;
 
 typedef struct _p_dJacobi *dJacobi;
 typedef struct _p_dEFS *dEFS;
@@ -53,6 +58,7 @@ typedef struct _p_dOperator *dOperator;
 typedef struct _p_dMat *dMat;
 typedef struct _p_dRulesetIterator *dRulesetIterator;
 typedef struct _p_dKSP *dKSP;
+typedef struct _p_dFacetIterator *dFacetIterator;
 
 /* Operator (pointwise q-function) kinds of the fused matrix-free apply */
 typedef enum {
@@ -205,6 +211,31 @@ dErr dRulesetIteratorFinish(dRulesetIterator it, dScalar *y, InsertMode imode);
  * either may be NULL, e.g. exact values computed from the x that GetPatchApplied returned) */
 dErr dRulesetIteratorErrorNorms(dRulesetIterator it, const dScalar *exact_u, const dScalar *exact_du, dReal uerr[3],
                                 dReal gerr[3]);
+
+/* ---------------------------------------------------------------- facet rules and boundary integrals */
+/* dQuadratureGetFacetRules (include/dohpjacobi.h:210; src/jacobi/quadrature/impls/tensor/tensorquad.c:309-355) and
+ * dRuleGetNodeWeight_Transformed (tensorquad.c:224-242) for one side of the reference hex: the tensor Gauss rule of
+ * the given 1-D order on [-1,1]^2 (X slowest), mapped by xi = R_side (X, Y, 0) + t_side. Sides in the MOAB order
+ * 0: y=-1, 1: x=+1, 2: y=+1, 3: x=-1, 4: z=-1, 5: z=+1; R_side's third column is the outward normal.
+ * nodes [n][3], weights [n]; room for 81 nodes covers orders up to 16 (FAST). Host only. */
+dErr dFSGetFacetRule(dInt side, dQuadratureMethod method, dInt order, dInt *nnodes, dReal *nodes, dReal *weights);
+/* Batched facet iterator over the faces of the sets registered with dFSBSTATUS_WEAK (the reference's weakFace set,
+ * src/fs/interface/fsbuild.c:87-90), the boundary analogue of the dRulesetIterator: FAST rules (p+1 Gauss points
+ * per face direction, order 2p as the volume rule), facets in (element, side) order, points X-major per facet.
+ * Any space (uniform or per-element orders, bs 1 or 3). */
+dErr dFacetIteratorCreate(dFS fs, dQuadratureMethod method, dFacetIterator *it);
+dErr dFacetIteratorDestroy(dFacetIterator *it);
+/* host arrays owned by the iterator: element and side of each facet, point offsets per facet [nfacets+1] */
+dErr dFacetIteratorGetFacets(dFacetIterator it, int64_t *nfacets, const dInt **elem, const dInt **side, const dInt **qoffset);
+dErr dFacetIteratorStart(dFacetIterator it, const dScalar *g, dFSHomogeneousMode hmode);
+/* device pointers: jw[nq] = w_X w_Y |t_X x t_Y| (area weight), x[nq][3] physical points, normal[nq][3] outward unit
+ * normals, u[nq][bs] the field of Start's g at the points; v[nq][bs] is the writable test array (zeroed) */
+dErr dFacetIteratorGetApplied(dFacetIterator it, int64_t *nq, const dReal **jw, const dReal **x, const dReal **normal,
+                              const dScalar **u, dScalar **v);
+/* integrate v back: y_exp[i] (+)= sum_q phi_i(xi_q) v_q over the facet points (v carries the caller's jw) */
+dErr dFacetIteratorCommit(dFacetIterator it, InsertMode imode);
+/* restrict the expanded boundary vector into y (INSERT_VALUES overwrites, ADD_VALUES adds to a volume residual) */
+dErr dFacetIteratorFinish(dFacetIterator it, dScalar *y, InsertMode imode);
 
 /* ---------------------------------------------------------------- Q1-embedded preconditioning matrix */
 /* dFSCreateMatrix (src/fs/interface/fs.c:770-813) as a device CSR over explicit scalar dofs; the sparsity is

@@ -1582,3 +1582,180 @@ int or_cg_solve(const or_fs *m, int kind, const double *qdata, const double *par
   free(r); free(z); free(p); free(q); free(dinv); free(w); free(d);
   return its;
 }
+
+/* ----------------------------------------------------------------------------------------------
+ * Facet rules and boundary integrals over the faces of weak boundary sets
+ * -------------------------------------------------------------------------------------------- */
+/* The side transforms of dQuadratureGetFacetRules_Tensor_Private (tensorquad.c:324-331): a node (X, Y) of the
+ * reference quad maps to xi = R (X, Y, 0) + t on side s of the reference hex (dRuleGetNodeWeight_Transformed,
+ * tensorquad.c:224-242). The reference's quad rule has no node accessor (ruletopo.c:184), so the quad node order is
+ * this restatement's convention: X slowest. */
+static const double or_side_R[6][3][3] = {
+  {{1, 0, 0}, {0, 0, -1}, {0, 1, 0}},  {{0, 0, 1}, {1, 0, 0}, {0, 1, 0}},   {{-1, 0, 0}, {0, 0, 1}, {0, 1, 0}},
+  {{0, 0, -1}, {-1, 0, 0}, {0, 1, 0}}, {{0, 1, 0}, {1, 0, 0}, {0, 0, -1}}, {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}}};
+static const double or_side_t[6][3] = {{0, -1, 0}, {1, 0, 0}, {0, 1, 0}, {-1, 0, 0}, {0, 0, -1}, {0, 0, 1}};
+
+int or_facet_rule(int side, int method, int order, double *nodes, double *weights)
+{
+  double x[128], w[128];
+  if (side < 0 || side > 5) return or_fail("side %d out of range", side);
+  const int n = or_rule_1d(method, 0, order, x, w);
+  if (n < 0) return -1;
+  for (int a = 0; a < n; a++)
+    for (int b = 0; b < n; b++) {
+      const double ref[3] = {x[a], x[b], 0.0};
+      for (int c = 0; c < 3; c++)
+        nodes[3 * (a * n + b) + c] = or_side_R[side][c][0] * ref[0] + or_side_R[side][c][1] * ref[1] +
+                                     or_side_R[side][c][2] * ref[2] + or_side_t[side][c];
+      weights[a * n + b] = w[a] * w[b];
+    }
+  return n * n;
+}
+
+/* the faces of the weak sets (bit0 100 walls, bit1 200 top, bit2 300 bottom; generator face sets 0..3 -> 100,
+ * 4 -> 300, 5 -> 200) as (region, side) pairs in region order, sides in the canonical order of the adjacency */
+static int64_t facet_list(const or_fs *m, int weak_mask, int32_t *fel, int32_t *fside)
+{
+  static const int setbit[6] = {0, 0, 0, 0, 2, 1};
+  const int64_t R0 = m->nv + m->ne + m->nf;
+  int64_t nf = 0;
+  for (int64_t r = 0; r < m->nr; r++)
+    for (int s = 0; s < 6; s++) {
+      const int st = m->fset[m->adjind[m->adjoff[R0 + r] + s]];
+      if (st < 0 || !((weak_mask >> setbit[st]) & 1)) continue;
+      if (fel) { fel[nf] = (int32_t)r; fside[nf] = s; }
+      nf++;
+    }
+  return nf;
+}
+
+/* direction of the reference hex that the facet's X (k=0) or Y (k=1) axis runs along */
+static int side_axis(int s, int k)
+{
+  for (int c = 0; c < 3; c++)
+    if (or_side_R[s][c][k] != 0) return c;
+  return -1;
+}
+
+int64_t or_facet_count(const or_fs *m, int weak_mask, int64_t *nfacets, int32_t *fel, int32_t *fside, int32_t *qoff)
+{
+  const int64_t nf = facet_list(m, weak_mask, NULL, NULL);
+  int32_t *e = malloc(sizeof(int32_t) * (nf + 1)), *s = malloc(sizeof(int32_t) * (nf + 1));
+  facet_list(m, weak_mask, e, s);
+  int64_t nq = 0;
+  if (qoff) qoff[0] = 0;
+  for (int64_t f = 0; f < nf; f++) {
+    const int r = e[f];
+    nq += (int64_t)(m->edeg[3 * r + side_axis(s[f], 0)] + 1) * (m->edeg[3 * r + side_axis(s[f], 1)] + 1);
+    if (fel) { fel[f] = e[f]; fside[f] = s[f]; }
+    if (qoff) qoff[f + 1] = (int32_t)nq;
+  }
+  free(e); free(s);
+  if (nfacets) *nfacets = nf;
+  return nq;
+}
+
+/* for one facet point: reference point xi, 1-D Lagrange values of the field's GLL basis per direction (full
+ * element: all P_c nodes, evaluated at xi_c by the TensorBasisCreate evaluation), area vector and physical point */
+typedef struct { double xi[3], w, L[3][16], x[3], cr[3]; int P[3]; } facet_pt;
+
+static int facet_point(const or_fs *m, int r, int s, int a, int b, facet_pt *fp)
+{
+  const int cx = side_axis(s, 0), cy = side_axis(s, 1);
+  double gx[16], gwx[16], gy[16], gwy[16], node[16], weight[16], dd[16], ci[3][2], cd[3][2];
+  for (int c = 0; c < 3; c++) fp->P[c] = m->edeg[3 * r + c] + 1;
+  if (or_rule_1d(0, 0, 2 * (fp->P[cx] - 1), gx, gwx) < 0 || or_rule_1d(0, 0, 2 * (fp->P[cy] - 1), gy, gwy) < 0) return -1;
+  const double ref[3] = {gx[a], gy[b], 0.0};
+  for (int c = 0; c < 3; c++)
+    fp->xi[c] = or_side_R[s][c][0] * ref[0] + or_side_R[s][c][1] * ref[1] + or_side_R[s][c][2] * ref[2] + or_side_t[s][c];
+  fp->w = gwx[a] * gwy[b];
+  for (int c = 0; c < 3; c++) {
+    if (or_tensor_basis(fp->P[c], 1, &fp->xi[c], fp->L[c], dd, node, weight)) return -1;
+    if (or_tensor_basis(2, 1, &fp->xi[c], ci[c], cd[c], node, weight)) return -1;
+  }
+  /* coordinate FS (Q1, tensor vertex order): x and J = dx/dxi */
+  const double *X = m->xexp + (int64_t)r * 24;
+  double J[3][3] = {{0}};
+  for (int d = 0; d < 3; d++) fp->x[d] = 0;
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++)
+      for (int k = 0; k < 2; k++) {
+        const double *v = X + 3 * ((i * 2 + j) * 2 + k);
+        for (int d = 0; d < 3; d++) {
+          fp->x[d] += ci[0][i] * ci[1][j] * ci[2][k] * v[d];
+          J[d][0] += cd[0][i] * ci[1][j] * ci[2][k] * v[d];
+          J[d][1] += ci[0][i] * cd[1][j] * ci[2][k] * v[d];
+          J[d][2] += ci[0][i] * ci[1][j] * cd[2][k] * v[d];
+        }
+      }
+  double tx[3], ty[3];
+  for (int d = 0; d < 3; d++) {
+    tx[d] = ty[d] = 0;
+    for (int c = 0; c < 3; c++) { tx[d] += J[d][c] * or_side_R[s][c][0]; ty[d] += J[d][c] * or_side_R[s][c][1]; }
+  }
+  fp->cr[0] = tx[1] * ty[2] - tx[2] * ty[1];
+  fp->cr[1] = tx[2] * ty[0] - tx[0] * ty[2];
+  fp->cr[2] = tx[0] * ty[1] - tx[1] * ty[0];
+  return 0;
+}
+
+int or_facet_points(const or_fs *m, int weak_mask, const double *g, double *jw, double *x, double *nrm, double *u)
+{
+  int64_t nf;
+  or_facet_count(m, weak_mask, &nf, NULL, NULL, NULL);
+  int32_t *fel = malloc(sizeof(int32_t) * (nf + 1)), *fside = malloc(sizeof(int32_t) * (nf + 1)), *qoff = malloc(sizeof(int32_t) * (nf + 1));
+  or_facet_count(m, weak_mask, &nf, fel, fside, qoff);
+  const int bs = m->bs;
+  double *xe = calloc((size_t)m->nexp * bs, sizeof(double));
+  if (g) or_fs_global_to_expanded(m, g, NULL, xe);
+  int rc = 0;
+  for (int64_t f = 0; f < nf && !rc; f++) {
+    const int r = fel[f], s = fside[f], nY = m->edeg[3 * r + side_axis(s, 1)] + 1;
+    for (int64_t q = qoff[f]; q < qoff[f + 1] && !rc; q++) {
+      facet_pt fp;
+      const int loc = (int)(q - qoff[f]);
+      if ((rc = facet_point(m, r, s, loc / nY, loc % nY, &fp))) break;
+      const double ar = sqrt(fp.cr[0] * fp.cr[0] + fp.cr[1] * fp.cr[1] + fp.cr[2] * fp.cr[2]);
+      jw[q] = fp.w * ar;
+      for (int d = 0; d < 3; d++) { x[3 * q + d] = fp.x[d]; nrm[3 * q + d] = fp.cr[d] / ar; }
+      for (int c = 0; c < bs; c++) { /* the whole element basis at the point */
+        double acc = 0;
+        for (int i = 0; i < fp.P[0]; i++)
+          for (int j = 0; j < fp.P[1]; j++)
+            for (int k = 0; k < fp.P[2]; k++)
+              acc += fp.L[0][i] * fp.L[1][j] * fp.L[2][k] * xe[((int64_t)m->xstart[r] + (i * fp.P[1] + j) * fp.P[2] + k) * bs + c];
+        u[q * bs + c] = acc;
+      }
+    }
+  }
+  free(fel); free(fside); free(qoff); free(xe);
+  return rc;
+}
+
+int or_facet_commit(const or_fs *m, int weak_mask, const double *v, double *y, int add)
+{
+  int64_t nf;
+  or_facet_count(m, weak_mask, &nf, NULL, NULL, NULL);
+  int32_t *fel = malloc(sizeof(int32_t) * (nf + 1)), *fside = malloc(sizeof(int32_t) * (nf + 1)), *qoff = malloc(sizeof(int32_t) * (nf + 1));
+  or_facet_count(m, weak_mask, &nf, fel, fside, qoff);
+  const int bs = m->bs;
+  double *ye = calloc((size_t)m->nexp * bs, sizeof(double));
+  int rc = 0;
+  for (int64_t f = 0; f < nf && !rc; f++) {
+    const int r = fel[f], s = fside[f], nY = m->edeg[3 * r + side_axis(s, 1)] + 1;
+    for (int64_t q = qoff[f]; q < qoff[f + 1]; q++) {
+      facet_pt fp;
+      const int loc = (int)(q - qoff[f]);
+      if ((rc = facet_point(m, r, s, loc / nY, loc % nY, &fp))) break;
+      for (int i = 0; i < fp.P[0]; i++)
+        for (int j = 0; j < fp.P[1]; j++)
+          for (int k = 0; k < fp.P[2]; k++) {
+            const double phi = fp.L[0][i] * fp.L[1][j] * fp.L[2][k];
+            for (int c = 0; c < bs; c++) ye[((int64_t)m->xstart[r] + (i * fp.P[1] + j) * fp.P[2] + k) * bs + c] += phi * v[q * bs + c];
+          }
+    }
+  }
+  if (!rc) or_fs_expanded_to_global(m, ye, y, add);
+  free(fel); free(fside); free(qoff); free(ye);
+  return rc;
+}

@@ -119,6 +119,20 @@ int64_t or_q1_assemble_plap(const or_fs *fs, double p, double eps, const double 
                             int32_t *rowptr, int32_t **col, double **val);
 void or_free(void *p);
 
+/* ---------------- facet rules and boundary integrals ---------------- */
+/* dQuadratureGetFacetRules_Tensor_Private (src/jacobi/quadrature/impls/tensor/tensorquad.c:309-355) with the node
+ * map of dRuleGetNodeWeight_Transformed (tensorquad.c:224-242): the 1-D rule of `order` squared (X slowest) on side
+ * `side` (0 y=-1, 1 x=+1, 2 y=+1, 3 x=-1, 4 z=-1, 5 z=+1). nodes [n][3], weights [n]; returns n or -1. */
+int or_facet_rule(int side, int method, int order, double *nodes, double *weights);
+/* faces of the weak sets (bit0 100, bit1 200, bit2 300) in (region, side) order; returns the number of FAST facet
+ * points ((p+1)^2 per face); fel/fside [nfacets], qoff [nfacets+1] optional */
+int64_t or_facet_count(const or_fs *fs, int weak_mask, int64_t *nfacets, int32_t *fel, int32_t *fside, int32_t *qoff);
+/* per facet point: jw = w |t_X x t_Y|, physical x, outward unit normal, and the field of g (homogeneous
+ * Dirichlet; NULL = 0) evaluated with the whole element basis at the point */
+int or_facet_points(const or_fs *fs, int weak_mask, const double *g, double *jw, double *x, double *nrm, double *u);
+/* y (+)= E^T sum_q phi(xi_q) v_q over the facet points (add = 0 insert, 1 add) */
+int or_facet_commit(const or_fs *fs, int weak_mask, const double *v, double *y, int add);
+
 /* deformation gradient F = I + Du [nq][9] at every FAST point of the state g (bs = 3, homogeneous Dirichlet;
  * ElastPointwiseComputeStore, elast.c:224-225) */
 int or_elast_state(const or_fs *fs, const double *g, double *Fq);

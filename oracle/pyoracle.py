@@ -92,6 +92,12 @@ def lib():
         L.or_cg_solve.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, _i32p, _i32p, _f64p,
                                   ctypes.c_int, _f64p, _f64p, ctypes.c_double, ctypes.c_int,
                                   ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+        L.or_facet_rule.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _f64p, _f64p]
+        L.or_facet_count.restype = ctypes.c_int64
+        L.or_facet_count.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int64), ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_void_p]
+        L.or_facet_points.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, _f64p, _f64p, _f64p, _f64p]
+        L.or_facet_commit.argtypes = [ctypes.c_void_p, ctypes.c_int, _f64p, _f64p, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -313,6 +319,29 @@ class FS:
         lib().or_free(ctypes.cast(valp, ctypes.c_void_p))
         return rp, col, val
 
+    def facets(self, weak_mask):
+        """(element, side, point offsets) of the faces of the weak sets"""
+        nf = ctypes.c_int64()
+        lib().or_facet_count(self.h, weak_mask, ctypes.byref(nf), None, None, None)
+        fel, fside, qoff = (np.zeros(nf.value + 1, np.int32) for _ in range(3))
+        lib().or_facet_count(self.h, weak_mask, ctypes.byref(nf), fel.ctypes.data, fside.ctypes.data, qoff.ctypes.data)
+        return fel[:nf.value], fside[:nf.value], qoff
+
+    def facet_points(self, weak_mask, g=None):
+        """jw [nq], x [nq,3], normal [nq,3], u [nq,bs] at the facet points"""
+        nq = lib().or_facet_count(self.h, weak_mask, None, None, None, None)
+        jw, x, nrm, u = np.zeros(nq), np.zeros(3 * nq), np.zeros(3 * nq), np.zeros(nq * self.bs)
+        gg = None if g is None else np.ascontiguousarray(g, np.float64)
+        if lib().or_facet_points(self.h, weak_mask, None if gg is None else gg.ctypes.data, jw, x, nrm, u):
+            raise RuntimeError(lib().or_last_error().decode())
+        return jw, x.reshape(nq, 3), nrm.reshape(nq, 3), u.reshape(nq, self.bs)
+
+    def facet_commit(self, weak_mask, v, y=None, add=False):
+        out = np.zeros(self.n * self.bs) if y is None else np.array(y, dtype=np.float64)
+        if lib().or_facet_commit(self.h, weak_mask, np.ascontiguousarray(v, np.float64).ravel(), out, 1 if add else 0):
+            raise RuntimeError(lib().or_last_error().decode())
+        return out
+
     def cg_solve(self, b, csr, kind=0, qdata=None, param=None, cheb_degree=3, rtol=1e-8, maxit=500, nthreads=1):
         rp, col, val = csr
         x = np.zeros(self.n * self.bs)
@@ -323,6 +352,15 @@ class FS:
                                 None if pa is None else pa.ctypes.data, rp, col, val, cheb_degree,
                                 np.ascontiguousarray(b, dtype=np.float64), x, rtol, maxit, ctypes.byref(rn), nthreads)
         return x, its, rn.value
+
+
+def facet_rule(side, order, method=0):
+    """nodes [n][3] and weights [n] of the facet rule on one hex side"""
+    nodes, w = np.zeros(3 * 4096), np.zeros(4096)
+    n = lib().or_facet_rule(side, method, order, nodes, w)
+    if n < 0:
+        raise RuntimeError(lib().or_last_error().decode())
+    return nodes[:3 * n].reshape(n, 3), w[:n]
 
 
 def grf_make(nf, var, ell, seed):

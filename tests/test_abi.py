@@ -36,7 +36,7 @@ def host_fs(npoints, degree, box=(0, 1, 0, 1, 0, 1), perturb=0.1, seed=1, bs=1, 
     dg.chk(L.dFSSetDegree(fs, ctypes.c_int32(degree), dg.ptr(ed)))
     dg.chk(L.dFSSetBlockSize(fs, ctypes.c_int32(bs)))
     for s in dirichlet:
-        dg.chk(L.dFSRegisterBoundary(fs, ctypes.c_int32(s), ctypes.c_int(1)))
+        dg.chk(L.dFSRegisterBoundary(fs, ctypes.c_int32(s), ctypes.c_int(dg.dFSBSTATUS_DIRICHLET)))
     rc = L.dFSBuildSpace(fs)
     if rc:
         msg = L.dGetLastError().decode()
@@ -83,7 +83,7 @@ def host_ecsr(npoints, degree, elem_degree, dirichlet=(100, 200, 300)):
     dg.chk(L.dFSCreate(mesh, None, ctypes.byref(fs)))
     dg.chk(L.dFSSetDegree(fs, ctypes.c_int32(degree), dg.ptr(np.ascontiguousarray(elem_degree, np.int32))))
     for s in dirichlet:
-        dg.chk(L.dFSRegisterBoundary(fs, ctypes.c_int32(s), ctypes.c_int(1)))
+        dg.chk(L.dFSRegisterBoundary(fs, ctypes.c_int32(s), ctypes.c_int(dg.dFSBSTATUS_DIRICHLET)))
     dg.chk(L.dFSBuildSpace(fs))
     sz = [ctypes.c_int32() for _ in range(5)]
     dg.chk(L.dFSGetSizes(fs, *[ctypes.byref(s) for s in sz]))
