@@ -58,25 +58,33 @@ __device__ void tmult(int D, const int P[3], const int Q[3], const double *const
   __syncthreads();
 }
 
-// one block per element; dynamic shared memory holds the element's input and temporaries
-__global__ void k_efs_apply(EFSDev f, int64_t nelem, const double *jinv, int D, const double *in, double *out, int amode, int imode) {
+// one block per element; dynamic shared memory holds the element's input and temporaries. Elements are
+// contiguous (element b at b * np nodes, b * nq points) unless an element list with node / point offsets is
+// given (the elements of one order in a mixed-order space: elist[b] = e, ioff[e] / ooff[e] = the element's first
+// input / output node or point)
+__global__ void k_efs_apply(EFSDev f, int64_t nelem, const int32_t *elist, const int32_t *ioff, const int32_t *ooff,
+                            const double *jinv, int D, const double *in, double *out, int amode, int imode) {
   extern __shared__ double sm[];
-  const int64_t e = blockIdx.x;
-  if (e >= nelem) return;
+  const int64_t b = blockIdx.x;
+  if (b >= nelem) return;
+  const int64_t e = elist ? elist[b] : b;
   const int P[3] = {f.P[0], f.P[1], f.P[2]}, Q[3] = {f.Q[0], f.Q[1], f.Q[2]};
   const int np = P[0] * P[1] * P[2], nq = Q[0] * Q[1] * Q[2], mx = max(np, nq) * D;
+  const bool fwd = amode == dAPPLY_INTERP || amode == dAPPLY_GRAD;
+  const int64_t ib = ioff ? (int64_t)ioff[e] : e * (fwd ? np : nq), ob = ooff ? (int64_t)ooff[e] : e * (fwd ? nq : np);
+  const int64_t qb = fwd ? ob : ib;  // first quadrature point of the element
   // generous scratch: each buffer holds max(P,Q)^3 * D
   const int m3 = max(max(P[0], Q[0]), max(max(P[1], Q[1]), max(P[2], Q[2])));
   const int buf = m3 * m3 * m3 * D;
   double *sin = sm, *t1 = sm + buf, *t2 = sm + 2 * buf, *g = sm + 3 * buf;  // g: 3 gradient buffers
   (void)mx;
   const bool add = imode == ADD_VALUES;
-  const double *Jq = jinv ? jinv + e * 9LL * nq : nullptr;
-  if (amode == dAPPLY_INTERP || amode == dAPPLY_GRAD) {
-    for (int t = threadIdx.x; t < np * D; t += blockDim.x) sin[t] = in[e * np * D + t];
+  const double *Jq = jinv ? jinv + qb * 9 : nullptr;
+  if (fwd) {
+    for (int t = threadIdx.x; t < np * D; t += blockDim.x) sin[t] = in[ib * D + t];
     __syncthreads();
     if (amode == dAPPLY_INTERP) {
-      double *o = out + e * nq * D;
+      double *o = out + ob * D;
       const double *A[3] = {f.B[0], f.B[1], f.B[2]};
       // write through shared then copy so that ADD semantics apply to global memory
       tmult(D, P, Q, A, 0, sin, t1, t2, g, false);
@@ -86,7 +94,7 @@ __global__ void k_efs_apply(EFSDev f, int64_t nelem, const double *jinv, int D, 
         const double *A[3] = {dir == 0 ? f.D[0] : f.B[0], dir == 1 ? f.D[1] : f.B[1], dir == 2 ? f.D[2] : f.B[2]};
         tmult(D, P, Q, A, 0, sin, t1, t2, g + dir * buf, false);
       }
-      double *o = out + e * nq * D * 3;
+      double *o = out + ob * D * 3;
       for (int t = threadIdx.x; t < nq * D; t += blockDim.x) {
         const int q = t / D;
         double gr[3] = {g[t], g[buf + t], g[2 * buf + t]};
@@ -98,14 +106,14 @@ __global__ void k_efs_apply(EFSDev f, int64_t nelem, const double *jinv, int D, 
     }
   } else {
     if (amode == dAPPLY_INTERP_TRANSPOSE) {
-      for (int t = threadIdx.x; t < nq * D; t += blockDim.x) sin[t] = in[e * nq * D + t];
+      for (int t = threadIdx.x; t < nq * D; t += blockDim.x) sin[t] = in[ib * D + t];
       __syncthreads();
       const double *A[3] = {f.B[0], f.B[1], f.B[2]};
       tmult(D, Q, P, A, 1, sin, t1, t2, g, false);
     } else {  // GRAD_TRANSPOSE: map with jinv^T then three transposed contractions accumulated
       for (int t = threadIdx.x; t < nq * D; t += blockDim.x) {
         const int q = t / D;
-        const double *v = in + (e * nq * D + t) * 3;
+        const double *v = in + (ib * D + t) * 3;
         for (int dir = 0; dir < 3; dir++)
           g[dir * buf + t] = Jq ? v[0] * Jq[q * 9 + dir * 3 + 0] + v[1] * Jq[q * 9 + dir * 3 + 1] + v[2] * Jq[q * 9 + dir * 3 + 2] : v[dir];
       }
@@ -117,13 +125,41 @@ __global__ void k_efs_apply(EFSDev f, int64_t nelem, const double *jinv, int D, 
         tmult(D, Q, P, A, 1, g + dir * buf, t1, t2, sin, true);
       }
     }
-    double *o = out + e * np * D;
+    double *o = out + ob * D;
     const double *src = amode == dAPPLY_INTERP_TRANSPOSE ? g : sin;
     for (int t = threadIdx.x; t < np * D; t += blockDim.x) o[t] = add ? o[t] + src[t] : src[t];
   }
 }
 
 }  // namespace
+
+// the batched apply over a list of elements with node / point offsets (dEFSApplyBatched: contiguous elements)
+dErr efs_apply_list(dEFS efs, int64_t nelem, const int32_t *elist, const int32_t *ioff, const int32_t *ooff, const double *jinv,
+                    int D, const double *in, double *out, dApplyMode amode, InsertMode imode, cudaStream_t stream) {
+  if (!efs) return set_error("null EFS");
+  if (amode < dAPPLY_INTERP || amode > dAPPLY_GRAD_TRANSPOSE) return set_error("invalid/unimplemented dApplyMode %d", (int)amode);
+  if (imode != INSERT_VALUES && imode != ADD_VALUES) return set_error("InsertMode %d invalid", (int)imode);
+  if (amode == dAPPLY_GRAD_TRANSPOSE && !jinv) return set_error("No Jinv, need a mapping");
+  if (D < 1 || D > 3) return set_error("D = %d not supported", D);
+  if (nelem <= 0) return 0;
+  EFSDev f;
+  const double *p = efs->d_tab;
+  for (int d = 0; d < 3; d++) {
+    f.P[d] = efs->P[d];
+    f.Q[d] = efs->Q[d];
+    f.B[d] = p;
+    f.D[d] = p + efs->P[d] * efs->Q[d];
+    p += 2 * efs->P[d] * efs->Q[d];
+  }
+  int m3 = 0;
+  for (int d = 0; d < 3; d++) m3 = std::max(m3, std::max(f.P[d], f.Q[d]));
+  const size_t smem = 6ull * m3 * m3 * m3 * D * sizeof(double);
+  if (smem > 220 * 1024) return set_error("element too large for the batched apply (%zu bytes of shared memory)", smem);
+  CUCHK(cudaFuncSetAttribute(k_efs_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_efs_apply<<<(unsigned)nelem, 256, smem, stream>>>(f, nelem, elist, ioff, ooff, jinv, D, in, out, (int)amode, (int)imode);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
 
 extern "C" {
 
@@ -210,29 +246,7 @@ dErr dEFSGetTensorNodes(dEFS efs, dInt P[3], dInt Q[3], dReal *basis_nodes, dRea
 
 dErr dEFSApplyBatched(dEFS efs, dInt nelem, const dReal *jinv, dInt D, const dScalar *in, dScalar *out, dApplyMode amode,
                       InsertMode imode, void *stream) {
-  if (!efs) return set_error("null EFS");
-  if (amode < dAPPLY_INTERP || amode > dAPPLY_GRAD_TRANSPOSE) return set_error("invalid/unimplemented dApplyMode %d", (int)amode);
-  if (imode != INSERT_VALUES && imode != ADD_VALUES) return set_error("InsertMode %d invalid", (int)imode);
-  if (amode == dAPPLY_GRAD_TRANSPOSE && !jinv) return set_error("No Jinv, need a mapping");
-  if (D < 1 || D > 3) return set_error("D = %d not supported", D);
-  if (nelem <= 0) return 0;
-  EFSDev f;
-  const double *p = efs->d_tab;
-  for (int d = 0; d < 3; d++) {
-    f.P[d] = efs->P[d];
-    f.Q[d] = efs->Q[d];
-    f.B[d] = p;
-    f.D[d] = p + efs->P[d] * efs->Q[d];
-    p += 2 * efs->P[d] * efs->Q[d];
-  }
-  int m3 = 0;
-  for (int d = 0; d < 3; d++) m3 = std::max(m3, std::max(f.P[d], f.Q[d]));
-  const size_t smem = 6ull * m3 * m3 * m3 * D * sizeof(double);
-  if (smem > 220 * 1024) return set_error("element too large for the batched apply (%zu bytes of shared memory)", smem);
-  CUCHK(cudaFuncSetAttribute(k_efs_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_efs_apply<<<nelem, 256, smem, (cudaStream_t)stream>>>(f, nelem, jinv, D, in, out, (int)amode, (int)imode);
-  CUCHK(cudaGetLastError());
-  return 0;
+  return efs_apply_list(efs, nelem, nullptr, nullptr, nullptr, jinv, D, in, out, amode, imode, (cudaStream_t)stream);
 }
 
 dErr dEFSApply(dEFS efs, const dReal *jinv, dInt D, const dScalar *in, dScalar *out, dApplyMode amode, InsertMode imode) {

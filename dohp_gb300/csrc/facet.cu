@@ -14,7 +14,9 @@
 //   Commit: y_exp[i] += sum_q phi_i(xi_q) v_q over each facet's points, one block per element so the facets of
 //           an element (edges and corners of the box) add into shared nodes in a fixed order;
 //   Finish: the deterministic E^T restriction of the volume path.
-// Boundary work is O(M^2) against the volume's O(M^3); it is latency-bound and is not tuned further.
+// The 1-D GLL Lagrange values at the facet's Gauss points come from tables built on the host: evaluating them
+// in the kernels put FP64 divisions on the (narrow) FP64 pipe and made a boundary cycle 4x slower. Start and
+// Finish still touch the whole expanded vector (expand, zero, restrict), which dominates what is left.
 #include <cmath>
 #include <vector>
 
@@ -35,17 +37,13 @@ constexpr double kSideT[6][3] = {{0, -1, 0}, {1, 0, 0}, {0, 1, 0}, {-1, 0, 0}, {
 
 struct FacetTables {
   double gx[MAXP + 1][MAXP], gw[MAXP + 1][MAXP];  // n-point Gauss rule (the FAST rule of order 2(n-1))
-  double gll[MAXP + 1][MAXP];                       // n GLL nodes
+  // L[0][n][a][i] = phi_i(+X_a), L[1][n][a][i] = phi_i(-X_a): the n GLL Lagrange functions at the n Gauss
+  // points (a facet axis runs along +xi or -xi of its reference direction)
+  double L[2][MAXP + 1][MAXP][MAXP];
   double R[6][3][3], t[6][3];
   int cx[6], cy[6], cn[6];  // reference direction of the facet's X, Y and normal axes
+  int sx[6], sy[6];         // 0: the axis runs along +xi, 1: along -xi
 };
-
-__device__ __forceinline__ double lagrange_at(int P, const double *nodes, int i, double xi) {
-  double v = 1;
-  for (int m = 0; m < P; m++)
-    if (m != i) v *= (xi - nodes[m]) / (nodes[i] - nodes[m]);
-  return v;
-}
 
 struct FacetGeom {
   int P[3], cx, cy, cn, iN;
@@ -104,9 +102,7 @@ __global__ void k_facet_points(int64_t nq, int bs, const int32_t *__restrict__ q
     x[3 * q + d] = xp[d];
     nrm[3 * q + d] = cr[d] / ar;
   }
-  double LX[MAXP], LY[MAXP];
-  for (int i = 0; i < G.P[G.cx]; i++) LX[i] = lagrange_at(G.P[G.cx], T.gll[G.P[G.cx]], i, xi[G.cx]);
-  for (int j = 0; j < G.P[G.cy]; j++) LY[j] = lagrange_at(G.P[G.cy], T.gll[G.P[G.cy]], j, xi[G.cy]);
+  const double *LX = T.L[T.sx[s]][nX][a], *LY = T.L[T.sy[s]][nY][b];
   for (int c = 0; c < bs; c++) {
     double acc = 0;
     for (int i = 0; i < G.P[G.cx]; i++) {
@@ -131,9 +127,9 @@ __global__ void k_facet_commit(int bs, const int32_t *__restrict__ bfoff, const 
       const int i = t / PY, j = t - i * PY;
       double acc[3] = {0, 0, 0};
       for (int a = 0; a < PX; a++) {
-        const double li = lagrange_at(PX, T.gll[PX], i, T.R[s][G.cx][0] * T.gx[PX][a]);
+        const double li = T.L[T.sx[s]][PX][a][i];
         for (int b = 0; b < PY; b++) {
-          const double l = li * lagrange_at(PY, T.gll[PY], j, T.R[s][G.cy][1] * T.gx[PY][b]);
+          const double l = li * T.L[T.sy[s]][PY][b][j];
           const int64_t q = foff[f] + a * PY + b;
           for (int c = 0; c < bs; c++) acc[c] += l * v[q * bs + c];
         }
@@ -186,18 +182,26 @@ dErr dFacetIteratorCreate(dFS fs, dQuadratureMethod method, dFacetIterator *it) 
   I->fs = fs;
   FacetTables T;
   for (int n = 1; n <= MAXP; n++) {
-    double x[MAXQ], w[MAXQ], lw[MAXP];
+    double x[MAXQ], w[MAXQ], gll[MAXP], lw[MAXP], der[MAXP];
     rule_1d(dQUADRATURE_METHOD_FAST, 2 * (n - 1), x, w);
     for (int i = 0; i < n; i++) T.gx[n][i] = x[i], T.gw[n][i] = w[i];
-    if (n >= 2) lobatto_rule(n, T.gll[n], lw);
-    else T.gll[n][0] = 0;
+    if (n >= 2) lobatto_rule(n, gll, lw);
+    else gll[0] = 0;
+    for (int a = 0; a < n; a++) {
+      if (n >= 2) {
+        lagrange(n, gll, x[a], T.L[0][n][a], der);
+        lagrange(n, gll, -x[a], T.L[1][n][a], der);
+      } else {
+        T.L[0][n][a][0] = T.L[1][n][a][0] = 1.0;
+      }
+    }
   }
   for (int s = 0; s < 6; s++) {
     for (int c = 0; c < 3; c++) {
       for (int k = 0; k < 3; k++) T.R[s][c][k] = kSideR[s][c][k];
       T.t[s][c] = kSideT[s][c];
-      if (kSideR[s][c][0] != 0) T.cx[s] = c;
-      if (kSideR[s][c][1] != 0) T.cy[s] = c;
+      if (kSideR[s][c][0] != 0) T.cx[s] = c, T.sx[s] = kSideR[s][c][0] < 0;
+      if (kSideR[s][c][1] != 0) T.cy[s] = c, T.sy[s] = kSideR[s][c][1] < 0;
       if (kSideR[s][c][2] != 0) T.cn[s] = c;
     }
   }

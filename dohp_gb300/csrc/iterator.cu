@@ -5,10 +5,13 @@
 // element's quadrature points, the caller's q-function fills v/dv, CommitPatchApplied integrates them back
 // (INTERP_TRANSPOSE, GRAD_TRANSPOSE) into the expanded test vector, and Finish restricts it. Here one call of
 // each step covers all elements: quadrature arrays are element-natural per element, elements back to back,
-// and every evaluation is one batched dEFSApply launch. FAST rules (one patch per element) on uniform-order
-// spaces.
+// and every evaluation is one batched dEFSApply launch per element order (one launch on a uniform-order
+// space; on a mixed-order space the elements of each order triple form a bucket, and the launches read and
+// write each element at its own expanded-node and quadrature-point offsets). FAST rules (one patch per element).
 #include <algorithm>
+#include <array>
 #include <cmath>
+#include <map>
 
 #include "internal.h"
 
@@ -16,24 +19,35 @@ using namespace dgb;
 
 dErr fs_expand(_p_dFS *fs, const double *g, double *x, bool inhomogeneous, int add);
 dErr fs_restrict(_p_dFS *fs, const double *x, double *g, int add);
+dErr efs_apply_list(dEFS efs, int64_t nelem, const int32_t *elist, const int32_t *ioff, const int32_t *ooff, const double *jinv,
+                    int D, const double *in, double *out, dApplyMode amode, InsertMode imode, cudaStream_t stream);
+
+namespace {
+struct IterBucket {
+  dEFS efs = nullptr, cefs = nullptr;  // field and coordinate element spaces on the same rule
+  int64_t nel = 0;
+  int32_t *d_elist = nullptr;  // the bucket's elements; null: every element, contiguous (uniform-order space)
+};
+}  // namespace
 
 struct _p_dRulesetIterator {
   dFS fs;
-  dEFS efs = nullptr, cefs = nullptr;  // field and coordinate element spaces on the same rule
+  std::vector<IterBucket> buckets;
   int64_t nq = 0, nel = 0;
   double *xexp = nullptr, *yexp = nullptr;
   double *jw = nullptr, *x = nullptr, *dx = nullptr, *jinv = nullptr, *u = nullptr, *du = nullptr, *v = nullptr, *dv = nullptr;
-  double *d_w = nullptr;  // rule weights per element-natural point
+  double *d_w = nullptr;  // rule weights: per element-natural point (uniform order) or per point (mixed orders)
+  bool per_point_w = false;
   bool started = false, applied = false;
 };
 
 namespace {
 
 // dRuleComputePhysical (src/jacobi/interface/jacobi.c:383-414): J^-1 by cofactors, jw = w det J, det < 0 is an error
-__global__ void k_physical(int64_t nel, int nq, const double *__restrict__ w, const double *__restrict__ dx,
+__global__ void k_physical(int64_t ntot, int nq, bool per_point, const double *__restrict__ w, const double *__restrict__ dx,
                            double *__restrict__ jinv, double *__restrict__ jw, int *neg) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= nel * nq) return;
+  if (t >= ntot) return;
   const double *a = dx + t * 9;
   double *b = jinv + t * 9;
   const double c0 = a[4] * a[8] - a[7] * a[5], c3 = -(a[3] * a[8] - a[6] * a[5]), c6 = a[3] * a[7] - a[6] * a[4];
@@ -48,7 +62,7 @@ __global__ void k_physical(int64_t nel, int nq, const double *__restrict__ w, co
   b[7] = -id * (a[0] * a[7] - a[6] * a[1]);
   b[8] = id * (a[0] * a[4] - a[3] * a[1]);
   if (det < 0) atomicExch(neg, 1);
-  jw[t] = w[t % nq] * det;
+  jw[t] = (per_point ? w[t] : w[t % nq]) * det;
 }
 
 // dNormsUpdate (src/util/util.c:121-144) over all points: per block partial sums of |r| jw, r^2 jw, max |r| and
@@ -95,38 +109,55 @@ dErr dRulesetIteratorCreate(dFS fs, dQuadratureMethod method, dRulesetIterator *
   if (!fs || !it) return set_error("null argument");
   if (!fs->setup) return set_error("dFS not set up");
   if (method != dQUADRATURE_METHOD_FAST) return set_error("batched iterator supports FAST rules (one patch per element)");
-  if (!fs->uniform) return set_error("batched iterator needs a uniform-order space");
   if (!fs->jac) return set_error("dFS was created without a dJacobi");
   _p_dRulesetIterator *I = new _p_dRulesetIterator();
   I->fs = fs;
-  const dInt deg[3] = {fs->p, fs->p, fs->p}, one[3] = {1, 1, 1}, ro[3] = {2 * fs->p, 2 * fs->p, 2 * fs->p};
-  dErr e = dJacobiGetEFS(fs->jac, deg, method, ro, &I->efs);
-  if (!e) e = dJacobiGetEFS(fs->jac, one, method, ro, &I->cefs);
-  if (e) {
-    delete I;
-    return e;
-  }
-  const int Q = I->efs->Q[0] * I->efs->Q[1] * I->efs->Q[2];
   I->nel = fs->nelem;
-  I->nq = fs->nelem * Q;
+  I->nq = fs->nq;
+  std::map<std::array<int, 3>, std::vector<int32_t>> groups;  // order triple -> elements, ascending
+  for (int64_t e = 0; e < fs->nelem; e++) groups[{fs->edeg[3 * e], fs->edeg[3 * e + 1], fs->edeg[3 * e + 2]}].push_back((int32_t)e);
+  I->per_point_w = groups.size() > 1;
+  std::vector<double> w(I->per_point_w ? std::max<int64_t>(fs->nq, 1) : 0);
+  for (auto &kv : groups) {
+    IterBucket B;
+    const dInt deg[3] = {kv.first[0], kv.first[1], kv.first[2]}, one[3] = {1, 1, 1};
+    const dInt ro[3] = {2 * deg[0], 2 * deg[1], 2 * deg[2]};
+    dErr e = dJacobiGetEFS(fs->jac, deg, method, ro, &B.efs);
+    if (!e) e = dJacobiGetEFS(fs->jac, one, method, ro, &B.cefs);
+    if (e) {
+      dRulesetIteratorDestroy(&I);
+      return e;
+    }
+    B.nel = (int64_t)kv.second.size();
+    const Basis1D *b = B.efs->b;
+    const int Q = b[0].Q * b[1].Q * b[2].Q;
+    std::vector<double> wq(Q);
+    for (int i = 0; i < b[0].Q; i++)
+      for (int j = 0; j < b[1].Q; j++)
+        for (int k = 0; k < b[2].Q; k++) wq[(i * b[1].Q + j) * b[2].Q + k] = b[0].w[i] * b[1].w[j] * b[2].w[k];
+    if (I->per_point_w) {
+      for (int32_t el : kv.second) std::copy(wq.begin(), wq.end(), w.begin() + fs->qoff[el]);
+      CUCHK(cudaMalloc(&B.d_elist, B.nel * sizeof(int32_t)));
+      CUCHK(cudaMemcpy(B.d_elist, kv.second.data(), B.nel * sizeof(int32_t), cudaMemcpyHostToDevice));
+    } else {
+      w = wq;
+    }
+    I->buckets.push_back(B);
+  }
   const int bs = fs->bs;
+  const int64_t nq = std::max<int64_t>(I->nq, 1);
   CUCHK(cudaMalloc(&I->xexp, fs->nexp * bs * sizeof(double)));
   CUCHK(cudaMalloc(&I->yexp, fs->nexp * bs * sizeof(double)));
-  CUCHK(cudaMalloc(&I->jw, I->nq * sizeof(double)));
-  CUCHK(cudaMalloc(&I->x, I->nq * 3 * sizeof(double)));
-  CUCHK(cudaMalloc(&I->dx, I->nq * 9 * sizeof(double)));
-  CUCHK(cudaMalloc(&I->jinv, I->nq * 9 * sizeof(double)));
-  CUCHK(cudaMalloc(&I->u, I->nq * bs * sizeof(double)));
-  CUCHK(cudaMalloc(&I->du, I->nq * bs * 3 * sizeof(double)));
-  CUCHK(cudaMalloc(&I->v, I->nq * bs * sizeof(double)));
-  CUCHK(cudaMalloc(&I->dv, I->nq * bs * 3 * sizeof(double)));
-  std::vector<double> w(Q);
-  const Basis1D *b = I->efs->b;
-  for (int i = 0; i < b[0].Q; i++)
-    for (int j = 0; j < b[1].Q; j++)
-      for (int k = 0; k < b[2].Q; k++) w[(i * b[1].Q + j) * b[2].Q + k] = b[0].w[i] * b[1].w[j] * b[2].w[k];
-  CUCHK(cudaMalloc(&I->d_w, Q * sizeof(double)));
-  CUCHK(cudaMemcpy(I->d_w, w.data(), Q * sizeof(double), cudaMemcpyHostToDevice));
+  CUCHK(cudaMalloc(&I->jw, nq * sizeof(double)));
+  CUCHK(cudaMalloc(&I->x, nq * 3 * sizeof(double)));
+  CUCHK(cudaMalloc(&I->dx, nq * 9 * sizeof(double)));
+  CUCHK(cudaMalloc(&I->jinv, nq * 9 * sizeof(double)));
+  CUCHK(cudaMalloc(&I->u, nq * bs * sizeof(double)));
+  CUCHK(cudaMalloc(&I->du, nq * bs * 3 * sizeof(double)));
+  CUCHK(cudaMalloc(&I->v, nq * bs * sizeof(double)));
+  CUCHK(cudaMalloc(&I->dv, nq * bs * 3 * sizeof(double)));
+  CUCHK(cudaMalloc(&I->d_w, std::max<size_t>(w.size(), 1) * sizeof(double)));
+  CUCHK(cudaMemcpy(I->d_w, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice));
   *it = I;
   return 0;
 }
@@ -135,6 +166,7 @@ dErr dRulesetIteratorDestroy(dRulesetIterator *it) {
   if (!it || !*it) return 0;
   _p_dRulesetIterator *I = *it;
   for (double *p : {I->xexp, I->yexp, I->jw, I->x, I->dx, I->jinv, I->u, I->du, I->v, I->dv, I->d_w}) cudaFree(p);
+  for (IterBucket &B : I->buckets) cudaFree(B.d_elist);
   delete I;
   *it = nullptr;
   return 0;
@@ -157,15 +189,18 @@ dErr dRulesetIteratorGetPatchApplied(dRulesetIterator it, int64_t *nq, const dRe
   _p_dFS *fs = it->fs;
   cudaStream_t s = fs->stream;
   const int bs = fs->bs;
-  const int Q = (int)(it->nq / it->nel);
-  if (!it->applied) {
-    // link 0 (coordinates): INTERP and GRAD without mapping, then the physical map
-    DCHK(dEFSApplyBatched(it->cefs, (dInt)it->nel, nullptr, 3, fs->d_coords, it->x, dAPPLY_INTERP, INSERT_VALUES, s));
-    DCHK(dEFSApplyBatched(it->cefs, (dInt)it->nel, nullptr, 3, fs->d_coords, it->dx, dAPPLY_GRAD, INSERT_VALUES, s));
+  const int Q = it->nel ? (int)(it->nq / it->nel) : 1;  // points per element when the order is uniform
+  if (!it->applied && it->nq) {
+    // link 0 (coordinates): INTERP and GRAD without mapping, then the physical map; coordinates are [nelem][8][3]
+    for (const IterBucket &B : it->buckets) {
+      const int32_t *qo = B.d_elist ? fs->d_qoff : nullptr;
+      DCHK(efs_apply_list(B.cefs, B.nel, B.d_elist, nullptr, qo, nullptr, 3, fs->d_coords, it->x, dAPPLY_INTERP, INSERT_VALUES, s));
+      DCHK(efs_apply_list(B.cefs, B.nel, B.d_elist, nullptr, qo, nullptr, 3, fs->d_coords, it->dx, dAPPLY_GRAD, INSERT_VALUES, s));
+    }
     int *neg;
     CUCHK(cudaMalloc(&neg, sizeof(int)));
     CUCHK(cudaMemsetAsync(neg, 0, sizeof(int), s));
-    k_physical<<<(unsigned)((it->nq + 255) / 256), 256, 0, s>>>(it->nel, Q, it->d_w, it->dx, it->jinv, it->jw, neg);
+    k_physical<<<(unsigned)((it->nq + 255) / 256), 256, 0, s>>>(it->nq, Q, it->per_point_w, it->d_w, it->dx, it->jinv, it->jw, neg);
     CUCHK(cudaGetLastError());
     int hneg = 0;
     CUCHK(cudaMemcpyAsync(&hneg, neg, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -173,12 +208,15 @@ dErr dRulesetIteratorGetPatchApplied(dRulesetIterator it, int64_t *nq, const dRe
     cudaFree(neg);
     if (hneg) return set_error("Negative Jacobian in the element geometry");
     // link 1 (field): INTERP and GRAD mapped to physical coordinates
-    DCHK(dEFSApplyBatched(it->efs, (dInt)it->nel, nullptr, bs, it->xexp, it->u, dAPPLY_INTERP, INSERT_VALUES, s));
-    DCHK(dEFSApplyBatched(it->efs, (dInt)it->nel, it->jinv, bs, it->xexp, it->du, dAPPLY_GRAD, INSERT_VALUES, s));
+    for (const IterBucket &B : it->buckets) {
+      const int32_t *xo = B.d_elist ? fs->d_xstart : nullptr, *qo = B.d_elist ? fs->d_qoff : nullptr;
+      DCHK(efs_apply_list(B.efs, B.nel, B.d_elist, xo, qo, nullptr, bs, it->xexp, it->u, dAPPLY_INTERP, INSERT_VALUES, s));
+      DCHK(efs_apply_list(B.efs, B.nel, B.d_elist, xo, qo, it->jinv, bs, it->xexp, it->du, dAPPLY_GRAD, INSERT_VALUES, s));
+    }
     CUCHK(cudaMemsetAsync(it->v, 0, it->nq * bs * sizeof(double), s));
     CUCHK(cudaMemsetAsync(it->dv, 0, it->nq * bs * 3 * sizeof(double), s));
-    it->applied = true;
   }
+  it->applied = true;
   if (nq) *nq = it->nq;
   if (jw) *jw = it->jw;
   if (x) *x = it->x;
@@ -193,12 +231,17 @@ dErr dRulesetIteratorGetPatchApplied(dRulesetIterator it, int64_t *nq, const dRe
 dErr dRulesetIteratorCommitPatchApplied(dRulesetIterator it, InsertMode imode, int use_v, int use_dv) {
   if (!it || !it->applied) return set_error("dRulesetIteratorGetPatchApplied first");
   _p_dFS *fs = it->fs;
-  InsertMode m = imode;
-  if (use_v) {
-    DCHK(dEFSApplyBatched(it->efs, (dInt)it->nel, it->jinv, fs->bs, it->v, it->yexp, dAPPLY_INTERP_TRANSPOSE, m, fs->stream));
-    m = ADD_VALUES;
+  if (!it->nq) return 0;
+  for (const IterBucket &B : it->buckets) {  // every element is in one bucket: per-element INSERT is exact
+    const int32_t *qo = B.d_elist ? fs->d_qoff : nullptr, *xo = B.d_elist ? fs->d_xstart : nullptr;
+    InsertMode m = imode;
+    if (use_v) {
+      DCHK(efs_apply_list(B.efs, B.nel, B.d_elist, qo, xo, it->jinv, fs->bs, it->v, it->yexp, dAPPLY_INTERP_TRANSPOSE, m, fs->stream));
+      m = ADD_VALUES;
+    }
+    if (use_dv)
+      DCHK(efs_apply_list(B.efs, B.nel, B.d_elist, qo, xo, it->jinv, fs->bs, it->dv, it->yexp, dAPPLY_GRAD_TRANSPOSE, m, fs->stream));
   }
-  if (use_dv) DCHK(dEFSApplyBatched(it->efs, (dInt)it->nel, it->jinv, fs->bs, it->dv, it->yexp, dAPPLY_GRAD_TRANSPOSE, m, fs->stream));
   return 0;
 }
 

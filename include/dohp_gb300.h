@@ -195,7 +195,9 @@ dErr dOperatorMultHost(dOperator op, const dScalar *x_host, dScalar *y_host);
 /* ---------------------------------------------------------------- dRulesetIterator (batched device form) */
 /* dRulesetIterator* (include/dohpfs.h:106-128, src/fs/interface/fsrulesetit.c): one Start / GetPatchApplied /
  * CommitPatchApplied / Finish cycle covers all elements at once on the device. Arrays are element-natural
- * per element, elements back to back (patch order = element order for FAST rules). */
+ * per element, elements back to back (patch order = element order for FAST rules); on spaces with per-element
+ * orders each element has (p_x+1)(p_y+1)(p_z+1) points, element e starting at the prefix sum of the counts
+ * before it (the layout of dFSGetNumQuadraturePoints and dOperatorGetQuadratureData). */
 dErr dRulesetIteratorCreate(dFS fs, dQuadratureMethod method, dRulesetIterator *it);
 dErr dRulesetIteratorDestroy(dRulesetIterator *it);
 dErr dRulesetIteratorStart(dRulesetIterator it, const dScalar *g, dFSHomogeneousMode hmode);

@@ -117,9 +117,44 @@ def test_errors():
     it = dg.RulesetIterator(fs)
     with pytest.raises(dg.DohpError):
         it.get()
-    ed = np.random.default_rng(0).integers(2, 5, size=fs.nelem).astype(np.int32)
-    with pytest.raises(dg.DohpError):
-        dg.RulesetIterator(dg.FS((3, 3, 3), degree=2, seed=1, elem_degree=ed))
+
+
+@pytest.mark.parametrize("bs", [1, 3])
+def test_mixed_order_space_matches_oracle_and_operator(bs):
+    """per-element orders 1..7: one batched apply per order bucket, each element at its own offsets"""
+    npoints = (4, 5, 4)
+    ne = 3 * 4 * 3
+    ed = np.random.default_rng(11 + bs).integers(1, 8, size=ne).astype(np.int32)
+    fs = dg.FS(npoints, degree=4, perturb=0.1, seed=5, bs=bs, elem_degree=ed)
+    o = po.FS(*npoints, degree=4, perturb=0.1, seed=5, bs=bs, elem_degree=ed)
+    assert fs.nq == o.num_qpts()[0]
+    g = np.random.default_rng(bs).uniform(-1, 1, fs.n * bs)
+    mass = lambda a: a["v"].copy_(a["jw"][:, None] * a["u"])
+    y, it, a = cycle(fs, g, mass, use_v=True, use_dv=False)
+    if bs == 1:  # the oracle's mass apply is scalar
+        yo = o.apply(g, kind=3)
+        assert np.linalg.norm(y - yo) / np.linalg.norm(yo) < 1e-12
+    np.testing.assert_allclose(a["x"].cpu().numpy(), o.qpt_coords(), rtol=0, atol=1e-14)
+    assert abs(float(a["jw"].sum()) - 1.0) < 1e-13
+    if bs == 1:
+        y, _, _ = cycle(fs, g, poisson)
+        yo = o.apply(g)
+        yf = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
+        fs.operator().mult(torch.as_tensor(g, device="cuda"), yf)
+    else:
+        def elast(a):
+            du = a["du"]
+            eps = 0.5 * (du + du.transpose(1, 2))
+            tr = eps.diagonal(dim1=1, dim2=2).sum(-1)
+            sig = LAM * tr[:, None, None] * torch.eye(3, dtype=du.dtype, device=du.device) + 2 * MU * eps
+            a["dv"].copy_(a["jw"][:, None, None] * sig)
+        y, _, _ = cycle(fs, g, elast)
+        yo = o.apply(g, kind=2, param=np.array([LAM, MU]))
+        yf = torch.zeros(fs.n * 3, dtype=torch.float64, device="cuda")
+        fs.operator(dg.dOP_ELASTICITY, param=(E0, NU)).mult(torch.as_tensor(g, device="cuda"), yf)
+    torch.cuda.synchronize()
+    assert np.linalg.norm(y - yo) / np.linalg.norm(yo) < 1e-12
+    assert np.linalg.norm(y - yf.cpu().numpy()) / np.linalg.norm(yo) < 1e-12
 
 
 def test_error_norms_match_numpy():
