@@ -104,11 +104,17 @@ class FS:
     """dFS on a seeded perturbed block mesh (dMeshGenerateBlock + dFSBuildSpace)."""
 
     def __init__(self, npoints, degree=4, box=(0, 1, 0, 1, 0, 1), perturb=0.1, seed=1, bs=1,
-                 dirichlet=(100, 200, 300), elem_degree=None, stream=None, weak=()):
+                 dirichlet=(100, 200, 300), elem_degree=None, stream=None, weak=(), mesh_of=None):
+        """mesh_of: another FS whose mesh this space shares (a second field on the same mesh, e.g. the pressure
+        of a Stokes pair); npoints, box, perturb and seed are then ignored"""
         L = lib()
         self.mesh = _vp()
-        chk(L.dMeshCreateBlock(ptr(np.asarray(npoints, np.int32)), ptr(np.asarray(box, np.float64)), _dbl(perturb),
-                               ctypes.c_uint64(seed), ctypes.byref(self.mesh)))
+        self._mesh_owner = mesh_of
+        if mesh_of is not None:
+            self.mesh = mesh_of.mesh
+        else:
+            chk(L.dMeshCreateBlock(ptr(np.asarray(npoints, np.int32)), ptr(np.asarray(box, np.float64)), _dbl(perturb),
+                                   ctypes.c_uint64(seed), ctypes.byref(self.mesh)))
         self.jac = Jacobi()
         self.h = _vp()
         chk(L.dFSCreate(self.mesh, self.jac.h, ctypes.byref(self.h)))
@@ -133,7 +139,7 @@ class FS:
             return
         if getattr(self, "h", None):
             _lib.dFSDestroy(ctypes.byref(self.h))
-        if getattr(self, "mesh", None):
+        if getattr(self, "mesh", None) and getattr(self, "_mesh_owner", None) is None:
             _lib.dMeshDestroy(ctypes.byref(self.mesh))
 
     def set_stream(self, stream):
@@ -405,6 +411,33 @@ def facet_rule(side, order, method=FAST):
     nodes, w, n = np.zeros(3 * 81), np.zeros(81), _i32()
     chk(lib().dFSGetFacetRule(_i32(side), ctypes.c_int(method), _i32(order), ctypes.byref(n), ptr(nodes), ptr(w)))
     return nodes[:3 * n.value].reshape(-1, 3), w[:n.value]
+
+
+dSTOKES_MULT_A, dSTOKES_MULT_BT, dSTOKES_MULT_B, dSTOKES_MULT_COUPLED = 0, 1, 2, 3
+
+
+class Stokes:
+    """dStokes on a velocity space fsu (bs 3) and a pressure space fsp (bs 1) sharing its mesh
+    (FS(..., mesh_of=fsu)); rheo = (B, eps, p, nu), Newtonian p = 2."""
+
+    def __init__(self, fsu, fsp, rheo=None):
+        self.fsu, self.fsp = fsu, fsp
+        self.h = _vp()
+        r = None if rheo is None else np.asarray(rheo, np.float64)
+        chk(lib().dStokesCreate(fsu.h, fsp.h, ptr(r), ctypes.byref(self.h)))
+
+    def __del__(self):
+        if _lib is not None and getattr(self, "h", None):
+            _lib.dStokesDestroy(ctypes.byref(self.h))
+
+    def mult(self, mode, xu=None, xp=None, yu=None, yp=None):
+        chk(lib().dStokesMult(self.h, ctypes.c_int(mode), ptr(xu), ptr(xp), ptr(yu), ptr(yp)))
+
+    def solve(self, bu, bp, xu, xp, rtol=1e-8, maxit=500):
+        its, rn = _i32(), _dbl()
+        chk(lib().dStokesSolve(self.h, ptr(bu), ptr(bp), ptr(xu), ptr(xp), _dbl(rtol), _i32(maxit), ctypes.byref(its),
+                               ctypes.byref(rn)))
+        return its.value, rn.value
 
 
 class dNewtonOptions(ctypes.Structure):

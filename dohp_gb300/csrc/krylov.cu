@@ -338,7 +338,38 @@ struct _p_dKSP {
   // optional per-iteration monitor (CG: after every iterate, with x and r)
   dErr (*monitor)(void *ctx, int it, const double *x, const double *r) = nullptr;
   void *monitor_ctx = nullptr;
+  // shell form (a coupled system without a dOperator, e.g. Stokes): the operator and the preconditioner are
+  // callbacks on vectors of length n, run on shell_stream
+  dErr (*shell_mult)(void *ctx, const double *x, double *y) = nullptr;
+  dErr (*shell_pc)(void *ctx, const double *r, double *z) = nullptr;
+  void *shell_ctx = nullptr;
+  cudaStream_t shell_stream = 0;
 };
+
+static cudaStream_t kstream(const _p_dKSP *k) { return k->shell_mult ? k->shell_stream : k->op->fs->stream; }
+dErr op_mult_prec(_p_dOperator *op, const double *x, double *y, dPrecision prec);
+static dErr kmult(_p_dKSP *k, const double *x, double *y, dPrecision prec) {
+  return k->shell_mult ? k->shell_mult(k->shell_ctx, x, y) : op_mult_prec(k->op, x, y, prec);
+}
+
+// a KSP over a shell operator and preconditioner (FGMRES or CG)
+dErr ksp_create_shell(int64_t n, cudaStream_t stream, dKSPType type, dErr (*mult)(void *, const double *, double *),
+                      dErr (*pc)(void *, const double *, double *), void *ctx, int restart, dKSP *ksp) {
+  if (!mult || !ksp) return set_error("null argument");
+  _p_dKSP *k = new _p_dKSP();
+  k->op = nullptr;
+  k->pmat = nullptr;
+  k->type = type;
+  k->pc = dPC_NONE;
+  k->n = n;
+  k->restart = restart;
+  k->shell_mult = mult;
+  k->shell_pc = pc;
+  k->shell_ctx = ctx;
+  k->shell_stream = stream;
+  *ksp = k;
+  return 0;
+}
 
 dErr ksp_get_operator(dKSP ksp, dOperator *op) {
   if (!ksp || !op) return set_error("null argument");
@@ -372,8 +403,7 @@ static dErr ksp_alloc(_p_dKSP *k) {
 
 static dErr pc_setup(_p_dKSP *k) {
   if (k->pc_ready || k->pc == dPC_NONE) return 0;
-  _p_dFS *fs = k->op->fs;
-  cudaStream_t s = fs->stream;
+  cudaStream_t s = kstream(k);
   const int64_t n = k->n;
   if (!k->pmat) return set_error("preconditioner needs the Q1 matrix");
   k_diag_inv<<<nb(n), 256, 0, s>>>(n, k->pmat->d_rowptr, k->pmat->d_col, k->pmat->d_val, k->d_dinv);
@@ -413,7 +443,7 @@ static dErr pc_setup(_p_dKSP *k) {
 // Chebyshev-Jacobi on the Q1 matrix in FP32 (values, vectors and arithmetic), FP64 in/out
 static dErr pc_apply_fp32(_p_dKSP *k, const double *r, double *z) {
   _p_dMat *J = k->pmat;
-  cudaStream_t s = k->op->fs->stream;
+  cudaStream_t s = kstream(k);
   DCHK(mat_sell(J, s));
   const int64_t n = k->n, nnz = J->sell_len;  // values converted in the sliced layout, padding included
   const bool bf = k->pc_prec == dPREC_BF16;
@@ -451,6 +481,7 @@ static dErr pc_apply_plain(_p_dKSP *k, const double *r, double *z);
 
 static dErr pc_apply(_p_dKSP *k, const double *r, double *z) {
   k->pc_applies++;
+  if (k->shell_pc) return k->shell_pc(k->shell_ctx, r, z);
   DCHK(pc_apply_plain(k, r, z));
   if (k->correction && k->correction_on && (k->active_policy == 0 || k->cycle_pos == 0))
     DCHK(k->correction(k->correction_ctx, r, z));
@@ -459,7 +490,7 @@ static dErr pc_apply(_p_dKSP *k, const double *r, double *z) {
 
 static dErr pc_apply_plain(_p_dKSP *k, const double *r, double *z) {
   const int64_t n = k->n;
-  cudaStream_t s = k->op->fs->stream;
+  cudaStream_t s = kstream(k);
   if (k->pc == dPC_CHEBYSHEV_Q1 && k->pc_prec != dPREC_FP64) return pc_apply_fp32(k, r, z);
   if (k->pc == dPC_NONE) {
     CUCHK(cudaMemcpyAsync(z, r, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -492,10 +523,10 @@ static dErr read_scalar(const double *d, double *h, cudaStream_t s) {
 
 static dErr cg_solve(_p_dKSP *k, const double *b, double *x, double rtol, int maxit, int *its, double *rnorm) {
   const int64_t n = k->n;
-  cudaStream_t s = k->op->fs->stream;
+  cudaStream_t s = kstream(k);
   double *r = k->d_work, *z = k->d_work + n, *p = k->d_work + 2 * n, *q = k->d_work + 3 * n;
   double *S = k->d_s;  // S[0]=rz S[1]=pq S[2]=rr S[3]=bb S[4]=rz_new
-  DCHK(op_mult(k->op, x, q));
+  DCHK(kmult(k, x, q, dPREC_FP64));
   CUCHK(cudaMemcpyAsync(r, b, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
   k_axpby<<<nb(n), 256, 0, s>>>(n, -1.0, nullptr, nullptr, q, 1.0, r);
   DCHK(device_dot(n, b, b, k->d_part, S + 3, s));
@@ -514,7 +545,7 @@ static dErr cg_solve(_p_dKSP *k, const double *b, double *x, double rtol, int ma
   CUCHK(cudaMemcpyAsync(p, z, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
   DCHK(device_dot(n, r, z, k->d_part, S, s));
   for (int it = 0; it < maxit; it++) {
-    DCHK(op_mult(k->op, p, q));
+    DCHK(kmult(k, p, q, dPREC_FP64));
     DCHK(device_dot(n, p, q, k->d_part, S + 1, s));
     k_axpby<<<nb(n), 256, 0, s>>>(n, 1.0, S, S + 1, p, 1.0, x);
     k_axpby<<<nb(n), 256, 0, s>>>(n, -1.0, S, S + 1, q, 1.0, r);
@@ -533,8 +564,6 @@ static dErr cg_solve(_p_dKSP *k, const double *b, double *x, double rtol, int ma
   return 0;
 }
 
-dErr op_mult_prec(_p_dOperator *op, const double *x, double *y, dPrecision prec);
-
 // Right-preconditioned FGMRES(m) (Saad Alg. 9.6) with classical Gram-Schmidt applied twice (CGS2) in FP64.
 // Each cycle starts from the true residual b - A x computed with the FP64 operator; the operator applies
 // inside a cycle and the preconditioner run in k->pc_prec (FP32 for the mixed-precision solver). The
@@ -542,7 +571,7 @@ dErr op_mult_prec(_p_dOperator *op, const double *x, double *y, dPrecision prec)
 static dErr fgmres_solve(_p_dKSP *k, const double *b, double *x, double rtol, int maxit, int *its, double *rnorm) {
   const int64_t n = k->n;
   const int m = std::max(1, k->restart);
-  cudaStream_t s = k->op->fs->stream;
+  cudaStream_t s = kstream(k);
   if (!k->d_V) {
     CUCHK(cudaMalloc(&k->d_V, (size_t)(m + 1) * n * sizeof(double)));
     CUCHK(cudaMalloc(&k->d_Z, (size_t)m * n * sizeof(double)));
@@ -558,7 +587,7 @@ static dErr fgmres_solve(_p_dKSP *k, const double *b, double *x, double rtol, in
   double res = 0, prev = -1, rho[2] = {-1, -1};
   k->correction_on = k->correction != nullptr;
   for (;;) {
-    DCHK(op_mult_prec(k->op, x, V, dPREC_FP64));
+    DCHK(kmult(k, x, V, dPREC_FP64));
     k_axpby<<<nb(n), 256, 0, s>>>(n, 1.0, nullptr, nullptr, b, -1.0, V);  // V0 = b - A x
     double rr;
     DCHK(device_dot(n, V, V, k->d_part, k->d_s, s));
@@ -587,7 +616,7 @@ static dErr fgmres_solve(_p_dKSP *k, const double *b, double *x, double rtol, in
       double *w = V + (size_t)(j + 1) * n;
       k->cycle_pos = j;
       DCHK(pc_apply(k, V + (size_t)j * n, Z + (size_t)j * n));
-      DCHK(op_mult_prec(k->op, Z + (size_t)j * n, w, k->pc_prec));
+      DCHK(kmult(k, Z + (size_t)j * n, w, k->pc_prec));
       const int nv = j + 1;
       k_mdot_partial<<<dim3(RED_BLOCKS, nv), RED_THREADS, 0, s>>>(n, nv, V, w, mpart);
       k_mdot_final<<<nv, 1024, 0, s>>>(mpart, h1, nullptr);
@@ -734,6 +763,14 @@ dErr ksp_solve(dKSP ksp, const double *b, double *x, double rtol, int maxit, int
   if (its) *its = it;
   if (rnorm) *rnorm = rn;
   return e;
+}
+
+// the KSP's preconditioner alone (set up on first use): z = M^-1 r, e.g. a block of a coupled preconditioner
+dErr ksp_pc_only(dKSP ksp, const double *r, double *z) {
+  if (!ksp) return set_error("null KSP");
+  DCHK(ksp_alloc(ksp));
+  DCHK(pc_setup(ksp));
+  return pc_apply_plain(ksp, r, z);
 }
 
 extern "C" {

@@ -1,0 +1,465 @@
+// Mixed velocity-pressure (Stokes) operator and its block-preconditioned solve (src/fs/tests/stokes.c).
+//
+// Spaces: velocity u in the dFS fsu (bs 3, degree k, Dirichlet sets), pressure p in fsp (bs 1, degree k - codim,
+// continuous, no boundary sets: StokesSetFromOptions, stokes.c:160-274) on the same mesh; every integral uses the
+// velocity's FAST rule (k+1 Gauss points per direction), the pressure basis is evaluated at those points.
+// Operator (MatMult_Nest_StokesCoupled stokes.c:541-577, StokesShellMatMult_All_IorA stokes.c:579-673):
+//   A:  int eta Dv:Du + lambda div v div u, lambda = nu/(1 - 2 nu)  (StokesPointwiseJacobian_A, stokes.c:489-494)
+//   Bt: -int p div v                                                 (StokesPointwiseJacobian_Bt, stokes.c:501-505)
+//   B:  -int q div u                                                 (StokesPointwiseJacobian_B, stokes.c:496-499)
+//   coupled [A Bt; B 0] without the penalty                          (StokesPointwiseJacobian, stokes.c:476-487)
+// with Du the symmetric gradient in [00, 11, 22, 01, 02, 12] storage (dTensorSymCompress3, include/dohp.h:79-82).
+// This build covers the Newtonian rheology (exponent p = 2: eta = B, the store's eta' = 0); the power-law store
+// is refused with an error.
+//
+// One fused kernel per element group does all of it: velocity gather through E, B and Dq passes per component,
+// pressure gather and three rectangular passes Bp (N x NP: the pressure's GLL basis at the velocity's Gauss
+// points), the pointwise coupling with the geometric factors {J^-1, w det J}, the transposed passes, and the
+// expanded outputs; the E^T restrictions of the two spaces follow.
+//
+// Solver (the reference's -pc_fieldsplit_type schur with a Q1-embedded velocity matrix and a viscosity-scaled
+// pressure mass for the Schur complement, StokesGetMatrices / StokesJacobianAssemble_Velocity / _Pressure,
+// stokes.c:367-505, 675-799): right-preconditioned FGMRES on the packed vector [u; p] with the block upper
+// triangular preconditioner
+//   z_p = -eta diag(M_p)^-1 r_p  (mean removed: the constant pressure is the null space with Dirichlet walls),
+//   z_u = Cheb-Jacobi(A_q1) (r_u - Bt z_p),
+// A_q1 the blocked Q1-embedded matrix of the A block (the elasticity assembly with 2 mu = eta, lambda as A).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "element.cuh"
+
+using namespace dgb;
+
+dErr fs_restrict(_p_dFS *fs, const double *x, double *g, int add);
+dErr geometry_fill(_p_dFS *fs, int mode, const double *kq, double *out);
+dErr q1_numeric_elast(_p_dFS *fs, _p_dMat *J, double lam, double mu, int quirk);
+dErr ksp_create_shell(int64_t n, cudaStream_t stream, dKSPType type, dErr (*mult)(void *, const double *, double *),
+                      dErr (*pc)(void *, const double *, double *), void *ctx, int restart, dKSP *ksp);
+dErr ksp_solve(dKSP ksp, const double *b, double *x, double rtol, int maxit, int *its, double *rnorm);
+dErr ksp_pc_only(dKSP ksp, const double *r, double *z);
+dErr device_dot(int64_t n, const double *a, const double *b, double *part, double *out, cudaStream_t s);
+
+namespace {
+
+struct StokesArgs {
+  ElemArgs U, P;     // velocity and pressure spaces (xstart, emap, n, x, yexp)
+  const double *bp;  // Bp [N][NP]
+  const double *geo; // velocity FAST geometry {J^-1 (9), w det J} per point, SoA per element
+  double eta, lam;
+};
+
+constexpr int SM_A = 0, SM_BT = 1, SM_B = 2, SM_COUPLED = 3;
+
+// one rectangular pass along DIR of ne elements with input dims (D0, D1, D2): the DIR dimension goes from NP
+// to N through Bp (TR false) or from N to NP through Bp^T (TR true)
+template <int N, int NP, int D0, int D1, int D2, int DIR, bool TR>
+__device__ __forceinline__ void rpass(const double *bp, const double *in, double *out, int ne) {
+  constexpr int K = TR ? N : NP, M = TR ? NP : N;
+  constexpr int O0 = DIR == 0 ? M : D0, O1 = DIR == 1 ? M : D1, O2 = DIR == 2 ? M : D2;
+  constexpr int OUT = O0 * O1 * O2, IN = D0 * D1 * D2;
+  for (int t = threadIdx.x; t < ne * OUT; t += blockDim.x) {
+    const int el = t / OUT, r = t - el * OUT, i0 = r / (O1 * O2), i1 = (r / O2) % O1, i2 = r % O2;
+    const int o = DIR == 0 ? i0 : DIR == 1 ? i1 : i2;
+    const double *src = in + el * IN;
+    double s = 0;
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+      const int j0 = DIR == 0 ? j : i0, j1 = DIR == 1 ? j : i1, j2 = DIR == 2 ? j : i2;
+      s += (TR ? bp[j * NP + o] : bp[o * NP + j]) * src[(j0 * D1 + j1) * D2 + j2];
+    }
+    out[t] = s;
+  }
+}
+
+template <int N, int NP>
+__host__ __device__ constexpr int stokes_smem_elems(int cap) {
+  return kTabElems + MAXP * MAXP + 12 * cap * N * N * N;
+}
+
+template <int N, int NP, int MODE>
+__global__ void __launch_bounds__(256) k_stokes(StokesArgs S, int64_t nelem, int cap) {
+  extern __shared__ double smem[];
+  constexpr int N3 = N * N * N, P3 = NP * NP * NP;
+  constexpr bool USE_U = MODE != SM_BT, USE_P = MODE == SM_BT || MODE == SM_COUPLED;
+  constexpr bool OUT_U = MODE != SM_B, OUT_P = MODE == SM_B || MODE == SM_COUPLED;
+  const int64_t first = (int64_t)blockIdx.x * cap;
+  const int ne = (int)min((int64_t)cap, nelem - first);
+  double *tab = smem, *bp = smem + kTabElems, *buf = bp + MAXP * MAXP;
+  const int L = cap * N3;
+  double *S0 = buf, *S1 = buf + L, *G = buf + 2 * L, *Pq = buf + 11 * L;
+  for (int i = threadIdx.x; i < N * NP; i += blockDim.x) bp[i] = S.bp[i];
+  load_tables<N, double>(S.U.tab_all, tab);  // ends with a barrier
+  if constexpr (USE_P) {
+    gather<NP, double, 1>(S.P, S.P.x, nullptr, first, ne, 0, S0);
+    __syncthreads();
+    rpass<N, NP, NP, NP, NP, 0, false>(bp, S0, S1, ne);
+    __syncthreads();
+    rpass<N, NP, N, NP, NP, 1, false>(bp, S1, S0, ne);
+    __syncthreads();
+    rpass<N, NP, N, N, NP, 2, false>(bp, S0, Pq, ne);
+    __syncthreads();
+  }
+  if constexpr (USE_U) {
+    for (int d = 0; d < 3; d++) {
+      gather<N, double, 3>(S.U, S.U.x, nullptr, first, ne, d, S0);
+      __syncthreads();
+      interp3<N, double>(tab, S0, S1, ne);
+      grad<N, double>(tab, S1, G + (d * 3 + 0) * L, G + (d * 3 + 1) * L, G + (d * 3 + 2) * L, ne);
+    }
+  }
+  for (int t = threadIdx.x; t < ne * N3; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3;
+    const double *gq = S.geo + (int64_t)S.U.qoff[first + el] * 10 + r;
+    double Ji[9];
+#pragma unroll
+    for (int i = 0; i < 9; i++) Ji[i] = gq[i * N3];
+    const double w = gq[9 * N3];
+    double Du[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if constexpr (USE_U) {
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        const double a0 = G[(d * 3 + 0) * L + t], a1 = G[(d * 3 + 1) * L + t], a2 = G[(d * 3 + 2) * L + t];
+#pragma unroll
+        for (int e = 0; e < 3; e++) Du[d * 3 + e] = a0 * Ji[0 * 3 + e] + a1 * Ji[1 * 3 + e] + a2 * Ji[2 * 3 + e];
+      }
+    }
+    const double tr = Du[0] + Du[4] + Du[8];
+    if constexpr (OUT_U) {
+      const double p = USE_P ? Pq[t] : 0.0;
+      const double lam = MODE == SM_A ? S.lam : 0.0, eta = MODE == SM_BT ? 0.0 : S.eta;
+      // Dv = w (eta Du_sym + lam tr(Du) I - p I), symmetric
+      const double diag = lam * tr - p;
+      double Dv[9];
+      Dv[0] = w * (eta * Du[0] + diag);
+      Dv[4] = w * (eta * Du[4] + diag);
+      Dv[8] = w * (eta * Du[8] + diag);
+      Dv[1] = Dv[3] = w * eta * 0.5 * (Du[1] + Du[3]);
+      Dv[2] = Dv[6] = w * eta * 0.5 * (Du[2] + Du[6]);
+      Dv[5] = Dv[7] = w * eta * 0.5 * (Du[5] + Du[7]);
+#pragma unroll
+      for (int d = 0; d < 3; d++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) G[(d * 3 + k) * L + t] = Dv[d * 3 + 0] * Ji[k * 3 + 0] + Dv[d * 3 + 1] * Ji[k * 3 + 1] + Dv[d * 3 + 2] * Ji[k * 3 + 2];
+    }
+    if constexpr (OUT_P) Pq[t] = -w * tr;
+  }
+  __syncthreads();
+  if constexpr (OUT_U) {
+    for (int d = 0; d < 3; d++)
+      back<N, double, 3>(tab, G + (d * 3 + 0) * L, G + (d * 3 + 1) * L, G + (d * 3 + 2) * L, S0, S1, S.U, nullptr, first, ne, d,
+                         (double *)S.U.yexp);
+  }
+  if constexpr (OUT_P) {
+    rpass<N, NP, N, N, N, 2, true>(bp, Pq, S0, ne);
+    __syncthreads();
+    rpass<N, NP, N, N, NP, 1, true>(bp, S0, S1, ne);
+    __syncthreads();
+    rpass<N, NP, N, NP, NP, 0, true>(bp, S1, S0, ne);
+    __syncthreads();
+    double *yp = (double *)S.P.yexp;
+    for (int t = threadIdx.x; t < ne * P3; t += blockDim.x) {
+      const int el = t / P3, r = t - el * P3;
+      yp[(int64_t)S.P.xstart[first + el] + r] = S0[t];
+    }
+  }
+}
+
+// diagonal of the pressure mass matrix on each element: sum_q w_q phi_i(x_q)^2, expanded layout
+template <int N, int NP>
+__global__ void k_pmass_diag(int64_t nelem, const int32_t *__restrict__ qoff, const int32_t *__restrict__ pxstart,
+                             const double *__restrict__ geo, const double *__restrict__ bpg, double *__restrict__ dexp) {
+  constexpr int N3 = N * N * N, P3 = NP * NP * NP;
+  const int64_t e = blockIdx.x;
+  if (e >= nelem) return;
+  const double *w = geo + (int64_t)qoff[e] * 10 + 9 * N3;
+  for (int r = threadIdx.x; r < P3; r += blockDim.x) {
+    const int i0 = r / (NP * NP), i1 = (r / NP) % NP, i2 = r % NP;
+    double s = 0;
+    for (int q = 0; q < N3; q++) {
+      const int a = q / (N * N), b = (q / N) % N, c = q % N;
+      const double phi = bpg[a * NP + i0] * bpg[b * NP + i1] * bpg[c * NP + i2];
+      s += w[q] * phi * phi;
+    }
+    dexp[(int64_t)pxstart[e] + r] = s;
+  }
+}
+
+// z_p = -eta r_p / d (the Schur block)
+__global__ void k_schur_diag(int64_t n, double eta, const double *__restrict__ d, const double *__restrict__ r, double *__restrict__ z) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) z[i] = -eta * r[i] / d[i];
+}
+__global__ void k_sub_mean(int64_t n, const double *__restrict__ sum, double *__restrict__ z) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) z[i] -= *sum / (double)n;
+}
+__global__ void k_rsub(int64_t n, const double *__restrict__ a, double *__restrict__ t) {  // t = a - t
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) t[i] = a[i] - t[i];
+}
+__global__ void k_fill(int64_t n, double v, double *__restrict__ y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = v;
+}
+
+inline unsigned nblk(int64_t n) { return (unsigned)std::max<int64_t>((n + 255) / 256, 1); }
+
+template <int N>
+struct STile {
+  static constexpr int EPB = N <= 3 ? 16 : N == 4 ? 8 : N == 5 ? 4 : 2;
+};
+
+template <int N, int NP, int MODE>
+dErr launch_stokes_mode(const StokesArgs &S, int64_t nelem, cudaStream_t s) {
+  constexpr int cap = STile<N>::EPB;
+  const size_t smem = (size_t)stokes_smem_elems<N, NP>(cap) * sizeof(double);
+  CUCHK(cudaFuncSetAttribute(k_stokes<N, NP, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_stokes<N, NP, MODE><<<(unsigned)((nelem + cap - 1) / cap), 256, smem, s>>>(S, nelem, cap);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+template <int N, int NP>
+dErr launch_stokes_np(const StokesArgs &S, int mode, int64_t nelem, cudaStream_t s) {
+  switch (mode) {
+    case SM_A: return launch_stokes_mode<N, NP, SM_A>(S, nelem, s);
+    case SM_BT: return launch_stokes_mode<N, NP, SM_BT>(S, nelem, s);
+    case SM_B: return launch_stokes_mode<N, NP, SM_B>(S, nelem, s);
+    case SM_COUPLED: return launch_stokes_mode<N, NP, SM_COUPLED>(S, nelem, s);
+  }
+  return set_error("Stokes mult mode %d", mode);
+}
+
+// velocity degree k = N - 1 in 2..6, pressure degree k - 1 or k - 2 (>= 1)
+dErr launch_stokes(const StokesArgs &S, int N, int NP, int mode, int64_t nelem, cudaStream_t s) {
+#define DGB_STOKES_CASE(a, b) \
+  if (N == a && NP == b) return launch_stokes_np<a, b>(S, mode, nelem, s);
+  DGB_STOKES_CASE(3, 2)
+  DGB_STOKES_CASE(4, 3)
+  DGB_STOKES_CASE(4, 2)
+  DGB_STOKES_CASE(5, 4)
+  DGB_STOKES_CASE(5, 3)
+  DGB_STOKES_CASE(6, 5)
+  DGB_STOKES_CASE(6, 4)
+  DGB_STOKES_CASE(7, 6)
+  DGB_STOKES_CASE(7, 5)
+#undef DGB_STOKES_CASE
+  return set_error("Stokes spaces of degrees %d / %d are not built (velocity 2..6, pressure codim 1 or 2)", N - 1, NP - 1);
+}
+
+dErr pmass_diag(int N, int NP, int64_t nelem, const int32_t *qoff, const int32_t *pxstart, const double *geo, const double *bp,
+                double *dexp, cudaStream_t s) {
+#define DGB_PM_CASE(a, b) \
+  if (N == a && NP == b) {                                                                        \
+    k_pmass_diag<a, b><<<(unsigned)std::max<int64_t>(nelem, 1), 64, 0, s>>>(nelem, qoff, pxstart, geo, bp, dexp); \
+    CUCHK(cudaGetLastError());                                                                     \
+    return 0;                                                                                      \
+  }
+  DGB_PM_CASE(3, 2)
+  DGB_PM_CASE(4, 3)
+  DGB_PM_CASE(4, 2)
+  DGB_PM_CASE(5, 4)
+  DGB_PM_CASE(5, 3)
+  DGB_PM_CASE(6, 5)
+  DGB_PM_CASE(6, 4)
+  DGB_PM_CASE(7, 6)
+  DGB_PM_CASE(7, 5)
+#undef DGB_PM_CASE
+  return set_error("Stokes spaces of degrees %d / %d are not built", N - 1, NP - 1);
+}
+
+}  // namespace
+
+struct _p_dStokes {
+  dFS fsu = nullptr, fsp = nullptr;
+  double B = 1, eps = 1, p = 2, nu = 0, lam = 0;
+  int N = 0, NP = 0;
+  int64_t nu3 = 0, np = 0;  // global sizes: velocity n*3, pressure n
+  double *d_geo = nullptr, *d_bp = nullptr, *d_yu = nullptr, *d_yp = nullptr;
+  double *d_mdiag = nullptr;  // diagonal of the pressure mass matrix (global)
+  double *d_t = nullptr;      // velocity temporary
+  double *d_part = nullptr, *d_s = nullptr;
+  dOperator opu = nullptr;    // velocity elasticity-kind operator: carries the velocity block's KSP
+  dMat Ap = nullptr;
+  dKSP kspu = nullptr, ksp = nullptr;
+  int restart = 30;
+};
+
+static dErr stokes_mult(_p_dStokes *S, int mode, const double *xu, const double *xp, double *yu, double *yp) {
+  _p_dFS *fu = S->fsu, *fp = S->fsp;
+  cudaStream_t s = fu->stream;
+  auto eargs = [](_p_dFS *fs, const double *x, double *yexp) {
+    ElemArgs A{};
+    A.xstart = fs->d_xstart;
+    A.qoff = fs->d_qoff;
+    A.emap = fs->d_emap;
+    A.n = fs->n;
+    A.x = x;
+    A.tab_all = fs->d_fast_tab;
+    A.yexp = yexp;
+    return A;
+  };
+  StokesArgs A;
+  A.U = eargs(fu, xu, S->d_yu);
+  A.P = eargs(fp, xp, S->d_yp);
+  A.bp = S->d_bp;
+  A.geo = S->d_geo;
+  A.eta = S->B;
+  A.lam = S->lam;
+  if (fu->nelem) DCHK(launch_stokes(A, S->N, S->NP, mode, fu->nelem, s));
+  if (mode != SM_B) DCHK(fs_restrict(fu, S->d_yu, yu, 0));
+  if (mode == SM_B || mode == SM_COUPLED) DCHK(fs_restrict(fp, S->d_yp, yp, 0));
+  return 0;
+}
+
+static dErr stokes_shell_mult(void *ctx, const double *x, double *y) {
+  _p_dStokes *S = (_p_dStokes *)ctx;
+  return stokes_mult(S, SM_COUPLED, x, x + S->nu3, y, y + S->nu3);
+}
+
+// block upper triangular preconditioner on the packed vector
+static dErr stokes_shell_pc(void *ctx, const double *r, double *z) {
+  _p_dStokes *S = (_p_dStokes *)ctx;
+  cudaStream_t s = S->fsu->stream;
+  const double *ru = r, *rp = r + S->nu3;
+  double *zu = z, *zp = z + S->nu3;
+  k_schur_diag<<<nblk(S->np), 256, 0, s>>>(S->np, S->B, S->d_mdiag, rp, zp);
+  CUCHK(cudaGetLastError());
+  // remove the constant (mean over the dofs): sum through a dot with the ones vector stored after d_t
+  const double *ones = S->d_t + S->nu3;
+  DCHK(device_dot(S->np, zp, ones, S->d_part, S->d_s, s));
+  k_sub_mean<<<nblk(S->np), 256, 0, s>>>(S->np, S->d_s, zp);
+  // t = r_u - Bt z_p, z_u = Cheb(A_q1) t
+  double *t = S->d_t;
+  DCHK(stokes_mult(S, SM_BT, nullptr, zp, t, nullptr));
+  k_rsub<<<nblk(S->nu3), 256, 0, s>>>(S->nu3, ru, t);
+  CUCHK(cudaGetLastError());
+  return ksp_pc_only(S->kspu, t, zu);
+}
+
+extern "C" {
+
+dErr dStokesCreate(dFS fsu, dFS fsp, const dReal rheo[4], dStokes *stk) {
+  if (!fsu || !fsp || !stk) return set_error("null argument");
+  if (!fsu->setup || !fsp->setup) return set_error("dFS not set up");
+  if (fsu->bs != 3 || fsp->bs != 1) return set_error("Stokes needs a bs 3 velocity space and a bs 1 pressure space");
+  if (fsu->nelem != fsp->nelem || fsu->mesh != fsp->mesh) return set_error("velocity and pressure spaces must share the mesh");
+  if (!fsu->uniform || !fsp->uniform) return set_error("Stokes spaces of uniform degree only");
+  if (fsp->dirichlet_mask) return set_error("the pressure space takes no Dirichlet sets (stokes.c:222)");
+  _p_dStokes *S = new _p_dStokes();
+  if (rheo) S->B = rheo[0], S->eps = rheo[1], S->p = rheo[2], S->nu = rheo[3];
+  if (S->p != 2) {
+    delete S;
+    return set_error("Stokes rheology exponent %g: only the Newtonian case (p = 2) is built", S->p);
+  }
+  if (!(S->B > 0) || !(S->nu < 0.5)) {
+    delete S;
+    return set_error("Stokes rheology needs B > 0 and nu < 1/2");
+  }
+  S->lam = S->nu / (1 - 2 * S->nu);  // StokesLambda (stokes.c:455-458)
+  S->fsu = fsu, S->fsp = fsp;
+  S->N = fsu->p + 1, S->NP = fsp->p + 1;
+  if (!(S->NP == S->N - 1 || S->NP == S->N - 2) || S->NP < 2 || S->N > 7) {
+    delete S;
+    return set_error("Stokes spaces of degrees %d / %d are not built (velocity 2..6, pressure codim 1 or 2)", fsu->p, fsp->p);
+  }
+  S->nu3 = fsu->n * 3;
+  S->np = fsp->n;
+  cudaStream_t s = fsu->stream;
+  // pressure GLL basis at the velocity's Gauss points
+  {
+    double x[MAXQ], w[MAXQ], gll[MAXP], lw[MAXP], val[MAXP], der[MAXP];
+    gauss_rule(S->N, x, w);
+    lobatto_rule(S->NP, gll, lw);
+    std::vector<double> bp(S->N * S->NP);
+    for (int a = 0; a < S->N; a++) {
+      lagrange(S->NP, gll, x[a], val, der);
+      for (int i = 0; i < S->NP; i++) bp[a * S->NP + i] = val[i];
+    }
+    CUCHK(cudaMalloc(&S->d_bp, bp.size() * sizeof(double)));
+    CUCHK(cudaMemcpy(S->d_bp, bp.data(), bp.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  CUCHK(cudaMalloc(&S->d_geo, std::max<int64_t>(fsu->nq, 1) * 10 * sizeof(double)));
+  DCHK(geometry_fill(fsu, 1, nullptr, S->d_geo));
+  CUCHK(cudaMalloc(&S->d_yu, std::max<int64_t>(fsu->nexp * 3, 1) * sizeof(double)));
+  CUCHK(cudaMalloc(&S->d_yp, std::max<int64_t>(fsp->nexp, 1) * sizeof(double)));
+  CUCHK(cudaMalloc(&S->d_mdiag, std::max<int64_t>(S->np, 1) * sizeof(double)));
+  CUCHK(cudaMalloc(&S->d_t, (S->nu3 + std::max<int64_t>(S->np, 1)) * sizeof(double)));
+  CUCHK(cudaMalloc(&S->d_part, 1024 * sizeof(double)));
+  CUCHK(cudaMalloc(&S->d_s, 8 * sizeof(double)));
+  k_fill<<<nblk(S->np), 256, 0, s>>>(S->np, 1.0, S->d_t + S->nu3);  // ones vector for the pressure mean
+  DCHK(pmass_diag(S->N, S->NP, fsu->nelem, fsu->d_qoff, fsp->d_xstart, S->d_geo, S->d_bp, S->d_yp, s));
+  DCHK(fs_restrict(fsp, S->d_yp, S->d_mdiag, 0));
+  CUCHK(cudaStreamSynchronize(s));
+  *stk = S;
+  return 0;
+}
+
+dErr dStokesDestroy(dStokes *stk) {
+  if (!stk || !*stk) return 0;
+  _p_dStokes *S = *stk;
+  for (double *p : {S->d_geo, S->d_bp, S->d_yu, S->d_yp, S->d_mdiag, S->d_t, S->d_part, S->d_s}) cudaFree(p);
+  dKSPDestroy(&S->ksp);
+  dKSPDestroy(&S->kspu);
+  dMatDestroy(&S->Ap);
+  dOperatorDestroy(&S->opu);
+  delete S;
+  *stk = nullptr;
+  return 0;
+}
+
+dErr dStokesMult(dStokes stk, dStokesMultMode mode, const dScalar *xu, const dScalar *xp, dScalar *yu, dScalar *yp) {
+  if (!stk) return set_error("null Stokes");
+  const int m = (int)mode;
+  if (m < SM_A || m > SM_COUPLED) return set_error("invalid Stokes mult mode %d", m);
+  if ((m != SM_BT && !xu) || ((m == SM_BT || m == SM_COUPLED) && !xp) || (m != SM_B && !yu) || ((m == SM_B || m == SM_COUPLED) && !yp))
+    return set_error("missing vector for Stokes mult mode %d", m);
+  return stokes_mult(stk, m, xu, xp, yu, yp);
+}
+
+dErr dStokesSolve(dStokes stk, const dScalar *bu, const dScalar *bp, dScalar *xu, dScalar *xp, dReal rtol, dInt maxit, dInt *its,
+                  dReal *rnorm) {
+  if (!stk || !bu || !bp || !xu || !xp) return set_error("null argument");
+  _p_dStokes *S = stk;
+  _p_dFS *fu = S->fsu;
+  cudaStream_t s = fu->stream;
+  if (!S->ksp) {  // the velocity block: Chebyshev-Jacobi on the Q1-embedded A (2 mu = eta, lambda as A)
+    DCHK(dFSCreateOperator(fu, dOP_ELASTICITY, nullptr, &S->opu));
+    DCHK(dFSCreateMatrix(fu, &S->Ap));
+    DCHK(q1_numeric_elast(fu, S->Ap, S->lam, 0.5 * S->B, 1));
+    DCHK(dKSPCreate(S->opu, S->Ap, dKSP_CG, dPC_CHEBYSHEV_Q1, &S->kspu));
+    DCHK(ksp_create_shell(S->nu3 + S->np, s, dKSP_FGMRES, stokes_shell_mult, stokes_shell_pc, S, S->restart, &S->ksp));
+  }
+  const int64_t n = S->nu3 + S->np;
+  double *b, *x;
+  CUCHK(cudaMalloc(&b, n * sizeof(double)));
+  CUCHK(cudaMalloc(&x, n * sizeof(double)));
+  CUCHK(cudaMemcpyAsync(b, bu, S->nu3 * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CUCHK(cudaMemcpyAsync(b + S->nu3, bp, S->np * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CUCHK(cudaMemcpyAsync(x, xu, S->nu3 * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CUCHK(cudaMemcpyAsync(x + S->nu3, xp, S->np * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  int it = 0;
+  double rn = 0;
+  dErr e = ksp_solve(S->ksp, b, x, rtol, maxit, &it, &rn);
+  if (!e) {  // the pressure is determined up to a constant: return the zero-mean one
+    const double *ones = S->d_t + S->nu3;
+    e = device_dot(S->np, x + S->nu3, ones, S->d_part, S->d_s, s);
+    if (!e) k_sub_mean<<<nblk(S->np), 256, 0, s>>>(S->np, S->d_s, x + S->nu3);
+  }
+  if (!e) {
+    CUCHK(cudaMemcpyAsync(xu, x, S->nu3 * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CUCHK(cudaMemcpyAsync(xp, x + S->nu3, S->np * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CUCHK(cudaStreamSynchronize(s));
+  }
+  cudaFree(b);
+  cudaFree(x);
+  if (e) return e;
+  if (its) *its = it;
+  if (rnorm) *rnorm = rn;
+  if (!(rn <= rtol)) return set_error("Stokes FGMRES did not converge in %d iterations (relative residual %g)", it, rn);
+  return 0;
+}
+
+}  // extern "C"

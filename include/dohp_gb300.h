@@ -59,6 +59,7 @@ typedef struct _p_dMat *dMat;
 typedef struct _p_dRulesetIterator *dRulesetIterator;
 typedef struct _p_dKSP *dKSP;
 typedef struct _p_dFacetIterator *dFacetIterator;
+typedef struct _p_dStokes *dStokes;
 
 /* Operator (pointwise q-function) kinds of the fused matrix-free apply */
 typedef enum {
@@ -238,6 +239,25 @@ dErr dFacetIteratorGetApplied(dFacetIterator it, int64_t *nq, const dReal **jw, 
 dErr dFacetIteratorCommit(dFacetIterator it, InsertMode imode);
 /* restrict the expanded boundary vector into y (INSERT_VALUES overwrites, ADD_VALUES adds to a volume residual) */
 dErr dFacetIteratorFinish(dFacetIterator it, dScalar *y, InsertMode imode);
+
+/* ---------------------------------------------------------------- mixed velocity-pressure (Stokes) */
+/* src/fs/tests/stokes.c: StokesMultMode (stokesimpl.h:34) plus the coupled MatMult_Nest_StokesCoupled */
+typedef enum { dSTOKES_MULT_A = 0, dSTOKES_MULT_BT = 1, dSTOKES_MULT_B = 2, dSTOKES_MULT_COUPLED = 3 } dStokesMultMode;
+/* StokesCreate / StokesSetFromOptions / StokesGetMatrices (stokes.c:102-130, 160-274, 367-445): fsu the velocity
+ * space (bs 3, degree k in 2..6, Dirichlet sets), fsp the pressure space (bs 1, degree k-1 or k-2, no boundary sets)
+ * on the same mesh; rheo = {B, eps, p, nu} (struct StokesRheology, stokesimpl.h:9-11; the reference's defaults
+ * 1, 1, 2, 0; NULL takes them). Newtonian rheology (p = 2) only. */
+dErr dStokesCreate(dFS fsu, dFS fsp, const dReal rheo[4], dStokes *stk);
+dErr dStokesDestroy(dStokes *stk);
+/* y = [A Bt; B 0] x blocks (StokesShellMatMult_All_IorA stokes.c:579-673, MatMult_Nest_StokesCoupled 541-577):
+ * A: xu -> yu (with the penalty nu/(1-2nu)); BT: xp -> yu; B: xu -> yp; COUPLED: (xu, xp) -> (yu, yp) without
+ * the penalty. Device vectors; the unused ones may be NULL. */
+dErr dStokesMult(dStokes stk, dStokesMultMode mode, const dScalar *xu, const dScalar *xp, dScalar *yu, dScalar *yp);
+/* the coupled system solved by FGMRES with the block upper triangular (Schur) preconditioner: velocity block
+ * Chebyshev-Jacobi on the Q1-embedded viscous matrix, Schur complement -diag(M_p)/eta (the viscosity-scaled
+ * pressure mass, stokes.c:742-799); (xu, xp) is the initial guess and the result, xp returned with zero mean */
+dErr dStokesSolve(dStokes stk, const dScalar *bu, const dScalar *bp, dScalar *xu, dScalar *xp, dReal rtol, dInt maxit, dInt *its,
+                  dReal *rnorm);
 
 /* ---------------------------------------------------------------- Q1-embedded preconditioning matrix */
 /* dFSCreateMatrix (src/fs/interface/fs.c:770-813) as a device CSR over explicit scalar dofs; the sparsity is

@@ -1759,3 +1759,89 @@ int or_facet_commit(const or_fs *m, int weak_mask, const double *v, double *y, i
   free(fel); free(fside); free(qoff); free(ye);
   return rc;
 }
+
+/* ----------------------------------------------------------------------------------------------
+ * Stokes (src/fs/tests/stokes.c, stokesimpl.h): velocity space (bs 3, degree k) and pressure space (bs 1,
+ * degree k - codim, continuous, no Dirichlet sets) on the same mesh, the velocity's FAST rule (order 2k).
+ * -------------------------------------------------------------------------------------------- */
+/* include/dohp.h:77-82 */
+static double colon_sym(const double a[6], const double b[6])
+{
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + 2 * a[3] * b[3] + 2 * a[4] * b[4] + 2 * a[5] * b[5];
+}
+static void sym_compress(const double du[9], double s[6])
+{
+  s[0] = du[0]; s[1] = du[4]; s[2] = du[8];
+  s[3] = (du[1] + du[3]) / 2; s[4] = (du[2] + du[6]) / 2; s[5] = (du[5] + du[7]) / 2;
+}
+static void sym_uncompress(const double s[6], double du[9])
+{
+  du[0] = s[0]; du[4] = s[1]; du[8] = s[2];
+  du[1] = du[3] = s[3]; du[2] = du[6] = s[4]; du[5] = du[7] = s[5];
+}
+
+/* MatMult_Nest_StokesCoupled (stokes.c:541-577 with StokesPointwiseJacobian, stokes.c:476-487) and
+ * StokesShellMatMult_All_IorA (stokes.c:579-673 with StokesPointwiseJacobian_A/_B/_Bt, stokes.c:489-505).
+ * mode 0 A (with the penalty lambda = nu/(1-2nu), StokesLambda stokes.c:455-458), 1 Bt, 2 B, 3 coupled (lambda = 0).
+ * The store (StokesPointwiseComputeStore stokes.c:447-453) is evaluated from the velocity state su (NULL: zero). */
+int or_stokes_apply(const or_fs *fu, const or_fs *fp, int mode, const double rheo[4], const double *su, const double *xu,
+                    const double *xp, double *yu, double *yp)
+{
+  if (fu->bs != 3 || fp->bs != 1) return or_fail("Stokes needs a bs 3 velocity space and a bs 1 pressure space");
+  if (fu->nr != fp->nr) return or_fail("velocity and pressure spaces are on different meshes");
+  const double Bv = rheo[0], eps = rheo[1], pw = rheo[2], nu = rheo[3];
+  const double lambda = mode == 0 ? nu / (1 - 2 * nu) : 0.0;
+  const int use_u = mode == 0 || mode == 2 || mode == 3, use_p = mode == 1 || mode == 3;
+  const int out_u = mode != 2, out_p = mode >= 2;
+  double *xeu = calloc((size_t)fu->nexp * 3, sizeof(double)), *xep = calloc((size_t)fp->nexp, sizeof(double));
+  double *seu = calloc((size_t)fu->nexp * 3, sizeof(double));
+  double *yeu = calloc((size_t)fu->nexp * 3, sizeof(double)), *yep = calloc((size_t)fp->nexp, sizeof(double));
+  if (use_u) or_fs_global_to_expanded(fu, xu, NULL, xeu);
+  if (use_p) or_fs_global_to_expanded(fp, xp, NULL, xep);
+  if (su) or_fs_global_to_expanded(fu, su, NULL, seu);
+  double *jinv = malloc(sizeof(double) * 9 * 1000), *jw = malloc(sizeof(double) * 1000);
+  double *du = malloc(sizeof(double) * 9000), *ds = malloc(sizeof(double) * 9000), *dv = malloc(sizeof(double) * 9000);
+  double *pq = malloc(sizeof(double) * 1000), *qv = malloc(sizeof(double) * 1000);
+  int rc = 0;
+  for (int64_t r = 0; r < fu->nr && !rc; r++) {
+    basis1d bu;
+    if (basis_for(0, fu->edeg[3 * r], &bu)) { rc = -1; break; }
+    const basis1d *b[3] = {&bu, &bu, &bu};
+    const int P[3] = {bu.P, bu.P, bu.P}, Q[3] = {bu.Q, bu.Q, bu.Q}, nq = bu.Q * bu.Q * bu.Q;
+    const int Pp1 = fp->edeg[3 * r] + 1, Pp[3] = {Pp1, Pp1, Pp1};
+    double bpi[11 * 16], bpd[11 * 16], node[16], weight[16];
+    if (or_tensor_basis(Pp1, bu.Q, bu.x, bpi, bpd, node, weight)) { rc = -1; break; }
+    const double *bi[3] = {bu.interp, bu.interp, bu.interp}, *bd[3] = {bu.deriv, bu.deriv, bu.deriv};
+    const double *pi3[3] = {bpi, bpi, bpi}, *pd3[3] = {bpd, bpd, bpd};
+    if (element_geometry(fu, r, b, NULL, jinv, jw)) { rc = -1; break; }
+    or_efs_apply_hex(P, Q, bi, bd, jinv, 3, xeu + (int64_t)fu->xstart[r] * 3, du, OR_GRAD, OR_INSERT);
+    or_efs_apply_hex(P, Q, bi, bd, jinv, 3, seu + (int64_t)fu->xstart[r] * 3, ds, OR_GRAD, OR_INSERT);
+    or_efs_apply_hex(Pp, Q, pi3, pd3, NULL, 1, xep + fp->xstart[r], pq, OR_INTERP, OR_INSERT);
+    for (int q = 0; q < nq; q++) {
+      double Du[6], Ds[6], Dv[6];
+      sym_compress(du + 9 * q, Du);
+      sym_compress(ds + 9 * q, Ds);
+      const double greg = 0.5 * eps * eps + 0.5 * colon_sym(Ds, Ds);
+      const double eta = Bv * pow(greg, 0.5 * (pw - 2)), deta = 0.5 * (pw - 2) * eta / greg;
+      const double w = jw[q], tr = Du[0] + Du[1] + Du[2], dc = deta * colon_sym(Ds, Du), p = pq[q];
+      for (int i = 0; i < 6; i++) {
+        switch (mode) {
+          case 0: Dv[i] = w * (eta * Du[i] + dc * Ds[i] + lambda * (i < 3) * tr); break;
+          case 1: Dv[i] = i < 3 ? -w * p : 0; break;
+          case 3: Dv[i] = w * (eta * Du[i] + dc * Ds[i] + lambda * (i < 3) * tr - p * (i < 3)); break;
+          default: Dv[i] = 0;
+        }
+      }
+      sym_uncompress(Dv, dv + 9 * q);
+      qv[q] = -w * tr;
+    }
+    if (out_u) or_efs_apply_hex(P, Q, bi, bd, jinv, 3, dv, yeu + (int64_t)fu->xstart[r] * 3, OR_GRAD_TRANSPOSE, OR_INSERT);
+    if (out_p) or_efs_apply_hex(Pp, Q, pi3, pd3, NULL, 1, qv, yep + fp->xstart[r], OR_INTERP_TRANSPOSE, OR_INSERT);
+  }
+  if (!rc) {
+    if (out_u) or_fs_expanded_to_global(fu, yeu, yu, 0);
+    if (out_p) or_fs_expanded_to_global(fp, yep, yp, 0);
+  }
+  free(xeu); free(xep); free(seu); free(yeu); free(yep); free(jinv); free(jw); free(du); free(ds); free(dv); free(pq); free(qv);
+  return rc ? (rc == -1 ? -1 : or_fail("negative Jacobian")) : 0;
+}

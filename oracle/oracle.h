@@ -133,6 +133,14 @@ int or_facet_points(const or_fs *fs, int weak_mask, const double *g, double *jw,
 /* y (+)= E^T sum_q phi(xi_q) v_q over the facet points (add = 0 insert, 1 add) */
 int or_facet_commit(const or_fs *fs, int weak_mask, const double *v, double *y, int add);
 
+/* ---------------- Stokes (src/fs/tests/stokes.c) ---------------- */
+/* Coupled and block applies of the Stokes Jacobian on a velocity space fu (bs 3, degree k) and a pressure space fp
+ * (bs 1, degree k - codim, no Dirichlet sets) of the same mesh, at the velocity FAST rule: mode 0 A (viscous block
+ * with the penalty nu/(1-2nu)), 1 Bt (pressure -> velocity), 2 B (velocity -> pressure), 3 coupled [A Bt; B 0]
+ * without penalty. rheo = {B, eps, p, nu}; the viscosity store comes from the velocity state su (NULL: zero). */
+int or_stokes_apply(const or_fs *fu, const or_fs *fp, int mode, const double rheo[4], const double *su, const double *xu,
+                    const double *xp, double *yu, double *yp);
+
 /* deformation gradient F = I + Du [nq][9] at every FAST point of the state g (bs = 3, homogeneous Dirichlet;
  * ElastPointwiseComputeStore, elast.c:224-225) */
 int or_elast_state(const or_fs *fs, const double *g, double *Fq);

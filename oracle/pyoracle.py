@@ -98,6 +98,7 @@ def lib():
                                      ctypes.c_void_p, ctypes.c_void_p]
         L.or_facet_points.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, _f64p, _f64p, _f64p, _f64p]
         L.or_facet_commit.argtypes = [ctypes.c_void_p, ctypes.c_int, _f64p, _f64p, ctypes.c_int]
+        L.or_stokes_apply.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _f64p] + [ctypes.c_void_p] * 5
         _lib = L
     return _lib
 
@@ -361,6 +362,16 @@ def facet_rule(side, order, method=0):
     if n < 0:
         raise RuntimeError(lib().or_last_error().decode())
     return nodes[:3 * n].reshape(n, 3), w[:n]
+
+
+def stokes_apply(fu, fp, mode, rheo=(1.0, 1.0, 2.0, 0.0), xu=None, xp=None, state=None):
+    """(yu, yp) of the Stokes block apply: mode 0 A, 1 Bt, 2 B, 3 coupled"""
+    yu, yp = np.zeros(fu.n * 3), np.zeros(fp.n)
+    keep = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (state, xu, xp)]
+    addr = [None if a is None else a.ctypes.data for a in keep]
+    if lib().or_stokes_apply(fu.h, fp.h, mode, np.asarray(rheo, np.float64), *addr, yu.ctypes.data, yp.ctypes.data):
+        raise RuntimeError(lib().or_last_error().decode())
+    return yu, yp
 
 
 def grf_make(nf, var, ell, seed):

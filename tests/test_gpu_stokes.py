@@ -1,0 +1,130 @@
+"""Stokes (src/fs/tests/stokes.c) on the device: every block apply (A with and without the penalty, Bt, B,
+coupled) against the oracle, and the block-preconditioned FGMRES solve of a manufactured problem (divergence-free
+velocity vanishing on the walls, zero-mean pressure) converging at the Taylor-Hood rates."""
+import os
+
+import numpy as np
+import pytest
+
+import dohp_gb300 as dg
+import pyoracle as po
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import subprocess, sys
+    subprocess.run([sys.executable, os.path.join(os.path.dirname(dg.__file__), "build.py")], check=True)
+    dg.lib()
+
+
+def dev(a):
+    return torch.as_tensor(np.ascontiguousarray(a), device="cuda")
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def spaces(M, k, codim, seed=1, perturb=0.1):
+    fsu = dg.FS((M + 1,) * 3, degree=k, perturb=perturb, seed=seed, bs=3)
+    fsp = dg.FS(None, degree=k - codim, bs=1, dirichlet=(), mesh_of=fsu)
+    return fsu, fsp
+
+
+@pytest.mark.parametrize("k,codim,nu", [(3, 2, 0.0), (2, 1, 0.3), (4, 1, 0.0), (6, 2, 0.2)])
+def test_blocks_match_oracle(k, codim, nu):
+    M = 3
+    fsu, fsp = spaces(M, k, codim, seed=k)
+    ou = po.FS(M + 1, M + 1, M + 1, degree=k, perturb=0.1, seed=k, bs=3, dirichlet_mask=7)
+    op = po.FS(M + 1, M + 1, M + 1, degree=k - codim, perturb=0.1, seed=k, bs=1, dirichlet_mask=0)
+    rheo = (1.7, 1.0, 2.0, nu)
+    st = dg.Stokes(fsu, fsp, rheo)
+    rng = np.random.default_rng(k)
+    xu, xp = rng.uniform(-1, 1, fsu.n * 3), rng.uniform(-1, 1, fsp.n)
+    yu = torch.zeros(fsu.n * 3, dtype=torch.float64, device="cuda")
+    yp = torch.zeros(fsp.n, dtype=torch.float64, device="cuda")
+    rel = lambda a, b: np.linalg.norm(a - b) / np.linalg.norm(b)
+    st.mult(dg.dSTOKES_MULT_A, xu=dev(xu), yu=yu)
+    assert rel(host(yu), po.stokes_apply(ou, op, 0, rheo, xu=xu)[0]) < 1e-12
+    st.mult(dg.dSTOKES_MULT_BT, xp=dev(xp), yu=yu)
+    assert rel(host(yu), po.stokes_apply(ou, op, 1, rheo, xp=xp)[0]) < 1e-12
+    st.mult(dg.dSTOKES_MULT_B, xu=dev(xu), yp=yp)
+    assert rel(host(yp), po.stokes_apply(ou, op, 2, rheo, xu=xu)[1]) < 1e-12
+    st.mult(dg.dSTOKES_MULT_COUPLED, xu=dev(xu), xp=dev(xp), yu=yu, yp=yp)
+    cu, cp = po.stokes_apply(ou, op, 3, rheo, xu=xu, xp=xp)
+    assert rel(host(yu), cu) < 1e-12 and rel(host(yp), cp) < 1e-12
+
+
+def test_errors():
+    fsu, fsp = spaces(2, 3, 2)
+    with pytest.raises(dg.DohpError):
+        dg.Stokes(fsu, fsp, (1.0, 1.0, 1.5, 0.0))  # power-law rheology is not built
+    other = dg.FS((3, 3, 3), degree=1, bs=1, dirichlet=())
+    with pytest.raises(dg.DohpError):
+        dg.Stokes(fsu, other)  # not the same mesh
+    with pytest.raises(dg.DohpError):
+        dg.Stokes(fsu, dg.FS(None, degree=1, bs=1, mesh_of=fsu))  # pressure with Dirichlet sets
+
+
+def exact(x, eta):
+    """u = (psi_y, -psi_x, 0), psi = sin^2(pi x) sin^2(pi y) sin(pi z); p = cos(pi x) cos(pi y) cos(pi z);
+    f = -div(eta Du) + grad p = -(eta/2) lap u + grad p (div u = 0)"""
+    x = x.detach().clone().requires_grad_(True)
+    pi = np.pi
+    sx, sy, sz = torch.sin(pi * x[:, 0]), torch.sin(pi * x[:, 1]), torch.sin(pi * x[:, 2])
+    cx, cy = torch.cos(pi * x[:, 0]), torch.cos(pi * x[:, 1])
+    u = [sx ** 2 * 2 * pi * sy * cy * sz, -2 * pi * sx * cx * sy ** 2 * sz, torch.zeros_like(sx)]
+    p = torch.cos(pi * x[:, 0]) * torch.cos(pi * x[:, 1]) * torch.cos(pi * x[:, 2])
+    f = []
+    for i in range(3):
+        lap = torch.zeros_like(sx)
+        if i < 2:
+            g = torch.autograd.grad(u[i].sum(), x, create_graph=True)[0]
+            for j in range(3):
+                lap = lap + torch.autograd.grad(g[:, j].sum(), x, retain_graph=True)[0][:, j]
+        gp = torch.autograd.grad(p.sum(), x, retain_graph=True)[0][:, i]
+        f.append(-0.5 * eta * lap + gp)
+    return (torch.stack([v.detach() for v in u], 1), p.detach(), torch.stack([v.detach() for v in f], 1))
+
+
+def manufactured(M, k, codim, eta=1.0):
+    fsu, fsp = spaces(M, k, codim, seed=7)
+    st = dg.Stokes(fsu, fsp, (eta, 1.0, 2.0, 0.0))
+    it = dg.RulesetIterator(fsu)
+    it.start(None)
+    a = it.get()
+    _, _, f = exact(a["x"], eta)
+    a["v"].copy_(a["jw"][:, None] * f)
+    it.commit(dg.INSERT_VALUES, use_v=True, use_dv=False)
+    bu = torch.zeros(fsu.n * 3, dtype=torch.float64, device="cuda")
+    it.finish(bu)
+    bp = torch.zeros(fsp.n, dtype=torch.float64, device="cuda")
+    xu, xp = torch.zeros_like(bu), torch.zeros_like(bp)
+    its, rn = st.solve(bu, bp, xu, xp, rtol=1e-10, maxit=1000)
+    # velocity error
+    it.start(xu)
+    a = it.get()
+    ue, _, _ = exact(a["x"], eta)
+    uerr, _ = it.error_norms(ue.contiguous(), None)
+    # pressure error modulo constants
+    ip = dg.RulesetIterator(fsp)
+    ip.start(xp)
+    b = ip.get()
+    _, pe, _ = exact(b["x"], eta)
+    e = b["u"][:, 0] - pe
+    e = e - (b["jw"] * e).sum() / b["jw"].sum()
+    perr = float(torch.sqrt((b["jw"] * e ** 2).sum()))
+    return uerr[1], perr, its, abs(float(xp.sum()))
+
+
+def test_manufactured_taylor_hood_converges():
+    eu4, ep4, its4, m4 = manufactured(4, 3, 1)
+    eu8, ep8, its8, m8 = manufactured(8, 3, 1)
+    assert m4 < 1e-10 and m8 < 1e-10  # zero-mean pressure returned
+    assert eu8 < 1e-3 and ep8 < 1e-2
+    assert eu4 / eu8 > 10 and ep4 / ep8 > 5, (eu4, eu8, ep4, ep8)  # h^4 velocity, h^3 pressure at k = 3
+    assert its8 < 2 * its4 + 20, (its4, its8)  # the block preconditioner keeps the count nearly mesh-independent
