@@ -307,9 +307,29 @@ def secondary_cfg4(args):
     ms, _ = time_loop(lambda: (op.mult_expanded(x, yexp), fs.expanded_to_global(yexp, y)), max(args.steps // 2, 5), stream)
     _, kms = time_loop(lambda: op.mult_expanded(x, yexp), max(args.steps // 2, 5), stream)
     _, _, issued = work_per_apply(fs, cfg, bs)
-    return {"workload": cfg["label"], "dofs": fs.n, "value": fs.n / (ms * 1e-3) / 1e9, "unit": "GDoF/s", "ms_per_apply": ms,
-            "element_kernel_ms": kms, "fp64_gflops": issued / (kms * 1e-3) / 1e9,
-            "fp64_frac_of_peak": issued / (kms * 1e-3) / 1e9 / FP64_PEAK_GFLOPS, "dtype": "f64"}
+    out = {"workload": cfg["label"], "dofs": fs.n, "value": fs.n / (ms * 1e-3) / 1e9, "unit": "GDoF/s", "ms_per_apply": ms,
+           "element_kernel_ms": kms, "fp64_gflops": issued / (kms * 1e-3) / 1e9,
+           "fp64_frac_of_peak": issued / (kms * 1e-3) / 1e9 / FP64_PEAK_GFLOPS, "dtype": "f64"}
+    out["float_float"] = float_float_leg(op, x, y, args, stream)
+    out["float_float"]["value"] = fs.n / (out["float_float"]["ms_per_apply"] * 1e-3) / 1e9
+    return out
+
+
+def float_float_leg(op, x, y64, args, stream):
+    """the same apply with dPREC_FF (values as FP32 pairs, unit roundoff ~2^-48, FP32 pipe), its time and its
+    relative difference from the FP64 result in y64 (computed by the caller with the same operator)"""
+    import torch
+    import dohp_gb300 as dg
+    op.mult(x, y64)
+    op.set_precision(dg.dPREC_FF)
+    yff = torch.empty_like(y64)
+    for _ in range(3):
+        op.mult(x, yff)
+    ms, _ = time_loop(lambda: op.mult(x, yff), max(args.steps, 5), stream)
+    err = float(torch.linalg.norm(yff - y64) / torch.linalg.norm(y64))
+    op.set_precision(dg.dPREC_FP64)
+    return {"unit": "GDoF/s", "ms_per_apply": ms, "rel_diff_vs_fp64": err,
+            "dtype": "float-float (2 x fp32 per value, unit roundoff ~2^-48, FP32 pipe)"}
 
 
 def secondary_newton(args):
@@ -510,6 +530,10 @@ def main():
         ms_step = max_over_ranks(ms_step, dist)
         dist.barrier()
 
+    # the same apply in float-float arithmetic, reported beside the FP64 headline (not in place of it)
+    ffleg = float_float_leg(op, x, y, args, stream)
+    ffleg["value"] = whole_job_gdofs(world, N, ffleg["ms_per_apply"] * 1e-3)
+
     # end to end through the host-vector entry point (pinned buffers, copies inside the timed region)
     xh = torch.empty(N, dtype=torch.float64).pin_memory()
     yh = torch.empty(N, dtype=torch.float64).pin_memory()
@@ -551,6 +575,7 @@ def main():
         "gpu_launches": 2 * args.steps,
         "clocks": clk.summary(),
     }
+    line["float_float"] = ffleg
     if cfg["hp"]:
         line["launch_forms"] = forms
         line["tiles"] = op.tiles()

@@ -278,6 +278,8 @@ dErr dOperatorDestroy(dOperator *op) {
   cudaFree(o->d_geo);
   cudaFree(o->d_geo32);
   cudaFree(o->d_geo16);
+  cudaFree(o->d_geoff);
+  cudaFree(o->d_yff);
   cudaFree(o->d_k);
   cudaFree(o->d_stash);
   cudaFree(o->d_yexp);
@@ -313,7 +315,7 @@ dErr dOperatorSetQuadratureData(dOperator op, const dReal *qdata) {
 
 dErr dOperatorSetPrecision(dOperator op, dPrecision prec) {
   if (!op) return set_error("null operator");
-  if (prec != dPREC_FP64 && prec != dPREC_FP32 && prec != dPREC_BF16) return set_error("precision %d not supported", (int)prec);
+  if (prec != dPREC_FP64 && prec != dPREC_FP32 && prec != dPREC_BF16 && prec != dPREC_FF) return set_error("precision %d not supported", (int)prec);
   op->prec = prec;
   return 0;
 }

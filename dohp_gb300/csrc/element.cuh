@@ -15,6 +15,7 @@
 
 #include <cuda_bf16.h>
 
+#include "ff.cuh"
 #include "internal.h"
 
 namespace dgb {
@@ -70,8 +71,8 @@ __device__ __forceinline__ void pass(const T *sm, const T *in, T *out, int ne) {
     const T *src = in + el * N3 + r - i * ST;
     T s = 0;
 #pragma unroll
-    for (int j = 0; j < N; j++) s += ((MAT & 1) ? M[j * N + i] : M[i * N + j]) * src[j * ST];
-    out[t] = s;
+    for (int j = 0; j < N; j++) fma_acc(s, (MAT & 1) ? M[j * N + i] : M[i * N + j], src[j * ST]);
+    out[t] = fin(s);
   }
 }
 
@@ -120,13 +121,13 @@ __device__ __forceinline__ void grad(const T *sm, const T *S1, T *G0, T *G1, T *
     T g0 = 0, g1 = 0, g2 = 0;
 #pragma unroll
     for (int i = 0; i < N; i++) {
-      g0 += sD[a * N + i] * U[i * NN + b * N + c];
-      g1 += sD[b * N + i] * U[a * NN + i * N + c];
-      g2 += sD[c * N + i] * U[a * NN + b * N + i];
+      fma_acc(g0, sD[a * N + i], U[i * NN + b * N + c]);
+      fma_acc(g1, sD[b * N + i], U[a * NN + i * N + c]);
+      fma_acc(g2, sD[c * N + i], U[a * NN + b * N + i]);
     }
-    G0[t] = g0;
-    G1[t] = g1;
-    G2[t] = g2;
+    G0[t] = fin(g0);
+    G1[t] = fin(g1);
+    G2[t] = fin(g2);
   }
   __syncthreads();
 }
@@ -143,8 +144,8 @@ __device__ __forceinline__ void back(const T *sm, const T *V0, const T *V1, cons
     T s = 0;
 #pragma unroll
     for (int i = 0; i < N; i++)
-      s += sD[i * N + a] * v0[i * NN + b * N + c] + sD[i * N + b] * v1[a * NN + i * N + c] + sD[i * N + c] * v2[a * NN + b * N + i];
-    S1[t] = s;
+      dot3_acc(s, sD[i * N + a], v0[i * NN + b * N + c], sD[i * N + b], v1[a * NN + i * N + c], sD[i * N + c], v2[a * NN + b * N + i]);
+    S1[t] = fin(s);
   }
   __syncthreads();
   pass<N, M_BT, 2>(sm, S1, S0, ne);
@@ -156,8 +157,8 @@ __device__ __forceinline__ void back(const T *sm, const T *V0, const T *V1, cons
     const T *in = &S1[el * N3 + jk];
     T s = 0;
 #pragma unroll
-    for (int a = 0; a < N; a++) s += sB[a * N + i] * in[a * NN];
-    yexp[((int64_t)A.xstart[elem_id(els, first, el)] + r) * BS + d] = s;
+    for (int a = 0; a < N; a++) fma_acc(s, sB[a * N + i], in[a * NN]);
+    yexp[((int64_t)A.xstart[elem_id(els, first, el)] + r) * BS + d] = fin(s);
   }
   __syncthreads();
 }

@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <numeric>
 
+#include "ff.cuh"
 #include "internal.h"
 
 using namespace dgb;
@@ -95,6 +96,19 @@ dErr fs_restrict32(_p_dFS *fs, const float *x, double *g, int add) {
     return 0;
   }
   k_restrict<float><<<(unsigned)((N + 255) / 256), 256, 0, fs->stream>>>(fs->n, fs->bs, fs->d_et_ptr, fs->d_et_idx, x, g, add);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+dErr fs_restrict_ff(_p_dFS *fs, const ff *x, double *g, int add) {
+  const int64_t N = fs->n * fs->bs;
+  if (N == 0) return 0;
+  if (!fs->boolean_e) {
+    k_restrict_w<ff><<<(unsigned)((N + 255) / 256), 256, 0, fs->stream>>>(fs->n, fs->bs, fs->d_et_ptr, fs->d_et_idx, fs->d_et_w, x, g, add);
+    CUCHK(cudaGetLastError());
+    return 0;
+  }
+  k_restrict<ff><<<(unsigned)((N + 255) / 256), 256, 0, fs->stream>>>(fs->n, fs->bs, fs->d_et_ptr, fs->d_et_idx, x, g, add);
   CUCHK(cudaGetLastError());
   return 0;
 }

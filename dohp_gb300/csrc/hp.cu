@@ -28,6 +28,7 @@ using namespace dgb;
 dErr op_compute_geometry(_p_dOperator *op);
 dErr fs_restrict(_p_dFS *fs, const double *x, double *g, int add);
 dErr fs_restrict32(_p_dFS *fs, const float *x, double *g, int add);
+dErr fs_restrict_ff(_p_dFS *fs, const ff *x, double *g, int add);
 
 namespace {
 
@@ -128,7 +129,7 @@ struct HpPlan {
   bool tuned = false;
   // graph form
   const double **d_ptrs = nullptr;  // [x, y]
-  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};  // per precision (fp64, fp32, float-float)
 };
 
 static void plan_free(HpPlan *p) {
@@ -137,7 +138,7 @@ static void plan_free(HpPlan *p) {
   cudaFree(p->d_work);
   cudaFree(p->d_counter);
   cudaFree((void *)p->d_ptrs);
-  for (int i = 0; i < 2; i++)
+  for (int i = 0; i < 3; i++)
     if (p->exec[i]) cudaGraphExecDestroy(p->exec[i]);
   delete p;
 }
@@ -198,7 +199,10 @@ static dErr plan_build(_p_dOperator *op) {
   return 0;
 }
 
-static HpArgs make_args(_p_dOperator *op, const double *x, bool fp32, void *yexp, const double *const *px) {
+// precision index: 0 FP64, 1 FP32, 2 float-float
+static int prec_index(const _p_dOperator *op) { return op->prec == dPREC_FP32 ? 1 : op->prec == dPREC_FF ? 2 : 0; }
+
+static HpArgs make_args(_p_dOperator *op, const double *x, int pi, void *yexp, const double *const *px) {
   _p_dFS *fs = op->fs;
   HpArgs A;
   A.xstart = fs->d_xstart;
@@ -211,7 +215,7 @@ static HpArgs make_args(_p_dOperator *op, const double *x, bool fp32, void *yexp
   A.n = fs->n;
   A.x = x;
   A.px = px;
-  A.geo = fp32 ? (const void *)op->d_geo32 : (const void *)op->d_geo;
+  A.geo = pi == 1 ? (const void *)op->d_geo32 : pi == 2 ? (const void *)op->d_geoff : (const void *)op->d_geo;
   A.tab_all = fs->d_fast_tab;
   A.yexp = yexp;
   A.lam = op->lam;
@@ -297,12 +301,12 @@ static dErr autotune(_p_dOperator *op, const HpArgs &A) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   P->tuned = true;
-  for (int i = 0; i < 2; i++)
+  for (int i = 0; i < 3; i++)
     if (P->exec[i]) cudaGraphExecDestroy(P->exec[i]), P->exec[i] = nullptr;
   return plan_work(P, op->kind, s);
 }
 
-static std::string tune_key(_p_dOperator *op, int N, bool fp32) {
+static std::string tune_key(_p_dOperator *op, int N, int pi) {
   char name[256] = "gpu";
   int dev;
   cudaDeviceProp prop;
@@ -310,12 +314,12 @@ static std::string tune_key(_p_dOperator *op, int N, bool fp32) {
   for (char *c = name; *c; c++)
     if (*c == ' ' || *c == '"') *c = '_';
   std::ostringstream k;
-  k << name << ":kind" << (int)op->kind << ":N" << N << ":" << (fp32 ? "fp32" : "fp64");
+  k << name << ":kind" << (int)op->kind << ":N" << N << ":" << (pi == 1 ? "fp32" : pi == 2 ? "ff" : "fp64");
   return k.str();
 }
 
 // JSON cache: {"key": [cap, threads], ...}
-static void tune_load(_p_dOperator *op, const char *path, bool fp32) {
+static void tune_load(_p_dOperator *op, const char *path, int pi) {
   std::ifstream f(path);
   if (!f) return;
   std::stringstream ss;
@@ -324,7 +328,7 @@ static void tune_load(_p_dOperator *op, const char *path, bool fp32) {
   HpPlan *P = (HpPlan *)op->hp_plan;
   int found = 0;
   for (int b = 0; b < P->nb; b++) {
-    const std::string key = "\"" + tune_key(op, P->N[b], fp32) + "\"";
+    const std::string key = "\"" + tune_key(op, P->N[b], pi) + "\"";
     const size_t at = js.find(key);
     if (at == std::string::npos) continue;
     int cap, thr;
@@ -335,7 +339,7 @@ static void tune_load(_p_dOperator *op, const char *path, bool fp32) {
   if (found == P->nb) P->tuned = true;
 }
 
-static void tune_save(_p_dOperator *op, const char *path, bool fp32) {
+static void tune_save(_p_dOperator *op, const char *path, int pi) {
   HpPlan *P = (HpPlan *)op->hp_plan;
   std::string js;
   {
@@ -358,7 +362,7 @@ static void tune_save(_p_dOperator *op, const char *path, bool fp32) {
     const size_t lb = js.find('[', end), rb = js.find(']', end);
     if (lb == std::string::npos || rb == std::string::npos) break;
     bool ours = false;
-    for (int b = 0; b < P->nb; b++) ours |= key == tune_key(op, P->N[b], fp32);
+    for (int b = 0; b < P->nb; b++) ours |= key == tune_key(op, P->N[b], pi);
     if (!ours) {
       o << (firstk ? "" : ",\n") << " \"" << key << "\": " << js.substr(lb, rb - lb + 1);
       firstk = false;
@@ -366,7 +370,7 @@ static void tune_save(_p_dOperator *op, const char *path, bool fp32) {
     pos = rb + 1;
   }
   for (int b = 0; b < P->nb; b++) {
-    o << (firstk ? "" : ",\n") << " \"" << tune_key(op, P->N[b], fp32) << "\": [" << P->cap[b] << ", " << P->threads[b] << "]";
+    o << (firstk ? "" : ",\n") << " \"" << tune_key(op, P->N[b], pi) << "\": [" << P->cap[b] << ", " << P->threads[b] << "]";
     firstk = false;
   }
   o << "\n}\n";
@@ -415,41 +419,55 @@ dErr hp_mult(_p_dOperator *op, const double *x, double *y) {
     }
   }
   DCHK(op_compute_geometry(op));
-  const bool fp32 = op->prec == dPREC_FP32;
-  if (fp32 && !op->d_geo32) {
+  const int pi = prec_index(op);
+  if (pi && !(pi == 1 ? op->d_geo32 : op->d_geoff)) {  // factors rounded to FP32 / split into float pairs once
     const int64_t ng = fs->nq * (op->kind == dOP_ELASTICITY ? 10 : 6);
     std::vector<double> h(ng);
     CUCHK(cudaMemcpy(h.data(), op->d_geo, ng * sizeof(double), cudaMemcpyDeviceToHost));
-    std::vector<float> f(h.begin(), h.end());
-    CUCHK(cudaMalloc(&op->d_geo32, ng * sizeof(float)));
-    CUCHK(cudaMemcpy(op->d_geo32, f.data(), ng * sizeof(float), cudaMemcpyHostToDevice));
+    if (pi == 1) {
+      std::vector<float> f(h.begin(), h.end());
+      CUCHK(cudaMalloc(&op->d_geo32, ng * sizeof(float)));
+      CUCHK(cudaMemcpy(op->d_geo32, f.data(), ng * sizeof(float), cudaMemcpyHostToDevice));
+    } else {
+      std::vector<ff> f(h.begin(), h.end());
+      CUCHK(cudaMalloc(&op->d_geoff, ng * sizeof(ff)));
+      CUCHK(cudaMemcpy(op->d_geoff, f.data(), ng * sizeof(ff), cudaMemcpyHostToDevice));
+    }
   }
   if (!op->hp_plan) {
     DCHK(plan_build(op));
-    if (op->tune_path[0]) tune_load(op, op->tune_path, fp32);
+    if (op->tune_path[0]) tune_load(op, op->tune_path, pi);
   }
   HpPlan *P = (HpPlan *)op->hp_plan;
   void *yexp;
-  if (fp32) {
+  if (pi == 1) {
     if (!op->d_y32) CUCHK(cudaMalloc(&op->d_y32, fs->nexp * fs->bs * sizeof(float)));
     yexp = op->d_y32;
+  } else if (pi == 2) {
+    if (!op->d_yff) CUCHK(cudaMalloc(&op->d_yff, fs->nexp * fs->bs * sizeof(ff)));
+    yexp = op->d_yff;
   } else {
     if (!op->d_yexp) CUCHK(cudaMalloc(&op->d_yexp, fs->nexp * fs->bs * sizeof(double)));
     yexp = op->d_yexp;
   }
   if (op->autotune && !P->tuned) {
-    const HpArgs A = make_args(op, x, fp32, yexp, nullptr);
-    if (fp32) DCHK(autotune<float>(op, A));
+    const HpArgs A = make_args(op, x, pi, yexp, nullptr);
+    if (pi == 1) DCHK(autotune<float>(op, A));
+    else if (pi == 2) DCHK(autotune<ff>(op, A));
     else DCHK(autotune<double>(op, A));
-    if (op->tune_path[0]) tune_save(op, op->tune_path, fp32);
+    if (op->tune_path[0]) tune_save(op, op->tune_path, pi);
   }
   cudaStream_t s = fs->stream;
+  auto persistent = [&](const HpArgs &A, cudaStream_t st, int grid) -> dErr {
+    return pi == 1 ? run_persistent<float>(op, A, st, grid) : pi == 2 ? run_persistent<ff>(op, A, st, grid) : run_persistent<double>(op, A, st, grid);
+  };
   int grid = 0;
-  if (op->launch == dLAUNCH_PERSISTENT || op->launch == dLAUNCH_GRAPH) DCHK(fp32 ? prepare_persistent<float>(op, &grid) : prepare_persistent<double>(op, &grid));
+  if (op->launch == dLAUNCH_PERSISTENT || op->launch == dLAUNCH_GRAPH)
+    DCHK(pi == 1 ? prepare_persistent<float>(op, &grid) : pi == 2 ? prepare_persistent<ff>(op, &grid) : prepare_persistent<double>(op, &grid));
   if (op->launch == dLAUNCH_GRAPH) {
     const double *ptrs[2] = {x, y};
     CUCHK(cudaMemcpyAsync((void *)P->d_ptrs, ptrs, sizeof ptrs, cudaMemcpyHostToDevice, s));
-    cudaGraphExec_t &ex = P->exec[fp32 ? 1 : 0];
+    cudaGraphExec_t &ex = P->exec[pi];
     if (!ex) {
       // capture on a private stream (the legacy default stream cannot be captured); the graph is then
       // launched on the operator's stream, ordered after the pointer-table copy above
@@ -457,14 +475,17 @@ dErr hp_mult(_p_dOperator *op, const double *x, double *y) {
       CUCHK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
       cudaGraph_t g;
       CUCHK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-      const HpArgs A = make_args(op, nullptr, fp32, yexp, P->d_ptrs);
-      dErr e = fp32 ? run_persistent<float>(op, A, cs, grid) : run_persistent<double>(op, A, cs, grid);
+      const HpArgs A = make_args(op, nullptr, pi, yexp, P->d_ptrs);
+      dErr e = persistent(A, cs, grid);
       const int64_t N = fs->n * fs->bs;
       if (!e && N) {
         const int32_t *eti = fs->d_et_idx;
         const double *etw = fs->boolean_e ? nullptr : fs->d_et_w;
-        if (fp32) k_restrict_table<float><<<(unsigned)((N + 255) / 256), 256, 0, cs>>>(fs->n, fs->bs, fs->d_et_ptr, eti, etw, (const float *)yexp, (double *const *)(P->d_ptrs + 1));
-        else k_restrict_table<double><<<(unsigned)((N + 255) / 256), 256, 0, cs>>>(fs->n, fs->bs, fs->d_et_ptr, eti, etw, (const double *)yexp, (double *const *)(P->d_ptrs + 1));
+        const unsigned nbk = (unsigned)((N + 255) / 256);
+        double *const *py = (double *const *)(P->d_ptrs + 1);
+        if (pi == 1) k_restrict_table<float><<<nbk, 256, 0, cs>>>(fs->n, fs->bs, fs->d_et_ptr, eti, etw, (const float *)yexp, py);
+        else if (pi == 2) k_restrict_table<ff><<<nbk, 256, 0, cs>>>(fs->n, fs->bs, fs->d_et_ptr, eti, etw, (const ff *)yexp, py);
+        else k_restrict_table<double><<<nbk, 256, 0, cs>>>(fs->n, fs->bs, fs->d_et_ptr, eti, etw, (const double *)yexp, py);
       }
       cudaError_t ce = cudaStreamEndCapture(cs, &g);
       cudaStreamDestroy(cs);
@@ -476,10 +497,12 @@ dErr hp_mult(_p_dOperator *op, const double *x, double *y) {
     CUCHK(cudaGraphLaunch(ex, s));
     return 0;
   }
-  const HpArgs A = make_args(op, x, fp32, yexp, nullptr);
-  if (op->launch == dLAUNCH_PERSISTENT) DCHK(fp32 ? run_persistent<float>(op, A, s, grid) : run_persistent<double>(op, A, s, grid));
-  else DCHK(fp32 ? run_per_order<float>(op, A) : run_per_order<double>(op, A));
-  return fp32 ? fs_restrict32(fs, (const float *)yexp, y, 0) : fs_restrict(fs, (const double *)yexp, y, 0);
+  const HpArgs A = make_args(op, x, pi, yexp, nullptr);
+  if (op->launch == dLAUNCH_PERSISTENT) DCHK(persistent(A, s, grid));
+  else DCHK(pi == 1 ? run_per_order<float>(op, A) : pi == 2 ? run_per_order<ff>(op, A) : run_per_order<double>(op, A));
+  if (pi == 1) return fs_restrict32(fs, (const float *)yexp, y, 0);
+  if (pi == 2) return fs_restrict_ff(fs, (const ff *)yexp, y, 0);
+  return fs_restrict(fs, (const double *)yexp, y, 0);
 }
 
 extern "C" {

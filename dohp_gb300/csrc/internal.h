@@ -107,6 +107,8 @@ struct _p_dOperator {
   double *d_geo = nullptr;       // fp64 geometric factors per qpt
   float *d_geo32 = nullptr;      // fp32 copy
   void *d_geo16 = nullptr;       // bf16 copy (scalar kinds)
+  void *d_geoff = nullptr;       // float-float copy
+  void *d_yff = nullptr;         // float-float expanded output
   double *d_k = nullptr;         // coefficient per qpt
   double *d_stash = nullptr;     // p-Laplacian stash [nq][4]
   double *d_gbase = nullptr;     // p-Laplacian: {J^-1, w det J} per qpt (10, SoA per element)

@@ -171,7 +171,7 @@ dErr launch_diffusion_bf16(_p_dFS *fs, const double *x, const __nv_bfloat16 *geo
 
 template <int N, typename T>
 dErr launch_elasticity(_p_dFS *fs, const double *x, const T *geo, T lam, T mu, T *yexp) {
-  return launch_uniform<N, T, dOP_ELASTICITY>(fs, x, geo, lam, mu, yexp);
+  return launch_uniform<N, T, dOP_ELASTICITY>(fs, x, geo, (double)lam, (double)mu, yexp);
 }
 
 }  // namespace
@@ -218,6 +218,10 @@ dErr op_compute_geometry(_p_dOperator *op) {
   if (op->d_geo16) {
     cudaFree(op->d_geo16);
     op->d_geo16 = nullptr;
+  }
+  if (op->d_geoff) {
+    cudaFree(op->d_geoff);
+    op->d_geoff = nullptr;
   }
   op->geo_valid = true;
   op->geo_kind = mode;
@@ -330,6 +334,36 @@ static dErr op_mult_bf16(_p_dOperator *op, const double *x, double *y) {
   return fs_restrict32(fs, op->d_y32, y, 0);
 }
 
+__global__ void k_to_ff(int64_t n, const double *__restrict__ a, ff *__restrict__ b) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = ff(a[i]);
+}
+
+dErr fs_restrict_ff(_p_dFS *fs, const ff *x, double *g, int add);
+
+// float-float element arithmetic (geometric factors split into float pairs once), FP64 input and restriction
+static dErr op_mult_ff(_p_dOperator *op, const double *x, double *y) {
+  _p_dFS *fs = op->fs;
+  if (op->kind != dOP_DIFFUSION && op->kind != dOP_ELASTICITY && op->kind != dOP_PLAPLACE_JACOBIAN)
+    return set_error("float-float apply for operator kind %d not built", (int)op->kind);
+  if (op->svk_state) return set_error("float-float St. Venant-Kirchhoff Jacobian not built (use FP64)");
+  DCHK(op_compute_geometry(op));
+  const int64_t ng = fs->nq * (op->kind == dOP_ELASTICITY ? 10 : 6);
+  if (!op->d_geoff) {
+    CUCHK(cudaMalloc(&op->d_geoff, ng * sizeof(ff)));
+    k_to_ff<<<(unsigned)((ng + 255) / 256), 256, 0, fs->stream>>>(ng, op->d_geo, (ff *)op->d_geoff);
+    CUCHK(cudaGetLastError());
+  }
+  if (!op->d_yff) CUCHK(cudaMalloc(&op->d_yff, fs->nexp * fs->bs * sizeof(ff)));
+  const ff *geo = (const ff *)op->d_geoff;
+  ff *yexp = (ff *)op->d_yff;
+  if (op->kind == dOP_ELASTICITY)
+    DCHK(elasticity_apply_t<ff>(fs, x, geo, ff(op->lam), ff(op->mu), yexp));
+  else
+    DCHK(diffusion_apply_t<ff>(fs, x, geo, yexp));
+  return fs_restrict_ff(fs, yexp, y, 0);
+}
+
 dErr hp_mult(_p_dOperator *op, const double *x, double *y);
 
 dErr op_mult(_p_dOperator *op, const double *x, double *y) {
@@ -340,6 +374,7 @@ dErr op_mult(_p_dOperator *op, const double *x, double *y) {
     return set_error("St. Venant-Kirchhoff Jacobian needs a uniform-order space and the default launch");
   if (!fs->uniform || op->launch != dLAUNCH_DEFAULT) return hp_mult(op, x, y);
   if (op->prec == dPREC_FP32) return op_mult_fp32(op, x, y);
+  if (op->prec == dPREC_FF) return op_mult_ff(op, x, y);
   if (op->prec == dPREC_BF16) return op_mult_bf16(op, x, y);
   if (!op->d_yexp) CUCHK(cudaMalloc(&op->d_yexp, fs->nexp * fs->bs * sizeof(double)));
   DCHK(op_mult_expanded(op, x, op->d_yexp));

@@ -224,6 +224,10 @@ dErr plap_prepare(_p_dOperator *op) {
     cudaFree(op->d_geo16);
     op->d_geo16 = nullptr;
   }
+  if (op->d_geoff) {
+    cudaFree(op->d_geoff);
+    op->d_geoff = nullptr;
+  }
   return 0;
 }
 

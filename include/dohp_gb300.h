@@ -67,11 +67,12 @@ typedef enum {
   dOP_PLAPLACE_JACOBIAN = 1, /* EllipPointwiseJacobian with the residual stash (ellip.c:333-377) */
   dOP_ELASTICITY = 2      /* ElastPointwiseJacobian at F = I (src/fs/tests/elast.c:256-280), bs = 3 */
 } dOperatorKind;
-/* Arithmetic of an operator apply */
 /* arithmetic of operator applies and of the Chebyshev-Jacobi preconditioner: FP64; FP32 (factors, inputs and
  * arithmetic in FP32); BF16 (geometric factors, inputs, basis tables and Q1 values stored in BF16, FP32
- * arithmetic and accumulation; scalar uniform-order operators) */
-typedef enum { dPREC_FP64 = 0, dPREC_FP32 = 1, dPREC_BF16 = 2 } dPrecision;
+ * arithmetic and accumulation; scalar uniform-order operators); FF (float-float: each value a pair of FP32
+ * words, unit roundoff ~2^-48, FP32 exponent range; the apply's arithmetic on the FP32 pipe with FP64-class
+ * accuracy, FP64 input and restriction; operator applies only) */
+typedef enum { dPREC_FP64 = 0, dPREC_FP32 = 1, dPREC_BF16 = 2, dPREC_FF = 3 } dPrecision;
 /* Launch form of an operator apply: DEFAULT = one fused kernel for uniform-order spaces (per-order form for
  * hp spaces); PER_ORDER = one launch per order bucket; PERSISTENT = one launch over all buckets with a device
  * work counter; GRAPH = the persistent launch and the restriction replayed from a CUDA graph. */
