@@ -70,6 +70,8 @@ def parse():
     ap.add_argument("--learned-ne", type=int, default=64, help="elements per side of the learned-correction solve")
     ap.add_argument("--learned-epochs", type=int, default=8)
     ap.add_argument("--newton-ne", type=int, default=24, help="elements per side of the p-Laplacian Newton run")
+    ap.add_argument("--newton-pc", default="mg", choices=("mg", "cheb"),
+                    help="Newton linear solves: Q1 multigrid (default) or the single-level Chebyshev-Jacobi")
     return ap.parse_args()
 
 
@@ -343,14 +345,16 @@ def secondary_newton(args):
     ne, p, pe, eps = args.newton_ne, 6, 1.5, 1e-6
     fs = dg.FS((ne + 1,) * 3, degree=p, perturb=0.1, seed=1)
     b = torch.as_tensor(np.random.default_rng(0).uniform(-1, 1, fs.n), device="cuda")
+    mg = args.newton_pc == "mg"
     out = {"workload": "plaplace-newton-%d^3-p6: exponent 1.5, eps 1e-6 (the 48^3 shape with --newton-ne 48)" % ne,
            "dofs": fs.n, "rtol": 1e-8, "lin_rtol": 1e-3, "lin_maxit": 300,
-           "ksp": "FGMRES(30) + Chebyshev(3)-Jacobi on the Q1-embedded Jacobian, inexact steps at lin_maxit"}
+           "ksp": ("FGMRES(30) + Q1 multigrid V-cycle (Chebyshev(3)-Jacobi smoothing, FP64)" if mg else
+                   "FGMRES(30) + Chebyshev(3)-Jacobi on the Q1-embedded Jacobian") + ", inexact steps at lin_maxit"}
     runs = {}
     for name, prec in (("fp64", dg.dPREC_FP64), ("fp32", dg.dPREC_FP32), ("bf16", dg.dPREC_BF16)):
         op = fs.operator(dg.dOP_PLAPLACE_JACOBIAN)
         m = fs.matrix()
-        ksp = dg.KSP(op, m, ksp_type=dg.dKSP_FGMRES, inner_prec=prec, restart=30)
+        ksp = dg.KSP(op, m, ksp_type=dg.dKSP_FGMRES, inner_prec=prec, restart=30, pc=dg.dPC_MG_Q1 if mg else dg.dPC_CHEBYSHEV_Q1)
         u = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
         runs[name] = dict(op=op, m=m, ksp=ksp, u=u, wall=0.0, fnorm=[], its=[], done=False)
     # both runs advance one Newton step at a time so that every iterate can be compared
@@ -467,8 +471,32 @@ def secondary_learned(args):
         applies, rejects, active = ksp.stats()
         out[name] = {"its": its, "wall_s": wall, "true_rel_residual": float(torch.linalg.norm(b - r) / torch.linalg.norm(b)),
                      "correction_dropped": bool(rejects), "correction_active_at_end": active}
+    # the Q1 multigrid preconditioner on the same problem (no network): CG with FP64 applies, and FGMRES with
+    # FP32 inner applies; the V-cycle is FP64 in both
+    for name, ktype, prec in (("multigrid_cg_fp64", dg.dKSP_CG, dg.dPREC_FP64), ("multigrid_mixed_fp32", dg.dKSP_FGMRES, dg.dPREC_FP32)):
+        ksp = dg.KSP(op, m, ksp_type=ktype, inner_prec=prec, restart=30, pc=dg.dPC_MG_Q1)
+        x = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        try:
+            ksp.solve(b, x, rtol=1e-1, maxit=50)
+        except dg.DohpError:
+            pass
+        torch.cuda.synchronize()
+        setup = time.perf_counter() - t0
+        x.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        its, _ = ksp.solve(b, x, rtol=1e-8, maxit=2000)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        r = torch.empty_like(x)
+        op.mult(x, r)
+        out[name] = {"its": its, "wall_s": wall, "setup_and_first_solve_s": setup,
+                     "true_rel_residual": float(torch.linalg.norm(b - r) / torch.linalg.norm(b))}
     out["speedup_vs_plain_fp64"] = {k: out["plain_fp64"]["wall_s"] / out[k]["wall_s"]
-                                    for k in ("mixed_fp32", "mixed_bf16", "learned_mixed", "learned_bf16", "learned_fp64")}
+                                    for k in ("mixed_fp32", "mixed_bf16", "learned_mixed", "learned_bf16", "learned_fp64",
+                                              "multigrid_cg_fp64", "multigrid_mixed_fp32")}
     return out
 
 

@@ -22,7 +22,7 @@ dFSBSTATUS_DIRICHLET, dFSBSTATUS_WEAK = 1 << 16, 1 << 17
 dOP_DIFFUSION, dOP_PLAPLACE_JACOBIAN, dOP_ELASTICITY = 0, 1, 2
 dPREC_FP64, dPREC_FP32, dPREC_BF16, dPREC_FF = 0, 1, 2, 3
 dKSP_CG, dKSP_FGMRES = 0, 1
-dPC_NONE, dPC_JACOBI, dPC_CHEBYSHEV_Q1 = 0, 1, 2
+dPC_NONE, dPC_JACOBI, dPC_CHEBYSHEV_Q1, dPC_MG_Q1 = 0, 1, 2, 3
 
 _lib = None
 _vp = ctypes.c_void_p

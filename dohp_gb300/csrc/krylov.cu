@@ -344,7 +344,12 @@ struct _p_dKSP {
   dErr (*shell_pc)(void *ctx, const double *r, double *z) = nullptr;
   void *shell_ctx = nullptr;
   cudaStream_t shell_stream = 0;
+  void *mg = nullptr;  // dPC_MG_Q1 hierarchy (mg.cu)
 };
+
+dErr mg_build(_p_dMat *J, int degree, void **out);
+dErr mg_apply(void *m, const double *r, double *z, cudaStream_t s);
+void mg_destroy(void *m);
 
 static cudaStream_t kstream(const _p_dKSP *k) { return k->shell_mult ? k->shell_stream : k->op->fs->stream; }
 dErr op_mult_prec(_p_dOperator *op, const double *x, double *y, dPrecision prec);
@@ -408,6 +413,11 @@ static dErr pc_setup(_p_dKSP *k) {
   if (!k->pmat) return set_error("preconditioner needs the Q1 matrix");
   k_diag_inv<<<nb(n), 256, 0, s>>>(n, k->pmat->d_rowptr, k->pmat->d_col, k->pmat->d_val, k->d_dinv);
   CUCHK(cudaGetLastError());
+  if (k->pc == dPC_MG_Q1) {
+    mg_destroy(k->mg);
+    k->mg = nullptr;
+    DCHK(mg_build(k->pmat, k->cheb_degree, &k->mg));
+  }
   if (k->pc == dPC_CHEBYSHEV_Q1) {  // lambda_max(D^-1 A_q1) by 20 power steps from a seeded vector
     std::vector<double> h(n);
     uint64_t st = 12345;
@@ -491,6 +501,7 @@ static dErr pc_apply(_p_dKSP *k, const double *r, double *z) {
 static dErr pc_apply_plain(_p_dKSP *k, const double *r, double *z) {
   const int64_t n = k->n;
   cudaStream_t s = kstream(k);
+  if (k->pc == dPC_MG_Q1) return mg_apply(k->mg, r, z, s);  // FP64 V-cycle in every precision mode
   if (k->pc == dPC_CHEBYSHEV_Q1 && k->pc_prec != dPREC_FP64) return pc_apply_fp32(k, r, z);
   if (k->pc == dPC_NONE) {
     CUCHK(cudaMemcpyAsync(z, r, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -689,6 +700,7 @@ dErr dKSPDestroy(dKSP *ksp) {
   cudaFree(k->d_dinv32);
   cudaFree(k->d_val32);
   cudaFree(k->d_val16);
+  mg_destroy(k->mg);
   delete k;
   *ksp = nullptr;
   return 0;
@@ -708,6 +720,8 @@ dErr dKSPSetOptions(dKSP ksp, dInt cheb_degree, dPrecision pc_precision, dInt re
   }
   ksp->restart = restart;
   ksp->pc_ready = false;
+  mg_destroy(ksp->mg);
+  ksp->mg = nullptr;
   cudaFree(ksp->d_w32);
   cudaFree(ksp->d_dinv32);
   cudaFree(ksp->d_val32);

@@ -1,0 +1,468 @@
+// Geometric multigrid on the Q1-embedded lattice (dPC_MG_Q1): a V-cycle preconditioner for the Q1-embedded
+// matrix of a scalar uniform-order space on a block mesh.
+//
+// The Q1-embedded matrix couples each GLL node with its lattice neighbours only (27-point stencil on the
+// lattice of GLL nodes, (M p + 1) nodes per direction). The fine level is that matrix in lattice order, stored as
+// 27 coefficient arrays (no column indices); Dirichlet nodes are masked rows. Coarse levels halve the lattice in
+// every direction (L -> (L + 1) / 2, L odd) with trilinear prolongation P in index space and Galerkin operators
+// P^T A P, which stay 27-point. Smoothing is the project's Chebyshev-Jacobi (the same polynomial as the
+// single-level preconditioner, degree and [0.1, 1.1] lambda_max bounds from 20 power steps per level); the
+// coarsest level (at most 9 nodes per direction) is solved exactly with a dense inverse built on the host. Pre-
+// and post-smoothing use the same polynomial in D^-1 A, so the V-cycle is a symmetric fixed linear operator
+// (usable inside CG as well as FGMRES). Deterministic: every kernel writes its own outputs, the eigenvalue
+// estimates use the fixed-order reductions of the solver module.
+//
+// PETSc's PCMG / PCGAMG on the assembled Q1 matrix is what the reference's callers would select for this; the
+// method here is the textbook geometric V-cycle (Trottenberg, Oosterlee, Schueller, Multigrid, 2001, ch. 2).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "internal.h"
+
+using namespace dgb;
+
+dErr device_dot(int64_t n, const double *a, const double *b, double *part, double *out, cudaStream_t s);
+
+namespace {
+
+inline unsigned nbk(int64_t n) { return (unsigned)std::max<int64_t>((n + 255) / 256, 1); }
+
+__device__ __forceinline__ void lat_coord(int64_t i, int Ly, int Lz, int &x, int &y, int &z) {
+  z = (int)(i % Lz);
+  y = (int)((i / Lz) % Ly);
+  x = (int)(i / ((int64_t)Ly * Lz));
+}
+
+// CSR (natural dof order) -> stencil in lattice order; bad != 0 when a column is not a lattice neighbour
+__global__ void k_stencil_fill(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ col, const double *__restrict__ val,
+                               const int32_t *__restrict__ lat, int Ly, int Lz, int64_t nl, double *__restrict__ A, int *bad) {
+  const int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (d >= n) return;
+  const int64_t li = lat[d];
+  int ix, iy, iz;
+  lat_coord(li, Ly, Lz, ix, iy, iz);
+  for (int32_t k = rp[d]; k < rp[d + 1]; k++) {
+    int jx, jy, jz;
+    lat_coord(lat[col[k]], Ly, Lz, jx, jy, jz);
+    const int dx = jx - ix, dy = jy - iy, dz = jz - iz;
+    if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) {
+      atomicExch(bad, 1);
+      continue;
+    }
+    A[(int64_t)((dx + 1) * 9 + (dy + 1) * 3 + dz + 1) * nl + li] = val[k];
+  }
+}
+
+__global__ void k_dinv(int64_t n, const double *__restrict__ A, double *__restrict__ dinv) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double a = A[13 * n + i];
+  dinv[i] = a != 0 ? 1.0 / a : 0.0;
+}
+
+// y = A x (27-point stencil), or y = b - A x when b is given
+__global__ void k_stencil_mv(int Lx, int Ly, int Lz, const double *__restrict__ A, const double *__restrict__ x,
+                             const double *__restrict__ b, double *__restrict__ y) {
+  const int64_t n = (int64_t)Lx * Ly * Lz;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int ix, iy, iz;
+  lat_coord(i, Ly, Lz, ix, iy, iz);
+  double s = 0;
+#pragma unroll
+  for (int a = -1; a <= 1; a++)
+#pragma unroll
+    for (int c = -1; c <= 1; c++)
+#pragma unroll
+      for (int e = -1; e <= 1; e++) {
+        const int jx = ix + a, jy = iy + c, jz = iz + e;
+        if (jx < 0 || jx >= Lx || jy < 0 || jy >= Ly || jz < 0 || jz >= Lz) continue;
+        s += A[(int64_t)((a + 1) * 9 + (c + 1) * 3 + e + 1) * n + i] * x[i + ((int64_t)a * Ly + c) * Lz + e];
+      }
+  y[i] = b ? b[i] - s : s;
+}
+
+// Galerkin coarse operator: Ac(I, J) = sum_{i, j} P(i, I) Af(i, j) P(j, J), trilinear P in index space,
+// coarse nodes whose fine node 2I is masked are masked (rows and columns)
+__global__ void k_galerkin(int Fx, int Fy, int Fz, int Cx, int Cy, int Cz, const double *__restrict__ Af, double *__restrict__ Ac) {
+  const int64_t nc = (int64_t)Cx * Cy * Cz, nf = (int64_t)Fx * Fy * Fz;
+  const int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (I >= nc) return;
+  int Ix, Iy, Iz;
+  lat_coord(I, Cy, Cz, Ix, Iy, Iz);
+  auto fidx = [&](int x, int y, int z) { return ((int64_t)x * Fy + y) * Fz + z; };
+  auto masked_c = [&](int x, int y, int z) { return Af[13 * nf + fidx(2 * x, 2 * y, 2 * z)] == 0.0; };
+  double acc[27];
+#pragma unroll
+  for (int s = 0; s < 27; s++) acc[s] = 0;
+  if (!masked_c(Ix, Iy, Iz)) {
+    for (int ux = -1; ux <= 1; ux++)
+      for (int uy = -1; uy <= 1; uy++)
+        for (int uz = -1; uz <= 1; uz++) {
+          const int ix = 2 * Ix + ux, iy = 2 * Iy + uy, iz = 2 * Iz + uz;
+          if (ix < 0 || ix >= Fx || iy < 0 || iy >= Fy || iz < 0 || iz >= Fz) continue;
+          const double wi = (ux ? 0.5 : 1.0) * (uy ? 0.5 : 1.0) * (uz ? 0.5 : 1.0);
+          const int64_t i = fidx(ix, iy, iz);
+          for (int s = 0; s < 27; s++) {
+            const double a = Af[(int64_t)s * nf + i];
+            if (a == 0.0) continue;
+            const int jx = ix + s / 9 - 1, jy = iy + (s / 3) % 3 - 1, jz = iz + s % 3 - 1;
+            // coarse parents of j per direction: even -> one (weight 1), odd -> two (weight 1/2)
+            const int px0 = jx >> 1, px1 = (jx + 1) >> 1, py0 = jy >> 1, py1 = (jy + 1) >> 1, pz0 = jz >> 1, pz1 = (jz + 1) >> 1;
+            const double wx = (jx & 1) ? 0.5 : 1.0, wy = (jy & 1) ? 0.5 : 1.0, wz = (jz & 1) ? 0.5 : 1.0;
+            for (int qx = px0; qx <= px1; qx++)
+              for (int qy = py0; qy <= py1; qy++)
+                for (int qz = pz0; qz <= pz1; qz++) {
+                  if (qx >= Cx || qy >= Cy || qz >= Cz || masked_c(qx, qy, qz)) continue;
+                  const int dx = qx - Ix, dy = qy - Iy, dz = qz - Iz;
+                  acc[(dx + 1) * 9 + (dy + 1) * 3 + dz + 1] += wi * a * wx * wy * wz;
+                }
+          }
+        }
+  }
+#pragma unroll
+  for (int s = 0; s < 27; s++) Ac[(int64_t)s * nc + I] = acc[s];
+}
+
+// b_c = P^T r_f
+__global__ void k_restrict_lat(int Fx, int Fy, int Fz, int Cx, int Cy, int Cz, const double *__restrict__ rf, double *__restrict__ bc) {
+  const int64_t nc = (int64_t)Cx * Cy * Cz;
+  const int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (I >= nc) return;
+  int Ix, Iy, Iz;
+  lat_coord(I, Cy, Cz, Ix, Iy, Iz);
+  double s = 0;
+  for (int ux = -1; ux <= 1; ux++)
+    for (int uy = -1; uy <= 1; uy++)
+      for (int uz = -1; uz <= 1; uz++) {
+        const int ix = 2 * Ix + ux, iy = 2 * Iy + uy, iz = 2 * Iz + uz;
+        if (ix < 0 || ix >= Fx || iy < 0 || iy >= Fy || iz < 0 || iz >= Fz) continue;
+        s += (ux ? 0.5 : 1.0) * (uy ? 0.5 : 1.0) * (uz ? 0.5 : 1.0) * rf[((int64_t)ix * Fy + iy) * Fz + iz];
+      }
+  bc[I] = s;
+}
+
+// x_f += P x_c on unmasked fine nodes (masked coarse values are zero)
+__global__ void k_prolong_lat(int Fx, int Fy, int Fz, int Cy, int Cz, const double *__restrict__ dinvf, const double *__restrict__ xc,
+                              double *__restrict__ xf) {
+  const int64_t nf = (int64_t)Fx * Fy * Fz;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nf || dinvf[i] == 0.0) return;
+  int ix, iy, iz;
+  lat_coord(i, Fy, Fz, ix, iy, iz);
+  double s = 0;
+  for (int qx = ix >> 1; qx <= (ix + 1) >> 1; qx++)
+    for (int qy = iy >> 1; qy <= (iy + 1) >> 1; qy++)
+      for (int qz = iz >> 1; qz <= (iz + 1) >> 1; qz++)
+        s += ((ix & 1) ? 0.5 : 1.0) * ((iy & 1) ? 0.5 : 1.0) * ((iz & 1) ? 0.5 : 1.0) * xc[((int64_t)qx * Cy + qy) * Cz + qz];
+  xf[i] += s;
+}
+
+__global__ void k_cheb0(int64_t n, const double *dinv, const double *r, double inv_theta, double *d, double *z) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = dinv[i] * r[i] * inv_theta;
+  d[i] = v;
+  z[i] = v;
+}
+__global__ void k_chebk(int64_t n, const double *dinv, const double *r, const double *w, double c1, double c2, double *d, double *z) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = c1 * d[i] + c2 * dinv[i] * (r[i] - w[i]);
+  d[i] = v;
+  z[i] += v;
+}
+__global__ void k_add(int64_t n, const double *a, double *y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] += a[i];
+}
+__global__ void k_scale(int64_t n, const double *s, double *y) {  // y *= 1 / sqrt(*s)
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] /= sqrt(*s);
+}
+__global__ void k_mulv(int64_t n, const double *a, double *y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] *= a[i];
+}
+__global__ void k_scatter(int64_t n, const int32_t *lat, const double *r, double *b) {
+  const int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (d < n) b[lat[d]] = r[d];
+}
+__global__ void k_gather(int64_t n, const int32_t *lat, const double *x, double *z) {
+  const int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (d < n) z[d] = x[lat[d]];
+}
+// y = M x for the dense coarsest inverse (one block per row)
+__global__ void k_dense_mv(int64_t n, const double *__restrict__ M, const double *__restrict__ x, double *__restrict__ y) {
+  __shared__ double red[256];
+  const int64_t r = blockIdx.x;
+  double s = 0;
+  for (int64_t j = threadIdx.x; j < n; j += blockDim.x) s += M[r * n + j] * x[j];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) y[r] = red[0];
+}
+
+}  // namespace
+
+struct MGLevel {
+  int L[3];
+  int64_t n = 0;
+  double *A = nullptr, *dinv = nullptr;
+  double *x = nullptr, *b = nullptr, *r = nullptr, *d = nullptr, *w = nullptr, *e = nullptr;
+  double emin = 0, emax = 0;
+  double *dense = nullptr;  // coarsest: dense inverse (masked rows and columns zero)
+};
+
+struct MGData {
+  std::vector<MGLevel> lev;
+  int64_t n = 0;  // explicit dofs
+  int32_t *lat = nullptr;
+  int degree = 3;
+  double *part = nullptr, *s = nullptr;
+};
+
+static void mg_free(MGData *M) {
+  if (!M) return;
+  for (MGLevel &l : M->lev)
+    for (double *p : {l.A, l.dinv, l.x, l.b, l.r, l.d, l.w, l.e, l.dense}) cudaFree(p);
+  cudaFree(M->lat);
+  cudaFree(M->part);
+  cudaFree(M->s);
+  delete M;
+}
+
+void mg_destroy(void *m) { mg_free((MGData *)m); }
+
+// Chebyshev-Jacobi on one level from a zero guess: z = p(D^-1 A) D^-1 r
+static dErr level_cheb(MGData *M, MGLevel &l, const double *r, double *z, cudaStream_t s) {
+  const double theta = 0.5 * (l.emax + l.emin), delta = 0.5 * (l.emax - l.emin), sigma = theta / delta;
+  double rho = 1.0 / sigma;
+  k_cheb0<<<nbk(l.n), 256, 0, s>>>(l.n, l.dinv, r, 1.0 / theta, l.d, z);
+  for (int it = 1; it < M->degree; it++) {
+    k_stencil_mv<<<nbk(l.n), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.A, z, nullptr, l.w);
+    const double rho1 = 1.0 / (2.0 * sigma - rho);
+    k_chebk<<<nbk(l.n), 256, 0, s>>>(l.n, l.dinv, r, l.w, rho1 * rho, 2.0 * rho1 / delta, l.d, z);
+    rho = rho1;
+  }
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+// x = V(b) on level k (b and x are the level's own arrays)
+static dErr vcycle(MGData *M, size_t k, cudaStream_t s) {
+  MGLevel &l = M->lev[k];
+  if (k + 1 == M->lev.size()) {
+    k_dense_mv<<<(unsigned)l.n, 256, 0, s>>>(l.n, l.dense, l.b, l.x);
+    CUCHK(cudaGetLastError());
+    return 0;
+  }
+  MGLevel &c = M->lev[k + 1];
+  DCHK(level_cheb(M, l, l.b, l.x, s));                                                      // pre-smooth
+  k_stencil_mv<<<nbk(l.n), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.A, l.x, l.b, l.r);        // r = b - A x
+  k_restrict_lat<<<nbk(c.n), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], c.L[0], c.L[1], c.L[2], l.r, c.b);
+  DCHK(vcycle(M, k + 1, s));
+  k_prolong_lat<<<nbk(l.n), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], c.L[1], c.L[2], l.dinv, c.x, l.x);
+  k_stencil_mv<<<nbk(l.n), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.A, l.x, l.b, l.r);        // post-smooth:
+  DCHK(level_cheb(M, l, l.r, l.e, s));                                                      // e = p(D^-1 A) D^-1 r
+  k_add<<<nbk(l.n), 256, 0, s>>>(l.n, l.e, l.x);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+dErr mg_apply(void *m, const double *r, double *z, cudaStream_t s) {
+  MGData *M = (MGData *)m;
+  MGLevel &f = M->lev[0];
+  CUCHK(cudaMemsetAsync(f.b, 0, f.n * sizeof(double), s));
+  k_scatter<<<nbk(M->n), 256, 0, s>>>(M->n, M->lat, r, f.b);
+  DCHK(vcycle(M, 0, s));
+  k_gather<<<nbk(M->n), 256, 0, s>>>(M->n, M->lat, f.x, z);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+// lambda_max(D^-1 A) by 20 power steps from a seeded vector (masked nodes stay 0)
+static dErr level_eig(MGData *M, MGLevel &l, cudaStream_t s) {
+  std::vector<double> h(l.n);
+  uint64_t st = 12345;
+  for (int64_t i = 0; i < l.n; i++) {
+    uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    h[i] = (double)(z >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+  }
+  CUCHK(cudaMemcpyAsync(l.x, h.data(), l.n * sizeof(double), cudaMemcpyHostToDevice, s));
+  k_mulv<<<nbk(l.n), 256, 0, s>>>(l.n, l.dinv, l.x);  // zero on masked nodes (dinv = 0 there)
+  double lam = 1, nrm[2];
+  for (int it = 0; it < 20; it++) {
+    k_stencil_mv<<<nbk(l.n), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.A, l.x, nullptr, l.w);
+    k_mulv<<<nbk(l.n), 256, 0, s>>>(l.n, l.dinv, l.w);
+    DCHK(device_dot(l.n, l.w, l.w, M->part, M->s, s));
+    DCHK(device_dot(l.n, l.x, l.x, M->part, M->s + 1, s));
+    CUCHK(cudaMemcpyAsync(nrm, M->s, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CUCHK(cudaStreamSynchronize(s));
+    lam = sqrt(nrm[0] / nrm[1]);
+    CUCHK(cudaMemcpyAsync(l.x, l.w, l.n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    k_scale<<<nbk(l.n), 256, 0, s>>>(l.n, M->s, l.x);
+  }
+  l.emax = 1.1 * lam;
+  l.emin = 0.1 * lam;
+  return 0;
+}
+
+// dense inverse of the coarsest operator on its unmasked nodes (Gauss-Jordan with partial pivoting, host)
+static dErr coarsest_dense(MGLevel &l, cudaStream_t s) {
+  const int64_t n = l.n;
+  std::vector<double> A(27 * n);
+  CUCHK(cudaMemcpyAsync(A.data(), l.A, 27 * n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CUCHK(cudaStreamSynchronize(s));
+  std::vector<int64_t> act;
+  for (int64_t i = 0; i < n; i++)
+    if (A[13 * n + i] != 0) act.push_back(i);
+  const int64_t m = (int64_t)act.size();
+  std::vector<int64_t> pos(n, -1);
+  for (int64_t a = 0; a < m; a++) pos[act[a]] = a;
+  std::vector<double> D(m * 2 * m, 0.0);  // [A | I]
+  const int Ly = l.L[1], Lz = l.L[2];
+  for (int64_t a = 0; a < m; a++) {
+    const int64_t i = act[a];
+    const int ix = (int)(i / ((int64_t)Ly * Lz)), iy = (int)((i / Lz) % Ly), iz = (int)(i % Lz);
+    for (int sidx = 0; sidx < 27; sidx++) {
+      const double v = A[sidx * n + i];
+      if (v == 0) continue;
+      const int jx = ix + sidx / 9 - 1, jy = iy + (sidx / 3) % 3 - 1, jz = iz + sidx % 3 - 1;
+      const int64_t j = ((int64_t)jx * Ly + jy) * Lz + jz;
+      if (pos[j] < 0) return set_error("multigrid coarsest level couples to a masked node");
+      D[a * 2 * m + pos[j]] = v;
+    }
+    D[a * 2 * m + m + a] = 1.0;
+  }
+  for (int64_t c = 0; c < m; c++) {
+    int64_t p = c;
+    for (int64_t r = c + 1; r < m; r++)
+      if (fabs(D[r * 2 * m + c]) > fabs(D[p * 2 * m + c])) p = r;
+    if (D[p * 2 * m + c] == 0) return set_error("multigrid coarsest operator is singular");
+    if (p != c)
+      for (int64_t k = 0; k < 2 * m; k++) std::swap(D[p * 2 * m + k], D[c * 2 * m + k]);
+    const double inv = 1.0 / D[c * 2 * m + c];
+    for (int64_t k = 0; k < 2 * m; k++) D[c * 2 * m + k] *= inv;
+    for (int64_t r = 0; r < m; r++) {
+      if (r == c) continue;
+      const double f = D[r * 2 * m + c];
+      if (f == 0) continue;
+      for (int64_t k = 0; k < 2 * m; k++) D[r * 2 * m + k] -= f * D[c * 2 * m + k];
+    }
+  }
+  std::vector<double> Minv(n * n, 0.0);
+  for (int64_t a = 0; a < m; a++)
+    for (int64_t b = 0; b < m; b++) Minv[act[a] * n + act[b]] = D[a * 2 * m + m + b];
+  CUCHK(cudaMalloc(&l.dense, n * n * sizeof(double)));
+  CUCHK(cudaMemcpy(l.dense, Minv.data(), n * n * sizeof(double), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+static dErr level_alloc(MGLevel &l) {
+  l.n = (int64_t)l.L[0] * l.L[1] * l.L[2];
+  CUCHK(cudaMalloc(&l.A, 27 * l.n * sizeof(double)));
+  CUCHK(cudaMemset(l.A, 0, 27 * l.n * sizeof(double)));
+  for (double **p : {&l.dinv, &l.x, &l.b, &l.r, &l.d, &l.w, &l.e}) {
+    CUCHK(cudaMalloc(p, l.n * sizeof(double)));
+    CUCHK(cudaMemset(*p, 0, l.n * sizeof(double)));
+  }
+  return 0;
+}
+
+// build the hierarchy from the assembled Q1 matrix of a scalar uniform-order space on a block mesh
+dErr mg_build(_p_dMat *J, int degree, void **out) {
+  _p_dFS *fs = J->fs;
+  if (fs->bs != 1 || J->bs != 1) return set_error("Q1 multigrid needs a scalar space");
+  if (!fs->uniform) return set_error("Q1 multigrid needs a uniform-order space");
+  const _p_dMesh *mesh = fs->mesh;
+  const int p = fs->p, Mx = mesh->nx - 1, My = mesh->ny - 1, Mz = mesh->nz - 1;
+  const int L0[3] = {Mx * p + 1, My * p + 1, Mz * p + 1};
+  for (int d = 0; d < 3; d++)
+    if (L0[d] % 2 == 0 || L0[d] < 5) return set_error("Q1 multigrid needs an even number of GLL intervals (elements x degree) per direction");
+  cudaStream_t s = fs->stream;
+  MGData *M = new MGData();
+  M->degree = std::max(2, degree);
+  M->n = fs->n;
+  // lattice position of every explicit dof (element (ex, ey, ez) local node (a, b, c) -> (ex p + a, ...))
+  std::vector<int32_t> lat(fs->n, -1);
+  const int P = p + 1;
+  for (int64_t r = 0; r < fs->nelem; r++) {
+    const int ex = (int)(r / ((int64_t)My * Mz)), ey = (int)((r / Mz) % My), ez = (int)(r % Mz);
+    for (int a = 0; a < P; a++)
+      for (int b = 0; b < P; b++)
+        for (int c = 0; c < P; c++) {
+          const int32_t d = fs->emap[fs->xstart[r] + (a * P + b) * P + c];
+          if (d >= fs->n) continue;
+          const int32_t L = (int32_t)((((int64_t)ex * p + a) * L0[1] + (ey * p + b)) * L0[2] + ez * p + c);
+          if (lat[d] >= 0 && lat[d] != L) {
+            mg_free(M);
+            return set_error("dof %d sits at two lattice positions: the mesh is not a structured block", d);
+          }
+          lat[d] = L;
+        }
+  }
+  for (int64_t d = 0; d < fs->n; d++)
+    if (lat[d] < 0) {
+      mg_free(M);
+      return set_error("dof %lld has no lattice position", (long long)d);
+    }
+  CUCHK(cudaMalloc(&M->lat, std::max<int64_t>(fs->n, 1) * sizeof(int32_t)));
+  CUCHK(cudaMemcpy(M->lat, lat.data(), fs->n * sizeof(int32_t), cudaMemcpyHostToDevice));
+  CUCHK(cudaMalloc(&M->part, 1024 * sizeof(double)));
+  CUCHK(cudaMalloc(&M->s, 4 * sizeof(double)));
+  // levels
+  int L[3] = {L0[0], L0[1], L0[2]};
+  for (;;) {
+    MGLevel l;
+    for (int d = 0; d < 3; d++) l.L[d] = L[d];
+    dErr e = level_alloc(l);
+    M->lev.push_back(l);
+    if (e) {
+      mg_free(M);
+      return e;
+    }
+    if (std::max(L[0], std::max(L[1], L[2])) <= 9 || L[0] % 2 == 0 || L[1] % 2 == 0 || L[2] % 2 == 0) break;
+    for (int d = 0; d < 3; d++) L[d] = (L[d] + 1) / 2;
+  }
+  // fine operator from the CSR, then Galerkin coarse operators
+  MGLevel &f = M->lev[0];
+  int *bad;
+  CUCHK(cudaMalloc(&bad, sizeof(int)));
+  CUCHK(cudaMemsetAsync(bad, 0, sizeof(int), s));
+  k_stencil_fill<<<nbk(fs->n), 256, 0, s>>>(fs->n, J->d_rowptr, J->d_col, J->d_val, M->lat, f.L[1], f.L[2], f.n, f.A, bad);
+  int hbad = 0;
+  CUCHK(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CUCHK(cudaStreamSynchronize(s));
+  cudaFree(bad);
+  if (hbad) {
+    mg_free(M);
+    return set_error("Q1 matrix couples nodes that are not lattice neighbours");
+  }
+  for (size_t k = 0; k < M->lev.size(); k++) {
+    MGLevel &l = M->lev[k];
+    if (k > 0) {
+      const MGLevel &fl = M->lev[k - 1];
+      k_galerkin<<<(unsigned)((l.n + 127) / 128), 128, 0, s>>>(fl.L[0], fl.L[1], fl.L[2], l.L[0], l.L[1], l.L[2], fl.A, l.A);
+      CUCHK(cudaGetLastError());
+    }
+    k_dinv<<<nbk(l.n), 256, 0, s>>>(l.n, l.A, l.dinv);
+    CUCHK(cudaGetLastError());
+    dErr e = k + 1 < M->lev.size() ? level_eig(M, l, s) : coarsest_dense(l, s);
+    if (e) {
+      mg_free(M);
+      return e;
+    }
+  }
+  CUCHK(cudaStreamSynchronize(s));
+  *out = M;
+  return 0;
+}
