@@ -29,6 +29,7 @@ dErr op_compute_geometry(_p_dOperator *op);
 dErr fs_restrict(_p_dFS *fs, const double *x, double *g, int add);
 dErr fs_restrict32(_p_dFS *fs, const float *x, double *g, int add);
 dErr fs_restrict_ff(_p_dFS *fs, const ff *x, double *g, int add);
+dErr fs_restrict_ff_to(_p_dFS *fs, const ff *x, double *const *py, double *g, int add, cudaStream_t s);
 
 namespace {
 
@@ -484,7 +485,7 @@ dErr hp_mult(_p_dOperator *op, const double *x, double *y) {
         const unsigned nbk = (unsigned)((N + 255) / 256);
         double *const *py = (double *const *)(P->d_ptrs + 1);
         if (pi == 1) k_restrict_table<float><<<nbk, 256, 0, cs>>>(fs->n, fs->bs, fs->d_et_ptr, eti, etw, (const float *)yexp, py);
-        else if (pi == 2) k_restrict_table<ff><<<nbk, 256, 0, cs>>>(fs->n, fs->bs, fs->d_et_ptr, eti, etw, (const ff *)yexp, py);
+        else if (pi == 2) e = fs_restrict_ff_to(fs, (const ff *)yexp, py, nullptr, 0, cs);
         else k_restrict_table<double><<<nbk, 256, 0, cs>>>(fs->n, fs->bs, fs->d_et_ptr, eti, etw, (const double *)yexp, py);
       }
       cudaError_t ce = cudaStreamEndCapture(cs, &g);

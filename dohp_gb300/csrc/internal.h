@@ -91,6 +91,7 @@ struct _p_dFS {
   int32_t *d_et_ptr = nullptr, *d_et_idx = nullptr;  // E^T over closure nodes (ascending expanded index)
   int32_t *d_eptr = nullptr, *d_ecol = nullptr;       // E as CSR (hp spaces only)
   double *d_eval = nullptr, *d_et_w = nullptr;        // E values and E^T weights (hp spaces only)
+  void *d_et_wff = nullptr;                          // E^T weights as float pairs (hp spaces only)
   double *d_coords = nullptr;                        // [nelem][8][3]
   double *d_dcache = nullptr;                        // Dirichlet values [(nc-n)*bs]
   // per-degree basis tables on the device for FAST rules: [p] -> B, Dq (Q=P)
