@@ -26,9 +26,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 CONFIGS = {
-    "cfg2": dict(ne=32, kind="elasticity", hp=True, p=4, grf=False, label="hp-elasticity-32^3-p2..8 (configs[1])"),
-    "cfg4": dict(ne=64, kind="diffusion", hp=False, p=4, grf=True, label="poisson-lognormal-64^3-p4 (configs[3])"),
-    "cfg1": dict(ne=8, kind="diffusion", hp=False, p=4, grf=False, label="poisson-8^3-p4 (configs[0])"),
+    "cfg2": dict(ne=32, kind="elasticity", hp=True, p=4, grf=False, label="hp-elasticity-32^3-p2..8"),
+    "cfg4": dict(ne=64, kind="diffusion", hp=False, p=4, grf=True, label="poisson-lognormal-64^3-p4"),
+    "cfg1": dict(ne=8, kind="diffusion", hp=False, p=4, grf=False, label="poisson-8^3-p4"),
     # reduced cases of the same kernels for full ncu captures (inputs still above L2)
     "cfg2_16": dict(ne=16, kind="elasticity", hp=True, p=4, grf=False, label="hp-elasticity-16^3-p2..8"),
     "cfg4_32": dict(ne=32, kind="diffusion", hp=False, p=4, grf=True, label="poisson-lognormal-32^3-p4"),
@@ -283,8 +283,18 @@ def time_loop(fn, steps, stream):
     return t0.elapsed_time(t1) / steps, per[len(per) // 2]
 
 
+# (kind, hp, p) -> (DRAM bytes per element per launch of the dominant kernel, where the figure comes from)
+NCU_DRAM_BYTES_PER_ELEMENT = {
+    ("elasticity", True, 4): (231.705600e6 / 4096, "ncu, k_hp_persistent<double,elasticity>, 16^3 elements: 212.5 MB read + 19.2 MB "
+                                                   "written per launch, scaled by elements"),
+    ("diffusion", False, 4): (253.2e6 / 32768, "ncu, k_uniform<5,double,diffusion>, 32^3 elements: 229.7 MB read + 23.5 MB written "
+                                               "per launch, scaled by elements"),
+}
+
+
 def work_per_apply(fs, cfg, bs):
-    """SURVEY 8(d) algorithmic bytes and flops per apply, and the flops the element kernels issue."""
+    """Algorithmic bytes and flops per apply (x and y once, the int32 element map and 8 vertex coordinates per
+    element; 36 n^4 + 30 n^3 flops per element and component), and the flops the element kernels issue."""
     import numpy as np
     deg = fs.elem_degree()[:, 0].astype(np.float64)
     n1 = deg + 1
@@ -421,7 +431,7 @@ def secondary_learned(args):
         m.assemble(grf=grf)
         return fs, op, m, grf
 
-    out = {"workload": "lognormal-poisson-%d^3-p4 (configs[4] on the configs[3] problem)" % ne, "rtol": 1e-8,
+    out = {"workload": "lognormal-poisson-%d^3-p4, learned correction and multigrid" % ne, "rtol": 1e-8,
            "ksp": "FGMRES(30), Chebyshev(3)-Jacobi on the Q1-embedded matrix",
            "network": "3-level U-Net 16/32/64 ch, 3^3 kernels, BF16 weights, FP32 accumulate, on the vertex lattice"}
     fs0, _, _, _ = problem(1000)
@@ -582,6 +592,13 @@ def main():
 
     hbm, src = peaks()
     alg_bytes, alg_flops, issued = work_per_apply(fs, cfg, bs)
+    # DRAM bytes per launch of the dominant kernel from one ncu capture (dram__bytes_read.sum +
+    # dram__bytes_write.sum) on a smaller case of the same workload, scaled by elements (the traffic is geometry,
+    # E map, input and expanded output, all proportional to the element count)
+    per_elem = NCU_DRAM_BYTES_PER_ELEMENT.get((cfg["kind"], cfg["hp"], cfg["p"]))
+    traffic = per_elem[0] * fs.nelem if per_elem else None
+    traffic_src = per_elem[1] if per_elem else "no capture for this workload"
+
     achieved = alg_bytes / (kms * 1e-3) / 1e9
     value = whole_job_gdofs(world, N, ms_step * 1e-3)
     line = {
@@ -592,7 +609,8 @@ def main():
                    "orders": "i.i.d. U{2..8}, seed 2" if cfg["hp"] else "p=%d" % cfg["p"], "quadrature": "Gauss (p+1)^3",
                    "launch": "persistent kernel + restriction in a CUDA graph" if cfg["hp"] else "fused element kernel + restriction",
                    "l2": "inputs larger than L2, no flush", "parallelism": "replicas" if world > 1 else "single GPU"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "traffic_source": traffic_src,
                      "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)", "kernel": kernel_name, "kernel_ms_median": kms,
                      "alg_bytes_per_launch": alg_bytes},
         "fp64_roofline": {"bound": "fp64 pipe", "achieved": issued / (kms * 1e-3) / 1e9, "peak": FP64_PEAK_GFLOPS,
@@ -620,7 +638,7 @@ def main():
             line["newton_mixed_precision"] = secondary_newton(args)
             torch.cuda.empty_cache()
     if not args.no_secondary and args.config == "cfg2":
-        line["time_to_rtol_cfg1"] = {"workload": "poisson-8^3-p4 (configs[0]), mass right-hand side, CG + Q1 Chebyshev(3)-Jacobi, rtol 1e-8",
+        line["time_to_rtol_cfg1"] = {"workload": "poisson-8^3-p4, mass right-hand side, CG + Q1 Chebyshev(3)-Jacobi, rtol 1e-8",
                                      "gpu": gpu_time_to_rtol_cfg1()}
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(cfg, os.cpu_count() or 1)

@@ -9,7 +9,7 @@
 //   B:  -int q div u                                                 (StokesPointwiseJacobian_B, stokes.c:496-499)
 //   coupled [A Bt; B 0] without the penalty                          (StokesPointwiseJacobian, stokes.c:476-487)
 // with Du the symmetric gradient in [00, 11, 22, 01, 02, 12] storage (dTensorSymCompress3, include/dohp.h:79-82).
-// This build covers the Newtonian rheology (exponent p = 2: eta = B, the store's eta' = 0); the power-law store
+// This file covers the Newtonian rheology (exponent p = 2: eta = B, the store's eta' = 0); the power-law store
 // is refused with an error.
 //
 // One fused kernel per element group does all of it: velocity gather through E, B and Dq passes per component,

@@ -1,6 +1,6 @@
 /* CPU oracle for dohp's matrix-free hp-FEM operator path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the GPU product (dohp_gb300). Only the tests, the smoke
+ * TEST INFRASTRUCTURE ONLY: the oracle the GPU product (dohp_gb300) is tested against. Only the tests, the smoke
  * check and the CPU-baseline leg of the benchmark load this library. Each function restates the
  * algorithm of the dohp source lines it cites; comments name the file:line (relative to the dohp
  * project root). Written from the algorithm, not copied: loops, names and data layout are our own

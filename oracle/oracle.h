@@ -1,6 +1,6 @@
 /* CPU oracle for the matrix-free hp-FEM operator path of dohp.
  *
- * TEST INFRASTRUCTURE ONLY. This library is the checker: the parity tests, the
+ * TEST INFRASTRUCTURE ONLY. This library is the oracle: the parity tests, the
  * smoke check and the CPU-baseline leg of the benchmark call it. The product
  * library (dohp_gb300) never links, loads or calls it.
  *

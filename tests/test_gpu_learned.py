@@ -173,7 +173,7 @@ def test_learned_correction_reduces_fgmres_iterations(trained):
 
 
 def test_fallback_to_plain_preconditioner(trained):
-    """a network that makes things worse is dropped by the restart judge; non-finite values are dropped"""
+    """a network that makes things worse is dropped by the restart test; non-finite values are dropped"""
     net, _, ne = trained
     fs, op, m, grf = lognormal(ne, 98)
     b = dev(np.random.default_rng(98).uniform(-1, 1, fs.n))

@@ -1,5 +1,5 @@
 """GPU parity: the product's CUDA path (through the C ABI) against the CPU oracle on identical seeded
-meshes and fields. Integer maps bit-exact; FP64 applies within 1e-12 relative (spec tolerance)."""
+meshes and fields. Integer maps bit-exact; FP64 applies within 1e-12 relative."""
 import numpy as np
 import pytest
 
