@@ -34,39 +34,53 @@ __device__ __forceinline__ void lat_coord(int64_t i, int Ly, int Lz, int &x, int
   x = (int)(i / ((int64_t)Ly * Lz));
 }
 
-// CSR (natural dof order) -> stencil in lattice order; bad != 0 when a column is not a lattice neighbour
-__global__ void k_stencil_fill(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ col, const double *__restrict__ val,
+// CSR (natural dof order, BS interleaved components per node) -> block stencil in lattice order:
+// A[((s BS + ci) BS + cj) nl + node]; bad != 0 when a column is not a lattice neighbour
+template <int BS>
+__global__ void k_stencil_fill(int64_t nrows, const int32_t *__restrict__ rp, const int32_t *__restrict__ col, const double *__restrict__ val,
                                const int32_t *__restrict__ lat, int Ly, int Lz, int64_t nl, double *__restrict__ A, int *bad) {
-  const int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (d >= n) return;
-  const int64_t li = lat[d];
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const int64_t li = lat[r / BS];
+  const int ci = (int)(r % BS);
   int ix, iy, iz;
   lat_coord(li, Ly, Lz, ix, iy, iz);
-  for (int32_t k = rp[d]; k < rp[d + 1]; k++) {
+  for (int32_t k = rp[r]; k < rp[r + 1]; k++) {
     int jx, jy, jz;
-    lat_coord(lat[col[k]], Ly, Lz, jx, jy, jz);
+    lat_coord(lat[col[k] / BS], Ly, Lz, jx, jy, jz);
+    const int cj = col[k] % BS;
     const int dx = jx - ix, dy = jy - iy, dz = jz - iz;
     if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) {
       atomicExch(bad, 1);
       continue;
     }
-    A[(int64_t)((dx + 1) * 9 + (dy + 1) * 3 + dz + 1) * nl + li] = val[k];
+    const int s = (dx + 1) * 9 + (dy + 1) * 3 + dz + 1;
+    A[((int64_t)(s * BS + ci) * BS + cj) * nl + li] = val[k];
   }
 }
 
-__global__ void k_dinv(int64_t n, const double *__restrict__ A, double *__restrict__ dinv) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double a = A[13 * n + i];
-  dinv[i] = a != 0 ? 1.0 / a : 0.0;
+template <int BS>
+__device__ __forceinline__ double center(const double *A, int64_t n, int64_t i, int c) {
+  return A[((int64_t)(13 * BS + c) * BS + c) * n + i];
 }
 
-// y = A x (27-point stencil), or y = b - A x when b is given
+template <int BS>
+__global__ void k_dinv(int64_t n, const double *__restrict__ A, double *__restrict__ dinv) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= n * BS) return;
+  const double a = center<BS>(A, n, t / BS, (int)(t % BS));
+  dinv[t] = a != 0 ? 1.0 / a : 0.0;
+}
+
+// y = A x (27-point block stencil), or y = b - A x when b is given; one thread per (node, component)
+template <int BS>
 __global__ void k_stencil_mv(int Lx, int Ly, int Lz, const double *__restrict__ A, const double *__restrict__ x,
                              const double *__restrict__ b, double *__restrict__ y) {
   const int64_t n = (int64_t)Lx * Ly * Lz;
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= n * BS) return;
+  const int64_t i = t / BS;
+  const int ci = (int)(t % BS);
   int ix, iy, iz;
   lat_coord(i, Ly, Lz, ix, iy, iz);
   double s = 0;
@@ -78,21 +92,28 @@ __global__ void k_stencil_mv(int Lx, int Ly, int Lz, const double *__restrict__ 
       for (int e = -1; e <= 1; e++) {
         const int jx = ix + a, jy = iy + c, jz = iz + e;
         if (jx < 0 || jx >= Lx || jy < 0 || jy >= Ly || jz < 0 || jz >= Lz) continue;
-        s += A[(int64_t)((a + 1) * 9 + (c + 1) * 3 + e + 1) * n + i] * x[i + ((int64_t)a * Ly + c) * Lz + e];
+        const int st = (a + 1) * 9 + (c + 1) * 3 + e + 1;
+        const int64_t j = i + ((int64_t)a * Ly + c) * Lz + e;
+#pragma unroll
+        for (int cj = 0; cj < BS; cj++) s += A[((int64_t)(st * BS + ci) * BS + cj) * n + i] * x[j * BS + cj];
       }
-  y[i] = b ? b[i] - s : s;
+  y[t] = b ? b[t] - s : s;
 }
 
-// Galerkin coarse operator: Ac(I, J) = sum_{i, j} P(i, I) Af(i, j) P(j, J), trilinear P in index space,
-// coarse nodes whose fine node 2I is masked are masked (rows and columns)
+// Galerkin coarse operator: Ac(I, J) = sum_{i, j} P(i, I) Af(i, j) P(j, J) block by block, trilinear P in index
+// space (the same for every component), coarse nodes whose fine node 2I is masked are masked (rows and
+// columns); one thread per (coarse node, block entry)
+template <int BS>
 __global__ void k_galerkin(int Fx, int Fy, int Fz, int Cx, int Cy, int Cz, const double *__restrict__ Af, double *__restrict__ Ac) {
   const int64_t nc = (int64_t)Cx * Cy * Cz, nf = (int64_t)Fx * Fy * Fz;
-  const int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (I >= nc) return;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nc * BS * BS) return;
+  const int64_t I = t / (BS * BS);
+  const int ci = (int)((t / BS) % BS), cj = (int)(t % BS);
   int Ix, Iy, Iz;
   lat_coord(I, Cy, Cz, Ix, Iy, Iz);
   auto fidx = [&](int x, int y, int z) { return ((int64_t)x * Fy + y) * Fz + z; };
-  auto masked_c = [&](int x, int y, int z) { return Af[13 * nf + fidx(2 * x, 2 * y, 2 * z)] == 0.0; };
+  auto masked_c = [&](int x, int y, int z) { return center<BS>(Af, nf, fidx(2 * x, 2 * y, 2 * z), 0) == 0.0; };
   double acc[27];
 #pragma unroll
   for (int s = 0; s < 27; s++) acc[s] = 0;
@@ -105,7 +126,7 @@ __global__ void k_galerkin(int Fx, int Fy, int Fz, int Cx, int Cy, int Cz, const
           const double wi = (ux ? 0.5 : 1.0) * (uy ? 0.5 : 1.0) * (uz ? 0.5 : 1.0);
           const int64_t i = fidx(ix, iy, iz);
           for (int s = 0; s < 27; s++) {
-            const double a = Af[(int64_t)s * nf + i];
+            const double a = Af[((int64_t)(s * BS + ci) * BS + cj) * nf + i];
             if (a == 0.0) continue;
             const int jx = ix + s / 9 - 1, jy = iy + (s / 3) % 3 - 1, jz = iz + s % 3 - 1;
             // coarse parents of j per direction: even -> one (weight 1), odd -> two (weight 1/2)
@@ -122,14 +143,17 @@ __global__ void k_galerkin(int Fx, int Fy, int Fz, int Cx, int Cy, int Cz, const
         }
   }
 #pragma unroll
-  for (int s = 0; s < 27; s++) Ac[(int64_t)s * nc + I] = acc[s];
+  for (int s = 0; s < 27; s++) Ac[((int64_t)(s * BS + ci) * BS + cj) * nc + I] = acc[s];
 }
 
-// b_c = P^T r_f
+// b_c = P^T r_f, per component
+template <int BS>
 __global__ void k_restrict_lat(int Fx, int Fy, int Fz, int Cx, int Cy, int Cz, const double *__restrict__ rf, double *__restrict__ bc) {
   const int64_t nc = (int64_t)Cx * Cy * Cz;
-  const int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (I >= nc) return;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nc * BS) return;
+  const int64_t I = t / BS;
+  const int c = (int)(t % BS);
   int Ix, Iy, Iz;
   lat_coord(I, Cy, Cz, Ix, Iy, Iz);
   double s = 0;
@@ -138,25 +162,28 @@ __global__ void k_restrict_lat(int Fx, int Fy, int Fz, int Cx, int Cy, int Cz, c
       for (int uz = -1; uz <= 1; uz++) {
         const int ix = 2 * Ix + ux, iy = 2 * Iy + uy, iz = 2 * Iz + uz;
         if (ix < 0 || ix >= Fx || iy < 0 || iy >= Fy || iz < 0 || iz >= Fz) continue;
-        s += (ux ? 0.5 : 1.0) * (uy ? 0.5 : 1.0) * (uz ? 0.5 : 1.0) * rf[((int64_t)ix * Fy + iy) * Fz + iz];
+        s += (ux ? 0.5 : 1.0) * (uy ? 0.5 : 1.0) * (uz ? 0.5 : 1.0) * rf[(((int64_t)ix * Fy + iy) * Fz + iz) * BS + c];
       }
-  bc[I] = s;
+  bc[t] = s;
 }
 
-// x_f += P x_c on unmasked fine nodes (masked coarse values are zero)
+// x_f += P x_c on unmasked fine unknowns (masked coarse values are zero)
+template <int BS>
 __global__ void k_prolong_lat(int Fx, int Fy, int Fz, int Cy, int Cz, const double *__restrict__ dinvf, const double *__restrict__ xc,
                               double *__restrict__ xf) {
   const int64_t nf = (int64_t)Fx * Fy * Fz;
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= nf || dinvf[i] == 0.0) return;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nf * BS || dinvf[t] == 0.0) return;
+  const int64_t i = t / BS;
+  const int c = (int)(t % BS);
   int ix, iy, iz;
   lat_coord(i, Fy, Fz, ix, iy, iz);
   double s = 0;
   for (int qx = ix >> 1; qx <= (ix + 1) >> 1; qx++)
     for (int qy = iy >> 1; qy <= (iy + 1) >> 1; qy++)
       for (int qz = iz >> 1; qz <= (iz + 1) >> 1; qz++)
-        s += ((ix & 1) ? 0.5 : 1.0) * ((iy & 1) ? 0.5 : 1.0) * ((iz & 1) ? 0.5 : 1.0) * xc[((int64_t)qx * Cy + qy) * Cz + qz];
-  xf[i] += s;
+        s += ((ix & 1) ? 0.5 : 1.0) * ((iy & 1) ? 0.5 : 1.0) * ((iz & 1) ? 0.5 : 1.0) * xc[(((int64_t)qx * Cy + qy) * Cz + qz) * BS + c];
+  xf[t] += s;
 }
 
 __global__ void k_cheb0(int64_t n, const double *dinv, const double *r, double inv_theta, double *d, double *z) {
@@ -185,13 +212,14 @@ __global__ void k_mulv(int64_t n, const double *a, double *y) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) y[i] *= a[i];
 }
-__global__ void k_scatter(int64_t n, const int32_t *lat, const double *r, double *b) {
-  const int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (d < n) b[lat[d]] = r[d];
+// natural (node, component) <-> lattice (node, component)
+__global__ void k_scatter(int64_t n, int bs, const int32_t *lat, const double *r, double *b) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t < n * bs) b[(int64_t)lat[t / bs] * bs + t % bs] = r[t];
 }
-__global__ void k_gather(int64_t n, const int32_t *lat, const double *x, double *z) {
-  const int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (d < n) z[d] = x[lat[d]];
+__global__ void k_gather(int64_t n, int bs, const int32_t *lat, const double *x, double *z) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t < n * bs) z[t] = x[(int64_t)lat[t / bs] * bs + t % bs];
 }
 // y = M x for the dense coarsest inverse (one block per row)
 __global__ void k_dense_mv(int64_t n, const double *__restrict__ M, const double *__restrict__ x, double *__restrict__ y) {
@@ -212,7 +240,7 @@ __global__ void k_dense_mv(int64_t n, const double *__restrict__ M, const double
 
 struct MGLevel {
   int L[3];
-  int64_t n = 0;
+  int64_t n = 0;  // lattice nodes (vectors hold n * bs values)
   double *A = nullptr, *dinv = nullptr;
   double *x = nullptr, *b = nullptr, *r = nullptr, *d = nullptr, *w = nullptr, *e = nullptr;
   double emin = 0, emax = 0;
@@ -221,7 +249,8 @@ struct MGLevel {
 
 struct MGData {
   std::vector<MGLevel> lev;
-  int64_t n = 0;  // explicit dofs
+  int bs = 1;
+  int64_t n = 0;  // explicit nodes
   int32_t *lat = nullptr;
   int degree = 3;
   double *part = nullptr, *s = nullptr;
@@ -239,15 +268,22 @@ static void mg_free(MGData *M) {
 
 void mg_destroy(void *m) { mg_free((MGData *)m); }
 
+static void stencil_mv(int bs, const MGLevel &l, const double *x, const double *b, double *y, cudaStream_t s) {
+  const unsigned g = nbk(l.n * bs);
+  if (bs == 3) k_stencil_mv<3><<<g, 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.A, x, b, y);
+  else k_stencil_mv<1><<<g, 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.A, x, b, y);
+}
+
 // Chebyshev-Jacobi on one level from a zero guess: z = p(D^-1 A) D^-1 r
 static dErr level_cheb(MGData *M, MGLevel &l, const double *r, double *z, cudaStream_t s) {
+  const int64_t nv = l.n * M->bs;
   const double theta = 0.5 * (l.emax + l.emin), delta = 0.5 * (l.emax - l.emin), sigma = theta / delta;
   double rho = 1.0 / sigma;
-  k_cheb0<<<nbk(l.n), 256, 0, s>>>(l.n, l.dinv, r, 1.0 / theta, l.d, z);
+  k_cheb0<<<nbk(nv), 256, 0, s>>>(nv, l.dinv, r, 1.0 / theta, l.d, z);
   for (int it = 1; it < M->degree; it++) {
-    k_stencil_mv<<<nbk(l.n), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.A, z, nullptr, l.w);
+    stencil_mv(M->bs, l, z, nullptr, l.w, s);
     const double rho1 = 1.0 / (2.0 * sigma - rho);
-    k_chebk<<<nbk(l.n), 256, 0, s>>>(l.n, l.dinv, r, l.w, rho1 * rho, 2.0 * rho1 / delta, l.d, z);
+    k_chebk<<<nbk(nv), 256, 0, s>>>(nv, l.dinv, r, l.w, rho1 * rho, 2.0 * rho1 / delta, l.d, z);
     rho = rho1;
   }
   CUCHK(cudaGetLastError());
@@ -257,20 +293,24 @@ static dErr level_cheb(MGData *M, MGLevel &l, const double *r, double *z, cudaSt
 // x = V(b) on level k (b and x are the level's own arrays)
 static dErr vcycle(MGData *M, size_t k, cudaStream_t s) {
   MGLevel &l = M->lev[k];
+  const int bs = M->bs;
+  const int64_t nv = l.n * bs;
   if (k + 1 == M->lev.size()) {
-    k_dense_mv<<<(unsigned)l.n, 256, 0, s>>>(l.n, l.dense, l.b, l.x);
+    k_dense_mv<<<(unsigned)nv, 256, 0, s>>>(nv, l.dense, l.b, l.x);
     CUCHK(cudaGetLastError());
     return 0;
   }
   MGLevel &c = M->lev[k + 1];
-  DCHK(level_cheb(M, l, l.b, l.x, s));                                                      // pre-smooth
-  k_stencil_mv<<<nbk(l.n), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.A, l.x, l.b, l.r);        // r = b - A x
-  k_restrict_lat<<<nbk(c.n), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], c.L[0], c.L[1], c.L[2], l.r, c.b);
+  DCHK(level_cheb(M, l, l.b, l.x, s));  // pre-smooth
+  stencil_mv(bs, l, l.x, l.b, l.r, s);  // r = b - A x
+  if (bs == 3) k_restrict_lat<3><<<nbk(c.n * 3), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], c.L[0], c.L[1], c.L[2], l.r, c.b);
+  else k_restrict_lat<1><<<nbk(c.n), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], c.L[0], c.L[1], c.L[2], l.r, c.b);
   DCHK(vcycle(M, k + 1, s));
-  k_prolong_lat<<<nbk(l.n), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], c.L[1], c.L[2], l.dinv, c.x, l.x);
-  k_stencil_mv<<<nbk(l.n), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.A, l.x, l.b, l.r);        // post-smooth:
-  DCHK(level_cheb(M, l, l.r, l.e, s));                                                      // e = p(D^-1 A) D^-1 r
-  k_add<<<nbk(l.n), 256, 0, s>>>(l.n, l.e, l.x);
+  if (bs == 3) k_prolong_lat<3><<<nbk(nv), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], c.L[1], c.L[2], l.dinv, c.x, l.x);
+  else k_prolong_lat<1><<<nbk(nv), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], c.L[1], c.L[2], l.dinv, c.x, l.x);
+  stencil_mv(bs, l, l.x, l.b, l.r, s);  // post-smooth: e = p(D^-1 A) D^-1 (b - A x), x += e
+  DCHK(level_cheb(M, l, l.r, l.e, s));
+  k_add<<<nbk(nv), 256, 0, s>>>(nv, l.e, l.x);
   CUCHK(cudaGetLastError());
   return 0;
 }
@@ -278,69 +318,73 @@ static dErr vcycle(MGData *M, size_t k, cudaStream_t s) {
 dErr mg_apply(void *m, const double *r, double *z, cudaStream_t s) {
   MGData *M = (MGData *)m;
   MGLevel &f = M->lev[0];
-  CUCHK(cudaMemsetAsync(f.b, 0, f.n * sizeof(double), s));
-  k_scatter<<<nbk(M->n), 256, 0, s>>>(M->n, M->lat, r, f.b);
+  CUCHK(cudaMemsetAsync(f.b, 0, f.n * M->bs * sizeof(double), s));
+  k_scatter<<<nbk(M->n * M->bs), 256, 0, s>>>(M->n, M->bs, M->lat, r, f.b);
   DCHK(vcycle(M, 0, s));
-  k_gather<<<nbk(M->n), 256, 0, s>>>(M->n, M->lat, f.x, z);
+  k_gather<<<nbk(M->n * M->bs), 256, 0, s>>>(M->n, M->bs, M->lat, f.x, z);
   CUCHK(cudaGetLastError());
   return 0;
 }
 
-// lambda_max(D^-1 A) by 20 power steps from a seeded vector (masked nodes stay 0)
+// lambda_max(D^-1 A) by 20 power steps from a seeded vector (masked unknowns stay 0)
 static dErr level_eig(MGData *M, MGLevel &l, cudaStream_t s) {
-  std::vector<double> h(l.n);
+  const int64_t nv = l.n * M->bs;
+  std::vector<double> h(nv);
   uint64_t st = 12345;
-  for (int64_t i = 0; i < l.n; i++) {
+  for (int64_t i = 0; i < nv; i++) {
     uint64_t z = (st += 0x9E3779B97F4A7C15ull);
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
     z ^= z >> 31;
     h[i] = (double)(z >> 11) * (1.0 / 9007199254740992.0) - 0.5;
   }
-  CUCHK(cudaMemcpyAsync(l.x, h.data(), l.n * sizeof(double), cudaMemcpyHostToDevice, s));
-  k_mulv<<<nbk(l.n), 256, 0, s>>>(l.n, l.dinv, l.x);  // zero on masked nodes (dinv = 0 there)
+  CUCHK(cudaMemcpyAsync(l.x, h.data(), nv * sizeof(double), cudaMemcpyHostToDevice, s));
+  k_mulv<<<nbk(nv), 256, 0, s>>>(nv, l.dinv, l.x);  // zero on masked unknowns (dinv = 0 there)
   double lam = 1, nrm[2];
   for (int it = 0; it < 20; it++) {
-    k_stencil_mv<<<nbk(l.n), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.A, l.x, nullptr, l.w);
-    k_mulv<<<nbk(l.n), 256, 0, s>>>(l.n, l.dinv, l.w);
-    DCHK(device_dot(l.n, l.w, l.w, M->part, M->s, s));
-    DCHK(device_dot(l.n, l.x, l.x, M->part, M->s + 1, s));
+    stencil_mv(M->bs, l, l.x, nullptr, l.w, s);
+    k_mulv<<<nbk(nv), 256, 0, s>>>(nv, l.dinv, l.w);
+    DCHK(device_dot(nv, l.w, l.w, M->part, M->s, s));
+    DCHK(device_dot(nv, l.x, l.x, M->part, M->s + 1, s));
     CUCHK(cudaMemcpyAsync(nrm, M->s, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
     CUCHK(cudaStreamSynchronize(s));
     lam = sqrt(nrm[0] / nrm[1]);
-    CUCHK(cudaMemcpyAsync(l.x, l.w, l.n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    k_scale<<<nbk(l.n), 256, 0, s>>>(l.n, M->s, l.x);
+    CUCHK(cudaMemcpyAsync(l.x, l.w, nv * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    k_scale<<<nbk(nv), 256, 0, s>>>(nv, M->s, l.x);
   }
   l.emax = 1.1 * lam;
   l.emin = 0.1 * lam;
   return 0;
 }
 
-// dense inverse of the coarsest operator on its unmasked nodes (Gauss-Jordan with partial pivoting, host)
-static dErr coarsest_dense(MGLevel &l, cudaStream_t s) {
-  const int64_t n = l.n;
-  std::vector<double> A(27 * n);
-  CUCHK(cudaMemcpyAsync(A.data(), l.A, 27 * n * sizeof(double), cudaMemcpyDeviceToHost, s));
+// dense inverse of the coarsest operator on its unmasked unknowns (Gauss-Jordan with partial pivoting, host)
+static dErr coarsest_dense(MGLevel &l, int bs, cudaStream_t s) {
+  const int64_t n = l.n, nv = n * bs;
+  std::vector<double> A(27 * bs * bs * n);
+  CUCHK(cudaMemcpyAsync(A.data(), l.A, A.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
   CUCHK(cudaStreamSynchronize(s));
-  std::vector<int64_t> act;
+  auto coef = [&](int st, int ci, int cj, int64_t i) { return A[((int64_t)(st * bs + ci) * bs + cj) * n + i]; };
+  std::vector<int64_t> act, pos(nv, -1);
   for (int64_t i = 0; i < n; i++)
-    if (A[13 * n + i] != 0) act.push_back(i);
+    if (coef(13, 0, 0, i) != 0)
+      for (int c = 0; c < bs; c++) act.push_back(i * bs + c);
   const int64_t m = (int64_t)act.size();
-  std::vector<int64_t> pos(n, -1);
   for (int64_t a = 0; a < m; a++) pos[act[a]] = a;
   std::vector<double> D(m * 2 * m, 0.0);  // [A | I]
   const int Ly = l.L[1], Lz = l.L[2];
   for (int64_t a = 0; a < m; a++) {
-    const int64_t i = act[a];
+    const int64_t i = act[a] / bs;
+    const int ci = (int)(act[a] % bs);
     const int ix = (int)(i / ((int64_t)Ly * Lz)), iy = (int)((i / Lz) % Ly), iz = (int)(i % Lz);
-    for (int sidx = 0; sidx < 27; sidx++) {
-      const double v = A[sidx * n + i];
-      if (v == 0) continue;
-      const int jx = ix + sidx / 9 - 1, jy = iy + (sidx / 3) % 3 - 1, jz = iz + sidx % 3 - 1;
-      const int64_t j = ((int64_t)jx * Ly + jy) * Lz + jz;
-      if (pos[j] < 0) return set_error("multigrid coarsest level couples to a masked node");
-      D[a * 2 * m + pos[j]] = v;
-    }
+    for (int st = 0; st < 27; st++)
+      for (int cj = 0; cj < bs; cj++) {
+        const double v = coef(st, ci, cj, i);
+        if (v == 0) continue;
+        const int jx = ix + st / 9 - 1, jy = iy + (st / 3) % 3 - 1, jz = iz + st % 3 - 1;
+        const int64_t j = (((int64_t)jx * Ly + jy) * Lz + jz) * bs + cj;
+        if (pos[j] < 0) return set_error("multigrid coarsest level couples to a masked node");
+        D[a * 2 * m + pos[j]] = v;
+      }
     D[a * 2 * m + m + a] = 1.0;
   }
   for (int64_t c = 0; c < m; c++) {
@@ -359,29 +403,32 @@ static dErr coarsest_dense(MGLevel &l, cudaStream_t s) {
       for (int64_t k = 0; k < 2 * m; k++) D[r * 2 * m + k] -= f * D[c * 2 * m + k];
     }
   }
-  std::vector<double> Minv(n * n, 0.0);
+  std::vector<double> Minv(nv * nv, 0.0);
   for (int64_t a = 0; a < m; a++)
-    for (int64_t b = 0; b < m; b++) Minv[act[a] * n + act[b]] = D[a * 2 * m + m + b];
-  CUCHK(cudaMalloc(&l.dense, n * n * sizeof(double)));
-  CUCHK(cudaMemcpy(l.dense, Minv.data(), n * n * sizeof(double), cudaMemcpyHostToDevice));
+    for (int64_t b = 0; b < m; b++) Minv[act[a] * nv + act[b]] = D[a * 2 * m + m + b];
+  CUCHK(cudaMalloc(&l.dense, nv * nv * sizeof(double)));
+  CUCHK(cudaMemcpy(l.dense, Minv.data(), nv * nv * sizeof(double), cudaMemcpyHostToDevice));
   return 0;
 }
 
-static dErr level_alloc(MGLevel &l) {
+static dErr level_alloc(MGLevel &l, int bs) {
   l.n = (int64_t)l.L[0] * l.L[1] * l.L[2];
-  CUCHK(cudaMalloc(&l.A, 27 * l.n * sizeof(double)));
-  CUCHK(cudaMemset(l.A, 0, 27 * l.n * sizeof(double)));
+  const int64_t nv = l.n * bs;
+  CUCHK(cudaMalloc(&l.A, 27 * bs * nv * sizeof(double)));
+  CUCHK(cudaMemset(l.A, 0, 27 * bs * nv * sizeof(double)));
   for (double **p : {&l.dinv, &l.x, &l.b, &l.r, &l.d, &l.w, &l.e}) {
-    CUCHK(cudaMalloc(p, l.n * sizeof(double)));
-    CUCHK(cudaMemset(*p, 0, l.n * sizeof(double)));
+    CUCHK(cudaMalloc(p, nv * sizeof(double)));
+    CUCHK(cudaMemset(*p, 0, nv * sizeof(double)));
   }
   return 0;
 }
 
-// build the hierarchy from the assembled Q1 matrix of a scalar uniform-order space on a block mesh
+// build the hierarchy from the assembled Q1 matrix (scalar, or the interleaved 3 x 3 blocked elasticity matrix)
+// of a uniform-order space on a block mesh
 dErr mg_build(_p_dMat *J, int degree, void **out) {
   _p_dFS *fs = J->fs;
-  if (fs->bs != 1 || J->bs != 1) return set_error("Q1 multigrid needs a scalar space");
+  const int bs = J->bs;
+  if (bs != 1 && bs != 3) return set_error("Q1 multigrid: block size %d", bs);
   if (!fs->uniform) return set_error("Q1 multigrid needs a uniform-order space");
   const _p_dMesh *mesh = fs->mesh;
   const int p = fs->p, Mx = mesh->nx - 1, My = mesh->ny - 1, Mz = mesh->nz - 1;
@@ -390,9 +437,10 @@ dErr mg_build(_p_dMat *J, int degree, void **out) {
     if (L0[d] % 2 == 0 || L0[d] < 5) return set_error("Q1 multigrid needs an even number of GLL intervals (elements x degree) per direction");
   cudaStream_t s = fs->stream;
   MGData *M = new MGData();
+  M->bs = bs;
   M->degree = std::max(2, degree);
   M->n = fs->n;
-  // lattice position of every explicit dof (element (ex, ey, ez) local node (a, b, c) -> (ex p + a, ...))
+  // lattice position of every explicit node (element (ex, ey, ez) local node (a, b, c) -> (ex p + a, ...))
   std::vector<int32_t> lat(fs->n, -1);
   const int P = p + 1;
   for (int64_t r = 0; r < fs->nelem; r++) {
@@ -419,26 +467,34 @@ dErr mg_build(_p_dMat *J, int degree, void **out) {
   CUCHK(cudaMemcpy(M->lat, lat.data(), fs->n * sizeof(int32_t), cudaMemcpyHostToDevice));
   CUCHK(cudaMalloc(&M->part, 1024 * sizeof(double)));
   CUCHK(cudaMalloc(&M->s, 4 * sizeof(double)));
-  // levels
+  // levels: halve until the coarsest is small enough for a dense inverse (9 nodes per direction for scalar
+  // matrices, 5 for blocked ones)
+  const int stop = bs == 1 ? 9 : 5;
   int L[3] = {L0[0], L0[1], L0[2]};
   for (;;) {
     MGLevel l;
     for (int d = 0; d < 3; d++) l.L[d] = L[d];
-    dErr e = level_alloc(l);
+    dErr e = level_alloc(l, bs);
     M->lev.push_back(l);
     if (e) {
       mg_free(M);
       return e;
     }
-    if (std::max(L[0], std::max(L[1], L[2])) <= 9 || L[0] % 2 == 0 || L[1] % 2 == 0 || L[2] % 2 == 0) break;
+    if (std::max(L[0], std::max(L[1], L[2])) <= stop || L[0] % 2 == 0 || L[1] % 2 == 0 || L[2] % 2 == 0) break;
     for (int d = 0; d < 3; d++) L[d] = (L[d] + 1) / 2;
+  }
+  if ((int64_t)M->lev.back().n * bs > 4096) {
+    mg_free(M);
+    return set_error("Q1 multigrid: the coarsest lattice is too large for a dense solve");
   }
   // fine operator from the CSR, then Galerkin coarse operators
   MGLevel &f = M->lev[0];
   int *bad;
   CUCHK(cudaMalloc(&bad, sizeof(int)));
   CUCHK(cudaMemsetAsync(bad, 0, sizeof(int), s));
-  k_stencil_fill<<<nbk(fs->n), 256, 0, s>>>(fs->n, J->d_rowptr, J->d_col, J->d_val, M->lat, f.L[1], f.L[2], f.n, f.A, bad);
+  const int64_t nrows = fs->n * bs;
+  if (bs == 3) k_stencil_fill<3><<<nbk(nrows), 256, 0, s>>>(nrows, J->d_rowptr, J->d_col, J->d_val, M->lat, f.L[1], f.L[2], f.n, f.A, bad);
+  else k_stencil_fill<1><<<nbk(nrows), 256, 0, s>>>(nrows, J->d_rowptr, J->d_col, J->d_val, M->lat, f.L[1], f.L[2], f.n, f.A, bad);
   int hbad = 0;
   CUCHK(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
   CUCHK(cudaStreamSynchronize(s));
@@ -451,12 +507,15 @@ dErr mg_build(_p_dMat *J, int degree, void **out) {
     MGLevel &l = M->lev[k];
     if (k > 0) {
       const MGLevel &fl = M->lev[k - 1];
-      k_galerkin<<<(unsigned)((l.n + 127) / 128), 128, 0, s>>>(fl.L[0], fl.L[1], fl.L[2], l.L[0], l.L[1], l.L[2], fl.A, l.A);
+      const int64_t nt = l.n * bs * bs;
+      if (bs == 3) k_galerkin<3><<<(unsigned)((nt + 127) / 128), 128, 0, s>>>(fl.L[0], fl.L[1], fl.L[2], l.L[0], l.L[1], l.L[2], fl.A, l.A);
+      else k_galerkin<1><<<(unsigned)((nt + 127) / 128), 128, 0, s>>>(fl.L[0], fl.L[1], fl.L[2], l.L[0], l.L[1], l.L[2], fl.A, l.A);
       CUCHK(cudaGetLastError());
     }
-    k_dinv<<<nbk(l.n), 256, 0, s>>>(l.n, l.A, l.dinv);
+    if (bs == 3) k_dinv<3><<<nbk(l.n * 3), 256, 0, s>>>(l.n, l.A, l.dinv);
+    else k_dinv<1><<<nbk(l.n), 256, 0, s>>>(l.n, l.A, l.dinv);
     CUCHK(cudaGetLastError());
-    dErr e = k + 1 < M->lev.size() ? level_eig(M, l, s) : coarsest_dense(l, s);
+    dErr e = k + 1 < M->lev.size() ? level_eig(M, l, s) : coarsest_dense(l, bs, s);
     if (e) {
       mg_free(M);
       return e;

@@ -22,8 +22,9 @@
 // stokes.c:367-505, 675-799): right-preconditioned FGMRES on the packed vector [u; p] with the block upper
 // triangular preconditioner
 //   z_p = -eta diag(M_p)^-1 r_p  (mean removed: the constant pressure is the null space with Dirichlet walls),
-//   z_u = Cheb-Jacobi(A_q1) (r_u - Bt z_p),
-// A_q1 the blocked Q1-embedded matrix of the A block (the elasticity assembly with 2 mu = eta, lambda as A).
+//   z_u = M_u (r_u - Bt z_p),
+// A_q1 the blocked Q1-embedded matrix of the A block (the elasticity assembly with 2 mu = eta, lambda as A) and
+// M_u one Q1 multigrid V-cycle on it (Chebyshev-Jacobi alone where the GLL lattice does not coarsen).
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -429,7 +430,12 @@ dErr dStokesSolve(dStokes stk, const dScalar *bu, const dScalar *bp, dScalar *xu
     DCHK(dFSCreateOperator(fu, dOP_ELASTICITY, nullptr, &S->opu));
     DCHK(dFSCreateMatrix(fu, &S->Ap));
     DCHK(q1_numeric_elast(fu, S->Ap, S->lam, 0.5 * S->B, 1));
-    DCHK(dKSPCreate(S->opu, S->Ap, dKSP_CG, dPC_CHEBYSHEV_Q1, &S->kspu));
+    // the velocity block's approximate inverse: one Q1 multigrid V-cycle where the GLL lattice coarsens (an even
+    // number of GLL intervals per direction), else the single-level Chebyshev-Jacobi
+    const _p_dMesh *mesh = fu->mesh;
+    const bool lattice = ((mesh->nx - 1) * fu->p) % 2 == 0 && ((mesh->ny - 1) * fu->p) % 2 == 0 && ((mesh->nz - 1) * fu->p) % 2 == 0 &&
+                         (mesh->nx - 1) * fu->p >= 4 && (mesh->ny - 1) * fu->p >= 4 && (mesh->nz - 1) * fu->p >= 4;
+    DCHK(dKSPCreate(S->opu, S->Ap, dKSP_CG, lattice ? dPC_MG_Q1 : dPC_CHEBYSHEV_Q1, &S->kspu));
     DCHK(ksp_create_shell(S->nu3 + S->np, s, dKSP_FGMRES, stokes_shell_mult, stokes_shell_pc, S, S->restart, &S->ksp));
   }
   const int64_t n = S->nu3 + S->np;
