@@ -66,7 +66,7 @@ def parse():
     ap.add_argument("--config", default="cfg2", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
-    ap.add_argument("--secondary", default="all", help="comma list of apply,learned,newton (or all)")
+    ap.add_argument("--secondary", default="all", help="comma list of apply,learned,newton,multigrid (or all: apply, learned (which includes the multigrid solves), newton)")
     ap.add_argument("--learned-ne", type=int, default=64, help="elements per side of the learned-correction solve")
     ap.add_argument("--learned-epochs", type=int, default=8)
     ap.add_argument("--newton-ne", type=int, default=24, help="elements per side of the p-Laplacian Newton run")
@@ -410,6 +410,57 @@ def secondary_newton(args):
     return out
 
 
+def multigrid_solves(fs, op, m, b):
+    """the Q1 multigrid preconditioner on a lognormal problem (no network): CG with FP64 applies, and FGMRES with
+    FP32 inner applies; the V-cycle is FP64 in both. Set-up (hierarchy, eigenvalue estimates) is timed apart."""
+    import torch
+    import dohp_gb300 as dg
+    out = {}
+    for name, ktype, prec in (("multigrid_cg_fp64", dg.dKSP_CG, dg.dPREC_FP64), ("multigrid_mixed_fp32", dg.dKSP_FGMRES, dg.dPREC_FP32)):
+        ksp = dg.KSP(op, m, ksp_type=ktype, inner_prec=prec, restart=30, pc=dg.dPC_MG_Q1)
+        x = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        try:
+            ksp.solve(b, x, rtol=1e-1, maxit=50)
+        except dg.DohpError:
+            pass
+        torch.cuda.synchronize()
+        setup = time.perf_counter() - t0
+        x.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        its, _ = ksp.solve(b, x, rtol=1e-8, maxit=2000)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        r = torch.empty_like(x)
+        op.mult(x, r)
+        out[name] = {"its": its, "wall_s": wall, "setup_and_first_solve_s": setup,
+                     "true_rel_residual": float(torch.linalg.norm(b - r) / torch.linalg.norm(b))}
+    return out
+
+
+def secondary_multigrid(args):
+    """the multigrid solves alone on the time-to-rtol problem (lognormal Poisson, p=4, --learned-ne elements
+    per side, fresh field seed 5000)"""
+    import numpy as np
+    import torch
+    import dohp_gb300 as dg
+    ne = args.learned_ne
+    fs = dg.FS((ne + 1,) * 3, degree=4, perturb=0.1, seed=1)
+    grf = dg.grf_create(64, 2.0, 0.1, 5000)
+    kq = torch.empty(fs.nq, dtype=torch.float64, device="cuda")
+    fs.lognormal(grf, kq)
+    op = fs.operator()
+    op.set_qdata(kq)
+    m = fs.matrix()
+    m.assemble(grf=grf)
+    b = torch.as_tensor(np.random.default_rng(5000).uniform(-1, 1, fs.n), device="cuda")
+    out = {"workload": "lognormal-poisson-%d^3-p4, Q1 multigrid" % ne, "dofs": fs.n, "rtol": 1e-8}
+    out.update(multigrid_solves(fs, op, m, b))
+    return out
+
+
 def secondary_learned(args):
     """Lognormal Poisson (64^3, p=4, ~16.6 M dofs), time to rtol 1e-8 on a fresh field: FGMRES(30) with the
     Q1 Chebyshev(3)-Jacobi preconditioner in FP64 (plain), with FP32 inner applies (mixed), and with the
@@ -481,29 +532,7 @@ def secondary_learned(args):
         applies, rejects, active = ksp.stats()
         out[name] = {"its": its, "wall_s": wall, "true_rel_residual": float(torch.linalg.norm(b - r) / torch.linalg.norm(b)),
                      "correction_dropped": bool(rejects), "correction_active_at_end": active}
-    # the Q1 multigrid preconditioner on the same problem (no network): CG with FP64 applies, and FGMRES with
-    # FP32 inner applies; the V-cycle is FP64 in both
-    for name, ktype, prec in (("multigrid_cg_fp64", dg.dKSP_CG, dg.dPREC_FP64), ("multigrid_mixed_fp32", dg.dKSP_FGMRES, dg.dPREC_FP32)):
-        ksp = dg.KSP(op, m, ksp_type=ktype, inner_prec=prec, restart=30, pc=dg.dPC_MG_Q1)
-        x = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        try:
-            ksp.solve(b, x, rtol=1e-1, maxit=50)
-        except dg.DohpError:
-            pass
-        torch.cuda.synchronize()
-        setup = time.perf_counter() - t0
-        x.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        its, _ = ksp.solve(b, x, rtol=1e-8, maxit=2000)
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-        r = torch.empty_like(x)
-        op.mult(x, r)
-        out[name] = {"its": its, "wall_s": wall, "setup_and_first_solve_s": setup,
-                     "true_rel_residual": float(torch.linalg.norm(b - r) / torch.linalg.norm(b))}
+    out.update(multigrid_solves(fs, op, m, b))
     out["speedup_vs_plain_fp64"] = {k: out["plain_fp64"]["wall_s"] / out[k]["wall_s"]
                                     for k in ("mixed_fp32", "mixed_bf16", "learned_mixed", "learned_bf16", "learned_fp64",
                                               "multigrid_cg_fp64", "multigrid_mixed_fp32")}
@@ -629,6 +658,8 @@ def main():
         del fs, op, x, y, yexp
         torch.cuda.empty_cache()
         which = {"apply", "learned", "newton"} if args.secondary == "all" else set(args.secondary.split(","))
+        if "multigrid" in which:
+            line["multigrid"] = secondary_multigrid(args)
         if "apply" in which:
             line["secondary"] = secondary_cfg4(args)
         if "learned" in which:

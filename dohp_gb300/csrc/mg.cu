@@ -100,6 +100,45 @@ __global__ void k_stencil_mv(int Lx, int Ly, int Lz, const double *__restrict__ 
   y[t] = b ? b[t] - s : s;
 }
 
+// the symmetric half of a level's stencil: the centre and the 13 forward neighbours (stencil slots 13..26);
+// A(i, i - o) is the transpose of A(i - o, i), which node i - o holds as a forward entry
+template <int BS>
+__global__ void k_sym_extract(int64_t n, const double *__restrict__ A, double *__restrict__ As) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= 14 * BS * BS * n) return;
+  As[t] = A[13 * BS * BS * n + t];
+}
+
+// y = A x (or b - A x) from the symmetric half: forward entries of node i, transposed forward entries of the
+// backward neighbours; about half the coefficient bytes of the full stencil
+template <int BS>
+__global__ void k_stencil_mv_sym(int Lx, int Ly, int Lz, const double *__restrict__ As, const double *__restrict__ x,
+                                 const double *__restrict__ b, double *__restrict__ y) {
+  const int64_t n = (int64_t)Lx * Ly * Lz;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= n * BS) return;
+  const int64_t i = t / BS;
+  const int ci = (int)(t % BS);
+  int ix, iy, iz;
+  lat_coord(i, Ly, Lz, ix, iy, iz);
+  double s = 0;
+#pragma unroll
+  for (int cj = 0; cj < BS; cj++) s += As[((int64_t)ci * BS + cj) * n + i] * x[i * BS + cj];
+#pragma unroll
+  for (int h = 1; h < 14; h++) {
+    const int st = 13 + h, a = st / 9 - 1, c = (st / 3) % 3 - 1, e = st % 3 - 1;
+    const int64_t o = ((int64_t)a * Ly + c) * Lz + e;
+    const int fx = ix + a, fy = iy + c, fz = iz + e, bx = ix - a, by = iy - c, bz = iz - e;
+    if (fx >= 0 && fx < Lx && fy >= 0 && fy < Ly && fz >= 0 && fz < Lz)
+#pragma unroll
+      for (int cj = 0; cj < BS; cj++) s += As[((int64_t)(h * BS + ci) * BS + cj) * n + i] * x[(i + o) * BS + cj];
+    if (bx >= 0 && bx < Lx && by >= 0 && by < Ly && bz >= 0 && bz < Lz)
+#pragma unroll
+      for (int cj = 0; cj < BS; cj++) s += As[((int64_t)(h * BS + cj) * BS + ci) * n + (i - o)] * x[(i - o) * BS + cj];
+  }
+  y[t] = b ? b[t] - s : s;
+}
+
 // Galerkin coarse operator: Ac(I, J) = sum_{i, j} P(i, I) Af(i, j) P(j, J) block by block, trilinear P in index
 // space (the same for every component), coarse nodes whose fine node 2I is masked are masked (rows and
 // columns); one thread per (coarse node, block entry)
@@ -241,7 +280,8 @@ __global__ void k_dense_mv(int64_t n, const double *__restrict__ M, const double
 struct MGLevel {
   int L[3];
   int64_t n = 0;  // lattice nodes (vectors hold n * bs values)
-  double *A = nullptr, *dinv = nullptr;
+  double *A = nullptr, *dinv = nullptr;  // full 27-entry stencil (set-up only) and Jacobi
+  double *As = nullptr;                   // symmetric half (14 entries) used by the cycle
   double *x = nullptr, *b = nullptr, *r = nullptr, *d = nullptr, *w = nullptr, *e = nullptr;
   double emin = 0, emax = 0;
   double *dense = nullptr;  // coarsest: dense inverse (masked rows and columns zero)
@@ -259,7 +299,7 @@ struct MGData {
 static void mg_free(MGData *M) {
   if (!M) return;
   for (MGLevel &l : M->lev)
-    for (double *p : {l.A, l.dinv, l.x, l.b, l.r, l.d, l.w, l.e, l.dense}) cudaFree(p);
+    for (double *p : {l.A, l.As, l.dinv, l.x, l.b, l.r, l.d, l.w, l.e, l.dense}) cudaFree(p);
   cudaFree(M->lat);
   cudaFree(M->part);
   cudaFree(M->s);
@@ -270,6 +310,11 @@ void mg_destroy(void *m) { mg_free((MGData *)m); }
 
 static void stencil_mv(int bs, const MGLevel &l, const double *x, const double *b, double *y, cudaStream_t s) {
   const unsigned g = nbk(l.n * bs);
+  if (l.As) {
+    if (bs == 3) k_stencil_mv_sym<3><<<g, 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.As, x, b, y);
+    else k_stencil_mv_sym<1><<<g, 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.As, x, b, y);
+    return;
+  }
   if (bs == 3) k_stencil_mv<3><<<g, 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.A, x, b, y);
   else k_stencil_mv<1><<<g, 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.A, x, b, y);
 }
@@ -515,6 +560,13 @@ dErr mg_build(_p_dMat *J, int degree, void **out) {
     if (bs == 3) k_dinv<3><<<nbk(l.n * 3), 256, 0, s>>>(l.n, l.A, l.dinv);
     else k_dinv<1><<<nbk(l.n), 256, 0, s>>>(l.n, l.A, l.dinv);
     CUCHK(cudaGetLastError());
+    if (k + 1 < M->lev.size()) {  // the cycle runs on the symmetric half
+      const int64_t ns = 14 * bs * bs * l.n;
+      CUCHK(cudaMalloc(&l.As, ns * sizeof(double)));
+      if (bs == 3) k_sym_extract<3><<<nbk(ns), 256, 0, s>>>(l.n, l.A, l.As);
+      else k_sym_extract<1><<<nbk(ns), 256, 0, s>>>(l.n, l.A, l.As);
+      CUCHK(cudaGetLastError());
+    }
     dErr e = k + 1 < M->lev.size() ? level_eig(M, l, s) : coarsest_dense(l, bs, s);
     if (e) {
       mg_free(M);
@@ -522,6 +574,10 @@ dErr mg_build(_p_dMat *J, int degree, void **out) {
     }
   }
   CUCHK(cudaStreamSynchronize(s));
+  for (MGLevel &l : M->lev) {  // the full stencils were needed for the Galerkin products and the dense solve only
+    cudaFree(l.A);
+    l.A = nullptr;
+  }
   *out = M;
   return 0;
 }
