@@ -347,7 +347,7 @@ struct _p_dKSP {
   void *mg = nullptr;  // dPC_MG_Q1 hierarchy (mg.cu)
 };
 
-dErr mg_build(_p_dMat *J, int degree, void **out);
+dErr mg_build(_p_dMat *J, int degree, bool fp32, void **out);
 dErr mg_apply(void *m, const double *r, double *z, cudaStream_t s);
 void mg_destroy(void *m);
 
@@ -418,7 +418,7 @@ static dErr pc_setup(_p_dKSP *k) {
     k->mg = nullptr;
     // smoothing one degree below the single-level Chebyshev (2 at the default 3): measured at 64^3, p=4, the
     // same iteration count as degree 3 for 20 % less time per solve
-    DCHK(mg_build(k->pmat, std::max(2, k->cheb_degree - 1), &k->mg));
+    DCHK(mg_build(k->pmat, std::max(2, k->cheb_degree - 1), k->pc_prec != dPREC_FP64, &k->mg));
   }
   if (k->pc == dPC_CHEBYSHEV_Q1) {  // lambda_max(D^-1 A_q1) by 20 power steps from a seeded vector
     std::vector<double> h(n);
@@ -503,7 +503,7 @@ static dErr pc_apply(_p_dKSP *k, const double *r, double *z) {
 static dErr pc_apply_plain(_p_dKSP *k, const double *r, double *z) {
   const int64_t n = k->n;
   cudaStream_t s = kstream(k);
-  if (k->pc == dPC_MG_Q1) return mg_apply(k->mg, r, z, s);  // FP64 V-cycle in every precision mode
+  if (k->pc == dPC_MG_Q1) return mg_apply(k->mg, r, z, s);  // FP64 V-cycle, or FP32 for FP32 / BF16 preconditioning
   if (k->pc == dPC_CHEBYSHEV_Q1 && k->pc_prec != dPREC_FP64) return pc_apply_fp32(k, r, z);
   if (k->pc == dPC_NONE) {
     CUCHK(cudaMemcpyAsync(z, r, n * sizeof(double), cudaMemcpyDeviceToDevice, s));

@@ -111,9 +111,9 @@ __global__ void k_sym_extract(int64_t n, const double *__restrict__ A, double *_
 
 // y = A x (or b - A x) from the symmetric half: forward entries of node i, transposed forward entries of the
 // backward neighbours; about half the coefficient bytes of the full stencil
-template <int BS>
-__global__ void k_stencil_mv_sym(int Lx, int Ly, int Lz, const double *__restrict__ As, const double *__restrict__ x,
-                                 const double *__restrict__ b, double *__restrict__ y) {
+template <int BS, typename T>
+__global__ void k_stencil_mv_sym(int Lx, int Ly, int Lz, const T *__restrict__ As, const T *__restrict__ x,
+                                 const T *__restrict__ b, T *__restrict__ y) {
   const int64_t n = (int64_t)Lx * Ly * Lz;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= n * BS) return;
@@ -121,7 +121,7 @@ __global__ void k_stencil_mv_sym(int Lx, int Ly, int Lz, const double *__restric
   const int ci = (int)(t % BS);
   int ix, iy, iz;
   lat_coord(i, Ly, Lz, ix, iy, iz);
-  double s = 0;
+  T s = 0;
 #pragma unroll
   for (int cj = 0; cj < BS; cj++) s += As[((int64_t)ci * BS + cj) * n + i] * x[i * BS + cj];
 #pragma unroll
@@ -186,8 +186,8 @@ __global__ void k_galerkin(int Fx, int Fy, int Fz, int Cx, int Cy, int Cz, const
 }
 
 // b_c = P^T r_f, per component
-template <int BS>
-__global__ void k_restrict_lat(int Fx, int Fy, int Fz, int Cx, int Cy, int Cz, const double *__restrict__ rf, double *__restrict__ bc) {
+template <int BS, typename T>
+__global__ void k_restrict_lat(int Fx, int Fy, int Fz, int Cx, int Cy, int Cz, const T *__restrict__ rf, T *__restrict__ bc) {
   const int64_t nc = (int64_t)Cx * Cy * Cz;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= nc * BS) return;
@@ -195,51 +195,54 @@ __global__ void k_restrict_lat(int Fx, int Fy, int Fz, int Cx, int Cy, int Cz, c
   const int c = (int)(t % BS);
   int Ix, Iy, Iz;
   lat_coord(I, Cy, Cz, Ix, Iy, Iz);
-  double s = 0;
+  T s = 0;
   for (int ux = -1; ux <= 1; ux++)
     for (int uy = -1; uy <= 1; uy++)
       for (int uz = -1; uz <= 1; uz++) {
         const int ix = 2 * Ix + ux, iy = 2 * Iy + uy, iz = 2 * Iz + uz;
         if (ix < 0 || ix >= Fx || iy < 0 || iy >= Fy || iz < 0 || iz >= Fz) continue;
-        s += (ux ? 0.5 : 1.0) * (uy ? 0.5 : 1.0) * (uz ? 0.5 : 1.0) * rf[(((int64_t)ix * Fy + iy) * Fz + iz) * BS + c];
+        s += (T)((ux ? 0.5 : 1.0) * (uy ? 0.5 : 1.0) * (uz ? 0.5 : 1.0)) * rf[(((int64_t)ix * Fy + iy) * Fz + iz) * BS + c];
       }
   bc[t] = s;
 }
 
 // x_f += P x_c on unmasked fine unknowns (masked coarse values are zero)
-template <int BS>
-__global__ void k_prolong_lat(int Fx, int Fy, int Fz, int Cy, int Cz, const double *__restrict__ dinvf, const double *__restrict__ xc,
-                              double *__restrict__ xf) {
+template <int BS, typename T>
+__global__ void k_prolong_lat(int Fx, int Fy, int Fz, int Cy, int Cz, const T *__restrict__ dinvf, const T *__restrict__ xc,
+                              T *__restrict__ xf) {
   const int64_t nf = (int64_t)Fx * Fy * Fz;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= nf * BS || dinvf[t] == 0.0) return;
+  if (t >= nf * BS || dinvf[t] == (T)0) return;
   const int64_t i = t / BS;
   const int c = (int)(t % BS);
   int ix, iy, iz;
   lat_coord(i, Fy, Fz, ix, iy, iz);
-  double s = 0;
+  T s = 0;
   for (int qx = ix >> 1; qx <= (ix + 1) >> 1; qx++)
     for (int qy = iy >> 1; qy <= (iy + 1) >> 1; qy++)
       for (int qz = iz >> 1; qz <= (iz + 1) >> 1; qz++)
-        s += ((ix & 1) ? 0.5 : 1.0) * ((iy & 1) ? 0.5 : 1.0) * ((iz & 1) ? 0.5 : 1.0) * xc[(((int64_t)qx * Cy + qy) * Cz + qz) * BS + c];
+        s += (T)(((ix & 1) ? 0.5 : 1.0) * ((iy & 1) ? 0.5 : 1.0) * ((iz & 1) ? 0.5 : 1.0)) * xc[(((int64_t)qx * Cy + qy) * Cz + qz) * BS + c];
   xf[t] += s;
 }
 
-__global__ void k_cheb0(int64_t n, const double *dinv, const double *r, double inv_theta, double *d, double *z) {
+template <typename T>
+__global__ void k_cheb0(int64_t n, const T *dinv, const T *r, T inv_theta, T *d, T *z) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double v = dinv[i] * r[i] * inv_theta;
+  const T v = dinv[i] * r[i] * inv_theta;
   d[i] = v;
   z[i] = v;
 }
-__global__ void k_chebk(int64_t n, const double *dinv, const double *r, const double *w, double c1, double c2, double *d, double *z) {
+template <typename T>
+__global__ void k_chebk(int64_t n, const T *dinv, const T *r, const T *w, T c1, T c2, T *d, T *z) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double v = c1 * d[i] + c2 * dinv[i] * (r[i] - w[i]);
+  const T v = c1 * d[i] + c2 * dinv[i] * (r[i] - w[i]);
   d[i] = v;
   z[i] += v;
 }
-__global__ void k_add(int64_t n, const double *a, double *y) {
+template <typename T>
+__global__ void k_add(int64_t n, const T *a, T *y) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) y[i] += a[i];
 }
@@ -251,20 +254,28 @@ __global__ void k_mulv(int64_t n, const double *a, double *y) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) y[i] *= a[i];
 }
-// natural (node, component) <-> lattice (node, component)
-__global__ void k_scatter(int64_t n, int bs, const int32_t *lat, const double *r, double *b) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t < n * bs) b[(int64_t)lat[t / bs] * bs + t % bs] = r[t];
+template <typename A, typename B>
+__global__ void k_conv(int64_t n, const A *__restrict__ a, B *__restrict__ b) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (B)a[i];
 }
-__global__ void k_gather(int64_t n, int bs, const int32_t *lat, const double *x, double *z) {
+// natural (node, component) FP64 <-> lattice (node, component) in the cycle's type
+template <typename T>
+__global__ void k_scatter(int64_t n, int bs, const int32_t *lat, const double *r, T *b) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t < n * bs) z[t] = x[(int64_t)lat[t / bs] * bs + t % bs];
+  if (t < n * bs) b[(int64_t)lat[t / bs] * bs + t % bs] = (T)r[t];
+}
+template <typename T>
+__global__ void k_gather(int64_t n, int bs, const int32_t *lat, const T *x, double *z) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t < n * bs) z[t] = (double)x[(int64_t)lat[t / bs] * bs + t % bs];
 }
 // y = M x for the dense coarsest inverse (one block per row)
-__global__ void k_dense_mv(int64_t n, const double *__restrict__ M, const double *__restrict__ x, double *__restrict__ y) {
-  __shared__ double red[256];
+template <typename T>
+__global__ void k_dense_mv(int64_t n, const T *__restrict__ M, const T *__restrict__ x, T *__restrict__ y) {
+  __shared__ T red[256];
   const int64_t r = blockIdx.x;
-  double s = 0;
+  T s = 0;
   for (int64_t j = threadIdx.x; j < n; j += blockDim.x) s += M[r * n + j] * x[j];
   red[threadIdx.x] = s;
   __syncthreads();
@@ -285,11 +296,15 @@ struct MGLevel {
   double *x = nullptr, *b = nullptr, *r = nullptr, *d = nullptr, *w = nullptr, *e = nullptr;
   double emin = 0, emax = 0;
   double *dense = nullptr;  // coarsest: dense inverse (masked rows and columns zero)
+  // FP32 cycle (mixed-precision solvers): the same level in single precision
+  float *As32 = nullptr, *dinv32 = nullptr, *dense32 = nullptr;
+  float *x32 = nullptr, *b32 = nullptr, *r32 = nullptr, *d32 = nullptr, *w32 = nullptr, *e32 = nullptr;
 };
 
 struct MGData {
   std::vector<MGLevel> lev;
   int bs = 1;
+  bool fp32 = false;
   int64_t n = 0;  // explicit nodes
   int32_t *lat = nullptr;
   int degree = 3;
@@ -298,8 +313,10 @@ struct MGData {
 
 static void mg_free(MGData *M) {
   if (!M) return;
-  for (MGLevel &l : M->lev)
+  for (MGLevel &l : M->lev) {
     for (double *p : {l.A, l.As, l.dinv, l.x, l.b, l.r, l.d, l.w, l.e, l.dense}) cudaFree(p);
+    for (float *p : {l.As32, l.dinv32, l.dense32, l.x32, l.b32, l.r32, l.d32, l.w32, l.e32}) cudaFree(p);
+  }
   cudaFree(M->lat);
   cudaFree(M->part);
   cudaFree(M->s);
@@ -308,27 +325,53 @@ static void mg_free(MGData *M) {
 
 void mg_destroy(void *m) { mg_free((MGData *)m); }
 
+// the arrays of one level in the cycle's type
+template <typename T>
+struct LV {
+  T *As, *dinv, *dense, *x, *b, *r, *d, *w, *e;
+};
+template <typename T>
+static LV<T> view(MGLevel &l);
+template <>
+LV<double> view<double>(MGLevel &l) {
+  return {l.As, l.dinv, l.dense, l.x, l.b, l.r, l.d, l.w, l.e};
+}
+template <>
+LV<float> view<float>(MGLevel &l) {
+  return {l.As32, l.dinv32, l.dense32, l.x32, l.b32, l.r32, l.d32, l.w32, l.e32};
+}
+
+// y = A x, or b - A x (the full stencil during set-up, the symmetric half afterwards)
 static void stencil_mv(int bs, const MGLevel &l, const double *x, const double *b, double *y, cudaStream_t s) {
   const unsigned g = nbk(l.n * bs);
   if (l.As) {
-    if (bs == 3) k_stencil_mv_sym<3><<<g, 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.As, x, b, y);
-    else k_stencil_mv_sym<1><<<g, 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.As, x, b, y);
+    if (bs == 3) k_stencil_mv_sym<3, double><<<g, 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.As, x, b, y);
+    else k_stencil_mv_sym<1, double><<<g, 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.As, x, b, y);
     return;
   }
   if (bs == 3) k_stencil_mv<3><<<g, 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.A, x, b, y);
   else k_stencil_mv<1><<<g, 256, 0, s>>>(l.L[0], l.L[1], l.L[2], l.A, x, b, y);
 }
 
+template <typename T>
+static void stencil_mv_t(int bs, const MGLevel &l, const T *As, const T *x, const T *b, T *y, cudaStream_t s) {
+  const unsigned g = nbk(l.n * bs);
+  if (bs == 3) k_stencil_mv_sym<3, T><<<g, 256, 0, s>>>(l.L[0], l.L[1], l.L[2], As, x, b, y);
+  else k_stencil_mv_sym<1, T><<<g, 256, 0, s>>>(l.L[0], l.L[1], l.L[2], As, x, b, y);
+}
+
 // Chebyshev-Jacobi on one level from a zero guess: z = p(D^-1 A) D^-1 r
-static dErr level_cheb(MGData *M, MGLevel &l, const double *r, double *z, cudaStream_t s) {
+template <typename T>
+static dErr level_cheb(MGData *M, MGLevel &l, const T *r, T *z, cudaStream_t s) {
+  LV<T> v = view<T>(l);
   const int64_t nv = l.n * M->bs;
   const double theta = 0.5 * (l.emax + l.emin), delta = 0.5 * (l.emax - l.emin), sigma = theta / delta;
   double rho = 1.0 / sigma;
-  k_cheb0<<<nbk(nv), 256, 0, s>>>(nv, l.dinv, r, 1.0 / theta, l.d, z);
+  k_cheb0<T><<<nbk(nv), 256, 0, s>>>(nv, v.dinv, r, (T)(1.0 / theta), v.d, z);
   for (int it = 1; it < M->degree; it++) {
-    stencil_mv(M->bs, l, z, nullptr, l.w, s);
+    stencil_mv_t<T>(M->bs, l, v.As, z, nullptr, v.w, s);
     const double rho1 = 1.0 / (2.0 * sigma - rho);
-    k_chebk<<<nbk(nv), 256, 0, s>>>(nv, l.dinv, r, l.w, rho1 * rho, 2.0 * rho1 / delta, l.d, z);
+    k_chebk<T><<<nbk(nv), 256, 0, s>>>(nv, v.dinv, r, v.w, (T)(rho1 * rho), (T)(2.0 * rho1 / delta), v.d, z);
     rho = rho1;
   }
   CUCHK(cudaGetLastError());
@@ -336,39 +379,48 @@ static dErr level_cheb(MGData *M, MGLevel &l, const double *r, double *z, cudaSt
 }
 
 // x = V(b) on level k (b and x are the level's own arrays)
+template <typename T>
 static dErr vcycle(MGData *M, size_t k, cudaStream_t s) {
   MGLevel &l = M->lev[k];
+  LV<T> v = view<T>(l);
   const int bs = M->bs;
   const int64_t nv = l.n * bs;
   if (k + 1 == M->lev.size()) {
-    k_dense_mv<<<(unsigned)nv, 256, 0, s>>>(nv, l.dense, l.b, l.x);
+    k_dense_mv<T><<<(unsigned)nv, 256, 0, s>>>(nv, v.dense, v.b, v.x);
     CUCHK(cudaGetLastError());
     return 0;
   }
   MGLevel &c = M->lev[k + 1];
-  DCHK(level_cheb(M, l, l.b, l.x, s));  // pre-smooth
-  stencil_mv(bs, l, l.x, l.b, l.r, s);  // r = b - A x
-  if (bs == 3) k_restrict_lat<3><<<nbk(c.n * 3), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], c.L[0], c.L[1], c.L[2], l.r, c.b);
-  else k_restrict_lat<1><<<nbk(c.n), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], c.L[0], c.L[1], c.L[2], l.r, c.b);
-  DCHK(vcycle(M, k + 1, s));
-  if (bs == 3) k_prolong_lat<3><<<nbk(nv), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], c.L[1], c.L[2], l.dinv, c.x, l.x);
-  else k_prolong_lat<1><<<nbk(nv), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], c.L[1], c.L[2], l.dinv, c.x, l.x);
-  stencil_mv(bs, l, l.x, l.b, l.r, s);  // post-smooth: e = p(D^-1 A) D^-1 (b - A x), x += e
-  DCHK(level_cheb(M, l, l.r, l.e, s));
-  k_add<<<nbk(nv), 256, 0, s>>>(nv, l.e, l.x);
+  LV<T> cv = view<T>(c);
+  DCHK(level_cheb<T>(M, l, v.b, v.x, s));             // pre-smooth
+  stencil_mv_t<T>(bs, l, v.As, v.x, v.b, v.r, s);   // r = b - A x
+  if (bs == 3) k_restrict_lat<3, T><<<nbk(c.n * 3), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], c.L[0], c.L[1], c.L[2], v.r, cv.b);
+  else k_restrict_lat<1, T><<<nbk(c.n), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], c.L[0], c.L[1], c.L[2], v.r, cv.b);
+  DCHK(vcycle<T>(M, k + 1, s));
+  if (bs == 3) k_prolong_lat<3, T><<<nbk(nv), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], c.L[1], c.L[2], v.dinv, cv.x, v.x);
+  else k_prolong_lat<1, T><<<nbk(nv), 256, 0, s>>>(l.L[0], l.L[1], l.L[2], c.L[1], c.L[2], v.dinv, cv.x, v.x);
+  stencil_mv_t<T>(bs, l, v.As, v.x, v.b, v.r, s);   // post-smooth: e = p(D^-1 A) D^-1 (b - A x), x += e
+  DCHK(level_cheb<T>(M, l, v.r, v.e, s));
+  k_add<T><<<nbk(nv), 256, 0, s>>>(nv, v.e, v.x);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+template <typename T>
+static dErr apply_t(MGData *M, const double *r, double *z, cudaStream_t s) {
+  MGLevel &f = M->lev[0];
+  LV<T> v = view<T>(f);
+  CUCHK(cudaMemsetAsync(v.b, 0, f.n * M->bs * sizeof(T), s));
+  k_scatter<T><<<nbk(M->n * M->bs), 256, 0, s>>>(M->n, M->bs, M->lat, r, v.b);
+  DCHK(vcycle<T>(M, 0, s));
+  k_gather<T><<<nbk(M->n * M->bs), 256, 0, s>>>(M->n, M->bs, M->lat, v.x, z);
   CUCHK(cudaGetLastError());
   return 0;
 }
 
 dErr mg_apply(void *m, const double *r, double *z, cudaStream_t s) {
   MGData *M = (MGData *)m;
-  MGLevel &f = M->lev[0];
-  CUCHK(cudaMemsetAsync(f.b, 0, f.n * M->bs * sizeof(double), s));
-  k_scatter<<<nbk(M->n * M->bs), 256, 0, s>>>(M->n, M->bs, M->lat, r, f.b);
-  DCHK(vcycle(M, 0, s));
-  k_gather<<<nbk(M->n * M->bs), 256, 0, s>>>(M->n, M->bs, M->lat, f.x, z);
-  CUCHK(cudaGetLastError());
-  return 0;
+  return M->fp32 ? apply_t<float>(M, r, z, s) : apply_t<double>(M, r, z, s);
 }
 
 // lambda_max(D^-1 A) by 20 power steps from a seeded vector (masked unknowns stay 0)
@@ -470,7 +522,7 @@ static dErr level_alloc(MGLevel &l, int bs) {
 
 // build the hierarchy from the assembled Q1 matrix (scalar, or the interleaved 3 x 3 blocked elasticity matrix)
 // of a uniform-order space on a block mesh
-dErr mg_build(_p_dMat *J, int degree, void **out) {
+dErr mg_build(_p_dMat *J, int degree, bool fp32, void **out) {
   _p_dFS *fs = J->fs;
   const int bs = J->bs;
   if (bs != 1 && bs != 3) return set_error("Q1 multigrid: block size %d", bs);
@@ -577,6 +629,30 @@ dErr mg_build(_p_dMat *J, int degree, void **out) {
   for (MGLevel &l : M->lev) {  // the full stencils were needed for the Galerkin products and the dense solve only
     cudaFree(l.A);
     l.A = nullptr;
+  }
+  if (fp32) {  // the single-precision cycle: every cycle array rounded once
+    M->fp32 = true;
+    for (size_t k = 0; k < M->lev.size(); k++) {
+      MGLevel &l = M->lev[k];
+      const int64_t nv = l.n * bs;
+      auto conv = [&](const double *a, float **b, int64_t cnt) -> dErr {
+        CUCHK(cudaMalloc(b, std::max<int64_t>(cnt, 1) * sizeof(float)));
+        if (a && cnt) k_conv<double, float><<<nbk(cnt), 256, 0, s>>>(cnt, a, *b);
+        else CUCHK(cudaMemsetAsync(*b, 0, std::max<int64_t>(cnt, 1) * sizeof(float), s));
+        CUCHK(cudaGetLastError());
+        return 0;
+      };
+      dErr e = conv(l.dinv, &l.dinv32, nv);
+      if (!e && l.As) e = conv(l.As, &l.As32, 14 * bs * nv);
+      if (!e && l.dense) e = conv(l.dense, &l.dense32, nv * nv);
+      for (float **p : {&l.x32, &l.b32, &l.r32, &l.d32, &l.w32, &l.e32})
+        if (!e) e = conv(nullptr, p, nv);
+      if (e) {
+        mg_free(M);
+        return e;
+      }
+    }
+    CUCHK(cudaStreamSynchronize(s));
   }
   *out = M;
   return 0;

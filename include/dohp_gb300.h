@@ -282,7 +282,8 @@ typedef enum { dKSP_CG = 0, dKSP_FGMRES = 1 } dKSPType;
 /* preconditioners on the Q1-embedded matrix: Jacobi; Chebyshev-Jacobi (degree from dKSPSetOptions); MG_Q1: geometric
  * V-cycle on the lattice of GLL nodes (scalar or 3 x 3 blocked matrices of uniform-order spaces on block meshes
  * with an even number of GLL intervals per direction; Chebyshev-Jacobi smoothing one degree below that degree,
- * at least 2; Galerkin coarse levels, exact coarsest solve; FP64 in every precision mode) */
+ * at least 2; Galerkin coarse levels, exact coarsest solve; the cycle in FP64, or in FP32 when the
+ * preconditioner precision of dKSPSetOptions is FP32 or BF16) */
 typedef enum { dPC_NONE = 0, dPC_JACOBI = 1, dPC_CHEBYSHEV_Q1 = 2, dPC_MG_Q1 = 3 } dPCType;
 dErr dKSPCreate(dOperator op, dMat pmat, dKSPType type, dPCType pc, dKSP *ksp);
 dErr dKSPDestroy(dKSP *ksp);
