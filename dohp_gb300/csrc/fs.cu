@@ -161,7 +161,9 @@ static void fs_free_device(_p_dFS *fs) {
   cudaFree(fs->d_eval);
   cudaFree(fs->d_et_w);
   cudaFree(fs->d_et_wff);
+  cudaFree(fs->d_mg_lat);
   fs->d_et_wff = nullptr;
+  fs->d_mg_lat = nullptr;
   fs->d_eptr = fs->d_ecol = nullptr;
   fs->d_eval = fs->d_et_w = nullptr;
   fs->d_emap = fs->d_xstart = fs->d_edeg = fs->d_qoff = fs->d_et_ptr = fs->d_et_idx = nullptr;

@@ -92,6 +92,7 @@ struct _p_dFS {
   int32_t *d_eptr = nullptr, *d_ecol = nullptr;       // E as CSR (hp spaces only)
   double *d_eval = nullptr, *d_et_w = nullptr;        // E values and E^T weights (hp spaces only)
   void *d_et_wff = nullptr;                          // E^T weights as float pairs (hp spaces only)
+  int32_t *d_mg_lat = nullptr;                       // Q1 multigrid: lattice position of each explicit node (made once)
   double *d_coords = nullptr;                        // [nelem][8][3]
   double *d_dcache = nullptr;                        // Dirichlet values [(nc-n)*bs]
   // per-degree basis tables on the device for FAST rules: [p] -> B, Dq (Q=P)

@@ -306,7 +306,7 @@ struct MGData {
   int bs = 1;
   bool fp32 = false;
   int64_t n = 0;  // explicit nodes
-  int32_t *lat = nullptr;
+  const int32_t *lat = nullptr;  // owned by the space (made once, reused by every rebuild)
   int degree = 3;
   double *part = nullptr, *s = nullptr;
 };
@@ -317,7 +317,6 @@ static void mg_free(MGData *M) {
     for (double *p : {l.A, l.As, l.dinv, l.x, l.b, l.r, l.d, l.w, l.e, l.dense}) cudaFree(p);
     for (float *p : {l.As32, l.dinv32, l.dense32, l.x32, l.b32, l.r32, l.d32, l.w32, l.e32}) cudaFree(p);
   }
-  cudaFree(M->lat);
   cudaFree(M->part);
   cudaFree(M->s);
   delete M;
@@ -520,6 +519,31 @@ static dErr level_alloc(MGLevel &l, int bs) {
   return 0;
 }
 
+// lattice position of every explicit node (element (ex, ey, ez) local node (a, b, c) -> (ex p + a, ...)),
+// made once per space and kept on it (every Newton step rebuilds the hierarchy, not the map)
+static dErr lattice_map(_p_dFS *fs, const int L0[3], int My, int Mz) {
+  if (fs->d_mg_lat) return 0;
+  const int p = fs->p, P = p + 1;
+  std::vector<int32_t> lat(fs->n, -1);
+  for (int64_t r = 0; r < fs->nelem; r++) {
+    const int ex = (int)(r / ((int64_t)My * Mz)), ey = (int)((r / Mz) % My), ez = (int)(r % Mz);
+    for (int a = 0; a < P; a++)
+      for (int b = 0; b < P; b++)
+        for (int c = 0; c < P; c++) {
+          const int32_t d = fs->emap[fs->xstart[r] + (a * P + b) * P + c];
+          if (d >= fs->n) continue;
+          const int32_t L = (int32_t)((((int64_t)ex * p + a) * L0[1] + (ey * p + b)) * L0[2] + ez * p + c);
+          if (lat[d] >= 0 && lat[d] != L) return set_error("dof %d sits at two lattice positions: the mesh is not a structured block", d);
+          lat[d] = L;
+        }
+  }
+  for (int64_t d = 0; d < fs->n; d++)
+    if (lat[d] < 0) return set_error("dof %lld has no lattice position", (long long)d);
+  CUCHK(cudaMalloc(&fs->d_mg_lat, std::max<int64_t>(fs->n, 1) * sizeof(int32_t)));
+  CUCHK(cudaMemcpy(fs->d_mg_lat, lat.data(), fs->n * sizeof(int32_t), cudaMemcpyHostToDevice));
+  return 0;
+}
+
 // build the hierarchy from the assembled Q1 matrix (scalar, or the interleaved 3 x 3 blocked elasticity matrix)
 // of a uniform-order space on a block mesh
 dErr mg_build(_p_dMat *J, int degree, bool fp32, void **out) {
@@ -537,31 +561,12 @@ dErr mg_build(_p_dMat *J, int degree, bool fp32, void **out) {
   M->bs = bs;
   M->degree = std::max(2, degree);
   M->n = fs->n;
-  // lattice position of every explicit node (element (ex, ey, ez) local node (a, b, c) -> (ex p + a, ...))
-  std::vector<int32_t> lat(fs->n, -1);
-  const int P = p + 1;
-  for (int64_t r = 0; r < fs->nelem; r++) {
-    const int ex = (int)(r / ((int64_t)My * Mz)), ey = (int)((r / Mz) % My), ez = (int)(r % Mz);
-    for (int a = 0; a < P; a++)
-      for (int b = 0; b < P; b++)
-        for (int c = 0; c < P; c++) {
-          const int32_t d = fs->emap[fs->xstart[r] + (a * P + b) * P + c];
-          if (d >= fs->n) continue;
-          const int32_t L = (int32_t)((((int64_t)ex * p + a) * L0[1] + (ey * p + b)) * L0[2] + ez * p + c);
-          if (lat[d] >= 0 && lat[d] != L) {
-            mg_free(M);
-            return set_error("dof %d sits at two lattice positions: the mesh is not a structured block", d);
-          }
-          lat[d] = L;
-        }
+  dErr le = lattice_map(fs, L0, My, Mz);
+  if (le) {
+    mg_free(M);
+    return le;
   }
-  for (int64_t d = 0; d < fs->n; d++)
-    if (lat[d] < 0) {
-      mg_free(M);
-      return set_error("dof %lld has no lattice position", (long long)d);
-    }
-  CUCHK(cudaMalloc(&M->lat, std::max<int64_t>(fs->n, 1) * sizeof(int32_t)));
-  CUCHK(cudaMemcpy(M->lat, lat.data(), fs->n * sizeof(int32_t), cudaMemcpyHostToDevice));
+  M->lat = fs->d_mg_lat;
   CUCHK(cudaMalloc(&M->part, 1024 * sizeof(double)));
   CUCHK(cudaMalloc(&M->s, 4 * sizeof(double)));
   // levels: halve until the coarsest is small enough for a dense inverse (9 nodes per direction for scalar
