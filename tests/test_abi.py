@@ -121,3 +121,31 @@ def test_errors_are_reported_not_aborted(L):
     rc = L.dMeshCreateBlock(dg.ptr(np.asarray([1, 2, 2], np.int32)), dg.ptr(np.zeros(6)), ctypes.c_double(0),
                             ctypes.c_uint64(0), ctypes.byref(mesh))
     assert rc != 0 and b"vertices" in L.dGetLastError()
+
+
+def test_facet_rules_host_side_match_oracle(L):
+    """dFSGetFacetRule is host code (tensorquad.c:309-355 restated): same nodes and weights as the oracle"""
+    for side in range(6):
+        for order in range(0, 17, 2):
+            n, w = dg.facet_rule(side, order)
+            no, wo = po.facet_rule(side, order)
+            np.testing.assert_allclose(n, no, rtol=0, atol=1e-15)
+            np.testing.assert_allclose(w, wo, rtol=1e-15, atol=0)
+    with pytest.raises(dg.DohpError):
+        dg.facet_rule(6, 4)
+
+
+def test_boundary_status_values(L):
+    """the reference's dFSBStatus values (include/dohpfs.h:41-47): DIRICHLET and WEAK above the 16-bit count"""
+    assert dg.dFSBSTATUS_DIRICHLET == 1 << 16 and dg.dFSBSTATUS_WEAK == 1 << 17
+    mesh, fs = ctypes.c_void_p(), ctypes.c_void_p()
+    dg.chk(L.dMeshCreateBlock(dg.ptr(np.asarray((3, 3, 3), np.int32)), dg.ptr(np.asarray((0, 1, 0, 1, 0, 1), np.float64)),
+                              ctypes.c_double(0.1), ctypes.c_uint64(1), ctypes.byref(mesh)))
+    dg.chk(L.dFSCreate(mesh, None, ctypes.byref(fs)))
+    dg.chk(L.dFSRegisterBoundary(fs, ctypes.c_int32(200), ctypes.c_int(dg.dFSBSTATUS_WEAK | dg.dFSBSTATUS_DIRICHLET)))
+    with pytest.raises(dg.DohpError):
+        dg.chk(L.dFSRegisterBoundary(fs, ctypes.c_int32(400), ctypes.c_int(dg.dFSBSTATUS_WEAK)))
+    with pytest.raises(dg.DohpError):
+        dg.chk(L.dFSRegisterBoundary(fs, ctypes.c_int32(100), ctypes.c_int(1 << 20)))
+    L.dFSDestroy(ctypes.byref(fs))
+    L.dMeshDestroy(ctypes.byref(mesh))
