@@ -7,7 +7,9 @@
 // each step covers all elements: quadrature arrays are element-natural per element, elements back to back,
 // and every evaluation is one batched dEFSApply launch per element order (one launch on a uniform-order
 // space; on a mixed-order space the elements of each order triple form a bucket, and the launches read and
-// write each element at its own expanded-node and quadrature-point offsets). FAST rules (one patch per element).
+// write each element at its own expanded-node and quadrature-point offsets). FAST rules (one patch per
+// element), and on uniform-order spaces the SPARSE rule (2 Gauss points in each GLL sub-interval, (2p)^3 points
+// per element in tensor order: the p^3 patches of the reference's patch loop are the 2 x 2 x 2 blocks of it).
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -108,12 +110,14 @@ extern "C" {
 dErr dRulesetIteratorCreate(dFS fs, dQuadratureMethod method, dRulesetIterator *it) {
   if (!fs || !it) return set_error("null argument");
   if (!fs->setup) return set_error("dFS not set up");
-  if (method != dQUADRATURE_METHOD_FAST) return set_error("batched iterator supports FAST rules (one patch per element)");
+  if (method != dQUADRATURE_METHOD_FAST && method != dQUADRATURE_METHOD_SPARSE)
+    return set_error("batched iterator supports FAST and SPARSE rules");
+  if (method == dQUADRATURE_METHOD_SPARSE && !fs->uniform) return set_error("SPARSE batched iterator needs a uniform-order space");
   if (!fs->jac) return set_error("dFS was created without a dJacobi");
   _p_dRulesetIterator *I = new _p_dRulesetIterator();
   I->fs = fs;
   I->nel = fs->nelem;
-  I->nq = fs->nq;
+  I->nq = fs->nq;  // FAST: (p+1)^3 points per element; SPARSE: set below from the rule
   std::map<std::array<int, 3>, std::vector<int32_t>> groups;  // order triple -> elements, ascending
   for (int64_t e = 0; e < fs->nelem; e++) groups[{fs->edeg[3 * e], fs->edeg[3 * e + 1], fs->edeg[3 * e + 2]}].push_back((int32_t)e);
   I->per_point_w = groups.size() > 1;
@@ -131,6 +135,7 @@ dErr dRulesetIteratorCreate(dFS fs, dQuadratureMethod method, dRulesetIterator *
     B.nel = (int64_t)kv.second.size();
     const Basis1D *b = B.efs->b;
     const int Q = b[0].Q * b[1].Q * b[2].Q;
+    if (method == dQUADRATURE_METHOD_SPARSE) I->nq = I->nel * Q;  // uniform: one bucket
     std::vector<double> wq(Q);
     for (int i = 0; i < b[0].Q; i++)
       for (int j = 0; j < b[1].Q; j++)

@@ -199,7 +199,9 @@ dErr dOperatorMultHost(dOperator op, const dScalar *x_host, dScalar *y_host);
  * CommitPatchApplied / Finish cycle covers all elements at once on the device. Arrays are element-natural
  * per element, elements back to back (patch order = element order for FAST rules); on spaces with per-element
  * orders each element has (p_x+1)(p_y+1)(p_z+1) points, element e starting at the prefix sum of the counts
- * before it (the layout of dFSGetNumQuadraturePoints and dOperatorGetQuadratureData). */
+ * before it (the layout of dFSGetNumQuadraturePoints and dOperatorGetQuadratureData). SPARSE rules (uniform-order
+ * spaces, degree <= 5): (2p)^3 points per element in tensor order; patch (a, b, c) of the reference's patch loop
+ * is the 2 x 2 x 2 block of points (2a..2a+1, 2b..2b+1, 2c..2c+1). */
 dErr dRulesetIteratorCreate(dFS fs, dQuadratureMethod method, dRulesetIterator *it);
 dErr dRulesetIteratorDestroy(dRulesetIterator *it);
 dErr dRulesetIteratorStart(dRulesetIterator it, const dScalar *g, dFSHomogeneousMode hmode);

@@ -113,7 +113,10 @@ def test_restart_and_add_mode():
 def test_errors():
     fs = dg.FS((3, 3, 3), degree=2, seed=1)
     with pytest.raises(dg.DohpError):
-        dg.RulesetIterator(fs, method=dg.SPARSE)
+        dg.RulesetIterator(fs, method=dg.SELF)
+    ed = np.random.default_rng(0).integers(2, 4, size=8).astype(np.int32)
+    with pytest.raises(dg.DohpError):  # SPARSE on mixed orders
+        dg.RulesetIterator(dg.FS((3, 3, 3), degree=2, seed=1, elem_degree=ed), method=dg.SPARSE)
     it = dg.RulesetIterator(fs)
     with pytest.raises(dg.DohpError):
         it.get()
@@ -202,3 +205,44 @@ def test_error_norms_of_an_exactly_represented_solution():
                     X[:, 0] * (1 - X[:, 0]) * X[:, 1] * (1 - X[:, 1]) * (1 - 2 * X[:, 2])], -1)[:, None, :]
     ue, ge = it.error_norms(torch.as_tensor(eu, device="cuda"), torch.as_tensor(edu, device="cuda"))
     assert ue[2] < 1e-15 and ge[2] < 1e-13 and ue[1] < 1e-15
+
+
+@pytest.mark.parametrize("p", [2, 3, 4])
+def test_sparse_rule_iterator(p):
+    """SPARSE rule (2 Gauss points per GLL sub-interval, (2p)^3 per element): the mesh volume on a perturbed mesh
+    (the trilinear det J is integrated exactly), and on an affine mesh the integrals of u^2 and |grad u|^2 of a
+    linear field agree with the FAST rule's (both rules are exact there); the stiffness energy identity holds"""
+    npts = (4, 3, 5)
+    fs = dg.FS(npts, degree=p, perturb=0.1, seed=p)
+    it = dg.RulesetIterator(fs, method=dg.SPARSE)
+    it.start(None)
+    a = it.get()
+    assert a["jw"].numel() == fs.nelem * (2 * p) ** 3
+    assert abs(float(a["jw"].sum()) - 1.0) < 1e-13
+    o = po.FS(*npts, degree=p, perturb=0.0, seed=p, dirichlet_mask=0)
+    fs = dg.FS(npts, degree=p, perturb=0.0, seed=p, dirichlet=())
+    em, xs, ce = o.emap(), o.xstart(), o.coords_expanded()
+    gll = po.lobatto(p + 1)[0]
+    f = lambda X: 0.3 * X[0] - 1.1 * X[1] + 0.7 * X[2] + 0.2
+    g = np.zeros(fs.n)
+    P = p + 1
+    for e in range(o.nelem):
+        lo, hi = ce[e].min(0), ce[e].max(0)
+        for loc in range(P ** 3):
+            ijk = (loc // (P * P), (loc // P) % P, loc % P)
+            g[em[xs[e] + loc]] = f([lo[k] + (1 + gll[ijk[k]]) / 2 * (hi[k] - lo[k]) for k in range(3)])
+    vals = {}
+    for m in (dg.FAST, dg.SPARSE):
+        it = dg.RulesetIterator(fs, method=m)
+        it.start(torch.as_tensor(g, device="cuda"))
+        a = it.get()
+        vals[m] = (float((a["jw"][:, None] * a["u"] ** 2).sum()), float((a["jw"][:, None, None] * a["du"] ** 2).sum()))
+        if m == dg.SPARSE:
+            np.testing.assert_allclose(a["u"][:, 0].cpu().numpy(), f(a["x"].cpu().numpy().T), rtol=0, atol=1e-13)
+            a["dv"].copy_(a["jw"][:, None, None] * a["du"])
+            it.commit(dg.INSERT_VALUES, use_v=False, use_dv=True)
+            y = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
+            it.finish(y)
+            torch.cuda.synchronize()
+            assert abs(g @ y.cpu().numpy() - vals[m][1]) < 1e-12 * abs(vals[m][1])
+    np.testing.assert_allclose(vals[dg.SPARSE], vals[dg.FAST], rtol=1e-13)
