@@ -240,7 +240,9 @@ def run_reference(args, cfg, rank):
     line = {"impl": "reference", "metric": "GDoF/s operator apply", "value": cb["value"], "unit": "GDoF/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": cfg["label"] + " (bounded CPU sample)", "parallelism": "host threads"},
+            "config": {"workload": cfg["label"], "block_size": 3 if cfg["kind"] == "elasticity" else 1,
+                       "orders": "i.i.d. U{2..8}, seed 2" if cfg["hp"] else "p=%d" % cfg["p"], "quadrature": "Gauss (p+1)^3",
+                       "parallelism": "host threads (%d)" % threads, "sample": cb["sample"]},
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "GDoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
