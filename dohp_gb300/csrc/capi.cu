@@ -12,6 +12,8 @@ using namespace dgb;
 dErr op_mult(_p_dOperator *op, const double *x, double *y);
 dErr op_compute_geometry(_p_dOperator *op);
 dErr q1_symbolic(_p_dFS *fs, _p_dMat *J);
+dErr fs_restrict_rows(_p_dFS *fs, const double *x, double *g, int64_t t0, int64_t t1, cudaStream_t s);
+dErr op_mult_expanded(_p_dOperator *op, const double *x, double *yexp);
 dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk, const double *dref, double pe, double eps);
 dErr q1_numeric_elast(_p_dFS *fs, _p_dMat *J, double lam, double mu, int quirk);
 dErr plap_set_stash(_p_dOperator *op, const double *stash);
@@ -285,6 +287,10 @@ dErr dOperatorDestroy(dOperator *op) {
   cudaFree(o->d_yexp);
   cudaFree(o->d_x32);
   cudaFree(o->d_y32);
+  if (o->copy_stream) {
+    cudaStreamDestroy((cudaStream_t)o->copy_stream);
+    for (int k = 0; k < 4; k++) cudaEventDestroy((cudaEvent_t)o->copy_events[k]);
+  }
   cudaFree(o->d_hx);
   cudaFree(o->d_hy);
   cudaFree(o->d_gbase);
@@ -334,9 +340,36 @@ dErr dOperatorMultHost(dOperator op, const dScalar *x_host, dScalar *y_host) {
     CUCHK(cudaMalloc(&op->d_hy, std::max<size_t>(bytes, 8)));
   }
   CUCHK(cudaMemcpyAsync(op->d_hx, x_host, bytes, cudaMemcpyHostToDevice, fs->stream));
-  DCHK(op_mult(op, op->d_hx, op->d_hy));
-  CUCHK(cudaMemcpyAsync(y_host, op->d_hy, bytes, cudaMemcpyDeviceToHost, fs->stream));
-  CUCHK(cudaStreamSynchronize(fs->stream));
+  const int64_t N = fs->n * fs->bs;
+  if (op->prec != dPREC_FP64 || op->svk_state || N < 4 * 65536) {
+    DCHK(op_mult(op, op->d_hx, op->d_hy));
+    CUCHK(cudaMemcpyAsync(y_host, op->d_hy, bytes, cudaMemcpyDeviceToHost, fs->stream));
+    CUCHK(cudaStreamSynchronize(fs->stream));
+    return 0;
+  }
+  // FP64: the element part, then the restriction in four row blocks; each block goes back to the host on a
+  // second stream as soon as it is restricted, so the copy of one block overlaps the restriction of the next
+  if (!op->copy_stream) {
+    cudaStream_t cs;
+    CUCHK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    op->copy_stream = cs;
+    for (int k = 0; k < 4; k++) {
+      cudaEvent_t ev;
+      CUCHK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+      op->copy_events[k] = ev;
+    }
+  }
+  cudaStream_t cs = (cudaStream_t)op->copy_stream;
+  if (!op->d_yexp) CUCHK(cudaMalloc(&op->d_yexp, fs->nexp * fs->bs * sizeof(double)));
+  DCHK(op_mult_expanded(op, op->d_hx, op->d_yexp));
+  for (int k = 0; k < 4; k++) {
+    const int64_t t0 = N * k / 4, t1 = N * (k + 1) / 4;
+    DCHK(fs_restrict_rows(fs, op->d_yexp, op->d_hy, t0, t1, fs->stream));
+    CUCHK(cudaEventRecord((cudaEvent_t)op->copy_events[k], fs->stream));
+    CUCHK(cudaStreamWaitEvent(cs, (cudaEvent_t)op->copy_events[k], 0));
+    CUCHK(cudaMemcpyAsync(y_host + t0, op->d_hy + t0, (t1 - t0) * sizeof(double), cudaMemcpyDeviceToHost, cs));
+  }
+  CUCHK(cudaStreamSynchronize(cs));
   return 0;
 }
 

@@ -72,7 +72,32 @@ __global__ void k_restrict_w(int64_t n, int bs, const int32_t *__restrict__ et_p
   g[t] = add ? g[t] + s : s;
 }
 
+// rows [t0, t1) of the restriction (one thread per explicit scalar dof), FP64, optionally weighted (hp)
+__global__ void k_restrict_rows(int64_t t0, int64_t t1, int bs, const int32_t *__restrict__ et_ptr, const int32_t *__restrict__ et_idx,
+                                const double *__restrict__ et_w, const double *__restrict__ x, double *__restrict__ g) {
+  const int64_t t = t0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= t1) return;
+  const int64_t c = t / bs;
+  const int b = (int)(t - c * bs);
+  double s = 0;
+  if (et_w)
+    for (int32_t k = et_ptr[c]; k < et_ptr[c + 1]; k++) s += et_w[k] * x[(int64_t)et_idx[k] * bs + b];
+  else
+    for (int32_t k = et_ptr[c]; k < et_ptr[c + 1]; k++) s += x[(int64_t)et_idx[k] * bs + b];
+  g[t] = s;
+}
+
 }  // namespace
+
+// a range of rows of the FP64 restriction (insert), on a given stream: the same sums, in the same order, as
+// fs_restrict
+dErr fs_restrict_rows(_p_dFS *fs, const double *x, double *g, int64_t t0, int64_t t1, cudaStream_t s) {
+  if (t1 <= t0) return 0;
+  k_restrict_rows<<<(unsigned)((t1 - t0 + 255) / 256), 256, 0, s>>>(t0, t1, fs->bs, fs->d_et_ptr, fs->d_et_idx,
+                                                                     fs->boolean_e ? nullptr : fs->d_et_w, x, g);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
 
 dErr fs_restrict(_p_dFS *fs, const double *x, double *g, int add) {
   const int64_t N = fs->n * fs->bs;

@@ -119,6 +119,8 @@ struct _p_dOperator {
   double *d_yexp = nullptr;      // expanded output scratch
   float *d_x32 = nullptr, *d_y32 = nullptr;
   double *d_hx = nullptr, *d_hy = nullptr;  // device staging for the host-vector form
+  void *copy_stream = nullptr;               // host-vector form: device-to-host copies beside the restriction
+  void *copy_events[4] = {nullptr, nullptr, nullptr, nullptr};
   bool geo_valid = false;
   int geo_kind = -1;
   void *hp_plan = nullptr;  // order buckets, tiles, work list, graphs (hp.cu)

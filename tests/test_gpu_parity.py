@@ -109,6 +109,30 @@ def test_apply_deterministic_and_host_form():
     np.testing.assert_array_equal(yh, host(y1))
 
 
+@pytest.mark.parametrize("hp", [False, True])
+def test_host_form_with_overlapped_copies(hp):
+    """spaces large enough for the chunked restriction whose blocks are copied back while the next is restricted:
+    bit-identical to the device apply (uniform diffusion, and hp elasticity in the graph form)"""
+    if hp:
+        ed = np.random.default_rng(8).integers(2, 9, size=12 ** 3).astype(np.int32)
+        fs = dg.FS((13, 13, 13), degree=4, perturb=0.1, seed=3, bs=3, elem_degree=ed)
+        op = fs.operator(dg.dOP_ELASTICITY, param=(1.0, 0.3))
+        op.set_launch(dg.dLAUNCH_GRAPH)
+    else:
+        fs = dg.FS((25, 25, 25), degree=4, perturb=0.1, seed=3)
+        op = fs.operator()
+    N = fs.n * fs.bs
+    assert N >= 4 * 65536
+    g = np.random.default_rng(9).uniform(-1, 1, N)
+    y = torch.zeros(N, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        op.mult(dev(g), y)
+    yh = np.zeros(N)
+    for _ in range(2):
+        op.mult_host(np.ascontiguousarray(g), yh)
+    np.testing.assert_array_equal(yh, host(y))
+
+
 @pytest.mark.parametrize("degree", [1, 2, 3, 4, 6])
 @pytest.mark.parametrize("quirk", [1, 0])
 def test_q1_assembly(degree, quirk):
