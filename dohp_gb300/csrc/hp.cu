@@ -200,6 +200,13 @@ static dErr plan_build(_p_dOperator *op) {
   return 0;
 }
 
+// geometric factors in the apply's storage type (FP32 rounding or float-float split), once per geometry
+template <typename T>
+__global__ void k_geo_to(int64_t n, const double *__restrict__ a, T *__restrict__ b) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = T(a[i]);
+}
+
 // precision index: 0 FP64, 1 FP32, 2 float-float
 static int prec_index(const _p_dOperator *op) { return op->prec == dPREC_FP32 ? 1 : op->prec == dPREC_FF ? 2 : 0; }
 
@@ -423,17 +430,15 @@ dErr hp_mult(_p_dOperator *op, const double *x, double *y) {
   const int pi = prec_index(op);
   if (pi && !(pi == 1 ? op->d_geo32 : op->d_geoff)) {  // factors rounded to FP32 / split into float pairs once
     const int64_t ng = fs->nq * (op->kind == dOP_ELASTICITY ? 10 : 6);
-    std::vector<double> h(ng);
-    CUCHK(cudaMemcpy(h.data(), op->d_geo, ng * sizeof(double), cudaMemcpyDeviceToHost));
+    const unsigned g = (unsigned)std::max<int64_t>((ng + 255) / 256, 1);
     if (pi == 1) {
-      std::vector<float> f(h.begin(), h.end());
-      CUCHK(cudaMalloc(&op->d_geo32, ng * sizeof(float)));
-      CUCHK(cudaMemcpy(op->d_geo32, f.data(), ng * sizeof(float), cudaMemcpyHostToDevice));
+      CUCHK(cudaMalloc(&op->d_geo32, std::max<int64_t>(ng, 1) * sizeof(float)));
+      k_geo_to<float><<<g, 256, 0, fs->stream>>>(ng, op->d_geo, (float *)op->d_geo32);
     } else {
-      std::vector<ff> f(h.begin(), h.end());
-      CUCHK(cudaMalloc(&op->d_geoff, ng * sizeof(ff)));
-      CUCHK(cudaMemcpy(op->d_geoff, f.data(), ng * sizeof(ff), cudaMemcpyHostToDevice));
+      CUCHK(cudaMalloc(&op->d_geoff, std::max<int64_t>(ng, 1) * sizeof(ff)));
+      k_geo_to<ff><<<g, 256, 0, fs->stream>>>(ng, op->d_geo, (ff *)op->d_geoff);
     }
+    CUCHK(cudaGetLastError());
   }
   if (!op->hp_plan) {
     DCHK(plan_build(op));

@@ -378,6 +378,7 @@ dErr ksp_create_shell(int64_t n, cudaStream_t stream, dKSPType type, dErr (*mult
 
 dErr ksp_get_operator(dKSP ksp, dOperator *op) {
   if (!ksp || !op) return set_error("null argument");
+  if (ksp->shell_mult) return set_error("this KSP runs a shell operator");
   *op = ksp->op;
   return 0;
 }
@@ -749,6 +750,7 @@ dErr dKSPGetStats(dKSP ksp, int64_t *pc_applies, int64_t *correction_rejects, in
 
 dErr dKSPSetOperators(dKSP ksp, dOperator op, dMat pmat) {
   if (!ksp) return set_error("null KSP");
+  if (ksp->shell_mult) return set_error("this KSP runs a shell operator (a coupled system); it takes no dOperator or dMat");
   if (op) {
     if (op->fs->n * op->fs->bs != ksp->n) return set_error("operator size differs from the KSP's");
     ksp->op = op;

@@ -286,6 +286,7 @@ struct _p_dStokes {
   dMat Ap = nullptr;
   dKSP kspu = nullptr, ksp = nullptr;
   int restart = 30;
+  double *d_pb = nullptr, *d_px = nullptr;  // packed [u; p] right-hand side and iterate of the solve
 };
 
 static dErr stokes_mult(_p_dStokes *S, int mode, const double *xu, const double *xp, double *yu, double *yp) {
@@ -401,7 +402,7 @@ dErr dStokesCreate(dFS fsu, dFS fsp, const dReal rheo[4], dStokes *stk) {
 dErr dStokesDestroy(dStokes *stk) {
   if (!stk || !*stk) return 0;
   _p_dStokes *S = *stk;
-  for (double *p : {S->d_geo, S->d_bp, S->d_yu, S->d_yp, S->d_mdiag, S->d_t, S->d_part, S->d_s}) cudaFree(p);
+  for (double *p : {S->d_geo, S->d_bp, S->d_yu, S->d_yp, S->d_mdiag, S->d_t, S->d_part, S->d_s, S->d_pb, S->d_px}) cudaFree(p);
   dKSPDestroy(&S->ksp);
   dKSPDestroy(&S->kspu);
   dMatDestroy(&S->Ap);
@@ -439,9 +440,11 @@ dErr dStokesSolve(dStokes stk, const dScalar *bu, const dScalar *bp, dScalar *xu
     DCHK(ksp_create_shell(S->nu3 + S->np, s, dKSP_FGMRES, stokes_shell_mult, stokes_shell_pc, S, S->restart, &S->ksp));
   }
   const int64_t n = S->nu3 + S->np;
-  double *b, *x;
-  CUCHK(cudaMalloc(&b, n * sizeof(double)));
-  CUCHK(cudaMalloc(&x, n * sizeof(double)));
+  if (!S->d_pb) {
+    CUCHK(cudaMalloc(&S->d_pb, n * sizeof(double)));
+    CUCHK(cudaMalloc(&S->d_px, n * sizeof(double)));
+  }
+  double *b = S->d_pb, *x = S->d_px;
   CUCHK(cudaMemcpyAsync(b, bu, S->nu3 * sizeof(double), cudaMemcpyDeviceToDevice, s));
   CUCHK(cudaMemcpyAsync(b + S->nu3, bp, S->np * sizeof(double), cudaMemcpyDeviceToDevice, s));
   CUCHK(cudaMemcpyAsync(x, xu, S->nu3 * sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -459,8 +462,6 @@ dErr dStokesSolve(dStokes stk, const dScalar *bu, const dScalar *bp, dScalar *xu
     CUCHK(cudaMemcpyAsync(xp, x + S->nu3, S->np * sizeof(double), cudaMemcpyDeviceToDevice, s));
     CUCHK(cudaStreamSynchronize(s));
   }
-  cudaFree(b);
-  cudaFree(x);
   if (e) return e;
   if (its) *its = it;
   if (rnorm) *rnorm = rn;
