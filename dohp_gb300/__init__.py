@@ -418,7 +418,7 @@ dSTOKES_MULT_A, dSTOKES_MULT_BT, dSTOKES_MULT_B, dSTOKES_MULT_COUPLED = 0, 1, 2,
 
 class Stokes:
     """dStokes on a velocity space fsu (bs 3) and a pressure space fsp (bs 1) sharing its mesh
-    (FS(..., mesh_of=fsu)); rheo = (B, eps, p, nu), Newtonian p = 2."""
+    (FS(..., mesh_of=fsu)); rheo = (B, eps, p, nu): eta = B (eps^2/2 + Du:Du/2)^((p-2)/2), Newtonian at p = 2."""
 
     def __init__(self, fsu, fsp, rheo=None):
         self.fsu, self.fsp = fsu, fsp
@@ -433,11 +433,26 @@ class Stokes:
     def mult(self, mode, xu=None, xp=None, yu=None, yp=None):
         chk(lib().dStokesMult(self.h, ctypes.c_int(mode), ptr(xu), ptr(xp), ptr(yu), ptr(yp)))
 
+    def function(self, xu, xp, yu, yp):
+        """dStokesFunction: (yu, yp) = N(xu, xp); the state of the following Jacobian applies"""
+        chk(lib().dStokesFunction(self.h, ptr(xu), ptr(xp), ptr(yu), ptr(yp)))
+
     def solve(self, bu, bp, xu, xp, rtol=1e-8, maxit=500):
         its, rn = _i32(), _dbl()
         chk(lib().dStokesSolve(self.h, ptr(bu), ptr(bp), ptr(xu), ptr(xp), _dbl(rtol), _i32(maxit), ctypes.byref(its),
                                ctypes.byref(rn)))
         return its.value, rn.value
+
+    def newton(self, bu, bp, xu, xp, rtol=1e-8, atol=0.0, lin_rtol=1e-4, lin_maxit=500, max_it=30):
+        """dStokesNewtonSolve: returns (steps, residual norms [steps+1], linear iterations [steps])."""
+        opt = dNewtonOptions(max_it, rtol, atol, lin_rtol, lin_maxit, 0)
+        its = _i32()
+        fn = np.zeros(max_it + 1)
+        li = np.zeros(max_it, np.int32)
+        chk(lib().dStokesNewtonSolve(self.h, ptr(bu), ptr(bp), ptr(xu), ptr(xp), ctypes.byref(opt), ctypes.byref(its),
+                                     ptr(fn), ptr(li)))
+        k = its.value
+        return k, fn[:k + 1], li[:k]
 
 
 class dNewtonOptions(ctypes.Structure):

@@ -9,8 +9,12 @@
 //   B:  -int q div u                                                 (StokesPointwiseJacobian_B, stokes.c:496-499)
 //   coupled [A Bt; B 0] without the penalty                          (StokesPointwiseJacobian, stokes.c:476-487)
 // with Du the symmetric gradient in [00, 11, 22, 01, 02, 12] storage (dTensorSymCompress3, include/dohp.h:79-82).
-// This file covers the Newtonian rheology (exponent p = 2: eta = B, the store's eta' = 0); the power-law store
-// is refused with an error.
+// Rheology (StokesPointwiseComputeStore, stokes.c:447-453): eta = B (eps^2/2 + Du:Du/2)^((p-2)/2). The Newtonian
+// case p = 2 is linear (eta = B). For p != 2, dStokesFunction evaluates the nonlinear function
+// [eta(Du) Du - p I; -div u] (StokesPointwiseFunction stokes.c:460-474, the forcing moved into the caller's
+// right-hand side) and keeps the store {eta, eta', Du} of its state at every point; the A and coupled applies are
+// then the Jacobian at that state (StokesPointwiseJacobian(_A), stokes.c:476-494), eta Dv:Du + eta' (Dw:Du)(Dw:Dv).
+// Before any function evaluation the state is zero (eta = B (eps^2/2)^((p-2)/2), no eta' term).
 //
 // One fused kernel per element group does all of it: velocity gather through E, B and Dq passes per component,
 // pressure gather and three rectangular passes Bp (N x NP: the pressure's GLL basis at the velocity's Gauss
@@ -48,10 +52,17 @@ struct StokesArgs {
   ElemArgs U, P;     // velocity and pressure spaces (xstart, emap, n, x, yexp)
   const double *bp;  // Bp [N][NP]
   const double *geo; // velocity FAST geometry {J^-1 (9), w det J} per point, SoA per element
-  double eta, lam;
+  double *store;     // {eta, eta', Du[6]} per velocity point, SoA per element; null: no state (eta constant)
+  double eta, lam;   // eta without a state
+  double B, heps2, hexp;  // rheology: B, eps^2 / 2, (p - 2) / 2
 };
 
-constexpr int SM_A = 0, SM_BT = 1, SM_B = 2, SM_COUPLED = 3;
+constexpr int SM_A = 0, SM_BT = 1, SM_B = 2, SM_COUPLED = 3, SM_FUNCTION = 4;
+
+// dColonSymScalar3 (include/dohp.h:77-78) on [00, 11, 22, 01, 02, 12] storage
+__device__ __forceinline__ double colon_sym(const double *a, const double *b) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + 2 * (a[3] * b[3] + a[4] * b[4] + a[5] * b[5]);
+}
 
 // one rectangular pass along DIR of ne elements with input dims (D0, D1, D2): the DIR dimension goes from NP
 // to N through Bp (TR false) or from N to NP through Bp^T (TR true)
@@ -83,8 +94,8 @@ template <int N, int NP, int MODE>
 __global__ void __launch_bounds__(256) k_stokes(StokesArgs S, int64_t nelem, int cap) {
   extern __shared__ double smem[];
   constexpr int N3 = N * N * N, P3 = NP * NP * NP;
-  constexpr bool USE_U = MODE != SM_BT, USE_P = MODE == SM_BT || MODE == SM_COUPLED;
-  constexpr bool OUT_U = MODE != SM_B, OUT_P = MODE == SM_B || MODE == SM_COUPLED;
+  constexpr bool USE_U = MODE != SM_BT, USE_P = MODE == SM_BT || MODE == SM_COUPLED || MODE == SM_FUNCTION;
+  constexpr bool OUT_U = MODE != SM_B, OUT_P = MODE == SM_B || MODE == SM_COUPLED || MODE == SM_FUNCTION;
   const int64_t first = (int64_t)blockIdx.x * cap;
   const int ne = (int)min((int64_t)cap, nelem - first);
   double *tab = smem, *bp = smem + kTabElems, *buf = bp + MAXP * MAXP;
@@ -129,16 +140,37 @@ __global__ void __launch_bounds__(256) k_stokes(StokesArgs S, int64_t nelem, int
     const double tr = Du[0] + Du[4] + Du[8];
     if constexpr (OUT_U) {
       const double p = USE_P ? Pq[t] : 0.0;
-      const double lam = MODE == SM_A ? S.lam : 0.0, eta = MODE == SM_BT ? 0.0 : S.eta;
-      // Dv = w (eta Du_sym + lam tr(Du) I - p I), symmetric
+      const double lam = MODE == SM_A ? S.lam : 0.0;
+      const double sd[6] = {Du[0], Du[4], Du[8], 0.5 * (Du[1] + Du[3]), 0.5 * (Du[2] + Du[6]), 0.5 * (Du[5] + Du[7])};
+      double eta = MODE == SM_BT ? 0.0 : S.eta, dc = 0, sw[6] = {0, 0, 0, 0, 0, 0};
+      if constexpr (MODE == SM_FUNCTION) {  // the store of this state
+        if (S.store) {
+          const double greg = S.heps2 + 0.5 * colon_sym(sd, sd);
+          eta = S.B * pow(greg, S.hexp);
+          double *st = S.store + (int64_t)S.U.qoff[first + el] * 8 + r;
+          st[0] = eta;
+          st[N3] = S.hexp * eta / greg;
+#pragma unroll
+          for (int i = 0; i < 6; i++) st[(2 + i) * N3] = sd[i];
+        }
+      } else if constexpr (MODE == SM_A || MODE == SM_COUPLED) {  // the Jacobian at the stored state
+        if (S.store) {
+          const double *st = S.store + (int64_t)S.U.qoff[first + el] * 8 + r;
+          eta = st[0];
+#pragma unroll
+          for (int i = 0; i < 6; i++) sw[i] = st[(2 + i) * N3];
+          dc = st[N3] * colon_sym(sw, sd);
+        }
+      }
+      // Dv = w (eta Du_sym + eta' (Dw:Du) Dw + lam tr(Du) I - p I), symmetric
       const double diag = lam * tr - p;
       double Dv[9];
-      Dv[0] = w * (eta * Du[0] + diag);
-      Dv[4] = w * (eta * Du[4] + diag);
-      Dv[8] = w * (eta * Du[8] + diag);
-      Dv[1] = Dv[3] = w * eta * 0.5 * (Du[1] + Du[3]);
-      Dv[2] = Dv[6] = w * eta * 0.5 * (Du[2] + Du[6]);
-      Dv[5] = Dv[7] = w * eta * 0.5 * (Du[5] + Du[7]);
+      Dv[0] = w * (eta * sd[0] + dc * sw[0] + diag);
+      Dv[4] = w * (eta * sd[1] + dc * sw[1] + diag);
+      Dv[8] = w * (eta * sd[2] + dc * sw[2] + diag);
+      Dv[1] = Dv[3] = w * (eta * sd[3] + dc * sw[3]);
+      Dv[2] = Dv[6] = w * (eta * sd[4] + dc * sw[4]);
+      Dv[5] = Dv[7] = w * (eta * sd[5] + dc * sw[5]);
 #pragma unroll
       for (int d = 0; d < 3; d++)
 #pragma unroll
@@ -200,6 +232,11 @@ __global__ void k_rsub(int64_t n, const double *__restrict__ a, double *__restri
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) t[i] = a[i] - t[i];
 }
+__global__ void k_axpby(int64_t n, double a, const double *x, double b, const double *y, double *w) {
+  // w = a x + b y (w may alias x or y: each thread reads its own entries before writing)
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) w[i] = a * x[i] + b * y[i];
+}
 __global__ void k_fill(int64_t n, double v, double *__restrict__ y) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) y[i] = v;
@@ -229,6 +266,7 @@ dErr launch_stokes_np(const StokesArgs &S, int mode, int64_t nelem, cudaStream_t
     case SM_BT: return launch_stokes_mode<N, NP, SM_BT>(S, nelem, s);
     case SM_B: return launch_stokes_mode<N, NP, SM_B>(S, nelem, s);
     case SM_COUPLED: return launch_stokes_mode<N, NP, SM_COUPLED>(S, nelem, s);
+    case SM_FUNCTION: return launch_stokes_mode<N, NP, SM_FUNCTION>(S, nelem, s);
   }
   return set_error("Stokes mult mode %d", mode);
 }
@@ -276,6 +314,9 @@ dErr pmass_diag(int N, int NP, int64_t nelem, const int32_t *qoff, const int32_t
 struct _p_dStokes {
   dFS fsu = nullptr, fsp = nullptr;
   double B = 1, eps = 1, p = 2, nu = 0, lam = 0;
+  double eta0 = 1;              // viscosity at the zero state: the scale of the preconditioner's blocks
+  double *d_store = nullptr;    // power law: {eta, eta', Du[6]} per velocity point at the last function's state
+  bool have_state = false;
   int N = 0, NP = 0;
   int64_t nu3 = 0, np = 0;  // global sizes: velocity n*3, pressure n
   double *d_geo = nullptr, *d_bp = nullptr, *d_yu = nullptr, *d_yp = nullptr;
@@ -308,11 +349,17 @@ static dErr stokes_mult(_p_dStokes *S, int mode, const double *xu, const double 
   A.P = eargs(fp, xp, S->d_yp);
   A.bp = S->d_bp;
   A.geo = S->d_geo;
-  A.eta = S->B;
+  A.store = nullptr;
+  if (S->d_store && (mode == SM_FUNCTION || (S->have_state && (mode == SM_A || mode == SM_COUPLED)))) A.store = S->d_store;
+  A.eta = S->eta0;
   A.lam = S->lam;
+  A.B = S->B;
+  A.heps2 = 0.5 * S->eps * S->eps;
+  A.hexp = 0.5 * (S->p - 2);
   if (fu->nelem) DCHK(launch_stokes(A, S->N, S->NP, mode, fu->nelem, s));
   if (mode != SM_B) DCHK(fs_restrict(fu, S->d_yu, yu, 0));
-  if (mode == SM_B || mode == SM_COUPLED) DCHK(fs_restrict(fp, S->d_yp, yp, 0));
+  if (mode == SM_B || mode == SM_COUPLED || mode == SM_FUNCTION) DCHK(fs_restrict(fp, S->d_yp, yp, 0));
+  if (mode == SM_FUNCTION && S->d_store) S->have_state = true;
   return 0;
 }
 
@@ -327,7 +374,7 @@ static dErr stokes_shell_pc(void *ctx, const double *r, double *z) {
   cudaStream_t s = S->fsu->stream;
   const double *ru = r, *rp = r + S->nu3;
   double *zu = z, *zp = z + S->nu3;
-  k_schur_diag<<<nblk(S->np), 256, 0, s>>>(S->np, S->B, S->d_mdiag, rp, zp);
+  k_schur_diag<<<nblk(S->np), 256, 0, s>>>(S->np, S->eta0, S->d_mdiag, rp, zp);
   CUCHK(cudaGetLastError());
   // remove the constant (mean over the dofs): sum through a dot with the ones vector stored after d_t
   const double *ones = S->d_t + S->nu3;
@@ -352,15 +399,12 @@ dErr dStokesCreate(dFS fsu, dFS fsp, const dReal rheo[4], dStokes *stk) {
   if (fsp->dirichlet_mask) return set_error("the pressure space takes no Dirichlet sets (stokes.c:222)");
   _p_dStokes *S = new _p_dStokes();
   if (rheo) S->B = rheo[0], S->eps = rheo[1], S->p = rheo[2], S->nu = rheo[3];
-  if (S->p != 2) {
+  if (!(S->B > 0) || !(S->nu < 0.5) || !(S->p > 1) || (S->p != 2 && !(S->eps > 0))) {
     delete S;
-    return set_error("Stokes rheology exponent %g: only the Newtonian case (p = 2) is built", S->p);
-  }
-  if (!(S->B > 0) || !(S->nu < 0.5)) {
-    delete S;
-    return set_error("Stokes rheology needs B > 0 and nu < 1/2");
+    return set_error("Stokes rheology needs B > 0, p > 1, eps > 0 (p != 2) and nu < 1/2");
   }
   S->lam = S->nu / (1 - 2 * S->nu);  // StokesLambda (stokes.c:455-458)
+  S->eta0 = S->p == 2 ? S->B : S->B * std::pow(0.5 * S->eps * S->eps, 0.5 * (S->p - 2));
   S->fsu = fsu, S->fsp = fsp;
   S->N = fsu->p + 1, S->NP = fsp->p + 1;
   if (!(S->NP == S->N - 1 || S->NP == S->N - 2) || S->NP < 2 || S->N > 7) {
@@ -385,6 +429,7 @@ dErr dStokesCreate(dFS fsu, dFS fsp, const dReal rheo[4], dStokes *stk) {
   }
   CUCHK(cudaMalloc(&S->d_geo, std::max<int64_t>(fsu->nq, 1) * 10 * sizeof(double)));
   DCHK(geometry_fill(fsu, 1, nullptr, S->d_geo));
+  if (S->p != 2) CUCHK(cudaMalloc(&S->d_store, std::max<int64_t>(fsu->nq, 1) * 8 * sizeof(double)));
   CUCHK(cudaMalloc(&S->d_yu, std::max<int64_t>(fsu->nexp * 3, 1) * sizeof(double)));
   CUCHK(cudaMalloc(&S->d_yp, std::max<int64_t>(fsp->nexp, 1) * sizeof(double)));
   CUCHK(cudaMalloc(&S->d_mdiag, std::max<int64_t>(S->np, 1) * sizeof(double)));
@@ -402,7 +447,8 @@ dErr dStokesCreate(dFS fsu, dFS fsp, const dReal rheo[4], dStokes *stk) {
 dErr dStokesDestroy(dStokes *stk) {
   if (!stk || !*stk) return 0;
   _p_dStokes *S = *stk;
-  for (double *p : {S->d_geo, S->d_bp, S->d_yu, S->d_yp, S->d_mdiag, S->d_t, S->d_part, S->d_s, S->d_pb, S->d_px}) cudaFree(p);
+  for (double *p : {S->d_geo, S->d_bp, S->d_yu, S->d_yp, S->d_mdiag, S->d_t, S->d_part, S->d_s, S->d_pb, S->d_px, S->d_store})
+    cudaFree(p);
   dKSPDestroy(&S->ksp);
   dKSPDestroy(&S->kspu);
   dMatDestroy(&S->Ap);
@@ -421,16 +467,22 @@ dErr dStokesMult(dStokes stk, dStokesMultMode mode, const dScalar *xu, const dSc
   return stokes_mult(stk, m, xu, xp, yu, yp);
 }
 
-dErr dStokesSolve(dStokes stk, const dScalar *bu, const dScalar *bp, dScalar *xu, dScalar *xp, dReal rtol, dInt maxit, dInt *its,
-                  dReal *rnorm) {
-  if (!stk || !bu || !bp || !xu || !xp) return set_error("null argument");
-  _p_dStokes *S = stk;
+dErr dStokesFunction(dStokes stk, const dScalar *xu, const dScalar *xp, dScalar *yu, dScalar *yp) {
+  if (!stk || !xu || !xp || !yu || !yp) return set_error("null argument");
+  return stokes_mult(stk, SM_FUNCTION, xu, xp, yu, yp);
+}
+
+}  // extern "C"
+
+// the solver objects: the velocity block (one Q1 multigrid V-cycle or Chebyshev-Jacobi on the Q1-embedded A with
+// 2 mu = eta0, lambda as A) and the FGMRES on the packed vector with the block preconditioner
+static dErr stokes_solver_setup(_p_dStokes *S) {
   _p_dFS *fu = S->fsu;
   cudaStream_t s = fu->stream;
-  if (!S->ksp) {  // the velocity block: Chebyshev-Jacobi on the Q1-embedded A (2 mu = eta, lambda as A)
+  if (!S->ksp) {
     DCHK(dFSCreateOperator(fu, dOP_ELASTICITY, nullptr, &S->opu));
     DCHK(dFSCreateMatrix(fu, &S->Ap));
-    DCHK(q1_numeric_elast(fu, S->Ap, S->lam, 0.5 * S->B, 1));
+    DCHK(q1_numeric_elast(fu, S->Ap, S->lam, 0.5 * S->eta0, 1));
     // the velocity block's approximate inverse: one Q1 multigrid V-cycle where the GLL lattice coarsens (an even
     // number of GLL intervals per direction), else the single-level Chebyshev-Jacobi
     const _p_dMesh *mesh = fu->mesh;
@@ -439,11 +491,22 @@ dErr dStokesSolve(dStokes stk, const dScalar *bu, const dScalar *bp, dScalar *xu
     DCHK(dKSPCreate(S->opu, S->Ap, dKSP_CG, lattice ? dPC_MG_Q1 : dPC_CHEBYSHEV_Q1, &S->kspu));
     DCHK(ksp_create_shell(S->nu3 + S->np, s, dKSP_FGMRES, stokes_shell_mult, stokes_shell_pc, S, S->restart, &S->ksp));
   }
-  const int64_t n = S->nu3 + S->np;
   if (!S->d_pb) {
+    const int64_t n = S->nu3 + S->np;
     CUCHK(cudaMalloc(&S->d_pb, n * sizeof(double)));
     CUCHK(cudaMalloc(&S->d_px, n * sizeof(double)));
   }
+  return 0;
+}
+
+extern "C" {
+
+dErr dStokesSolve(dStokes stk, const dScalar *bu, const dScalar *bp, dScalar *xu, dScalar *xp, dReal rtol, dInt maxit, dInt *its,
+                  dReal *rnorm) {
+  if (!stk || !bu || !bp || !xu || !xp) return set_error("null argument");
+  _p_dStokes *S = stk;
+  cudaStream_t s = S->fsu->stream;
+  DCHK(stokes_solver_setup(S));
   double *b = S->d_pb, *x = S->d_px;
   CUCHK(cudaMemcpyAsync(b, bu, S->nu3 * sizeof(double), cudaMemcpyDeviceToDevice, s));
   CUCHK(cudaMemcpyAsync(b + S->nu3, bp, S->np * sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -467,6 +530,86 @@ dErr dStokesSolve(dStokes stk, const dScalar *bu, const dScalar *bp, dScalar *xu
   if (rnorm) *rnorm = rn;
   if (!(rn <= rtol)) return set_error("Stokes FGMRES did not converge in %d iterations (relative residual %g)", it, rn);
   return 0;
+}
+
+// Newton for the power-law Stokes system N(x) = b (the SNES of stokes.c: StokesFunction / StokesJacobian,
+// stokes.c:507-540, 675-740): each step solves J(x) dx = -F with the block-preconditioned FGMRES (the Jacobian at
+// the store of the last function evaluation) and backtracks on ||F||.
+dErr dStokesNewtonSolve(dStokes stk, const dScalar *bu, const dScalar *bp, dScalar *xu, dScalar *xp, const dNewtonOptions *opt,
+                        dInt *its, dReal *fnorm, dInt *lin_its) {
+  if (!stk || !bu || !bp || !xu || !xp || !opt) return set_error("null argument");
+  _p_dStokes *S = stk;
+  cudaStream_t s = S->fsu->stream;
+  DCHK(stokes_solver_setup(S));
+  const int64_t n = S->nu3 + S->np;
+  const unsigned g = nblk(n);
+  double *b = S->d_pb, *x = S->d_px, *block = nullptr;
+  CUCHK(cudaMalloc(&block, 4 * n * sizeof(double)));
+  double *F = block, *dx = F + n, *xt = dx + n, *Ft = xt + n;
+  CUCHK(cudaMemcpyAsync(b, bu, S->nu3 * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CUCHK(cudaMemcpyAsync(b + S->nu3, bp, S->np * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CUCHK(cudaMemcpyAsync(x, xu, S->nu3 * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CUCHK(cudaMemcpyAsync(x + S->nu3, xp, S->np * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  auto residual = [&](const double *xx, double *r, double *nrm) -> dErr {  // r = N(xx) - b, keeps the store of xx
+    DCHK(stokes_mult(S, SM_FUNCTION, xx, xx + S->nu3, r, r + S->nu3));
+    k_axpby<<<g, 256, 0, s>>>(n, 1.0, r, -1.0, b, r);
+    CUCHK(cudaGetLastError());
+    DCHK(device_dot(n, r, r, S->d_part, S->d_s, s));
+    double h = 0;
+    CUCHK(cudaMemcpyAsync(&h, S->d_s, sizeof h, cudaMemcpyDeviceToHost, s));
+    CUCHK(cudaStreamSynchronize(s));
+    *nrm = std::sqrt(h);
+    return 0;
+  };
+  double fn = 0, fn0 = 0;
+  int k = 0;
+  dErr err = residual(x, F, &fn);
+  fn0 = fn;
+  if (fnorm && !err) fnorm[0] = fn;
+  for (; !err && k < opt->max_it && fn > opt->rtol * fn0 && fn > opt->atol; k++) {
+    k_axpby<<<g, 256, 0, s>>>(n, -1.0, F, 0.0, F, Ft);  // rhs = -F (Ft as scratch)
+    if (cudaMemsetAsync(dx, 0, n * sizeof(double), s) != cudaSuccess) {
+      err = set_error("cudaMemsetAsync failed");
+      break;
+    }
+    int li = 0;
+    double rn = 0;
+    err = ksp_solve(S->ksp, Ft, dx, opt->lin_rtol, opt->lin_maxit, &li, &rn);
+    if (err) break;
+    if (!(rn < 1)) {
+      err = set_error("Stokes Newton step %d: linear solve made no progress (relative residual %g)", k, rn);
+      break;
+    }
+    if (lin_its) lin_its[k] = li;
+    double lam = 1, fnt = 0;
+    int ls = 0;
+    for (; ls < 12; ls++, lam *= 0.5) {
+      k_axpby<<<g, 256, 0, s>>>(n, 1.0, x, lam, dx, xt);
+      err = residual(xt, Ft, &fnt);
+      if (err || fnt < (1 - 1e-4 * lam) * fn) break;
+    }
+    if (err) break;
+    if (ls == 12) {
+      err = set_error("Stokes Newton line search failed at step %d (||F|| %g)", k, fn);
+      break;
+    }
+    std::swap(x, xt);  // the store is that of the accepted iterate, the last one evaluated
+    std::swap(F, Ft);
+    fn = fnt;
+    if (fnorm) fnorm[k + 1] = fn;
+  }
+  if (!err) {  // the pressure is determined up to a constant: return the zero-mean one
+    const double *ones = S->d_t + S->nu3;
+    err = device_dot(S->np, x + S->nu3, ones, S->d_part, S->d_s, s);
+    if (!err) k_sub_mean<<<nblk(S->np), 256, 0, s>>>(S->np, S->d_s, x + S->nu3);
+  }
+  if (!err && (cudaMemcpyAsync(xu, x, S->nu3 * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+               cudaMemcpyAsync(xp, x + S->nu3, S->np * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess))
+    err = set_error("cudaMemcpyAsync failed");
+  cudaStreamSynchronize(s);
+  cudaFree(block);
+  if (its) *its = k;
+  return err;
 }
 
 }  // extern "C"

@@ -249,16 +249,25 @@ typedef enum { dSTOKES_MULT_A = 0, dSTOKES_MULT_BT = 1, dSTOKES_MULT_B = 2, dSTO
 /* StokesCreate / StokesSetFromOptions / StokesGetMatrices (stokes.c:102-130, 160-274, 367-445): fsu the velocity
  * space (bs 3, degree k in 2..6, Dirichlet sets), fsp the pressure space (bs 1, degree k-1 or k-2, no boundary sets)
  * on the same mesh; rheo = {B, eps, p, nu} (struct StokesRheology, stokesimpl.h:9-11; the reference's defaults
- * 1, 1, 2, 0; NULL takes them). Newtonian rheology (p = 2) only. */
+ * 1, 1, 2, 0; NULL takes them): viscosity eta = B (eps^2/2 + Du:Du/2)^((p-2)/2) (StokesPointwiseComputeStore,
+ * stokes.c:447-453), p > 1; p = 2 is the linear (Newtonian) case. */
 dErr dStokesCreate(dFS fsu, dFS fsp, const dReal rheo[4], dStokes *stk);
 dErr dStokesDestroy(dStokes *stk);
 /* y = [A Bt; B 0] x blocks (StokesShellMatMult_All_IorA stokes.c:579-673, MatMult_Nest_StokesCoupled 541-577):
  * A: xu -> yu (with the penalty nu/(1-2nu)); BT: xp -> yu; B: xu -> yp; COUPLED: (xu, xp) -> (yu, yp) without
- * the penalty. Device vectors; the unused ones may be NULL. */
+ * the penalty. Device vectors; the unused ones may be NULL. With p != 2 the A and COUPLED blocks are the Jacobian
+ * at the state of the last dStokesFunction (StokesPointwiseJacobian(_A), stokes.c:476-494; the zero state before
+ * one). */
 dErr dStokesMult(dStokes stk, dStokesMultMode mode, const dScalar *xu, const dScalar *xp, dScalar *yu, dScalar *yp);
-/* the coupled system solved by FGMRES with the block upper triangular (Schur) preconditioner: velocity block
- * Chebyshev-Jacobi on the Q1-embedded viscous matrix, Schur complement -diag(M_p)/eta (the viscosity-scaled
- * pressure mass, stokes.c:742-799); (xu, xp) is the initial guess and the result, xp returned with zero mean */
+/* StokesFunction (stokes.c:507-540, StokesPointwiseFunction 460-474) without the forcing, which the caller puts in
+ * the right-hand side: yu = int eta(Du) Dv:Du - p div v, yp = -int q div u; keeps the store {eta, eta', Du} of
+ * (xu, xp) as the state of the Jacobian applies */
+dErr dStokesFunction(dStokes stk, const dScalar *xu, const dScalar *xp, dScalar *yu, dScalar *yp);
+/* the coupled system (the Jacobian at the current state) solved by FGMRES with the block upper triangular (Schur)
+ * preconditioner: velocity block one Q1 multigrid V-cycle (Chebyshev-Jacobi where the GLL lattice does not
+ * coarsen) on the Q1-embedded viscous matrix, Schur complement -diag(M_p)/eta (the viscosity-scaled pressure
+ * mass, stokes.c:742-799), both at the zero-state viscosity; (xu, xp) is the initial guess and the result, xp
+ * returned with zero mean */
 dErr dStokesSolve(dStokes stk, const dScalar *bu, const dScalar *bp, dScalar *xu, dScalar *xp, dReal rtol, dInt maxit, dInt *its,
                   dReal *rnorm);
 
@@ -353,6 +362,12 @@ typedef struct {
 } dNewtonOptions;
 dErr dPLaplaceNewtonSolve(dOperator op, dMat Jp, dKSP ksp, const dScalar *b, dScalar *u, dReal p, dReal eps,
                           const dNewtonOptions *opt, dInt *its, dReal *fnorm, dInt *lin_its);
+/* Newton-Krylov for the Stokes function N(x) = b (dStokesFunction; stokes.c's SNES with StokesFunction and
+ * StokesJacobian, stokes.c:507-540, 675-740): each step solves the Jacobian at x with dStokesSolve's FGMRES and
+ * block preconditioner to opt->lin_rtol and backtracks on ||F||; (xu, xp) is the initial guess and the result, xp
+ * returned with zero mean. fnorm receives max_it+1 norms, lin_its max_it counts (reference_quirk is unused). */
+dErr dStokesNewtonSolve(dStokes stk, const dScalar *bu, const dScalar *bp, dScalar *xu, dScalar *xp, const dNewtonOptions *opt,
+                        dInt *its, dReal *fnorm, dInt *lin_its);
 /* KSPSetOperators: new operator and/or preconditioning matrix (NULL keeps the current one); the
  * preconditioner is set up again on the next solve (a Newton step that re-assembled the Q1 matrix) */
 dErr dKSPSetOperators(dKSP ksp, dOperator op, dMat pmat);

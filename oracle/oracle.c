@@ -1783,7 +1783,9 @@ static void sym_uncompress(const double s[6], double du[9])
 /* MatMult_Nest_StokesCoupled (stokes.c:541-577 with StokesPointwiseJacobian, stokes.c:476-487) and
  * StokesShellMatMult_All_IorA (stokes.c:579-673 with StokesPointwiseJacobian_A/_B/_Bt, stokes.c:489-505).
  * mode 0 A (with the penalty lambda = nu/(1-2nu), StokesLambda stokes.c:455-458), 1 Bt, 2 B, 3 coupled (lambda = 0).
- * The store (StokesPointwiseComputeStore stokes.c:447-453) is evaluated from the velocity state su (NULL: zero). */
+ * The store (StokesPointwiseComputeStore stokes.c:447-453) is evaluated from the velocity state su (NULL: zero).
+ * mode 4 is the nonlinear function of StokesFunction (stokes.c:507-540, StokesPointwiseFunction stokes.c:460-474)
+ * without the forcing terms: Dv = w (eta(Du) Du - p I), q = -w div u, the store taken from xu itself (su unused). */
 int or_stokes_apply(const or_fs *fu, const or_fs *fp, int mode, const double rheo[4], const double *su, const double *xu,
                     const double *xp, double *yu, double *yp)
 {
@@ -1791,8 +1793,10 @@ int or_stokes_apply(const or_fs *fu, const or_fs *fp, int mode, const double rhe
   if (fu->nr != fp->nr) return or_fail("velocity and pressure spaces are on different meshes");
   const double Bv = rheo[0], eps = rheo[1], pw = rheo[2], nu = rheo[3];
   const double lambda = mode == 0 ? nu / (1 - 2 * nu) : 0.0;
-  const int use_u = mode == 0 || mode == 2 || mode == 3, use_p = mode == 1 || mode == 3;
+  if (mode < 0 || mode > 4) return or_fail("invalid Stokes mode");
+  const int use_u = mode != 1, use_p = mode == 1 || mode == 3 || mode == 4;
   const int out_u = mode != 2, out_p = mode >= 2;
+  if (mode == 4) su = xu;
   double *xeu = calloc((size_t)fu->nexp * 3, sizeof(double)), *xep = calloc((size_t)fp->nexp, sizeof(double));
   double *seu = calloc((size_t)fu->nexp * 3, sizeof(double));
   double *yeu = calloc((size_t)fu->nexp * 3, sizeof(double)), *yep = calloc((size_t)fp->nexp, sizeof(double));
@@ -1829,6 +1833,7 @@ int or_stokes_apply(const or_fs *fu, const or_fs *fp, int mode, const double rhe
           case 0: Dv[i] = w * (eta * Du[i] + dc * Ds[i] + lambda * (i < 3) * tr); break;
           case 1: Dv[i] = i < 3 ? -w * p : 0; break;
           case 3: Dv[i] = w * (eta * Du[i] + dc * Ds[i] + lambda * (i < 3) * tr - p * (i < 3)); break;
+          case 4: Dv[i] = w * (eta * Du[i] - p * (i < 3)); break;
           default: Dv[i] = 0;
         }
       }

@@ -137,7 +137,9 @@ int or_facet_commit(const or_fs *fs, int weak_mask, const double *v, double *y, 
 /* Coupled and block applies of the Stokes Jacobian on a velocity space fu (bs 3, degree k) and a pressure space fp
  * (bs 1, degree k - codim, no Dirichlet sets) of the same mesh, at the velocity FAST rule: mode 0 A (viscous block
  * with the penalty nu/(1-2nu)), 1 Bt (pressure -> velocity), 2 B (velocity -> pressure), 3 coupled [A Bt; B 0]
- * without penalty. rheo = {B, eps, p, nu}; the viscosity store comes from the velocity state su (NULL: zero). */
+ * without penalty, 4 the nonlinear function [eta(Du) Du - p I; -div u] (the state is xu itself, forcing left to
+ * the caller's right-hand side). rheo = {B, eps, p, nu}; the viscosity store of modes 0-3 comes from the velocity
+ * state su (NULL: zero). */
 int or_stokes_apply(const or_fs *fu, const or_fs *fp, int mode, const double rheo[4], const double *su, const double *xu,
                     const double *xp, double *yu, double *yp);
 

@@ -365,7 +365,8 @@ def facet_rule(side, order, method=0):
 
 
 def stokes_apply(fu, fp, mode, rheo=(1.0, 1.0, 2.0, 0.0), xu=None, xp=None, state=None):
-    """(yu, yp) of the Stokes block apply: mode 0 A, 1 Bt, 2 B, 3 coupled"""
+    """(yu, yp) of the Stokes block apply: mode 0 A, 1 Bt, 2 B, 3 coupled (Jacobian at the velocity state), 4 the
+    nonlinear function at xu, xp"""
     yu, yp = np.zeros(fu.n * 3), np.zeros(fp.n)
     keep = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (state, xu, xp)]
     addr = [None if a is None else a.ctypes.data for a in keep]

@@ -1,6 +1,7 @@
 """Stokes (src/fs/tests/stokes.c) on the device: every block apply (A with and without the penalty, Bt, B,
-coupled) against the oracle, and the block-preconditioned FGMRES solve of a manufactured problem (divergence-free
-velocity vanishing on the walls, zero-mean pressure) converging at the Taylor-Hood rates."""
+coupled) against the oracle, the block-preconditioned FGMRES solve of a manufactured problem (divergence-free
+velocity vanishing on the walls, zero-mean pressure) converging at the Taylor-Hood rates, and the power-law
+rheology: the nonlinear function, the Jacobian at its state, and Newton recovering a discrete solution."""
 import os
 
 import numpy as np
@@ -62,7 +63,9 @@ def test_blocks_match_oracle(k, codim, nu):
 def test_errors():
     fsu, fsp = spaces(2, 3, 2)
     with pytest.raises(dg.DohpError):
-        dg.Stokes(fsu, fsp, (1.0, 1.0, 1.5, 0.0))  # power-law rheology is not built
+        dg.Stokes(fsu, fsp, (1.0, 1.0, 1.0, 0.0))  # the power law needs p > 1
+    with pytest.raises(dg.DohpError):
+        dg.Stokes(fsu, fsp, (1.0, 0.0, 1.5, 0.0))  # and a positive regularisation when p != 2
     other = dg.FS((3, 3, 3), degree=1, bs=1, dirichlet=())
     with pytest.raises(dg.DohpError):
         dg.Stokes(fsu, other)  # not the same mesh
@@ -128,3 +131,63 @@ def test_manufactured_taylor_hood_converges():
     assert eu8 < 1e-3 and ep8 < 1e-2
     assert eu4 / eu8 > 10 and ep4 / ep8 > 5, (eu4, eu8, ep4, ep8)  # h^4 velocity, h^3 pressure at k = 3
     assert its8 < 2 * its4 + 20, (its4, its8)  # the block preconditioner keeps the count nearly mesh-independent
+
+
+@pytest.mark.parametrize("k,codim", [(3, 2), (2, 1)])
+def test_power_law_function_and_jacobian_match_oracle(k, codim):
+    """p = 4/3 (Glen n = 3): the Jacobian at the zero state, the function (StokesFunction without forcing) at a
+    random state, and the A / coupled Jacobian at that state (StokesPointwiseJacobian(_A)) against the oracle"""
+    M = 3
+    fsu, fsp = spaces(M, k, codim, seed=10 + k)
+    ou = po.FS(M + 1, M + 1, M + 1, degree=k, perturb=0.1, seed=10 + k, bs=3, dirichlet_mask=7)
+    op = po.FS(M + 1, M + 1, M + 1, degree=k - codim, perturb=0.1, seed=10 + k, bs=1, dirichlet_mask=0)
+    rheo = (1.3, 0.7, 4.0 / 3.0, 0.2)
+    st = dg.Stokes(fsu, fsp, rheo)
+    rng = np.random.default_rng(20 + k)
+    su, sp = 2.0 * rng.standard_normal(fsu.n * 3), rng.standard_normal(fsp.n)
+    vu, vp = rng.standard_normal(fsu.n * 3), rng.standard_normal(fsp.n)
+    yu = torch.zeros(fsu.n * 3, dtype=torch.float64, device="cuda")
+    yp = torch.zeros(fsp.n, dtype=torch.float64, device="cuda")
+    rel = lambda a, b: np.linalg.norm(a - b) / np.linalg.norm(b)
+    st.mult(dg.dSTOKES_MULT_A, xu=dev(vu), yu=yu)  # no state yet: eta = B (eps^2/2)^((p-2)/2)
+    assert rel(host(yu), po.stokes_apply(ou, op, 0, rheo, xu=vu)[0]) < 1e-12
+    st.function(dev(su), dev(sp), yu, yp)
+    fu, fp = po.stokes_apply(ou, op, 4, rheo, xu=su, xp=sp)
+    assert rel(host(yu), fu) < 1e-12 and rel(host(yp), fp) < 1e-12
+    st.mult(dg.dSTOKES_MULT_A, xu=dev(vu), yu=yu)
+    assert rel(host(yu), po.stokes_apply(ou, op, 0, rheo, xu=vu, state=su)[0]) < 1e-12
+    st.mult(dg.dSTOKES_MULT_COUPLED, xu=dev(vu), xp=dev(vp), yu=yu, yp=yp)
+    cu, cp = po.stokes_apply(ou, op, 3, rheo, xu=vu, xp=vp, state=su)
+    assert rel(host(yu), cu) < 1e-12 and rel(host(yp), cp) < 1e-12
+    st.mult(dg.dSTOKES_MULT_BT, xp=dev(vp), yu=yu)  # the pressure blocks do not depend on the state
+    assert rel(host(yu), po.stokes_apply(ou, op, 1, rheo, xp=vp)[0]) < 1e-12
+
+
+def test_power_law_newton_recovers_a_discrete_solution():
+    """x* = the Newtonian solution of the manufactured forcing (scaled to strain rates of order one); b = N(x*) for
+    the power law p = 4/3, eps = 0.5 (viscosity varying between about 0.7 and 2); Newton from zero with the
+    block-preconditioned FGMRES (one Q1 multigrid V-cycle on the velocity block) returns x*"""
+    fsu, fsp = spaces(4, 3, 2, seed=7)
+    lin = dg.Stokes(fsu, fsp, (1.0, 1.0, 2.0, 0.0))
+    it = dg.RulesetIterator(fsu)
+    it.start(None)
+    a = it.get()
+    _, _, f = exact(a["x"], 1.0)
+    a["v"].copy_(0.1 * a["jw"][:, None] * f)
+    it.commit(dg.INSERT_VALUES, use_v=True, use_dv=False)
+    bu = torch.zeros(fsu.n * 3, dtype=torch.float64, device="cuda")
+    it.finish(bu)
+    bp = torch.zeros(fsp.n, dtype=torch.float64, device="cuda")
+    xs_u, xs_p = torch.zeros_like(bu), torch.zeros_like(bp)
+    lin.solve(bu, bp, xs_u, xs_p, rtol=1e-12, maxit=2000)
+    pl = dg.Stokes(fsu, fsp, (1.0, 0.5, 4.0 / 3.0, 0.0))
+    b2u, b2p = torch.zeros_like(bu), torch.zeros_like(bp)
+    pl.function(xs_u, xs_p, b2u, b2p)
+    xu, xp = torch.zeros_like(bu), torch.zeros_like(bp)
+    k, fn, li = pl.newton(b2u, b2p, xu, xp, rtol=1e-11, lin_rtol=1e-6, lin_maxit=1000, max_it=40)
+    assert fn[-1] <= 1e-11 * fn[0], (k, fn, li)
+    assert 2 <= k <= 25, (k, fn)
+    ru = float(torch.linalg.norm(xu - xs_u) / torch.linalg.norm(xs_u))
+    rp = float(torch.linalg.norm(xp - xs_p) / torch.linalg.norm(xs_p))
+    assert ru < 1e-7 and rp < 1e-6, (ru, rp, k, fn)
+    assert abs(float(xp.sum())) < 1e-10

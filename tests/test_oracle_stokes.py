@@ -71,3 +71,39 @@ def test_divergence_of_a_linear_field():
                     loc += 1
     _, B = po.stokes_apply(fu, fp, 2, xu=g)
     assert abs(B.sum() + np.trace(M)) < 1e-12
+
+
+def test_function_is_the_coupled_apply_when_newtonian():
+    """p = 2: eta = B whatever the state, so the function is the penalty-free coupled Jacobian"""
+    fu, fp = pair(k=3, codim=1, seed=2)
+    rng = np.random.default_rng(4)
+    xu, xp = rng.standard_normal(fu.n * 3), rng.standard_normal(fp.n)
+    rheo = (1.6, 0.5, 2.0, 0.25)
+    Fu, Fp = po.stokes_apply(fu, fp, 4, rheo=rheo, xu=xu, xp=xp)
+    Cu, Cp = po.stokes_apply(fu, fp, 3, rheo=rheo, xu=xu, xp=xp)
+    np.testing.assert_allclose(Fu, Cu, rtol=0, atol=1e-14 * np.abs(Cu).max())
+    np.testing.assert_array_equal(Fp, Cp)
+
+
+def test_power_law_jacobian_is_the_derivative_of_the_function():
+    """shear-thinning power law (p = 4/3, Glen n = 3): the Jacobian at the state x (the store eta, eta', Du of
+    StokesPointwiseComputeStore) is the derivative of the function, checked by central differences; its A block
+    stays symmetric positive (eta (p - 1) > 0 along the state's own direction)"""
+    fu, fp = pair(k=2, codim=1, seed=6)
+    rng = np.random.default_rng(8)
+    xu, xp = 2.0 * rng.standard_normal(fu.n * 3), rng.standard_normal(fp.n)
+    vu, vp = rng.standard_normal(fu.n * 3), rng.standard_normal(fp.n)
+    rheo = (1.3, 0.7, 4.0 / 3.0, 0.0)
+    h = 1e-5
+    Fpu, Fpp = po.stokes_apply(fu, fp, 4, rheo=rheo, xu=xu + h * vu, xp=xp + h * vp)
+    Fmu, Fmp = po.stokes_apply(fu, fp, 4, rheo=rheo, xu=xu - h * vu, xp=xp - h * vp)
+    Ju, Jp = po.stokes_apply(fu, fp, 3, rheo=rheo, xu=vu, xp=vp, state=xu)
+    du, dp = (Fpu - Fmu) / (2 * h), (Fpp - Fmp) / (2 * h)
+    assert np.linalg.norm(du - Ju) < 1e-7 * np.linalg.norm(Ju)
+    assert np.linalg.norm(dp - Jp) < 1e-9 * np.linalg.norm(Jp)
+    # the Jacobian really depends on the state: at the zero state it differs
+    J0u, _ = po.stokes_apply(fu, fp, 3, rheo=rheo, xu=vu, xp=vp)
+    assert np.linalg.norm(J0u - Ju) > 1e-2 * np.linalg.norm(Ju)
+    Au, _ = po.stokes_apply(fu, fp, 0, rheo=rheo, xu=vu, state=xu)
+    Aw, _ = po.stokes_apply(fu, fp, 0, rheo=rheo, xu=xu, state=xu)
+    assert abs(xu @ Au - vu @ Aw) < 1e-12 * abs(vu @ Au) and vu @ Au > 0 and xu @ Aw > 0
