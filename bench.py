@@ -66,7 +66,8 @@ def parse():
     ap.add_argument("--config", default="cfg2", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
-    ap.add_argument("--secondary", default="all", help="comma list of apply,learned,newton,multigrid (or all: apply, learned (which includes the multigrid solves), newton)")
+    ap.add_argument("--secondary", default="all", help="comma list of apply,learned,newton,multigrid,stokes (or all: apply, learned (which includes the multigrid "
+                         "solves), newton)")
     ap.add_argument("--learned-ne", type=int, default=64, help="elements per side of the learned-correction solve")
     ap.add_argument("--learned-epochs", type=int, default=8)
     ap.add_argument("--newton-ne", type=int, default=24, help="elements per side of the p-Laplacian Newton run")
@@ -463,6 +464,66 @@ def secondary_multigrid(args):
     return out
 
 
+def secondary_stokes(args):
+    """Stokes with the power-law rheology (p = 4/3, the Glen exponent n = 3; eps = 0.5, B = 1): the nonlinear
+    function and the Jacobian apply at its state on 32^3 elements (Q3-Q2), then Newton from zero with FGMRES and
+    the block preconditioner (one Q1 multigrid V-cycle on the velocity block) on Q3-Q1 spaces with the
+    divergence-free body force f = 10 (sin(pi y) sin(pi z), sin(pi z) sin(pi x), sin(pi x) sin(pi y))."""
+    import math
+    import torch
+    import dohp_gb300 as dg
+    rheo = (1.0, 0.5, 4.0 / 3.0, 0.0)
+    out = {"workload": "stokes power law p=4/3 eps=0.5 B=1", "newton": []}
+
+    def spaces(M, k, codim):
+        fsu = dg.FS((M + 1,) * 3, degree=k, perturb=0.1, seed=7, bs=3)
+        return fsu, dg.FS(None, degree=k - codim, bs=1, dirichlet=(), mesh_of=fsu)
+
+    fsu, fsp = spaces(32, 3, 1)
+    st = dg.Stokes(fsu, fsp, rheo)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    xu = torch.rand(fsu.n * 3, dtype=torch.float64, device="cuda", generator=g) - 0.5
+    xp = torch.rand(fsp.n, dtype=torch.float64, device="cuda", generator=g) - 0.5
+    yu, yp = torch.zeros_like(xu), torch.zeros_like(xp)
+    stream = torch.cuda.default_stream()
+    n = fsu.n * 3 + fsp.n
+    for _ in range(3):
+        st.function(xu, xp, yu, yp)
+    tf, _ = time_loop(lambda: st.function(xu, xp, yu, yp), 10, stream)
+    tj, _ = time_loop(lambda: st.mult(dg.dSTOKES_MULT_COUPLED, xu=xu, xp=xp, yu=yu, yp=yp), 10, stream)
+    out["apply_32^3_q3q2"] = {"dofs": n, "function_ms": tf, "jacobian_ms": tj, "function_gdofs": n / tf / 1e6,
+                              "jacobian_gdofs": n / tj / 1e6}
+    del st, fsu, fsp, xu, xp, yu, yp
+    torch.cuda.empty_cache()
+    for M in (8, 16):
+        fsu, fsp = spaces(M, 3, 2)
+        st = dg.Stokes(fsu, fsp, rheo)
+        it = dg.RulesetIterator(fsu)
+        it.start(None)
+        a = it.get()
+        x = a["x"]
+        sx, sy, sz = (torch.sin(math.pi * x[:, i]) for i in range(3))
+        a["v"].copy_(10.0 * a["jw"][:, None] * torch.stack([sy * sz, sz * sx, sx * sy], 1))
+        it.commit(dg.INSERT_VALUES, use_v=True, use_dv=False)
+        bu = torch.zeros(fsu.n * 3, dtype=torch.float64, device="cuda")
+        it.finish(bu)
+        bp = torch.zeros(fsp.n, dtype=torch.float64, device="cuda")
+        walls = []
+        for rep in range(2):  # the first solve includes the set-up (Q1 matrix, multigrid hierarchy, FGMRES)
+            uu, pp = torch.zeros_like(bu), torch.zeros_like(bp)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            k, fn, li = st.newton(bu, bp, uu, pp, rtol=1e-10, lin_rtol=1e-6, lin_maxit=2000, max_it=40)
+            torch.cuda.synchronize()
+            walls.append(time.perf_counter() - t0)
+        out["newton"].append({"elements": "%d^3" % M, "spaces": "Q3-Q1", "dofs": fsu.n * 3 + fsp.n, "steps": k,
+                              "fnorm": [float(fn[0]), float(fn[-1])], "fgmres_its": [int(v) for v in li],
+                              "wall_s_with_setup": walls[0], "wall_s": walls[1]})
+        del st, it, fsu, fsp
+        torch.cuda.empty_cache()
+    return out
+
+
 def secondary_learned(args):
     """Lognormal Poisson (64^3, p=4, ~16.6 M dofs), time to rtol 1e-8 on a fresh field: FGMRES(30) with the
     Q1 Chebyshev(3)-Jacobi preconditioner in FP64 (plain), with FP32 inner applies (mixed), and with the
@@ -669,6 +730,9 @@ def main():
             torch.cuda.empty_cache()
         if "newton" in which:
             line["newton_mixed_precision"] = secondary_newton(args)
+            torch.cuda.empty_cache()
+        if "stokes" in which:
+            line["stokes_power_law"] = secondary_stokes(args)
             torch.cuda.empty_cache()
     if not args.no_secondary and args.config == "cfg2":
         line["time_to_rtol_cfg1"] = {"workload": "poisson-8^3-p4, mass right-hand side, CG + Q1 Chebyshev(3)-Jacobi, rtol 1e-8",

@@ -38,6 +38,7 @@
 using namespace dgb;
 
 dErr fs_restrict(_p_dFS *fs, const double *x, double *g, int add);
+dErr fs_restrict_rows(_p_dFS *fs, const double *x, double *g, int64_t t0, int64_t t1, cudaStream_t s);
 dErr geometry_fill(_p_dFS *fs, int mode, const double *kq, double *out);
 dErr q1_numeric_elast(_p_dFS *fs, _p_dMat *J, double lam, double mu, int quirk);
 dErr ksp_create_shell(int64_t n, cudaStream_t stream, dKSPType type, dErr (*mult)(void *, const double *, double *),
@@ -358,7 +359,9 @@ static dErr stokes_mult(_p_dStokes *S, int mode, const double *xu, const double 
   A.hexp = 0.5 * (S->p - 2);
   if (fu->nelem) DCHK(launch_stokes(A, S->N, S->NP, mode, fu->nelem, s));
   if (mode != SM_B) DCHK(fs_restrict(fu, S->d_yu, yu, 0));
-  if (mode == SM_B || mode == SM_COUPLED || mode == SM_FUNCTION) DCHK(fs_restrict(fp, S->d_yp, yp, 0));
+  // the pressure restriction runs on the velocity space's stream, after the kernel that wrote d_yp, whatever
+  // stream the pressure space carries
+  if (mode == SM_B || mode == SM_COUPLED || mode == SM_FUNCTION) DCHK(fs_restrict_rows(fp, S->d_yp, yp, 0, fp->n, s));
   if (mode == SM_FUNCTION && S->d_store) S->have_state = true;
   return 0;
 }
@@ -438,7 +441,7 @@ dErr dStokesCreate(dFS fsu, dFS fsp, const dReal rheo[4], dStokes *stk) {
   CUCHK(cudaMalloc(&S->d_s, 8 * sizeof(double)));
   k_fill<<<nblk(S->np), 256, 0, s>>>(S->np, 1.0, S->d_t + S->nu3);  // ones vector for the pressure mean
   DCHK(pmass_diag(S->N, S->NP, fsu->nelem, fsu->d_qoff, fsp->d_xstart, S->d_geo, S->d_bp, S->d_yp, s));
-  DCHK(fs_restrict(fsp, S->d_yp, S->d_mdiag, 0));
+  DCHK(fs_restrict_rows(fsp, S->d_yp, S->d_mdiag, 0, fsp->n, s));
   CUCHK(cudaStreamSynchronize(s));
   *stk = S;
   return 0;
