@@ -434,8 +434,13 @@ class Stokes:
         chk(lib().dStokesMult(self.h, ctypes.c_int(mode), ptr(xu), ptr(xp), ptr(yu), ptr(yp)))
 
     def function(self, xu, xp, yu, yp):
-        """dStokesFunction: (yu, yp) = N(xu, xp); the state of the following Jacobian applies"""
+        """dStokesFunction: (yu, yp) = N(xu, xp) (velocity Dirichlet values from fsu.dirichlet_commit); the state of
+        the following Jacobian applies"""
         chk(lib().dStokesFunction(self.h, ptr(xu), ptr(xp), ptr(yu), ptr(yp)))
+
+    def integrate_pressure(self, fq, yp):
+        """dStokesIntegratePressure: yp = int q f, f at the velocity's quadrature points"""
+        chk(lib().dStokesIntegratePressure(self.h, ptr(fq), ptr(yp)))
 
     def solve(self, bu, bp, xu, xp, rtol=1e-8, maxit=500):
         its, rn = _i32(), _dbl()

@@ -54,11 +54,25 @@ struct StokesArgs {
   const double *bp;  // Bp [N][NP]
   const double *geo; // velocity FAST geometry {J^-1 (9), w det J} per point, SoA per element
   double *store;     // {eta, eta', Du[6]} per velocity point, SoA per element; null: no state (eta constant)
+  const double *udir;  // function mode: Dirichlet values of the velocity closure [(nc - n) * 3] (dFS_INHOMOGENEOUS)
+  const double *fpq;   // pressure-integral mode: the integrand at the velocity's points
   double eta, lam;   // eta without a state
   double B, heps2, hexp;  // rheology: B, eps^2 / 2, (p - 2) / 2
 };
 
-constexpr int SM_A = 0, SM_BT = 1, SM_B = 2, SM_COUPLED = 3, SM_FUNCTION = 4;
+constexpr int SM_A = 0, SM_BT = 1, SM_B = 2, SM_COUPLED = 3, SM_FUNCTION = 4, SM_PINT = 5;
+
+// the velocity gather of the function: closure nodes beyond the explicit ones take the committed Dirichlet values
+// (a uniform space: Boolean E through emap)
+template <int N>
+__device__ __forceinline__ void gather_inhomogeneous(const ElemArgs &A, const double *dir, int64_t first, int ne, int d, double *dst) {
+  constexpr int N3 = N * N * N;
+  for (int t = threadIdx.x; t < ne * N3; t += blockDim.x) {
+    const int el = t / N3, r = t - el * N3;
+    const int32_t c = A.emap[A.xstart[first + el] + r];
+    dst[t] = c < A.n ? A.x[(int64_t)c * 3 + d] : dir[(int64_t)(c - A.n) * 3 + d];
+  }
+}
 
 // dColonSymScalar3 (include/dohp.h:77-78) on [00, 11, 22, 01, 02, 12] storage
 __device__ __forceinline__ double colon_sym(const double *a, const double *b) {
@@ -95,8 +109,9 @@ template <int N, int NP, int MODE>
 __global__ void __launch_bounds__(256) k_stokes(StokesArgs S, int64_t nelem, int cap) {
   extern __shared__ double smem[];
   constexpr int N3 = N * N * N, P3 = NP * NP * NP;
-  constexpr bool USE_U = MODE != SM_BT, USE_P = MODE == SM_BT || MODE == SM_COUPLED || MODE == SM_FUNCTION;
-  constexpr bool OUT_U = MODE != SM_B, OUT_P = MODE == SM_B || MODE == SM_COUPLED || MODE == SM_FUNCTION;
+  constexpr bool USE_U = MODE != SM_BT && MODE != SM_PINT, USE_P = MODE == SM_BT || MODE == SM_COUPLED || MODE == SM_FUNCTION;
+  constexpr bool OUT_U = MODE != SM_B && MODE != SM_PINT;
+  constexpr bool OUT_P = MODE == SM_B || MODE == SM_COUPLED || MODE == SM_FUNCTION || MODE == SM_PINT;
   const int64_t first = (int64_t)blockIdx.x * cap;
   const int ne = (int)min((int64_t)cap, nelem - first);
   double *tab = smem, *bp = smem + kTabElems, *buf = bp + MAXP * MAXP;
@@ -116,7 +131,10 @@ __global__ void __launch_bounds__(256) k_stokes(StokesArgs S, int64_t nelem, int
   }
   if constexpr (USE_U) {
     for (int d = 0; d < 3; d++) {
-      gather<N, double, 3>(S.U, S.U.x, nullptr, first, ne, d, S0);
+      if (MODE == SM_FUNCTION && S.udir)
+        gather_inhomogeneous<N>(S.U, S.udir, first, ne, d, S0);
+      else
+        gather<N, double, 3>(S.U, S.U.x, nullptr, first, ne, d, S0);
       __syncthreads();
       interp3<N, double>(tab, S0, S1, ne);
       grad<N, double>(tab, S1, G + (d * 3 + 0) * L, G + (d * 3 + 1) * L, G + (d * 3 + 2) * L, ne);
@@ -177,7 +195,10 @@ __global__ void __launch_bounds__(256) k_stokes(StokesArgs S, int64_t nelem, int
 #pragma unroll
         for (int k = 0; k < 3; k++) G[(d * 3 + k) * L + t] = Dv[d * 3 + 0] * Ji[k * 3 + 0] + Dv[d * 3 + 1] * Ji[k * 3 + 1] + Dv[d * 3 + 2] * Ji[k * 3 + 2];
     }
-    if constexpr (OUT_P) Pq[t] = -w * tr;
+    if constexpr (MODE == SM_PINT)
+      Pq[t] = w * S.fpq[(int64_t)S.U.qoff[first + el] + r];
+    else if constexpr (OUT_P)
+      Pq[t] = -w * tr;
   }
   __syncthreads();
   if constexpr (OUT_U) {
@@ -268,6 +289,7 @@ dErr launch_stokes_np(const StokesArgs &S, int mode, int64_t nelem, cudaStream_t
     case SM_B: return launch_stokes_mode<N, NP, SM_B>(S, nelem, s);
     case SM_COUPLED: return launch_stokes_mode<N, NP, SM_COUPLED>(S, nelem, s);
     case SM_FUNCTION: return launch_stokes_mode<N, NP, SM_FUNCTION>(S, nelem, s);
+    case SM_PINT: return launch_stokes_mode<N, NP, SM_PINT>(S, nelem, s);
   }
   return set_error("Stokes mult mode %d", mode);
 }
@@ -331,7 +353,8 @@ struct _p_dStokes {
   double *d_pb = nullptr, *d_px = nullptr;  // packed [u; p] right-hand side and iterate of the solve
 };
 
-static dErr stokes_mult(_p_dStokes *S, int mode, const double *xu, const double *xp, double *yu, double *yp) {
+static dErr stokes_mult(_p_dStokes *S, int mode, const double *xu, const double *xp, double *yu, double *yp,
+                        const double *fpq = nullptr) {
   _p_dFS *fu = S->fsu, *fp = S->fsp;
   cudaStream_t s = fu->stream;
   auto eargs = [](_p_dFS *fs, const double *x, double *yexp) {
@@ -351,6 +374,8 @@ static dErr stokes_mult(_p_dStokes *S, int mode, const double *xu, const double 
   A.bp = S->d_bp;
   A.geo = S->d_geo;
   A.store = nullptr;
+  A.udir = mode == SM_FUNCTION && fu->nc > fu->n ? fu->d_dcache : nullptr;
+  A.fpq = fpq;
   if (S->d_store && (mode == SM_FUNCTION || (S->have_state && (mode == SM_A || mode == SM_COUPLED)))) A.store = S->d_store;
   A.eta = S->eta0;
   A.lam = S->lam;
@@ -358,10 +383,11 @@ static dErr stokes_mult(_p_dStokes *S, int mode, const double *xu, const double 
   A.heps2 = 0.5 * S->eps * S->eps;
   A.hexp = 0.5 * (S->p - 2);
   if (fu->nelem) DCHK(launch_stokes(A, S->N, S->NP, mode, fu->nelem, s));
-  if (mode != SM_B) DCHK(fs_restrict(fu, S->d_yu, yu, 0));
+  if (mode != SM_B && mode != SM_PINT) DCHK(fs_restrict(fu, S->d_yu, yu, 0));
   // the pressure restriction runs on the velocity space's stream, after the kernel that wrote d_yp, whatever
   // stream the pressure space carries
-  if (mode == SM_B || mode == SM_COUPLED || mode == SM_FUNCTION) DCHK(fs_restrict_rows(fp, S->d_yp, yp, 0, fp->n, s));
+  if (mode == SM_B || mode == SM_COUPLED || mode == SM_FUNCTION || mode == SM_PINT)
+    DCHK(fs_restrict_rows(fp, S->d_yp, yp, 0, fp->n, s));
   if (mode == SM_FUNCTION && S->d_store) S->have_state = true;
   return 0;
 }
@@ -473,6 +499,11 @@ dErr dStokesMult(dStokes stk, dStokesMultMode mode, const dScalar *xu, const dSc
 dErr dStokesFunction(dStokes stk, const dScalar *xu, const dScalar *xp, dScalar *yu, dScalar *yp) {
   if (!stk || !xu || !xp || !yu || !yp) return set_error("null argument");
   return stokes_mult(stk, SM_FUNCTION, xu, xp, yu, yp);
+}
+
+dErr dStokesIntegratePressure(dStokes stk, const dScalar *fq, dScalar *yp) {
+  if (!stk || !fq || !yp) return set_error("null argument");
+  return stokes_mult(stk, SM_PINT, nullptr, nullptr, nullptr, yp, fq);
 }
 
 }  // extern "C"

@@ -261,8 +261,14 @@ dErr dStokesDestroy(dStokes *stk);
 dErr dStokesMult(dStokes stk, dStokesMultMode mode, const dScalar *xu, const dScalar *xp, dScalar *yu, dScalar *yp);
 /* StokesFunction (stokes.c:507-540, StokesPointwiseFunction 460-474) without the forcing, which the caller puts in
  * the right-hand side: yu = int eta(Du) Dv:Du - p div v, yp = -int q div u; keeps the store {eta, eta', Du} of
- * (xu, xp) as the state of the Jacobian applies */
+ * (xu, xp) as the state of the Jacobian applies. The velocity is expanded dFS_INHOMOGENEOUS, as StokesFunction
+ * does: the Dirichlet nodes take the values committed to fsu by dFSInhomogeneousDirichletCommit (zero when none
+ * were); the Jacobian applies act on homogeneous increments (MatMult_Nest_StokesCoupled, stokes.c:556). */
 dErr dStokesFunction(dStokes stk, const dScalar *xu, const dScalar *xp, dScalar *yu, dScalar *yp);
+/* yp = int q f over the velocity's FAST rule (the rule of the reference's Stokes iterator), f given at its points
+ * in the dRulesetIterator order of fsu: the pressure forcing term int q fp of StokesPointwiseFunction as a
+ * right-hand side */
+dErr dStokesIntegratePressure(dStokes stk, const dScalar *fq, dScalar *yp);
 /* the coupled system (the Jacobian at the current state) solved by FGMRES with the block upper triangular (Schur)
  * preconditioner: velocity block one Q1 multigrid V-cycle (Chebyshev-Jacobi where the GLL lattice does not
  * coarsen) on the Q1-embedded viscous matrix, Schur complement -diag(M_p)/eta (the viscosity-scaled pressure

@@ -1123,6 +1123,50 @@ void or_fs_qpt_coords(const or_fs *m, double *xq)
   }
 }
 
+/* the field of g (closure tail dcache: inhomogeneous Dirichlet values, NULL = 0) at the FAST points in
+ * or_fs_qpt_coords order, as dRulesetIteratorGetPatchApplied yields it (fsrulesetit.c:517-589): u [nq][bs],
+ * du [nq][bs][3] (physical gradient), jw [nq]; any output may be NULL. rule_deg > 0 takes the FAST rule of that
+ * degree instead of the space's own (a second space on the first one's ruleset, as in a multi-field iterator). */
+int or_fs_eval_points(const or_fs *m, int rule_deg, const double *g, const double *dcache, double *u, double *du, double *jw)
+{
+  const int bs = m->bs;
+  double *xe = malloc(sizeof(double) * (size_t)m->nexp * bs);
+  double *jinv = malloc(sizeof(double) * 9 * 1000), *w = malloc(sizeof(double) * 1000);
+  double *tu = malloc(sizeof(double) * 1000 * bs), *tdu = malloc(sizeof(double) * 3000 * bs);
+  or_fs_global_to_expanded(m, g, dcache, xe);
+  int rc = 0;
+  int64_t off = 0;
+  for (int64_t r = 0; r < m->nr && !rc; r++) {
+    basis1d B[3];
+    double fi[3][16 * 16], fd[3][16 * 16], node[16], weight[16];
+    const double *bi[3], *bd[3];
+    int P[3], Q[3];
+    for (int a = 0; a < 3 && !rc; a++) {
+      if (basis_for(0, rule_deg > 0 ? rule_deg : m->edeg[3 * r + a], &B[a])) { rc = -1; break; }
+      P[a] = m->edeg[3 * r + a] + 1, Q[a] = B[a].Q;
+      if (rule_deg > 0) { /* the space's basis at the rule's points */
+        if (or_tensor_basis(P[a], Q[a], B[a].x, fi[a], fd[a], node, weight)) { rc = -1; break; }
+        bi[a] = fi[a], bd[a] = fd[a];
+      } else {
+        bi[a] = B[a].interp, bd[a] = B[a].deriv;
+      }
+    }
+    if (rc) break;
+    const basis1d *b[3] = {&B[0], &B[1], &B[2]};
+    const int nq = Q[0] * Q[1] * Q[2];
+    if ((rc = element_geometry(m, r, b, NULL, jinv, w))) break;
+    const double *xr = xe + (int64_t)m->xstart[r] * bs;
+    or_efs_apply_hex(P, Q, bi, bd, NULL, bs, xr, tu, OR_INTERP, OR_INSERT);
+    or_efs_apply_hex(P, Q, bi, bd, jinv, bs, xr, tdu, OR_GRAD, OR_INSERT);
+    if (u) memcpy(u + off * bs, tu, sizeof(double) * nq * bs);
+    if (du) memcpy(du + off * bs * 3, tdu, sizeof(double) * nq * bs * 3);
+    if (jw) memcpy(jw + off, w, sizeof(double) * nq);
+    off += nq;
+  }
+  free(xe); free(jinv); free(w); free(tu); free(tdu);
+  return rc ? or_fail("negative Jacobian or unsupported degree") : 0;
+}
+
 /* Pointwise q-functions: EllipPointwiseJacobian (ellip.c:369-377; p=2 gives eta=1, s=0) and
  * ElastPointwiseJacobian at F=I (elast.c:269-280: dS = lambda tr(dE) I + 2 mu dE, Dv = F dS + dF S). */
 /* St. Venant-Kirchhoff pieces (elast.c:224-254): column dot, S = lambda tr(E) I + 2 mu E with the Green-Lagrange
@@ -1786,8 +1830,9 @@ static void sym_uncompress(const double s[6], double du[9])
  * The store (StokesPointwiseComputeStore stokes.c:447-453) is evaluated from the velocity state su (NULL: zero).
  * mode 4 is the nonlinear function of StokesFunction (stokes.c:507-540, StokesPointwiseFunction stokes.c:460-474)
  * without the forcing terms: Dv = w (eta(Du) Du - p I), q = -w div u, the store taken from xu itself (su unused). */
-int or_stokes_apply(const or_fs *fu, const or_fs *fp, int mode, const double rheo[4], const double *su, const double *xu,
-                    const double *xp, double *yu, double *yp)
+static int stokes_eval(const or_fs *fu, const or_fs *fp, int mode, const double rheo[4], const double *su, const double *sudir,
+                       const double *xu, const double *udir, const double *xp, const double *fq, const double *fpq, double *yu,
+                       double *yp)
 {
   if (fu->bs != 3 || fp->bs != 1) return or_fail("Stokes needs a bs 3 velocity space and a bs 1 pressure space");
   if (fu->nr != fp->nr) return or_fail("velocity and pressure spaces are on different meshes");
@@ -1796,17 +1841,18 @@ int or_stokes_apply(const or_fs *fu, const or_fs *fp, int mode, const double rhe
   if (mode < 0 || mode > 4) return or_fail("invalid Stokes mode");
   const int use_u = mode != 1, use_p = mode == 1 || mode == 3 || mode == 4;
   const int out_u = mode != 2, out_p = mode >= 2;
-  if (mode == 4) su = xu;
   double *xeu = calloc((size_t)fu->nexp * 3, sizeof(double)), *xep = calloc((size_t)fp->nexp, sizeof(double));
   double *seu = calloc((size_t)fu->nexp * 3, sizeof(double));
   double *yeu = calloc((size_t)fu->nexp * 3, sizeof(double)), *yep = calloc((size_t)fp->nexp, sizeof(double));
-  if (use_u) or_fs_global_to_expanded(fu, xu, NULL, xeu);
+  if (use_u) or_fs_global_to_expanded(fu, xu, udir, xeu);
   if (use_p) or_fs_global_to_expanded(fp, xp, NULL, xep);
-  if (su) or_fs_global_to_expanded(fu, su, NULL, seu);
+  if (mode == 4) memcpy(seu, xeu, sizeof(double) * (size_t)fu->nexp * 3); /* the function's state is its argument */
+  else if (su) or_fs_global_to_expanded(fu, su, sudir, seu);
   double *jinv = malloc(sizeof(double) * 9 * 1000), *jw = malloc(sizeof(double) * 1000);
   double *du = malloc(sizeof(double) * 9000), *ds = malloc(sizeof(double) * 9000), *dv = malloc(sizeof(double) * 9000);
-  double *pq = malloc(sizeof(double) * 1000), *qv = malloc(sizeof(double) * 1000);
+  double *pq = malloc(sizeof(double) * 1000), *qv = malloc(sizeof(double) * 1000), *vq = malloc(sizeof(double) * 3000);
   int rc = 0;
+  int64_t qo = 0; /* offset of the element's first point in fq / fpq */
   for (int64_t r = 0; r < fu->nr && !rc; r++) {
     basis1d bu;
     if (basis_for(0, fu->edeg[3 * r], &bu)) { rc = -1; break; }
@@ -1838,15 +1884,45 @@ int or_stokes_apply(const or_fs *fu, const or_fs *fp, int mode, const double rhe
         }
       }
       sym_uncompress(Dv, dv + 9 * q);
-      qv[q] = -w * tr;
+      /* StokesPointwiseFunction's forcing terms: v = -w fu, q = -w (div u + fp) */
+      qv[q] = -w * (tr + (fpq ? fpq[qo + q] : 0.0));
+      if (fq)
+        for (int c = 0; c < 3; c++) vq[3 * q + c] = -w * fq[3 * (qo + q) + c];
     }
     if (out_u) or_efs_apply_hex(P, Q, bi, bd, jinv, 3, dv, yeu + (int64_t)fu->xstart[r] * 3, OR_GRAD_TRANSPOSE, OR_INSERT);
+    if (out_u && fq) or_efs_apply_hex(P, Q, bi, bd, NULL, 3, vq, yeu + (int64_t)fu->xstart[r] * 3, OR_INTERP_TRANSPOSE, OR_ADD);
     if (out_p) or_efs_apply_hex(Pp, Q, pi3, pd3, NULL, 1, qv, yep + fp->xstart[r], OR_INTERP_TRANSPOSE, OR_INSERT);
+    qo += nq;
   }
   if (!rc) {
     if (out_u) or_fs_expanded_to_global(fu, yeu, yu, 0);
     if (out_p) or_fs_expanded_to_global(fp, yep, yp, 0);
   }
   free(xeu); free(xep); free(seu); free(yeu); free(yep); free(jinv); free(jw); free(du); free(ds); free(dv); free(pq); free(qv);
+  free(vq);
   return rc ? (rc == -1 ? -1 : or_fail("negative Jacobian")) : 0;
+}
+
+int or_stokes_apply(const or_fs *fu, const or_fs *fp, int mode, const double rheo[4], const double *su, const double *xu,
+                    const double *xp, double *yu, double *yp)
+{
+  return stokes_eval(fu, fp, mode, rheo, su, NULL, xu, NULL, xp, NULL, NULL, yu, yp);
+}
+
+/* or_stokes_apply with a state that carries inhomogeneous Dirichlet values sudir ([nc - n][3]); x is expanded
+ * homogeneously (MatMult_Nest_StokesCoupled, stokes.c:556) */
+int or_stokes_apply_state(const or_fs *fu, const or_fs *fp, int mode, const double rheo[4], const double *su, const double *sudir,
+                          const double *xu, const double *xp, double *yu, double *yp)
+{
+  if (mode == 4) return or_fail("the function takes its state from its argument (or_stokes_function)");
+  return stokes_eval(fu, fp, mode, rheo, su, sudir, xu, NULL, xp, NULL, NULL, yu, yp);
+}
+
+/* StokesFunction (stokes.c:507-540) in full: inhomogeneous Dirichlet velocity values udir (closure tail, [nc - n][3],
+ * NULL = 0; dFS_INHOMOGENEOUS expansion) and the forcing fq [nq][3], fpq [nq] at the velocity FAST points in
+ * or_fs_qpt_coords order (NULL = 0) */
+int or_stokes_function(const or_fs *fu, const or_fs *fp, const double rheo[4], const double *xu, const double *udir,
+                       const double *xp, const double *fq, const double *fpq, double *yu, double *yp)
+{
+  return stokes_eval(fu, fp, 4, rheo, NULL, NULL, xu, udir, xp, fq, fpq, yu, yp);
 }

@@ -102,6 +102,9 @@ int or_operator_apply(const or_fs *fs, int kind, const double *qdata, const doub
 int64_t or_fs_num_qpts(const or_fs *fs, int32_t *qoffset);
 /* Physical coordinates of FAST quadrature points [nq][3] (coordinate-FS INTERP). */
 void or_fs_qpt_coords(const or_fs *fs, double *xq);
+/* the field of g (+ Dirichlet values dcache, NULL = 0) at those points: u [nq][bs], physical du [nq][bs][3], jw [nq];
+ * rule_deg > 0: at the FAST rule of that degree instead (the points of another space on the same mesh) */
+int or_fs_eval_points(const or_fs *fs, int rule_deg, const double *g, const double *dcache, double *u, double *du, double *jw);
 /* p-Laplacian residual stash (ellip.c:333-367) from the global state g (homogeneous Dirichlet):
  * writes [eta, sqrt_mdeta_Du[3]] per FAST qpt. */
 int or_plap_stash(const or_fs *fs, double p, double eps, const double *g, double *stash);
@@ -142,6 +145,13 @@ int or_facet_commit(const or_fs *fs, int weak_mask, const double *v, double *y, 
  * state su (NULL: zero). */
 int or_stokes_apply(const or_fs *fu, const or_fs *fp, int mode, const double rheo[4], const double *su, const double *xu,
                     const double *xp, double *yu, double *yp);
+/* the full nonlinear function (mode 4 with the reference's forcing terms and inhomogeneous Dirichlet velocity
+ * values): udir [nc - n][3] (NULL = 0), fq [nq][3] and fpq [nq] at the points of or_fs_qpt_coords (NULL = 0) */
+int or_stokes_function(const or_fs *fu, const or_fs *fp, const double rheo[4], const double *xu, const double *udir,
+                       const double *xp, const double *fq, const double *fpq, double *yu, double *yp);
+/* modes 0-3 at a velocity state su whose closure carries the Dirichlet values sudir [nc - n][3] */
+int or_stokes_apply_state(const or_fs *fu, const or_fs *fp, int mode, const double rheo[4], const double *su, const double *sudir,
+                          const double *xu, const double *xp, double *yu, double *yp);
 
 /* deformation gradient F = I + Du [nq][9] at every FAST point of the state g (bs = 3, homogeneous Dirichlet;
  * ElastPointwiseComputeStore, elast.c:224-225) */

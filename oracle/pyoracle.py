@@ -99,6 +99,9 @@ def lib():
         L.or_facet_points.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, _f64p, _f64p, _f64p, _f64p]
         L.or_facet_commit.argtypes = [ctypes.c_void_p, ctypes.c_int, _f64p, _f64p, ctypes.c_int]
         L.or_stokes_apply.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _f64p] + [ctypes.c_void_p] * 5
+        L.or_fs_eval_points.argtypes = [ctypes.c_void_p, ctypes.c_int, _f64p] + [ctypes.c_void_p] * 4
+        L.or_stokes_function.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _f64p] + [ctypes.c_void_p] * 7
+        L.or_stokes_apply_state.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _f64p] + [ctypes.c_void_p] * 6
         _lib = L
     return _lib
 
@@ -270,6 +273,20 @@ class FS:
         lib().or_fs_qpt_coords(self.h, xq)
         return xq.reshape(nq, 3)
 
+    def eval_points(self, g, dcache=None, rule_deg=0):
+        """(u [nq, bs], du [nq, bs, 3], jw [nq]) of the field g (+ Dirichlet values dcache) at qpt_coords(), or at the
+        FAST points of degree rule_deg (uniform spaces)"""
+        if rule_deg > 0:
+            nq = self.nelem * (rule_deg + 1) ** 3
+        else:
+            nq, _ = self.num_qpts()
+        u, du, jw = np.zeros(nq * self.bs), np.zeros(nq * self.bs * 3), np.zeros(nq)
+        dc = None if dcache is None else np.ascontiguousarray(dcache, dtype=np.float64)
+        if lib().or_fs_eval_points(self.h, rule_deg, np.ascontiguousarray(g, dtype=np.float64), None if dc is None else dc.ctypes.data,
+                                   u.ctypes.data, du.ctypes.data, jw.ctypes.data):
+            raise RuntimeError(lib().or_last_error().decode())
+        return u.reshape(nq, self.bs), du.reshape(nq, self.bs, 3), jw
+
     def apply(self, g, kind=0, qdata=None, param=None, nthreads=1):
         y = np.zeros(self.n * self.bs)
         qd = None if qdata is None else np.ascontiguousarray(qdata, dtype=np.float64)
@@ -364,13 +381,31 @@ def facet_rule(side, order, method=0):
     return nodes[:3 * n].reshape(n, 3), w[:n]
 
 
-def stokes_apply(fu, fp, mode, rheo=(1.0, 1.0, 2.0, 0.0), xu=None, xp=None, state=None):
-    """(yu, yp) of the Stokes block apply: mode 0 A, 1 Bt, 2 B, 3 coupled (Jacobian at the velocity state), 4 the
-    nonlinear function at xu, xp"""
+def stokes_apply(fu, fp, mode, rheo=(1.0, 1.0, 2.0, 0.0), xu=None, xp=None, state=None, state_dir=None):
+    """(yu, yp) of the Stokes block apply: mode 0 A, 1 Bt, 2 B, 3 coupled (Jacobian at the velocity state, whose
+    Dirichlet values are state_dir [nc - n, 3], None = 0), 4 the nonlinear function at xu, xp"""
     yu, yp = np.zeros(fu.n * 3), np.zeros(fp.n)
-    keep = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (state, xu, xp)]
+    if state_dir is None:
+        keep = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (state, xu, xp)]
+        addr = [None if a is None else a.ctypes.data for a in keep]
+        rc = lib().or_stokes_apply(fu.h, fp.h, mode, np.asarray(rheo, np.float64), *addr, yu.ctypes.data, yp.ctypes.data)
+    else:
+        keep = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (state, state_dir, xu, xp)]
+        addr = [None if a is None else a.ctypes.data for a in keep]
+        rc = lib().or_stokes_apply_state(fu.h, fp.h, mode, np.asarray(rheo, np.float64), *addr, yu.ctypes.data,
+                                         yp.ctypes.data)
+    if rc:
+        raise RuntimeError(lib().or_last_error().decode())
+    return yu, yp
+
+
+def stokes_function(fu, fp, rheo, xu, xp, udir=None, fq=None, fpq=None):
+    """(yu, yp) of StokesFunction: Dirichlet velocity values udir [nc - n, 3], forcing fq [nq, 3] and fpq [nq] at
+    fu.qpt_coords() (None = 0)"""
+    yu, yp = np.zeros(fu.n * 3), np.zeros(fp.n)
+    keep = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (xu, udir, xp, fq, fpq)]
     addr = [None if a is None else a.ctypes.data for a in keep]
-    if lib().or_stokes_apply(fu.h, fp.h, mode, np.asarray(rheo, np.float64), *addr, yu.ctypes.data, yp.ctypes.data):
+    if lib().or_stokes_function(fu.h, fp.h, np.asarray(rheo, np.float64), *addr, yu.ctypes.data, yp.ctypes.data):
         raise RuntimeError(lib().or_last_error().decode())
     return yu, yp
 

@@ -124,6 +124,26 @@ def bu0(root):
     }
 
 
+def stokes(root, name):
+    """stokes-q3q2-{scr,fgmres} (src/fs/tests/CMakeLists.txt:62-70, the Exact1 case on the default 4^3 block of
+    [-1,1]^3): residual norms at the nodal interpolant of the exact solution, the first SNES function norm, and
+    the five norm triples printed after the solve (stokes.c:1128-1133, 1161-1169)."""
+    lines = read(root, f"src/fs/tests/refout/{name}.refout")
+    out = {}
+    for ln in lines:
+        m = re.match(r"Norm of discrete (linear )?residual (?:for|at) exact solution (\S+)", ln)
+        if m:
+            out["linear_residual_exact" if m.group(1) else "residual_exact"] = np.array([float(m.group(2))])
+        m = re.match(r"\s*0 SNES Function norm (\S+)", ln)
+        if m and "fnorm0" not in out:
+            out["fnorm0"] = np.array([float(m.group(1))])
+        m = re.match(r"(Algebraic|Interpolation) residual\s+\|x\|_1 (\S+)\s+\|x\|_2 (\S+)\s+\|x\|_inf (\S+)", ln)
+        m = m or re.match(r"Pointwise (velocity|gradient|pressure) error\s+\|x\|_1 (\S+)\s+\|x\|_2 (\S+)\s+\|x\|_inf (\S+)", ln)
+        if m:
+            out[m.group(1).lower()] = np.array([float(m.group(k)) for k in (2, 3, 4)])
+    return out
+
+
 def main(root):
     fixtures = {
         "jacobi3_gauss": explicit_bases(root, "jacobi-3-tensor-gauss"),
@@ -135,6 +155,8 @@ def main(root):
         "jacobi1_gauss": interp_errors(root, "jacobi-1"),
         "jacobi1_lobatto": interp_errors(root, "jacobi-1-lobatto"),
         "bu0": bu0(root),
+        "stokes_q3q2_scr": stokes(root, "stokes-q3q2-scr"),
+        "stokes_q3q2_fgmres": stokes(root, "stokes-q3q2-fgmres"),
     }
     meta = {}
     for name, arrs in fixtures.items():

@@ -191,3 +191,57 @@ def test_power_law_newton_recovers_a_discrete_solution():
     rp = float(torch.linalg.norm(xp - xs_p) / torch.linalg.norm(xs_p))
     assert ru < 1e-7 and rp < 1e-6, (ru, rp, k, fn)
     assert abs(float(xp.sum())) < 1e-10
+
+
+def test_reference_stokes_targets_through_the_product():
+    """the reference's two Stokes targets (src/fs/tests/CMakeLists.txt:62-70; the problem and the oracle side are in
+    tests/test_oracle_stokes_golden.py) through the product: Dirichlet values of the exact solution committed to the
+    velocity space, the forcing integrated by the iterator (velocity) and dStokesIntegratePressure on the same rule,
+    dStokesFunction and the Jacobian at its state reproduce the printed residual norms to six digits, and
+    dStokesNewtonSolve's solution reproduces the printed error norms"""
+    import test_oracle_stokes_golden as G
+    here = os.path.dirname(os.path.abspath(__file__))
+    for name, rheo in sorted(G.CASES.items()):
+        ref = np.load(os.path.join(here, "golden", name + ".npz"))
+        O = G.Problem(rheo)
+        fsu = dg.FS((5, 5, 5), degree=3, box=G.BOX, perturb=0.0, seed=1, bs=3)
+        fsp = dg.FS(None, degree=2, bs=1, dirichlet=(), mesh_of=fsu)
+        assert (fsu.n, fsu.nc, fsp.n) == (O.fu.n, O.fu.nc, O.fp.n)
+        nu3 = O.nu3
+        fsu.dirichlet_commit(dev(np.concatenate([O.s[:nu3], O.ud])))
+        st = dg.Stokes(fsu, fsp, rheo)
+        it = dg.RulesetIterator(fsu)
+        it.start(None)
+        a = it.get()
+        np.testing.assert_allclose(a["x"].cpu().numpy(), O.xq, rtol=0, atol=1e-14)
+        a["v"].copy_(a["jw"][:, None] * dev(O.fq))
+        it.commit(dg.INSERT_VALUES, use_v=True, use_dv=False)
+        bu = torch.zeros(nu3, dtype=torch.float64, device="cuda")
+        it.finish(bu)
+        bp = torch.zeros(fsp.n, dtype=torch.float64, device="cuda")
+        st.integrate_pressure(dev(O.fpq), bp)
+        yu, yp = torch.zeros_like(bu), torch.zeros_like(bp)
+
+        def F(x):
+            st.function(dev(x[:nu3]), dev(x[nu3:]), yu, yp)
+            return np.concatenate([host(yu) - host(bu), host(yp) - host(bp)])
+
+        rel = lambda a, b: abs(a - b) / abs(b)
+        F0 = F(np.zeros_like(O.s))
+        assert rel(np.linalg.norm(F0), ref["fnorm0"][0]) < 3e-6, name
+        Fs = F(O.s)  # leaves the state at s
+        assert rel(np.linalg.norm(Fs), ref["residual_exact"][0]) < 3e-6, name
+        np.testing.assert_allclose(Fs, O.F(O.s), rtol=0, atol=1e-12 * np.linalg.norm(Fs))
+        st.mult(dg.dSTOKES_MULT_COUPLED, xu=dev(O.s[:nu3]), xp=dev(O.s[nu3:]), yu=yu, yp=yp)
+        lin = np.concatenate([host(yu), host(yp)]) + F0
+        assert rel(np.linalg.norm(lin), ref["linear_residual_exact"][0]) < 3e-6, name
+        # the solve: from zero for the linear (Newtonian) target, from the interpolant for the power law
+        x0 = np.zeros_like(O.s) if rheo[2] == 2.0 else O.s
+        xu, xp = dev(x0[:nu3]), dev(x0[nu3:])
+        k, fn, li = st.newton(bu, bp, xu, xp, rtol=1e-9, atol=1e-12, lin_rtol=1e-9, lin_maxit=3000, max_it=20)
+        assert fn[-1] <= max(1e-9 * fn[0], 1e-12), (name, k, fn, li)
+        x = np.concatenate([host(xu), host(xp)])
+        assert np.linalg.norm(O.F(x)) < 1e-8, name  # the oracle's residual of the product's solution
+        got = O.norms(x)
+        for key in ("interpolation", "velocity", "gradient", "pressure"):
+            np.testing.assert_allclose(got[key], ref[key], rtol=0.012, err_msg=name + " " + key)
