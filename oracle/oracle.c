@@ -1233,6 +1233,12 @@ static void qfunction(int kind, int D, const double *qd, const double *param, do
     mult_gesy3(dv, du, S, 1);
     for (int i = 0; i < 9; i++) dv[i] *= w;
     v[0] = v[1] = v[2] = 0;
+  } else if (kind == 6) { /* EllipPointwiseFunction (ellip.c:355-367) without forcing, lambda = 0: Dv = w eta Du */
+    const double pe = param[0], eps = param[1];
+    const double gamma = 0.5 * (du[0] * du[0] + du[1] * du[1] + du[2] * du[2]);
+    const double etaw = pow(eps * eps + gamma, (pe - 2) / 2) * w;
+    v[0] = 0;
+    for (int i = 0; i < 3; i++) dv[i] = etaw * du[i];
   } else if (kind == 3) { /* mass: the right-hand side b = int v f_h of src/fs/tests/ex1.c:399-430 */
     v[0] = w * u[0];
     dv[0] = dv[1] = dv[2] = 0;
@@ -1257,8 +1263,8 @@ static void qfunction(int kind, int D, const double *qd, const double *param, do
   }
 }
 
-int or_operator_apply(const or_fs *m, int kind, const double *qdata, const double *param,
-                      const double *g, double *y, int nthreads)
+static int operator_eval(const or_fs *m, int kind, const double *qdata, const double *param, const double *g,
+                         const double *dcache, const double *fq, double *y, int nthreads)
 {
   const int bs = m->bs, D = bs;
   const int elastic = kind == 2 || kind == 4 || kind == 5;
@@ -1268,7 +1274,7 @@ int or_operator_apply(const or_fs *m, int kind, const double *qdata, const doubl
   double *xexp = malloc(sizeof(double) * m->nexp * bs), *yexp = malloc(sizeof(double) * m->nexp * bs);
   int32_t *qoff = malloc(sizeof(int32_t) * (m->nr + 1));
   or_fs_num_qpts(m, qoff);
-  or_fs_global_to_expanded(m, g, NULL, xexp);
+  or_fs_global_to_expanded(m, g, dcache, xexp);
   int err = 0;
 #ifdef _OPENMP
   if (nthreads < 1) nthreads = 1;
@@ -1297,6 +1303,8 @@ int or_operator_apply(const or_fs *m, int kind, const double *qdata, const doubl
         if (kind == 1) qd = qdata + 4 * (int64_t)(qoff[r] + q);
         if (kind == 5) qd = qdata + 9 * (int64_t)(qoff[r] + q);
         qfunction(kind, D, qd, param, jw[q], u + q * D, du + q * 3 * D, v + q * D, dv + q * 3 * D);
+        if (fq) /* body force: the coefficient of v is -w f (ellip.c:362, elast.c:261) */
+          for (int c = 0; c < D; c++) v[q * D + c] += -jw[q] * fq[(int64_t)(qoff[r] + q) * D + c];
       }
       or_efs_apply_hex(P, Q, bi, bd, jinv, D, v, ye, OR_INTERP_TRANSPOSE, OR_INSERT);
       or_efs_apply_hex(P, Q, bi, bd, jinv, D, dv, ye, OR_GRAD_TRANSPOSE, OR_ADD);
@@ -1306,6 +1314,19 @@ int or_operator_apply(const or_fs *m, int kind, const double *qdata, const doubl
   if (!err) or_fs_expanded_to_global(m, yexp, y, 0);
   free(xexp); free(yexp); free(qoff);
   return err ? or_fail("negative Jacobian") : 0;
+}
+
+int or_operator_apply(const or_fs *m, int kind, const double *qdata, const double *param,
+                      const double *g, double *y, int nthreads)
+{
+  return operator_eval(m, kind, qdata, param, g, NULL, NULL, y, nthreads);
+}
+
+int or_operator_function(const or_fs *m, int kind, const double *param, const double *g, const double *dcache,
+                         const double *fq, double *y, int nthreads)
+{
+  if (kind != 4 && kind != 6) return or_fail("or_operator_function: kind 4 (St. Venant-Kirchhoff) or 6 (p-Laplacian)");
+  return operator_eval(m, kind, NULL, param, g, dcache, fq, y, nthreads);
 }
 
 /* EllipPointwiseComputeStore (ellip.c:333-342) at the FAST points from the state g. */

@@ -95,9 +95,15 @@ void or_fs_expanded_to_global(const or_fs *fs, const double *x, double *g, int a
  * kind 3: mass, v = w u (the right-hand side of ex1.c:399-430 and of configuration 1)
  * kind 4: St. Venant-Kirchhoff function at the state g (ElastPointwiseFunction, elast.c:256-266, no body force)
  * kind 5: St. Venant-Kirchhoff Jacobian at the stashed deformation gradients qdata [nq][9] (elast.c:268-280)
+ * kind 6: p-Laplacian function, param = {p, eps} (EllipPointwiseFunction, ellip.c:355-367, lambda = 0, no forcing)
  * nthreads: OpenMP threads over element ranges (the reference runs one MPI rank per core). */
 int or_operator_apply(const or_fs *fs, int kind, const double *qdata, const double *param,
                       const double *g, double *y, int nthreads);
+/* EllipFunction / ElastFunction (ellip.c:407-440, elast.c:282-309) in full: kind 6 or 4 at the state g expanded
+ * dFS_INHOMOGENEOUS with the Dirichlet values dcache ([nc - n][bs], NULL = 0), the body force fq [nq][bs] at the
+ * points of or_fs_qpt_coords (NULL = 0) entering as v = -w f */
+int or_operator_function(const or_fs *fs, int kind, const double *param, const double *g, const double *dcache,
+                         const double *fq, double *y, int nthreads);
 /* Number of FAST quadrature points over all elements and per-element offsets (nelem+1). */
 int64_t or_fs_num_qpts(const or_fs *fs, int32_t *qoffset);
 /* Physical coordinates of FAST quadrature points [nq][3] (coordinate-FS INTERP). */

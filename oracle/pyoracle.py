@@ -99,6 +99,8 @@ def lib():
         L.or_facet_points.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, _f64p, _f64p, _f64p, _f64p]
         L.or_facet_commit.argtypes = [ctypes.c_void_p, ctypes.c_int, _f64p, _f64p, ctypes.c_int]
         L.or_stokes_apply.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _f64p] + [ctypes.c_void_p] * 5
+        L.or_operator_function.argtypes = [ctypes.c_void_p, ctypes.c_int, _f64p, _f64p, ctypes.c_void_p, ctypes.c_void_p,
+                                           _f64p, ctypes.c_int]
         L.or_fs_eval_points.argtypes = [ctypes.c_void_p, ctypes.c_int, _f64p] + [ctypes.c_void_p] * 4
         L.or_stokes_function.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _f64p] + [ctypes.c_void_p] * 7
         L.or_stokes_apply_state.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _f64p] + [ctypes.c_void_p] * 6
@@ -272,6 +274,16 @@ class FS:
         xq = np.zeros(nq * 3)
         lib().or_fs_qpt_coords(self.h, xq)
         return xq.reshape(nq, 3)
+
+    def function(self, g, kind, param, dcache=None, fq=None, nthreads=1):
+        """or_operator_function: EllipFunction (kind 6, param (p, eps)) or ElastFunction (kind 4, param (lambda, mu))
+        with the Dirichlet values dcache and the body force fq at qpt_coords()"""
+        y = np.zeros(self.n * self.bs)
+        keep = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (dcache, fq)]
+        if lib().or_operator_function(self.h, kind, np.asarray(param, np.float64), np.ascontiguousarray(g, np.float64),
+                                      *[None if a is None else a.ctypes.data for a in keep], y, nthreads):
+            raise RuntimeError(lib().or_last_error().decode())
+        return y
 
     def eval_points(self, g, dcache=None, rule_deg=0):
         """(u [nq, bs], du [nq, bs, 3], jw [nq]) of the field g (+ Dirichlet values dcache) at qpt_coords(), or at the

@@ -124,10 +124,11 @@ def bu0(root):
     }
 
 
-def stokes(root, name):
-    """stokes-q3q2-{scr,fgmres} (src/fs/tests/CMakeLists.txt:62-70, the Exact1 case on the default 4^3 block of
-    [-1,1]^3): residual norms at the nodal interpolant of the exact solution, the first SNES function norm, and
-    the five norm triples printed after the solve (stokes.c:1128-1133, 1161-1169)."""
+def solver_log(root, name):
+    """stokes-q3q2-{scr,fgmres}, ellip-e0-*, elast-e0-b3-g01 (src/fs/tests/CMakeLists.txt:49-70, manufactured
+    solutions on the default 4^3 block of [-1,1]^3): residual norms at the nodal interpolant of the exact solution
+    (Stokes only), the first SNES function norm (at zero with the exact Dirichlet values), and the norm triples
+    printed after the solve (stokes.c:1128-1133, 1161-1169; ellip.c:750-757; elast.c:539-546)."""
     lines = read(root, f"src/fs/tests/refout/{name}.refout")
     out = {}
     for ln in lines:
@@ -138,7 +139,7 @@ def stokes(root, name):
         if m and "fnorm0" not in out:
             out["fnorm0"] = np.array([float(m.group(1))])
         m = re.match(r"(Algebraic|Interpolation) residual\s+\|x\|_1 (\S+)\s+\|x\|_2 (\S+)\s+\|x\|_inf (\S+)", ln)
-        m = m or re.match(r"Pointwise (velocity|gradient|pressure) error\s+\|x\|_1 (\S+)\s+\|x\|_2 (\S+)\s+\|x\|_inf (\S+)", ln)
+        m = m or re.match(r"Pointwise (velocity|solution|gradient|pressure) error\s+\|x\|_1 (\S+)\s+\|x\|_2 (\S+)\s+\|x\|_inf (\S+)", ln)
         if m:
             out[m.group(1).lower()] = np.array([float(m.group(k)) for k in (2, 3, 4)])
     return out
@@ -155,8 +156,12 @@ def main(root):
         "jacobi1_gauss": interp_errors(root, "jacobi-1"),
         "jacobi1_lobatto": interp_errors(root, "jacobi-1-lobatto"),
         "bu0": bu0(root),
-        "stokes_q3q2_scr": stokes(root, "stokes-q3q2-scr"),
-        "stokes_q3q2_fgmres": stokes(root, "stokes-q3q2-fgmres"),
+        "stokes_q3q2_scr": solver_log(root, "stokes-q3q2-scr"),
+        "stokes_q3q2_fgmres": solver_log(root, "stokes-q3q2-fgmres"),
+        "ellip_e0_b1_p16": solver_log(root, "ellip-e0-b1-p16"),
+        "ellip_e0_b3_p16": solver_log(root, "ellip-e0-b3-p16"),
+        "ellip_e0_b3_p14": solver_log(root, "ellip-e0-b3-p14-sse"),
+        "elast_e0_b3_g01": solver_log(root, "elast-e0-b3-g01"),
     }
     meta = {}
     for name, arrs in fixtures.items():

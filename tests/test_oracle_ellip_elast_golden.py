@@ -1,0 +1,139 @@
+"""The oracle's p-Laplacian and St. Venant-Kirchhoff paths pinned to the reference's own outputs for its ellip and
+elast test targets (src/fs/tests/CMakeLists.txt:49-58; expected output src/fs/tests/refout/ellip-e0-*.refout and
+elast-e0-b3-g01.refout, extracted into tests/golden/ by make_golden.py): exact solution 0 of each program on the
+default block mesh (5^3 vertices on [-1,1]^3, src/fs/mesh/interface/genblock.c:169) with Dirichlet values on all
+walls (sets 100, 200, 300).
+
+  ellip-e0-b{1,3}-p16, -b3-p14: u = cos(a x) exp(b y) sin(c z), (a, b, c) = (1.6, 1.7, 1.8) (ellip.c:42-57), the
+    p-Laplacian with eps = 1 (ellip.c:153-161) at p = 1.6 / 1.4, degree 1 or 3;
+  elast-e0-b3-g01: ElastExact_0 (elastexact.py:74-79), (a, b, c) = (0.98, 1.01, 1.01), E = 1, nu = 0.3
+    (elast.c:91-96, 99-110), degree 3.
+
+The forcing of each is the strong residual of the program's weak form, written here with sympy from the exact
+solution (ellip.c:42-48: f = -div(eta grad u), eta = (eps^2 + |grad u|^2 / 2)^((p-2)/2); elastexact.py:14-25 with
+the conversion of dohpexact.py:115-134: f = -div(F S)). Without a solve: ||F(0)||, the first SNES function norm
+(six printed digits). After solving to roundoff (exact Jacobians from the oracle's applies at the stored state,
+chord iteration from the interpolant): the interpolation residual and the pointwise solution and gradient error
+norms (ellip.c:538-566, 750-757; elast.c:409-438, 539-546; three printed digits)."""
+import os
+
+import numpy as np
+import pytest
+import scipy.linalg as sl
+
+import pyoracle as po
+from test_oracle_stokes_golden import BOX, closure_coords, columns
+
+sp = pytest.importorskip("sympy")
+HERE = os.path.dirname(os.path.abspath(__file__))
+X = sp.symbols("x0:3")
+
+
+def ellip_exact(a, b, c, pe, eps):
+    x, y, z = X
+    u = sp.cos(a * x) * sp.exp(b * y) * sp.sin(c * z)
+    g = [sp.diff(u, v) for v in X]
+    eta = (eps ** 2 + sum(t ** 2 for t in g) / 2) ** ((pe - 2) / 2)
+    f = -sum(sp.diff(eta * g[i], X[i]) for i in range(3))
+    return sp.lambdify(X, [[u], [f], g], "numpy")
+
+
+def elast_exact(a, b, c, lam, mu):
+    x, y, z = X
+    u = sp.Matrix([sp.cos(a * x) * sp.exp(b * y) * z + sp.sin(c * z), sp.sin(a * x) * sp.tanh(b * y) + x * sp.cosh(c * z),
+                   sp.exp(a * x) * sp.sinh(b * y) + y * sp.log(1 + (c * z) ** 2)])
+    H = u.jacobian(X)
+    F = sp.eye(3) + H
+    E = (F.T * F - sp.eye(3)) / 2
+    P = F * (lam * E.trace() * sp.eye(3) + 2 * mu * E)  # first Piola-Kirchhoff stress
+    f = [-sum(sp.diff(P[i, j], X[j]) for j in range(3)) for i in range(3)]
+    return sp.lambdify(X, [list(u), f, list(H)], "numpy")
+
+
+NU = 0.3
+LAM, MU = NU / ((1 + NU) * (1 - 2 * NU)), 1 / (2 * (1 + NU))  # ElastSetMaterial (elast.c:91-96), E = 1
+CASES = {  # name: (degree, bs, function kind, param, exact)
+    "ellip_e0_b1_p16": (1, 1, 6, (1.6, 1.0), lambda: ellip_exact(1.6, 1.7, 1.8, 1.6, 1.0)),
+    "ellip_e0_b3_p16": (3, 1, 6, (1.6, 1.0), lambda: ellip_exact(1.6, 1.7, 1.8, 1.6, 1.0)),
+    "ellip_e0_b3_p14": (3, 1, 6, (1.4, 1.0), lambda: ellip_exact(1.6, 1.7, 1.8, 1.4, 1.0)),
+    "elast_e0_b3_g01": (3, 3, 4, (LAM, MU), lambda: elast_exact(0.98, 1.01, 1.01, LAM, MU)),
+}
+
+
+class Problem:
+    def __init__(self, degree, bs, kind, param, exact):
+        self.bs, self.kind, self.param = bs, kind, param
+        self.fs = po.FS(5, 5, 5, degree=degree, box=BOX, perturb=0.0, seed=1, bs=bs, dirichlet_mask=7)
+        f = exact()
+        Xc = closure_coords(self.fs, degree + 1)
+        U = columns(f(*Xc.T)[0], len(Xc))
+        self.s = U[:self.fs.n].ravel()
+        self.dc = U[self.fs.n:].ravel()
+        xq = self.fs.qpt_coords()
+        r = f(*xq.T)
+        nq = len(xq)
+        self.fq = columns(r[1], nq)
+        self.ue, self.due = columns(r[0], nq), columns(r[2], nq).reshape(nq, bs, 3)
+
+    def F(self, x):
+        return self.fs.function(x, self.kind, self.param, dcache=self.dc, fq=self.fq)
+
+    def qdata(self, x):
+        """the Jacobian's store at the state x with the Dirichlet values: [eta, sqrt(-eta') Du] of
+        EllipPointwiseComputeStore (ellip.c:333-342), or the deformation gradient I + Du (elast.c:224-225)"""
+        _, du, _ = self.fs.eval_points(x, self.dc)
+        if self.kind == 6:
+            pe, eps = self.param
+            g = du[:, 0, :]
+            espg = eps ** 2 + 0.5 * (g ** 2).sum(1)
+            eta = espg ** ((pe - 2) / 2)
+            return np.concatenate([eta[:, None], np.sqrt(-(pe - 2) / 2 * eta / espg)[:, None] * g], 1).ravel()
+        return (np.eye(3)[None] + du).reshape(-1)
+
+    def solve(self):
+        n = self.s.size
+        qd = self.qdata(self.s)
+        J = np.zeros((n, n))
+        e = np.zeros(n)
+        for j in range(n):
+            e[j] = 1
+            J[:, j] = self.fs.apply(e, kind=1 if self.kind == 6 else 5, qdata=qd, param=self.param)
+            e[j] = 0
+        lu = sl.lu_factor(J)
+        x = self.s.copy()
+        for _ in range(40):
+            Fx = self.F(x)
+            if np.linalg.norm(Fx) < 1e-12 * max(1.0, np.linalg.norm(self.F(np.zeros(n)))):
+                break
+            x = x - sl.lu_solve(lu, Fx)
+        return x
+
+    def norms(self, x):
+        d = x - self.s
+        n = d.size // self.bs  # dNormsAlgebraicScaled divides by the number of blocks (util.c:155-171)
+        out = {"interpolation": np.array([np.abs(d).sum() / n, np.linalg.norm(d) / np.sqrt(n), np.abs(d).max()])}
+        uh, duh, jw = self.fs.eval_points(x, self.dc)
+        e = self.ue - uh
+        out["solution"] = np.array([(np.abs(e).sum(1) * jw).sum(), np.sqrt(((e ** 2).sum(1) * jw).sum()), np.abs(e).max()])
+        g = np.sqrt(((self.due - duh) ** 2).sum(2))
+        out["gradient"] = np.array([(g * jw[:, None]).sum(), np.sqrt((g ** 2 * jw[:, None]).sum()), g.max()])
+        return out
+
+
+@pytest.fixture(scope="module", params=sorted(CASES))
+def case(request):
+    g = np.load(os.path.join(HERE, "golden", request.param + ".npz"))
+    return request.param, Problem(*CASES[request.param]), {k: g[k] for k in g}
+
+
+def test_first_function_norm(case):
+    name, P, ref = case
+    got = np.linalg.norm(P.F(np.zeros_like(P.s)))
+    assert abs(got - ref["fnorm0"][0]) < 3e-6 * ref["fnorm0"][0], (name, got)
+
+
+def test_solution_error_norms(case):
+    name, P, ref = case
+    got = P.norms(P.solve())
+    for key in ("interpolation", "solution", "gradient"):
+        np.testing.assert_allclose(got[key], ref[key], rtol=0.006, err_msg=name + " " + key)  # the printed digits
