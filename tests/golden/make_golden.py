@@ -124,6 +124,37 @@ def bu0(root):
     }
 
 
+def sparse_efs(root, name="jacobi-3-tensor-sparse-gauss"):
+    """jacobi-3-tensor-sparse-gauss (src/jacobi/tests/CMakeLists.txt:13, -just_view): per element basis size P, the
+    first direction's SPARSE rule (points, weights) and the basis at it (interp, deriv rows, nodes)."""
+    lines = read(root, f"src/jacobi/tests/refout/{name}.refout")
+    out = {}
+    i = 0
+    rule = None
+    while i < len(lines):
+        ln = lines[i]
+        m = re.match(r"\s*TensorRule with (\d+) nodes", ln)
+        if m and rule is None:
+            q = [float(v) for v in lines[i + 1].split("]")[-1].split()]
+            w = [float(v) for v in lines[i + 2].split("]")[-1].split()]
+            rule = (q, w)
+        m = re.match(r"TensorBasis with rule=(\d+) basis=(\d+)", ln)
+        if m:
+            Q, P = int(m.group(1)), int(m.group(2))
+            if f"P{P}_interp" not in out:
+                rows = lambda k: np.array([[float(v) for v in lines[k + r].split("]")[-1].split()] for r in range(Q)])
+                out[f"P{P}_q"], out[f"P{P}_w"] = np.array(rule[0]), np.array(rule[1])
+                out[f"P{P}_interp"] = rows(i + 1)
+                out[f"P{P}_deriv"] = rows(i + 1 + Q)
+                out[f"P{P}_node"] = np.array([float(v) for v in lines[i + 1 + 2 * Q].split("]")[-1].split()])
+            i += 1 + 2 * Q
+            continue
+        if ln.startswith("dEFS type"):
+            rule = None
+        i += 1
+    return out
+
+
 def solver_log(root, name):
     """stokes-q3q2-{scr,fgmres}, ellip-e0-*, elast-e0-b3-g01 (src/fs/tests/CMakeLists.txt:49-70, manufactured
     solutions on the default 4^3 block of [-1,1]^3): residual norms at the nodal interpolant of the exact solution
@@ -158,6 +189,7 @@ def main(root):
         "bu0": bu0(root),
         "stokes_q3q2_scr": solver_log(root, "stokes-q3q2-scr"),
         "stokes_q3q2_fgmres": solver_log(root, "stokes-q3q2-fgmres"),
+        "jacobi3_sparse_efs": sparse_efs(root),
         "ellip_e0_b1_p16": solver_log(root, "ellip-e0-b1-p16"),
         "ellip_e0_b3_p16": solver_log(root, "ellip-e0-b3-p16"),
         "ellip_e0_b3_p14": solver_log(root, "ellip-e0-b3-p14-sse"),

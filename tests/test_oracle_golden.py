@@ -236,3 +236,18 @@ def test_q1_assembly_and_cg_solve():
     assert its > 0 and rn <= 1e-8
     r = b - fs.apply(x)
     assert np.linalg.norm(r) <= 1.01e-8 * np.linalg.norm(b)
+
+
+def test_sparse_rule_efs_golden():
+    """jacobi-3-tensor-sparse-gauss (dEFSView on the SPARSE rule of degree 4, tensorquad.c:32-49, 68-80): the rule's
+    points and weights (2 Gauss points in each GLL sub-interval, weight h/2) and the GLL bases of 2..5 nodes at them
+    (tensor.c:22-109), to the 5 printed decimals"""
+    g = gold("jacobi3_sparse_efs")
+    rx, rw = po.rule_1d(1, 0, 4)
+    for P in range(2, 6):
+        np.testing.assert_allclose(rx, g[f"P{P}_q"], atol=6e-6)
+        np.testing.assert_allclose(rw, g[f"P{P}_w"], atol=6e-6)
+        interp, deriv, node, _ = po.tensor_basis(P, rx)
+        np.testing.assert_allclose(interp, g[f"P{P}_interp"], atol=6e-6)
+        np.testing.assert_allclose(deriv, g[f"P{P}_deriv"], atol=6e-6)
+        np.testing.assert_allclose(node, g[f"P{P}_node"], atol=6e-6)
