@@ -918,6 +918,15 @@ static int add_constraints_hex(or_fs *m, int64_t r, int xs)
 /* dFSBuildSpace_Cont (src/fs/impls/cont/cont.c:258-385) with natural ordering: explicit entities in
  * handle order, then Dirichlet entities (dMeshPopulateOrderedSet_Private cont.c:93-178, partition
  * fsbuild.c:55-95, offsets fsbuild.c:107-146, element offsets cont.c:371-376). */
+/* expanded coordinates, tensor vertex order (dFSCreateGeometryFromMesh_Private fsgeom.c:146-156) */
+static void expanded_coords(or_fs *m)
+{
+  static const int connidx[8] = {0, 4, 3, 7, 1, 5, 2, 6};
+  for (int64_t r = 0; r < m->nr; r++)
+    for (int i = 0; i < 8; i++)
+      for (int d = 0; d < 3; d++) m->xexp[(r * 8 + i) * 3 + d] = m->vx[3 * m->hconn[8 * r + connidx[i]] + d];
+}
+
 or_fs *or_fs_create(int nx, int ny, int nz, const double box[6], double perturb, uint64_t seed,
                     int degree, const int *elem_degree, int bs, int dirichlet_mask)
 {
@@ -990,13 +999,17 @@ or_fs *or_fs_create(int nx, int ny, int nz, const double box[6], double perturb,
     }
     m->eptr[m->nexp] = o;
   }
-  /* expanded coordinates, tensor vertex order (dFSCreateGeometryFromMesh_Private fsgeom.c:146-156) */
-  static const int connidx[8] = {0, 4, 3, 7, 1, 5, 2, 6};
   m->xexp = malloc(sizeof(double) * 24 * m->nr);
-  for (int64_t r = 0; r < m->nr; r++)
-    for (int i = 0; i < 8; i++)
-      for (int d = 0; d < 3; d++) m->xexp[(r * 8 + i) * 3 + d] = m->vx[3 * m->hconn[8 * r + connidx[i]] + d];
+  expanded_coords(m);
   return m;
+}
+
+/* dMeshMorph (src/fs/mesh/interface/mesh.c): new vertex coordinates [nv][3] (same topology), e.g. the morph and
+ * twist of ellip.c:173-181; the expanded coordinates follow */
+void or_fs_set_vertex_coords(or_fs *m, const double *vx)
+{
+  memcpy(m->vx, vx, sizeof(double) * 3 * m->nv);
+  expanded_coords(m);
 }
 
 void or_fs_destroy(or_fs *m)

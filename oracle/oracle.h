@@ -79,6 +79,8 @@ const int32_t *or_fs_xstart(const or_fs *fs);      /* element offsets in expande
 const int32_t *or_fs_elem_degree(const or_fs *fs); /* per element degree (x,y,z) triples */
 const double *or_fs_coords_expanded(const or_fs *fs); /* [nelem][8][3] in tensor vertex order */
 const double *or_fs_vertex_coords(const or_fs *fs);   /* [nverts][3] */
+/* replace the vertex coordinates (same topology; a mesh morph), the expanded coordinates follow */
+void or_fs_set_vertex_coords(or_fs *fs, const double *vx);
 /* entity ordering (ordered set), per entity index arrays of length nents */
 void or_fs_entity_info(const or_fs *fs, int32_t *ordered, int32_t *goffset, int32_t *gcoffset, int32_t *inodes);
 

@@ -99,6 +99,7 @@ def lib():
         L.or_facet_points.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, _f64p, _f64p, _f64p, _f64p]
         L.or_facet_commit.argtypes = [ctypes.c_void_p, ctypes.c_int, _f64p, _f64p, ctypes.c_int]
         L.or_stokes_apply.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _f64p] + [ctypes.c_void_p] * 5
+        L.or_fs_set_vertex_coords.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.or_operator_function.argtypes = [ctypes.c_void_p, ctypes.c_int, _f64p, _f64p, ctypes.c_void_p, ctypes.c_void_p,
                                            _f64p, ctypes.c_int]
         L.or_fs_eval_points.argtypes = [ctypes.c_void_p, ctypes.c_int, _f64p] + [ctypes.c_void_p] * 4
@@ -246,6 +247,11 @@ class FS:
 
     def vertex_coords(self):
         return np.ctypeslib.as_array(lib().or_fs_vertex_coords(self.h), shape=(self.nv, 3)).copy()
+
+    def set_vertex_coords(self, vx):
+        """move the vertices (a mesh morph); the expanded coordinates follow"""
+        vx = np.ascontiguousarray(vx, dtype=np.float64).reshape(self.nv, 3)
+        lib().or_fs_set_vertex_coords(self.h, vx.ctypes.data)
 
     def entity_info(self):
         o = np.zeros(self.nents, np.int32); g = np.zeros_like(o); gc = np.zeros_like(o); ino = np.zeros_like(o)

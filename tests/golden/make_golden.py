@@ -162,7 +162,11 @@ def solver_log(root, name):
     printed after the solve (stokes.c:1128-1133, 1161-1169; ellip.c:750-757; elast.c:539-546)."""
     lines = read(root, f"src/fs/tests/refout/{name}.refout")
     out = {}
+    ksp = []
     for ln in lines:
+        m = re.match(r"\s*(\d+) KSP Residual norm ([-+0-9.e]+)", ln)
+        if m and (int(m.group(1)) == len(ksp)) and len(ksp) < 20:  # the first linear solve's history
+            ksp.append(float(m.group(2)))
         m = re.match(r"Norm of discrete (linear )?residual (?:for|at) exact solution (\S+)", ln)
         if m:
             out["linear_residual_exact" if m.group(1) else "residual_exact"] = np.array([float(m.group(2))])
@@ -173,6 +177,8 @@ def solver_log(root, name):
         m = m or re.match(r"Pointwise (velocity|solution|gradient|pressure) error\s+\|x\|_1 (\S+)\s+\|x\|_2 (\S+)\s+\|x\|_inf (\S+)", ln)
         if m:
             out[m.group(1).lower()] = np.array([float(m.group(k)) for k in (2, 3, 4)])
+    if ksp:
+        out["ksp_first_solve"] = np.array(ksp)
     return out
 
 
@@ -194,6 +200,8 @@ def main(root):
         "ellip_e0_b3_p16": solver_log(root, "ellip-e0-b3-p16"),
         "ellip_e0_b3_p14": solver_log(root, "ellip-e0-b3-p14-sse"),
         "elast_e0_b3_g01": solver_log(root, "elast-e0-b3-g01"),
+        "ellip_morph": solver_log(root, "ellip-morph"),
+        "ellip_morph_qfast": solver_log(root, "ellip-morph-qfast"),
     }
     meta = {}
     for name, arrs in fixtures.items():

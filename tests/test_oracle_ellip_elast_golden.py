@@ -137,3 +137,114 @@ def test_solution_error_norms(case):
     got = P.norms(P.solve())
     for key in ("interpolation", "solution", "gradient"):
         np.testing.assert_allclose(got[key], ref[key], rtol=0.006, err_msg=name + " " + key)  # the printed digits
+
+
+def morph(v, morph, twist, stretch=0.0):
+    """the vertex map of ellip.c:173-181 (-morph, -twist, -stretch)"""
+    x, y, z = v.T
+    return np.stack([np.cos(twist * z) * x + np.sin(twist * z) * y, -np.sin(twist * z) * x + np.cos(twist * z) * y,
+                     -1 + (z + 1) * (1 + morph * ((x + 1) ** 2 + (y + 1) ** 2)) + stretch * z], 1)
+
+
+def test_morphed_mesh_cg_history_and_errors():
+    """ellip-morph (src/fs/tests/CMakeLists.txt:55: -morph 1 -twist 0.4, p = 2, exact 0 with a = b = c = 1, degree 3,
+    one Newton step solved by CG preconditioned with the LU of the Q1-embedded matrix): on the twisted, non-affine
+    mesh the first linear solve's preconditioned residual history (KSPSolve_CG, preconditioned norm) is reproduced
+    to the six printed digits through all 20 printed iterations, which pins the matrix-free apply, the Q1-embedded
+    assembly with the reference's quirks (the variant without them differs in the fourth digit) and the Dirichlet
+    handling; the solution's error norms match the printed ones"""
+    import scipy.sparse as ssp
+    import scipy.sparse.linalg as sla
+    g = np.load(os.path.join(HERE, "golden", "ellip_morph.npz"))
+    P = Problem.__new__(Problem)
+    P.bs, P.kind, P.param = 1, 6, (2.0, 1.0)
+    P.fs = po.FS(5, 5, 5, degree=3, box=BOX, perturb=0.0, seed=1, bs=1, dirichlet_mask=7)
+    P.fs.set_vertex_coords(morph(P.fs.vertex_coords(), 1.0, 0.4))
+    f = ellip_exact(1.0, 1.0, 1.0, 2.0, 1.0)
+    Xc = closure_coords(P.fs, 4)
+    U = columns(f(*Xc.T)[0], len(Xc))
+    P.s, P.dc = U[:P.fs.n].ravel(), U[P.fs.n:].ravel()
+    xq = P.fs.qpt_coords()
+    r = f(*xq.T)
+    P.fq = columns(r[1], len(xq))
+    P.ue, P.due = columns(r[0], len(xq)), columns(r[2], len(xq)).reshape(-1, 1, 3)
+    n = P.fs.n
+    b = -P.F(np.zeros(n))
+    lus = {}
+    for quirk in (1, 0):
+        rp, ci, val = P.fs.q1_assemble(kind=0, quirk=quirk)
+        lus[quirk] = sla.splu(ssp.csr_matrix((val, ci, rp), shape=(n, n)).tocsc())
+    ref = g["ksp_first_solve"]
+    assert abs(np.linalg.norm(lus[0].solve(b)) - ref[0]) > 1e-4 * ref[0]  # the quirk matters at this precision
+    lu = lus[1]
+    x, rr = np.zeros(n), b.copy()
+    z = lu.solve(rr)
+    norms = [np.linalg.norm(z)]
+    beta = z @ rr
+    p = z.copy()
+    for it in range(200):
+        w = P.fs.apply(p, kind=0)
+        a = beta / (p @ w)
+        x += a * p
+        rr -= a * w
+        z = lu.solve(rr)
+        norms.append(np.linalg.norm(z))
+        if norms[-1] < 1e-13 * norms[0]:
+            break
+        bnew = z @ rr
+        p = z + (bnew / beta) * p
+        beta = bnew
+    np.testing.assert_allclose(norms[:len(ref)], ref, rtol=6e-6)
+    got = P.norms(x)
+    for key in ("interpolation", "solution", "gradient"):
+        np.testing.assert_allclose(got[key], g[key], rtol=0.006, err_msg=key)
+
+
+def ellip_exact3(a, b, c, pe, eps):
+    """exact solution 3 of ellip.c:91-104, u = a x^3 + b y^2 z + c (1 - z^2) x, with its p-Laplacian forcing"""
+    x, y, z = X
+    u = a * x ** 3 + b * y ** 2 * z + c * (1 - z ** 2) * x
+    g = [sp.diff(u, v) for v in X]
+    eta = (eps ** 2 + sum(t ** 2 for t in g) / 2) ** ((pe - 2) / 2)
+    f = -sum(sp.diff(eta * g[i], X[i]) for i in range(3))
+    return sp.lambdify(X, [[u], [f], g], "numpy")
+
+
+def test_morphed_mesh_newton_step():
+    """ellip-morph-qfast (src/fs/tests/CMakeLists.txt:56: -morph 0.5 -twist 0.1, p = 1.9, exact 3, one Newton step
+    with the Jacobian assembled on the FAST rule, so that Richardson with its LU converges in one iteration): the
+    Newton step's norm ||J(0)^-1 F(0)|| (the printed first preconditioned residual), and after the step the
+    algebraic residual ||F(x1)|| (scaled norms), the interpolation residual and the error norms, all at a state far
+    from the solution (the Jacobian at the Dirichlet lift)"""
+    g = np.load(os.path.join(HERE, "golden", "ellip_morph_qfast.npz"))
+    P = Problem.__new__(Problem)
+    P.bs, P.kind, P.param = 1, 6, (1.9, 1.0)
+    P.fs = po.FS(5, 5, 5, degree=3, box=BOX, perturb=0.0, seed=1, bs=1, dirichlet_mask=7)
+    P.fs.set_vertex_coords(morph(P.fs.vertex_coords(), 0.5, 0.1))
+    f = ellip_exact3(1.0, 1.0, 1.0, 1.9, 1.0)
+    Xc = closure_coords(P.fs, 4)
+    U = columns(f(*Xc.T)[0], len(Xc))
+    P.s, P.dc = U[:P.fs.n].ravel(), U[P.fs.n:].ravel()
+    xq = P.fs.qpt_coords()
+    r = f(*xq.T)
+    P.fq = columns(r[1], len(xq))
+    P.ue, P.due = columns(r[0], len(xq)), columns(r[2], len(xq)).reshape(-1, 1, 3)
+    n = P.fs.n
+    x0 = np.zeros(n)
+    F0 = P.F(x0)
+    qd = P.qdata(x0)
+    J = np.zeros((n, n))
+    e = np.zeros(n)
+    for j in range(n):
+        e[j] = 1
+        J[:, j] = P.fs.apply(e, kind=1, qdata=qd, param=P.param)
+        e[j] = 0
+    dx = -np.linalg.solve(J, F0)
+    assert abs(np.linalg.norm(dx) - g["ksp_first_solve"][0]) < 6e-6 * g["ksp_first_solve"][0]
+    x1 = x0 + dx
+    F1 = P.F(x1)
+    alg = np.array([np.abs(F1).sum() / n, np.linalg.norm(F1) / np.sqrt(n), np.abs(F1).max()])
+    np.testing.assert_allclose(alg, g["algebraic"], rtol=0.006)
+    got = P.norms(x1)
+    for key in ("interpolation", "solution", "gradient"):
+        np.testing.assert_allclose(got[key], g[key], rtol=0.006, err_msg=key)
