@@ -1454,7 +1454,7 @@ static int cmp_pair(const void *a, const void *b)
  * GetPatchApplied (element GRAD with the point's own inverse Jacobian, then patch order), the store from
  * EllipPointwiseComputeStore, and the patch matrix from EllipPointwiseJacobian with the Q1 patch bases. */
 static int64_t q1_assemble(const or_fs *m, int kind, const double *param, const double *grf, int quirk,
-                           const double *state, int32_t *rowptr, int32_t **colp, double **valp)
+                           const double *state, const double *sdcache, int32_t *rowptr, int32_t **colp, double **valp)
 {
   const int bs = m->bs;
   if (kind == 1 && (!state || bs != 1)) return or_fail("p-Laplacian Q1 assembly needs a scalar space and the state");
@@ -1465,7 +1465,7 @@ static int64_t q1_assemble(const or_fs *m, int kind, const double *param, const 
   double *sexp = NULL;
   if (kind == 1) {
     sexp = malloc(sizeof(double) * m->nexp);
-    or_fs_global_to_expanded(m, state, NULL, sexp);
+    or_fs_global_to_expanded(m, state, sdcache, sexp);
   }
   for (int64_t r = 0; r < m->nr; r++) {
     const basis1d *b[3] = {&B[m->edeg[3 * r]], &B[m->edeg[3 * r + 1]], &B[m->edeg[3 * r + 2]]};
@@ -1566,14 +1566,21 @@ int64_t or_q1_assemble(const or_fs *m, int kind, const double *param, const doub
                        int32_t *rowptr, int32_t **colp, double **valp)
 {
   if (kind == 1) return or_fail("p-Laplacian Q1 assembly needs the state: use or_q1_assemble_plap");
-  return q1_assemble(m, kind, param, grf, quirk, NULL, rowptr, colp, valp);
+  return q1_assemble(m, kind, param, grf, quirk, NULL, NULL, rowptr, colp, valp);
 }
 
 int64_t or_q1_assemble_plap(const or_fs *m, double p, double eps, const double *g, int quirk,
                             int32_t *rowptr, int32_t **colp, double **valp)
 {
   const double param[2] = {p, eps};
-  return q1_assemble(m, 1, param, NULL, quirk, g, rowptr, colp, valp);
+  return q1_assemble(m, 1, param, NULL, quirk, g, NULL, rowptr, colp, valp);
+}
+
+int64_t or_q1_assemble_plap_dir(const or_fs *m, double p, double eps, const double *g, const double *dcache, int quirk,
+                                int32_t *rowptr, int32_t **colp, double **valp)
+{
+  const double param[2] = {p, eps};
+  return q1_assemble(m, 1, param, NULL, quirk, g, dcache, rowptr, colp, valp);
 }
 
 /* ----------------------------------------------------------------------------------------------

@@ -128,6 +128,10 @@ int64_t or_q1_assemble(const or_fs *fs, int kind, const double *param, const dou
  * EllipJacobian (ellip.c:474-536), store at every SPARSE point (ellip.c:333-342). */
 int64_t or_q1_assemble_plap(const or_fs *fs, double p, double eps, const double *g, int quirk,
                             int32_t *rowptr, int32_t **col, double **val);
+/* the same at a state whose closure carries the Dirichlet values dcache [nc - n] (EllipJacobian's
+ * dFS_INHOMOGENEOUS expansion) */
+int64_t or_q1_assemble_plap_dir(const or_fs *fs, double p, double eps, const double *g, const double *dcache, int quirk,
+                                int32_t *rowptr, int32_t **col, double **val);
 void or_free(void *p);
 
 /* ---------------- facet rules and boundary integrals ---------------- */

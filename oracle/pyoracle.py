@@ -78,6 +78,10 @@ def lib():
         L.or_q1_assemble.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                      _i32p, ctypes.POINTER(ctypes.POINTER(ctypes.c_int32)),
                                      ctypes.POINTER(ctypes.POINTER(ctypes.c_double))]
+        L.or_q1_assemble_plap_dir.restype = ctypes.c_int64
+        L.or_q1_assemble_plap_dir.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, _f64p, _f64p, ctypes.c_int,
+                                              _i32p, ctypes.POINTER(ctypes.POINTER(ctypes.c_int32)),
+                                              ctypes.POINTER(ctypes.POINTER(ctypes.c_double))]
         L.or_q1_assemble_plap.restype = ctypes.c_int64
         L.or_q1_assemble_plap.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, _f64p, ctypes.c_int,
                                           _i32p, ctypes.POINTER(ctypes.POINTER(ctypes.c_int32)),
@@ -332,15 +336,20 @@ class FS:
             raise RuntimeError(lib().or_last_error().decode())
         return st
 
-    def q1_assemble(self, kind=0, param=None, grf=None, quirk=1, state=None):
-        """Q1-embedded matrix; kind 1 (p-Laplacian Jacobian) takes param = (p, eps) and the state g."""
+    def q1_assemble(self, kind=0, param=None, grf=None, quirk=1, state=None, state_dcache=None):
+        """Q1-embedded matrix; kind 1 (p-Laplacian Jacobian) takes param = (p, eps) and the state g (whose Dirichlet
+        values are state_dcache, None = 0)."""
         nrows = self.n * self.bs
         rp = np.zeros(nrows + 1, np.int32)
         colp = ctypes.POINTER(ctypes.c_int32)()
         valp = ctypes.POINTER(ctypes.c_double)()
         pa = None if param is None else np.ascontiguousarray(param, dtype=np.float64)
         gr = None if grf is None else np.ascontiguousarray(grf, dtype=np.float64)
-        if kind == 1:
+        if kind == 1 and state_dcache is not None:
+            nnz = lib().or_q1_assemble_plap_dir(self.h, float(pa[0]), float(pa[1]), np.ascontiguousarray(state, np.float64),
+                                                np.ascontiguousarray(state_dcache, np.float64), quirk, rp,
+                                                ctypes.byref(colp), ctypes.byref(valp))
+        elif kind == 1:
             nnz = lib().or_q1_assemble_plap(self.h, float(pa[0]), float(pa[1]), np.ascontiguousarray(state, np.float64),
                                             quirk, rp, ctypes.byref(colp), ctypes.byref(valp))
         else:

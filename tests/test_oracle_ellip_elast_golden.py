@@ -248,3 +248,46 @@ def test_morphed_mesh_newton_step():
     got = P.norms(x1)
     for key in ("interpolation", "solution", "gradient"):
         np.testing.assert_allclose(got[key], g[key], rtol=0.006, err_msg=key)
+
+
+def gmres_history(apply, prec, b, steps):
+    """left-preconditioned GMRES residual norms ||B (b - A x_k)|| over the first steps Arnoldi steps (KSPGMRES with
+    the preconditioned norm, zero initial guess; the minimal residual of each Krylov space, computed here by
+    least squares on the Arnoldi relation with twice-orthogonalised vectors)"""
+    r0 = prec(b)
+    beta = np.linalg.norm(r0)
+    V, H, norms = [r0 / beta], np.zeros((steps + 1, steps)), [beta]
+    for k in range(steps):
+        w = prec(apply(V[k]))
+        for _ in range(2):
+            for j in range(k + 1):
+                c = V[j] @ w
+                H[j, k] += c
+                w = w - c * V[j]
+        H[k + 1, k] = np.linalg.norm(w)
+        V.append(w / H[k + 1, k])
+        e1 = np.zeros(k + 2)
+        e1[0] = beta
+        y = np.linalg.lstsq(H[:k + 2, :k + 1], e1, rcond=None)[0]
+        norms.append(np.linalg.norm(e1 - H[:k + 2, :k + 1] @ y))
+    return np.array(norms)
+
+
+@pytest.mark.parametrize("name", ["ellip_e0_b1_p16", "ellip_e0_b3_p16", "ellip_e0_b3_p14"])
+def test_first_newton_linear_solve_history(name):
+    """the first Newton step's linear solve of the ellip targets (GMRES preconditioned with the LU of the Q1-embedded
+    p-Laplacian Jacobian, EllipJacobian ellip.c:474-536, at the state zero with the exact Dirichlet values; the
+    operator the matrix-free Jacobian there): the printed preconditioned residual norms, to six digits"""
+    import scipy.sparse as ssp
+    import scipy.sparse.linalg as sla
+    g = np.load(os.path.join(HERE, "golden", name + ".npz"))
+    P = Problem(*CASES[name])
+    n = P.fs.n
+    x0 = np.zeros(n)
+    F0 = P.F(x0)
+    rp, ci, val = P.fs.q1_assemble(kind=1, param=P.param, quirk=1, state=x0, state_dcache=P.dc)
+    lu = sla.splu(ssp.csr_matrix((val, ci, rp), shape=(n, n)).tocsc())
+    qd = P.qdata(x0)
+    ref = g["ksp_first_solve"]
+    got = gmres_history(lambda v: P.fs.apply(v, kind=1, qdata=qd, param=P.param), lu.solve, -F0, min(len(ref) - 1, n - 1))
+    np.testing.assert_allclose(got[:len(ref)], ref[:len(got)], rtol=6e-6)
