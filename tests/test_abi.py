@@ -2,12 +2,15 @@
 declares, and its host-side space build (block mesh, adjacency, numbering, E map) is bit-exact with the
 oracle. No GPU is touched."""
 import ctypes
+import os
 
 import numpy as np
 import pytest
 
 import dohp_gb300 as dg
 import pyoracle as po
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 @pytest.fixture(scope="module")
@@ -149,3 +152,25 @@ def test_boundary_status_values(L):
         dg.chk(L.dFSRegisterBoundary(fs, ctypes.c_int32(100), ctypes.c_int(1 << 20)))
     L.dFSDestroy(ctypes.byref(fs))
     L.dMeshDestroy(ctypes.byref(mesh))
+
+
+def test_null_handles_are_errors_not_crashes(L):
+    """every entry point that takes an object handle returns a nonzero dErr with a message for a NULL handle (and
+    NULL or zero everywhere else) instead of dereferencing it: the reference's error convention (dCHK / dERROR,
+    include/dohp.h:43-44; invalid input returns an error, never aborts). Runs without a GPU: each check comes
+    before any device call."""
+    import re
+    src = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "dohp_gb300.h")).read(), flags=re.S)
+    handles = set(re.findall(r"typedef struct _p_\w+ \*(d\w+);", src))
+    checked = []
+    for m in re.finditer(r"dErr (d\w+)\(([^;]*?)\);", src, flags=re.S):
+        name, params = m.group(1), [a.strip() for a in " ".join(m.group(2).split()).split(",") if a.strip()]
+        if not params or name.endswith("Destroy"):
+            continue
+        first = params[0]
+        if first.replace("const", "").split()[0] not in handles or "*" in first:
+            continue
+        rc = getattr(L, name)(*([None] * len(params)))
+        assert rc != 0 and L.dGetLastError(), name
+        checked.append(name)
+    assert len(checked) > 80
