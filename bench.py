@@ -1,15 +1,15 @@
 """Benchmark: GDoF/s of the matrix-free hp-FEM operator apply (dohp's ElastShellMatMult / EllipShellMatMult)
 on one GB300.
 
-Default workload (--config cfg2, the hp-batching configuration): 3-D linear elasticity (E=1, nu=0.3,
+Default workload (--config hp-elasticity-32, the hp-batching configuration): 3-D linear elasticity (E=1, nu=0.3,
 ElastPointwiseJacobian at F=I) on a 32^3 structured hex mesh of the unit cube, interior vertices perturbed
 U[-0.1h, 0.1h] (seed 1), per-element order drawn i.i.d. uniform from {2..8} (seed 2), min-order shared
 faces/edges with interpolation constraints, Gauss (p+1)^3 quadrature, Dirichlet walls, FP64. A step is one
 operator apply y = A x on a seeded x ~ U[-1,1]: one persistent kernel over all order buckets plus the
 deterministic E^T restriction, replayed from a CUDA graph. The per-order-launch and persistent forms are timed
 beside it. Inputs (geometric factors ~3 GB, E ~1 GB) exceed the 129 MB L2: no flush between steps.
-A secondary entry times the uniform FP64 Poisson apply (lognormal k, 64^3, p=4; --config cfg4 makes it the
-headline).
+A secondary entry times the uniform FP64 Poisson apply (lognormal k, 64^3, p=4; --config poisson-lognormal-64
+makes it the headline).
 
 Prints one JSON line: value = explicit scalar dofs / device seconds per apply (CUDA events on the launching
 stream); e2e = dOperatorMultHost (host vectors, copies inside the timed region); roofline of the dominant
@@ -26,12 +26,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 CONFIGS = {
-    "cfg2": dict(ne=32, kind="elasticity", hp=True, p=4, grf=False, label="hp-elasticity-32^3-p2..8"),
-    "cfg4": dict(ne=64, kind="diffusion", hp=False, p=4, grf=True, label="poisson-lognormal-64^3-p4"),
-    "cfg1": dict(ne=8, kind="diffusion", hp=False, p=4, grf=False, label="poisson-8^3-p4"),
+    "hp-elasticity-32": dict(ne=32, kind="elasticity", hp=True, p=4, grf=False, label="hp-elasticity-32^3-p2..8"),
+    "poisson-lognormal-64": dict(ne=64, kind="diffusion", hp=False, p=4, grf=True, label="poisson-lognormal-64^3-p4"),
+    "poisson-8": dict(ne=8, kind="diffusion", hp=False, p=4, grf=False, label="poisson-8^3-p4"),
     # reduced cases of the same kernels for full ncu captures (inputs still above L2)
-    "cfg2_16": dict(ne=16, kind="elasticity", hp=True, p=4, grf=False, label="hp-elasticity-16^3-p2..8"),
-    "cfg4_32": dict(ne=32, kind="diffusion", hp=False, p=4, grf=True, label="poisson-lognormal-32^3-p4"),
+    "hp-elasticity-16": dict(ne=16, kind="elasticity", hp=True, p=4, grf=False, label="hp-elasticity-16^3-p2..8"),
+    "poisson-lognormal-32": dict(ne=32, kind="diffusion", hp=False, p=4, grf=True, label="poisson-lognormal-32^3-p4"),
 }
 E0, NU = 1.0, 0.3
 FP64_PEAK_GFLOPS = 1203.0  # FP64 FMA issue rate measured on this GB300 (FMA-chain probe)
@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="cfg2", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="hp-elasticity-32", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--secondary", default="all", help="comma list of apply,learned,newton,multigrid,stokes (or all: apply, learned (which includes the multigrid "
@@ -183,7 +183,7 @@ def cpu_baseline(cfg, threads, budget_s=20.0):
                       % (ne, fs.n * bs, len(times), threads)}
 
 
-def cpu_time_to_rtol_cfg1(threads):
+def cpu_time_to_rtol_poisson8(threads):
     """The CPU-runnable configuration (Poisson 8^3, p=4, mass right-hand side of f ~ U[-1,1], CG + Q1
     Chebyshev(3)-Jacobi to rtol 1e-8) solved by the oracle on the host cores: wall seconds."""
     import numpy as np
@@ -199,7 +199,7 @@ def cpu_time_to_rtol_cfg1(threads):
     return {"its": its, "solve_s": t2 - t1, "q1_assembly_s": t1 - t0, "rel_residual": rn, "threads": threads}
 
 
-def gpu_time_to_rtol_cfg1():
+def gpu_time_to_rtol_poisson8():
     """Same problem on the GPU: mass right-hand side through the batched dRulesetIterator, Q1 assembly on the
     device, CG with Chebyshev(3)-Jacobi, FP64."""
     import numpy as np
@@ -308,10 +308,10 @@ def work_per_apply(fs, cfg, bs):
     return alg_bytes, alg_flops, issued
 
 
-def secondary_cfg4(args):
+def secondary_lognormal_apply(args):
     """uniform FP64 Poisson apply (lognormal k, 64^3, p=4): element kernel + restrict, device-timed."""
     import torch
-    cfg = CONFIGS["cfg4"]
+    cfg = CONFIGS["poisson-lognormal-64"]
     stream = torch.cuda.current_stream()
     fs, op, x, bs = setup(cfg, stream)
     y = torch.empty(fs.n, dtype=torch.float64, device="cuda")
@@ -717,14 +717,14 @@ def main():
     if cfg["hp"]:
         line["launch_forms"] = forms
         line["tiles"] = op.tiles()
-    if not args.no_secondary and args.config == "cfg2":
+    if not args.no_secondary and args.config == "hp-elasticity-32":
         del fs, op, x, y, yexp
         torch.cuda.empty_cache()
         which = {"apply", "learned", "newton"} if args.secondary == "all" else set(args.secondary.split(","))
         if "multigrid" in which:
             line["multigrid"] = secondary_multigrid(args)
         if "apply" in which:
-            line["secondary"] = secondary_cfg4(args)
+            line["secondary"] = secondary_lognormal_apply(args)
         if "learned" in which:
             line["time_to_rtol"] = secondary_learned(args)
             torch.cuda.empty_cache()
@@ -734,13 +734,13 @@ def main():
         if "stokes" in which:
             line["stokes_power_law"] = secondary_stokes(args)
             torch.cuda.empty_cache()
-    if not args.no_secondary and args.config == "cfg2":
-        line["time_to_rtol_cfg1"] = {"workload": "poisson-8^3-p4, mass right-hand side, CG + Q1 Chebyshev(3)-Jacobi, rtol 1e-8",
-                                     "gpu": gpu_time_to_rtol_cfg1()}
+    if not args.no_secondary and args.config == "hp-elasticity-32":
+        line["time_to_rtol_poisson_8"] = {"workload": "poisson-8^3-p4, mass right-hand side, CG + Q1 Chebyshev(3)-Jacobi, rtol 1e-8",
+                                     "gpu": gpu_time_to_rtol_poisson8()}
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(cfg, os.cpu_count() or 1)
-        if "time_to_rtol_cfg1" in line:
-            line["time_to_rtol_cfg1"]["cpu_oracle"] = cpu_time_to_rtol_cfg1(os.cpu_count() or 1)
+        if "time_to_rtol_poisson_8" in line:
+            line["time_to_rtol_poisson_8"]["cpu_oracle"] = cpu_time_to_rtol_poisson8(os.cpu_count() or 1)
     print(json.dumps(line, default=_plain))
     if dist:
         dist.destroy_process_group()

@@ -29,7 +29,7 @@ def solve(fs, op, m, b, pc, ksp_type=dg.dKSP_CG, rtol=1e-8, maxit=3000):
     return its, float(torch.linalg.norm(b - r) / torch.linalg.norm(b)), x
 
 
-def test_configuration_one_with_multigrid():
+def test_poisson_8_with_multigrid():
     fs = dg.FS((9, 9, 9), degree=4, perturb=0.1, seed=1)
     o = po.FS(9, 9, 9, degree=4, perturb=0.1, seed=1)
     f = np.random.default_rng(0).uniform(-1, 1, fs.n)

@@ -33,7 +33,7 @@ def mass_rhs(fs, f):
     return b
 
 
-def test_configuration_one_end_to_end():
+def test_poisson_8_end_to_end():
     fs = dg.FS((9, 9, 9), degree=4, perturb=0.1, seed=1)
     o = po.FS(9, 9, 9, degree=4, perturb=0.1, seed=1)
     assert fs.n == 29791

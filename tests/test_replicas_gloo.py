@@ -47,5 +47,5 @@ def test_reference_arm_other_ranks_exit_without_work(monkeypatch):
         steps, warmup, gpus = 3, 3, 2
     called = []
     monkeypatch.setattr(bench, "cpu_baseline", lambda *a, **k: called.append(1) or {"value": 1.0})
-    assert bench.run_reference(A(), bench.CONFIGS["cfg2"], 1) is None
+    assert bench.run_reference(A(), bench.CONFIGS["hp-elasticity-32"], 1) is None
     assert not called
