@@ -609,7 +609,7 @@ static dErr fgmres_solve(_p_dKSP *k, const double *b, double *x, double rtol, in
     const double beta = sqrt(rr);
     res = beta / bn;
     if (!(beta > rtol * bn) || total >= maxit) break;
-    // the plain preconditioner judges the correction: a restart cycle that stagnated (less than 1 %
+    // the true residual decides whether the correction stays: a restart cycle that stagnated (less than 1 %
     // reduction of the true residual, or a non-finite one) drops the correction for the rest of this solve
     if (k->correction_on && prev > 0 && !(beta < 0.99 * prev)) {
       k->correction_on = false;
