@@ -174,3 +174,13 @@ def test_null_handles_are_errors_not_crashes(L):
         assert rc != 0 and L.dGetLastError(), name
         checked.append(name)
     assert len(checked) > 80
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """without the built CUDA library the package raises instead of falling back to any CPU path"""
+    monkeypatch.setattr(dg, "_lib", None)
+    monkeypatch.setattr(dg, "LIB_PATH", str(tmp_path / "absent.so"))
+    with pytest.raises(dg.DohpError, match="not built"):
+        dg.lib()
+    with pytest.raises(dg.DohpError):
+        dg.FS((3, 3, 3), degree=2)
