@@ -158,3 +158,33 @@ def test_newton_fp64_and_mixed_reach_the_oracle_solution():
         r = o.apply(u, kind=1, qdata=st.ravel()) - b
         assert np.linalg.norm(r) <= 1e-7 * fn64[0]
     assert rel(u32, u64) < 1e-6
+
+
+@pytest.mark.parametrize("name", ["ellip_e0_b3_p16", "ellip_e0_b3_p14"])
+def test_reference_ellip_target_through_the_product(name):
+    """the reference's ellip-e0-b3-p16 / -p14 targets (src/fs/tests/CMakeLists.txt:50-51; the problem and its oracle
+    side are in tests/test_oracle_ellip_elast_golden.py) through the product: the exact solution's Dirichlet values
+    committed to the space (dFSInhomogeneousDirichletCommit, as ellip.c:719-724), the forcing integrated by the
+    dRulesetIterator, dOperatorPLaplaceFunction at zero (its dFS_INHOMOGENEOUS expansion, as EllipFunction):
+    ||F(0)|| is the printed first SNES function norm to six digits, and the residual vector is the oracle's"""
+    import test_oracle_ellip_elast_golden as G
+    ref = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", name + ".npz"))
+    O = G.Problem(*G.CASES[name])
+    pe, eps = O.param
+    fs = dg.FS((5, 5, 5), degree=3, box=G.BOX, perturb=0.0, seed=1)
+    assert (fs.n, fs.nc) == (O.fs.n, O.fs.nc)
+    fs.dirichlet_commit(dev(np.concatenate([O.s, O.dc])))
+    it = dg.RulesetIterator(fs)
+    it.start(None)
+    a = it.get()
+    np.testing.assert_allclose(a["x"].cpu().numpy(), O.fs.qpt_coords(), rtol=0, atol=1e-14)
+    a["v"].copy_(a["jw"][:, None] * dev(O.fq))
+    it.commit(dg.INSERT_VALUES, use_v=True, use_dv=False)
+    b = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
+    it.finish(b)
+    op = fs.operator(dg.dOP_PLAPLACE_JACOBIAN)
+    y = torch.zeros_like(b)
+    op.plap_function(torch.zeros_like(b), pe, eps, y)
+    F0 = host(y) - host(b)
+    assert abs(np.linalg.norm(F0) - ref["fnorm0"][0]) < 3e-6 * ref["fnorm0"][0], np.linalg.norm(F0)
+    assert rel(F0, O.F(np.zeros(fs.n))) < 1e-12
