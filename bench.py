@@ -70,7 +70,7 @@ def parse():
                          "solves), newton)")
     ap.add_argument("--learned-ne", type=int, default=64, help="elements per side of the learned-correction solve")
     ap.add_argument("--learned-epochs", type=int, default=8)
-    ap.add_argument("--newton-ne", type=int, default=24, help="elements per side of the p-Laplacian Newton run")
+    ap.add_argument("--newton-ne", type=int, default=48, help="elements per side of the p-Laplacian Newton run")
     ap.add_argument("--newton-pc", default="mg", choices=("mg", "cheb"),
                     help="Newton linear solves: Q1 multigrid (default) or the single-level Chebyshev-Jacobi")
     return ap.parse_args()
@@ -129,6 +129,15 @@ class ClockSampler:
         return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def workload_config(cfg, dofs):
+    """the `config` object of both arms' lines (identical for the same workload)"""
+    return {"workload": cfg["label"], "elements": cfg["ne"] ** 3, "dofs": dofs,
+            "block_size": 3 if cfg["kind"] == "elasticity" else 1,
+            "orders": "i.i.d. U{2..8}, seed 2" if cfg["hp"] else "p=%d" % cfg["p"], "quadrature": "Gauss (p+1)^3",
+            "mesh": "unit cube, interior vertices perturbed U[-0.1h, 0.1h], seed 1",
+            "l2": "inputs larger than L2, no flush"}
+
+
 def elem_orders(cfg, ne):
     import numpy as np
     if not cfg["hp"]:
@@ -150,13 +159,14 @@ def grf_numpy(grf, X):
 
 def cpu_baseline(cfg, threads, budget_s=20.0):
     """Oracle (CPU restatement of the reference apply: per-element geometry recompute, INTERP+GRAD, q-function,
-    INTERP_T+GRAD_T, E/E^T) timed on a bounded sample of the workload (a smaller block of the same kind, order
-    distribution and coefficient), all host threads (OpenMP; the reference runs one MPI rank per core)."""
+    INTERP_T+GRAD_T, E/E^T) timed on the full workload (same mesh, orders, coefficient and input as the GPU arm),
+    all host threads (OpenMP over elements, expand and restrict; the reference runs one MPI rank per core, each
+    on its own elements). The median of up to 10 applies after one warm-up, within budget_s."""
     import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as po
     po.build()
-    ne = min(cfg["ne"], 12 if cfg["hp"] else 32)
+    ne = cfg["ne"]
     bs = 3 if cfg["kind"] == "elasticity" else 1
     fs = po.FS(ne + 1, ne + 1, ne + 1, degree=cfg["p"], perturb=0.1, seed=1, bs=bs, elem_degree=elem_orders(cfg, ne))
     qd, kind, param = None, 0, None
@@ -178,8 +188,8 @@ def cpu_baseline(cfg, threads, budget_s=20.0):
             break
     times.sort()
     t = times[len(times) // 2]
-    return {"value": fs.n * bs / t / 1e9, "unit": "GDoF/s", "cores": threads, "kind": "port",
-            "sample": "%d^3 elements of the same workload (%d dofs), median of %d applies, oracle C restatement, %d OpenMP threads"
+    return {"value": fs.n * bs / t / 1e9, "unit": "GDoF/s", "cores": threads, "kind": "port", "dofs": fs.n * bs,
+            "sample": "the full workload, %d^3 elements (%d dofs), median of %d applies, oracle C restatement, %d OpenMP threads"
                       % (ne, fs.n * bs, len(times), threads)}
 
 
@@ -240,10 +250,11 @@ def run_reference(args, cfg, rank):
     cb = cpu_baseline(cfg, threads, budget_s=max(10.0, min(60.0, 3.0 * args.steps)))
     line = {"impl": "reference", "metric": "GDoF/s operator apply", "value": cb["value"], "unit": "GDoF/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": cfg["label"], "block_size": 3 if cfg["kind"] == "elasticity" else 1,
-                       "orders": "i.i.d. U{2..8}, seed 2" if cfg["hp"] else "p=%d" % cfg["p"], "quadrature": "Gauss (p+1)^3",
-                       "parallelism": "host threads (%d)" % threads, "sample": cb["sample"]},
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded mesh perturbation, orders, field and input)",
+            "config": workload_config(cfg, cb["dofs"]),
+            "arm": {"parallelism": "host threads (%d)" % threads, "implementation": "oracle C restatement of the reference "
+                    "apply (EllipShellMatMult / ElastShellMatMult element loop with geometry recompute, E and E^T)",
+                    "sample": cb["sample"]},
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "GDoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -348,29 +359,48 @@ def float_float_leg(op, x, y64, args, stream):
 
 
 def secondary_newton(args):
-    """p-Laplacian Newton-Krylov (exponent 1.5, eps 1e-6, p=6, f ~ U[-1,1] per dof): FP64, FP32 and BF16 inner
-    applies (Jacobian and Chebyshev-Jacobi) inside FGMRES with FP64 residuals and orthogonalisation. Per Newton
-    step: ||F||, FGMRES iterations, and the relative error of each reduced-precision run's iterate and of its
-    Jacobian apply against the FP64 run (the FP64 path is the one pinned to the oracle)."""
+    """p-Laplacian Newton-Krylov (exponent 1.5, eps 1e-6, p=6, f ~ U[-1,1] per dof; 48^3 elements by default, the
+    mixed-precision configuration's size): FP64, FP32 and BF16 inner applies (Jacobian, and the Q1 multigrid V-cycle
+    in the same precision) inside FGMRES with FP64 residuals and orthogonalisation. Each run advances one Newton step
+    at a time (wall time per step, the oracle checks between steps are not timed). Per step and per reduced-precision
+    run: the relative error of its Jacobian apply against the FP64 oracle's Jacobian apply at that run's own iterate
+    (EllipShellMatMult at the store of the iterate, ellip.c:333-377, 442-472), and the iterate's distance from the
+    FP64 run's iterate. At the first step and at each run's final iterate: the nonlinear residual ||F(u) - b|| measured
+    by the oracle's own EllipFunction (ellip.c:407-440) and the product's FP64 function against it."""
     import numpy as np
     import torch
     import dohp_gb300 as dg
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    threads = os.cpu_count() or 1
     ne, p, pe, eps = args.newton_ne, 6, 1.5, 1e-6
     fs = dg.FS((ne + 1,) * 3, degree=p, perturb=0.1, seed=1)
-    b = torch.as_tensor(np.random.default_rng(0).uniform(-1, 1, fs.n), device="cuda")
+    o = po.FS(ne + 1, ne + 1, ne + 1, degree=p, perturb=0.1, seed=1)
+    bh = np.random.default_rng(0).uniform(-1, 1, fs.n)
+    b = torch.as_tensor(bh, device="cuda")
     mg = args.newton_pc == "mg"
-    out = {"workload": "plaplace-newton-%d^3-p6: exponent 1.5, eps 1e-6 (the 48^3 shape with --newton-ne 48)" % ne,
+    out = {"workload": "plaplace-newton-%d^3-p6: exponent 1.5, eps 1e-6" % ne,
            "dofs": fs.n, "rtol": 1e-8, "lin_rtol": 1e-3, "lin_maxit": 300,
-           "ksp": ("FGMRES(30) + Q1 multigrid V-cycle (Chebyshev(3)-Jacobi smoothing, FP64)" if mg else
-                   "FGMRES(30) + Chebyshev(3)-Jacobi on the Q1-embedded Jacobian") + ", inexact steps at lin_maxit"}
+           "ksp": ("FGMRES(30) + Q1 multigrid V-cycle (Chebyshev(2)-Jacobi smoothing) in the inner precision" if mg else
+                   "FGMRES(30) + Chebyshev(3)-Jacobi on the Q1-embedded Jacobian") + ", inexact steps at lin_maxit",
+           "oracle_threads": threads}
+
+    def oracle_residual(u):
+        """||F(u) - b|| by the oracle's EllipFunction, and the product's FP64 function's relative error against it"""
+        Fo = o.function(u, 6, (pe, eps), nthreads=threads)
+        op = fs.operator(dg.dOP_PLAPLACE_JACOBIAN)
+        y = torch.zeros_like(b)
+        op.plap_function(torch.as_tensor(u, device="cuda"), pe, eps, y)
+        yh = y.cpu().numpy()
+        return float(np.linalg.norm(Fo - bh)), float(np.linalg.norm(yh - Fo) / np.linalg.norm(Fo))
+
     runs = {}
     for name, prec in (("fp64", dg.dPREC_FP64), ("fp32", dg.dPREC_FP32), ("bf16", dg.dPREC_BF16)):
         op = fs.operator(dg.dOP_PLAPLACE_JACOBIAN)
         m = fs.matrix()
         ksp = dg.KSP(op, m, ksp_type=dg.dKSP_FGMRES, inner_prec=prec, restart=30, pc=dg.dPC_MG_Q1 if mg else dg.dPC_CHEBYSHEV_Q1)
         u = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
-        runs[name] = dict(op=op, m=m, ksp=ksp, u=u, wall=0.0, fnorm=[], its=[], done=False)
-    # both runs advance one Newton step at a time so that every iterate can be compared
+        runs[name] = dict(op=op, m=m, ksp=ksp, u=u, wall=0.0, fnorm=[], its=[], done=False, prec=prec)
     per = []
     for k in range(30):
         for name, r in runs.items():
@@ -387,29 +417,39 @@ def secondary_newton(args):
             r["fnorm"].append(float(fn[1]))
             r["its"].append(int(li[0]))
             r["done"] = bool(fn[1] <= 1e-8 * r["fnorm"][0])
+            r["last_step"] = k + 1
+        row = {"step": k + 1}
         r64 = runs["fp64"]
-        if all(len(r["its"]) == k + 1 for r in runs.values()):
-            row = {"step": k + 1}
-            d = torch.as_tensor(np.random.default_rng(k).uniform(-1, 1, fs.n), device="cuda")
-            for name, prec in (("fp32", dg.dPREC_FP32), ("bf16", dg.dPREC_BF16)):
-                r = runs[name]
-                op = r["op"]
-                op.plap_stash(r["u"], pe, eps)
-                y64, yl = torch.empty_like(d), torch.empty_like(d)
-                op.set_precision(dg.dPREC_FP64)
-                op.mult(d, y64)
-                op.set_precision(prec)
-                op.mult(d, yl)
-                op.set_precision(dg.dPREC_FP64)
-                row[name + "_iterate_rel_err"] = float(torch.linalg.norm(r["u"] - r64["u"]) / torch.linalg.norm(r64["u"]))
-                row[name + "_jacobian_apply_rel_err"] = float(torch.linalg.norm(yl - y64) / torch.linalg.norm(y64))
-            per.append(row)
+        d = np.random.default_rng(100 + k).uniform(-1, 1, fs.n)
+        dd = torch.as_tensor(d, device="cuda")
+        for name in ("fp32", "bf16"):
+            r = runs[name]
+            if r.get("last_step") != k + 1:
+                continue
+            uh = r["u"].cpu().numpy()
+            st = o.plap_stash(uh, pe, eps, nthreads=threads)
+            Jo = o.apply(d, kind=1, qdata=st, nthreads=threads)
+            op = r["op"]
+            op.plap_stash(r["u"], pe, eps)
+            yl = torch.empty_like(dd)
+            op.set_precision(r["prec"])
+            op.mult(dd, yl)
+            op.set_precision(dg.dPREC_FP64)
+            row[name + "_jacobian_apply_rel_err_vs_oracle"] = float(np.linalg.norm(yl.cpu().numpy() - Jo) / np.linalg.norm(Jo))
+            row[name + "_iterate_rel_diff_vs_fp64_run"] = float(torch.linalg.norm(r["u"] - r64["u"]) / torch.linalg.norm(r64["u"]))
+        if r64.get("last_step") == k + 1 and k == 0:
+            row["fp64_oracle_residual"], row["fp64_function_rel_err_vs_oracle"] = oracle_residual(r64["u"].cpu().numpy())
+        per.append(row)
         if all(r["done"] for r in runs.values()):
             break
+    f0 = float(np.linalg.norm(bh))  # F(0) = -b: the oracle's function vanishes at u = 0
     for name, r in runs.items():
+        res, ferr = oracle_residual(r["u"].cpu().numpy())
         out[name] = {"newton_steps": len(r["its"]), "fnorm": r["fnorm"], "fgmres_its": r["its"], "wall_s": r["wall"],
-                     "converged": r["done"]}
-    out["per_step_vs_fp64"] = per
+                     "converged": r["done"], "oracle_final_rel_residual": res / f0,
+                     "fp64_function_rel_err_vs_oracle_at_final_iterate": ferr}
+    out["per_step"] = per
+    out["speedup_vs_fp64"] = {n: runs["fp64"]["wall"] / runs[n]["wall"] for n in ("fp32", "bf16")}
     return out
 
 
@@ -697,10 +737,9 @@ def main():
         "metric": "GDoF/s operator apply", "value": value, "unit": "GDoF/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded mesh perturbation, orders, field and input)",
-        "config": {"workload": cfg["label"], "elements": fs.nelem, "dofs": N, "block_size": bs,
-                   "orders": "i.i.d. U{2..8}, seed 2" if cfg["hp"] else "p=%d" % cfg["p"], "quadrature": "Gauss (p+1)^3",
-                   "launch": "persistent kernel + restriction in a CUDA graph" if cfg["hp"] else "fused element kernel + restriction",
-                   "l2": "inputs larger than L2, no flush", "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": workload_config(cfg, N),
+        "arm": {"parallelism": "replicas" if world > 1 else "single GPU",
+                "launch": "persistent kernel + restriction in a CUDA graph" if cfg["hp"] else "fused element kernel + restriction"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "traffic_source": traffic_src,
                      "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)", "kernel": kernel_name, "kernel_ms_median": kms,

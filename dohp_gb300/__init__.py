@@ -77,7 +77,7 @@ class Jacobi:
         degree = np.asarray(degree if np.ndim(degree) else [degree] * 3, dtype=np.int32)
         rule_order = np.asarray(rule_order if rule_order is not None else 2 * degree, dtype=np.int32)
         h = _vp()
-        chk(lib().dJacobiGetEFS(self.h, ptr(degree), ctypes.c_int(method), ptr(rule_order), ctypes.byref(h)))
+        chk(lib().dJacobiGetEFSTensor(self.h, ptr(degree), ctypes.c_int(method), ptr(rule_order), ctypes.byref(h)))
         return EFS(h, self)
 
     def __del__(self):

@@ -177,12 +177,19 @@ dErr dJacobiDestroy(dJacobi *jac) {
     cudaFree(kv.second->d_tab);
     delete kv.second;
   }
+  jacobi_free_quadratures(*jac);
   delete *jac;
   *jac = nullptr;
   return 0;
 }
 
-dErr dJacobiGetEFS(dJacobi jac, const dInt degree[3], dQuadratureMethod method, const dInt rule_order[3], dEFS *efs) {
+dErr dJacobiGetEFSTensor(dJacobi jac, const dInt degree[3], dQuadratureMethod method, const dInt rule_order[3], dEFS *efs) {
+  return jacobi_efs(jac, degree, method, rule_order, efs);
+}
+
+}  // extern "C"
+
+dErr jacobi_efs(dJacobi jac, const dInt degree[3], dQuadratureMethod method, const dInt rule_order[3], dEFS *efs) {
   if (!jac || !efs) return set_error("null argument");
   std::vector<int> key = {degree[0], degree[1], degree[2], (int)method, rule_order[0], rule_order[1], rule_order[2]};
   auto it = jac->efs.find(key);
@@ -213,12 +220,22 @@ dErr dJacobiGetEFS(dJacobi jac, const dInt degree[3], dQuadratureMethod method, 
     tab.insert(tab.end(), b.B, b.B + b.P * b.Q);
     tab.insert(tab.end(), b.D, b.D + b.P * b.Q);
   }
+  {
+    const int ro[3] = {rule_order[0], rule_order[1], rule_order[2]};
+    dErr e = jacobi_rule(jac, method, ro, &f->rule);
+    if (e) {
+      delete f;
+      return e;
+    }
+  }
   CUCHK(cudaMalloc(&f->d_tab, tab.size() * sizeof(double)));
   CUCHK(cudaMemcpy(f->d_tab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
   jac->efs[key] = f;
   *efs = f;
   return 0;
 }
+
+extern "C" {
 
 dErr dEFSGetSizes(dEFS efs, dInt *dim, dInt *inodes, dInt *total) {
   if (!efs) return set_error("null EFS");

@@ -50,13 +50,18 @@ int make_basis(int p, dQuadratureMethod method, Basis1D *b);
 struct _p_dEFS {
   int P[3], Q[3];
   dQuadratureMethod method;
+  _p_dRule *rule = nullptr;  // the rule the basis is evaluated on (owned by the dJacobi's quadrature)
   dgb::Basis1D b[3];
   double *d_tab = nullptr;  // device: per direction B[Q][P], D[Q][P] packed
 };
 
 struct _p_dJacobi {
   std::map<std::vector<int>, _p_dEFS *> efs;
+  _p_dQuadrature *quad[3] = {nullptr, nullptr, nullptr};  // per dQuadratureMethod, made on first request
 };
+void jacobi_free_quadratures(dJacobi jac);
+dErr jacobi_rule(dJacobi jac, dQuadratureMethod method, const int order[3], _p_dRule **out);
+dErr jacobi_efs(dJacobi jac, const dInt degree[3], dQuadratureMethod method, const dInt rule_order[3], dEFS *efs);
 
 struct _p_dMesh {
   int nx, ny, nz;

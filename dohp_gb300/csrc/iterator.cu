@@ -126,8 +126,8 @@ dErr dRulesetIteratorCreate(dFS fs, dQuadratureMethod method, dRulesetIterator *
     IterBucket B;
     const dInt deg[3] = {kv.first[0], kv.first[1], kv.first[2]}, one[3] = {1, 1, 1};
     const dInt ro[3] = {2 * deg[0], 2 * deg[1], 2 * deg[2]};
-    dErr e = dJacobiGetEFS(fs->jac, deg, method, ro, &B.efs);
-    if (!e) e = dJacobiGetEFS(fs->jac, one, method, ro, &B.cefs);
+    dErr e = jacobi_efs(fs->jac, deg, method, ro, &B.efs);
+    if (!e) e = jacobi_efs(fs->jac, one, method, ro, &B.cefs);
     if (e) {
       dRulesetIteratorDestroy(&I);
       return e;

@@ -230,7 +230,7 @@ dErr op_compute_geometry(_p_dOperator *op) {
 
 template <typename T>
 dErr diffusion_apply_t(_p_dFS *fs, const double *x, const T *geo, T *yexp) {
-  if (!fs->uniform) return set_error("fused diffusion apply needs a uniform-degree space (hp path not built yet)");
+  if (!fs->uniform) return set_error("fused uniform-order diffusion apply called on a space with per-element orders (hp spaces apply through the order-bucket launches)");
   switch (fs->p + 1) {
     case 2: return launch_diffusion<2, T>(fs, x, geo, yexp);
     case 3: return launch_diffusion<3, T>(fs, x, geo, yexp);
@@ -461,6 +461,10 @@ extern "C" dErr dOperatorMultNoAlloc(dOperator op, const dScalar *x, dScalar *y)
   if (!op) return set_error("null operator");
   _p_dFS *fs = op->fs;
   if (op->kind != dOP_DIFFUSION) return set_error("dOperatorMultNoAlloc: operator kind %d not supported", (int)op->kind);
+  if (!fs->uniform) return set_error("dOperatorMultNoAlloc: uniform-order spaces only (this space has per-element orders)");
+  if (op->prec != dPREC_FP64)
+    return set_error("dOperatorMultNoAlloc: applies in FP64 only; the operator's precision is set to %d (dOperatorSetPrecision "
+                     "dPREC_FP64 first, or use dOperatorMult)", (int)op->prec);
   if (!op->geo_valid || op->geo_kind != 0)
     return set_error("dOperatorMultNoAlloc: the operator's geometric factors do not exist yet; make one dOperatorMult "
                      "call at set-up time (where allocation is allowed) after the last dOperatorSetQuadratureData");

@@ -324,7 +324,7 @@ dErr dFSAssembleQ1PLaplace(dFS fs, dMat J, const dScalar *g, dReal p, dReal eps,
   if (!(p > 1 && p <= 2)) return set_error("p-Laplacian exponent %g outside (1, 2]", p);
   const dInt deg[3] = {fs->p, fs->p, fs->p}, ro[3] = {2 * fs->p, 2 * fs->p, 2 * fs->p};
   dEFS sefs;
-  DCHK(dJacobiGetEFS(fs->jac, deg, dQUADRATURE_METHOD_SPARSE, ro, &sefs));
+  DCHK(jacobi_efs(fs->jac, deg, dQUADRATURE_METHOD_SPARSE, ro, &sefs));
   const int64_t npts = fs->nelem * (int64_t)sefs->Q[0] * sefs->Q[1] * sefs->Q[2];
   double *dref;
   CUCHK(cudaMalloc(&dref, npts * 3 * sizeof(double)));

@@ -1,0 +1,308 @@
+// dJacobi quadrature, rules and explicit element bases on the host (src/jacobi/interface/jacobi.c,
+// quadrature.c; src/jacobi/quadrature/impls/tensor/tensorquad.c; src/jacobi/impls/tensor/efstopo.c:660-717),
+// plus the vector constructors of a dFS.
+//
+// A dQuadrature is owned by its dJacobi (one per method, made on first request, as dJacobiGetQuadrature caches
+// it); a dRule is a tensor Gauss (FAST), composite two-point (SPARSE) or Lobatto (SELF) rule on the reference
+// hex, owned by its dQuadrature and shared by every caller that asks for the same orders. Arrays of handles
+// returned by dQuadratureGetRules / dJacobiGetEFS are the caller's and are released with dFree, as in dohp.
+#include <stdlib.h>
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <vector>
+
+#include "internal.h"
+
+using namespace dgb;
+
+struct _p_dRule {
+  dQuadratureMethod method;
+  int order[3];  // polynomial order integrated exactly, per direction
+  int Q[3];
+  double x[3][MAXQ], w[3][MAXQ];
+};
+
+struct _p_dQuadrature {
+  dQuadratureMethod method;
+  std::map<std::vector<int>, _p_dRule *> rules;
+};
+
+dErr jacobi_efs(dJacobi jac, const dInt degree[3], dQuadratureMethod method, const dInt rule_order[3], dEFS *efs);
+
+void jacobi_free_quadratures(dJacobi jac) {
+  for (auto &q : jac->quad) {
+    if (!q) continue;
+    for (auto &kv : q->rules) delete kv.second;
+    delete q;
+    q = nullptr;
+  }
+}
+
+dErr quad_rule(_p_dQuadrature *q, const int order[3], _p_dRule **out);
+
+// the rule of the given method and orders, owned by the dJacobi's quadrature (used for every dEFS's rule)
+dErr jacobi_rule(dJacobi jac, dQuadratureMethod method, const int order[3], _p_dRule **out) {
+  dQuadrature q;
+  DCHK(dJacobiGetQuadrature(jac, method, &q));
+  return quad_rule(q, order, out);
+}
+
+dErr quad_rule(_p_dQuadrature *q, const int order[3], _p_dRule **out) {
+  std::vector<int> key = {order[0], order[1], order[2]};
+  auto it = q->rules.find(key);
+  if (it != q->rules.end()) {
+    *out = it->second;
+    return 0;
+  }
+  _p_dRule *r = new _p_dRule();
+  r->method = q->method;
+  for (int d = 0; d < 3; d++) {
+    if (order[d] < 0 || order[d] > 2 * MAXQ) {
+      delete r;
+      return set_error("rule order %d out of range", order[d]);
+    }
+    r->order[d] = order[d];
+    double x[64], w[64];
+    const int n = rule_1d(q->method, order[d], x, w);
+    if (n < 1 || n > MAXQ) {
+      delete r;
+      return set_error("rule of order %d has %d points (at most %d supported)", order[d], n, MAXQ);
+    }
+    r->Q[d] = n;
+    std::copy(x, x + n, r->x[d]);
+    std::copy(w, w + n, r->w[d]);
+  }
+  q->rules[key] = r;
+  *out = r;
+  return 0;
+}
+
+namespace {
+
+// dGeomInvert3 (include/dohpgeom.h:57-79): cofactor inverse and determinant
+double invert3_host(const double a[9], double b[9]) {
+  const double c0 = a[4] * a[8] - a[7] * a[5], c3 = -(a[3] * a[8] - a[6] * a[5]), c6 = a[3] * a[7] - a[6] * a[4];
+  const double det = a[0] * c0 + a[1] * c3 + a[2] * c6, id = 1.0 / det;
+  b[0] = id * c0;
+  b[1] = -id * (a[1] * a[8] - a[7] * a[2]);
+  b[2] = id * (a[1] * a[5] - a[4] * a[2]);
+  b[3] = id * c3;
+  b[4] = id * (a[0] * a[8] - a[6] * a[2]);
+  b[5] = -id * (a[0] * a[5] - a[3] * a[2]);
+  b[6] = id * c6;
+  b[7] = -id * (a[0] * a[7] - a[6] * a[1]);
+  b[8] = id * (a[0] * a[4] - a[3] * a[1]);
+  return det;
+}
+
+}  // namespace
+
+extern "C" {
+
+dErr dFree(void *ptr) {
+  free(ptr);
+  return 0;
+}
+
+dErr dJacobiGetQuadrature(dJacobi jac, dQuadratureMethod method, dQuadrature *quad) {
+  if (!jac || !quad) return set_error("null argument");
+  if (method != dQUADRATURE_METHOD_FAST && method != dQUADRATURE_METHOD_SPARSE && method != dQUADRATURE_METHOD_SELF)
+    return set_error("invalid quadrature method %d", (int)method);
+  if (!jac->quad[method]) {
+    jac->quad[method] = new _p_dQuadrature();
+    jac->quad[method]->method = method;
+  }
+  *quad = jac->quad[method];
+  return 0;
+}
+
+dErr dQuadratureGetRules(dQuadrature quad, dInt n, const dEntTopology topo[], const dPolynomialOrder order[], dRule **rules) {
+  if (!quad || !rules || (n > 0 && (!topo || !order))) return set_error("null argument");
+  *rules = nullptr;
+  dRule *arr = (dRule *)malloc(sizeof(dRule) * (size_t)std::max<dInt>(n, 1));
+  if (!arr) return set_error("out of host memory");
+  for (dInt i = 0; i < n; i++) {
+    if (topo[i] != dTOPO_HEX) {
+      free(arr);
+      return set_error("dQuadratureGetRules: topology %d not supported (hexahedra only)", (int)topo[i]);
+    }
+    const int o[3] = {dPolynomialOrder1D(order[i], 0), dPolynomialOrder1D(order[i], 1), dPolynomialOrder1D(order[i], 2)};
+    dErr e = quad_rule(quad, o, &arr[i]);
+    if (e) {
+      free(arr);
+      return e;
+    }
+  }
+  *rules = arr;
+  return 0;
+}
+
+dErr dRuleGetSize(dRule rule, dInt *dim, dInt *nnodes) {
+  if (!rule) return set_error("null rule");
+  if (dim) *dim = 3;
+  if (nnodes) *nnodes = rule->Q[0] * rule->Q[1] * rule->Q[2];
+  return 0;
+}
+
+dErr dRuleGetTensorNodeWeight(dRule rule, dInt *dim, dInt nnodes[3], const dReal *coord[3], const dReal *weight[3]) {
+  if (!rule) return set_error("null rule");
+  if (dim) *dim = 3;
+  for (int d = 0; d < 3; d++) {
+    if (nnodes) nnodes[d] = rule->Q[d];
+    if (coord) coord[d] = rule->x[d];
+    if (weight) weight[d] = rule->w[d];
+  }
+  return 0;
+}
+
+dErr dRuleGetNodeWeight(dRule rule, dReal *coord, dReal *weight) {
+  if (!rule) return set_error("null rule");
+  const int *Q = rule->Q;
+  for (int i = 0; i < Q[0]; i++)
+    for (int j = 0; j < Q[1]; j++)
+      for (int k = 0; k < Q[2]; k++) {
+        const int q = (i * Q[1] + j) * Q[2] + k;
+        if (coord) coord[3 * q] = rule->x[0][i], coord[3 * q + 1] = rule->x[1][j], coord[3 * q + 2] = rule->x[2][k];
+        if (weight) weight[q] = rule->w[0][i] * rule->w[1][j] * rule->w[2][k];
+      }
+  return 0;
+}
+
+dErr dRuleComputePhysical(dRule rule, const dScalar jac[], dReal jinv[], dReal jw[]) {
+  if (!rule || !jinv || !jw) return set_error("null argument");
+  const int n = rule->Q[0] * rule->Q[1] * rule->Q[2];
+  DCHK(dRuleGetNodeWeight(rule, nullptr, jw));
+  for (int i = 0; i < n; i++) {
+    if (!jac) {
+      for (int k = 0; k < 9; k++) jinv[9 * i + k] = (k % 4 == 0) ? 1.0 : 0.0;
+      continue;
+    }
+    const double det = invert3_host(jac + 9 * i, jinv + 9 * i);
+    if (det < 0.) return set_error("Negative Jacobian at node %d", i);
+    jw[i] *= det;
+  }
+  return 0;
+}
+
+dErr dJacobiGetEFS(dJacobi jac, dInt n, const dEntTopology topo[], const dPolynomialOrder order[], const dRule rules[], dEFS **efs) {
+  if (!jac || !efs || (n > 0 && (!topo || !order || !rules))) return set_error("null argument");
+  *efs = nullptr;
+  dEFS *arr = (dEFS *)malloc(sizeof(dEFS) * (size_t)std::max<dInt>(n, 1));
+  if (!arr) return set_error("out of host memory");
+  for (dInt i = 0; i < n; i++) {
+    if (topo[i] != dTOPO_HEX) {
+      free(arr);
+      return set_error("dJacobiGetEFS: topology %d not supported (hexahedra only)", (int)topo[i]);
+    }
+    const dInt deg[3] = {dPolynomialOrder1D(order[i], 0), dPolynomialOrder1D(order[i], 1), dPolynomialOrder1D(order[i], 2)};
+    dErr e = jacobi_efs(jac, deg, rules[i]->method, rules[i]->order, &arr[i]);
+    if (e) {
+      free(arr);
+      return e;
+    }
+  }
+  *efs = arr;
+  return 0;
+}
+
+dErr dEFSGetRule(dEFS efs, dRule *rule) {
+  if (!efs || !rule) return set_error("null argument");
+  *rule = efs->rule;
+  return 0;
+}
+
+// dEFSGetExplicitSparse (src/jacobi/interface/jacobi.c:592-609): Q1 bases on the GLL sub-cells of a SPARSE rule
+// (dEFSGetExplicitSparse_Tensor_Hex, efstopo.c:660-717, when every patch has 8 points and the patches are the
+// element's sub-cells) or else the element's own basis at each patch's points (dEFSGetExplicitSparse_Basic,
+// jacobi.c:611-643). cjinv: inverse Jacobians of the element's points, read at index pidx*8+q on the sub-cell
+// path (the reference's indexing; the points are element-natural there) and through qidx on the basic path.
+dErr dEFSGetExplicitSparse(dEFS efs, dInt npatches, dInt Q, const dInt qidx[], const dReal cjinv[], dInt eoffset, dInt *P, dInt eidx[],
+                           dReal interp[], dReal deriv[]) {
+  if (!efs || !qidx || !P || !eidx || !interp || !deriv) return set_error("null argument");
+  if (npatches <= 0 || Q <= 0) return set_error("dEFSGetExplicitSparse: npatches and Q must be positive");
+  const int px = efs->P[0] - 1, py = efs->P[1] - 1, pz = efs->P[2] - 1;
+  static const double s1 = 0.78867513459481287, s0 = 0.21132486540518713;
+  const double interp1[2][2] = {{s1, s0}, {s0, s1}}, deriv1[2][2] = {{-1., 1.}, {-1., 1.}};
+  if (Q == 8 && px * py * pz == npatches) {
+    *P = 8;
+    for (int i = 0; i < px; i++)
+      for (int j = 0; j < py; j++)
+        for (int k = 0; k < pz; k++) {
+          const int pidx = (i * py + j) * pz + k;
+          for (int b = 0; b < 8; b++) {
+            const int bi = b >> 2, bj = (b >> 1) & 1, bk = b & 1;
+            eidx[pidx * 8 + b] = eoffset + ((i + bi) * (py + 1) + j + bj) * (pz + 1) + k + bk;
+          }
+          for (int q = 0; q < 8; q++) {
+            const int ii = q >> 2, jj = (q >> 1) & 1, kk = q & 1;
+            if (qidx[pidx * Q + q] != ((i * 2 + ii) * py * 2 + (j * 2 + jj)) * pz * 2 + (k * 2 + kk))
+              return set_error("dEFSGetExplicitSparse: unexpected qidx at patch %d point %d", pidx, q);
+            double M[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+            if (cjinv) std::copy(cjinv + (pidx * 8 + q) * 9, cjinv + (pidx * 8 + q) * 9 + 9, M);
+            for (int b = 0; b < 8; b++) {
+              const int bi = b >> 2, bj = (b >> 1) & 1, bk = b & 1;
+              const int off = (pidx * Q + q) * 8 + b;
+              const double dX = deriv1[ii][bi] * interp1[jj][bj] * interp1[kk][bk];
+              const double dY = interp1[ii][bi] * deriv1[jj][bj] * interp1[kk][bk];
+              const double dZ = interp1[ii][bi] * interp1[jj][bj] * deriv1[kk][bk];
+              interp[off] = interp1[ii][bi] * interp1[jj][bj] * interp1[kk][bk];
+              for (int l = 0; l < 3; l++) deriv[off * 3 + l] = dX * M[0 * 3 + l] + dY * M[1 * 3 + l] + dZ * M[2 * 3 + l];
+            }
+          }
+        }
+    return 0;
+  }
+  // the element's own basis, one row per patch point (through qidx into element-natural order)
+  const int *Pn = efs->P, *Qn = efs->Q, eP = Pn[0] * Pn[1] * Pn[2], eQ = Qn[0] * Qn[1] * Qn[2];
+  *P = eP;
+  for (int pt = 0; pt < npatches; pt++) {
+    for (int k = 0; k < eP; k++) eidx[pt * eP + k] = eoffset + k;
+    for (int j = 0; j < Q; j++) {
+      const int pq = pt * Q + j, eq = qidx[pq];
+      if (eq < 0 || eq >= eQ) return set_error("dEFSGetExplicitSparse: qidx %d out of range", eq);
+      const int a = eq / (Qn[1] * Qn[2]), b = (eq / Qn[2]) % Qn[1], c = eq % Qn[2];
+      double M[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+      if (cjinv) std::copy(cjinv + eq * 9, cjinv + eq * 9 + 9, M);
+      for (int k = 0; k < eP; k++) {
+        const int ki = k / (Pn[1] * Pn[2]), kj = (k / Pn[2]) % Pn[1], kk = k % Pn[2];
+        const double Bx = efs->b[0].B[a * Pn[0] + ki], By = efs->b[1].B[b * Pn[1] + kj], Bz = efs->b[2].B[c * Pn[2] + kk];
+        const double Dx = efs->b[0].D[a * Pn[0] + ki], Dy = efs->b[1].D[b * Pn[1] + kj], Dz = efs->b[2].D[c * Pn[2] + kk];
+        const double d0 = Dx * By * Bz, d1 = Bx * Dy * Bz, d2 = Bx * By * Dz;
+        interp[pq * eP + k] = Bx * By * Bz;
+        for (int l = 0; l < 3; l++) deriv[(pq * eP + k) * 3 + l] = d0 * M[0 * 3 + l] + d1 * M[1 * 3 + l] + d2 * M[2 * 3 + l];
+      }
+    }
+  }
+  return 0;
+}
+
+// dFSCreateExpandedVector / dFSCreateGlobalVector (include/dohpfs.h:77-78): zeroed device vectors of the space's
+// expanded (nexp * bs) and global (n * bs) sizes; released with dVecDestroy
+dErr dFSCreateExpandedVector(dFS fs, dScalar **x) {
+  if (!fs || !x) return set_error("null argument");
+  if (!fs->setup) return set_error("dFS not set up");
+  const size_t bytes = (size_t)std::max<int64_t>(fs->nexp * fs->bs, 1) * sizeof(double);
+  CUCHK(cudaMalloc(x, bytes));
+  CUCHK(cudaMemsetAsync(*x, 0, bytes, fs->stream));
+  return 0;
+}
+
+dErr dFSCreateGlobalVector(dFS fs, dScalar **x) {
+  if (!fs || !x) return set_error("null argument");
+  if (!fs->setup) return set_error("dFS not set up");
+  const size_t bytes = (size_t)std::max<int64_t>(fs->n * fs->bs, 1) * sizeof(double);
+  CUCHK(cudaMalloc(x, bytes));
+  CUCHK(cudaMemsetAsync(*x, 0, bytes, fs->stream));
+  return 0;
+}
+
+dErr dVecDestroy(dScalar **x) {
+  if (!x || !*x) return 0;
+  CUCHK(cudaFree(*x));
+  *x = nullptr;
+  return 0;
+}
+
+}  // extern "C"

@@ -50,7 +50,31 @@ typedef enum {
   dFSBSTATUS_WEAK = (0xffff + 1) << 1
 } dFSBStatus;
 
+/* include/dohptype.h:84-86: entity topologies (the element loop and the rules handle dTOPO_HEX) */
+typedef enum {
+  dTOPO_POINT, dTOPO_LINE, dTOPO_POLYGON, dTOPO_TRIANGLE, dTOPO_QUAD, dTOPO_POLYHEDRON, dTOPO_TET, dTOPO_HEX,
+  dTOPO_PRISM, dTOPO_PYRAMID, dTOPO_SEPTAHEDRON, dTOPO_ALL
+} dEntTopology;
+/* include/dohpjacobi.h:51-81: a polynomial order in 3-D, four bytes {max, x, y, z}; a zero direction takes max */
+typedef union {
+  struct {
+    unsigned char max, x, y, z;
+  } s;
+  int padding_;
+} dPolynomialOrder;
+static inline dPolynomialOrder dPolynomialOrderCreate(dInt max, dInt x, dInt y, dInt z) {
+  dPolynomialOrder o;
+  o.s.max = (unsigned char)max, o.s.x = (unsigned char)x, o.s.y = (unsigned char)y, o.s.z = (unsigned char)z;
+  return o;
+}
+static inline dInt dPolynomialOrder1D(dPolynomialOrder o, dInt dir) {
+  const dInt d = dir == 0 ? o.s.x : dir == 1 ? o.s.y : dir == 2 ? o.s.z : 0;
+  return d ? d : o.s.max;
+}
+
 typedef struct _p_dJacobi *dJacobi;
+typedef struct _p_dQuadrature *dQuadrature;
+typedef struct _p_dRule *dRule;
 typedef struct _p_dEFS *dEFS;
 typedef struct _p_dMesh *dMesh;
 typedef struct _p_dFS *dFS;
@@ -84,10 +108,38 @@ const char *dGetLastError(void);
 /* dJacobiCreate (src/jacobi/interface/jacobi.c) with the tensor (GLL nodal) type */
 dErr dJacobiCreate(dJacobi *jac);
 dErr dJacobiDestroy(dJacobi *jac);
-/* dJacobiGetEFS (include/dohpjacobi.h:169) for one hex topology: basis degree per direction and a
- * tensor rule (method, rule order per direction as produced by dFSGetPreferredQuadratureRuleSet).
- * The EFS is cached and owned by the dJacobi. */
-dErr dJacobiGetEFS(dJacobi jac, const dInt degree[3], dQuadratureMethod method, const dInt rule_order[3], dEFS *efs);
+/* release an array the library allocated for the caller (dQuadratureGetRules, dJacobiGetEFS), as dohp's dFree */
+dErr dFree(void *ptr);
+/* dJacobiGetQuadrature (include/dohpjacobi.h:170, src/jacobi/interface/jacobi.c:268-285): the dJacobi's quadrature
+ * for a method, made on first request and owned by the dJacobi */
+dErr dJacobiGetQuadrature(dJacobi jac, dQuadratureMethod method, dQuadrature *quad);
+/* dQuadratureGetRules (src/jacobi/interface/quadrature.c:17-29): *rules = a new array (dFree) of n rules integrating
+ * order[i] exactly on the reference hex (tensorquad.c:51-118: FAST n = 1 + order/2 Gauss points, SPARSE two Gauss
+ * points per GLL sub-interval, SELF Lobatto); the rules themselves are owned by the quadrature. Hexahedra only. */
+dErr dQuadratureGetRules(dQuadrature quad, dInt n, const dEntTopology topo[], const dPolynomialOrder order[], dRule **rules);
+/* dRuleGetSize / dRuleGetNodeWeight / dRuleGetTensorNodeWeight (include/dohpjacobi.h:186-189): host arrays; nodes
+ * [n][3] and weights [n] in tensor order (x slowest); the 1-D tables are owned by the rule */
+dErr dRuleGetSize(dRule rule, dInt *dim, dInt *nnodes);
+dErr dRuleGetNodeWeight(dRule rule, dReal *coord, dReal *weight);
+dErr dRuleGetTensorNodeWeight(dRule rule, dInt *dim, dInt nnodes[3], const dReal *coord[3], const dReal *weight[3]);
+/* dRuleComputePhysical (src/jacobi/interface/jacobi.c:383-414): jinv [n][9] = jac^-1 (dGeomInvert3), jw [n] = w det jac;
+ * jac NULL gives identities and the rule weights; a negative determinant is an error. Host arrays. */
+dErr dRuleComputePhysical(dRule rule, const dScalar jac[], dReal jinv[], dReal jw[]);
+/* dJacobiGetEFS (include/dohpjacobi.h:169): *efs = a new array (dFree) of n element spaces, basis degrees order[i] on
+ * rules[i]; the dEFS objects are cached and owned by the dJacobi. Hexahedra only. */
+dErr dJacobiGetEFS(dJacobi jac, dInt n, const dEntTopology topo[], const dPolynomialOrder order[], const dRule rules[], dEFS **efs);
+/* the same for one hex from plain arrays (basis degree and rule order per direction) */
+dErr dJacobiGetEFSTensor(dJacobi jac, const dInt degree[3], dQuadratureMethod method, const dInt rule_order[3], dEFS *efs);
+/* dEFSGetRule (include/dohpjacobi.h:176) */
+dErr dEFSGetRule(dEFS efs, dRule *rule);
+/* dEFSGetExplicitSparse (include/dohpjacobi.h:181, src/jacobi/interface/jacobi.c:592-643): explicit bases of npatches
+ * patches of Q points each (qidx [npatches][Q]: the patch points' element-natural indices, dRuleGetPatches): with 8
+ * points per patch and the p_x p_y p_z GLL sub-cells as patches, the Q1 sub-cell bases of efstopo.c:660-717 (P = 8,
+ * derivatives with respect to the unit sub-cell coordinate mapped by cjinv [pidx*8+q]), otherwise the element's own
+ * basis at each patch point (P = nodes of the element, cjinv read through qidx). cjinv NULL: reference coordinates.
+ * Outputs (host): eidx [npatches][P] = eoffset + element node, interp [npatches][Q][P], deriv [npatches][Q][P][3]. */
+dErr dEFSGetExplicitSparse(dEFS efs, dInt npatches, dInt Q, const dInt qidx[], const dReal cjinv[], dInt eoffset, dInt *P,
+                           dInt eidx[], dReal interp[], dReal deriv[]);
 /* dEFSGetSizes (include/dohpjacobi.h:172): dim, interior nodes, total nodes */
 dErr dEFSGetSizes(dEFS efs, dInt *dim, dInt *inodes, dInt *total);
 /* dEFSGetTensorNodes / dRuleGetTensorNodeWeight: host copies of basis nodes, rule points, weights */
@@ -133,6 +185,11 @@ dErr dFSGetExpandedMap(dFS fs, dInt *emap, dInt *xstart);
 dErr dFSGetElementAssemblyMatrix(dFS fs, int64_t *nnz, dInt *rowptr, dInt *col, dReal *val);
 /* host copy of per-element degrees (3 per element after propagation) */
 dErr dFSGetElementDegrees(dFS fs, dInt *deg);
+/* dFSCreateExpandedVector / dFSCreateGlobalVector (include/dohpfs.h:77-78): new zeroed device vectors of nexp*bs and
+ * n*bs values (PETSc Vec -> device array), released with dVecDestroy */
+dErr dFSCreateExpandedVector(dFS fs, dScalar **x);
+dErr dFSCreateGlobalVector(dFS fs, dScalar **x);
+dErr dVecDestroy(dScalar **x);
 /* dFSGetGeometryVectorExpanded (src/fs/interface/fsgeom.c:216-227): device [nelem][8][3] */
 dErr dFSGetGeometryVectorExpanded(dFS fs, const dReal **coords);
 /* dFSInhomogeneousDirichletCommit (src/fs/interface/fs.c:527-541): cache the Dirichlet part of a closure vector */
@@ -186,7 +243,8 @@ dErr dOperatorMultExpanded(dOperator op, const dScalar *x, dScalar *yexp);
  * call cudaMalloc/cudaFree while they run: applications that give all device memory to their own pool or
  * arena, and solver callbacks running beside other streams, where cudaMalloc/cudaFree may synchronize
  * the device. Its temporary lives in a fixed 8 MiB device array per GPU (at most 1,048,576 expanded
- * values, nexp*bs); larger spaces are rejected with an error. dOP_DIFFUSION only. Requires one ordinary
+ * values, nexp*bs); larger spaces are rejected with an error. dOP_DIFFUSION on uniform-order spaces only, and
+ * always in FP64: an operator whose precision (dOperatorSetPrecision) is not dPREC_FP64 is refused. Requires one ordinary
  * dOperatorMult call first (after the last dOperatorSetQuadratureData), which builds the geometric factors.
  * The first call on a device looks up the array's device address; make it before any stream capture.
  * All calls share the array: calls that overlap on the GPU race. */

@@ -446,6 +446,9 @@ struct or_fs {
   int64_t *eptr;
   int32_t *ecol;
   double *eval;
+  /* E^T as CSR over closure nodes, expanded rows ascending (made on the first threaded apply) */
+  int64_t *tptr, *trow;
+  double *tval;
 };
 
 /* Lagrange basis on the degree-p GLL nodes at t */
@@ -1020,6 +1023,7 @@ void or_fs_destroy(or_fs *m)
   free(m->ordered); free(m->goff); free(m->gcoff); free(m->inodes);
   free(m->xstart); free(m->emap); free(m->edeg); free(m->xexp);
   free(m->cptr); free(m->ccol); free(m->cval); free(m->eptr); free(m->ecol); free(m->eval);
+  free(m->tptr); free(m->trow); free(m->tval);
   free(m);
 }
 
@@ -1072,6 +1076,64 @@ void or_fs_expanded_to_global(const or_fs *m, const double *x, double *g, int ad
       for (int b = 0; b < bs; b++) cl[(int64_t)m->ecol[k] * bs + b] += m->eval[k] * x[r * bs + b];
   for (int64_t i = 0; i < m->n * bs; i++) g[i] = add ? g[i] + cl[i] : cl[i];
   free(cl);
+}
+
+/* The same expand and restrict with host threads: the reference runs one MPI rank per core, each expanding
+ * and restricting its own partition; here rows of E (expand) and rows of E^T (restrict, each closure node's
+ * terms summed in ascending expanded order, the order of the serial loop above) are split over threads, so
+ * the results are bit-identical to the serial forms. */
+static void fs_make_et(or_fs *m)
+{
+  if (m->tptr) return;
+  const int64_t nnz = m->eptr[m->nexp];
+  int64_t *ptr = calloc((size_t)m->nc + 1, sizeof(int64_t)), *row = malloc(sizeof(int64_t) * (nnz ? nnz : 1));
+  double *val = malloc(sizeof(double) * (nnz ? nnz : 1));
+  for (int64_t k = 0; k < nnz; k++) ptr[m->ecol[k] + 1]++;
+  for (int64_t c = 0; c < m->nc; c++) ptr[c + 1] += ptr[c];
+  int64_t *fill = malloc(sizeof(int64_t) * ((size_t)m->nc + 1));
+  memcpy(fill, ptr, sizeof(int64_t) * ((size_t)m->nc + 1));
+  for (int64_t r = 0; r < m->nexp; r++)
+    for (int64_t k = m->eptr[r]; k < m->eptr[r + 1]; k++) {
+      const int64_t at = fill[m->ecol[k]]++;
+      row[at] = r;
+      val[at] = m->eval[k];
+    }
+  free(fill);
+  m->tptr = ptr, m->trow = row, m->tval = val;
+}
+
+static void fs_expand_par(const or_fs *m, const double *g, const double *dcache, double *x, int nthreads)
+{
+  const int bs = m->bs;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+#endif
+  for (int64_t r = 0; r < m->nexp; r++)
+    for (int b = 0; b < bs; b++) {
+      double v = 0;
+      for (int64_t k = m->eptr[r]; k < m->eptr[r + 1]; k++) {
+        const int64_t c = m->ecol[k];
+        const double cv = c < m->n ? g[c * bs + b] : (dcache ? dcache[(c - m->n) * bs + b] : 0.0);
+        v = (k == m->eptr[r]) ? m->eval[k] * cv : v + m->eval[k] * cv;
+      }
+      x[r * bs + b] = v;
+    }
+  (void)nthreads;
+}
+
+static void fs_restrict_par(const or_fs *m, const double *x, double *g, int nthreads)
+{
+  const int bs = m->bs;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+#endif
+  for (int64_t c = 0; c < m->n; c++)
+    for (int b = 0; b < bs; b++) {
+      double v = 0;
+      for (int64_t k = m->tptr[c]; k < m->tptr[c + 1]; k++) v += m->tval[k] * x[m->trow[k] * bs + b];
+      g[c * bs + b] = v;
+    }
+  (void)nthreads;
 }
 
 /* ----------------------------------------------------------------------------------------------
@@ -1287,10 +1349,11 @@ static int operator_eval(const or_fs *m, int kind, const double *qdata, const do
   double *xexp = malloc(sizeof(double) * m->nexp * bs), *yexp = malloc(sizeof(double) * m->nexp * bs);
   int32_t *qoff = malloc(sizeof(int32_t) * (m->nr + 1));
   or_fs_num_qpts(m, qoff);
-  or_fs_global_to_expanded(m, g, dcache, xexp);
+  if (nthreads < 1) nthreads = 1;
+  fs_make_et((or_fs *)m);
+  fs_expand_par(m, g, dcache, xexp, nthreads);
   int err = 0;
 #ifdef _OPENMP
-  if (nthreads < 1) nthreads = 1;
 #pragma omp parallel num_threads(nthreads) reduction(| : err)
 #endif
   {
@@ -1299,7 +1362,7 @@ static int operator_eval(const or_fs *m, int kind, const double *qdata, const do
     double *u = malloc(sizeof(double) * D * maxq), *du = malloc(sizeof(double) * 3 * D * maxq);
     double *v = malloc(sizeof(double) * D * maxq), *dv = malloc(sizeof(double) * 3 * D * maxq);
 #ifdef _OPENMP
-#pragma omp for schedule(static)
+#pragma omp for schedule(dynamic, 16)
 #endif
     for (int64_t r = 0; r < m->nr; r++) {
       const basis1d *b[3] = {&B[m->edeg[3 * r]], &B[m->edeg[3 * r + 1]], &B[m->edeg[3 * r + 2]]};
@@ -1324,7 +1387,7 @@ static int operator_eval(const or_fs *m, int kind, const double *qdata, const do
     }
     free(xq); free(jinv); free(jw); free(u); free(du); free(v); free(dv);
   }
-  if (!err) or_fs_expanded_to_global(m, yexp, y, 0);
+  if (!err) fs_restrict_par(m, yexp, y, nthreads);
   free(xexp); free(yexp); free(qoff);
   return err ? or_fail("negative Jacobian") : 0;
 }
@@ -1343,34 +1406,52 @@ int or_operator_function(const or_fs *m, int kind, const double *param, const do
 }
 
 /* EllipPointwiseComputeStore (ellip.c:333-342) at the FAST points from the state g. */
-int or_plap_stash(const or_fs *m, double p, double eps, const double *g, double *stash)
+/* EllipPointwiseComputeStore (ellip.c:333-342) at every FAST point; elements split over nthreads host threads
+ * (each point's store depends only on its own element: the result does not depend on the thread count) */
+int or_plap_stash_mt(const or_fs *m, double p, double eps, const double *g, double *stash, int nthreads)
 {
   if (m->bs != 1) return or_fail("p-Laplacian is scalar");
   basis1d B[11];
   for (int k = 1; k <= 10; k++) if (basis_for(0, k, &B[k])) return -1;
+  if (nthreads < 1) nthreads = 1;
   double *xexp = malloc(sizeof(double) * m->nexp);
-  or_fs_global_to_expanded(m, g, NULL, xexp);
-  double *jinv = malloc(sizeof(double) * 9 * 1000), *jw = malloc(sizeof(double) * 1000), *du = malloc(sizeof(double) * 3000);
-  int64_t off = 0;
-  for (int64_t r = 0; r < m->nr; r++) {
-    const basis1d *b[3] = {&B[m->edeg[3 * r]], &B[m->edeg[3 * r + 1]], &B[m->edeg[3 * r + 2]]};
-    const int P[3] = {b[0]->P, b[1]->P, b[2]->P}, Q[3] = {b[0]->Q, b[1]->Q, b[2]->Q}, nq = Q[0] * Q[1] * Q[2];
-    const double *bi[3] = {b[0]->interp, b[1]->interp, b[2]->interp}, *bd[3] = {b[0]->deriv, b[1]->deriv, b[2]->deriv};
-    if (element_geometry(m, r, b, NULL, jinv, jw)) { free(xexp); free(jinv); free(jw); free(du); return -1; }
-    or_efs_apply_hex(P, Q, bi, bd, jinv, 1, xexp + m->xstart[r], du, OR_GRAD, OR_INSERT);
-    for (int q = 0; q < nq; q++) {
-      const double *Du = du + 3 * q;
-      double gamma = 0.5 * (Du[0] * Du[0] + Du[1] * Du[1] + Du[2] * Du[2]);
-      double espg = eps * eps + gamma, eta = pow(espg, (p - 2) / 2);
-      double sm = sqrt(-((p - 2) / 2) * eta / espg);
-      double *st = stash + 4 * (off + q);
-      st[0] = eta;
-      for (int i = 0; i < 3; i++) st[1 + i] = sm * Du[i];
+  int32_t *qoff = malloc(sizeof(int32_t) * (m->nr + 1));
+  or_fs_num_qpts(m, qoff);
+  fs_expand_par(m, g, NULL, xexp, nthreads);
+  int err = 0;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nthreads) reduction(| : err)
+#endif
+  {
+    double *jinv = malloc(sizeof(double) * 9 * 1000), *jw = malloc(sizeof(double) * 1000), *du = malloc(sizeof(double) * 3000);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 16)
+#endif
+    for (int64_t r = 0; r < m->nr; r++) {
+      const basis1d *b[3] = {&B[m->edeg[3 * r]], &B[m->edeg[3 * r + 1]], &B[m->edeg[3 * r + 2]]};
+      const int P[3] = {b[0]->P, b[1]->P, b[2]->P}, Q[3] = {b[0]->Q, b[1]->Q, b[2]->Q}, nq = Q[0] * Q[1] * Q[2];
+      const double *bi[3] = {b[0]->interp, b[1]->interp, b[2]->interp}, *bd[3] = {b[0]->deriv, b[1]->deriv, b[2]->deriv};
+      if (element_geometry(m, r, b, NULL, jinv, jw)) { err = 1; continue; }
+      or_efs_apply_hex(P, Q, bi, bd, jinv, 1, xexp + m->xstart[r], du, OR_GRAD, OR_INSERT);
+      for (int q = 0; q < nq; q++) {
+        const double *Du = du + 3 * q;
+        double gamma = 0.5 * (Du[0] * Du[0] + Du[1] * Du[1] + Du[2] * Du[2]);
+        double espg = eps * eps + gamma, eta = pow(espg, (p - 2) / 2);
+        double sm = sqrt(-((p - 2) / 2) * eta / espg);
+        double *st = stash + 4 * ((int64_t)qoff[r] + q);
+        st[0] = eta;
+        for (int i = 0; i < 3; i++) st[1 + i] = sm * Du[i];
+      }
     }
-    off += nq;
+    free(jinv); free(jw); free(du);
   }
-  free(xexp); free(jinv); free(jw); free(du);
-  return 0;
+  free(xexp); free(qoff);
+  return err ? -1 : 0;
+}
+
+int or_plap_stash(const or_fs *m, double p, double eps, const double *g, double *stash)
+{
+  return or_plap_stash_mt(m, p, eps, g, stash, 1);
 }
 
 int or_elast_state(const or_fs *m, const double *g, double *Fq)

@@ -116,6 +116,7 @@ int or_fs_eval_points(const or_fs *fs, int rule_deg, const double *g, const doub
 /* p-Laplacian residual stash (ellip.c:333-367) from the global state g (homogeneous Dirichlet):
  * writes [eta, sqrt_mdeta_Du[3]] per FAST qpt. */
 int or_plap_stash(const or_fs *fs, double p, double eps, const double *g, double *stash);
+int or_plap_stash_mt(const or_fs *m, double p, double eps, const double *g, double *stash, int nthreads);
 
 /* Q1-embedded preconditioner assembly (EllipJacobian ellip.c:474-536 with the SPARSE rule, and the
  * elasticity analogue elast.c:343-407), into CSR over explicit scalar dofs (n*bs rows).

@@ -22,9 +22,10 @@ _f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
 
 
-def build(quiet=True):
-    """Compile the oracle (and oracle/_ref when the reference tree is present)."""
-    out = subprocess.run(["make", "-C", HERE], capture_output=True, text=True)
+def build(quiet=True, refdir=None):
+    """Compile the oracle, and oracle/_ref from the dohp source tree at refdir (or $DOHP_REF_DIR) when given."""
+    refdir = refdir or os.environ.get("DOHP_REF_DIR", "")
+    out = subprocess.run(["make", "-C", HERE, "REFDIR=" + refdir], capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
     if not quiet:
@@ -74,6 +75,7 @@ def lib():
         L.or_fs_num_qpts.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.or_fs_qpt_coords.argtypes = [ctypes.c_void_p, _f64p]
         L.or_plap_stash.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, _f64p, _f64p]
+        L.or_plap_stash_mt.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, _f64p, _f64p, ctypes.c_int]
         L.or_q1_assemble.restype = ctypes.c_int64
         L.or_q1_assemble.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                      _i32p, ctypes.POINTER(ctypes.POINTER(ctypes.c_int32)),
@@ -328,10 +330,10 @@ class FS:
             raise RuntimeError(lib().or_last_error().decode())
         return F
 
-    def plap_stash(self, g, p, eps):
+    def plap_stash(self, g, p, eps, nthreads=1):
         nq, _ = self.num_qpts()
         st = np.zeros(nq * 4)
-        rc = lib().or_plap_stash(self.h, p, eps, np.ascontiguousarray(g, dtype=np.float64), st)
+        rc = lib().or_plap_stash_mt(self.h, p, eps, np.ascontiguousarray(g, dtype=np.float64), st, nthreads)
         if rc:
             raise RuntimeError(lib().or_last_error().decode())
         return st

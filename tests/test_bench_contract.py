@@ -21,5 +21,9 @@ def test_reference_arm_prints_one_contract_line():
         assert key in d, key
     assert d["impl"] == "reference" and d["value"] > 0 and d["unit"] == "GDoF/s" and d["higher_is_better"] is True
     assert d["config"]["workload"] == "poisson-8^3-p4"
+    # the same config object as the GPU arm's line for this workload (the full workload, not a sample of it)
+    sys.path.insert(0, ROOT)
+    import bench
+    assert d["config"] == bench.workload_config(bench.CONFIGS["poisson-8"], 29791)
     assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0

@@ -64,3 +64,28 @@ def test_no_alloc_needs_geometry_from_an_ordinary_call():
     x = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
     with pytest.raises(dg.DohpError, match="geometric factors"):
         no_alloc_mult(op, x, torch.zeros_like(x))
+
+
+def test_no_alloc_refuses_reduced_precision_and_hp_spaces():
+    # the entry point always applies in FP64: a reduced precision set on the operator is refused, not ignored
+    fs = dg.FS((4, 4, 4), degree=3, perturb=0.1, seed=2)
+    op = fs.operator(dg.dOP_DIFFUSION)
+    x = torch.as_tensor(np.random.default_rng(1).uniform(-1, 1, fs.n), device="cuda")
+    y = torch.zeros_like(x)
+    op.mult(x, y)
+    op.set_precision(dg.dPREC_FP32)
+    with pytest.raises(dg.DohpError, match="FP64 only"):
+        no_alloc_mult(op, x, y)
+    op.set_precision(dg.dPREC_FP64)
+    y2 = torch.zeros_like(x)
+    no_alloc_mult(op, x, y2)
+    torch.cuda.synchronize()
+    assert (torch.linalg.norm(y2 - y) / torch.linalg.norm(y)).item() < 1e-12
+    # per-element orders: refused with a message naming the entry point
+    ed = np.random.default_rng(2).integers(2, 5, size=27).astype(np.int32)
+    fsh = dg.FS((4, 4, 4), degree=3, perturb=0.1, seed=2, elem_degree=ed)
+    oph = fsh.operator(dg.dOP_DIFFUSION)
+    xh = torch.zeros(fsh.n, dtype=torch.float64, device="cuda")
+    oph.mult(xh, torch.zeros_like(xh))
+    with pytest.raises(dg.DohpError, match="dOperatorMultNoAlloc: uniform-order spaces only"):
+        no_alloc_mult(oph, xh, torch.zeros_like(xh))
