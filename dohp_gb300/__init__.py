@@ -318,40 +318,110 @@ class _DeviceArray:
                                          "version": 3, "strides": None}
 
 
+def _np(t):
+    """pointer argument of a variadic call: the address, or an explicit NULL pointer"""
+    q = ptr(t)
+    return q if q is not None else _vp(0)
+
+
 class RulesetIterator:
-    """dRulesetIterator over all elements at once (FAST rule, uniform order). get() returns torch views of the
-    library's quadrature arrays: jw[nq], x[nq,3], dx[nq,3,3], u[nq,bs], du[nq,bs,3], v[nq,bs], dv[nq,bs,3].
-    Only v and dv are meant to be written (torch has no read-only device tensors)."""
+    """dRulesetIterator over all elements at once (the batched device form of dohp's element loop): link 0 is the
+    coordinate space, link 1 the space fs, links 2.. the spaces given to add_fs (same mesh). get() returns torch views
+    of the library's quadrature arrays for link 1: jw[nq], x[nq,3], dx[nq,3,3], u[nq,bs], du[nq,bs,3], v[nq,bs],
+    dv[nq,bs,3], and under "fields" the (u, du, v, dv) views of every field link. Only v and dv are meant to be
+    written (torch has no read-only device tensors). The test vectors of Start are the wrapper's own global
+    buffers; finish(y) restricts into them and copies (or adds) link 1's into y."""
 
     def __init__(self, fs, method=FAST):
         self.fs = fs
+        self.fields = [fs]
         self.h = _vp()
+        self._y = []
         chk(lib().dRulesetIteratorCreate(fs.h, ctypes.c_int(method), ctypes.byref(self.h)))
 
     def __del__(self):
         if _lib is not None and getattr(self, "h", None):
             _lib.dRulesetIteratorDestroy(ctypes.byref(self.h))
 
-    def start(self, g=None, hmode=dFS_HOMOGENEOUS):
-        chk(lib().dRulesetIteratorStart(self.h, ptr(g), ctypes.c_int(hmode)))
+    def add_fs(self, fs):
+        chk(lib().dRulesetIteratorAddFS(self.h, fs.h))
+        self.fields.append(fs)
+
+    def add_stash(self, elembytes, nodebytes):
+        chk(lib().dRulesetIteratorAddStash(self.h, _i32(elembytes), _i32(nodebytes)))
+
+    def stash(self):
+        """device addresses of the element and point stashes (0 when absent)"""
+        e, n = _vp(), _vp()
+        chk(lib().dRulesetIteratorGetStash(self.h, ctypes.byref(e), ctypes.byref(n)))
+        return e.value or 0, n.value or 0
+
+    def start(self, g=None, hmode=dFS_HOMOGENEOUS, *more):
+        """g: link 1's trial vector; more: (trial vector, mode) pairs for links 2.."""
+        import torch
+        xs = [(g, hmode)] + [(more[i], more[i + 1]) for i in range(0, len(more), 2)]
+        xs += [(None, dFS_HOMOGENEOUS)] * (len(self.fields) - len(xs))
+        self._y = [torch.zeros(f.n * f.bs, dtype=torch.float64, device="cuda") for f in self.fields]
+        args = [_vp(0), _vp(0)]  # link 0: the space's own coordinates, no test vector
+        for (x, m), y in zip(xs, self._y):
+            args.append(_np(x))
+            if x is not None:
+                args.append(ctypes.c_int(m))
+            args += [_np(y), ctypes.c_int(dFS_HOMOGENEOUS)]
+        chk(lib().dRulesetIteratorStart(self.h, *args))
 
     def get(self):
         import torch
-        nq = _i64()
-        p = [_vp() for _ in range(7)]
-        chk(lib().dRulesetIteratorGetPatchApplied(self.h, ctypes.byref(nq), *[ctypes.byref(q) for q in p]))
-        n, bs = nq.value, self.fs.bs
-        shapes = [(n,), (n, 3), (n, 3, 3), (n, bs), (n, bs, 3), (n, bs), (n, bs, 3)]
-        names = ["jw", "x", "dx", "u", "du", "v", "dv"]
-        return {k: torch.as_tensor(_DeviceArray(q.value, s), device="cuda")
-                for k, q, s in zip(names, p, shapes)}
+        Q = _i32()
+        jw = _vp()
+        link0 = [_vp(), _vp()]
+        per = [[_vp() for _ in range(4)] for _ in self.fields]
+        args = [ctypes.byref(Q), ctypes.byref(jw), ctypes.byref(link0[0]), ctypes.byref(link0[1]), _vp(0), _vp(0)]
+        for q in per:
+            args += [ctypes.byref(v) for v in q]
+        chk(lib().dRulesetIteratorGetPatchApplied(self.h, *args))
+        n = Q.value
+        view = lambda q, shape: torch.as_tensor(_DeviceArray(q.value, shape), device="cuda")
+        fields = []
+        for f, q in zip(self.fields, per):
+            bs = f.bs
+            fields.append({k: view(v, s) for k, v, s in zip(("u", "du", "v", "dv"), q, [(n, bs), (n, bs, 3), (n, bs), (n, bs, 3)])})
+        out = {"jw": view(jw, (n,)), "x": view(link0[0], (n, 3)), "dx": view(link0[1], (n, 3, 3))}
+        out.update(fields[0])
+        out["fields"] = fields
+        return out
 
-    def commit(self, imode=INSERT_VALUES, use_v=True, use_dv=True):
-        chk(lib().dRulesetIteratorCommitPatchApplied(self.h, ctypes.c_int(imode), ctypes.c_int(int(use_v)),
-                                                     ctypes.c_int(int(use_dv))))
+    def _field_ptrs(self):
+        """(v, dv) addresses of every field link (the arrays GetPatchApplied returned)"""
+        Q, jw = _i32(), _vp()
+        per = [[_vp() for _ in range(4)] for _ in self.fields]
+        args = [ctypes.byref(Q), ctypes.byref(jw), _vp(0), _vp(0), _vp(0), _vp(0)]
+        for q in per:
+            args += [_vp(0), _vp(0), ctypes.byref(q[2]), ctypes.byref(q[3])]
+        chk(lib().dRulesetIteratorGetPatchApplied(self.h, *args))
+        return [(q[2], q[3]) for q in per]
 
-    def finish(self, y=None, imode=INSERT_VALUES):
-        chk(lib().dRulesetIteratorFinish(self.h, ptr(y), ctypes.c_int(imode)))
+    def commit(self, imode=INSERT_VALUES, use_v=True, use_dv=True, links=None):
+        """integrate v / dv of link 1 (use_v, use_dv), or of the field links listed in links as (use_v, use_dv) pairs"""
+        flags = links if links is not None else [(use_v, use_dv)] + [(False, False)] * (len(self.fields) - 1)
+        ptrs = self._field_ptrs()
+        args = [_vp(0), _vp(0)]
+        for (uv, udv), (v, dv) in zip(flags, ptrs):
+            args += [v if uv else _vp(0), dv if udv else _vp(0)]
+        chk(lib().dRulesetIteratorCommitPatchApplied(self.h, ctypes.c_int(imode), *args))
+
+    def finish(self, y=None, imode=INSERT_VALUES, ys=None):
+        """restrict the test vectors; y receives link 1's (copied, or added with ADD_VALUES), ys those of all links"""
+        chk(lib().dRulesetIteratorSetMode(self.h, ctypes.c_int(INSERT_VALUES)))
+        chk(lib().dRulesetIteratorFinish(self.h))
+        outs = [y] if ys is None else ys
+        for out, buf in zip(outs, self._y):
+            if out is None:
+                continue
+            if imode == ADD_VALUES:
+                out.add_(buf)
+            else:
+                out.copy_(buf)
 
     def error_norms(self, exact_u=None, exact_du=None):
         """dRulesetIteratorErrorNorms: ({L1, L2, Linf} of u - exact_u, the same of |grad u - exact_du|)"""

@@ -8,7 +8,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libdohp_gb300.so")
-SOURCES = ["basis.cu", "mesh_fs.cu", "fs.cu", "operator.cu", "q1.cu", "krylov.cu", "capi.cu", "hp.cu", "iterator.cu", "plap.cu", "unet.cu", "facet.cu", "stokes.cu", "mg.cu", "rules.cu"]
+SOURCES = ["basis.cu", "mesh_fs.cu", "fs.cu", "operator.cu", "q1.cu", "krylov.cu", "capi.cu", "hp.cu", "iterator.cu", "plap.cu", "unet.cu", "facet.cu", "stokes.cu", "mg.cu", "rules.cu", "tc_apply.cu", "dhm.cu"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
          "--extended-lambda", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]

@@ -14,7 +14,7 @@ dErr op_compute_geometry(_p_dOperator *op);
 dErr q1_symbolic(_p_dFS *fs, _p_dMat *J);
 dErr fs_restrict_rows(_p_dFS *fs, const double *x, double *g, int64_t t0, int64_t t1, cudaStream_t s);
 dErr op_mult_expanded(_p_dOperator *op, const double *x, double *yexp);
-dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk, const double *dref, double pe, double eps);
+dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk, const double *dref, double pe, double eps, bool single);
 dErr q1_numeric_elast(_p_dFS *fs, _p_dMat *J, double lam, double mu, int quirk);
 dErr plap_set_stash(_p_dOperator *op, const double *stash);
 dErr mat_mult(_p_dMat *J, const double *x, double *y, cudaStream_t s);
@@ -144,6 +144,10 @@ dErr efs_apply_list(dEFS efs, int64_t nelem, const int32_t *elist, const int32_t
   if (amode == dAPPLY_GRAD_TRANSPOSE && !jinv) return set_error("No Jinv, need a mapping");
   if (D < 1 || D > 3) return set_error("D = %d not supported", D);
   if (nelem <= 0) return 0;
+  if (!efs->d_tab) {
+    CUCHK(cudaMalloc(&efs->d_tab, efs->h_tab.size() * sizeof(double)));
+    CUCHK(cudaMemcpy(efs->d_tab, efs->h_tab.data(), efs->h_tab.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
   EFSDev f;
   const double *p = efs->d_tab;
   for (int d = 0; d < 3; d++) {
@@ -228,8 +232,7 @@ dErr jacobi_efs(dJacobi jac, const dInt degree[3], dQuadratureMethod method, con
       return e;
     }
   }
-  CUCHK(cudaMalloc(&f->d_tab, tab.size() * sizeof(double)));
-  CUCHK(cudaMemcpy(f->d_tab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
+  f->h_tab = tab;  // uploaded on the first device use (host-only queries need no GPU)
   jac->efs[key] = f;
   *efs = f;
   return 0;
@@ -297,6 +300,7 @@ dErr dOperatorDestroy(dOperator *op) {
   cudaFree(o->d_geo);
   cudaFree(o->d_geo32);
   cudaFree(o->d_geo16);
+  cudaFree(o->d_tcb);
   cudaFree(o->d_geoff);
   cudaFree(o->d_yff);
   cudaFree(o->d_k);
@@ -431,7 +435,7 @@ dErr dFSAssembleQ1(dFS fs, dMat J, dOperatorKind kind, const dReal *param, const
   }
   if (kind != dOP_DIFFUSION) return set_error("Q1 assembly for operator kind %d not built yet", (int)kind);
   if (fs->bs != 1) return set_error("diffusion Q1 assembly needs block size 1");
-  return q1_numeric(fs, J, grf, reference_quirk, nullptr, 0, 0);
+  return q1_numeric(fs, J, grf, reference_quirk, nullptr, 0, 0, false);
 }
 
 dErr dMatGetCSR(dMat J, dInt *nrows, int64_t *nnz, const dInt **rowptr, const dInt **col, const dScalar **val) {

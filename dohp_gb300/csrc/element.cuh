@@ -33,6 +33,7 @@ struct ElemArgs {
   void *yexp;
   double lam, mu;
   double *stash;  // St. Venant-Kirchhoff: {F (9), S (6)} per point, SoA per element
+  const double *dcache;  // Dirichlet values of the closure nodes beyond n (inhomogeneous gather), or NULL: zero
 };
 
 // element kinds beyond the ABI's operator kinds: St. Venant-Kirchhoff function (writes the stash) and
@@ -78,7 +79,7 @@ __device__ __forceinline__ void pass(const T *sm, const T *in, T *out, int ne) {
 
 __device__ __forceinline__ int64_t elem_id(const int32_t *els, int64_t first, int el) { return els ? els[el] : first + el; }
 
-// gather one component of the element's nodes through E (homogeneous Dirichlet: closure beyond n is 0)
+// gather one component of the element's nodes through E (closure nodes beyond n: A.dcache, or 0 when NULL)
 template <int N, typename T, int BS, bool BF = false>
 __device__ __forceinline__ void gather(const ElemArgs &A, const double *x, const int32_t *els, int64_t first, int ne, int d, T *dst) {
   constexpr int N3 = N * N * N;
@@ -90,10 +91,12 @@ __device__ __forceinline__ void gather(const ElemArgs &A, const double *x, const
       for (int32_t k = A.eptr[row]; k < A.eptr[row + 1]; k++) {
         const int32_t c = A.ecol[k];
         if (c < A.n) v += A.eval[k] * x[(int64_t)c * BS + d];
+        else if (A.dcache) v += A.eval[k] * A.dcache[(int64_t)(c - A.n) * BS + d];
       }
     } else {
       const int32_t c = A.emap[row];
       if (c < A.n) v = x[(int64_t)c * BS + d];
+      else if (A.dcache) v = A.dcache[(int64_t)(c - A.n) * BS + d];
     }
     dst[t] = BF ? bf16_round<T>(v) : (T)v;
   }

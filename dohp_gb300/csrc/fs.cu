@@ -215,6 +215,7 @@ dErr dFSCreate(dMesh mesh, dJacobi jac, dFS *fs) {
 
 dErr dFSDestroy(dFS *fs) {
   if (!fs || !*fs) return 0;
+  if ((*fs)->coord_fs) dFSDestroy(&(*fs)->coord_fs);
   fs_free_device(*fs);
   delete *fs;
   *fs = nullptr;

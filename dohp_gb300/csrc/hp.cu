@@ -212,7 +212,7 @@ static int prec_index(const _p_dOperator *op) { return op->prec == dPREC_FP32 ? 
 
 static HpArgs make_args(_p_dOperator *op, const double *x, int pi, void *yexp, const double *const *px) {
   _p_dFS *fs = op->fs;
-  HpArgs A;
+  HpArgs A{};
   A.xstart = fs->d_xstart;
   A.qoff = fs->d_qoff;
   A.eptr = fs->d_eptr;

@@ -52,7 +52,8 @@ struct _p_dEFS {
   dQuadratureMethod method;
   _p_dRule *rule = nullptr;  // the rule the basis is evaluated on (owned by the dJacobi's quadrature)
   dgb::Basis1D b[3];
-  double *d_tab = nullptr;  // device: per direction B[Q][P], D[Q][P] packed
+  std::vector<double> h_tab;  // per direction B[Q][P], D[Q][P] packed
+  double *d_tab = nullptr;      // device copy of h_tab, made on first use
 };
 
 struct _p_dJacobi {
@@ -103,6 +104,7 @@ struct _p_dFS {
   // per-degree basis tables on the device for FAST rules: [p] -> B, Dq (Q=P)
   double *d_fast_tab = nullptr;
   double *d_scratch_exp = nullptr;  // expanded-size scratch (nexp*bs)
+  _p_dFS *coord_fs = nullptr;       // the Q1 coordinate space on the same mesh (dFSGetCoordinateFS), made on request
 };
 
 struct _p_dOperator {
@@ -114,6 +116,8 @@ struct _p_dOperator {
   double *d_geo = nullptr;       // fp64 geometric factors per qpt
   float *d_geo32 = nullptr;      // fp32 copy
   void *d_geo16 = nullptr;       // bf16 copy (scalar kinds)
+  void *d_tcb = nullptr;         // BF16 tensor-core apply: the six B operands (block tables of the 1-D bases)
+  bool tc_checked = false;       // the first tensor-core apply was checked for a timed-out wait
   void *d_geoff = nullptr;       // float-float copy
   void *d_yff = nullptr;         // float-float expanded output
   double *d_k = nullptr;         // coefficient per qpt

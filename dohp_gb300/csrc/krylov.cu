@@ -94,29 +94,64 @@ __global__ void k_sell_fill(int64_t n, int64_t nslices, const int32_t *__restric
   }
 }
 
-__global__ void k_dot_partial(int64_t n, const double *__restrict__ a, const double *__restrict__ b, double *__restrict__ part) {
+// block partial of a . b, then the last block to finish (ticket counter) sums the partials in block order: one
+// launch, deterministic for a given n (the grid depends on n only). part holds RED_BLOCKS partials followed by the
+// ticket, which the last block resets to zero.
+__device__ __forceinline__ void dot_finish(double acc, double *part, double *out) {
   __shared__ double s[RED_THREADS];
-  double acc = 0;
-  for (int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; i < n; i += (int64_t)RED_BLOCKS * RED_THREADS) acc += a[i] * b[i];
+  __shared__ bool last;
   s[threadIdx.x] = acc;
   __syncthreads();
   for (int off = RED_THREADS / 2; off > 0; off >>= 1) {
     if (threadIdx.x < off) s[threadIdx.x] += s[threadIdx.x + off];
     __syncthreads();
   }
-  if (threadIdx.x == 0) part[blockIdx.x] = s[0];
-}
-
-__global__ void k_dot_final(const double *__restrict__ part, int nparts, double *__restrict__ out) {
-  __shared__ double s[RED_BLOCKS];
-  for (int i = threadIdx.x; i < RED_BLOCKS; i += blockDim.x) s[i] = i < nparts ? part[i] : 0.0;
+  unsigned *ticket = reinterpret_cast<unsigned *>(part + RED_BLOCKS);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = s[0];
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
   __syncthreads();
-  for (int off = RED_BLOCKS / 2; off > 0; off >>= 1) {
-    for (int i = threadIdx.x; i < off; i += blockDim.x) s[i] += s[i + off];
+  if (!last) return;
+  __threadfence();
+  double a = 0;
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += RED_THREADS) a += ((volatile double *)part)[i];
+  s[threadIdx.x] = a;
+  __syncthreads();
+  for (int off = RED_THREADS / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) s[threadIdx.x] += s[threadIdx.x + off];
     __syncthreads();
   }
-  if (threadIdx.x == 0) *out = s[0];
+  if (threadIdx.x == 0) {
+    *out = s[0];
+    *ticket = 0;
+  }
 }
+
+__global__ void __launch_bounds__(RED_THREADS) k_dot1(int64_t n, const double *__restrict__ a, const double *__restrict__ b, double *part,
+                                                     double *out) {
+  double acc = 0;
+  for (int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; i < n; i += (int64_t)gridDim.x * RED_THREADS) acc += a[i] * b[i];
+  dot_finish(acc, part, out);
+}
+
+// CG update fused with the residual norm: alpha = S[0] / S[1]; x += alpha p; r -= alpha q; out = r . r
+__global__ void __launch_bounds__(RED_THREADS) k_cg_update(int64_t n, const double *__restrict__ S, const double *__restrict__ p,
+                                                          const double *__restrict__ q, double *__restrict__ x, double *__restrict__ r,
+                                                          double *part, double *out) {
+  const double alpha = S[0] / S[1];
+  double acc = 0;
+  for (int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; i < n; i += (int64_t)gridDim.x * RED_THREADS) {
+    x[i] += alpha * p[i];
+    const double ri = r[i] - alpha * q[i];
+    r[i] = ri;
+    acc += ri * ri;
+  }
+  dot_finish(acc, part, out);
+}
+
+static unsigned dot_grid(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(RED_BLOCKS, (n + RED_THREADS - 1) / RED_THREADS)); }
 
 __global__ void k_diag_inv(int64_t n, const int32_t *rp, const int32_t *col, const double *val, double *dinv) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -300,11 +335,18 @@ dErr mat_mult(_p_dMat *J, const double *x, double *y, cudaStream_t s) {
   return 0;
 }
 
-// deterministic dot product into a device scalar (uses `part` of RED_BLOCKS doubles)
+// deterministic dot product into a device scalar, one launch (part: RED_BLOCKS doubles and a zeroed ticket, see
+// dot_part_alloc)
 dErr device_dot(int64_t n, const double *a, const double *b, double *part, double *out, cudaStream_t s) {
-  k_dot_partial<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, a, b, part);
-  k_dot_final<<<1, 1024, 0, s>>>(part, RED_BLOCKS, out);
+  k_dot1<<<dot_grid(n), RED_THREADS, 0, s>>>(n, a, b, part, out);
   CUCHK(cudaGetLastError());
+  return 0;
+}
+
+// workspace of device_dot: RED_BLOCKS partials and the ticket word, zeroed
+dErr dot_part_alloc(double **part) {
+  CUCHK(cudaMalloc(part, (RED_BLOCKS + 1) * sizeof(double)));
+  CUCHK(cudaMemset(*part, 0, (RED_BLOCKS + 1) * sizeof(double)));
   return 0;
 }
 
@@ -401,7 +443,7 @@ dErr ksp_set_correction(dKSP ksp, dErr (*fn)(void *, const double *, double *), 
 static dErr ksp_alloc(_p_dKSP *k) {
   if (k->d_work) return 0;
   CUCHK(cudaMalloc(&k->d_work, 8 * std::max<int64_t>(k->n, 1) * sizeof(double)));
-  CUCHK(cudaMalloc(&k->d_part, RED_BLOCKS * sizeof(double)));
+  DCHK(dot_part_alloc(&k->d_part));
   CUCHK(cudaMalloc(&k->d_s, 64 * sizeof(double)));
   CUCHK(cudaMalloc(&k->d_dinv, std::max<int64_t>(k->n, 1) * sizeof(double)));
   return 0;
@@ -535,6 +577,31 @@ static dErr read_scalar(const double *d, double *h, cudaStream_t s) {
   return 0;
 }
 
+// one CG step after the convergence test: z = M r, rz' = r.z, p = z + (rz'/rz) p, rz = rz', q = A p, pq = p.q,
+// x += (rz/pq) p, r -= (rz/pq) q, rr = r.r (S[0] = rz, S[1] = pq, S[2] = rr, S[4] = rz')
+static dErr cg_step(_p_dKSP *k, double *x, double *r, double *z, double *p, double *q, double *S, bool first) {
+  const int64_t n = k->n;
+  cudaStream_t s = kstream(k);
+  DCHK(pc_apply(k, r, z));
+  if (first) {
+    CUCHK(cudaMemcpyAsync(p, z, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    DCHK(device_dot(n, r, z, k->d_part, S, s));
+  } else {
+    DCHK(device_dot(n, r, z, k->d_part, S + 4, s));
+    k_xpay_ratio<<<nb(n), 256, 0, s>>>(n, z, S + 4, S, p);
+    CUCHK(cudaMemcpyAsync(S, S + 4, sizeof(double), cudaMemcpyDeviceToDevice, s));
+  }
+  DCHK(kmult(k, p, q, dPREC_FP64));
+  DCHK(device_dot(n, p, q, k->d_part, S + 1, s));
+  k_cg_update<<<dot_grid(n), RED_THREADS, 0, s>>>(n, S, p, q, x, r, k->d_part, S + 2);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
+// Preconditioned CG (PETSc KSPCG). After the first step, the step's launches (preconditioner, operator, dots,
+// updates) are captured once into a CUDA graph and replayed, so an iteration costs one graph launch and one read of
+// r.r; capture is skipped with a monitor (host code per iterate), a learned correction, a shell operator or an
+// operator on mixed orders / with its own launch form.
 static dErr cg_solve(_p_dKSP *k, const double *b, double *x, double rtol, int maxit, int *its, double *rnorm) {
   const int64_t n = k->n;
   cudaStream_t s = kstream(k);
@@ -555,24 +622,43 @@ static dErr cg_solve(_p_dKSP *k, const double *b, double *x, double rtol, int ma
     return 0;
   }
   if (k->monitor) DCHK(k->monitor(k->monitor_ctx, 0, x, r));
-  DCHK(pc_apply(k, r, z));
-  CUCHK(cudaMemcpyAsync(p, z, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  DCHK(device_dot(n, r, z, k->d_part, S, s));
-  for (int it = 0; it < maxit; it++) {
-    DCHK(kmult(k, p, q, dPREC_FP64));
-    DCHK(device_dot(n, p, q, k->d_part, S + 1, s));
-    k_axpby<<<nb(n), 256, 0, s>>>(n, 1.0, S, S + 1, p, 1.0, x);
-    k_axpby<<<nb(n), 256, 0, s>>>(n, -1.0, S, S + 1, q, 1.0, r);
-    if (k->monitor) DCHK(k->monitor(k->monitor_ctx, it + 1, x, r));
-    DCHK(device_dot(n, r, r, k->d_part, S + 2, s));
-    DCHK(read_scalar(S + 2, &rr, s));
+  // the operator's own launch forms for mixed orders (persistent kernel, its own graph) stay eager
+  const bool capture = !k->monitor && !k->correction && !k->shell_mult && k->op->fs->uniform && k->op->launch == dLAUNCH_DEFAULT;
+  cudaGraphExec_t exec = nullptr;
+  dErr err = 0;
+  for (int it = 0; it < maxit && !err; it++) {
+    if (it == 0 || !capture) {
+      err = cg_step(k, x, r, z, p, q, S, it == 0);
+    } else {
+      if (!exec) {  // capture on a private stream (the legacy default stream cannot be captured)
+        _p_dFS *fs = k->op->fs;
+        cudaStream_t cs;
+        CUCHK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        fs->stream = cs;
+        cudaGraph_t g = nullptr;
+        cudaError_t ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (ce == cudaSuccess) {
+          err = cg_step(k, x, r, z, p, q, S, false);
+          ce = cudaStreamEndCapture(cs, &g);
+        }
+        fs->stream = s;
+        cudaStreamDestroy(cs);
+        if (!err && ce != cudaSuccess) err = set_error("CG graph capture failed: %s", cudaGetErrorString(ce));
+        if (!err && cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) err = set_error("CG graph instantiation failed");
+        if (g) cudaGraphDestroy(g);
+        if (err) break;
+      }
+      if (cudaGraphLaunch(exec, s) != cudaSuccess) err = set_error("CG graph launch failed");
+      k->pc_applies++;  // the replayed step's preconditioner application
+    }
+    if (err) break;
+    if (k->monitor) err = k->monitor(k->monitor_ctx, it + 1, x, r);
+    if (!err) err = read_scalar(S + 2, &rr, s);
     *its = it + 1;
-    if (!(sqrt(rr) > rtol * bn)) break;
-    DCHK(pc_apply(k, r, z));
-    DCHK(device_dot(n, r, z, k->d_part, S + 4, s));
-    k_xpay_ratio<<<nb(n), 256, 0, s>>>(n, z, S + 4, S, p);
-    CUCHK(cudaMemcpyAsync(S, S + 4, sizeof(double), cudaMemcpyDeviceToDevice, s));
+    if (err || !(sqrt(rr) > rtol * bn)) break;
   }
+  if (exec) cudaGraphExecDestroy(exec);
+  if (err) return err;
   CUCHK(cudaGetLastError());
   *rnorm = sqrt(rr) / bn;
   return 0;
@@ -673,6 +759,8 @@ static dErr fgmres_solve(_p_dKSP *k, const double *b, double *x, double rtol, in
   *rnorm = res;
   return 0;
 }
+
+dPrecision ksp_pc_precision(dKSP ksp) { return ksp ? ksp->pc_prec : dPREC_FP64; }
 
 extern "C" {
 

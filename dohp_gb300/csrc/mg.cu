@@ -23,6 +23,7 @@
 using namespace dgb;
 
 dErr device_dot(int64_t n, const double *a, const double *b, double *part, double *out, cudaStream_t s);
+dErr dot_part_alloc(double **part);
 
 namespace {
 
@@ -567,7 +568,7 @@ dErr mg_build(_p_dMat *J, int degree, bool fp32, void **out) {
     return le;
   }
   M->lat = fs->d_mg_lat;
-  CUCHK(cudaMalloc(&M->part, 1024 * sizeof(double)));
+  DCHK(dot_part_alloc(&M->part));
   CUCHK(cudaMalloc(&M->s, 4 * sizeof(double)));
   // levels: halve until the coarsest is small enough for a dense inverse (9 nodes per direction for scalar
   // matrices, 5 for blocked ones)

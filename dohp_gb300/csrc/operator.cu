@@ -21,6 +21,8 @@ using namespace dgb;
 
 dErr fs_restrict(_p_dFS *fs, const double *x, double *g, int add);
 dErr fs_restrict32(_p_dFS *fs, const float *x, double *g, int add);
+dErr tc_diffusion_apply(_p_dFS *fs, const double *x, const void *geo16, void **bops_cache, float *yexp, double *y);
+dErr tc_check(_p_dFS *fs);
 
 namespace {
 
@@ -123,7 +125,8 @@ __global__ void __launch_bounds__(256) k_uniform(ElemArgs A, int64_t nelem, int 
 }
 
 template <int N, typename T, int KIND, typename GT = T, bool BF = false>
-dErr launch_uniform(_p_dFS *fs, const double *x, const GT *geo, double lam, double mu, T *yexp, double *stash = nullptr) {
+dErr launch_uniform(_p_dFS *fs, const double *x, const GT *geo, double lam, double mu, T *yexp, double *stash = nullptr,
+                    const double *dcache = nullptr) {
   constexpr int cap = KIND == dOP_ELASTICITY ? ETile<N>::EPB : Tile<N>::EPB;
   ElemArgs A{};
   A.xstart = fs->d_xstart;
@@ -137,6 +140,7 @@ dErr launch_uniform(_p_dFS *fs, const double *x, const GT *geo, double lam, doub
   A.lam = lam;
   A.mu = mu;
   A.stash = stash;
+  A.dcache = dcache;
   const size_t smem = (size_t)group_smem_elems(N, KIND, cap) * sizeof(T);
   CUCHK(cudaFuncSetAttribute(k_uniform<N, T, KIND, GT, BF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   k_uniform<N, T, KIND, GT, BF><<<(unsigned)((fs->nelem + cap - 1) / cap), 256, smem, fs->stream>>>(A, fs->nelem, cap);
@@ -150,16 +154,17 @@ dErr launch_diffusion(_p_dFS *fs, const double *x, const T *geo, T *yexp) {
 }
 
 template <int KIND>
-dErr svk_launch(_p_dFS *fs, const double *x, const double *geo, double lam, double mu, double *yexp, double *stash) {
+dErr svk_launch(_p_dFS *fs, const double *x, const double *geo, double lam, double mu, double *yexp, double *stash,
+                const double *dcache = nullptr) {
   switch (fs->p + 1) {
-    case 2: return launch_uniform<2, double, KIND>(fs, x, geo, lam, mu, yexp, stash);
-    case 3: return launch_uniform<3, double, KIND>(fs, x, geo, lam, mu, yexp, stash);
-    case 4: return launch_uniform<4, double, KIND>(fs, x, geo, lam, mu, yexp, stash);
-    case 5: return launch_uniform<5, double, KIND>(fs, x, geo, lam, mu, yexp, stash);
-    case 6: return launch_uniform<6, double, KIND>(fs, x, geo, lam, mu, yexp, stash);
-    case 7: return launch_uniform<7, double, KIND>(fs, x, geo, lam, mu, yexp, stash);
-    case 8: return launch_uniform<8, double, KIND>(fs, x, geo, lam, mu, yexp, stash);
-    case 9: return launch_uniform<9, double, KIND>(fs, x, geo, lam, mu, yexp, stash);
+    case 2: return launch_uniform<2, double, KIND>(fs, x, geo, lam, mu, yexp, stash, dcache);
+    case 3: return launch_uniform<3, double, KIND>(fs, x, geo, lam, mu, yexp, stash, dcache);
+    case 4: return launch_uniform<4, double, KIND>(fs, x, geo, lam, mu, yexp, stash, dcache);
+    case 5: return launch_uniform<5, double, KIND>(fs, x, geo, lam, mu, yexp, stash, dcache);
+    case 6: return launch_uniform<6, double, KIND>(fs, x, geo, lam, mu, yexp, stash, dcache);
+    case 7: return launch_uniform<7, double, KIND>(fs, x, geo, lam, mu, yexp, stash, dcache);
+    case 8: return launch_uniform<8, double, KIND>(fs, x, geo, lam, mu, yexp, stash, dcache);
+    case 9: return launch_uniform<9, double, KIND>(fs, x, geo, lam, mu, yexp, stash, dcache);
   }
   return ::dgb::set_error("degree %d not supported", fs->p);
 }
@@ -317,6 +322,15 @@ static dErr op_mult_bf16(_p_dOperator *op, const double *x, double *y) {
     CUCHK(cudaGetLastError());
   }
   if (!op->d_y32) CUCHK(cudaMalloc(&op->d_y32, fs->nexp * fs->bs * sizeof(float)));
+  if (fs->bs == 1 && fs->boolean_e && fs->p >= 1 && fs->p <= 7) {
+    // the contractions on the tensor cores (tc_apply.cu); the first apply of an operator is checked synchronously
+    DCHK(tc_diffusion_apply(fs, x, op->d_geo16, &op->d_tcb, op->d_y32, y));
+    if (!op->tc_checked) {
+      DCHK(tc_check(fs));
+      op->tc_checked = true;
+    }
+    return 0;
+  }
   const __nv_bfloat16 *g = (const __nv_bfloat16 *)op->d_geo16;
   dErr e = 0;
   switch (fs->p + 1) {
@@ -403,7 +417,9 @@ static dErr svk_state(_p_dOperator *op, const double *g, double *y) {
   DCHK(op_compute_geometry(op));
   if (!op->d_svk) CUCHK(cudaMalloc(&op->d_svk, (size_t)fs->nq * 15 * sizeof(double)));
   if (!op->d_yexp) CUCHK(cudaMalloc(&op->d_yexp, fs->nexp * fs->bs * sizeof(double)));
-  DCHK(svk_launch<K_SVK_FUNC>(fs, g, op->d_geo, op->lam, op->mu, op->d_yexp, op->d_svk));
+  // the state is expanded dFS_INHOMOGENEOUS, as ElastFunction starts its iterator (elast.c:293): Dirichlet nodes take
+  // the values committed with dFSInhomogeneousDirichletCommit (zero when none were)
+  DCHK(svk_launch<K_SVK_FUNC>(fs, g, op->d_geo, op->lam, op->mu, op->d_yexp, op->d_svk, fs->nc > fs->n ? fs->d_dcache : nullptr));
   op->svk_state = true;
   if (y) DCHK(fs_restrict(fs, op->d_yexp, y, 0));
   return 0;

@@ -19,8 +19,10 @@ using namespace dgb;
 dErr fs_expand(_p_dFS *fs, const double *g, double *x, bool inhomogeneous, int add);
 dErr fs_restrict(_p_dFS *fs, const double *x, double *g, int add);
 dErr geometry_fill(_p_dFS *fs, int mode, const double *kq, double *out);
-dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk, const double *dref, double pe, double eps);
+dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk, const double *dref, double pe, double eps, bool single);
+dPrecision ksp_pc_precision(dKSP ksp);
 dErr device_dot(int64_t n, const double *a, const double *b, double *part, double *out, cudaStream_t s);
+dErr dot_part_alloc(double **part);
 dErr ksp_solve(dKSP ksp, const double *b, double *x, double rtol, int maxit, int *its, double *rnorm);
 
 namespace {
@@ -317,7 +319,9 @@ dErr dOperatorGetQuadratureData(dOperator op, dReal *qdata) {
   return set_error("operator kind %d has no quadrature data", (int)op->kind);
 }
 
-dErr dFSAssembleQ1PLaplace(dFS fs, dMat J, const dScalar *g, dReal p, dReal eps, int reference_quirk) {
+// the Q1-embedded p-Laplacian Jacobian at g; single: the patch matrices in FP32 arithmetic (the preconditioner of a
+// solve whose preconditioning runs in FP32 or BF16), else FP64
+static dErr assemble_q1_plap(dFS fs, dMat J, const dScalar *g, dReal p, dReal eps, int reference_quirk, bool single) {
   if (!fs || !J || !g) return set_error("null argument");
   if (fs->bs != 1 || !fs->uniform) return set_error("p-Laplacian Q1 assembly needs a scalar uniform-order space");
   if (!fs->jac) return set_error("dFS was created without a dJacobi");
@@ -330,9 +334,13 @@ dErr dFSAssembleQ1PLaplace(dFS fs, dMat J, const dScalar *g, dReal p, dReal eps,
   CUCHK(cudaMalloc(&dref, npts * 3 * sizeof(double)));
   dErr e = fs_expand(fs, g, fs->d_scratch_exp, true, 0);
   if (!e) e = dEFSApplyBatched(sefs, (dInt)fs->nelem, nullptr, 1, fs->d_scratch_exp, dref, dAPPLY_GRAD, INSERT_VALUES, fs->stream);
-  if (!e) e = q1_numeric(fs, J, nullptr, reference_quirk, dref, p, eps);
+  if (!e) e = q1_numeric(fs, J, nullptr, reference_quirk, dref, p, eps, single);
   cudaFree(dref);
   return e;
+}
+
+dErr dFSAssembleQ1PLaplace(dFS fs, dMat J, const dScalar *g, dReal p, dReal eps, int reference_quirk) {
+  return assemble_q1_plap(fs, J, g, p, eps, reference_quirk, false);
 }
 
 // Newton's method for N(u) = b (the SNES side of ellip.c: SNESSetFunction(EllipFunction),
@@ -350,7 +358,7 @@ dErr dPLaplaceNewtonSolve(dOperator op, dMat Jp, dKSP ksp, const dScalar *b, dSc
   double *F, *du, *ut, *Ft, *part, *d_s;
   CUCHK(cudaMalloc(&F, 4 * std::max<int64_t>(n, 1) * sizeof(double)));
   du = F + n, ut = du + n, Ft = ut + n;
-  CUCHK(cudaMalloc(&part, 1024 * sizeof(double)));
+  DCHK(dot_part_alloc(&part));
   CUCHK(cudaMalloc(&d_s, sizeof(double)));
   auto residual = [&](const double *x, double *r, double *nrm) -> dErr {
     DCHK(dOperatorPLaplaceFunction(op, x, p, eps, r));
@@ -370,7 +378,8 @@ dErr dPLaplaceNewtonSolve(dOperator op, dMat Jp, dKSP ksp, const dScalar *b, dSc
   fn0 = fn;
   if (fnorm && !err) fnorm[0] = fn;
   for (; !err && k < opt->max_it && fn > opt->rtol * fn0 && fn > opt->atol; k++) {
-    err = dFSAssembleQ1PLaplace(fs, Jp, u, p, eps, opt->reference_quirk);
+    // the preconditioning matrix in the precision its preconditioner runs in (FP32 arithmetic for FP32 / BF16)
+    err = assemble_q1_plap(fs, Jp, u, p, eps, opt->reference_quirk, ksp_pc_precision(ksp) != dPREC_FP64);
     if (!err) err = dKSPSetOperators(ksp, nullptr, Jp);
     if (err) break;
     k_waxpby<<<grid, 256, 0, s>>>(n, -1.0, F, 0.0, F, Ft);  // rhs = -F (Ft as scratch)

@@ -134,81 +134,110 @@ struct SparseRules {
   double x[MAXP][2 * (MAXP - 1)], w[MAXP][2 * (MAXP - 1)];  // [p][2p points]
 };
 
-// phase 1: one 64-thread group per patch computes the 8x8 patch matrix K[i][j] = sum_q w k dphi_i . dphi_j
-// p-Laplacian Jacobian (dref != NULL): the state's reference gradient at every SPARSE point, element-natural
-// per element (8 points per patch, elements back to back), gives the store of EllipPointwiseComputeStore
-// (ellip.c:333-342) at the patch point and K[i][j] = sum_q dphi_i . (w eta dphi_j - w (s . dphi_j) s)
-// (EllipPointwiseJacobian, ellip.c:369-377).
-__global__ void __launch_bounds__(256) k_q1_patch(int64_t nelem, const int32_t *edeg, const int64_t *pstart, const double *coords,
-                                                  const SparseRules *rules, const double *grf, int quirk, int64_t npatch_total,
-                                                  const double *dref, double pe, double eps, double *K) {
-  __shared__ double sJ[4][8][9], sW[4][8], sDer[4][8][8][3], sSt[4][8][4];
+// Scalar patch matrices K[i][j] = sum_q w k dphi_i . dphi_j (EllipJacobian, ellip.c:474-536) and, for the
+// p-Laplacian Jacobian (dref != NULL: the state's reference gradient at every SPARSE point, element-natural per element,
+// 8 points per patch, elements back to back), the store of EllipPointwiseComputeStore (ellip.c:333-342) at the patch
+// point with K[i][j] = sum_q dphi_i . (w eta dphi_j - w (s . dphi_j) s) (EllipPointwiseJacobian, ellip.c:369-377).
+// Two phases for a chunk of elements whose SPARSE points are [t0, t0 + nt) (point index = pstart[e] * 8 +
+// element-natural index):
+//   k_q1_points: one thread per point: J^-1 and w det J (times k) at the point, and the p-Laplacian store from the
+//                state's gradient mapped by that J^-1; every point is computed once;
+//   k_q1_patchK: one 64-thread group per patch reads its 8 points (J^-1 at the reference's quirk index pidx*8+q when
+//                quirk is set) and forms the 8 x 8 matrix.
+// T is the arithmetic: double (the assembled preconditioner of FP64 solves) or float (FP32 / BF16 preconditioning).
+template <typename T>
+struct PointData {
+  T *w, *ji, *st;  // [nt], [9][nt], [4][nt] (SoA over the chunk's points)
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_q1_points(int64_t e0, int64_t e1, const int32_t *edeg, const int64_t *pstart, const double *coords,
+                                                   const SparseRules *rules, const double *grf, const double *dref, double pe, double eps,
+                                                   int64_t t0, int64_t nt, PointData<T> P) {
+  const int64_t tl = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (tl >= nt) return;
+  const int64_t t = t0 + tl;
+  int64_t lo = e0, hi = e1;  // element of point t: largest e with pstart[e] * 8 <= t
+  while (hi - lo > 1) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (pstart[mid] * 8 <= t) lo = mid;
+    else hi = mid;
+  }
+  const int64_t e = lo;
+  const int px = edeg[3 * e], py = edeg[3 * e + 1], pz = edeg[3 * e + 2];
+  const int a = (int)(t - pstart[e] * 8), Qy = 2 * py, Qz = 2 * pz;
+  const int ai = a / (Qy * Qz), aj = (a / Qz) % Qy, ak = a % Qz;
+  double xo[3], J[9], Ji[9];
+  q1_map(coords + e * 24, rules->x[px][ai], rules->x[py][aj], rules->x[pz][ak], xo, J);
+  const double det = inv3(J, Ji);
+  double w = rules->w[px][ai] * rules->w[py][aj] * rules->w[pz][ak] * det;
+  if (grf) w *= exp(grf_eval_dev(grf, xo));
+  P.w[tl] = (T)w;
+  for (int i = 0; i < 9; i++) P.ji[i * nt + tl] = (T)Ji[i];
+  if (dref) {
+    const double *dr = dref + t * 3;
+    double Du[3];
+    for (int c = 0; c < 3; c++) Du[c] = dr[0] * Ji[0 * 3 + c] + dr[1] * Ji[1 * 3 + c] + dr[2] * Ji[2 * 3 + c];
+    const double gamma = 0.5 * (Du[0] * Du[0] + Du[1] * Du[1] + Du[2] * Du[2]);
+    const double espg = eps * eps + gamma, eta = pow(espg, (pe - 2) / 2);
+    const double sm = sqrt(-((pe - 2) / 2) * eta / espg);
+    P.st[tl] = (T)eta;
+    for (int c = 0; c < 3; c++) P.st[(1 + c) * nt + tl] = (T)(sm * Du[c]);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_q1_patchK(int64_t e0, int64_t e1, const int32_t *edeg, const int64_t *pstart, int quirk, bool plap,
+                                                   int64_t p0, int64_t np, int64_t t0, int64_t nt, PointData<T> P, double *K) {
+  __shared__ T sW[4][8], sDer[4][8][8][3], sSt[4][8][4];
   const int g = threadIdx.x >> 6, lt = threadIdx.x & 63;
-  const int64_t gp = (int64_t)blockIdx.x * 4 + g;
-  const bool active = gp < npatch_total;
-  int64_t e = 0;
-  int px = 1, py = 1, pz = 1, pidx = 0;
+  const int64_t gp = p0 + (int64_t)blockIdx.x * 4 + g;
+  const bool active = gp < p0 + np;
+  int64_t e = e0;
+  int py = 1, pz = 1, pidx = 0;
   if (active) {
-    int64_t lo = 0, hi = nelem;
+    int64_t lo = e0, hi = e1;
     while (hi - lo > 1) {
       const int64_t mid = (lo + hi) >> 1;
       if (pstart[mid] <= gp) lo = mid;
       else hi = mid;
     }
     e = lo;
-    px = edeg[3 * e], py = edeg[3 * e + 1], pz = edeg[3 * e + 2];
+    py = edeg[3 * e + 1], pz = edeg[3 * e + 2];
     pidx = (int)(gp - pstart[e]);
   }
   const int pi = pidx / (py * pz), pj = (pidx / pz) % py, pk = pidx % pz;
-  // Q1 sub-cell basis values at the two Gauss points and unit-coordinate derivatives (efstopo.c:665-666)
-  const double I1[2][2] = {{0.78867513459481287, 0.21132486540518713}, {0.21132486540518713, 0.78867513459481287}};
-  const double D1[2][2] = {{-1., 1.}, {-1., 1.}};
+  const int Qy = 2 * py, Qz = 2 * pz;
+  const T I1[2][2] = {{(T)0.78867513459481287, (T)0.21132486540518713}, {(T)0.21132486540518713, (T)0.78867513459481287}};
+  const T D1[2][2] = {{-1, 1}, {-1, 1}};
+  const int64_t ebase = pstart[e] * 8 - t0;  // the element's first point in the chunk arrays
   if (active && lt < 8) {
     const int q = lt, qi = q >> 2, qj = (q >> 1) & 1, qk = q & 1;
-    const double *X = coords + e * 24;
-    // weight and coefficient at the patch point (element-natural point index of this patch point)
-    const int ai = 2 * pi + qi, aj = 2 * pj + qj, ak = 2 * pk + qk;
-    double xo[3], J[9], Ji[9];
-    q1_map(X, rules->x[px][ai], rules->x[py][aj], rules->x[pz][ak], xo, J);
-    double det = inv3(J, Ji);
-    double w = rules->w[px][ai] * rules->w[py][aj] * rules->w[pz][ak] * det;
-    if (grf) w *= exp(grf_eval_dev(grf, xo));
-    sW[g][q] = w;
-    if (dref) {  // state gradient mapped by the inverse Jacobian of this point
-      const double *dr = dref + (pstart[e] * 8 + (int64_t)(ai * (2 * py) + aj) * (2 * pz) + ak) * 3;
-      double Du[3];
-      for (int c = 0; c < 3; c++) Du[c] = dr[0] * Ji[0 * 3 + c] + dr[1] * Ji[1 * 3 + c] + dr[2] * Ji[2 * 3 + c];
-      const double gamma = 0.5 * (Du[0] * Du[0] + Du[1] * Du[1] + Du[2] * Du[2]);
-      const double espg = eps * eps + gamma, eta = pow(espg, (pe - 2) / 2);
-      const double sm = sqrt(-((pe - 2) / 2) * eta / espg);
-      sSt[g][q][0] = eta;
-      for (int c = 0; c < 3; c++) sSt[g][q][1 + c] = sm * Du[c];
-    }
-    if (quirk) {  // inverse Jacobian read at element-natural index pidx*8+q (efstopo.c:700)
-      const int t = pidx * 8 + q, Qy = 2 * py, Qz = 2 * pz;
-      const int ti = t / (Qy * Qz), tj = (t / Qz) % Qy, tk = t % Qz;
-      q1_map(X, rules->x[px][ti], rules->x[py][tj], rules->x[pz][tk], xo, J);
-      inv3(J, Ji);
-    }
-    for (int i = 0; i < 9; i++) sJ[g][q][i] = Ji[i];
+    const int64_t a = ebase + ((2 * pi + qi) * Qy + 2 * pj + qj) * Qz + 2 * pk + qk;
+    sW[g][q] = P.w[a];
+    if (plap)
+      for (int c = 0; c < 4; c++) sSt[g][q][c] = P.st[c * nt + a];
   }
   __syncthreads();
   if (active) {
     const int q = lt >> 3, b = lt & 7, qi = q >> 2, qj = (q >> 1) & 1, qk = q & 1, bi = b >> 2, bj = (b >> 1) & 1, bk = b & 1;
-    const double dX = D1[qi][bi] * I1[qj][bj] * I1[qk][bk], dY = I1[qi][bi] * D1[qj][bj] * I1[qk][bk], dZ = I1[qi][bi] * I1[qj][bj] * D1[qk][bk];
-    const double *Ji = sJ[g][q];
+    const T dX = D1[qi][bi] * I1[qj][bj] * I1[qk][bk], dY = I1[qi][bi] * D1[qj][bj] * I1[qk][bk], dZ = I1[qi][bi] * I1[qj][bj] * D1[qk][bk];
+    // inverse Jacobian: the patch point's own, or the one at element-natural index pidx*8+q (efstopo.c:700)
+    const int64_t aj = quirk ? ebase + pidx * 8 + q : ebase + ((2 * pi + qi) * Qy + 2 * pj + qj) * Qz + 2 * pk + qk;
+    T Ji[9];
+    for (int i = 0; i < 9; i++) Ji[i] = P.ji[i * nt + aj];
     for (int d = 0; d < 3; d++) sDer[g][q][b][d] = dX * Ji[0 * 3 + d] + dY * Ji[1 * 3 + d] + dZ * Ji[2 * 3 + d];
   }
   __syncthreads();
   if (active) {
     const int i = lt >> 3, j = lt & 7;
-    double s = 0;
+    T s = 0;
     for (int q = 0; q < 8; q++) {
-      const double w = sW[g][q];
-      double dv0, dv1, dv2;
-      if (dref) {
-        const double *st = sSt[g][q], *dj = sDer[g][q][j];
-        const double dotw = (st[1] * dj[0] + st[2] * dj[1] + st[3] * dj[2]) * w, etaw = st[0] * w;
+      const T w = sW[g][q];
+      T dv0, dv1, dv2;
+      if (plap) {
+        const T *st = sSt[g][q], *dj = sDer[g][q][j];
+        const T dotw = (st[1] * dj[0] + st[2] * dj[1] + st[3] * dj[2]) * w, etaw = st[0] * w;
         dv0 = etaw * dj[0] - dotw * st[1];
         dv1 = etaw * dj[1] - dotw * st[2];
         dv2 = etaw * dj[2] - dotw * st[3];
@@ -217,7 +246,7 @@ __global__ void __launch_bounds__(256) k_q1_patch(int64_t nelem, const int32_t *
       }
       s += sDer[g][q][i][0] * dv0 + sDer[g][q][i][1] * dv1 + sDer[g][q][i][2] * dv2;
     }
-    K[gp * 64 + lt] = s;
+    K[gp * 64 + lt] = (double)s;
   }
 }
 
@@ -419,7 +448,43 @@ dErr q1_symbolic(_p_dFS *fs, _p_dMat *J) {
   return 0;
 }
 
-dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk, const double *dref, double pe, double eps) {
+template <typename T>
+static dErr q1_patches_two_phase(_p_dFS *fs, const std::vector<int64_t> &pstart, const int64_t *d_pstart, const SparseRules *d_rules,
+                                 const double *d_grf, int quirk, const double *dref, double pe, double eps, double *d_K) {
+  // chunks of whole elements with at most kPts SPARSE points, so the point arrays stay near 1 GB
+  constexpr int64_t kPts = 1 << 24;
+  const int64_t npt = pstart[fs->nelem] * 8, cap = std::min<int64_t>(std::max<int64_t>(npt, 1), kPts);
+  PointData<T> P;
+  T *buf;
+  CUCHK(cudaMalloc(&buf, (size_t)cap * 14 * sizeof(T)));
+  P.w = buf, P.ji = buf + cap, P.st = buf + 10 * cap;
+  dErr err = 0;
+  for (int64_t e0 = 0; e0 < fs->nelem && !err;) {
+    int64_t e1 = e0 + 1;
+    while (e1 < fs->nelem && (pstart[e1 + 1] - pstart[e0]) * 8 <= cap) e1++;
+    const int64_t t0 = pstart[e0] * 8, nt = (pstart[e1] - pstart[e0]) * 8;
+    if (nt > cap) {
+      err = set_error("Q1 assembly: one element has more SPARSE points than the chunk");
+      break;
+    }
+    PointData<T> Pc = {P.w, P.ji, P.st};
+    k_q1_points<T><<<(unsigned)((nt + 255) / 256), 256, 0, fs->stream>>>(e0, e1, fs->d_edeg, d_pstart, fs->d_coords, d_rules, d_grf, dref, pe,
+                                                                          eps, t0, nt, Pc);
+    if (cudaGetLastError() != cudaSuccess) err = set_error("k_q1_points launch failed");
+    const int64_t p0 = pstart[e0], np = pstart[e1] - pstart[e0];
+    if (!err && np) {
+      k_q1_patchK<T><<<(unsigned)((np + 3) / 4), 256, 0, fs->stream>>>(e0, e1, fs->d_edeg, d_pstart, quirk, dref != nullptr, p0, np, t0, nt, Pc,
+                                                                        d_K);
+      if (cudaGetLastError() != cudaSuccess) err = set_error("k_q1_patchK launch failed");
+    }
+    e0 = e1;
+  }
+  CUCHK(cudaStreamSynchronize(fs->stream));
+  cudaFree(buf);
+  return err;
+}
+
+dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk, const double *dref, double pe, double eps, bool single) {
   std::vector<int64_t> pstart(fs->nelem + 1, 0);
   for (int64_t e = 0; e < fs->nelem; e++)
     pstart[e + 1] = pstart[e] + (int64_t)fs->edeg[3 * e] * fs->edeg[3 * e + 1] * fs->edeg[3 * e + 2];
@@ -440,8 +505,15 @@ dErr q1_numeric(_p_dFS *fs, _p_dMat *J, const double *grf_host, int quirk, const
     CUCHK(cudaMemcpyAsync(d_grf, grf_host, (3 + 4 * nf) * sizeof(double), cudaMemcpyHostToDevice, fs->stream));
   }
   if (np) {
-    k_q1_patch<<<(unsigned)((np + 3) / 4), 256, 0, fs->stream>>>(fs->nelem, fs->d_edeg, d_pstart, fs->d_coords, d_rules, d_grf, quirk, np, dref, pe, eps, d_K);
-    CUCHK(cudaGetLastError());
+    const dErr e = single ? q1_patches_two_phase<float>(fs, pstart, d_pstart, d_rules, d_grf, quirk, dref, pe, eps, d_K)
+                          : q1_patches_two_phase<double>(fs, pstart, d_pstart, d_rules, d_grf, quirk, dref, pe, eps, d_K);
+    if (e) {
+      cudaFree(d_pstart);
+      cudaFree(d_rules);
+      cudaFree(d_K);
+      cudaFree(d_grf);
+      return e;
+    }
   }
   if (fs->n) {
     k_q1_rows<<<(unsigned)((fs->n + 127) / 128), 128, 0, fs->stream>>>(fs->n, fs->d_et_ptr, fs->d_et_idx, fs->d_xstart, fs->d_edeg,

@@ -22,6 +22,9 @@ struct _p_dRule {
   int order[3];  // polynomial order integrated exactly, per direction
   int Q[3];
   double x[3][MAXQ], w[3][MAXQ];
+  int npatches = 0, patchsize = 0;  // patch tables (dRuleGetPatches), made on first request
+  std::vector<int32_t> patchind;
+  std::vector<double> patchweight;
 };
 
 struct _p_dQuadrature {
@@ -170,6 +173,47 @@ dErr dRuleGetNodeWeight(dRule rule, dReal *coord, dReal *weight) {
   return 0;
 }
 
+// dRulePatchSetup_Tensor (tensorquad.c:120-169): SPARSE rules are tiled into 2 x 2 x 2 patches of points, other
+// rules are one patch; ind = element-natural index of each patch point. The weights repeat the reference's z factor
+// (the y rule's weight at the point's y index, tensorquad.c:159-161); nothing computes with them.
+dErr dRuleGetPatches(dRule rule, dInt *npatches, dInt *patchsize, const dInt **ind, const dReal **weight) {
+  if (!rule) return set_error("null rule");
+  if (rule->patchind.empty()) {
+    int N[3], P[3];
+    const int *Q = rule->Q;
+    for (int d = 0; d < 3; d++) {
+      if (rule->method == dQUADRATURE_METHOD_SPARSE) {
+        P[d] = Q[d] > 1 ? 2 : 1;
+        N[d] = Q[d] / P[d];
+        if (N[d] * P[d] != Q[d]) return set_error("sparse rule with an odd number of points %d", Q[d]);
+      } else {
+        N[d] = 1;
+        P[d] = Q[d];
+      }
+    }
+    rule->npatches = N[0] * N[1] * N[2];
+    rule->patchsize = P[0] * P[1] * P[2];
+    rule->patchind.resize((size_t)rule->npatches * rule->patchsize);
+    rule->patchweight.resize(rule->patchind.size());
+    for (int i = 0; i < N[0]; i++)
+      for (int j = 0; j < N[1]; j++)
+        for (int k = 0; k < N[2]; k++)
+          for (int a = 0; a < P[0]; a++)
+            for (int b = 0; b < P[1]; b++)
+              for (int c = 0; c < P[2]; c++) {
+                const int patch = (i * N[1] + j) * N[2] + k, pi = (a * P[1] + b) * P[2] + c;
+                const int ie = i * P[0] + a, je = j * P[1] + b, ke = k * P[2] + c;
+                rule->patchind[patch * rule->patchsize + pi] = (ie * Q[1] + je) * Q[2] + ke;
+                rule->patchweight[patch * rule->patchsize + pi] = rule->w[0][ie] * rule->w[1][je] * rule->w[2][je];
+              }
+  }
+  if (npatches) *npatches = rule->npatches;
+  if (patchsize) *patchsize = rule->patchsize;
+  if (ind) *ind = rule->patchind.data();
+  if (weight) *weight = rule->patchweight.data();
+  return 0;
+}
+
 dErr dRuleComputePhysical(dRule rule, const dScalar jac[], dReal jinv[], dReal jw[]) {
   if (!rule || !jinv || !jw) return set_error("null argument");
   const int n = rule->Q[0] * rule->Q[1] * rule->Q[2];
@@ -217,7 +261,7 @@ dErr dEFSGetRule(dEFS efs, dRule *rule) {
 // (dEFSGetExplicitSparse_Tensor_Hex, efstopo.c:660-717, when every patch has 8 points and the patches are the
 // element's sub-cells) or else the element's own basis at each patch's points (dEFSGetExplicitSparse_Basic,
 // jacobi.c:611-643). cjinv: inverse Jacobians of the element's points, read at index pidx*8+q on the sub-cell
-// path (the reference's indexing; the points are element-natural there) and through qidx on the basic path.
+// path and at qidx[qidx[pidx*Q+q]] on the basic path (both the reference's indexing).
 dErr dEFSGetExplicitSparse(dEFS efs, dInt npatches, dInt Q, const dInt qidx[], const dReal cjinv[], dInt eoffset, dInt *P, dInt eidx[],
                            dReal interp[], dReal deriv[]) {
   if (!efs || !qidx || !P || !eidx || !interp || !deriv) return set_error("null argument");
@@ -263,8 +307,13 @@ dErr dEFSGetExplicitSparse(dEFS efs, dInt npatches, dInt Q, const dInt qidx[], c
       const int pq = pt * Q + j, eq = qidx[pq];
       if (eq < 0 || eq >= eQ) return set_error("dEFSGetExplicitSparse: qidx %d out of range", eq);
       const int a = eq / (Qn[1] * Qn[2]), b = (eq / Qn[2]) % Qn[1], c = eq % Qn[2];
+      // the reference first reorders cjinv with ecjinv[i] = cjinv[qidx[i]] and then evaluates the element basis at
+      // element point eq with ecjinv[eq] (jacobi.c:620-626): the point's inverse Jacobian is cjinv[qidx[eq]]
       double M[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-      if (cjinv) std::copy(cjinv + eq * 9, cjinv + eq * 9 + 9, M);
+      if (cjinv) {
+        const int src = qidx[eq];
+        std::copy(cjinv + src * 9, cjinv + src * 9 + 9, M);
+      }
       for (int k = 0; k < eP; k++) {
         const int ki = k / (Pn[1] * Pn[2]), kj = (k / Pn[2]) % Pn[1], kk = k % Pn[2];
         const double Bx = efs->b[0].B[a * Pn[0] + ki], By = efs->b[1].B[b * Pn[1] + kj], Bz = efs->b[2].B[c * Pn[2] + kk];

@@ -46,6 +46,7 @@ dErr ksp_create_shell(int64_t n, cudaStream_t stream, dKSPType type, dErr (*mult
 dErr ksp_solve(dKSP ksp, const double *b, double *x, double rtol, int maxit, int *its, double *rnorm);
 dErr ksp_pc_only(dKSP ksp, const double *r, double *z);
 dErr device_dot(int64_t n, const double *a, const double *b, double *part, double *out, cudaStream_t s);
+dErr dot_part_alloc(double **part);
 
 namespace {
 
@@ -463,7 +464,7 @@ dErr dStokesCreate(dFS fsu, dFS fsp, const dReal rheo[4], dStokes *stk) {
   CUCHK(cudaMalloc(&S->d_yp, std::max<int64_t>(fsp->nexp, 1) * sizeof(double)));
   CUCHK(cudaMalloc(&S->d_mdiag, std::max<int64_t>(S->np, 1) * sizeof(double)));
   CUCHK(cudaMalloc(&S->d_t, (S->nu3 + std::max<int64_t>(S->np, 1)) * sizeof(double)));
-  CUCHK(cudaMalloc(&S->d_part, 1024 * sizeof(double)));
+  DCHK(dot_part_alloc(&S->d_part));
   CUCHK(cudaMalloc(&S->d_s, 8 * sizeof(double)));
   k_fill<<<nblk(S->np), 256, 0, s>>>(S->np, 1.0, S->d_t + S->nu3);  // ones vector for the pressure mean
   DCHK(pmass_diag(S->N, S->NP, fsu->nelem, fsu->d_qoff, fsp->d_xstart, S->d_geo, S->d_bp, S->d_yp, s));

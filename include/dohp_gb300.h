@@ -16,6 +16,7 @@
 #ifndef DOHP_GB300_H
 #define DOHP_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -122,6 +123,10 @@ dErr dQuadratureGetRules(dQuadrature quad, dInt n, const dEntTopology topo[], co
 dErr dRuleGetSize(dRule rule, dInt *dim, dInt *nnodes);
 dErr dRuleGetNodeWeight(dRule rule, dReal *coord, dReal *weight);
 dErr dRuleGetTensorNodeWeight(dRule rule, dInt *dim, dInt nnodes[3], const dReal *coord[3], const dReal *weight[3]);
+/* dRuleGetPatches (src/jacobi/interface/jacobi.c:320-330, tensorquad.c:120-169): SPARSE rules tiled into 2 x 2 x 2 point
+ * patches, other rules one patch; ind [npatches][patchsize] element-natural point indices; weights as the reference
+ * tabulates them (its z factor is the y rule's weight at the y index; no computation uses them). Owned by the rule. */
+dErr dRuleGetPatches(dRule rule, dInt *npatches, dInt *patchsize, const dInt **ind, const dReal **weight);
 /* dRuleComputePhysical (src/jacobi/interface/jacobi.c:383-414): jinv [n][9] = jac^-1 (dGeomInvert3), jw [n] = w det jac;
  * jac NULL gives identities and the rule weights; a negative determinant is an error. Host arrays. */
 dErr dRuleComputePhysical(dRule rule, const dScalar jac[], dReal jinv[], dReal jw[]);
@@ -136,7 +141,8 @@ dErr dEFSGetRule(dEFS efs, dRule *rule);
  * patches of Q points each (qidx [npatches][Q]: the patch points' element-natural indices, dRuleGetPatches): with 8
  * points per patch and the p_x p_y p_z GLL sub-cells as patches, the Q1 sub-cell bases of efstopo.c:660-717 (P = 8,
  * derivatives with respect to the unit sub-cell coordinate mapped by cjinv [pidx*8+q]), otherwise the element's own
- * basis at each patch point (P = nodes of the element, cjinv read through qidx). cjinv NULL: reference coordinates.
+ * basis at each patch point (P = nodes of the element, cjinv read at qidx[qidx[pidx*Q+q]] as jacobi.c:620-626 does).
+ * cjinv NULL: reference coordinates.
  * Outputs (host): eidx [npatches][P] = eoffset + element node, interp [npatches][Q][P], deriv [npatches][Q][P][3]. */
 dErr dEFSGetExplicitSparse(dEFS efs, dInt npatches, dInt Q, const dInt qidx[], const dReal cjinv[], dInt eoffset, dInt *P,
                            dInt eidx[], dReal interp[], dReal deriv[]);
@@ -220,10 +226,13 @@ dErr dOperatorComputePLaplaceStash(dOperator op, const dScalar *g, dReal p, dRea
 dErr dOperatorPLaplaceFunction(dOperator op, const dScalar *g, dReal p, dReal eps, dScalar *y);
 /* St. Venant-Kirchhoff elasticity (dOP_ELASTICITY operators, uniform-order spaces, FP64): the state at g
  * (deformation gradient F = I + Du and second Piola-Kirchhoff stress S at every FAST point,
- * ElastPointwiseComputeStore elast.c:224-225), after which dOperatorMult applies ElastShellMatMult at that
- * state (ElastPointwiseJacobian, elast.c:268-280); g = NULL returns to F = I (linear elasticity) */
+ * ElastPointwiseComputeStore elast.c:224-225; g expanded dFS_INHOMOGENEOUS as in dOperatorElasticityFunction), after which
+ * dOperatorMult applies ElastShellMatMult at that state (ElastPointwiseJacobian, elast.c:268-280); g = NULL returns to
+ * F = I (linear elasticity) */
 dErr dOperatorElasticityState(dOperator op, const dScalar *g);
-/* ElastFunction without body force (elast.c:282-309): y = sum_e E^T B^T (w F S) at g; also sets the state */
+/* ElastFunction without body force (elast.c:282-309): y = sum_e E^T B^T (w F S) at g; also sets the state. g is expanded
+ * dFS_INHOMOGENEOUS (elast.c:293): Dirichlet nodes take the values of dFSInhomogeneousDirichletCommit (zero without one);
+ * the Jacobian applies at that state act on homogeneous increments (ElastShellMatMult, elast.c:322) */
 dErr dOperatorElasticityFunction(dOperator op, const dScalar *g, dScalar *y);
 /* copy out the per-point data: dOP_DIFFUSION coefficient [nq], dOP_PLAPLACE_JACOBIAN stash [nq][4] (device) */
 dErr dOperatorGetQuadratureData(dOperator op, dReal *qdata);
@@ -252,25 +261,67 @@ dErr dOperatorMultNoAlloc(dOperator op, const dScalar *x, dScalar *y);
 /* MatMult with host vectors: copies in, applies, copies out, synchronizes (end-to-end form) */
 dErr dOperatorMultHost(dOperator op, const dScalar *x_host, dScalar *y_host);
 
-/* ---------------------------------------------------------------- dRulesetIterator (batched device form) */
-/* dRulesetIterator* (include/dohpfs.h:106-128, src/fs/interface/fsrulesetit.c): one Start / GetPatchApplied /
- * CommitPatchApplied / Finish cycle covers all elements at once on the device. Arrays are element-natural
- * per element, elements back to back (patch order = element order for FAST rules); on spaces with per-element
- * orders each element has (p_x+1)(p_y+1)(p_z+1) points, element e starting at the prefix sum of the counts
- * before it (the layout of dFSGetNumQuadraturePoints and dOperatorGetQuadratureData). SPARSE rules (uniform-order
- * spaces, degree <= 5): (2p)^3 points per element in tensor order; patch (a, b, c) of the reference's patch loop
- * is the 2 x 2 x 2 block of points (2a..2a+1, 2b..2b+1, 2c..2c+1). */
-dErr dRulesetIteratorCreate(dFS fs, dQuadratureMethod method, dRulesetIterator *it);
+/* ---------------------------------------------------------------- dRuleset / dRulesetIterator (batched device form) */
+/* include/dohpfs.h:97-128, src/fs/interface/fsruleset.c, fsrulesetit.c. One Start / GetPatchApplied / CommitPatchApplied /
+ * Finish cycle covers all elements at once on the device: dRulesetIteratorHasPatch is true once after Start and
+ * dRulesetIteratorNextPatch ends the traversal, so the reference's loop
+ *     while (dRulesetIteratorHasPatch(it)) { GetPatchApplied; q-function; CommitPatchApplied; NextPatch; }
+ * runs its body once, over every point. Arrays are element-natural per element, elements back to back: element e's
+ * points start at the ruleset's offset of e (dRulesetGetNumPoints; (p_x+1)(p_y+1)(p_z+1) points per element for FAST
+ * rules, the layout of dFSGetNumQuadraturePoints). SPARSE rules (uniform-order spaces): (2p)^3 points per element in
+ * tensor order; patch (a, b, c) of the reference's patch loop is the 2 x 2 x 2 block of points (2a..2a+1, 2b..2b+1,
+ * 2c..2c+1). Link 0 is the coordinate space, links 1.. the spaces added with dRulesetIteratorAddFS, in order; varargs
+ * repeat the per-link arguments for links 1.. exactly as in dohp. */
+typedef struct _p_dRuleset *dRuleset;
+/* dFSGetPreferredQuadratureRuleSet (include/dohpfs.h:97): the rules of the space's elements (order 2p per direction,
+ * fsruleset.c:32-37) for FAST, or SPARSE on uniform-order spaces; over all regions of the mesh */
+dErr dFSGetPreferredQuadratureRuleSet(dFS fs, dQuadratureMethod method, dRuleset *rset);
+dErr dRulesetGetSize(dRuleset rset, dInt *size);
+/* total points and the host array of per-element point offsets [nelem+1] (owned by the ruleset) */
+dErr dRulesetGetNumPoints(dRuleset rset, int64_t *nq, const dInt **qoffset);
+dErr dRulesetDestroy(dRuleset *rset);
+/* dFSGetCoordinateFS (src/fs/interface/fsgeom.c:176-204): the Q1, block size 3 space of vertex coordinates on the same mesh,
+ * owned by fs; its expanded vector is dFSGetGeometryVectorExpanded's [nelem][8][3] */
+dErr dFSGetCoordinateFS(dFS fs, dFS *cfs);
+/* dRulesetCreateIterator (fsrulesetit.c:129-150): link 0 = cfs (coordinates) */
+dErr dRulesetCreateIterator(dRuleset rset, dFS cfs, dRulesetIterator *it);
+/* dRulesetIteratorAddFS (fsrulesetit.c:161-181): one more field link (same mesh, any degrees on FAST rules) */
+dErr dRulesetIteratorAddFS(dRulesetIterator it, dFS fs);
+/* dRulesetIteratorSetMode (fsrulesetit.c:152-158): INSERT_VALUES (default) or ADD_VALUES for Finish's restriction */
+dErr dRulesetIteratorSetMode(dRulesetIterator it, InsertMode imode);
+/* dRulesetIteratorAddStash / GetStash (fsrulesetit.c:779-798): device memory of elembytes per element and nodebytes per
+ * point (zeroed when made at the next Start, then kept across traversals); GetStash gives the start of each (element e's
+ * point stash begins at its point offset times nodebytes) */
+dErr dRulesetIteratorAddStash(dRulesetIterator it, dInt elembytes, dInt nodebytes);
+dErr dRulesetIteratorGetStash(dRulesetIterator it, void *elemstash, void *nodestash);
+/* dRulesetIteratorStart (fsrulesetit.c:234-303): per link (X, [xmode if X], Y, [ymode if Y]); link 0's X is the expanded
+ * coordinate vector (NULL: the space's own geometry), the other links' X are global vectors expanded with xmode
+ * (dFS_HOMOGENEOUS / dFS_INHOMOGENEOUS) or NULL (zero); Y are global test vectors filled at Finish, or NULL. Device pointers. */
+dErr dRulesetIteratorStart(dRulesetIterator it, const dScalar *X, ...);
+int dRulesetIteratorHasPatch(dRulesetIterator it);
+dErr dRulesetIteratorNextPatch(dRulesetIterator it);
+/* dRulesetIteratorGetPatchApplied (fsrulesetit.c:517-589): Q = points; jw [Q]; per link (u, du, v, dv): link 0 gives
+ * u = x [Q][3] and du = dx [Q][3][3] (reference gradient of the coordinates), field links u [Q][bs] and du [Q][bs][3]
+ * (physical gradient); v [Q][bs] and dv [Q][bs][3] are zeroed test arrays. NULL skips an output (and its work). */
+dErr dRulesetIteratorGetPatchApplied(dRulesetIterator it, dInt *Q, const dReal **jw, dScalar **u, dScalar **du, dScalar **v,
+                                     dScalar **dv, ...);
+/* dRulesetIteratorCommitPatchApplied (fsrulesetit.c:595-643): per link (v, dv) as returned by GetPatchApplied or NULL;
+ * integrates v (INTERP_TRANSPOSE) and dv (GRAD_TRANSPOSE) into the link's expanded test vector (imode per element) */
+dErr dRulesetIteratorCommitPatchApplied(dRulesetIterator it, InsertMode imode, const dScalar *v, const dScalar *dv, ...);
+/* dRulesetIteratorGetPatchAssembly (fsrulesetit.c:657-701), SPARSE rulesets, after GetPatchApplied: per link (P, rowcol,
+ * interp, deriv), NULL for link 0: the Q1 sub-cell bases of every patch of every element (dEFSGetExplicitSparse,
+ * efstopo.c:660-717, the inverse Jacobian read at the reference's patch-natural index): P = 8, device arrays rowcol
+ * [nelem*p^3][8] (expanded node indices), interp [nelem*p^3][8][8], deriv [nelem*p^3][8][8][3], patches element-major in
+ * the reference's patch order, owned by the iterator */
+dErr dRulesetIteratorGetPatchAssembly(dRulesetIterator it, dInt *P, const dInt **rowcol, const dReal **interp, const dReal **deriv,
+                                      ...);
+/* dRulesetIteratorFinish (fsrulesetit.c:309-322): restrict each link's expanded test vector into its Y */
+dErr dRulesetIteratorFinish(dRulesetIterator it);
 dErr dRulesetIteratorDestroy(dRulesetIterator *it);
-dErr dRulesetIteratorStart(dRulesetIterator it, const dScalar *g, dFSHomogeneousMode hmode);
-/* device pointers: jw[nq], x[nq][3], dx[nq][3][3], u[nq][bs], du[nq][bs][3]; v/dv are writable test arrays */
-dErr dRulesetIteratorGetPatchApplied(dRulesetIterator it, int64_t *nq, const dReal **jw, const dScalar **x,
-                                     const dScalar **dx, const dScalar **u, const dScalar **du, dScalar **v, dScalar **dv);
-/* integrate v (INTERP_TRANSPOSE) and dv (GRAD_TRANSPOSE) back into the expanded test vector */
-dErr dRulesetIteratorCommitPatchApplied(dRulesetIterator it, InsertMode imode, int use_v, int use_dv);
-/* dRulesetIteratorFinish: restrict the expanded test vector into the global vector y */
-dErr dRulesetIteratorFinish(dRulesetIterator it, dScalar *y, InsertMode imode);
-/* dNormsStart/Update/Finish (src/util/util.c:110-153) over every point of the last GetPatchApplied: uerr =
+/* one field on its own preferred ruleset: dFSGetPreferredQuadratureRuleSet + dFSGetCoordinateFS + dRulesetCreateIterator +
+ * dRulesetIteratorAddFS(fs) (link 1 = fs) */
+dErr dRulesetIteratorCreate(dFS fs, dQuadratureMethod method, dRulesetIterator *it);
+/* dNormsStart/Update/Finish (src/util/util.c:110-153) over every point of the last GetPatchApplied, for link 1: uerr =
  * {L1, L2, Linf} of u - exact_u, gerr = the same of |grad u - exact_du| (device arrays [nq][bs], [nq][bs][3],
  * either may be NULL, e.g. exact values computed from the x that GetPatchApplied returned) */
 dErr dRulesetIteratorErrorNorms(dRulesetIterator it, const dScalar *exact_u, const dScalar *exact_du, dReal uerr[3],
@@ -435,6 +486,42 @@ dErr dStokesNewtonSolve(dStokes stk, const dScalar *bu, const dScalar *bp, dScal
 /* KSPSetOperators: new operator and/or preconditioning matrix (NULL keeps the current one); the
  * preconditioner is set up again on the next solve (a Newton step that re-assembled the Q1 matrix) */
 dErr dKSPSetOperators(dKSP ksp, dOperator op, dMat pmat);
+
+/* ---------------------------------------------------------------- DHM files (src/viewer/dhm.c, contviewdhm.c) */
+/* HDF5 files with the reference's DHM group layout: /dohp/{type, mesh, fs, step}; committed types Units_type, Time_type,
+ * BoundingBox_type, FS_type, Vec_type; one group per time step (000, 001, ...) with attribute "time"; one FS record per
+ * space; one dataset [closure nodes][bs] per vector with attribute "meta". Written from the HDF5 file format
+ * specification (version 2 superblock and object headers, compact links, contiguous data, lookup3 checksums). Against
+ * the reference: strings are fixed-length (64 bytes), object and region references are path strings, and the mesh
+ * (vertices, hexahedra, block extents, the space's degree and boundary-status tags) is stored in the file where the
+ * reference names a MOAB file. The file is written when a write-mode viewer is destroyed. */
+typedef struct _p_dViewer *dViewer;
+/* PetscFileMode values */
+typedef enum { dFILE_MODE_READ = 0, dFILE_MODE_WRITE = 1 } dFileMode;
+/* PetscViewerCreate + PetscViewerSetType(PETSCVIEWERDHM) + FileSetMode + FileSetName; read mode parses the file */
+dErr dViewerDHMOpen(const char *path, dFileMode mode, dViewer *viewer);
+dErr dViewerDestroy(dViewer *viewer);
+/* dViewerDHMSetTime / SetTimeUnits (dhm.c:339-360): a new time starts a new step group */
+dErr dViewerDHMSetTime(dViewer viewer, dReal time);
+dErr dViewerDHMSetTimeUnits(dViewer viewer, const char *units, dReal scale);
+/* dViewerDHMGetSteps (dhm.c:525-553): number of steps and their times (times may be NULL; room for nsteps) */
+dErr dViewerDHMGetSteps(dViewer viewer, dInt *nsteps, dReal *times);
+/* dViewerDHMSetTimeStep (dhm.c:484-500): select a step (read mode: its time becomes the viewer's time) */
+dErr dViewerDHMSetTimeStep(dViewer viewer, dInt step);
+dErr dViewerDHMGetTime(dViewer viewer, dReal *time);
+/* dFSView_Cont_DHM (contviewdhm.c:58-116): the space's mesh and its record /dohp/fs/<name> (host data; the space must be
+ * built) */
+dErr dFSViewDHM(dFS fs, const char *name, dViewer viewer);
+/* VecView_Dohp_FSCont_DHM (contviewdhm.c:133-209): a closure vector ([global | Dirichlet] x bs, host or device pointer)
+ * of a space written with dFSViewDHM, as dataset <name> of the current step */
+dErr dVecViewDHM(dFS fs, const char *name, const dScalar *closure, int on_device, dViewer viewer);
+/* VecDohpLoadIntoVector (contviewdhm.c:350-401): the closure vector <name> of the current step, scaled by its units */
+dErr dVecLoadDHM(dViewer viewer, const char *name, dFS fs, dScalar *closure, int on_device);
+/* dFSLoadIntoFS_Cont_DHM (contviewdhm.c:228-348): the mesh and the space recorded as <name>, built (dFSBuildSpace); the
+ * caller owns both (dFSDestroy, dMeshDestroy) and calls dFSSetUp before device use */
+dErr dFSLoadDHM(dViewer viewer, const char *name, dJacobi jac, dMesh *mesh, dFS *fs);
+/* Jenkins' lookup3 hash, the checksum of HDF5 metadata blocks */
+uint32_t dHDF5Checksum(const void *data, size_t len, uint32_t initval);
 
 /* ---------------------------------------------------------------- lognormal coefficient */
 /* g(x) = sqrt(2 var / nf) sum_f cos(w_f . x + b_f), random Fourier features of the squared-exponential

@@ -108,3 +108,37 @@ def test_newton_krylov_large_deformation():
     r = o.apply(host(u), kind=4, param=PAR) - host(b)
     assert np.linalg.norm(r) <= 1e-8 * f0
     assert float(torch.linalg.norm(u)) > 0
+
+
+def test_reference_elast_target_through_the_product():
+    """the reference's elast-e0-b3-g01 target (src/fs/tests/CMakeLists.txt:58; the problem and its oracle side are in
+    tests/test_oracle_ellip_elast_golden.py) through the product: the exact solution's Dirichlet values committed to the
+    space (dFSInhomogeneousDirichletCommit), the body force integrated by the dRulesetIterator, and
+    dOperatorElasticityFunction at zero, whose dFS_INHOMOGENEOUS expansion is ElastFunction's (elast.c:293): ||F(0)|| is
+    the printed first SNES function norm 14965.9 to six digits, and the residual vector is the oracle's"""
+    import test_oracle_ellip_elast_golden as G
+    name = "elast_e0_b3_g01"
+    ref = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", name + ".npz"))
+    O = G.Problem(*G.CASES[name])
+    fs = dg.FS((5, 5, 5), degree=3, box=G.BOX, perturb=0.0, seed=1, bs=3)
+    assert (fs.n, fs.nc) == (O.fs.n, O.fs.nc)
+    fs.dirichlet_commit(dev(np.concatenate([O.s, O.dc])))
+    it = dg.RulesetIterator(fs)
+    it.start(None)
+    a = it.get()
+    np.testing.assert_allclose(a["x"].cpu().numpy(), O.fs.qpt_coords(), rtol=0, atol=1e-14)
+    a["v"].copy_(a["jw"][:, None] * dev(O.fq))
+    it.commit(dg.INSERT_VALUES, use_v=True, use_dv=False)
+    b = torch.zeros(fs.n * 3, dtype=torch.float64, device="cuda")
+    it.finish(b)
+    op = fs.operator(dg.dOP_ELASTICITY, param=(E0, NU))
+    y = torch.zeros_like(b)
+    op.elasticity_function(torch.zeros_like(b), y)
+    F0 = host(y) - host(b)
+    assert abs(np.linalg.norm(F0) - ref["fnorm0"][0]) < 3e-6 * ref["fnorm0"][0], np.linalg.norm(F0)
+    assert rel(F0, O.F(np.zeros(fs.n * 3))) < 1e-12
+    # the Jacobian at that state (F from the inhomogeneous expansion) against the oracle's at the same state
+    d = np.random.default_rng(3).uniform(-1, 1, fs.n * 3)
+    jd = torch.zeros_like(b)
+    op.mult(dev(d), jd)
+    assert rel(host(jd), O.fs.apply(d, kind=5, qdata=O.qdata(np.zeros(fs.n * 3)), param=PAR)) < 1e-12
