@@ -360,9 +360,18 @@ dErr dOperatorMultHost(dOperator op, const dScalar *x_host, dScalar *y_host) {
     CUCHK(cudaMalloc(&op->d_hx, std::max<size_t>(bytes, 8)));
     CUCHK(cudaMalloc(&op->d_hy, std::max<size_t>(bytes, 8)));
   }
-  CUCHK(cudaMemcpyAsync(op->d_hx, x_host, bytes, cudaMemcpyHostToDevice, fs->stream));
   const int64_t N = fs->n * fs->bs;
-  if (op->prec != dPREC_FP64 || op->svk_state || N < 4 * 65536) {
+  const bool big = op->prec == dPREC_FP64 && !op->svk_state && N >= 4 * 65536;
+  // page-locked input of a large FP64 apply: the element kernel reads it in place over the host link (the gather's
+  // host reads overlap the kernel's FP64 arithmetic instead of a copy before it); otherwise one copy to the device
+  const double *xd = op->d_hx;
+  cudaPointerAttributes pa;
+  if (big && cudaPointerGetAttributes(&pa, x_host) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer)
+    xd = (const double *)pa.devicePointer;
+  else
+    CUCHK(cudaMemcpyAsync(op->d_hx, x_host, bytes, cudaMemcpyHostToDevice, fs->stream));
+  cudaGetLastError();  // a pointer the runtime does not know leaves an error state behind
+  if (!big) {
     DCHK(op_mult(op, op->d_hx, op->d_hy));
     CUCHK(cudaMemcpyAsync(y_host, op->d_hy, bytes, cudaMemcpyDeviceToHost, fs->stream));
     CUCHK(cudaStreamSynchronize(fs->stream));
@@ -382,7 +391,7 @@ dErr dOperatorMultHost(dOperator op, const dScalar *x_host, dScalar *y_host) {
   }
   cudaStream_t cs = (cudaStream_t)op->copy_stream;
   if (!op->d_yexp) CUCHK(cudaMalloc(&op->d_yexp, fs->nexp * fs->bs * sizeof(double)));
-  DCHK(op_mult_expanded(op, op->d_hx, op->d_yexp));
+  DCHK(op_mult_expanded(op, xd, op->d_yexp));
   for (int k = 0; k < 4; k++) {
     const int64_t t0 = N * k / 4, t1 = N * (k + 1) / 4;
     DCHK(fs_restrict_rows(fs, op->d_yexp, op->d_hy, t0, t1, fs->stream));

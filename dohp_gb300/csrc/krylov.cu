@@ -598,15 +598,23 @@ static dErr cg_step(_p_dKSP *k, double *x, double *r, double *z, double *p, doub
   return 0;
 }
 
-// Preconditioned CG (PETSc KSPCG). After the first step, the step's launches (preconditioner, operator, dots,
-// updates) are captured once into a CUDA graph and replayed, so an iteration costs one graph launch and one read of
-// r.r; capture is skipped with a monitor (host code per iterate), a learned correction, a shell operator or an
-// operator on mixed orders / with its own launch form.
+// the convergence test of a device-looped CG: S[8] counts iterations; the loop continues while ||r|| > tol and fewer
+// than maxit iterations were done (the host loop's test, on the device)
+__global__ void k_cg_check(cudaGraphConditionalHandle h, double *S, double tol, double maxit) {
+  S[8] += 1.0;
+  cudaGraphSetConditional(h, (sqrt(S[2]) > tol && S[8] < maxit) ? 1u : 0u);
+}
+
+// Preconditioned CG (PETSc KSPCG). The first step runs eagerly (it makes the lazily allocated work arrays); the
+// remaining steps run as one CUDA graph: a while-conditional node whose body is the step's launches (captured once per
+// solve) followed by the convergence test on the device, so the whole solve costs one graph launch and one read of
+// r.r. The graph is skipped with a monitor (host code per iterate), a learned correction, a shell operator or an
+// operator on mixed orders / with its own launch form, which step eagerly with a host test per iteration.
 static dErr cg_solve(_p_dKSP *k, const double *b, double *x, double rtol, int maxit, int *its, double *rnorm) {
   const int64_t n = k->n;
   cudaStream_t s = kstream(k);
   double *r = k->d_work, *z = k->d_work + n, *p = k->d_work + 2 * n, *q = k->d_work + 3 * n;
-  double *S = k->d_s;  // S[0]=rz S[1]=pq S[2]=rr S[3]=bb S[4]=rz_new
+  double *S = k->d_s;  // S[0]=rz S[1]=pq S[2]=rr S[3]=bb S[4]=rz_new S[8]=iterations (device loop)
   DCHK(kmult(k, x, q, dPREC_FP64));
   CUCHK(cudaMemcpyAsync(r, b, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
   k_axpby<<<nb(n), 256, 0, s>>>(n, -1.0, nullptr, nullptr, q, 1.0, r);
@@ -623,43 +631,74 @@ static dErr cg_solve(_p_dKSP *k, const double *b, double *x, double rtol, int ma
   }
   if (k->monitor) DCHK(k->monitor(k->monitor_ctx, 0, x, r));
   // the operator's own launch forms for mixed orders (persistent kernel, its own graph) stay eager
-  const bool capture = !k->monitor && !k->correction && !k->shell_mult && k->op->fs->uniform && k->op->launch == dLAUNCH_DEFAULT;
-  cudaGraphExec_t exec = nullptr;
-  dErr err = 0;
-  for (int it = 0; it < maxit && !err; it++) {
-    if (it == 0 || !capture) {
-      err = cg_step(k, x, r, z, p, q, S, it == 0);
-    } else {
-      if (!exec) {  // capture on a private stream (the legacy default stream cannot be captured)
-        _p_dFS *fs = k->op->fs;
-        cudaStream_t cs;
-        CUCHK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-        fs->stream = cs;
-        cudaGraph_t g = nullptr;
-        cudaError_t ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-        if (ce == cudaSuccess) {
-          err = cg_step(k, x, r, z, p, q, S, false);
-          ce = cudaStreamEndCapture(cs, &g);
-        }
-        fs->stream = s;
-        cudaStreamDestroy(cs);
-        if (!err && ce != cudaSuccess) err = set_error("CG graph capture failed: %s", cudaGetErrorString(ce));
-        if (!err && cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) err = set_error("CG graph instantiation failed");
-        if (g) cudaGraphDestroy(g);
-        if (err) break;
-      }
-      if (cudaGraphLaunch(exec, s) != cudaSuccess) err = set_error("CG graph launch failed");
-      k->pc_applies++;  // the replayed step's preconditioner application
-    }
-    if (err) break;
-    if (k->monitor) err = k->monitor(k->monitor_ctx, it + 1, x, r);
-    if (!err) err = read_scalar(S + 2, &rr, s);
-    *its = it + 1;
-    if (err || !(sqrt(rr) > rtol * bn)) break;
+  const bool graph = !k->monitor && !k->correction && !k->shell_mult && k->op->fs->uniform && k->op->launch == dLAUNCH_DEFAULT;
+  DCHK(cg_step(k, x, r, z, p, q, S, true));
+  if (k->monitor) DCHK(k->monitor(k->monitor_ctx, 1, x, r));
+  DCHK(read_scalar(S + 2, &rr, s));
+  *its = 1;
+  if (!(sqrt(rr) > rtol * bn) || maxit <= 1) {
+    *rnorm = sqrt(rr) / bn;
+    return 0;
   }
+  if (!graph) {
+    for (int it = 1; it < maxit; it++) {
+      DCHK(cg_step(k, x, r, z, p, q, S, false));
+      if (k->monitor) DCHK(k->monitor(k->monitor_ctx, it + 1, x, r));
+      DCHK(read_scalar(S + 2, &rr, s));
+      *its = it + 1;
+      if (!(sqrt(rr) > rtol * bn)) break;
+    }
+    *rnorm = sqrt(rr) / bn;
+    return 0;
+  }
+  const double one = 1.0;
+  CUCHK(cudaMemcpyAsync(S + 8, &one, sizeof one, cudaMemcpyHostToDevice, s));
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t cs = nullptr;
+  dErr err = 0;
+  cudaGraphConditionalHandle h;
+  cudaGraphNodeParams cp = {};
+  cudaGraphNode_t node;
+  if (cudaGraphCreate(&g, 0) != cudaSuccess || cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) {
+    err = set_error("CG graph: conditional handle creation failed");
+  } else {
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    if (cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) != cudaSuccess) err = set_error("CG graph: conditional node creation failed");
+  }
+  const int64_t applies = k->pc_applies;  // the capture runs pc_apply's host bookkeeping once; the loop counts below
+  if (!err) {  // the body: one step and the test, captured on a private stream (the legacy stream cannot be captured)
+    _p_dFS *fs = k->op->fs;
+    CUCHK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    fs->stream = cs;
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cudaError_t ce = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (ce == cudaSuccess) {
+      err = cg_step(k, x, r, z, p, q, S, false);
+      if (!err) {
+        k_cg_check<<<1, 1, 0, cs>>>(h, S, rtol * bn, (double)maxit);
+        if (cudaGetLastError() != cudaSuccess) err = set_error("CG graph: test kernel launch failed");
+      }
+      ce = cudaStreamEndCapture(cs, &body);
+    }
+    fs->stream = s;
+    if (!err && ce != cudaSuccess) err = set_error("CG graph capture failed: %s", cudaGetErrorString(ce));
+  }
+  if (!err && cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) err = set_error("CG graph instantiation failed");
+  if (!err && cudaGraphLaunch(exec, s) != cudaSuccess) err = set_error("CG graph launch failed");
+  double hs[9];
+  if (!err && cudaMemcpyAsync(hs, S, sizeof hs, cudaMemcpyDeviceToHost, s) != cudaSuccess) err = set_error("CG: reading the result failed");
+  if (!err && cudaStreamSynchronize(s) != cudaSuccess) err = set_error("CG graph execution failed");
   if (exec) cudaGraphExecDestroy(exec);
+  if (g) cudaGraphDestroy(g);
+  if (cs) cudaStreamDestroy(cs);
   if (err) return err;
-  CUCHK(cudaGetLastError());
+  rr = hs[2];
+  *its = (int)hs[8];
+  k->pc_applies = applies + (*its - 1);  // one preconditioner application per iteration of the device loop
   *rnorm = sqrt(rr) / bn;
   return 0;
 }

@@ -113,29 +113,40 @@ __global__ void k_sym_extract(int64_t n, const double *__restrict__ A, double *_
 // y = A x (or b - A x) from the symmetric half: forward entries of node i, transposed forward entries of the
 // backward neighbours; about half the coefficient bytes of the full stencil
 template <int BS, typename T>
-__global__ void k_stencil_mv_sym(int Lx, int Ly, int Lz, const T *__restrict__ As, const T *__restrict__ x,
-                                 const T *__restrict__ b, T *__restrict__ y) {
-  const int64_t n = (int64_t)Lx * Ly * Lz;
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(256) k_stencil_mv_sym(int Lx, int Ly, int Lz, const T *__restrict__ As, const T *__restrict__ x,
+                                                        const T *__restrict__ b, T *__restrict__ y) {
+  // 32-bit lattice arithmetic (levels have fewer than 2^31 / BS nodes); interior nodes skip the bounds tests
+  const int n = Lx * Ly * Lz, Lyz = Ly * Lz;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * BS) return;
-  const int64_t i = t / BS;
-  const int ci = (int)(t % BS);
-  int ix, iy, iz;
-  lat_coord(i, Ly, Lz, ix, iy, iz);
+  const int i = t / BS, ci = t - i * BS;
+  const int ix = i / Lyz, r = i - ix * Lyz, iy = r / Lz, iz = r - iy * Lz;
   T s = 0;
 #pragma unroll
-  for (int cj = 0; cj < BS; cj++) s += As[((int64_t)ci * BS + cj) * n + i] * x[i * BS + cj];
+  for (int cj = 0; cj < BS; cj++) s += As[(ci * BS + cj) * (int64_t)n + i] * x[i * BS + cj];
+  if (ix > 0 && ix < Lx - 1 && iy > 0 && iy < Ly - 1 && iz > 0 && iz < Lz - 1) {
 #pragma unroll
-  for (int h = 1; h < 14; h++) {
-    const int st = 13 + h, a = st / 9 - 1, c = (st / 3) % 3 - 1, e = st % 3 - 1;
-    const int64_t o = ((int64_t)a * Ly + c) * Lz + e;
-    const int fx = ix + a, fy = iy + c, fz = iz + e, bx = ix - a, by = iy - c, bz = iz - e;
-    if (fx >= 0 && fx < Lx && fy >= 0 && fy < Ly && fz >= 0 && fz < Lz)
+    for (int h = 1; h < 14; h++) {
+      const int st = 13 + h, a = st / 9 - 1, c = (st / 3) % 3 - 1, e = st % 3 - 1;
+      const int o = a * Lyz + c * Lz + e;
 #pragma unroll
-      for (int cj = 0; cj < BS; cj++) s += As[((int64_t)(h * BS + ci) * BS + cj) * n + i] * x[(i + o) * BS + cj];
-    if (bx >= 0 && bx < Lx && by >= 0 && by < Ly && bz >= 0 && bz < Lz)
+      for (int cj = 0; cj < BS; cj++) s += As[((h * BS + ci) * BS + cj) * (int64_t)n + i] * x[(i + o) * BS + cj];
 #pragma unroll
-      for (int cj = 0; cj < BS; cj++) s += As[((int64_t)(h * BS + cj) * BS + ci) * n + (i - o)] * x[(i - o) * BS + cj];
+      for (int cj = 0; cj < BS; cj++) s += As[((h * BS + cj) * BS + ci) * (int64_t)n + (i - o)] * x[(i - o) * BS + cj];
+    }
+  } else {
+#pragma unroll
+    for (int h = 1; h < 14; h++) {
+      const int st = 13 + h, a = st / 9 - 1, c = (st / 3) % 3 - 1, e = st % 3 - 1;
+      const int o = a * Lyz + c * Lz + e;
+      const int fx = ix + a, fy = iy + c, fz = iz + e, bx = ix - a, by = iy - c, bz = iz - e;
+      if (fx >= 0 && fx < Lx && fy >= 0 && fy < Ly && fz >= 0 && fz < Lz)
+#pragma unroll
+        for (int cj = 0; cj < BS; cj++) s += As[((h * BS + ci) * BS + cj) * (int64_t)n + i] * x[(i + o) * BS + cj];
+      if (bx >= 0 && bx < Lx && by >= 0 && by < Ly && bz >= 0 && bz < Lz)
+#pragma unroll
+        for (int cj = 0; cj < BS; cj++) s += As[((h * BS + cj) * BS + ci) * (int64_t)n + (i - o)] * x[(i - o) * BS + cj];
+    }
   }
   y[t] = b ? b[t] - s : s;
 }
