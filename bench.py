@@ -338,7 +338,32 @@ def secondary_lognormal_apply(args):
            "fp64_frac_of_peak": issued / (kms * 1e-3) / 1e9 / FP64_PEAK_GFLOPS, "dtype": "f64"}
     out["float_float"] = float_float_leg(op, x, y, args, stream)
     out["float_float"]["value"] = fs.n / (out["float_float"]["ms_per_apply"] * 1e-3) / 1e9
+    out["bf16_tensor_core"] = bf16_tc_leg(fs, op, x, y, args, stream)
     return out
+
+
+def bf16_tc_leg(fs, op, x, y64, args, stream):
+    """the same apply with dPREC_BF16 (tcgen05 MMAs, BF16 operands, FP32 accumulation in tensor memory; BF16 geometric
+    factors; FP32 expanded output restricted in FP64): time, relative difference from the FP64 result, and the HBM rate
+    of its algorithmic bytes (x and y once in FP64, the int32 element map, 6 BF16 factors per Gauss point, the FP32
+    expanded output written and read once)"""
+    import numpy as np
+    import torch
+    import dohp_gb300 as dg
+    op.mult(x, y64)
+    op.set_precision(dg.dPREC_BF16)
+    yb = torch.empty_like(y64)
+    for _ in range(3):
+        op.mult(x, yb)
+    ms, _ = time_loop(lambda: op.mult(x, yb), max(args.steps, 5), stream)
+    err = float(torch.linalg.norm(yb - y64) / torch.linalg.norm(y64))
+    op.set_precision(dg.dPREC_FP64)
+    n1 = fs.elem_degree()[:, 0].astype(np.float64) + 1
+    nbytes = 16.0 * fs.nc + float(np.sum(4.0 * n1 ** 3 + 12.0 * n1 ** 3 + 8.0 * n1 ** 3))
+    hbm, src = peaks()
+    return {"unit": "GDoF/s", "value": fs.n / (ms * 1e-3) / 1e9, "ms_per_apply": ms, "rel_diff_vs_fp64": err,
+            "alg_bytes_per_apply": nbytes, "hbm_gbs": nbytes / (ms * 1e-3) / 1e9, "hbm_frac": nbytes / (ms * 1e-3) / 1e9 / hbm,
+            "dtype": "bf16 operands, fp32 accumulation (tcgen05 tensor cores)"}
 
 
 def float_float_leg(op, x, y64, args, stream):
