@@ -70,6 +70,8 @@ def parse():
                          "solves), newton)")
     ap.add_argument("--learned-ne", type=int, default=64, help="elements per side of the learned-correction solve")
     ap.add_argument("--learned-epochs", type=int, default=8)
+    ap.add_argument("--learned-grids", default="vertex,gll",
+                    help="lattices of the learned correction: vertex (mesh vertices), gll (GLL nodes, the Q1-embedded grid)")
     ap.add_argument("--newton-ne", type=int, default=48, help="elements per side of the p-Laplacian Newton run")
     ap.add_argument("--newton-pc", default="mg", choices=("mg", "cheb"),
                     help="Newton linear solves: Q1 multigrid (default) or the single-level Chebyshev-Jacobi")
@@ -610,40 +612,60 @@ def secondary_learned(args):
         m.assemble(grf=grf)
         return fs, op, m, grf
 
+    grids = [g for g in args.learned_grids.split(",") if g]
     out = {"workload": "lognormal-poisson-%d^3-p4, learned correction and multigrid" % ne, "rtol": 1e-8,
            "ksp": "FGMRES(30), Chebyshev(3)-Jacobi on the Q1-embedded matrix",
-           "network": "3-level U-Net 16/32/64 ch, 3^3 kernels, BF16 weights, FP32 accumulate, on the vertex lattice"}
-    fs0, _, _, _ = problem(1000)
-    net = dg.Learned(fs0, seed=7)
-    del fs0
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for f in range(nfields):
-        fs, op, m, grf = problem(1000 + f)
-        net.set_field(grf)
-        ksp = dg.KSP(op, m, ksp_type=dg.dKSP_CG)
-        b = torch.as_tensor(np.random.default_rng(1000 + f).uniform(-1, 1, fs.n), device="cuda")
-        net.collect(ksp, b, rtol=1e-10, every=3, max_pairs=per_field)
-        del fs, op, m, ksp, b
-    torch.cuda.synchronize()
-    out["pairs"] = net.npairs
-    out["collect_s"] = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    losses = net.train(epochs=epochs, batch=16, lr=1e-3, seed=1)
-    torch.cuda.synchronize()
-    out["train_s"] = time.perf_counter() - t0
-    out["epochs"] = epochs
-    out["loss_per_epoch"] = [float(v) for v in losses]
+           "network": "3-level U-Net 16/32/64 ch, 3^3 kernels, BF16 weights, FP32 accumulate; the stride-1 16/32-channel "
+                      "convolutions on the tcgen05 tensor cores (BF16 activations at their inputs), the others on CUDA cores"}
+    nets = {}
+    for grid in grids:  # learned_* keys: the vertex lattice; learned_gll_*: the GLL lattice of the Q1-embedded matrix
+        fs0, _, _, _ = problem(1000)
+        if grid == "gll":
+            net = dg.Learned(fs0, seed=7, grid=dg.LEARNED_GRID_GLL, crop=65)
+        else:
+            net = dg.Learned(fs0, seed=7)
+        del fs0
+        info = {"lattice": "x".join(str(v) for v in net.dims)}
+        if grid == "gll":
+            info["training_window"] = "65^3 windows at origins that are multiples of 4"
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for f in range(nfields):
+            fs, op, m, grf = problem(1000 + f)
+            net.set_field(grf)
+            ksp = dg.KSP(op, m, ksp_type=dg.dKSP_CG)
+            b = torch.as_tensor(np.random.default_rng(1000 + f).uniform(-1, 1, fs.n), device="cuda")
+            net.collect(ksp, b, rtol=1e-10, every=3, max_pairs=per_field)
+            del fs, op, m, ksp, b
+        torch.cuda.synchronize()
+        info["pairs"] = net.npairs
+        info["collect_s"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        losses = net.train(epochs=epochs, batch=16, lr=1e-3, seed=1)
+        torch.cuda.synchronize()
+        info["train_s"] = time.perf_counter() - t0
+        info["epochs"] = epochs
+        info["loss_per_epoch"] = [float(v) for v in losses]
+        nets[grid] = net
+        if grid == "vertex":
+            out.update(info)
+        else:
+            out["gll_network"] = info
     fs, op, m, grf = problem(5000)
-    net.set_field(grf)
+    for net in nets.values():
+        net.set_field(grf)
     b = torch.as_tensor(np.random.default_rng(5000).uniform(-1, 1, fs.n), device="cuda")
     out["dofs"] = fs.n
-    for name, prec, learned in (("plain_fp64", dg.dPREC_FP64, False), ("mixed_fp32", dg.dPREC_FP32, False),
-                                ("mixed_bf16", dg.dPREC_BF16, False), ("learned_mixed", dg.dPREC_FP32, True),
-                                ("learned_bf16", dg.dPREC_BF16, True), ("learned_fp64", dg.dPREC_FP64, True)):
+    legs = [("plain_fp64", dg.dPREC_FP64, None), ("mixed_fp32", dg.dPREC_FP32, None), ("mixed_bf16", dg.dPREC_BF16, None)]
+    if "vertex" in nets:
+        legs += [("learned_mixed", dg.dPREC_FP32, "vertex"), ("learned_bf16", dg.dPREC_BF16, "vertex"),
+                 ("learned_fp64", dg.dPREC_FP64, "vertex")]
+    if "gll" in nets:
+        legs += [("learned_gll_mixed", dg.dPREC_FP32, "gll")]
+    for name, prec, learned in legs:
         ksp = dg.KSP(op, m, ksp_type=dg.dKSP_FGMRES, inner_prec=prec, restart=30)
         if learned:
-            ksp.set_learned(net)
+            ksp.set_learned(nets[learned])
         x = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
         try:  # set-up (power iteration, FP32 copies) outside the timed solve
             ksp.solve(b, x, rtol=1e-1, maxit=200)
@@ -663,7 +685,7 @@ def secondary_learned(args):
     out.update(multigrid_solves(fs, op, m, b))
     out["speedup_vs_plain_fp64"] = {k: out["plain_fp64"]["wall_s"] / out[k]["wall_s"]
                                     for k in ("mixed_fp32", "mixed_bf16", "learned_mixed", "learned_bf16", "learned_fp64",
-                                              "multigrid_cg_fp64", "multigrid_mixed_fp32")}
+                                              "learned_gll_mixed", "multigrid_cg_fp64", "multigrid_mixed_fp32") if k in out}
     return out
 
 

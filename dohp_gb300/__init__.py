@@ -547,13 +547,20 @@ def plap_newton(op, pmat, ksp, b, u, p, eps, rtol=1e-8, atol=0.0, lin_rtol=1e-3,
     return k, fn[:k + 1], li[:k]
 
 
-class Learned:
-    """dLearned: learned coarse correction (U-Net on the vertex lattice) for FGMRES."""
+LEARNED_GRID_VERTEX, LEARNED_GRID_GLL = 0, 1
 
-    def __init__(self, fs, seed=0):
+
+class Learned:
+    """dLearned: learned correction (U-Net on the vertex lattice, or on the GLL lattice of the Q1-embedded matrix
+    trained on crop^3 windows) for FGMRES."""
+
+    def __init__(self, fs, seed=0, grid=LEARNED_GRID_VERTEX, crop=0):
         self.fs = fs
         self.h = _vp()
-        chk(lib().dLearnedCreate(fs.h, ctypes.c_uint64(seed), ctypes.byref(self.h)))
+        if grid == LEARNED_GRID_VERTEX and not crop:
+            chk(lib().dLearnedCreate(fs.h, ctypes.c_uint64(seed), ctypes.byref(self.h)))
+        else:
+            chk(lib().dLearnedCreateOnGrid(fs.h, ctypes.c_int(grid), _i32(crop), ctypes.c_uint64(seed), ctypes.byref(self.h)))
         d = np.zeros(3, np.int32)
         npar, npairs = _i64(), _i64()
         chk(lib().dLearnedGetSizes(self.h, ptr(d), ctypes.byref(npar), ctypes.byref(npairs)))
@@ -618,6 +625,22 @@ class Learned:
         a, d = _i64(), _i64()
         chk(lib().dLearnedGetStats(self.h, ctypes.byref(a), ctypes.byref(d)))
         return a.value, d.value
+
+    def layer(self, layer, x, y, dims, transpose=False):
+        """one convolution layer on device FP32 arrays (forward, or its data gradient with transpose)"""
+        d = np.asarray(dims, np.int32)
+        chk(lib().dLearnedLayerApply(self.h, _i32(layer), _i32(int(transpose)), _i32(x.shape[0]), ptr(d), ptr(x), ptr(y)))
+
+    def set_tensor_cores(self, on=True):
+        chk(lib().dLearnedSetTensorCores(self.h, ctypes.c_int(int(on))))
+
+    def pair(self, p):
+        """recorded pair p: (origin, input, target), the arrays shaped as its window"""
+        win, org = np.zeros(3, np.int32), np.zeros(3, np.int32)
+        chk(lib().dLearnedGetPair(self.h, _i32(p), ptr(win), ptr(org), None, None))
+        inp, tg = np.zeros(tuple(win), np.float32), np.zeros(tuple(win), np.float32)
+        chk(lib().dLearnedGetPair(self.h, _i32(p), ptr(win), ptr(org), ptr(inp), ptr(tg)))
+        return tuple(int(v) for v in org), inp, tg
 
 
 def _ksp_set_learned(self, net, policy=2):

@@ -8,7 +8,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libdohp_gb300.so")
-SOURCES = ["basis.cu", "mesh_fs.cu", "fs.cu", "operator.cu", "q1.cu", "krylov.cu", "capi.cu", "hp.cu", "iterator.cu", "plap.cu", "unet.cu", "facet.cu", "stokes.cu", "mg.cu", "rules.cu", "tc_apply.cu", "dhm.cu"]
+SOURCES = ["basis.cu", "mesh_fs.cu", "fs.cu", "operator.cu", "q1.cu", "krylov.cu", "capi.cu", "hp.cu", "iterator.cu", "plap.cu", "unet.cu", "facet.cu", "stokes.cu", "mg.cu", "rules.cu", "tc_apply.cu", "dhm.cu", "conv_tc.cu"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
          "--extended-lambda", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
@@ -17,7 +17,8 @@ FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std
 def _compile(src):
     obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
     path = os.path.join(CSRC, src)
-    deps = [path, os.path.join(CSRC, "internal.h"), os.path.join(CSRC, "element.cuh"), os.path.join(HERE, "..", "include", "dohp_gb300.h")]
+    deps = [path, os.path.join(HERE, "..", "include", "dohp_gb300.h")] + \
+        [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj, ""
     cmd = [NVCC] + FLAGS + ["-c", path, "-o", obj]

@@ -531,12 +531,15 @@ static dErr level_alloc(MGLevel &l, int bs) {
   return 0;
 }
 
-// lattice position of every explicit node (element (ex, ey, ez) local node (a, b, c) -> (ex p + a, ...)),
-// made once per space and kept on it (every Newton step rebuilds the hierarchy, not the map)
-static dErr lattice_map(_p_dFS *fs, const int L0[3], int My, int Mz) {
-  if (fs->d_mg_lat) return 0;
-  const int p = fs->p, P = p + 1;
-  std::vector<int32_t> lat(fs->n, -1);
+// lattice position of every explicit node of a uniform-order space on a block mesh: elements in x-major order,
+// element (ex, ey, ez) local node (a, b, c) -> GLL lattice node (ex p + a, ey p + b, ez p + c) of the
+// (M p + 1)-per-direction lattice L0; also used by the learned correction on the GLL lattice
+dErr fs_gll_lattice(_p_dFS *fs, std::vector<int32_t> &lat, int L0[3]) {
+  if (!fs->uniform) return set_error("the GLL lattice needs a uniform-order space");
+  const _p_dMesh *mesh = fs->mesh;
+  const int p = fs->p, P = p + 1, My = mesh->ny - 1, Mz = mesh->nz - 1;
+  L0[0] = (mesh->nx - 1) * p + 1, L0[1] = My * p + 1, L0[2] = Mz * p + 1;
+  lat.assign(fs->n, -1);
   for (int64_t r = 0; r < fs->nelem; r++) {
     const int ex = (int)(r / ((int64_t)My * Mz)), ey = (int)((r / Mz) % My), ez = (int)(r % Mz);
     for (int a = 0; a < P; a++)
@@ -551,6 +554,16 @@ static dErr lattice_map(_p_dFS *fs, const int L0[3], int My, int Mz) {
   }
   for (int64_t d = 0; d < fs->n; d++)
     if (lat[d] < 0) return set_error("dof %lld has no lattice position", (long long)d);
+  return 0;
+}
+
+// the lattice map on the device, made once per space and kept on it (every Newton step rebuilds the hierarchy,
+// not the map)
+static dErr lattice_map(_p_dFS *fs) {
+  if (fs->d_mg_lat) return 0;
+  std::vector<int32_t> lat;
+  int L0[3];
+  DCHK(fs_gll_lattice(fs, lat, L0));
   CUCHK(cudaMalloc(&fs->d_mg_lat, std::max<int64_t>(fs->n, 1) * sizeof(int32_t)));
   CUCHK(cudaMemcpy(fs->d_mg_lat, lat.data(), fs->n * sizeof(int32_t), cudaMemcpyHostToDevice));
   return 0;
@@ -573,7 +586,7 @@ dErr mg_build(_p_dMat *J, int degree, bool fp32, void **out) {
   M->bs = bs;
   M->degree = std::max(2, degree);
   M->n = fs->n;
-  dErr le = lattice_map(fs, L0, My, Mz);
+  dErr le = lattice_map(fs);
   if (le) {
     mg_free(M);
     return le;

@@ -25,6 +25,7 @@
 #include <stdint.h>
 
 #include "internal.h"
+#include "tcgen05.cuh"
 
 using namespace dgb;
 
@@ -42,68 +43,6 @@ constexpr int kThreads = 256;
 constexpr long long kWaitCycles = 4000000000LL;  // about 2 s at the maximum SM clock
 
 __device__ int g_tc_error;  // 1: an mbarrier wait timed out
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// shared-memory matrix descriptor: no swizzle, K-major, core matrices of 8 rows x 16 bytes
-__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) | ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) |
-         (1ull << 46);
-}
-
-// instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, M = 128, N = n
-__host__ __device__ constexpr uint32_t idesc_bf16(int n) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t dt, uint64_t a, uint64_t b, uint32_t id, uint32_t accum) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dt), "l"(a),
-      "l"(b), "r"(id), "r"(accum));
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t *bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// bounded wait for the phase with the given parity; false on timeout (the error flag is set)
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  const long long t0 = clock64();
-  while (!mbar_try(bar, parity)) {
-    if (clock64() - t0 > kWaitCycles) {
-      atomicExch(&g_tc_error, 1);
-      return false;
-    }
-  }
-  return true;
-}
-
-// 32 lanes x 32 bits, 16 consecutive columns of this thread's lane
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]),
-        "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-#pragma unroll
-  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void async_proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // byte offset of (row, k) in a K-major no-swizzle operand with kp columns (kp = 16 or 32) and 128-row tiles
 __device__ __forceinline__ uint32_t aoff(int row, int k, int kp) {
@@ -142,7 +81,7 @@ __device__ __forceinline__ bool run_pass(uint32_t tmem, uint32_t a_base, int kp,
                  sdesc(b_base + (uint32_t)(s * 256), 128, 4 * 128), id, s > 0);
     mma_commit(bar);
   }
-  const bool mine = mbar_wait(bar, phase);
+  const bool mine = mbar_wait(bar, phase, kWaitCycles, &g_tc_error);
   phase ^= 1u;
   const bool ok = __syncthreads_and(mine) != 0;  // every thread leaves with the same verdict
   tc_fence_after();

@@ -1,18 +1,22 @@
 // Learned coarse correction for the Q1-embedded Chebyshev-Jacobi preconditioner (no counterpart in the
 // reference; the preconditioner it augments is the one EllipJacobian assembles, ellip.c:474-536).
 //
-// A 3-level 3-D convolutional U-Net (16/32/64 channels, 3x3x3 kernels, BF16 weights, FP32 accumulation)
-// runs on the Q1 lattice of the mesh vertices, the coarsest level of the embedded Q1 hierarchy. Input
-// channels: the restricted residual R r (R = P^T, normalised by its RMS over interior vertices) and log k at
-// the vertices. Output: the error at the vertices, which P (trilinear interpolation of the vertex lattice
-// onto every GLL node, element by element) carries back to the global dofs: FGMRES uses
-// z = Chebyshev(r) + P N(R r). The smoother handles the high frequencies; the network supplies the coarse
-// correction that Chebyshev-Jacobi lacks.
+// A 3-level 3-D convolutional U-Net (16/32/64 channels, 3x3x3 kernels, BF16 weights, FP32 accumulation) runs on one
+// of two lattices. The vertex lattice (the coarsest level of the embedded Q1 hierarchy): input channels R r
+// (R = P^T, normalised by its RMS over interior vertices) and log k at the vertices, output the error at the
+// vertices, which P (trilinear interpolation of the vertex lattice onto every GLL node, element by element) carries
+// back to the global dofs. Or the GLL-node lattice of the Q1-embedded matrix itself ((M p + 1) nodes per direction):
+// R and P are then the injection of the explicit dofs, and the network is trained on windows of the lattice (the
+// recorded pairs are cut to crop^3 windows at seeded origins that are multiples of 4, so the coarse levels of a
+// window line up with those of the whole lattice) and applied to the whole lattice. FGMRES uses
+// z = Chebyshev(r) + P N(R r).
 //
-// Training pairs (residual, error) come from the plain solver: a CG monitor records R r_k and x_k at the
-// vertices; once the solve has converged, the targets are x* - x_k at the vertices. Training is plain
-// minibatch Adam on the mean squared error over interior vertices, with hand-written forward and backward
-// kernels (direct convolutions, FP32 activations, deterministic two-stage weight-gradient sums).
+// Training pairs (residual, error) come from the plain solver: a CG monitor records R r_k and x_k on the lattice
+// (or its window); once the solve has converged, the targets are x* - x_k there. Training is plain minibatch Adam on
+// the mean squared error over interior nodes, with hand-written forward and backward kernels: the stride-1
+// convolutions of 16 / 32 channels and their data gradients on the tcgen05 tensor cores (conv_tc.cu, BF16 operands,
+// FP32 accumulation), the other convolutions and every weight gradient as direct FP32 convolutions on the CUDA
+// cores (deterministic two-stage weight-gradient sums), activations FP32 in memory.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -29,6 +33,12 @@ dErr ksp_set_correction(dKSP ksp, dErr (*fn)(void *, const double *, double *), 
 dErr ksp_solve(dKSP ksp, const double *b, double *x, double rtol, int maxit, int *its, double *rnorm);
 dErr op_mult(_p_dOperator *op, const double *x, double *y);
 dErr ksp_get_operator(dKSP ksp, dOperator *op);
+dErr fs_gll_lattice(_p_dFS *fs, std::vector<int32_t> &lat, int L0[3]);
+bool conv_tc_supported(int ci, int co);
+dErr conv_tc_pack(int ci, int co, bool transpose, const __nv_bfloat16 *W, __nv_bfloat16 *out, cudaStream_t s);
+dErr conv_tc(int B, int ci, int co, const int d[3], const float *x, const __nv_bfloat16 *wpack, const float *bias, int relu,
+             int accumulate, float *y, cudaStream_t s);
+dErr conv_tc_check(cudaStream_t s);
 
 namespace {
 
@@ -54,6 +64,16 @@ __device__ __forceinline__ void vox(int64_t r, Dims d, int &i, int &j, int &k) {
   j = (int)(q % d.y);
   i = (int)(q / d.y);
 }
+
+// a t-sized window of the lattice d: voxel v of the window at origin o[3] -> its index in the whole lattice
+struct Win {
+  Dims t, d;
+  __device__ int64_t full(const int32_t *o, int64_t v) const {
+    int i, j, k;
+    vox(v, t, i, j, k);
+    return ((int64_t)(o[0] + i) * d.y + o[1] + j) * d.z + o[2] + k;
+  }
+};
 
 // y = act(conv(x) + bias) [+ skip]; x [B][Ci][di], W [Co][Ci][27] (bf16), y [B][Co][dout]
 template <int CO_T>
@@ -506,14 +526,15 @@ __global__ void k_copy_f(int64_t n, const float *__restrict__ a, float *__restri
   if (i < n) b[i] = a[i];
 }
 
-// MSE over interior vertices: grad = 2 (y - t) / count, block partial sums of (y - t)^2
+// MSE over interior lattice nodes (mask [B][nv], one per sample): grad = 2 (y - t) / count, block partial sums
+// of (y - t)^2
 __global__ void k_mse(int B, int64_t nv, const float *__restrict__ y, const float *__restrict__ tg, const uint8_t *__restrict__ mask,
                       float inv_count, float *__restrict__ grad, double *__restrict__ part) {
   __shared__ double red[256];
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double l = 0;
   if (i < (int64_t)B * nv) {
-    const bool in = mask[i % nv];
+    const bool in = mask[i];
     const float d = in ? y[i] - tg[i] : 0.f;
     grad[i] = 2.f * d * inv_count;
     l = (double)d * d;
@@ -527,13 +548,12 @@ __global__ void k_mse(int B, int64_t nv, const float *__restrict__ y, const floa
   if (threadIdx.x == 0) part[blockIdx.x] = red[0];
 }
 
-// partial sums of squares of the targets over interior vertices
-__global__ void k_masked_sumsq(int64_t total, int64_t nv, const float *__restrict__ t, const uint8_t *__restrict__ mask,
-                               double *__restrict__ part) {
+// partial sums of squares of the targets (zero at the masked nodes, where x* and x_k are gathered as zero)
+__global__ void k_sumsq(int64_t total, const float *__restrict__ t, double *__restrict__ part) {
   __shared__ double red[256];
   double l = 0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
-    if (mask[i % nv]) l += (double)t[i] * t[i];
+    l += (double)t[i] * t[i];
   red[threadIdx.x] = l;
   __syncthreads();
   for (int s = 128; s > 0; s >>= 1) {
@@ -598,33 +618,60 @@ __global__ void k_prolong_add(int64_t n, const int32_t *__restrict__ rp, const i
   z[i] += s;
 }
 
-// x at the lattice vertices (0 where the vertex is not an explicit dof)
+// x at the lattice nodes (0 where the node is not an explicit dof)
 __global__ void k_gather_vertices(int64_t nv, const int32_t *__restrict__ vdof, const double *__restrict__ x, double *__restrict__ xv) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < nv) xv[i] = vdof[i] >= 0 ? x[vdof[i]] : 0.0;
 }
 
-// target = (x* - x_k) / scale_k at the vertices
-__global__ void k_targets(int64_t nv, int npairs, const double *__restrict__ xstar, const double *__restrict__ xk,
-                          const double *__restrict__ scale, float *__restrict__ tg) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= nv * npairs) return;
-  const int64_t p = t / nv, i = t % nv;
-  const double s = scale[p];
-  tg[t] = s > 0 ? (float)((xstar[i] - xk[t]) / s) : 0.f;
+// a window of a lattice array (FP32), and x at the nodes of a window (FP64, 0 where the node is not an explicit dof)
+__global__ void k_crop_f(Win w, int o0, int o1, int o2, const float *__restrict__ full, float *__restrict__ out) {
+  const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (v >= w.t.n()) return;
+  const int32_t o[3] = {o0, o1, o2};
+  out[v] = full[w.full(o, v)];
 }
 
-// minibatch: in[b][0] = pair input, in[b][1] = log k of the pair's field; tb[b] = target / ysc
-__global__ void k_batch(int B, int64_t nv, const int32_t *__restrict__ idx, const int32_t *__restrict__ pfield,
-                        const float *__restrict__ pin, const float *__restrict__ ptg, const float *__restrict__ flogk, float inv_ysc,
-                        float *__restrict__ in, float *__restrict__ tb) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= (int64_t)B * nv) return;
-  const int64_t b = t / nv, i = t % nv;
+__global__ void k_gather_crop(Win w, int o0, int o1, int o2, const int32_t *__restrict__ vdof, const double *__restrict__ x,
+                              double *__restrict__ out) {
+  const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (v >= w.t.n()) return;
+  const int32_t o[3] = {o0, o1, o2};
+  const int32_t d = vdof[w.full(o, v)];
+  out[v] = d >= 0 ? x[d] : 0.0;
+}
+
+// target = (x* - x_k) / scale_k on each pair's window (origins orig[p][3]; x* on the whole lattice)
+__global__ void k_targets(Win w, int npairs, const int32_t *__restrict__ orig, const double *__restrict__ xstar,
+                          const double *__restrict__ xk, const double *__restrict__ scale, float *__restrict__ tg) {
+  const int64_t nt = w.t.n(), t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nt * npairs) return;
+  const int64_t p = t / nt, v = t % nt;
+  const double s = scale[p];
+  tg[t] = s > 0 ? (float)((xstar[w.full(orig + 3 * p, v)] - xk[t]) / s) : 0.f;
+}
+
+// minibatch: in[b][0] = pair input, in[b][1] = log k of the pair's field on its window; tb[b] = target / ysc;
+// bmask[b] = the interior mask on the window
+__global__ void k_batch(int B, Win w, const int32_t *__restrict__ idx, const int32_t *__restrict__ pfield,
+                        const int32_t *__restrict__ porig, const float *__restrict__ pin, const float *__restrict__ ptg,
+                        const float *__restrict__ flogk, const uint8_t *__restrict__ mask, float inv_ysc, float *__restrict__ in,
+                        float *__restrict__ tb, uint8_t *__restrict__ bmask) {
+  const int64_t nt = w.t.n(), n0 = w.d.n(), t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)B * nt) return;
+  const int64_t b = t / nt, v = t % nt;
   const int p = idx[b];
-  in[(b * 2) * nv + i] = pin[(int64_t)p * nv + i];
-  in[(b * 2 + 1) * nv + i] = flogk[(int64_t)pfield[p] * nv + i];
-  tb[t] = ptg[(int64_t)p * nv + i] * inv_ysc;
+  const int64_t f = w.full(porig + 3 * p, v);
+  in[(b * 2) * nt + v] = pin[(int64_t)p * nt + v];
+  in[(b * 2 + 1) * nt + v] = flogk[(int64_t)pfield[p] * n0 + f];
+  tb[t] = ptg[(int64_t)p * nt + v] * inv_ysc;
+  bmask[t] = mask[f];
+}
+
+// the interior mask repeated for B samples
+__global__ void k_bmask(int B, int64_t nv, const uint8_t *__restrict__ mask, uint8_t *__restrict__ bmask) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t < (int64_t)B * nv) bmask[t] = mask[t % nv];
 }
 
 // seeded uniform values in [-1, 1) (splitmix64 of the index)
@@ -665,9 +712,13 @@ inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)((n + t - 1) / t
 // ------------------------------------------------------------------------------------------ object
 struct _p_dLearned {
   _p_dFS *fs = nullptr;
-  Dims d[3];
-  int64_t nint = 0;
-  // transfer between the global dofs and the vertex lattice
+  int grid = dLEARNED_GRID_VERTEX;
+  Dims d[3];                   // the lattice and its two coarse levels (inference)
+  Dims dt[3];                  // the training window and its coarse levels (d when training on the whole lattice)
+  const Dims *cur = nullptr;   // the dims the network runs on next (d or dt)
+  int64_t nint = 0;            // interior (explicit dof) nodes of the lattice
+  double lnorm = 1;            // nodes per sample the loss is averaged over (nint, or the window's size)
+  // transfer between the global dofs and the lattice
   int32_t *Pp = nullptr, *Pc = nullptr, *Rp = nullptr, *Rc = nullptr, *vdof = nullptr;
   double *Pv = nullptr, *Rv = nullptr, *vxyz = nullptr;
   uint8_t *mask = nullptr;
@@ -676,26 +727,34 @@ struct _p_dLearned {
   int64_t woff[NLAYER], boff[NLAYER], nparam = 0;
   float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
   __nv_bfloat16 *wb = nullptr;
+  // tensor-core convolutions (conv_tc.cu) for the stride-1 layers of 16 / 32 channels: packed B operands of the
+  // forward convolution and of its data gradient per layer (-1: the layer runs on the CUDA cores)
+  bool use_tc = true, tc_checked = false;
+  __nv_bfloat16 *wtc = nullptr;
+  int64_t tcf[16], tct[16];
   int64_t adam_t = 0;
   double ysc = 1.0;
   bool trained = false;
-  // activations and gradients for a batch of up to cap samples
-  int cap = 0;
+  // activations and gradients, each grown to the largest (batch, dims) requested so far
   float *act[16] = {};
+  int64_t acap[16] = {};
   float *G1 = nullptr, *G2 = nullptr, *GZ = nullptr, *ga1 = nullptr, *ga2 = nullptr, *tb = nullptr, *partial = nullptr;
-  int64_t partial_len = 0;
+  int64_t gcap[6] = {}, partial_len = 0, bmcap = 0, lpcap = 0;
+  uint8_t *bmask = nullptr;  // interior mask per sample of a batch
   double *lpart = nullptr;
   // correction workspace
   double *rc = nullptr, *ss = nullptr, *scale = nullptr, *dpart = nullptr;
   int *bad = nullptr;
   int64_t applies = 0, dropped = 0;
-  // training pairs
+  // training pairs: input and target on a window (dt) of the lattice at origin porig[p][3], the field of each pair
   int maxpairs = 0, npairs = 0, nfields = 0, maxfields = 0;
   float *pin = nullptr, *ptg = nullptr, *flogk = nullptr;
-  int32_t *pfield = nullptr;
-  std::vector<int32_t> h_pfield;
+  int32_t *pfield = nullptr, *porig = nullptr;
+  std::vector<int32_t> h_pfield, h_porig;
+  std::mt19937_64 wgen;  // window origins
   // collection in progress
   double *cxk = nullptr, *cscale = nullptr, *cxstar = nullptr;
+  float *cin = nullptr;  // the whole lattice's input channel of the current iterate
   int cfirst = 0, ccount = 0, cevery = 1, cmax = 0;
 };
 
@@ -710,45 +769,72 @@ struct Shape {
 constexpr Shape kAct[NACT] = {{2, 0},  {16, 0}, {16, 0}, {32, 1}, {32, 1}, {64, 2}, {64, 2}, {64, 2},
                               {32, 2}, {32, 1}, {32, 1}, {16, 1}, {16, 0}, {16, 0}, {1, 0}};
 
-dErr ensure_cap(_p_dLearned *L, int B) {
-  if (B <= L->cap) return 0;
-  for (int i = 0; i < NACT; i++) {
-    cudaFree(L->act[i]);
-    L->act[i] = nullptr;
-  }
-  for (float **p : {&L->G1, &L->G2, &L->GZ, &L->ga1, &L->ga2, &L->tb, &L->partial}) {
-    cudaFree(*p);
-    *p = nullptr;
-  }
-  cudaFree(L->lpart);
-  L->lpart = nullptr;
-  for (int i = 0; i < NACT; i++) CUCHK(cudaMalloc(&L->act[i], (size_t)B * kAct[i].c * L->d[kAct[i].level].n() * sizeof(float)));
+// grow a device buffer to at least n elements (its contents are not kept)
+template <typename T>
+dErr grow(T **p, int64_t *cap, int64_t n) {
+  if (n <= *cap) return 0;
+  cudaFree(*p);
+  *p = nullptr;
+  CUCHK(cudaMalloc(p, std::max<int64_t>(n, 1) * sizeof(T)));
+  *cap = n;
+  return 0;
+}
+
+// buffers for a batch of B samples on the dims L->cur: the activations, and with grads the gradient buffers
+dErr ensure_cap(_p_dLearned *L, int B, bool grads) {
+  const Dims *d = L->cur;
+  for (int i = 0; i < NACT; i++) DCHK(grow(&L->act[i], &L->acap[i], (int64_t)B * kAct[i].c * d[kAct[i].level].n()));
+  if (!grads) return 0;
   int64_t gmax = 0;
-  for (int i = 0; i < NACT; i++) gmax = std::max<int64_t>(gmax, (int64_t)kAct[i].c * L->d[kAct[i].level].n());
-  for (float **p : {&L->G1, &L->G2, &L->GZ}) CUCHK(cudaMalloc(p, (size_t)B * gmax * sizeof(float)));
-  CUCHK(cudaMalloc(&L->ga1, (size_t)B * 16 * L->d[0].n() * sizeof(float)));
-  CUCHK(cudaMalloc(&L->ga2, (size_t)B * 32 * L->d[1].n() * sizeof(float)));
-  CUCHK(cudaMalloc(&L->tb, (size_t)B * L->d[0].n() * sizeof(float)));
-  CUCHK(cudaMalloc(&L->lpart, (size_t)nblk((int64_t)B * L->d[0].n()) * sizeof(double)));
+  for (int i = 0; i < NACT; i++) gmax = std::max<int64_t>(gmax, (int64_t)kAct[i].c * d[kAct[i].level].n());
+  DCHK(grow(&L->G1, &L->gcap[0], B * gmax));
+  DCHK(grow(&L->G2, &L->gcap[1], B * gmax));
+  DCHK(grow(&L->GZ, &L->gcap[2], B * gmax));
+  DCHK(grow(&L->ga1, &L->gcap[3], (int64_t)B * 16 * d[0].n()));
+  DCHK(grow(&L->ga2, &L->gcap[4], (int64_t)B * 32 * d[1].n()));
+  DCHK(grow(&L->tb, &L->gcap[5], (int64_t)B * d[0].n()));
+  DCHK(grow(&L->bmask, &L->bmcap, (int64_t)B * d[0].n()));
+  DCHK(grow(&L->lpart, &L->lpcap, (int64_t)nblk((int64_t)B * d[0].n())));
   // weight-gradient partials: the largest chunk count times parameters over the layers
   int64_t need = 0;
   for (int l = 0; l < NLAYER; l++) {
     const LayerDef &ld = kLayer[l];
-    const Dims dout = ld.stride == 2 ? L->d[ld.level_in + 1] : L->d[ld.level_in];
+    const Dims dout = ld.stride == 2 ? d[ld.level_in + 1] : d[ld.level_in];
     const int64_t nch = ((int64_t)B * dout.x * dout.y * ((dout.z + VZ - 1) / VZ) + kQuadChunk - 1) / kQuadChunk;
     need = std::max<int64_t>(need, nch * ((int64_t)ld.co * ld.ci * 27 + ld.co));
   }
-  CUCHK(cudaMalloc(&L->partial, need * sizeof(float)));
-  L->partial_len = need;
-  L->cap = B;
+  DCHK(grow(&L->partial, &L->partial_len, need));
   return 0;
+}
+
+bool layer_tc(const _p_dLearned *L, int l) { return L->use_tc && L->tcf[l] >= 0; }
+
+// the tensor-core layers' packed weights from the BF16 copies (after every change of the weights)
+dErr repack_tc(_p_dLearned *L, cudaStream_t s) {
+  for (int l = 0; l < NLAYER; l++) {
+    if (L->tcf[l] < 0) continue;
+    DCHK(conv_tc_pack(kLayer[l].ci, kLayer[l].co, false, L->wb + L->woff[l], L->wtc + L->tcf[l], s));
+    DCHK(conv_tc_pack(kLayer[l].ci, kLayer[l].co, true, L->wb + L->woff[l], L->wtc + L->tct[l], s));
+  }
+  return 0;
+}
+
+// the first tensor-core convolutions of a network are checked synchronously for a timed-out MMA wait
+dErr tc_first_check(_p_dLearned *L, cudaStream_t s) {
+  if (L->tc_checked || !L->use_tc) return 0;
+  L->tc_checked = true;
+  return conv_tc_check(s);
 }
 
 dErr conv_fwd(_p_dLearned *L, int l, int B, const float *x, float *y, int relu, cudaStream_t s) {
   const LayerDef &ld = kLayer[l];
-  const Dims di = L->d[ld.level_in], dout = ld.stride == 2 ? L->d[ld.level_in + 1] : di;
+  const Dims di = L->cur[ld.level_in], dout = ld.stride == 2 ? L->cur[ld.level_in + 1] : di;
   const __nv_bfloat16 *W = L->wb + L->woff[l];
   const float *bias = L->w + L->boff[l];
+  if (layer_tc(L, l)) {
+    const int d3[3] = {di.x, di.y, di.z};
+    return conv_tc(B, ld.ci, ld.co, d3, x, L->wtc + L->tcf[l], bias, relu, 0, y, s);
+  }
   if (ld.co >= 16) {
     const int64_t nq = (int64_t)dout.x * dout.y * ((dout.z + VZ - 1) / VZ);
     dim3 grid(nblk((int64_t)B * nq, 128), (ld.co + 15) / 16);
@@ -762,9 +848,29 @@ dErr conv_fwd(_p_dLearned *L, int l, int B, const float *x, float *y, int relu, 
   return 0;
 }
 
+// gx (=, or += with accumulate) = the data gradient of layer l for the output gradient gz
+dErr conv_data(_p_dLearned *L, int l, int B, const float *gz, float *gx, int accumulate, cudaStream_t s) {
+  const LayerDef &ld = kLayer[l];
+  const Dims di = L->cur[ld.level_in], dout = ld.stride == 2 ? L->cur[ld.level_in + 1] : di;
+  if (layer_tc(L, l)) {  // the convolution of gz with the flipped kernel, channels swapped
+    const int d3[3] = {di.x, di.y, di.z};
+    return conv_tc(B, ld.co, ld.ci, d3, gz, L->wtc + L->tct[l], nullptr, 0, accumulate, gx, s);
+  }
+  if (ld.stride == 1) {
+    const int64_t nq = (int64_t)di.x * di.y * ((di.z + VZ - 1) / VZ);
+    dim3 grid(nblk((int64_t)B * nq, 128), (ld.ci + 15) / 16);
+    k_conv_bwd_data_rb<16><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, gz, L->wb + L->woff[l], gx, accumulate);
+  } else {
+    dim3 grid(nblk((int64_t)B * di.n(), 128), (ld.ci + 15) / 16);
+    k_conv_bwd_data<16><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, dout, ld.stride, gz, L->wb + L->woff[l], gx, accumulate);
+  }
+  CUCHK(cudaGetLastError());
+  return 0;
+}
+
 dErr conv_bwd(_p_dLearned *L, int l, int B, const float *x, const float *gz, float *gx, int accumulate, cudaStream_t s) {
   const LayerDef &ld = kLayer[l];
-  const Dims di = L->d[ld.level_in], dout = ld.stride == 2 ? L->d[ld.level_in + 1] : di;
+  const Dims di = L->cur[ld.level_in], dout = ld.stride == 2 ? L->cur[ld.level_in + 1] : di;
   const int64_t total = (int64_t)B * dout.x * dout.y * ((dout.z + VZ - 1) / VZ);
   const int nch = (int)((total + kQuadChunk - 1) / kQuadChunk);
   const int64_t np = (int64_t)ld.co * ld.ci * 27 + ld.co;
@@ -780,29 +886,18 @@ dErr conv_bwd(_p_dLearned *L, int l, int B, const float *x, const float *gz, flo
   }
   k_sum_chunks<<<nblk(np), 256, 0, s>>>(np, nch, L->partial, L->g + L->woff[l]);
   CUCHK(cudaGetLastError());
-  if (gx) {
-    if (ld.stride == 1) {
-      const int64_t nq = (int64_t)di.x * di.y * ((di.z + VZ - 1) / VZ);
-      dim3 grid(nblk((int64_t)B * nq, 128), (ld.ci + 15) / 16);
-      k_conv_bwd_data_rb<16><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, gz, L->wb + L->woff[l], gx, accumulate);
-    } else {
-      dim3 grid(nblk((int64_t)B * di.n(), 128), (ld.ci + 15) / 16);
-      k_conv_bwd_data<16><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, dout, ld.stride, gz, L->wb + L->woff[l], gx, accumulate);
-    }
-    CUCHK(cudaGetLastError());
-  }
-  return 0;
+  return gx ? conv_data(L, l, B, gz, gx, accumulate, s) : 0;
 }
 
 dErr up_fwd(_p_dLearned *L, int B, int C, int lc, const float *in, const float *skip, float *out, cudaStream_t s) {
-  const Dims dc = L->d[lc], df = L->d[lc - 1];
+  const Dims dc = L->cur[lc], df = L->cur[lc - 1];
   k_up_fwd<<<nblk((int64_t)B * C * df.n()), 256, 0, s>>>(B * C, dc, df, in, skip, out);
   CUCHK(cudaGetLastError());
   return 0;
 }
 
 dErr up_bwd(_p_dLearned *L, int B, int C, int lc, const float *gf, float *gc, cudaStream_t s) {
-  const Dims dc = L->d[lc], df = L->d[lc - 1];
+  const Dims dc = L->cur[lc], df = L->cur[lc - 1];
   k_up_bwd<<<nblk((int64_t)B * C * dc.n()), 256, 0, s>>>(B * C, dc, df, gf, gc);
   CUCHK(cudaGetLastError());
   return 0;
@@ -831,13 +926,13 @@ dErr forward(_p_dLearned *L, int B, cudaStream_t s) {
   DCHK(up_fwd(L, B, 16, 1, a[W1], a[A1], a[S1], s));  // s1 = up(w1) + a1
   DCHK(conv_fwd(L, C1C, B, a[S1], a[B1], 1, s));
   DCHK(conv_fwd(L, OUT, B, a[B1], a[Y], 0, s));
-  return 0;
+  return tc_first_check(L, s);
 }
 
 // backward from dL/dy in G1 [B][1][n0]; parameter gradients into L->g
 dErr backward(_p_dLearned *L, int B, cudaStream_t s) {
   float **a = L->act;
-  const int64_t n0 = L->d[0].n(), n1 = L->d[1].n(), n2 = L->d[2].n();
+  const int64_t n0 = L->cur[0].n(), n1 = L->cur[1].n(), n2 = L->cur[2].n();
   float *G1 = L->G1, *G2 = L->G2, *GZ = L->GZ;
   DCHK(conv_bwd(L, OUT, B, a[B1], G1, G2, 0, s));  // dL/db1
   DCHK(mask((int64_t)B * 16 * n0, G2, a[B1], GZ, s));
@@ -871,9 +966,9 @@ dErr backward(_p_dLearned *L, int B, cudaStream_t s) {
 
 // loss of act[Y] against L->tb; gradient into G1
 dErr loss(_p_dLearned *L, int B, double *out, cudaStream_t s) {
-  const int64_t n0 = L->d[0].n(), tot = (int64_t)B * n0;
+  const int64_t n0 = L->cur[0].n(), tot = (int64_t)B * n0;
   const unsigned nb = nblk(tot);
-  k_mse<<<nb, 256, 0, s>>>(B, n0, L->act[Y], L->tb, L->mask, (float)(1.0 / ((double)B * L->nint)), L->G1, L->lpart);
+  k_mse<<<nb, 256, 0, s>>>(B, n0, L->act[Y], L->tb, L->bmask, (float)(1.0 / ((double)B * L->lnorm)), L->G1, L->lpart);
   CUCHK(cudaGetLastError());
   if (out) {
     std::vector<double> h(nb);
@@ -881,7 +976,7 @@ dErr loss(_p_dLearned *L, int B, double *out, cudaStream_t s) {
     CUCHK(cudaStreamSynchronize(s));
     double t = 0;
     for (double v : h) t += v;
-    *out = t / ((double)B * L->nint);
+    *out = t / ((double)B * L->lnorm);
   }
   return 0;
 }
@@ -892,7 +987,7 @@ dErr adam_step(_p_dLearned *L, double lr, cudaStream_t s) {
   const float bc1 = 1.f - powf(b1, (float)L->adam_t), bc2 = 1.f - powf(b2, (float)L->adam_t);
   k_adam<<<nblk(L->nparam), 256, 0, s>>>(L->nparam, L->w, L->g, L->m, L->v, (float)lr, b1, b2, 1e-8f, bc1, bc2, L->wb);
   CUCHK(cudaGetLastError());
-  return 0;
+  return repack_tc(L, s);
 }
 
 // the correction z += P N(R r); called by FGMRES after the Chebyshev step
@@ -901,7 +996,8 @@ dErr apply_correction(void *ctx, const double *r, double *z) {
   _p_dFS *fs = L->fs;
   cudaStream_t s = fs->stream;
   const int64_t n0 = L->d[0].n();
-  DCHK(ensure_cap(L, 1));
+  L->cur = L->d;
+  DCHK(ensure_cap(L, 1, false));
   k_csr_mv<<<nblk(n0), 256, 0, s>>>(n0, L->Rp, L->Rc, L->Rv, r, L->rc);
   DCHK(device_dot(n0, L->rc, L->rc, L->dpart, L->ss, s));
   k_make_input<<<nblk(n0), 256, 0, s>>>(n0, L->rc, L->ss, (double)L->nint, L->mask, L->logk, L->act[X0], L->scale);
@@ -913,19 +1009,25 @@ dErr apply_correction(void *ctx, const double *r, double *z) {
   return 0;
 }
 
-// CG monitor during pair collection: every cevery-th iterate, R r_k (normalised) and x_k at the vertices
+// CG monitor during pair collection: every cevery-th iterate, R r_k (normalised over the whole lattice) and x_k on a
+// window of the lattice (the whole lattice when training on it), at a seeded origin that is a multiple of 4
 dErr collect_monitor(void *ctx, int it, const double *x, const double *r) {
   _p_dLearned *L = (_p_dLearned *)ctx;
   if (it % L->cevery || L->ccount >= L->cmax) return 0;
   cudaStream_t s = L->fs->stream;
-  const int64_t n0 = L->d[0].n();
+  const int64_t n0 = L->d[0].n(), nt = L->dt[0].n();
   const int p = L->cfirst + L->ccount;
+  int32_t o[3];
+  const int dd[3] = {L->d[0].x, L->d[0].y, L->d[0].z}, tt[3] = {L->dt[0].x, L->dt[0].y, L->dt[0].z};
+  for (int c = 0; c < 3; c++) o[c] = 4 * (int32_t)(L->wgen() % (uint64_t)((dd[c] - tt[c]) / 4 + 1));
+  const Win w{L->dt[0], L->d[0]};
   k_csr_mv<<<nblk(n0), 256, 0, s>>>(n0, L->Rp, L->Rc, L->Rv, r, L->rc);
   DCHK(device_dot(n0, L->rc, L->rc, L->dpart, L->ss, s));
-  k_make_input<<<nblk(n0), 256, 0, s>>>(n0, L->rc, L->ss, (double)L->nint, L->mask, nullptr, L->pin + (int64_t)p * n0,
-                                        L->cscale + L->ccount);
-  k_gather_vertices<<<nblk(n0), 256, 0, s>>>(n0, L->vdof, x, L->cxk + (int64_t)L->ccount * n0);
+  k_make_input<<<nblk(n0), 256, 0, s>>>(n0, L->rc, L->ss, (double)L->nint, L->mask, nullptr, L->cin, L->cscale + L->ccount);
+  k_crop_f<<<nblk(nt), 256, 0, s>>>(w, o[0], o[1], o[2], L->cin, L->pin + (int64_t)p * nt);
+  k_gather_crop<<<nblk(nt), 256, 0, s>>>(w, o[0], o[1], o[2], L->vdof, x, L->cxk + (int64_t)L->ccount * nt);
   CUCHK(cudaGetLastError());
+  L->h_porig.insert(L->h_porig.end(), o, o + 3);
   L->ccount++;
   return 0;
 }
@@ -935,72 +1037,118 @@ dErr collect_monitor(void *ctx, int it, const double *x, const double *r) {
 // ------------------------------------------------------------------------------------------ C ABI
 extern "C" {
 
-dErr dLearnedCreate(dFS fs, uint64_t seed, dLearned *out) {
+dErr dLearnedCreate(dFS fs, uint64_t seed, dLearned *out) { return dLearnedCreateOnGrid(fs, dLEARNED_GRID_VERTEX, 0, seed, out); }
+
+dErr dLearnedCreateOnGrid(dFS fs, dLearnedGrid grid, dInt crop, uint64_t seed, dLearned *out) {
   if (!fs || !out) return set_error("null argument");
   if (!fs->setup) return set_error("dFS not set up");
   if (!fs->uniform || fs->bs != 1) return set_error("learned correction needs a scalar uniform-order space");
+  if (grid != dLEARNED_GRID_VERTEX && grid != dLEARNED_GRID_GLL) return set_error("unknown lattice %d", (int)grid);
+  if (grid == dLEARNED_GRID_VERTEX && crop) return set_error("the vertex lattice is trained whole (crop 0)");
+  if (crop && (crop < 9 || crop % 4 != 1)) return set_error("training window %d: needs 4 m + 1 >= 9 nodes", crop);
   _p_dMesh *mesh = fs->mesh;
   const int p = fs->p, N = p + 1, N3 = N * N * N;
-  _p_dLearned *L = new _p_dLearned();
-  L->fs = fs;
-  L->d[0] = {mesh->nx, mesh->ny, mesh->nz};
-  L->d[1] = coarsen(L->d[0]);
-  L->d[2] = coarsen(L->d[1]);
-  if (std::min({L->d[2].x, L->d[2].y, L->d[2].z}) < 2) {
-    delete L;
-    return set_error("learned correction needs at least 4 elements per direction");
-  }
-  const Dims d0 = L->d[0];
-  const int64_t n0 = d0.n(), n = fs->n;
-  // lattice index of every mesh vertex from its position (interior vertices move by less than half a cell)
-  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-  for (int64_t i = 0; i < mesh->nv; i++)
-    for (int c = 0; c < 3; c++) lo[c] = std::min(lo[c], mesh->vx[3 * i + c]), hi[c] = std::max(hi[c], mesh->vx[3 * i + c]);
-  const int Ld[3] = {d0.x, d0.y, d0.z};
-  auto lat = [&](const double *X, int c) { return (int)std::lround((X[c] - lo[c]) / (hi[c] - lo[c]) * (Ld[c] - 1)); };
-  std::vector<double> coords((size_t)fs->nelem * 24), vxyz((size_t)n0 * 3, 0.0);
+  const int64_t n = fs->n;
+  std::vector<double> coords((size_t)fs->nelem * 24);
   CUCHK(cudaMemcpy(coords.data(), fs->d_coords, coords.size() * sizeof(double), cudaMemcpyDeviceToHost));
-  for (int64_t i = 0; i < mesh->nv; i++) {
-    const double *X = &mesh->vx[3 * i];
-    const int64_t li = ((int64_t)lat(X, 0) * d0.y + lat(X, 1)) * d0.z + lat(X, 2);
-    for (int c = 0; c < 3; c++) vxyz[3 * li + c] = X[c];
-  }
-  // P: every explicit dof from its first occurrence in the expanded ordering; trilinear weights of the
-  // element's corner vertices at the dof's GLL reference coordinates; Dirichlet vertices carry no value
   double gll[MAXP], wgll[MAXP];
   lobatto_rule(N, gll, wgll);
-  std::vector<int64_t> first(n, -1);
-  for (int64_t x = 0; x < fs->nexp; x++) {
-    const int32_t c = fs->emap[x];
-    if (c < n && first[c] < 0) first[c] = x;
-  }
-  std::vector<int32_t> vdof(n0, -1);
-  std::vector<int64_t> corner_lat((size_t)fs->nelem * 8);
-  for (int64_t e = 0; e < fs->nelem; e++)
-    for (int v = 0; v < 8; v++) {
-      const double *X = &coords[(size_t)e * 24 + 3 * v];
-      corner_lat[e * 8 + v] = ((int64_t)lat(X, 0) * d0.y + lat(X, 1)) * d0.z + lat(X, 2);
-      const int i = v >> 2, j = (v >> 1) & 1, k = v & 1;
-      const int32_t c = fs->emap[e * N3 + ((i * p) * N + j * p) * N + k * p];
-      if (c < n) vdof[corner_lat[e * 8 + v]] = c;
+  // the lattice: vdof (the explicit dof at each node, or -1), node coordinates, P (dofs x lattice) and R = P^T
+  Dims d0;
+  std::vector<int32_t> vdof, Pp, Pc;
+  std::vector<double> Pv, vxyz;
+  if (grid == dLEARNED_GRID_VERTEX) {
+    d0 = {mesh->nx, mesh->ny, mesh->nz};
+    if (std::min({d0.x, d0.y, d0.z}) < 5) return set_error("learned correction needs at least 4 elements per direction");
+    const int64_t n0 = d0.n();
+    // lattice index of every mesh vertex from its position (interior vertices move by less than half a cell)
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int64_t i = 0; i < mesh->nv; i++)
+      for (int c = 0; c < 3; c++) lo[c] = std::min(lo[c], mesh->vx[3 * i + c]), hi[c] = std::max(hi[c], mesh->vx[3 * i + c]);
+    const int Ld[3] = {d0.x, d0.y, d0.z};
+    auto lat = [&](const double *X, int c) { return (int)std::lround((X[c] - lo[c]) / (hi[c] - lo[c]) * (Ld[c] - 1)); };
+    vxyz.assign((size_t)n0 * 3, 0.0);
+    for (int64_t i = 0; i < mesh->nv; i++) {
+      const double *X = &mesh->vx[3 * i];
+      const int64_t li = ((int64_t)lat(X, 0) * d0.y + lat(X, 1)) * d0.z + lat(X, 2);
+      for (int c = 0; c < 3; c++) vxyz[3 * li + c] = X[c];
     }
-  std::vector<int32_t> Pp(n + 1, 0), Pc;
-  std::vector<double> Pv;
-  Pc.reserve(n * 8), Pv.reserve(n * 8);
-  for (int64_t d = 0; d < n; d++) {
-    const int64_t x = first[d], e = x / N3;
-    const int loc = (int)(x - e * N3), a = loc / (N * N), b = (loc / N) % N, c = loc % N;
-    std::vector<std::pair<int64_t, double>> row;
-    for (int v = 0; v < 8; v++) {
-      const int i = v >> 2, j = (v >> 1) & 1, k = v & 1;
-      const double w = (i ? 1 + gll[a] : 1 - gll[a]) * (j ? 1 + gll[b] : 1 - gll[b]) * (k ? 1 + gll[c] : 1 - gll[c]) / 8;
-      const int64_t lt = corner_lat[e * 8 + v];
-      if (w != 0 && vdof[lt] >= 0) row.push_back({lt, w});
+    // P: every explicit dof from its first occurrence in the expanded ordering; trilinear weights of the
+    // element's corner vertices at the dof's GLL reference coordinates; Dirichlet vertices carry no value
+    std::vector<int64_t> first(n, -1);
+    for (int64_t x = 0; x < fs->nexp; x++) {
+      const int32_t c = fs->emap[x];
+      if (c < n && first[c] < 0) first[c] = x;
     }
-    std::sort(row.begin(), row.end());
-    for (auto &q : row) Pc.push_back((int32_t)q.first), Pv.push_back(q.second);
-    Pp[d + 1] = (int32_t)Pc.size();
+    vdof.assign(n0, -1);
+    std::vector<int64_t> corner_lat((size_t)fs->nelem * 8);
+    for (int64_t e = 0; e < fs->nelem; e++)
+      for (int v = 0; v < 8; v++) {
+        const double *X = &coords[(size_t)e * 24 + 3 * v];
+        corner_lat[e * 8 + v] = ((int64_t)lat(X, 0) * d0.y + lat(X, 1)) * d0.z + lat(X, 2);
+        const int i = v >> 2, j = (v >> 1) & 1, k = v & 1;
+        const int32_t c = fs->emap[e * N3 + ((i * p) * N + j * p) * N + k * p];
+        if (c < n) vdof[corner_lat[e * 8 + v]] = c;
+      }
+    Pp.assign(n + 1, 0);
+    Pc.reserve(n * 8), Pv.reserve(n * 8);
+    for (int64_t d = 0; d < n; d++) {
+      const int64_t x = first[d], e = x / N3;
+      const int loc = (int)(x - e * N3), a = loc / (N * N), b = (loc / N) % N, c = loc % N;
+      std::vector<std::pair<int64_t, double>> row;
+      for (int v = 0; v < 8; v++) {
+        const int i = v >> 2, j = (v >> 1) & 1, k = v & 1;
+        const double w = (i ? 1 + gll[a] : 1 - gll[a]) * (j ? 1 + gll[b] : 1 - gll[b]) * (k ? 1 + gll[c] : 1 - gll[c]) / 8;
+        const int64_t lt = corner_lat[e * 8 + v];
+        if (w != 0 && vdof[lt] >= 0) row.push_back({lt, w});
+      }
+      std::sort(row.begin(), row.end());
+      for (auto &q : row) Pc.push_back((int32_t)q.first), Pv.push_back(q.second);
+      Pp[d + 1] = (int32_t)Pc.size();
+    }
+  } else {
+    // the GLL nodes of the space (the lattice of the Q1-embedded matrix); P and R the injection of the explicit dofs
+    std::vector<int32_t> lat;
+    int L0[3];
+    DCHK(fs_gll_lattice(fs, lat, L0));
+    d0 = {L0[0], L0[1], L0[2]};
+    if (std::min({d0.x, d0.y, d0.z}) < 9) return set_error("learned correction needs at least 9 GLL nodes per direction");
+    const int64_t n0 = d0.n();
+    vdof.assign(n0, -1);
+    Pp.resize(n + 1), Pc.resize(n), Pv.assign(n, 1.0);
+    for (int64_t d = 0; d < n; d++) vdof[lat[d]] = (int32_t)d, Pp[d] = (int32_t)d, Pc[d] = lat[d];
+    Pp[n] = (int32_t)n;
+    // node coordinates from each element's trilinear map at the GLL reference points
+    vxyz.assign((size_t)n0 * 3, 0.0);
+    const int My = mesh->ny - 1, Mz = mesh->nz - 1;
+    for (int64_t e = 0; e < fs->nelem; e++) {
+      const int ex = (int)(e / ((int64_t)My * Mz)), ey = (int)((e / Mz) % My), ez = (int)(e % Mz);
+      for (int a = 0; a < N; a++)
+        for (int b = 0; b < N; b++)
+          for (int c = 0; c < N; c++) {
+            const int64_t li = (((int64_t)ex * p + a) * d0.y + ey * p + b) * d0.z + ez * p + c;
+            double X[3] = {0, 0, 0};
+            for (int v = 0; v < 8; v++) {
+              const int i = v >> 2, j = (v >> 1) & 1, k = v & 1;
+              const double w = (i ? 1 + gll[a] : 1 - gll[a]) * (j ? 1 + gll[b] : 1 - gll[b]) * (k ? 1 + gll[c] : 1 - gll[c]) / 8;
+              for (int q = 0; q < 3; q++) X[q] += w * coords[(size_t)e * 24 + 3 * v + q];
+            }
+            for (int q = 0; q < 3; q++) vxyz[3 * li + q] = X[q];
+          }
+    }
   }
+  _p_dLearned *L = new _p_dLearned();
+  L->fs = fs;
+  L->grid = grid;
+  L->d[0] = d0;
+  L->d[1] = coarsen(L->d[0]);
+  L->d[2] = coarsen(L->d[1]);
+  L->dt[0] = crop ? Dims{std::min(crop, d0.x), std::min(crop, d0.y), std::min(crop, d0.z)} : d0;
+  L->dt[1] = coarsen(L->dt[0]);
+  L->dt[2] = coarsen(L->dt[1]);
+  L->cur = L->d;
+  L->wgen.seed(seed ^ 0x9E3779B97F4A7C15ull);
+  const int64_t n0 = d0.n();
   // R = P^T with ascending dof order per lattice row
   std::vector<int32_t> Rp(n0 + 1, 0), Rc(Pc.size());
   std::vector<double> Rv(Pc.size());
@@ -1016,20 +1164,22 @@ dErr dLearnedCreate(dFS fs, uint64_t seed, dLearned *out) {
   }
   std::vector<uint8_t> msk(n0);
   for (int64_t i = 0; i < n0; i++) msk[i] = vdof[i] >= 0, L->nint += msk[i];
+  L->lnorm = crop ? (double)L->dt[0].n() : (double)L->nint;
   auto up = [](auto **dst, const auto &src) -> dErr {
     CUCHK(cudaMalloc(dst, std::max<size_t>(src.size(), 1) * sizeof(src[0])));
     if (src.size()) CUCHK(cudaMemcpy(*dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice));
     return 0;
   };
-  DCHK(up(&L->Pp, Pp));
-  DCHK(up(&L->Pc, Pc));
-  DCHK(up(&L->Pv, Pv));
-  DCHK(up(&L->Rp, Rp));
-  DCHK(up(&L->Rc, Rc));
-  DCHK(up(&L->Rv, Rv));
-  DCHK(up(&L->vdof, vdof));
-  DCHK(up(&L->mask, msk));
-  DCHK(up(&L->vxyz, vxyz));
+  dErr err = 0;
+  auto fail = [&](dErr e) {
+    _p_dLearned *q = L;
+    dLearnedDestroy(&q);
+    return e;
+  };
+  if ((err = up(&L->Pp, Pp)) || (err = up(&L->Pc, Pc)) || (err = up(&L->Pv, Pv)) || (err = up(&L->Rp, Rp)) ||
+      (err = up(&L->Rc, Rc)) || (err = up(&L->Rv, Rv)) || (err = up(&L->vdof, vdof)) || (err = up(&L->mask, msk)) ||
+      (err = up(&L->vxyz, vxyz)))
+    return fail(err);
   CUCHK(cudaMalloc(&L->logk, n0 * sizeof(float)));
   CUCHK(cudaMemset(L->logk, 0, n0 * sizeof(float)));
   CUCHK(cudaMalloc(&L->rc, n0 * sizeof(double)));
@@ -1054,7 +1204,7 @@ dErr dLearnedCreate(dFS fs, uint64_t seed, dLearned *out) {
     std::uniform_real_distribution<double> U(-bound, bound);
     for (int64_t i = L->woff[l]; i < L->boff[l]; i++) w[i] = (float)U(gen);
   }
-  DCHK(up(&L->w, w));
+  if ((err = up(&L->w, w))) return fail(err);
   for (float **q : {&L->g, &L->m, &L->v}) {
     CUCHK(cudaMalloc(q, off * sizeof(float)));
     CUCHK(cudaMemset(*q, 0, off * sizeof(float)));
@@ -1062,6 +1212,16 @@ dErr dLearnedCreate(dFS fs, uint64_t seed, dLearned *out) {
   CUCHK(cudaMalloc(&L->wb, off * sizeof(__nv_bfloat16)));
   k_to_bf16<<<nblk(off), 256>>>(off, L->w, L->wb);
   CUCHK(cudaGetLastError());
+  int64_t toff = 0;
+  for (int l = 0; l < NLAYER; l++) {
+    const bool tc = kLayer[l].stride == 1 && conv_tc_supported(kLayer[l].ci, kLayer[l].co);
+    L->tcf[l] = tc ? toff : -1;
+    toff += tc ? 27LL * kLayer[l].ci * kLayer[l].co : 0;
+    L->tct[l] = tc ? toff : -1;
+    toff += tc ? 27LL * kLayer[l].ci * kLayer[l].co : 0;
+  }
+  CUCHK(cudaMalloc(&L->wtc, std::max<int64_t>(toff, 1) * sizeof(__nv_bfloat16)));
+  if ((err = repack_tc(L, 0))) return fail(err);
   CUCHK(cudaDeviceSynchronize());
   *out = L;
   return 0;
@@ -1076,7 +1236,7 @@ dErr dLearnedDestroy(dLearned *net) {
                   (void *)L->wb, (void *)L->G1, (void *)L->G2, (void *)L->GZ, (void *)L->ga1, (void *)L->ga2, (void *)L->tb,
                   (void *)L->partial, (void *)L->lpart, (void *)L->rc, (void *)L->ss, (void *)L->scale, (void *)L->dpart,
                   (void *)L->bad, (void *)L->pin, (void *)L->ptg, (void *)L->flogk, (void *)L->pfield, (void *)L->cxk,
-                  (void *)L->cscale, (void *)L->cxstar})
+                  (void *)L->cscale, (void *)L->cxstar, (void *)L->bmask, (void *)L->porig, (void *)L->cin, (void *)L->wtc})
     cudaFree(p);
   delete L;
   *net = nullptr;
@@ -1118,6 +1278,7 @@ dErr dLearnedSetWeights(dLearned L, const float *w_host, dReal ysc) {
   CUCHK(cudaMemcpy(L->w, w_host, L->nparam * sizeof(float), cudaMemcpyHostToDevice));
   k_to_bf16<<<nblk(L->nparam), 256>>>(L->nparam, L->w, L->wb);
   CUCHK(cudaGetLastError());
+  DCHK(repack_tc(L, 0));
   CUCHK(cudaDeviceSynchronize());
   if (ysc > 0) L->ysc = ysc, L->trained = true;
   return 0;
@@ -1127,7 +1288,8 @@ dErr dLearnedSetWeights(dLearned L, const float *w_host, dReal ysc) {
 dErr dLearnedForward(dLearned L, dInt B, const float *in, float *out) {
   if (!L || !in || !out || B < 1) return set_error("bad argument");
   cudaStream_t s = L->fs->stream;
-  DCHK(ensure_cap(L, B));
+  L->cur = L->d;
+  DCHK(ensure_cap(L, B, false));
   const int64_t n0 = L->d[0].n();
   CUCHK(cudaMemcpyAsync(L->act[X0], in, (size_t)B * 2 * n0 * sizeof(float), cudaMemcpyDeviceToDevice, s));
   DCHK(forward(L, B, s));
@@ -1140,10 +1302,13 @@ dErr dLearnedForward(dLearned L, dInt B, const float *in, float *out) {
 dErr dLearnedLossGrad(dLearned L, dInt B, const float *in, const float *target, dReal *lossv, float *grad) {
   if (!L || !in || !target || B < 1) return set_error("bad argument");
   cudaStream_t s = L->fs->stream;
-  DCHK(ensure_cap(L, B));
+  L->cur = L->d;
+  DCHK(ensure_cap(L, B, true));
   const int64_t n0 = L->d[0].n();
   CUCHK(cudaMemcpyAsync(L->act[X0], in, (size_t)B * 2 * n0 * sizeof(float), cudaMemcpyDeviceToDevice, s));
   CUCHK(cudaMemcpyAsync(L->tb, target, (size_t)B * n0 * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  k_bmask<<<nblk((int64_t)B * n0), 256, 0, s>>>(B, n0, L->mask, L->bmask);
+  CUCHK(cudaGetLastError());
   DCHK(forward(L, B, s));
   double lv = 0;
   DCHK(loss(L, B, &lv, s));
@@ -1163,21 +1328,22 @@ dErr dLearnedCollectPairs(dLearned L, dKSP ksp, const dScalar *b, dReal rtol, dI
   if (every < 1 || max_pairs < 1) return set_error("every and max_pairs must be positive");
   _p_dFS *fs = L->fs;
   cudaStream_t s = fs->stream;
-  const int64_t n0 = L->d[0].n();
-  // grow the pair store and the field store
+  const int64_t n0 = L->d[0].n(), nt = L->dt[0].n();
+  // grow the pair store (pairs on their windows, nt values each) and the field store (whole lattice)
   const int newmax = L->npairs + max_pairs;
   if (newmax > L->maxpairs) {
     float *pin, *ptg;
-    int32_t *pf;
-    CUCHK(cudaMalloc(&pin, (size_t)newmax * n0 * sizeof(float)));
-    CUCHK(cudaMalloc(&ptg, (size_t)newmax * n0 * sizeof(float)));
+    int32_t *pf, *po;
+    CUCHK(cudaMalloc(&pin, (size_t)newmax * nt * sizeof(float)));
+    CUCHK(cudaMalloc(&ptg, (size_t)newmax * nt * sizeof(float)));
     CUCHK(cudaMalloc(&pf, (size_t)newmax * sizeof(int32_t)));
+    CUCHK(cudaMalloc(&po, (size_t)newmax * 3 * sizeof(int32_t)));
     if (L->npairs) {
-      CUCHK(cudaMemcpy(pin, L->pin, (size_t)L->npairs * n0 * sizeof(float), cudaMemcpyDeviceToDevice));
-      CUCHK(cudaMemcpy(ptg, L->ptg, (size_t)L->npairs * n0 * sizeof(float), cudaMemcpyDeviceToDevice));
+      CUCHK(cudaMemcpy(pin, L->pin, (size_t)L->npairs * nt * sizeof(float), cudaMemcpyDeviceToDevice));
+      CUCHK(cudaMemcpy(ptg, L->ptg, (size_t)L->npairs * nt * sizeof(float), cudaMemcpyDeviceToDevice));
     }
-    cudaFree(L->pin), cudaFree(L->ptg), cudaFree(L->pfield);
-    L->pin = pin, L->ptg = ptg, L->pfield = pf, L->maxpairs = newmax;
+    cudaFree(L->pin), cudaFree(L->ptg), cudaFree(L->pfield), cudaFree(L->porig);
+    L->pin = pin, L->ptg = ptg, L->pfield = pf, L->porig = po, L->maxpairs = newmax;
   }
   if (L->nfields + 1 > L->maxfields) {
     const int nm = std::max(8, 2 * L->maxfields);
@@ -1188,10 +1354,12 @@ dErr dLearnedCollectPairs(dLearned L, dKSP ksp, const dScalar *b, dReal rtol, dI
     L->flogk = fl, L->maxfields = nm;
   }
   CUCHK(cudaMemcpy(L->flogk + (int64_t)L->nfields * n0, L->logk, n0 * sizeof(float), cudaMemcpyDeviceToDevice));
-  CUCHK(cudaMalloc(&L->cxk, (size_t)max_pairs * n0 * sizeof(double)));
+  CUCHK(cudaMalloc(&L->cxk, (size_t)max_pairs * nt * sizeof(double)));
   CUCHK(cudaMalloc(&L->cscale, (size_t)max_pairs * sizeof(double)));
   CUCHK(cudaMalloc(&L->cxstar, (size_t)n0 * sizeof(double)));
+  CUCHK(cudaMalloc(&L->cin, (size_t)n0 * sizeof(float)));
   L->cfirst = L->npairs, L->ccount = 0, L->cevery = every, L->cmax = max_pairs;
+  L->h_porig.resize((size_t)L->npairs * 3);
   double *x;
   CUCHK(cudaMalloc(&x, std::max<int64_t>(fs->n, 1) * sizeof(double)));
   CUCHK(cudaMemsetAsync(x, 0, fs->n * sizeof(double), s));
@@ -1220,19 +1388,25 @@ dErr dLearnedCollectPairs(dLearned L, dKSP ksp, const dScalar *b, dReal rtol, dI
   if (!err) {
     const int np = L->ccount;
     k_gather_vertices<<<nblk(n0), 256, 0, s>>>(n0, L->vdof, x, L->cxstar);
-    if (np) k_targets<<<nblk((int64_t)np * n0), 256, 0, s>>>(n0, np, L->cxstar, L->cxk, L->cscale, L->ptg + (int64_t)L->cfirst * n0);
     L->h_pfield.resize(L->cfirst + np, L->nfields);
-    if (L->cfirst + np)
+    if (L->cfirst + np) {
       CUCHK(cudaMemcpyAsync(L->pfield, L->h_pfield.data(), (L->cfirst + np) * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+      CUCHK(cudaMemcpyAsync(L->porig, L->h_porig.data(), (size_t)(L->cfirst + np) * 3 * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    }
+    if (np)
+      k_targets<<<nblk((int64_t)np * nt), 256, 0, s>>>(Win{L->dt[0], L->d[0]}, np, L->porig + 3 * L->cfirst, L->cxstar, L->cxk,
+                                                       L->cscale, L->ptg + (int64_t)L->cfirst * nt);
     CUCHK(cudaStreamSynchronize(s));
     CUCHK(cudaGetLastError());
     L->npairs += np;
     L->nfields++;
     if (collected) *collected = np;
   }
+  if (err) L->h_porig.resize((size_t)L->npairs * 3);
   cudaFree(x);
-  cudaFree(L->cxk), cudaFree(L->cscale), cudaFree(L->cxstar);
+  cudaFree(L->cxk), cudaFree(L->cscale), cudaFree(L->cxstar), cudaFree(L->cin);
   L->cxk = L->cscale = L->cxstar = nullptr;
+  L->cin = nullptr;
   return err;
 }
 
@@ -1243,19 +1417,20 @@ dErr dLearnedTrain(dLearned L, dInt epochs, dInt batch, dReal lr, uint64_t seed,
   if (epochs < 1 || batch < 1) return set_error("epochs and batch must be positive");
   _p_dFS *fs = L->fs;
   cudaStream_t s = fs->stream;
-  const int64_t n0 = L->d[0].n();
+  const int64_t nt = L->dt[0].n();
   const int B = std::min<int>(batch, L->npairs);
-  DCHK(ensure_cap(L, B));
-  // target scale: RMS of all targets over interior vertices (fixed once, kept with the network)
+  L->cur = L->dt;
+  DCHK(ensure_cap(L, B, true));
+  // target scale: RMS of all targets over the nodes the loss averages over (fixed once, kept with the network)
   if (!L->trained) {
-    k_masked_sumsq<<<1024, 256, 0, s>>>((int64_t)L->npairs * n0, n0, L->ptg, L->mask, L->dpart);
+    k_sumsq<<<1024, 256, 0, s>>>((int64_t)L->npairs * nt, L->ptg, L->dpart);
     CUCHK(cudaGetLastError());
     std::vector<double> h(1024);
     CUCHK(cudaMemcpyAsync(h.data(), L->dpart, 1024 * sizeof(double), cudaMemcpyDeviceToHost, s));
     CUCHK(cudaStreamSynchronize(s));
     double ss = 0;
     for (double v : h) ss += v;
-    L->ysc = std::sqrt(ss / ((double)L->npairs * L->nint));
+    L->ysc = std::sqrt(ss / ((double)L->npairs * L->lnorm));
     if (!(L->ysc > 0)) L->ysc = 1;
   }
   int32_t *didx;
@@ -1270,8 +1445,8 @@ dErr dLearnedTrain(dLearned L, dInt epochs, dInt batch, dReal lr, uint64_t seed,
     int nb = 0;
     for (int i0 = 0; i0 + B <= L->npairs && !err; i0 += B, nb++) {
       CUCHK(cudaMemcpyAsync(didx, perm.data() + i0, B * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-      k_batch<<<nblk((int64_t)B * n0), 256, 0, s>>>(B, n0, didx, L->pfield, L->pin, L->ptg, L->flogk, (float)(1.0 / L->ysc),
-                                                    L->act[X0], L->tb);
+      k_batch<<<nblk((int64_t)B * nt), 256, 0, s>>>(B, Win{L->dt[0], L->d[0]}, didx, L->pfield, L->porig, L->pin, L->ptg, L->flogk,
+                                                    L->mask, (float)(1.0 / L->ysc), L->act[X0], L->tb, L->bmask);
       CUCHK(cudaGetLastError());
       DCHK(forward(L, B, s));
       double lv = 0;
@@ -1284,6 +1459,7 @@ dErr dLearnedTrain(dLearned L, dInt epochs, dInt batch, dReal lr, uint64_t seed,
   }
   CUCHK(cudaStreamSynchronize(s));
   cudaFree(didx);
+  if (!err && L->use_tc) err = conv_tc_check(s);
   L->trained = true;
   return err;
 }
@@ -1323,6 +1499,44 @@ dErr dKSPSetLearnedCorrection(dKSP ksp, dLearned L) {
   if (!ksp) return set_error("null KSP");
   if (L && !L->trained) return set_error("the network has not been trained or loaded");
   return L ? ksp_set_correction(ksp, apply_correction, L) : ksp_set_correction(ksp, nullptr, nullptr);
+}
+
+// one convolution layer on device FP32 arrays: transpose 0: out = act(conv(in) + bias) (ReLU on every layer but the
+// last), in [B][ci][dims] -> out [B][co][dims, halved for stride 2]; transpose 1: its data gradient, in [B][co][...]
+// -> out [B][ci][dims]
+dErr dLearnedLayerApply(dLearned L, dInt layer, dInt transpose, dInt B, const dInt dims[3], const float *in, float *out) {
+  if (!L || !dims || !in || !out || B < 1) return set_error("bad argument");
+  if (layer < 0 || layer >= NLAYER) return set_error("layer %d of %d", layer, NLAYER);
+  const LayerDef &ld = kLayer[layer];
+  Dims tmp[3] = {};
+  tmp[ld.level_in] = {dims[0], dims[1], dims[2]};
+  if (ld.level_in < 2) tmp[ld.level_in + 1] = coarsen(tmp[ld.level_in]);
+  cudaStream_t s = L->fs->stream;
+  L->cur = tmp;
+  dErr e = transpose ? conv_data(L, layer, B, in, out, 0, s) : conv_fwd(L, layer, B, in, out, layer != OUT, s);
+  L->cur = L->d;
+  DCHK(e);
+  CUCHK(cudaStreamSynchronize(s));
+  return conv_tc_check(s);
+}
+
+dErr dLearnedSetTensorCores(dLearned L, int on) {
+  if (!L) return set_error("null network");
+  L->use_tc = on != 0;
+  L->tc_checked = false;
+  return 0;
+}
+
+dErr dLearnedGetPair(dLearned L, dInt p, dInt window[3], dInt origin[3], float *input, float *target) {
+  if (!L) return set_error("null network");
+  if (p < 0 || p >= L->npairs) return set_error("pair %d of %d", p, L->npairs);
+  const int64_t nt = L->dt[0].n();
+  if (window) window[0] = L->dt[0].x, window[1] = L->dt[0].y, window[2] = L->dt[0].z;
+  if (origin)
+    for (int c = 0; c < 3; c++) origin[c] = L->h_porig[(size_t)p * 3 + c];
+  if (input) CUCHK(cudaMemcpy(input, L->pin + (int64_t)p * nt, nt * sizeof(float), cudaMemcpyDeviceToHost));
+  if (target) CUCHK(cudaMemcpy(target, L->ptg + (int64_t)p * nt, nt * sizeof(float), cudaMemcpyDeviceToHost));
+  return 0;
 }
 
 dErr dLearnedGetStats(dLearned L, int64_t *applies, int64_t *dropped_values) {

@@ -428,8 +428,15 @@ dErr dKSPGetStats(dKSP ksp, int64_t *pc_applies, int64_t *correction_rejects, in
  * meshes with at least 4 elements per direction. */
 typedef struct _p_dLearned *dLearned;
 dErr dLearnedCreate(dFS fs, uint64_t seed, dLearned *net);
+/* the lattice the network runs on: the mesh vertices (R = P^T with P trilinear, as dLearnedCreate), or the GLL
+ * nodes of the space, the lattice of the Q1-embedded matrix ((M p + 1) per direction; R and P the injection of the
+ * explicit dofs). On the GLL lattice the network is trained on crop^3 windows of the recorded pairs (crop = 4 m + 1
+ * >= 9, windows at origins that are multiples of 4, so that its coarse levels line up with those of the whole
+ * lattice; 0: the whole lattice) and applied to the whole lattice. */
+typedef enum { dLEARNED_GRID_VERTEX = 0, dLEARNED_GRID_GLL = 1 } dLearnedGrid;
+dErr dLearnedCreateOnGrid(dFS fs, dLearnedGrid grid, dInt crop, uint64_t seed, dLearned *net);
 dErr dLearnedDestroy(dLearned *net);
-/* vertex lattice dims, parameter count, collected pairs */
+/* lattice dims (vertices or GLL nodes), parameter count, collected pairs */
 dErr dLearnedGetSizes(dLearned net, dInt dims[3], int64_t *nparam, int64_t *npairs);
 /* coefficient field of the next pairs / corrections: log k at the vertices from dGRFCreate data (NULL: k = 1) */
 dErr dLearnedSetField(dLearned net, const dReal *grf);
@@ -448,9 +455,16 @@ dErr dKSPSetLearnedCorrection(dKSP ksp, dLearned net);
  * each restart cycle (the true residual, the kind of input the network was trained on), 2 = adaptive
  * (default): one cycle with each, then the one whose cycle reduced the residual more */
 dErr dKSPSetCorrectionPolicy(dKSP ksp, int policy);
+/* the stride-1 convolutions of 16 / 32 channels (and their data gradients) on the tcgen05 tensor cores, with the
+ * activations rounded to BF16 at their input (on = 1, the default), or every convolution on the CUDA cores in FP32 */
+dErr dLearnedSetTensorCores(dLearned net, int on);
 /* raw network (device FP32 arrays): in [B][2][lattice] -> out [B][1][lattice]; loss and parameter gradient */
 dErr dLearnedForward(dLearned net, dInt B, const float *in, float *out);
 dErr dLearnedLossGrad(dLearned net, dInt B, const float *in, const float *target, dReal *loss, float *grad);
+/* one convolution layer (0..11 in the order C1A C1B D1 C2A D2 C3A C3B U2 C2B U1 C1C OUT) on device FP32 arrays:
+ * transpose 0: out [B][co][dims'] = act(conv(in [B][ci][dims]) + bias) (dims' = dims, or halved for the stride-2
+ * layers; ReLU on every layer but OUT); transpose 1: its data gradient, in [B][co][dims'] -> out [B][ci][dims] */
+dErr dLearnedLayerApply(dLearned net, dInt layer, dInt transpose, dInt B, const dInt dims[3], const float *in, float *out);
 /* parameters (host FP32 [nparam], layer by layer: W[co][ci][27] then bias[co]); target scale */
 dErr dLearnedGetWeights(dLearned net, float *w);
 dErr dLearnedSetWeights(dLearned net, const float *w, dReal target_scale);
@@ -458,6 +472,9 @@ dErr dLearnedGetScale(dLearned net, dReal *target_scale);
 /* transfer operators on their own: rc = R r (lattice), z = P c (global) */
 dErr dLearnedRestrict(dLearned net, const dScalar *r, dScalar *rc);
 dErr dLearnedProlong(dLearned net, const dScalar *c, dScalar *z);
+/* recorded pair p on its window: window dims, its origin on the lattice, and (host FP32 arrays of the window's size,
+ * either may be NULL) the input channel R r_k / rms and the target (x* - x_k) / rms */
+dErr dLearnedGetPair(dLearned net, dInt p, dInt window[3], dInt origin[3], float *input, float *target);
 /* corrections applied and non-finite values dropped */
 dErr dLearnedGetStats(dLearned net, int64_t *applies, int64_t *dropped_values);
 

@@ -92,36 +92,52 @@ def relu(a):
     return np.maximum(a, 0.0)
 
 
-def forward(w, x, dims):
-    """w flat float64 (already bf16-rounded weights), x [B][2][dims] -> (y [B][1][dims], activations)"""
+# the layers the product runs on the tensor cores when they are enabled (stride 1, 16 or 32 channels in and out):
+# their input activations (forward) and incoming gradients (data gradient) are rounded to bf16
+TC_LAYERS = {name for name, ci, co, s, _ in LAYERS if s == 1 and ci in (16, 32) and co in (16, 32)}
+
+
+def _rnd(a, name, tc):
+    return bf16_round(a).astype(np.float64) if tc and name in TC_LAYERS else a
+
+
+def forward(w, x, dims, tc=False):
+    """w flat float64 (already bf16-rounded weights), x [B][2][dims] -> (y [B][1][dims], activations); tc: the
+    inputs of the tensor-core layers rounded to bf16"""
     P = unpack(np.asarray(w, np.float64))
     d0 = tuple(dims)
     d1 = coarsen(d0)
     d2 = coarsen(d1)
     A = {"X0": np.asarray(x, np.float64)}
-    A["H1"] = relu(conv(A["X0"], *P["C1A"], 1, d0))
-    A["A1"] = relu(conv(A["H1"], *P["C1B"], 1, d0))
-    A["H2"] = relu(conv(A["A1"], *P["D1"], 2, d1))
-    A["A2"] = relu(conv(A["H2"], *P["C2A"], 1, d1))
-    A["H3"] = relu(conv(A["A2"], *P["D2"], 2, d2))
-    A["H3B"] = relu(conv(A["H3"], *P["C3A"], 1, d2))
-    A["A3"] = relu(conv(A["H3B"], *P["C3B"], 1, d2))
-    A["W2"] = relu(conv(A["A3"], *P["U2"], 1, d2))
+
+    def cv(name, a, s, d):
+        return conv(_rnd(a, name, tc), *P[name], s, d)
+
+    A["H1"] = relu(cv("C1A", A["X0"], 1, d0))
+    A["A1"] = relu(cv("C1B", A["H1"], 1, d0))
+    A["H2"] = relu(cv("D1", A["A1"], 2, d1))
+    A["A2"] = relu(cv("C2A", A["H2"], 1, d1))
+    A["H3"] = relu(cv("D2", A["A2"], 2, d2))
+    A["H3B"] = relu(cv("C3A", A["H3"], 1, d2))
+    A["A3"] = relu(cv("C3B", A["H3B"], 1, d2))
+    A["W2"] = relu(cv("U2", A["A3"], 1, d2))
     A["S2"] = up(A["W2"], d1) + A["A2"]
-    A["B2"] = relu(conv(A["S2"], *P["C2B"], 1, d1))
-    A["W1"] = relu(conv(A["B2"], *P["U1"], 1, d1))
+    A["B2"] = relu(cv("C2B", A["S2"], 1, d1))
+    A["W1"] = relu(cv("U1", A["B2"], 1, d1))
     A["S1"] = up(A["W1"], d0) + A["A1"]
-    A["B1"] = relu(conv(A["S1"], *P["C1C"], 1, d0))
-    A["Y"] = conv(A["B1"], *P["OUT"], 1, d0)
+    A["B1"] = relu(cv("C1C", A["S1"], 1, d0))
+    A["Y"] = cv("OUT", A["B1"], 1, d0)
     return A["Y"], A
 
 
-def loss_grad(w, x, t, mask):
-    """MSE over interior vertices (mask [dims] bool) and its gradient w.r.t. the flat parameters"""
+def loss_grad(w, x, t, mask, tc=False):
+    """MSE over interior vertices (mask [dims] bool) and its gradient w.r.t. the flat parameters; tc: the
+    tensor-core layers' forward inputs and data-gradient inputs rounded to bf16 (their weight gradients use the
+    unrounded activations, as the product's CUDA-core weight-gradient kernel does)"""
     dims = x.shape[2:]
     B = x.shape[0]
     nint = int(mask.sum())
-    y, A = forward(w, x, dims)
+    y, A = forward(w, x, dims, tc)
     m = mask[None, None].astype(np.float64)
     d = (y - t) * m
     loss = float((d ** 2).sum() / (B * nint))
@@ -130,6 +146,8 @@ def loss_grad(w, x, t, mask):
 
     def step(name, xin, g, s):
         gx, gW, gb = conv_bwd(xin, P[name][0], g, s)
+        if tc and name in TC_LAYERS:
+            gx = conv_bwd(xin, P[name][0], _rnd(g, name, tc), s)[0]
         G[name] = (gW, gb)
         return gx
 

@@ -40,36 +40,77 @@ def interior(dims):
     return m
 
 
-def test_forward_matches_oracle():
+@pytest.mark.parametrize("tc", [False, True])
+def test_every_layer_and_its_data_gradient_match_oracle(tc):
+    """each convolution layer alone on a lattice with partial tiles (13 x 18 x 21), forward and data gradient, against
+    the oracle's float64 convolution; on the tensor cores the oracle's operand is the same FP32 input rounded to bf16,
+    so the only difference left is the FP32 accumulation"""
+    fs = dg.FS((7, 6, 7), degree=2, seed=1)
+    net = dg.Learned(fs, seed=11)
+    net.set_tensor_cores(tc)
+    P = uo.unpack(rounded(net.get_weights()))
+    rng = np.random.default_rng(4)
+    dims = (13, 18, 21)
+    for l, (name, ci, co, s, _) in enumerate(uo.LAYERS):
+        dout = uo.coarsen(dims) if s == 2 else dims
+        on_tc = tc and name in uo.TC_LAYERS
+        x = rng.standard_normal((2, ci) + dims).astype(np.float32)
+        y = torch.zeros((2, co) + dout, dtype=torch.float32, device="cuda")
+        net.layer(l, dev(x), y, dims)
+        xin = uo.bf16_round(x).astype(np.float64) if on_tc else x.astype(np.float64)
+        ref = uo.conv(xin, *P[name], s, dout)
+        if name != "OUT":
+            ref = uo.relu(ref)
+        assert np.linalg.norm(y.cpu().numpy() - ref) <= 1e-5 * np.linalg.norm(ref), name
+        gy = rng.standard_normal((2, co) + dout).astype(np.float32)
+        gx = torch.zeros((2, ci) + dims, dtype=torch.float32, device="cuda")
+        net.layer(l, dev(gy), gx, dims, transpose=True)
+        gin = uo.bf16_round(gy).astype(np.float64) if on_tc else gy.astype(np.float64)
+        gref = uo.conv_bwd(np.zeros((2, ci) + dims), P[name][0], gin, s)[0]
+        assert np.linalg.norm(gx.cpu().numpy() - gref) <= 1e-5 * np.linalg.norm(gref), name
+
+
+# tc: the stride-1 16/32-channel convolutions on the tensor cores (BF16 activations at their inputs), checked
+# against the oracle with the same roundings; otherwise every convolution on the CUDA cores in FP32
+@pytest.mark.parametrize("tc", [False, True])
+def test_forward_matches_oracle(tc):
     fs = dg.FS((7, 6, 7), degree=2, seed=1)
     net = dg.Learned(fs, seed=3)
+    net.set_tensor_cores(tc)
     assert net.dims == (7, 6, 7) and net.nparam == uo.nparams()
     w = net.get_weights()
     x = np.random.default_rng(0).standard_normal((2, 2) + net.dims).astype(np.float32)
     y = torch.zeros((2, 1) + net.dims, dtype=torch.float32, device="cuda")
     net.forward(dev(x), y)
-    yo, _ = uo.forward(rounded(w), x.astype(np.float64), net.dims)
+    yo, _ = uo.forward(rounded(w), x.astype(np.float64), net.dims, tc=tc)
     yg = y.cpu().numpy()
-    assert np.linalg.norm(yg - yo) / np.linalg.norm(yo) < 2e-5
+    # with BF16 activations one rounding that falls the other way (FP32 against the oracle's float64 value) moves the
+    # output by up to ~2e-3 relative, so the whole network is held to that; every layer is checked exactly above
+    assert np.linalg.norm(yg - yo) / np.linalg.norm(yo) < (5e-3 if tc else 2e-5)
+    if tc:  # against the unrounded network: the size of the BF16 activation rounding
+        y32, _ = uo.forward(rounded(w), x.astype(np.float64), net.dims)
+        assert np.linalg.norm(yg - y32) / np.linalg.norm(y32) < 2e-2
 
 
-def test_loss_and_gradient_match_oracle():
+@pytest.mark.parametrize("tc", [False, True])
+def test_loss_and_gradient_match_oracle(tc):
     fs = dg.FS((7, 7, 6), degree=2, seed=2)
     net = dg.Learned(fs, seed=5)
+    net.set_tensor_cores(tc)
     rng = np.random.default_rng(1)
     x = rng.standard_normal((3, 2) + net.dims).astype(np.float32)
     t = rng.standard_normal((3, 1) + net.dims).astype(np.float32)
     g = torch.zeros(net.nparam, dtype=torch.float32, device="cuda")
     lv = net.loss_grad(dev(x), dev(t), g)
-    lo, go, _ = uo.loss_grad(rounded(net.get_weights()), x.astype(np.float64), t.astype(np.float64), interior(net.dims))
-    assert abs(lv - lo) / lo < 1e-5
+    lo, go, _ = uo.loss_grad(rounded(net.get_weights()), x.astype(np.float64), t.astype(np.float64), interior(net.dims), tc=tc)
+    assert abs(lv - lo) / lo < (5e-3 if tc else 1e-5)
     gg = g.cpu().numpy()
-    assert np.linalg.norm(gg - go) / np.linalg.norm(go) < 1e-4
+    assert np.linalg.norm(gg - go) / np.linalg.norm(go) < (2e-2 if tc else 1e-4)
     # every layer's block of the gradient, not just the norm
     o = 0
     for name, ci, co, _, _ in uo.LAYERS:
         n = co * ci * 27 + co
-        assert np.linalg.norm(gg[o:o + n] - go[o:o + n]) <= 1e-3 * np.linalg.norm(go[o:o + n]) + 1e-12, name
+        assert np.linalg.norm(gg[o:o + n] - go[o:o + n]) <= (5e-2 if tc else 1e-3) * np.linalg.norm(go[o:o + n]) + 1e-12, name
         o += n
 
 
