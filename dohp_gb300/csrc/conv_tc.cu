@@ -86,24 +86,35 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3_tc(ConvArgs A) {
     const int tx = (int)(r % A.ntx);
     const int b = (int)(r / A.ntx);
     const int x0 = tx * TX, y0 = ty * TY, z0 = tz * TZ;
-    // stage the halo: plane q holds channels 8q..8q+7 of every halo voxel as 8 BF16 values (zero outside the lattice)
+    // stage the halo: plane q holds channels 8q..8q+7 of every halo voxel as 8 BF16 values (zero outside the lattice);
+    // each thread loads four items (32 independent loads) before it converts and stores them
     const float *xb = A.x + (int64_t)b * CI * nv;
-    for (int it = tid; it < CI / 8 * kHalo; it += kThreads) {
-      const int q = it / kHalo, h = it - q * kHalo;
-      const int hx = h / (HY * HZ), hy = (h / HZ) % HY, hz = h % HZ;
-      const int gx = x0 + hx - 1, gy = y0 + hy - 1, gz = z0 + hz - 1;
-      uint4 pk = make_uint4(0, 0, 0, 0);
-      if (gx >= 0 && gx < A.dx && gy >= 0 && gy < A.dy && gz >= 0 && gz < A.dz) {
-        const float *src = xb + (int64_t)q * 8 * nv + ((int64_t)gx * A.dy + gy) * A.dz + gz;
-        float v[8];
+    constexpr int kItems = CI / 8 * kHalo, kU = 4;
+    for (int it0 = tid; it0 < kItems; it0 += kU * kThreads) {
+      float v[kU][8];
+      bool in[kU];
 #pragma unroll
-        for (int c = 0; c < 8; c++) v[c] = src[(int64_t)c * nv];
-        __nv_bfloat162 p0 = __floats2bfloat162_rn(v[0], v[1]), p1 = __floats2bfloat162_rn(v[2], v[3]);
-        __nv_bfloat162 p2 = __floats2bfloat162_rn(v[4], v[5]), p3 = __floats2bfloat162_rn(v[6], v[7]);
-        pk = make_uint4(*reinterpret_cast<uint32_t *>(&p0), *reinterpret_cast<uint32_t *>(&p1), *reinterpret_cast<uint32_t *>(&p2),
-                        *reinterpret_cast<uint32_t *>(&p3));
+      for (int u = 0; u < kU; u++) {
+        const int it = it0 + u * kThreads;
+        const int q = it / kHalo, h = it - q * kHalo;
+        const int hx = h / (HY * HZ), hy = (h / HZ) % HY, hz = h % HZ;
+        const int gx = x0 + hx - 1, gy = y0 + hy - 1, gz = z0 + hz - 1;
+        in[u] = it < kItems && gx >= 0 && gx < A.dx && gy >= 0 && gy < A.dy && gz >= 0 && gz < A.dz;
+        const float *src = xb + (int64_t)q * 8 * nv + ((int64_t)gx * A.dy + gy) * A.dz + gz;
+#pragma unroll
+        for (int c = 0; c < 8; c++) v[u][c] = in[u] ? src[(int64_t)c * nv] : 0.f;
       }
-      *reinterpret_cast<uint4 *>(asm_ + q * kPlane + h * 16) = pk;
+#pragma unroll
+      for (int u = 0; u < kU; u++) {
+        const int it = it0 + u * kThreads;
+        if (it >= kItems) break;
+        const int q = it / kHalo, h = it - q * kHalo;
+        __nv_bfloat162 p0 = __floats2bfloat162_rn(v[u][0], v[u][1]), p1 = __floats2bfloat162_rn(v[u][2], v[u][3]);
+        __nv_bfloat162 p2 = __floats2bfloat162_rn(v[u][4], v[u][5]), p3 = __floats2bfloat162_rn(v[u][6], v[u][7]);
+        *reinterpret_cast<uint4 *>(asm_ + q * kPlane + h * 16) =
+            make_uint4(*reinterpret_cast<uint32_t *>(&p0), *reinterpret_cast<uint32_t *>(&p1), *reinterpret_cast<uint32_t *>(&p2),
+                       *reinterpret_cast<uint32_t *>(&p3));
+      }
     }
     async_proxy_fence();
     tc_fence_before();

@@ -431,12 +431,12 @@ __global__ void k_sum_chunks(int64_t np, int nchunk, const float *__restrict__ p
   grad[p] = s;
 }
 
-// trilinear interpolation between vertex-centred grids (align corners): weight of coarse i at fine f
+// trilinear interpolation between vertex-centred grids (align corners): fine point f sits at coarse position
+// f (Lc - 1) / (Lf - 1), kept as the exact fraction num / den in integers (no FP64 on the way)
 __device__ __forceinline__ float tent(int f, int Lf, int i, int Lc) {
   if (Lc == 1) return 1.f;
-  const double pos = (double)f * (Lc - 1) / (Lf - 1);
-  const double w = 1.0 - fabs(pos - i);
-  return w > 0 ? (float)w : 0.f;
+  const int den = Lf - 1, d = abs(f * (Lc - 1) - i * den);
+  return d < den ? (float)(den - d) / (float)den : 0.f;
 }
 
 __device__ __forceinline__ void lohi(int f, int Lf, int Lc, int &lo, float &fr) {
@@ -444,76 +444,82 @@ __device__ __forceinline__ void lohi(int f, int Lf, int Lc, int &lo, float &fr) 
     lo = 0, fr = 0.f;
     return;
   }
-  const double pos = (double)f * (Lc - 1) / (Lf - 1);
-  lo = min((int)floor(pos), Lc - 2);
-  fr = (float)(pos - lo);
+  const int num = f * (Lc - 1), den = Lf - 1;
+  lo = min(num / den, Lc - 2);
+  fr = (float)(num - lo * den) / (float)den;
 }
 
-// out[B][C][df] = interp(in[B][C][dc]); add: out += skip
-__global__ void k_up_fwd(int BC, Dims dc, Dims df, const float *__restrict__ in, const float *__restrict__ skip, float *__restrict__ out) {
-  const int64_t nf = df.n(), t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= (int64_t)BC * nf) return;
-  const int64_t bc = t / nf, r = t % nf;
+// out[B][C][df] = interp(in[B][C][dc]); add: out += skip. One thread per fine voxel (z fastest across threads): the
+// eight coarse neighbours and weights once, then every channel
+__global__ void k_up_fwd(int B, int C, Dims dc, Dims df, const float *__restrict__ in, const float *__restrict__ skip,
+                         float *__restrict__ out) {
+  const int64_t nf = df.n(), nc = dc.n(), t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)B * nf) return;
+  const int64_t b = t / nf, r = t % nf;
   int fx, fy, fz, lx, ly, lz;
   float ax, ay, az;
   vox(r, df, fx, fy, fz);
   lohi(fx, df.x, dc.x, lx, ax);
   lohi(fy, df.y, dc.y, ly, ay);
   lohi(fz, df.z, dc.z, lz, az);
-  const float *c = in + bc * dc.n();
-  float s = 0.f;
-  for (int a = 0; a < 2; a++) {
-    const float wa = a ? ax : 1.f - ax;
-    const int ix = min(lx + a, dc.x - 1);
-    for (int b = 0; b < 2; b++) {
-      const float wb = b ? ay : 1.f - ay;
-      const int iy = min(ly + b, dc.y - 1);
-      for (int cc = 0; cc < 2; cc++) {
-        const float wc = cc ? az : 1.f - az;
-        const int iz = min(lz + cc, dc.z - 1);
-        s += wa * wb * wc * c[((int64_t)ix * dc.y + iy) * dc.z + iz];
-      }
-    }
+  int64_t idx[8];
+  float w[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const int a = k >> 2, bb = (k >> 1) & 1, cc = k & 1;
+    const int ix = min(lx + a, dc.x - 1), iy = min(ly + bb, dc.y - 1), iz = min(lz + cc, dc.z - 1);
+    idx[k] = ((int64_t)ix * dc.y + iy) * dc.z + iz;
+    w[k] = (a ? ax : 1.f - ax) * (bb ? ay : 1.f - ay) * (cc ? az : 1.f - az);
   }
-  out[t] = skip ? s + skip[t] : s;
+  for (int c = 0; c < C; c++) {
+    const float *cp = in + (b * C + c) * nc;
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) s += w[k] * cp[idx[k]];
+    const int64_t o = (b * C + c) * nf + r;
+    out[o] = skip ? s + skip[o] : s;
+  }
 }
 
-// adjoint of the interpolation, as a gather over the fine points in each coarse point's support
-__global__ void k_up_bwd(int BC, Dims dc, Dims df, const float *__restrict__ gf, float *__restrict__ gc) {
-  const int64_t nc = dc.n(), t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= (int64_t)BC * nc) return;
-  const int64_t bc = t / nc, r = t % nc;
+// adjoint of the interpolation, as a gather over the fine points in each coarse point's support (at most 2 r + 1 per
+// direction, r = (Lf - 1) / (Lc - 1) <= 3 for the halving lattices here); one thread per coarse voxel, the weights once,
+// then every channel in the same summation order
+__global__ void k_up_bwd(int B, int C, Dims dc, Dims df, const float *__restrict__ gf, float *__restrict__ gc) {
+  const int64_t nc = dc.n(), nf = df.n(), t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)B * nc) return;
+  const int64_t b = t / nc, r = t % nc;
   int cx, cy, cz;
   vox(r, dc, cx, cy, cz);
-  auto range = [](int i, int Lc, int Lf, int &f0, int &f1) {
+  constexpr int MS = 8;
+  auto support = [](int i, int Lc, int Lf, int &f0, float *w) {  // fine points within one coarse spacing of i
+    int f1;
     if (Lc == 1) {
       f0 = 0, f1 = Lf - 1;
-      return;
+    } else {
+      f0 = i > 0 ? (i - 1) * (Lf - 1) / (Lc - 1) : 0;
+      f1 = min(Lf - 1, ((i + 1) * (Lf - 1) + Lc - 2) / (Lc - 1));
     }
-    const double rr = (double)(Lf - 1) / (Lc - 1);
-    f0 = max(0, (int)floor((i - 1) * rr));
-    f1 = min(Lf - 1, (int)ceil((i + 1) * rr));
+    const int n = min(f1 - f0 + 1, MS);
+    for (int k = 0; k < MS; k++) w[k] = k < n ? tent(f0 + k, Lf, i, Lc) : 0.f;
+    return n;
   };
-  int x0, x1, y0, y1, z0, z1;
-  range(cx, dc.x, df.x, x0, x1);
-  range(cy, dc.y, df.y, y0, y1);
-  range(cz, dc.z, df.z, z0, z1);
-  const float *g = gf + bc * df.n();
-  float s = 0.f;
-  for (int fx = x0; fx <= x1; fx++) {
-    const float wx = tent(fx, df.x, cx, dc.x);
-    if (wx == 0.f) continue;
-    for (int fy = y0; fy <= y1; fy++) {
-      const float wy = tent(fy, df.y, cy, dc.y);
-      if (wy == 0.f) continue;
-      for (int fz = z0; fz <= z1; fz++) {
-        const float wz = tent(fz, df.z, cz, dc.z);
-        if (wz == 0.f) continue;
-        s += wx * wy * wz * g[((int64_t)fx * df.y + fy) * df.z + fz];
+  int x0, y0, z0;
+  float wx[MS], wy[MS], wz[MS];
+  const int nx = support(cx, dc.x, df.x, x0, wx), ny = support(cy, dc.y, df.y, y0, wy), nz = support(cz, dc.z, df.z, z0, wz);
+  for (int c = 0; c < C; c++) {
+    const float *g = gf + (b * C + c) * nf;
+    float s = 0.f;
+    for (int i = 0; i < nx; i++) {
+      if (wx[i] == 0.f) continue;
+      for (int j = 0; j < ny; j++) {
+        if (wy[j] == 0.f) continue;
+        const float *gr = g + ((int64_t)(x0 + i) * df.y + y0 + j) * df.z + z0;
+        for (int k = 0; k < nz; k++)
+          if (wz[k] != 0.f) s += wx[i] * wy[j] * wz[k] * gr[k];
       }
     }
+    gc[(b * C + c) * nc + r] = s;
   }
-  gc[t] = s;
 }
 
 __global__ void k_mask(int64_t n, const float *__restrict__ g, const float *__restrict__ act, float *__restrict__ out) {
@@ -840,6 +846,10 @@ dErr conv_fwd(_p_dLearned *L, int l, int B, const float *x, float *y, int relu, 
     dim3 grid(nblk((int64_t)B * nq, 128), (ld.co + 15) / 16);
     if (ld.stride == 1) k_conv_fwd_rb<16, 1><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, dout, x, W, bias, relu, y);
     else k_conv_fwd_rb<16, 2><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, dout, x, W, bias, relu, y);
+  } else if (ld.stride == 1) {  // the one-channel output layer: register-blocked along z as the others
+    const int64_t nq = (int64_t)dout.x * dout.y * ((dout.z + VZ - 1) / VZ);
+    dim3 grid(nblk((int64_t)B * nq, 128), ld.co);
+    k_conv_fwd_rb<1, 1><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, dout, x, W, bias, relu, y);
   } else {
     dim3 grid(nblk((int64_t)B * dout.n(), 128), ld.co);
     k_conv_fwd<1><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, dout, ld.stride, x, W, bias, relu, y);
@@ -891,14 +901,14 @@ dErr conv_bwd(_p_dLearned *L, int l, int B, const float *x, const float *gz, flo
 
 dErr up_fwd(_p_dLearned *L, int B, int C, int lc, const float *in, const float *skip, float *out, cudaStream_t s) {
   const Dims dc = L->cur[lc], df = L->cur[lc - 1];
-  k_up_fwd<<<nblk((int64_t)B * C * df.n()), 256, 0, s>>>(B * C, dc, df, in, skip, out);
+  k_up_fwd<<<nblk((int64_t)B * df.n()), 256, 0, s>>>(B, C, dc, df, in, skip, out);
   CUCHK(cudaGetLastError());
   return 0;
 }
 
 dErr up_bwd(_p_dLearned *L, int B, int C, int lc, const float *gf, float *gc, cudaStream_t s) {
   const Dims dc = L->cur[lc], df = L->cur[lc - 1];
-  k_up_bwd<<<nblk((int64_t)B * C * dc.n()), 256, 0, s>>>(B * C, dc, df, gf, gc);
+  k_up_bwd<<<nblk((int64_t)B * dc.n()), 256, 0, s>>>(B, C, dc, df, gf, gc);
   CUCHK(cudaGetLastError());
   return 0;
 }
