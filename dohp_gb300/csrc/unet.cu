@@ -136,70 +136,6 @@ __global__ void __launch_bounds__(128) k_conv_fwd(int B, int Ci, int Co, Dims di
   }
 }
 
-// gx (=, or += with accumulate) = conv^T(gy): gx[ci][u] = sum_{co, taps with s v + t - 1 = u} W[co][ci][t] gy[co][v]
-template <int CI_T>
-__global__ void __launch_bounds__(128) k_conv_bwd_data(int B, int Ci, int Co, Dims di, Dims dout, int stride,
-                                                       const float *__restrict__ gy, const __nv_bfloat16 *__restrict__ W,
-                                                       float *__restrict__ gx, int accumulate) {
-  constexpr int CK = 8;
-  __shared__ float sW[CK][CI_T][27];
-  const int64_t nvo = dout.n(), nvi = di.n();
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const bool active = t < (int64_t)B * nvi;
-  const int ci0 = blockIdx.y * CI_T;
-  const int64_t b = active ? t / nvi : 0, r = active ? t % nvi : 0;
-  int ix, iy, iz;
-  vox(r, di, ix, iy, iz);
-  float acc[CI_T];
-#pragma unroll
-  for (int c = 0; c < CI_T; c++) acc[c] = 0.f;
-  for (int co0 = 0; co0 < Co; co0 += CK) {
-    __syncthreads();
-    for (int i = threadIdx.x; i < CK * CI_T * 27; i += blockDim.x) {
-      const int k = i / (CI_T * 27), rr = i % (CI_T * 27), c = rr / 27, tap = rr % 27;
-      sW[k][c][tap] = (co0 + k < Co && ci0 + c < Ci) ? __bfloat162float(W[((size_t)(co0 + k) * Ci + ci0 + c) * 27 + tap]) : 0.f;
-    }
-    __syncthreads();
-    if (!active) continue;
-    const int kmax = min(CK, Co - co0);
-    for (int k = 0; k < kmax; k++) {
-      const float *gc = gy + ((size_t)b * Co + co0 + k) * nvo;
-#pragma unroll
-      for (int a = 0; a < 3; a++) {
-        const int nx = ix + 1 - a;
-        if (nx < 0 || nx % stride) continue;
-        const int vx = nx / stride;
-        if (vx >= dout.x) continue;
-#pragma unroll
-        for (int bb = 0; bb < 3; bb++) {
-          const int ny = iy + 1 - bb;
-          if (ny < 0 || ny % stride) continue;
-          const int vy = ny / stride;
-          if (vy >= dout.y) continue;
-#pragma unroll
-          for (int cc = 0; cc < 3; cc++) {
-            const int nz = iz + 1 - cc;
-            if (nz < 0 || nz % stride) continue;
-            const int vz = nz / stride;
-            if (vz >= dout.z) continue;
-            const float g = gc[((int64_t)vx * dout.y + vy) * dout.z + vz];
-            const int tap = (a * 3 + bb) * 3 + cc;
-#pragma unroll
-            for (int c = 0; c < CI_T; c++) acc[c] = fmaf(sW[k][c][tap], g, acc[c]);
-          }
-        }
-      }
-    }
-  }
-  if (!active) return;
-#pragma unroll
-  for (int c = 0; c < CI_T; c++) {
-    if (ci0 + c >= Ci) break;
-    float *o = gx + ((size_t)b * Ci + ci0 + c) * nvi + r;
-    *o = accumulate ? *o + acc[c] : acc[c];
-  }
-}
-
 // Register-blocked forms: a thread computes VZ consecutive outputs along z, so every weight read from
 // shared memory feeds VZ multiply-adds and the 3 x 3 x ZW input window is shared by the VZ outputs.
 constexpr int VZ = 4;
@@ -286,6 +222,71 @@ __global__ void __launch_bounds__(128) k_conv_fwd_rb(int B, int Ci, int Co, Dims
 #pragma unroll
     for (int v = 0; v < VZ; v++)
       if (oz0 + v < dout.z) yo[(size_t)(co0 + c) * nvo + v] = relu ? fmaxf(acc[c][v], 0.f) : acc[c][v];
+  }
+}
+
+// stride-2 data gradient, two z-outputs per thread (2m even, 2m + 1 odd) so that the z parity is the same across a
+// warp: the even output takes tap cc = 1 of gy[.., m]; the odd one cc = 0 of gy[.., m + 1], then cc = 2 of gy[.., m]
+// (taps in ascending order, as the adjoint of the forward convolution lists them)
+template <int CI_T>
+__global__ void __launch_bounds__(128) k_conv_bwd_data_s2(int B, int Ci, int Co, Dims di, Dims dout, const float *__restrict__ gy,
+                                                          const __nv_bfloat16 *__restrict__ W, float *__restrict__ gx, int accumulate) {
+  constexpr int CK = 8;
+  __shared__ float sW[CK][CI_T][27];
+  const int nzp = (di.z + 1) / 2;
+  const int64_t np = (int64_t)di.x * di.y * nzp, nvo = dout.n(), nvi = di.n();
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool active = t < (int64_t)B * np;
+  const int ci0 = blockIdx.y * CI_T;
+  const int64_t b = active ? t / np : 0, r = active ? t % np : 0;
+  const int m = (int)(r % nzp), iy = (int)((r / nzp) % di.y), ix = (int)(r / ((int64_t)nzp * di.y));
+  const bool odd_in = 2 * m + 1 < di.z, m1_in = m + 1 < dout.z;
+  float ae[CI_T], ao[CI_T];
+#pragma unroll
+  for (int c = 0; c < CI_T; c++) ae[c] = ao[c] = 0.f;
+  for (int co0 = 0; co0 < Co; co0 += CK) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < CK * CI_T * 27; i += blockDim.x) {
+      const int k = i / (CI_T * 27), rr = i % (CI_T * 27), c = rr / 27, tap = rr % 27;
+      sW[k][c][tap] = (co0 + k < Co && ci0 + c < Ci) ? __bfloat162float(W[((size_t)(co0 + k) * Ci + ci0 + c) * 27 + tap]) : 0.f;
+    }
+    __syncthreads();
+    if (!active) continue;
+    const int kmax = min(CK, Co - co0);
+    for (int k = 0; k < kmax; k++) {
+      const float *gc = gy + ((size_t)b * Co + co0 + k) * nvo;
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        const int nx = ix + 1 - a;
+        if (nx < 0 || (nx & 1)) continue;
+        const int vx = nx >> 1;
+        if (vx >= dout.x) continue;
+#pragma unroll
+        for (int bb = 0; bb < 3; bb++) {
+          const int ny = iy + 1 - bb;
+          if (ny < 0 || (ny & 1)) continue;
+          const int vy = ny >> 1;
+          if (vy >= dout.y) continue;
+          const float *gl = gc + ((int64_t)vx * dout.y + vy) * dout.z;
+          const float g0 = gl[m], g1 = m1_in ? gl[m + 1] : 0.f;
+          const int t0 = (a * 3 + bb) * 3;
+#pragma unroll
+          for (int c = 0; c < CI_T; c++) {
+            ae[c] = fmaf(sW[k][c][t0 + 1], g0, ae[c]);
+            if (m1_in) ao[c] = fmaf(sW[k][c][t0], g1, ao[c]);
+            ao[c] = fmaf(sW[k][c][t0 + 2], g0, ao[c]);
+          }
+        }
+      }
+    }
+  }
+  if (!active) return;
+#pragma unroll
+  for (int c = 0; c < CI_T; c++) {
+    if (ci0 + c >= Ci) break;
+    float *o = gx + ((size_t)b * Ci + ci0 + c) * nvi + ((int64_t)ix * di.y + iy) * di.z + 2 * m;
+    o[0] = accumulate ? o[0] + ae[c] : ae[c];
+    if (odd_in) o[1] = accumulate ? o[1] + ao[c] : ao[c];
   }
 }
 
@@ -871,8 +872,9 @@ dErr conv_data(_p_dLearned *L, int l, int B, const float *gz, float *gx, int acc
     dim3 grid(nblk((int64_t)B * nq, 128), (ld.ci + 15) / 16);
     k_conv_bwd_data_rb<16><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, gz, L->wb + L->woff[l], gx, accumulate);
   } else {
-    dim3 grid(nblk((int64_t)B * di.n(), 128), (ld.ci + 15) / 16);
-    k_conv_bwd_data<16><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, dout, ld.stride, gz, L->wb + L->woff[l], gx, accumulate);
+    const int64_t np = (int64_t)di.x * di.y * ((di.z + 1) / 2);
+    dim3 grid(nblk((int64_t)B * np, 128), (ld.ci + 15) / 16);
+    k_conv_bwd_data_s2<16><<<grid, 128, 0, s>>>(B, ld.ci, ld.co, di, dout, gz, L->wb + L->woff[l], gx, accumulate);
   }
   CUCHK(cudaGetLastError());
   return 0;
@@ -1150,6 +1152,7 @@ dErr dLearnedCreateOnGrid(dFS fs, dLearnedGrid grid, dInt crop, uint64_t seed, d
   _p_dLearned *L = new _p_dLearned();
   L->fs = fs;
   L->grid = grid;
+  L->use_tc = grid == dLEARNED_GRID_GLL;  // the whole-lattice forward at (M p + 1)^3 nodes is where the tensor cores pay
   L->d[0] = d0;
   L->d[1] = coarsen(L->d[0]);
   L->d[2] = coarsen(L->d[1]);

@@ -456,7 +456,8 @@ dErr dKSPSetLearnedCorrection(dKSP ksp, dLearned net);
  * (default): one cycle with each, then the one whose cycle reduced the residual more */
 dErr dKSPSetCorrectionPolicy(dKSP ksp, int policy);
 /* the stride-1 convolutions of 16 / 32 channels (and their data gradients) on the tcgen05 tensor cores, with the
- * activations rounded to BF16 at their input (on = 1, the default), or every convolution on the CUDA cores in FP32 */
+ * activations rounded to BF16 at their input (on = 1; the default on the GLL lattice), or every convolution on the
+ * CUDA cores in FP32 (on = 0; the default on the vertex lattice) */
 dErr dLearnedSetTensorCores(dLearned net, int on);
 /* raw network (device FP32 arrays): in [B][2][lattice] -> out [B][1][lattice]; loss and parameter gradient */
 dErr dLearnedForward(dLearned net, dInt B, const float *in, float *out);
