@@ -631,6 +631,11 @@ class Learned:
         d = np.asarray(dims, np.int32)
         chk(lib().dLearnedLayerApply(self.h, _i32(layer), _i32(int(transpose)), _i32(x.shape[0]), ptr(d), ptr(x), ptr(y)))
 
+    def layer_weight_grad(self, layer, x, gy, grad, dims):
+        """one layer's weight and bias gradient (device FP32 arrays)"""
+        d = np.asarray(dims, np.int32)
+        chk(lib().dLearnedLayerWeightGrad(self.h, _i32(layer), _i32(x.shape[0]), ptr(d), ptr(x), ptr(gy), ptr(grad)))
+
     def set_tensor_cores(self, on=True):
         chk(lib().dLearnedSetTensorCores(self.h, ctypes.c_int(int(on))))
 

@@ -14,9 +14,9 @@
 // Training pairs (residual, error) come from the plain solver: a CG monitor records R r_k and x_k on the lattice
 // (or its window); once the solve has converged, the targets are x* - x_k there. Training is plain minibatch Adam on
 // the mean squared error over interior nodes, with hand-written forward and backward kernels: the stride-1
-// convolutions of 16 / 32 channels and their data gradients on the tcgen05 tensor cores (conv_tc.cu, BF16 operands,
-// FP32 accumulation), the other convolutions and every weight gradient as direct FP32 convolutions on the CUDA
-// cores (deterministic two-stage weight-gradient sums), activations FP32 in memory.
+// convolutions of 16 / 32 channels with their data and weight gradients on the tcgen05 tensor cores (conv_tc.cu,
+// BF16 operands, FP32 accumulation; dLearnedSetTensorCores), the other convolutions as direct FP32 convolutions on
+// the CUDA cores; weight gradients summed in a fixed order (deterministic); activations FP32 in memory.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -39,6 +39,8 @@ dErr conv_tc_pack(int ci, int co, bool transpose, const __nv_bfloat16 *W, __nv_b
 dErr conv_tc(int B, int ci, int co, const int d[3], const float *x, const __nv_bfloat16 *wpack, const float *bias, int relu,
              int accumulate, float *y, cudaStream_t s);
 dErr conv_tc_check(cudaStream_t s);
+dErr conv_tc_wgrad(int B, int ci, int co, const int d[3], const float *x, const float *gy, float *partial, int64_t max_chunks,
+                   int *nchunks, cudaStream_t s);
 
 namespace {
 
@@ -884,10 +886,13 @@ dErr conv_bwd(_p_dLearned *L, int l, int B, const float *x, const float *gz, flo
   const LayerDef &ld = kLayer[l];
   const Dims di = L->cur[ld.level_in], dout = ld.stride == 2 ? L->cur[ld.level_in + 1] : di;
   const int64_t total = (int64_t)B * dout.x * dout.y * ((dout.z + VZ - 1) / VZ);
-  const int nch = (int)((total + kQuadChunk - 1) / kQuadChunk);
+  int nch = (int)((total + kQuadChunk - 1) / kQuadChunk);
   const int64_t np = (int64_t)ld.co * ld.ci * 27 + ld.co;
   if ((int64_t)nch * np > L->partial_len) return set_error("learned correction: gradient workspace too small");
-  if (ld.co % 2 == 0) {
+  if (layer_tc(L, l)) {  // per-CTA sums of the tensor-core weight gradient, then the same ordered sum over them
+    const int d3[3] = {di.x, di.y, di.z};
+    DCHK(conv_tc_wgrad(B, ld.ci, ld.co, d3, x, gz, L->partial, L->partial_len / np, &nch, s));
+  } else if (ld.co % 2 == 0) {
     const dim3 grid(ld.co / 2 * ld.ci, nch);
     if (ld.stride == 1) k_conv_bwd_weight_rb<2, 1><<<grid, 256, 0, s>>>(B, ld.ci, ld.co, di, dout, x, gz, L->partial);
     else k_conv_bwd_weight_rb<2, 2><<<grid, 256, 0, s>>>(B, ld.ci, ld.co, di, dout, x, gz, L->partial);
@@ -1529,6 +1534,27 @@ dErr dLearnedLayerApply(dLearned L, dInt layer, dInt transpose, dInt B, const dI
   dErr e = transpose ? conv_data(L, layer, B, in, out, 0, s) : conv_fwd(L, layer, B, in, out, layer != OUT, s);
   L->cur = L->d;
   DCHK(e);
+  CUCHK(cudaStreamSynchronize(s));
+  return conv_tc_check(s);
+}
+
+// the weight and bias gradient of one layer for input x [B][ci][dims] and output gradient gy [B][co][dims'], into
+// grad [co ci 27 + co] (device FP32)
+dErr dLearnedLayerWeightGrad(dLearned L, dInt layer, dInt B, const dInt dims[3], const float *x, const float *gy, float *grad) {
+  if (!L || !dims || !x || !gy || !grad || B < 1) return set_error("bad argument");
+  if (layer < 0 || layer >= NLAYER) return set_error("layer %d of %d", layer, NLAYER);
+  const LayerDef &ld = kLayer[layer];
+  Dims tmp[3] = {};
+  tmp[ld.level_in] = {dims[0], dims[1], dims[2]};
+  if (ld.level_in < 2) tmp[ld.level_in + 1] = coarsen(tmp[ld.level_in]);
+  cudaStream_t s = L->fs->stream;
+  L->cur = tmp;
+  dErr e = ensure_cap(L, B, true);
+  if (!e) e = conv_bwd(L, layer, B, x, gy, nullptr, 0, s);
+  L->cur = L->d;
+  DCHK(e);
+  const int64_t np = (int64_t)ld.co * ld.ci * 27 + ld.co;
+  CUCHK(cudaMemcpyAsync(grad, L->g + L->woff[layer], np * sizeof(float), cudaMemcpyDeviceToDevice, s));
   CUCHK(cudaStreamSynchronize(s));
   return conv_tc_check(s);
 }

@@ -455,8 +455,8 @@ dErr dKSPSetLearnedCorrection(dKSP ksp, dLearned net);
  * each restart cycle (the true residual, the kind of input the network was trained on), 2 = adaptive
  * (default): one cycle with each, then the one whose cycle reduced the residual more */
 dErr dKSPSetCorrectionPolicy(dKSP ksp, int policy);
-/* the stride-1 convolutions of 16 / 32 channels (and their data gradients) on the tcgen05 tensor cores, with the
- * activations rounded to BF16 at their input (on = 1; the default on the GLL lattice), or every convolution on the
+/* the stride-1 convolutions of 16 / 32 channels (and their data and weight gradients) on the tcgen05 tensor
+ * cores, with their operands rounded to BF16 (on = 1; the default on the GLL lattice), or every convolution on the
  * CUDA cores in FP32 (on = 0; the default on the vertex lattice) */
 dErr dLearnedSetTensorCores(dLearned net, int on);
 /* raw network (device FP32 arrays): in [B][2][lattice] -> out [B][1][lattice]; loss and parameter gradient */
@@ -466,6 +466,9 @@ dErr dLearnedLossGrad(dLearned net, dInt B, const float *in, const float *target
  * transpose 0: out [B][co][dims'] = act(conv(in [B][ci][dims]) + bias) (dims' = dims, or halved for the stride-2
  * layers; ReLU on every layer but OUT); transpose 1: its data gradient, in [B][co][dims'] -> out [B][ci][dims] */
 dErr dLearnedLayerApply(dLearned net, dInt layer, dInt transpose, dInt B, const dInt dims[3], const float *in, float *out);
+/* that layer's weight and bias gradient for input x [B][ci][dims] and output gradient gy [B][co][dims'] into grad
+ * [co ci 27 + co] (device FP32, W[co][ci][27] then bias[co]) */
+dErr dLearnedLayerWeightGrad(dLearned net, dInt layer, dInt B, const dInt dims[3], const float *x, const float *gy, float *grad);
 /* parameters (host FP32 [nparam], layer by layer: W[co][ci][27] then bias[co]); target scale */
 dErr dLearnedGetWeights(dLearned net, float *w);
 dErr dLearnedSetWeights(dLearned net, const float *w, dReal target_scale);

@@ -132,8 +132,8 @@ def forward(w, x, dims, tc=False):
 
 def loss_grad(w, x, t, mask, tc=False):
     """MSE over interior vertices (mask [dims] bool) and its gradient w.r.t. the flat parameters; tc: the
-    tensor-core layers' forward inputs and data-gradient inputs rounded to bf16 (their weight gradients use the
-    unrounded activations, as the product's CUDA-core weight-gradient kernel does)"""
+    tensor-core layers' forward inputs, and the activations and incoming gradients of their data and weight
+    gradients, rounded to bf16 (their bias gradients sum the unrounded incoming gradients)"""
     dims = x.shape[2:]
     B = x.shape[0]
     nint = int(mask.sum())
@@ -146,8 +146,8 @@ def loss_grad(w, x, t, mask, tc=False):
 
     def step(name, xin, g, s):
         gx, gW, gb = conv_bwd(xin, P[name][0], g, s)
-        if tc and name in TC_LAYERS:
-            gx = conv_bwd(xin, P[name][0], _rnd(g, name, tc), s)[0]
+        if tc and name in TC_LAYERS:  # data and weight gradients from bf16 operands; the bias gradient from g itself
+            gx, gW, _ = conv_bwd(_rnd(xin, name, tc), P[name][0], _rnd(g, name, tc), s)
         G[name] = (gW, gb)
         return gx
 

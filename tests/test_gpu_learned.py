@@ -68,6 +68,14 @@ def test_every_layer_and_its_data_gradient_match_oracle(tc):
         gin = uo.bf16_round(gy).astype(np.float64) if on_tc else gy.astype(np.float64)
         gref = uo.conv_bwd(np.zeros((2, ci) + dims), P[name][0], gin, s)[0]
         assert np.linalg.norm(gx.cpu().numpy() - gref) <= 1e-5 * np.linalg.norm(gref), name
+        # weight and bias gradient (on the tensor cores from bf16 x and gy, the bias from the FP32 gy)
+        gw = torch.zeros(co * ci * 27 + co, dtype=torch.float32, device="cuda")
+        net.layer_weight_grad(l, dev(x), dev(gy), gw, dims)
+        _, wref, bref = uo.conv_bwd(xin, P[name][0], gin, s)
+        _, _, bref = uo.conv_bwd(x.astype(np.float64), P[name][0], gy.astype(np.float64), s)
+        gw = gw.cpu().numpy()
+        assert np.linalg.norm(gw[:co * ci * 27] - wref.ravel()) <= 3e-5 * np.linalg.norm(wref), name
+        assert np.linalg.norm(gw[co * ci * 27:] - bref) <= 3e-5 * np.linalg.norm(bref), name
 
 
 # tc: the stride-1 16/32-channel convolutions on the tensor cores (BF16 activations at their inputs), checked
