@@ -136,11 +136,13 @@ __global__ void __launch_bounds__(RED_THREADS) k_dot1(int64_t n, const double *_
   dot_finish(acc, part, out);
 }
 
-// CG update fused with the residual norm: alpha = S[0] / S[1]; x += alpha p; r -= alpha q; out = r . r
-__global__ void __launch_bounds__(RED_THREADS) k_cg_update(int64_t n, const double *__restrict__ S, const double *__restrict__ p,
+// CG update fused with the residual norm: x += alpha p, r -= alpha q with alpha = rz / pq (S[4] / S[1]), out = r.r;
+// S[0] takes rz for the next step's ratio (no other block of this launch reads S[0])
+__global__ void __launch_bounds__(RED_THREADS) k_cg_update(int64_t n, double *S, const double *__restrict__ p,
                                                           const double *__restrict__ q, double *__restrict__ x, double *__restrict__ r,
                                                           double *part, double *out) {
-  const double alpha = S[0] / S[1];
+  const double alpha = S[4] / S[1];
+  if (blockIdx.x == 0 && threadIdx.x == 0) S[0] = S[4];
   double acc = 0;
   for (int64_t i = blockIdx.x * (int64_t)RED_THREADS + threadIdx.x; i < n; i += (int64_t)gridDim.x * RED_THREADS) {
     x[i] += alpha * p[i];
@@ -185,14 +187,6 @@ __global__ void k_cheb_first(int64_t n, const double *dinv, const double *r, dou
   z[i] = v;
 }
 
-__global__ void k_cheb_step(int64_t n, const double *dinv, const double *r, const double *w, double c1, double c2, double *d, double *z) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double v = c1 * d[i] + c2 * dinv[i] * (r[i] - w[i]);
-  d[i] = v;
-  z[i] += v;
-}
-
 template <typename A, typename B>
 __global__ void k_convert(int64_t n, const A *__restrict__ a, B *__restrict__ b) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -208,13 +202,21 @@ __global__ void k_cheb_first_t(int64_t n, const T *dinv, const T *r, T inv_theta
   z[i] = v;
 }
 
-template <typename T>
-__global__ void k_cheb_step_t(int64_t n, const T *dinv, const T *r, const T *w, T c1, T c2, T *d, T *z) {
+// one Chebyshev step with its matrix product fused: w_i = (A zin)_i (the sliced rows of k_sell, same order), then
+// d_i = c1 d_i + c2 dinv_i (r_i - w_i) and zout_i = zin_i + d_i, the same arithmetic as a product followed by an
+// elementwise step (zout must not alias zin: other rows still read zin)
+template <typename V, typename T>
+__global__ void k_sell_cheb(int64_t n, const int64_t *__restrict__ off, const int32_t *__restrict__ col, const V *__restrict__ val,
+                            const T *__restrict__ dinv, const T *__restrict__ r, const T *__restrict__ zin, T c1, T c2,
+                            T *__restrict__ d, T *__restrict__ zout) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const T v = c1 * d[i] + c2 * dinv[i] * (r[i] - w[i]);
+  const int64_t b = off[i >> 5] + (i & 31), w = (off[(i >> 5) + 1] - off[i >> 5]) >> 5;
+  T s = 0;
+  for (int64_t k = 0; k < w; k++) s += sell_val(val[b + 32 * k]) * zin[col[b + 32 * k]];
+  const T v = c1 * d[i] + c2 * dinv[i] * (r[i] - s);
   d[i] = v;
-  z[i] += v;
+  zout[i] = zin[i] + v;
 }
 
 // out[v] = <V_v, w> for v < nv (V row-major [nv][n]), fixed-order partials then a fixed-order tree
@@ -519,12 +521,19 @@ static dErr pc_apply_fp32(_p_dKSP *k, const double *r, double *z) {
   k_convert<double, float><<<nb(n), 256, 0, s>>>(n, r, r32);
   const double theta = 0.5 * (k->emax + k->emin), delta = 0.5 * (k->emax - k->emin), sigma = theta / delta;
   double rho = 1.0 / sigma;
-  k_cheb_first_t<float><<<nb(n), 256, 0, s>>>(n, k->d_dinv32, r32, (float)(1.0 / theta), d32, z32);
+  // the iterate alternates between z32 and w32 (each step reads one and writes the other) and ends in z32
+  float *zc = (k->cheb_degree - 1) % 2 == 0 ? z32 : w32;
+  k_cheb_first_t<float><<<nb(n), 256, 0, s>>>(n, k->d_dinv32, r32, (float)(1.0 / theta), d32, zc);
   for (int it = 1; it < k->cheb_degree; it++) {
-    if (bf) k_sell<__nv_bfloat16, float><<<nb(n), 256, 0, s>>>(n, J->d_sell_off, J->d_sell_col, k->d_val16, z32, w32);
-    else k_sell<float, float><<<nb(n), 256, 0, s>>>(n, J->d_sell_off, J->d_sell_col, k->d_val32, z32, w32);
     const double rho1 = 1.0 / (2.0 * sigma - rho);
-    k_cheb_step_t<float><<<nb(n), 256, 0, s>>>(n, k->d_dinv32, r32, w32, (float)(rho1 * rho), (float)(2.0 * rho1 / delta), d32, z32);
+    float *zn = zc == z32 ? w32 : z32;
+    if (bf)
+      k_sell_cheb<__nv_bfloat16, float><<<nb(n), 256, 0, s>>>(n, J->d_sell_off, J->d_sell_col, k->d_val16, k->d_dinv32, r32, zc,
+                                                              (float)(rho1 * rho), (float)(2.0 * rho1 / delta), d32, zn);
+    else
+      k_sell_cheb<float, float><<<nb(n), 256, 0, s>>>(n, J->d_sell_off, J->d_sell_col, k->d_val32, k->d_dinv32, r32, zc,
+                                                      (float)(rho1 * rho), (float)(2.0 * rho1 / delta), d32, zn);
+    zc = zn;
     rho = rho1;
   }
   k_convert<float, double><<<nb(n), 256, 0, s>>>(n, z32, z);
@@ -560,11 +569,18 @@ static dErr pc_apply_plain(_p_dKSP *k, const double *r, double *z) {
   const double theta = 0.5 * (k->emax + k->emin), delta = 0.5 * (k->emax - k->emin), sigma = theta / delta;
   double rho = 1.0 / sigma;
   double *d = k->d_work + 6 * n, *w = k->d_work + 7 * n;
-  k_cheb_first<<<nb(n), 256, 0, s>>>(n, k->d_dinv, r, 1.0 / theta, d, z);
+  _p_dMat *J = k->pmat;
+  DCHK(mat_sell(J, s));
+  // the iterate alternates between z and w (each fused step reads one and writes the other) and ends in z
+  double *zc = (k->cheb_degree - 1) % 2 == 0 ? z : w;
+  k_cheb_first<<<nb(n), 256, 0, s>>>(n, k->d_dinv, r, 1.0 / theta, d, zc);
   for (int it = 1; it < k->cheb_degree; it++) {
-    DCHK(mat_mult(k->pmat, z, w, s));
     const double rho1 = 1.0 / (2.0 * sigma - rho);
-    k_cheb_step<<<nb(n), 256, 0, s>>>(n, k->d_dinv, r, w, rho1 * rho, 2.0 * rho1 / delta, d, z);
+    double *zn = zc == z ? w : z;
+    if (n > 0)
+      k_sell_cheb<double, double><<<nb(n), 256, 0, s>>>(n, J->d_sell_off, J->d_sell_col, J->d_sell_val, k->d_dinv, r, zc, rho1 * rho,
+                                                        2.0 * rho1 / delta, d, zn);
+    zc = zn;
     rho = rho1;
   }
   CUCHK(cudaGetLastError());
@@ -578,19 +594,14 @@ static dErr read_scalar(const double *d, double *h, cudaStream_t s) {
 }
 
 // one CG step after the convergence test: z = M r, rz' = r.z, p = z + (rz'/rz) p, rz = rz', q = A p, pq = p.q,
-// x += (rz/pq) p, r -= (rz/pq) q, rr = r.r (S[0] = rz, S[1] = pq, S[2] = rr, S[4] = rz')
+// x += (rz/pq) p, r -= (rz/pq) q, rr = r.r (S[4] = rz, S[1] = pq, S[2] = rr; S[0] = the previous step's rz)
 static dErr cg_step(_p_dKSP *k, double *x, double *r, double *z, double *p, double *q, double *S, bool first) {
   const int64_t n = k->n;
   cudaStream_t s = kstream(k);
   DCHK(pc_apply(k, r, z));
-  if (first) {
-    CUCHK(cudaMemcpyAsync(p, z, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    DCHK(device_dot(n, r, z, k->d_part, S, s));
-  } else {
-    DCHK(device_dot(n, r, z, k->d_part, S + 4, s));
-    k_xpay_ratio<<<nb(n), 256, 0, s>>>(n, z, S + 4, S, p);
-    CUCHK(cudaMemcpyAsync(S, S + 4, sizeof(double), cudaMemcpyDeviceToDevice, s));
-  }
+  DCHK(device_dot(n, r, z, k->d_part, S + 4, s));
+  if (first) CUCHK(cudaMemcpyAsync(p, z, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  else k_xpay_ratio<<<nb(n), 256, 0, s>>>(n, z, S + 4, S, p);  // S[0]: the previous step's rz
   DCHK(kmult(k, p, q, dPREC_FP64));
   DCHK(device_dot(n, p, q, k->d_part, S + 1, s));
   k_cg_update<<<dot_grid(n), RED_THREADS, 0, s>>>(n, S, p, q, x, r, k->d_part, S + 2);
@@ -614,7 +625,7 @@ static dErr cg_solve(_p_dKSP *k, const double *b, double *x, double rtol, int ma
   const int64_t n = k->n;
   cudaStream_t s = kstream(k);
   double *r = k->d_work, *z = k->d_work + n, *p = k->d_work + 2 * n, *q = k->d_work + 3 * n;
-  double *S = k->d_s;  // S[0]=rz S[1]=pq S[2]=rr S[3]=bb S[4]=rz_new S[8]=iterations (device loop)
+  double *S = k->d_s;  // S[0]=previous rz S[1]=pq S[2]=rr S[3]=bb S[4]=rz S[8]=iterations (device loop)
   DCHK(kmult(k, x, q, dPREC_FP64));
   CUCHK(cudaMemcpyAsync(r, b, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
   k_axpby<<<nb(n), 256, 0, s>>>(n, -1.0, nullptr, nullptr, q, 1.0, r);
