@@ -159,7 +159,7 @@ def grf_numpy(grf, X):
     return out
 
 
-def cpu_baseline(cfg, threads, budget_s=20.0):
+def cpu_baseline(cfg, threads, budget_s=20.0, compare=None):
     """Oracle (CPU restatement of the reference apply: per-element geometry recompute, INTERP+GRAD, q-function,
     INTERP_T+GRAD_T, E/E^T) timed on the full workload (same mesh, orders, coefficient and input as the GPU arm),
     all host threads (OpenMP over elements, expand and restrict; the reference runs one MPI rank per core, each
@@ -190,9 +190,13 @@ def cpu_baseline(cfg, threads, budget_s=20.0):
             break
     times.sort()
     t = times[len(times) // 2]
-    return {"value": fs.n * bs / t / 1e9, "unit": "GDoF/s", "cores": threads, "kind": "port", "dofs": fs.n * bs,
-            "sample": "the full workload, %d^3 elements (%d dofs), median of %d applies, oracle C restatement, %d OpenMP threads"
-                      % (ne, fs.n * bs, len(times), threads)}
+    out = {"value": fs.n * bs / t / 1e9, "unit": "GDoF/s", "cores": threads, "kind": "port", "dofs": fs.n * bs,
+           "sample": "the full workload, %d^3 elements (%d dofs), median of %d applies, oracle C restatement, %d OpenMP threads"
+                     % (ne, fs.n * bs, len(times), threads)}
+    if compare:  # the GPU arm's results on the same input against the oracle's apply
+        yo = fs.apply(x, kind=kind, qdata=qd, param=param, nthreads=threads)
+        out["gpu_rel_err_vs_this_apply"] = {k: float(np.linalg.norm(v - yo) / np.linalg.norm(yo)) for k, v in compare.items()}
+    return out
 
 
 def cpu_time_to_rtol_poisson8(threads):
@@ -368,9 +372,10 @@ def bf16_tc_leg(fs, op, x, y64, args, stream):
             "dtype": "bf16 operands, fp32 accumulation (tcgen05 tensor cores)"}
 
 
-def float_float_leg(op, x, y64, args, stream):
+def float_float_leg(op, x, y64, args, stream, keep=None):
     """the same apply with dPREC_FF (values as FP32 pairs, unit roundoff ~2^-48, FP32 pipe), its time and its
-    relative difference from the FP64 result in y64 (computed by the caller with the same operator)"""
+    relative difference from the FP64 result in y64 (computed by the caller with the same operator); with keep (a
+    dict) the FP64 and float-float results are left there as host arrays for the comparison with the oracle"""
     import torch
     import dohp_gb300 as dg
     op.mult(x, y64)
@@ -381,6 +386,8 @@ def float_float_leg(op, x, y64, args, stream):
     ms, _ = time_loop(lambda: op.mult(x, yff), max(args.steps, 5), stream)
     err = float(torch.linalg.norm(yff - y64) / torch.linalg.norm(y64))
     op.set_precision(dg.dPREC_FP64)
+    if keep is not None:
+        keep["fp64"], keep["float_float"] = y64.cpu().numpy(), yff.cpu().numpy()
     return {"unit": "GDoF/s", "ms_per_apply": ms, "rel_diff_vs_fp64": err,
             "dtype": "float-float (2 x fp32 per value, unit roundoff ~2^-48, FP32 pipe)"}
 
@@ -748,7 +755,8 @@ def main():
         dist.barrier()
 
     # the same apply in float-float arithmetic, reported beside the FP64 headline (not in place of it)
-    ffleg = float_float_leg(op, x, y, args, stream)
+    gpu_results = {}
+    ffleg = float_float_leg(op, x, y, args, stream, keep=gpu_results)
     ffleg["value"] = whole_job_gdofs(world, N, ffleg["ms_per_apply"] * 1e-3)
 
     # end to end through the host-vector entry point (pinned buffers, copies inside the timed region)
@@ -824,7 +832,7 @@ def main():
         line["time_to_rtol_poisson_8"] = {"workload": "poisson-8^3-p4, mass right-hand side, CG + Q1 Chebyshev(3)-Jacobi, rtol 1e-8",
                                      "gpu": gpu_time_to_rtol_poisson8()}
     if not args.no_cpu_baseline and world == 1:
-        line["cpu_baseline"] = cpu_baseline(cfg, os.cpu_count() or 1)
+        line["cpu_baseline"] = cpu_baseline(cfg, os.cpu_count() or 1, compare=gpu_results)
         if "time_to_rtol_poisson_8" in line:
             line["time_to_rtol_poisson_8"]["cpu_oracle"] = cpu_time_to_rtol_poisson8(os.cpu_count() or 1)
     print(json.dumps(line, default=_plain))
