@@ -69,7 +69,9 @@ def parse():
     ap.add_argument("--secondary", default="all", help="comma list of apply,learned,newton,multigrid,stokes (or all: apply, learned (which includes the multigrid "
                          "solves), newton)")
     ap.add_argument("--learned-ne", type=int, default=64, help="elements per side of the learned-correction solve")
-    ap.add_argument("--learned-epochs", type=int, default=8)
+    ap.add_argument("--learned-epochs", type=int, default=24,
+                    help="training epochs of the vertex-lattice network: two thirds at lr 1e-3, the rest at 5e-4")
+    ap.add_argument("--learned-gll-epochs", type=int, default=8, help="the same for the GLL-lattice network")
     ap.add_argument("--learned-grids", default="vertex,gll",
                     help="lattices of the learned correction: vertex (mesh vertices), gll (GLL nodes, the Q1-embedded grid)")
     ap.add_argument("--newton-ne", type=int, default=48, help="elements per side of the p-Laplacian Newton run")
@@ -606,7 +608,7 @@ def secondary_learned(args):
     import numpy as np
     import torch
     import dohp_gb300 as dg
-    ne, nfields, per_field, epochs = args.learned_ne, 8, 250, args.learned_epochs
+    ne, nfields, per_field = args.learned_ne, 8, 250
 
     def problem(seed):
         fs = dg.FS((ne + 1,) * 3, degree=4, perturb=0.1, seed=1)
@@ -647,11 +649,16 @@ def secondary_learned(args):
         torch.cuda.synchronize()
         info["pairs"] = net.npairs
         info["collect_s"] = time.perf_counter() - t0
+        epochs = args.learned_gll_epochs if grid == "gll" else args.learned_epochs
+        e1 = (2 * epochs + 2) // 3
         t0 = time.perf_counter()
-        losses = net.train(epochs=epochs, batch=16, lr=1e-3, seed=1)
+        losses = list(net.train(epochs=e1, batch=16, lr=1e-3, seed=1))
+        if epochs > e1:  # a step down of the learning rate for the last third
+            losses += list(net.train(epochs=epochs - e1, batch=16, lr=5e-4, seed=2))
         torch.cuda.synchronize()
         info["train_s"] = time.perf_counter() - t0
         info["epochs"] = epochs
+        info["lr_schedule"] = "%d epochs at 1e-3, %d at 5e-4 (Adam, batch 16)" % (e1, epochs - e1)
         info["loss_per_epoch"] = [float(v) for v in losses]
         nets[grid] = net
         if grid == "vertex":

@@ -804,13 +804,17 @@ dErr ensure_cap(_p_dLearned *L, int B, bool grads) {
   DCHK(grow(&L->tb, &L->gcap[5], (int64_t)B * d[0].n()));
   DCHK(grow(&L->bmask, &L->bmcap, (int64_t)B * d[0].n()));
   DCHK(grow(&L->lpart, &L->lpcap, (int64_t)nblk((int64_t)B * d[0].n())));
-  // weight-gradient partials: the largest chunk count times parameters over the layers
+  // weight-gradient partials: the largest chunk count times parameters over the layers, and room for one partial
+  // per block of the grid-stride tensor-core weight-gradient kernel (up to two blocks per SM)
+  int dev = 0, nsm = 0;
+  CUCHK(cudaGetDevice(&dev));
+  CUCHK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   int64_t need = 0;
   for (int l = 0; l < NLAYER; l++) {
     const LayerDef &ld = kLayer[l];
     const Dims dout = ld.stride == 2 ? d[ld.level_in + 1] : d[ld.level_in];
     const int64_t nch = ((int64_t)B * dout.x * dout.y * ((dout.z + VZ - 1) / VZ) + kQuadChunk - 1) / kQuadChunk;
-    need = std::max<int64_t>(need, nch * ((int64_t)ld.co * ld.ci * 27 + ld.co));
+    need = std::max<int64_t>(need, std::max<int64_t>(nch, dout.n() > 0 ? 2 * nsm : 0) * ((int64_t)ld.co * ld.ci * 27 + ld.co));
   }
   DCHK(grow(&L->partial, &L->partial_len, need));
   return 0;
