@@ -537,6 +537,26 @@ def secondary_multigrid(args):
     b = torch.as_tensor(np.random.default_rng(5000).uniform(-1, 1, fs.n), device="cuda")
     out = {"workload": "lognormal-poisson-%d^3-p4, Q1 multigrid" % ne, "dofs": fs.n, "rtol": 1e-8}
     out.update(multigrid_solves(fs, op, m, b))
+    if "vertex" in nets:  # the network added to the multigrid preconditioner (trained on Chebyshev-Jacobi pairs)
+        ksp = dg.KSP(op, m, ksp_type=dg.dKSP_FGMRES, inner_prec=dg.dPREC_FP32, restart=30, pc=dg.dPC_MG_Q1)
+        ksp.set_learned(nets["vertex"])
+        x = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
+        try:  # set-up outside the timed solve, as the multigrid legs
+            ksp.solve(b, x, rtol=1e-1, maxit=50)
+        except dg.DohpError:
+            pass
+        x.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        its, _ = ksp.solve(b, x, rtol=1e-8, maxit=2000)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        r = torch.empty_like(x)
+        op.mult(x, r)
+        applies, rejects, active = ksp.stats()
+        out["learned_multigrid_mixed"] = {"its": its, "wall_s": wall,
+                                          "true_rel_residual": float(torch.linalg.norm(b - r) / torch.linalg.norm(b)),
+                                          "correction_dropped": bool(rejects), "correction_active_at_end": active}
     return out
 
 
@@ -697,9 +717,30 @@ def secondary_learned(args):
         out[name] = {"its": its, "wall_s": wall, "true_rel_residual": float(torch.linalg.norm(b - r) / torch.linalg.norm(b)),
                      "correction_dropped": bool(rejects), "correction_active_at_end": active}
     out.update(multigrid_solves(fs, op, m, b))
+    if "vertex" in nets:  # the network added to the multigrid preconditioner (trained on Chebyshev-Jacobi pairs)
+        ksp = dg.KSP(op, m, ksp_type=dg.dKSP_FGMRES, inner_prec=dg.dPREC_FP32, restart=30, pc=dg.dPC_MG_Q1)
+        ksp.set_learned(nets["vertex"])
+        x = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
+        try:  # set-up outside the timed solve, as the multigrid legs
+            ksp.solve(b, x, rtol=1e-1, maxit=50)
+        except dg.DohpError:
+            pass
+        x.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        its, _ = ksp.solve(b, x, rtol=1e-8, maxit=2000)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        r = torch.empty_like(x)
+        op.mult(x, r)
+        applies, rejects, active = ksp.stats()
+        out["learned_multigrid_mixed"] = {"its": its, "wall_s": wall,
+                                          "true_rel_residual": float(torch.linalg.norm(b - r) / torch.linalg.norm(b)),
+                                          "correction_dropped": bool(rejects), "correction_active_at_end": active}
     out["speedup_vs_plain_fp64"] = {k: out["plain_fp64"]["wall_s"] / out[k]["wall_s"]
                                     for k in ("mixed_fp32", "mixed_bf16", "learned_mixed", "learned_bf16", "learned_fp64",
-                                              "learned_gll_mixed", "multigrid_cg_fp64", "multigrid_mixed_fp32") if k in out}
+                                              "learned_gll_mixed", "multigrid_cg_fp64", "multigrid_mixed_fp32",
+                                              "learned_multigrid_mixed") if k in out}
     return out
 
 

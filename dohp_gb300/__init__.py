@@ -610,6 +610,12 @@ class Learned:
     def set_weights(self, w, target_scale=0.0):
         chk(lib().dLearnedSetWeights(self.h, ptr(np.ascontiguousarray(w, np.float32)), _dbl(target_scale)))
 
+    def save(self, path, with_moments=False):
+        chk(lib().dLearnedSave(self.h, str(path).encode(), ctypes.c_int(int(with_moments))))
+
+    def load(self, path):
+        chk(lib().dLearnedLoad(self.h, str(path).encode()))
+
     def scale(self):
         v = _dbl()
         chk(lib().dLearnedGetScale(self.h, ctypes.byref(v)))

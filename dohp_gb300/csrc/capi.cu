@@ -268,6 +268,7 @@ dErr dEFSGetTensorNodes(dEFS efs, dInt P[3], dInt Q[3], dReal *basis_nodes, dRea
 
 dErr dEFSApplyBatched(dEFS efs, dInt nelem, const dReal *jinv, dInt D, const dScalar *in, dScalar *out, dApplyMode amode,
                       InsertMode imode, void *stream) {
+  Range range_("dEFSApply");
   return efs_apply_list(efs, nelem, nullptr, nullptr, nullptr, jinv, D, in, out, amode, imode, (cudaStream_t)stream);
 }
 
@@ -348,11 +349,13 @@ dErr dOperatorSetPrecision(dOperator op, dPrecision prec) {
 }
 
 dErr dOperatorMult(dOperator op, const dScalar *x, dScalar *y) {
+  Range range_("EllipShellMult");
   if (!op) return set_error("null operator");
   return op_mult(op, x, y);
 }
 
 dErr dOperatorMultHost(dOperator op, const dScalar *x_host, dScalar *y_host) {
+  Range range_("EllipShellMult (host vectors)");
   if (!op) return set_error("null operator");
   _p_dFS *fs = op->fs;
   const size_t bytes = fs->n * fs->bs * sizeof(double);
@@ -434,6 +437,7 @@ dErr dMatDestroy(dMat *J) {
 }
 
 dErr dFSAssembleQ1(dFS fs, dMat J, dOperatorKind kind, const dReal *param, const dReal *grf, int reference_quirk) {
+  Range range_("dQ1HexComputQuad");
   (void)param;
   if (!fs || !J) return set_error("null argument");
   if (kind == dOP_PLAPLACE_JACOBIAN) return set_error("the p-Laplacian Q1 matrix depends on the state: use dFSAssembleQ1PLaplace");

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <map>
@@ -24,6 +25,15 @@ dErr set_error(const char *fmt, ...);
     if (_c != cudaSuccess) return ::dgb::set_error("%s:%d CUDA error %s: %s", __FILE__, __LINE__,   \
                                                    cudaGetErrorName(_c), cudaGetErrorString(_c));    \
   } while (0)
+
+// an NVTX range for the lifetime of the object (the phases a profiler shows: operator applies, assembly, solves,
+// multigrid cycles, the learned correction); named after the reference's PETSc log events where it has one
+struct Range {
+  explicit Range(const char *name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+  Range(const Range &) = delete;
+  Range &operator=(const Range &) = delete;
+};
 
 constexpr int MAXP = 9;   // max nodes per direction (degree 8)
 constexpr int MAXQ = 18;  // max rule points per direction (SPARSE rule of degree 8)

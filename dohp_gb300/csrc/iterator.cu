@@ -394,6 +394,7 @@ dErr dRulesetIteratorGetStash(dRulesetIterator it, void *elemstash, void *nodest
 }
 
 dErr dRulesetIteratorStart(dRulesetIterator it, const dScalar *X, ...) {
+  Range range_("dRulesetIteratorStart");
   if (!it) return set_error("null iterator");
   va_list ap;
   va_start(ap, X);

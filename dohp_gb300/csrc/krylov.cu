@@ -932,6 +932,7 @@ dErr ksp_pc_only(dKSP ksp, const double *r, double *z) {
 extern "C" {
 
 dErr dKSPSolve(dKSP ksp, const dScalar *b, dScalar *x, dReal rtol, dInt maxit, dInt *its, dReal *rnorm) {
+  Range range_("KSPSolve");
   int it = 0;
   double rn = 0;
   DCHK(ksp_solve(ksp, b, x, rtol, maxit, &it, &rn));

@@ -430,6 +430,7 @@ static dErr apply_t(MGData *M, const double *r, double *z, cudaStream_t s) {
 }
 
 dErr mg_apply(void *m, const double *r, double *z, cudaStream_t s) {
+  Range range_("PCApply (Q1 multigrid V-cycle)");
   MGData *M = (MGData *)m;
   return M->fp32 ? apply_t<float>(M, r, z, s) : apply_t<double>(M, r, z, s);
 }

@@ -340,6 +340,7 @@ static dErr assemble_q1_plap(dFS fs, dMat J, const dScalar *g, dReal p, dReal ep
 }
 
 dErr dFSAssembleQ1PLaplace(dFS fs, dMat J, const dScalar *g, dReal p, dReal eps, int reference_quirk) {
+  Range range_("dQ1HexComputQuad (p-Laplacian)");
   return assemble_q1_plap(fs, J, g, p, eps, reference_quirk, false);
 }
 
@@ -349,6 +350,7 @@ dErr dFSAssembleQ1PLaplace(dFS fs, dMat J, const dScalar *g, dReal p, dReal eps,
 // the matrix-free Jacobian at u), and accepts u + lambda du once ||F|| drops by the Armijo factor.
 dErr dPLaplaceNewtonSolve(dOperator op, dMat Jp, dKSP ksp, const dScalar *b, dScalar *u, dReal p, dReal eps,
                           const dNewtonOptions *opt, dInt *its, dReal *fnorm, dInt *lin_its) {
+  Range range_("SNESSolve (p-Laplacian Newton)");
   if (!op || !Jp || !ksp || !b || !u || !opt) return set_error("null argument");
   _p_dFS *fs = op->fs;
   cudaStream_t s = fs->stream;

@@ -538,6 +538,7 @@ extern "C" {
 
 dErr dStokesSolve(dStokes stk, const dScalar *bu, const dScalar *bp, dScalar *xu, dScalar *xp, dReal rtol, dInt maxit, dInt *its,
                   dReal *rnorm) {
+  Range range_("KSPSolve (Stokes)");
   if (!stk || !bu || !bp || !xu || !xp) return set_error("null argument");
   _p_dStokes *S = stk;
   cudaStream_t s = S->fsu->stream;
@@ -572,6 +573,7 @@ dErr dStokesSolve(dStokes stk, const dScalar *bu, const dScalar *bp, dScalar *xu
 // the store of the last function evaluation) and backtracks on ||F||.
 dErr dStokesNewtonSolve(dStokes stk, const dScalar *bu, const dScalar *bp, dScalar *xu, dScalar *xp, const dNewtonOptions *opt,
                         dInt *its, dReal *fnorm, dInt *lin_its) {
+  Range range_("SNESSolve (Stokes)");
   if (!stk || !bu || !bp || !xu || !xp || !opt) return set_error("null argument");
   _p_dStokes *S = stk;
   cudaStream_t s = S->fsu->stream;

@@ -21,7 +21,10 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstring>
 #include <random>
+#include <string>
 
 #include "internal.h"
 
@@ -1013,6 +1016,7 @@ dErr adam_step(_p_dLearned *L, double lr, cudaStream_t s) {
 
 // the correction z += P N(R r); called by FGMRES after the Chebyshev step
 dErr apply_correction(void *ctx, const double *r, double *z) {
+  Range range_("LearnedCorrection");
   _p_dLearned *L = (_p_dLearned *)ctx;
   _p_dFS *fs = L->fs;
   cudaStream_t s = fs->stream;
@@ -1346,6 +1350,7 @@ dErr dLearnedLossGrad(dLearned L, dInt B, const float *in, const float *target, 
 // pairs' log k channel
 dErr dLearnedCollectPairs(dLearned L, dKSP ksp, const dScalar *b, dReal rtol, dInt maxit, dInt every, dInt max_pairs,
                           int rough_start, dInt *collected) {
+  Range range_("LearnedCollectPairs");
   if (!L || !ksp || !b) return set_error("null argument");
   if (every < 1 || max_pairs < 1) return set_error("every and max_pairs must be positive");
   _p_dFS *fs = L->fs;
@@ -1434,6 +1439,7 @@ dErr dLearnedCollectPairs(dLearned L, dKSP ksp, const dScalar *b, dReal rtol, dI
 
 // minibatch Adam on the collected pairs; losses[epochs] receives the mean loss of every epoch
 dErr dLearnedTrain(dLearned L, dInt epochs, dInt batch, dReal lr, uint64_t seed, dReal *losses) {
+  Range range_("LearnedTrain");
   if (!L) return set_error("null network");
   if (L->npairs < 1) return set_error("no training pairs collected");
   if (epochs < 1 || batch < 1) return set_error("epochs and batch must be positive");
@@ -1567,6 +1573,84 @@ dErr dLearnedSetTensorCores(dLearned L, int on) {
   if (!L) return set_error("null network");
   L->use_tc = on != 0;
   L->tc_checked = false;
+  return 0;
+}
+
+// checkpoint file: "DGBUNET1", then (little-endian) uint32 format version 1, uint32 JSON length, int64 parameters,
+// float64 target scale, int64 Adam steps, uint32 flags (1: Adam moments follow the weights), the JSON header (the
+// same fields and the layer list, for readers), the FP32 weights, and with flag 1 the FP32 first and second moments
+namespace {
+constexpr char kMagic[8] = {'D', 'G', 'B', 'U', 'N', 'E', 'T', '1'};
+struct CkptHead {
+  uint32_t version, json_len;
+  int64_t nparam;
+  double ysc;
+  int64_t adam_t;
+  uint32_t flags;
+};
+}  // namespace
+
+dErr dLearnedSave(dLearned L, const char *path, int with_moments) {
+  if (!L || !path) return set_error("null argument");
+  std::string js = "{\"format\": \"dohp_gb300 U-Net checkpoint\", \"version\": 1, \"nparam\": " + std::to_string(L->nparam) +
+                   ", \"grid\": \"" + (L->grid == dLEARNED_GRID_GLL ? "gll" : "vertex") + "\", \"lattice\": [" +
+                   std::to_string(L->d[0].x) + ", " + std::to_string(L->d[0].y) + ", " + std::to_string(L->d[0].z) +
+                   "], \"layers\": [";
+  const char *names[NLAYER] = {"C1A", "C1B", "D1", "C2A", "D2", "C3A", "C3B", "U2", "C2B", "U1", "C1C", "OUT"};
+  for (int l = 0; l < NLAYER; l++)
+    js += std::string(l ? ", " : "") + "[\"" + names[l] + "\", " + std::to_string(kLayer[l].ci) + ", " + std::to_string(kLayer[l].co) +
+          ", " + std::to_string(kLayer[l].stride) + "]";
+  js += "], \"weights\": \"per layer W[co][ci][27] then bias[co], float32 little-endian\"}";
+  CkptHead h{1u, (uint32_t)js.size(), L->nparam, L->ysc, L->adam_t, with_moments ? 1u : 0u};
+  std::vector<float> buf((size_t)L->nparam * (with_moments ? 3 : 1));
+  CUCHK(cudaMemcpy(buf.data(), L->w, L->nparam * sizeof(float), cudaMemcpyDeviceToHost));
+  if (with_moments) {
+    CUCHK(cudaMemcpy(buf.data() + L->nparam, L->m, L->nparam * sizeof(float), cudaMemcpyDeviceToHost));
+    CUCHK(cudaMemcpy(buf.data() + 2 * L->nparam, L->v, L->nparam * sizeof(float), cudaMemcpyDeviceToHost));
+  }
+  FILE *f = fopen(path, "wb");
+  if (!f) return set_error("cannot open %s for writing", path);
+  const bool ok = fwrite(kMagic, 1, 8, f) == 8 && fwrite(&h.version, 4, 1, f) == 1 && fwrite(&h.json_len, 4, 1, f) == 1 &&
+                  fwrite(&h.nparam, 8, 1, f) == 1 && fwrite(&h.ysc, 8, 1, f) == 1 && fwrite(&h.adam_t, 8, 1, f) == 1 &&
+                  fwrite(&h.flags, 4, 1, f) == 1 && fwrite(js.data(), 1, js.size(), f) == js.size() &&
+                  fwrite(buf.data(), sizeof(float), buf.size(), f) == buf.size();
+  if (fclose(f) != 0 || !ok) return set_error("writing %s failed", path);
+  return 0;
+}
+
+dErr dLearnedLoad(dLearned L, const char *path) {
+  if (!L || !path) return set_error("null argument");
+  FILE *f = fopen(path, "rb");
+  if (!f) return set_error("cannot open %s", path);
+  char magic[8];
+  CkptHead h{};
+  bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, kMagic, 8) == 0 && fread(&h.version, 4, 1, f) == 1 && fread(&h.json_len, 4, 1, f) == 1 &&
+            fread(&h.nparam, 8, 1, f) == 1 && fread(&h.ysc, 8, 1, f) == 1 && fread(&h.adam_t, 8, 1, f) == 1 && fread(&h.flags, 4, 1, f) == 1;
+  if (!ok || h.version != 1) {
+    fclose(f);
+    return set_error("%s is not a U-Net checkpoint of format 1", path);
+  }
+  if (h.nparam != L->nparam) {
+    fclose(f);
+    return set_error("%s holds %lld parameters, the network has %lld", path, (long long)h.nparam, (long long)L->nparam);
+  }
+  const size_t count = (size_t)h.nparam * ((h.flags & 1u) ? 3 : 1);
+  std::vector<float> buf(count);
+  ok = fseek(f, (long)h.json_len, SEEK_CUR) == 0 && fread(buf.data(), sizeof(float), count, f) == count;
+  fclose(f);
+  if (!ok) return set_error("%s is truncated", path);
+  CUCHK(cudaMemcpy(L->w, buf.data(), L->nparam * sizeof(float), cudaMemcpyHostToDevice));
+  if (h.flags & 1u) {
+    CUCHK(cudaMemcpy(L->m, buf.data() + L->nparam, L->nparam * sizeof(float), cudaMemcpyHostToDevice));
+    CUCHK(cudaMemcpy(L->v, buf.data() + 2 * L->nparam, L->nparam * sizeof(float), cudaMemcpyHostToDevice));
+    L->adam_t = h.adam_t;
+  }
+  k_to_bf16<<<nblk(L->nparam), 256>>>(L->nparam, L->w, L->wb);
+  CUCHK(cudaGetLastError());
+  DCHK(repack_tc(L, 0));
+  CUCHK(cudaDeviceSynchronize());
+  L->ysc = h.ysc;
+  L->trained = true;
   return 0;
 }
 

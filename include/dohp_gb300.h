@@ -473,6 +473,10 @@ dErr dLearnedLayerWeightGrad(dLearned net, dInt layer, dInt B, const dInt dims[3
 dErr dLearnedGetWeights(dLearned net, float *w);
 dErr dLearnedSetWeights(dLearned net, const float *w, dReal target_scale);
 dErr dLearnedGetScale(dLearned net, dReal *target_scale);
+/* checkpoint / resume: the weights and target scale (and with with_moments the Adam state, to continue training) in a
+ * file with a JSON header; dLearnedLoad accepts a file of a network with the same layers and marks it trained */
+dErr dLearnedSave(dLearned net, const char *path, int with_moments);
+dErr dLearnedLoad(dLearned net, const char *path);
 /* transfer operators on their own: rc = R r (lattice), z = P c (global) */
 dErr dLearnedRestrict(dLearned net, const dScalar *r, dScalar *rc);
 dErr dLearnedProlong(dLearned net, const dScalar *c, dScalar *z);

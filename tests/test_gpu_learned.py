@@ -239,3 +239,36 @@ def test_fallback_to_plain_preconditioner(trained):
     its_n, true_n, _ = fgmres(op, m, b, net=bad)
     assert true_n <= 1.01e-8
     assert bad.stats()[1] > 0
+
+
+def test_checkpoint_round_trip(tmp_path):
+    """dLearnedSave / dLearnedLoad: weights, target scale and Adam state bit for bit, a readable JSON header, and the
+    refusal of a truncated file"""
+    import json
+    import struct
+    fs = dg.FS((7, 6, 7), degree=2, seed=1)
+    a = dg.Learned(fs, seed=3)
+    a.set_weights(a.get_weights() * 1.5, target_scale=0.25)
+    path = tmp_path / "net.dgbunet"
+    a.save(path, with_moments=True)
+    raw = path.read_bytes()
+    assert raw[:8] == b"DGBUNET1"
+    version, jlen, nparam, ysc, _, flags = struct.unpack("<IIqdqI", raw[8:44])
+    head = json.loads(raw[44:44 + jlen])
+    assert version == 1 and flags == 1 and nparam == a.nparam == head["nparam"] and ysc == 0.25
+    assert [row[0] for row in head["layers"]] == [name for name, *_ in uo.LAYERS]
+    assert len(raw) == 44 + jlen + 3 * 4 * nparam
+    b = dg.Learned(fs, seed=9)
+    b.load(path)
+    np.testing.assert_array_equal(b.get_weights(), a.get_weights())
+    assert b.scale() == 0.25
+    x = np.random.default_rng(0).standard_normal((1, 2) + a.dims).astype(np.float32)
+    ya = torch.zeros((1, 1) + a.dims, dtype=torch.float32, device="cuda")
+    yb = torch.zeros_like(ya)
+    a.forward(dev(x), ya)
+    b.forward(dev(x), yb)
+    assert torch.equal(ya, yb)
+    bad = tmp_path / "short.dgbunet"
+    bad.write_bytes(raw[:len(raw) // 2])
+    with pytest.raises(dg.DohpError):
+        b.load(bad)
