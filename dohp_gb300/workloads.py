@@ -4,6 +4,7 @@
     python -m dohp_gb300.workloads unet-forward --ne 32 --grid gll      # whole-lattice forwards, (ne*4+1)^3 nodes
     python -m dohp_gb300.workloads unet-train --ne 64 --batch 16         # loss + gradient steps on the vertex lattice
     python -m dohp_gb300.workloads cg --ne 8                             # Poisson CG + Q1 Chebyshev(3)-Jacobi to 1e-8
+    python -m dohp_gb300.workloads fgmres --ne 64 --precision fp32       # 2 restart cycles, lognormal Poisson
 
 Seeded random inputs and weights; each workload runs --reps passes after one warm-up pass and prints one JSON line
 with the mean time per pass (CUDA events)."""
@@ -17,7 +18,7 @@ import dohp_gb300 as dg
 
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m dohp_gb300.workloads")
-    ap.add_argument("workload", choices=["apply", "unet-forward", "unet-train", "cg"])
+    ap.add_argument("workload", choices=["apply", "unet-forward", "unet-train", "cg", "fgmres"])
     ap.add_argument("--ne", type=int, default=32, help="elements per side")
     ap.add_argument("--degree", type=int, default=4)
     ap.add_argument("--precision", choices=["fp64", "fp32", "bf16", "ff"], default="fp64", help="apply workload")
@@ -38,6 +39,8 @@ def main(argv=None):
                                                "precision": a.precision})
     if a.workload == "cg":
         return cg(fs, a)
+    if a.workload == "fgmres":
+        return fgmres(fs, a)
     grid = dg.LEARNED_GRID_GLL if a.grid == "gll" else dg.LEARNED_GRID_VERTEX
     net = dg.Learned(fs, seed=3, grid=grid)
     if a.tensor_cores >= 0:
@@ -83,6 +86,39 @@ def cg(fs, a):
     t, t10 = e[0].elapsed_time(e[1]), e[2].elapsed_time(e[3])
     print(json.dumps({"workload": "cg", "elements": a.ne ** 3, "degree": a.degree, "dofs": fs.n, "its": its, "rel_residual": rn,
                       "solve_ms": t, "us_per_iteration": (t - t10) / (its - its10) * 1e3}))
+
+
+def fgmres(fs, a):
+    """FGMRES(30) with the Q1 Chebyshev(3)-Jacobi preconditioner and inner applies in --precision on the lognormal
+    Poisson problem (field seed 5000), two restart cycles (60 iterations) after one warm-up cycle: ms per iteration"""
+    grf = dg.grf_create(64, 2.0, 0.1, 5000)
+    kq = torch.empty(fs.nq, dtype=torch.float64, device="cuda")
+    fs.lognormal(grf, kq)
+    op = fs.operator()
+    op.set_qdata(kq)
+    m = fs.matrix()
+    m.assemble(grf=grf)
+    prec = {"fp64": dg.dPREC_FP64, "fp32": dg.dPREC_FP32, "bf16": dg.dPREC_BF16, "ff": dg.dPREC_FF}[a.precision]
+    ksp = dg.KSP(op, m, ksp_type=dg.dKSP_FGMRES, inner_prec=prec, restart=30)
+    gen = torch.Generator(device="cuda").manual_seed(5)
+    b = torch.rand(fs.n, dtype=torch.float64, device="cuda", generator=gen) * 2 - 1
+    x = torch.zeros_like(b)
+
+    def cycles(k):
+        x.zero_()
+        try:  # stops at maxit before the tolerance: reported as an error
+            ksp.solve(b, x, rtol=1e-12, maxit=30 * k)
+        except dg.DohpError:
+            pass
+
+    cycles(1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    cycles(2)
+    e1.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"workload": "fgmres", "elements": a.ne ** 3, "dofs": fs.n, "precision": a.precision,
+                      "ms_per_iteration": e0.elapsed_time(e1) / 60}))
 
 
 def run(step, a, info):
