@@ -367,15 +367,16 @@ struct _p_dKSP {
   double *d_dinv = nullptr, *d_work = nullptr, *d_part = nullptr, *d_s = nullptr;
   dPrecision inner_prec = dPREC_FP64;  // precision of the operator applies inside an FGMRES cycle
   double *d_V = nullptr, *d_Z = nullptr, *d_h = nullptr;  // FGMRES bases [(m+1) x n], [m x n], coefficients
+  double *d_trial = nullptr;  // FGMRES with a correction: saved iterate and residual, the plain trial's iterate [3 x n]
   float *d_w32 = nullptr, *d_dinv32 = nullptr, *d_val32 = nullptr;  // FP32 Chebyshev workspace
   __nv_bfloat16 *d_val16 = nullptr;                                // BF16 Q1 values
   // optional preconditioner correction applied after the Chebyshev step: z += corr(r) (learned correction,
-  // FGMRES only); dropped for the rest of a solve when a restart cycle with it fails to reduce the residual
+  // FGMRES only), judged against the plain preconditioner by paired trial cycles (fgmres_solve)
   dErr (*correction)(void *ctx, const double *r, double *z) = nullptr;
   void *correction_ctx = nullptr;
-  bool correction_on = false;
+  bool correction_on = false, plain_cycle = false;
   // 0: every preconditioner application; 1: first vector of each restart cycle (the true residual);
-  // 2: adaptive -- one cycle of each, then the one that reduced the residual more
+  // 2: adaptive -- a trial of each against a plain cycle, then the one that won by more
   int correction_policy = 2, active_policy = 0;
   int cycle_pos = 0;  // position of the vector being preconditioned within the FGMRES cycle
   int64_t pc_applies = 0, correction_rejects = 0;
@@ -547,7 +548,7 @@ static dErr pc_apply(_p_dKSP *k, const double *r, double *z) {
   k->pc_applies++;
   if (k->shell_pc) return k->shell_pc(k->shell_ctx, r, z);
   DCHK(pc_apply_plain(k, r, z));
-  if (k->correction && k->correction_on && (k->active_policy == 0 || k->cycle_pos == 0))
+  if (k->correction && k->correction_on && !k->plain_cycle && (k->active_policy == 0 || k->cycle_pos == 0))
     DCHK(k->correction(k->correction_ctx, r, z));
   return 0;
 }
@@ -718,6 +719,13 @@ static dErr cg_solve(_p_dKSP *k, const double *b, double *x, double rtol, int ma
 // Each cycle starts from the true residual b - A x computed with the FP64 operator; the operator applies
 // inside a cycle and the preconditioner run in k->pc_prec (FP32 for the mixed-precision solver). The
 // flexible (Z) basis makes the varying inner precision and a learned correction admissible.
+//
+// With a correction the plain preconditioner judges it: a trial runs one cycle with the plain preconditioner and one
+// with the correction from the same iterate and keeps the iterate with the smaller true residual (both cycles count
+// as iterations). Policy 2 (adaptive) tries the correction on every vector, then on the first vector of the cycle;
+// policies 0 and 1 try theirs once. Afterwards the correction runs in the mode that beat its plain cycle by the larger
+// margin, or is dropped for the rest of the solve if neither did; a later cycle with it that reduces the true residual
+// by less than 1 % (or gives a non-finite one) drops it too.
 static dErr fgmres_solve(_p_dKSP *k, const double *b, double *x, double rtol, int maxit, int *its, double *rnorm) {
   const int64_t n = k->n;
   const int m = std::max(1, k->restart);
@@ -727,37 +735,26 @@ static dErr fgmres_solve(_p_dKSP *k, const double *b, double *x, double rtol, in
     CUCHK(cudaMalloc(&k->d_Z, (size_t)m * n * sizeof(double)));
     CUCHK(cudaMalloc(&k->d_h, (size_t)(2 * (m + 2) + (m + 1) * RED_BLOCKS) * sizeof(double)));
   }
+  if (k->correction && !k->d_trial) CUCHK(cudaMalloc(&k->d_trial, 3 * std::max<int64_t>(n, 1) * sizeof(double)));
   double *V = k->d_V, *Z = k->d_Z, *h1 = k->d_h, *h2 = k->d_h + (m + 2), *mpart = k->d_h + 2 * (m + 2);
   std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), yv(m), hcol(m + 2);
   double bb;
   DCHK(device_dot(n, b, b, k->d_part, k->d_s, s));
   DCHK(read_scalar(k->d_s, &bb, s));
   const double bn = sqrt(bb) > 0 ? sqrt(bb) : 1.0;
-  int total = 0, cycle = 0;
-  double res = 0, prev = -1, rho[2] = {-1, -1};
-  k->correction_on = k->correction != nullptr;
-  for (;;) {
+  int total = 0;
+  // V0 = b - A x (FP64 operator) and its norm
+  auto true_residual = [&](double &beta) -> dErr {
     DCHK(kmult(k, x, V, dPREC_FP64));
-    k_axpby<<<nb(n), 256, 0, s>>>(n, 1.0, nullptr, nullptr, b, -1.0, V);  // V0 = b - A x
+    k_axpby<<<nb(n), 256, 0, s>>>(n, 1.0, nullptr, nullptr, b, -1.0, V);
     double rr;
     DCHK(device_dot(n, V, V, k->d_part, k->d_s, s));
     DCHK(read_scalar(k->d_s, &rr, s));
-    const double beta = sqrt(rr);
-    res = beta / bn;
-    if (!(beta > rtol * bn) || total >= maxit) break;
-    // the true residual decides whether the correction stays: a restart cycle that stagnated (less than 1 %
-    // reduction of the true residual, or a non-finite one) drops the correction for the rest of this solve
-    if (k->correction_on && prev > 0 && !(beta < 0.99 * prev)) {
-      k->correction_on = false;
-      k->correction_rejects++;
-    }
-    if (k->correction_on && prev > 0 && rho[k->active_policy] < 0) rho[k->active_policy] = beta / prev;
-    if (k->correction_policy == 2)
-      k->active_policy = cycle == 0 ? 0 : cycle == 1 ? 1 : (rho[0] >= 0 && (rho[1] < 0 || rho[0] <= rho[1]) ? 0 : 1);
-    else
-      k->active_policy = k->correction_policy;
-    cycle++;
-    prev = beta;
+    beta = sqrt(rr);
+    return 0;
+  };
+  // one restart cycle from x, whose residual (norm beta) is in V0: Arnoldi with the preconditioner as set, x += Z y
+  auto run_cycle = [&](double beta) -> dErr {
     k_scale_into<<<nb(n), 256, 0, s>>>(n, V, nullptr, 1.0 / beta, V);
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
@@ -804,7 +801,66 @@ static dErr fgmres_solve(_p_dKSP *k, const double *b, double *x, double rtol, in
     k_maxpy<<<nb(n), 256, 0, s>>>(n, j, 1.0, h1, Z, x);
     CUCHK(cudaStreamSynchronize(s));
     CUCHK(cudaGetLastError());
+    return 0;
+  };
+  const int policy = k->correction_policy;
+  const int ntrials = policy == 2 ? 2 : 1;  // policy 2: every vector, then the first vector
+  double ratio[2] = {-1, -1};              // trial: corrected / plain true residual, per correction mode
+  int trials = 0;
+  double res = 0, prev = -1;
+  k->correction_on = k->correction != nullptr;
+  k->plain_cycle = false;
+  for (;;) {
+    double beta;
+    DCHK(true_residual(beta));
+    res = beta / bn;
+    if (!(beta > rtol * bn) || total >= maxit) break;
+    if (k->correction_on && trials == ntrials) {  // after the trials: a stagnating corrected cycle drops it
+      if (prev > 0 && !(beta < 0.99 * prev)) {
+        k->correction_on = false;
+        k->correction_rejects++;
+      }
+    }
+    prev = beta;
+    if (k->correction_on && trials < ntrials) {
+      const int mode = policy == 2 ? trials : policy;
+      double *xs = k->d_trial, *rs = k->d_trial + n, *xp = k->d_trial + 2 * n;
+      CUCHK(cudaMemcpyAsync(xs, x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      CUCHK(cudaMemcpyAsync(rs, V, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      k->plain_cycle = true;  // the plain cycle
+      DCHK(run_cycle(beta));
+      double bp;
+      DCHK(true_residual(bp));
+      CUCHK(cudaMemcpyAsync(xp, x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      double bc = bp;
+      if (bp > rtol * bn && total < maxit) {  // the corrected cycle from the same iterate
+        CUCHK(cudaMemcpyAsync(x, xs, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        CUCHK(cudaMemcpyAsync(V, rs, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        k->plain_cycle = false;
+        k->active_policy = mode;
+        DCHK(run_cycle(beta));
+        DCHK(true_residual(bc));
+        if (!(bc < bp)) CUCHK(cudaMemcpyAsync(x, xp, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        ratio[mode] = std::isfinite(bc) ? bc / bp : 1e300;
+      }
+      k->plain_cycle = false;
+      if (++trials == ntrials) {  // the better mode, or no correction if none beat its plain cycle
+        int best = -1;
+        for (int q = 0; q < 2; q++)
+          if (ratio[q] >= 0 && ratio[q] < 1.0 && (best < 0 || ratio[q] < ratio[best])) best = q;
+        if (best < 0) {
+          k->correction_on = false;
+          k->correction_rejects++;
+        } else {
+          k->active_policy = best;
+        }
+      }
+      prev = -1;  // the stagnation test applies to cycles after the trials
+      continue;   // the next restart recomputes the true residual of the iterate kept
+    }
+    DCHK(run_cycle(beta));
   }
+  k->plain_cycle = false;
   *its = total;
   *rnorm = res;
   return 0;
@@ -837,6 +893,7 @@ dErr dKSPDestroy(dKSP *ksp) {
   cudaFree(k->d_V);
   cudaFree(k->d_Z);
   cudaFree(k->d_h);
+  cudaFree(k->d_trial);
   cudaFree(k->d_w32);
   cudaFree(k->d_dinv32);
   cudaFree(k->d_val32);

@@ -453,7 +453,10 @@ dErr dLearnedApply(dLearned net, const dScalar *r, dScalar *z);
 dErr dKSPSetLearnedCorrection(dKSP ksp, dLearned net);
 /* where the correction is applied: 0 = every preconditioner application, 1 = only to the first vector of
  * each restart cycle (the true residual, the kind of input the network was trained on), 2 = adaptive
- * (default): one cycle with each, then the one whose cycle reduced the residual more */
+ * (default). The plain preconditioner judges it: a trial runs a plain cycle and a corrected cycle (policy 2: one
+ * trial with each placement) from the same iterate and keeps the better iterate; the correction then runs in the
+ * placement that beat the plain cycle by more, or is dropped when none did; a later corrected cycle that reduces
+ * the true residual by less than 1 % drops it too */
 dErr dKSPSetCorrectionPolicy(dKSP ksp, int policy);
 /* the stride-1 convolutions of 16 / 32 channels (and their data and weight gradients) on the tcgen05 tensor
  * cores, with their operands rounded to BF16 (on = 1; the default on the GLL lattice), or every convolution on the

@@ -119,8 +119,8 @@ def test_windows_are_windows_of_the_whole_lattice_pairs():
 
 def test_window_training_and_fgmres():
     """a network trained on 17^3 windows of a 33^3 GLL lattice, applied to the whole lattice inside FGMRES: the
-    loss falls and the FP64 true residual reaches 1e-8 whatever the network does (on this small lattice the
-    window network is dropped by the restart test, as on the 257^3 one)"""
+    loss falls, the FP64 true residual reaches 1e-8 whatever the network does, and the plain preconditioner judges
+    the correction (paired trial cycles from the same iterate)"""
     ne = 8
     fs0, _, _, _ = lognormal(ne, 31)
     net = dg.Learned(fs0, seed=7, grid=GLL, crop=17)
@@ -149,10 +149,11 @@ def test_window_training_and_fgmres():
     assert res["plain"][1] <= 1.01e-8 and res["learned"][1] <= 1.01e-8
     assert net.stats()[0] > 0 and net.stats()[1] == 0
     _, rejects, active = res["learned"][2]
-    if active:  # kept to the end: it must have paid
-        assert res["learned"][0] <= res["plain"][0], res
-    else:  # dropped by the restart test; the cycles it ran with the correction slowed the solve, not stopped it
-        assert rejects >= 1 and res["learned"][0] <= 3 * res["plain"][0], res
+    if active:  # kept: it beat its plain trial cycles; the trials' extra cycles are the price of the judgement
+        assert res["learned"][0] <= res["plain"][0] + 2 * 30, res
+    else:  # dropped after its paired trials against plain cycles, which keep the better iterate: at most the two
+        # corrected trial cycles (and a partial cycle) more than the plain solve
+        assert rejects >= 1 and res["learned"][0] <= res["plain"][0] + 3 * 30, res
 
 
 def test_refusals():
