@@ -514,6 +514,15 @@ dErr fs_build_space(_p_dFS *fs) {
   fs->qoff.assign(m->nr + 1, 0);
   fs->uniform = true;
   fs->p = deg[R0].x;
+  {  // expanded nodes (and Gauss points) times the block size are indexed in 32 bits
+    int64_t ne = 0;
+    for (int64_t r = 0; r < m->nr; r++) {
+      const Ord o = deg[R0 + r];
+      ne += (int64_t)(o.x + 1) * (o.y + 1) * (o.z + 1);
+    }
+    if (ne * std::max(fs->bs, 1) > INT32_MAX)
+      return set_error("space too large for 32-bit indices: %lld expanded values", (long long)(ne * std::max(fs->bs, 1)));
+  }
   for (int64_t r = 0; r < m->nr; r++) {
     const Ord o = deg[R0 + r];
     fs->edeg[3 * r] = o.x, fs->edeg[3 * r + 1] = o.y, fs->edeg[3 * r + 2] = o.z;
