@@ -184,3 +184,9 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
         dg.lib()
     with pytest.raises(dg.DohpError):
         dg.FS((3, 3, 3), degree=2)
+
+
+def test_refuses_spaces_beyond_32_bit_indices():
+    """1e6 degree-8 elements with 3 components: 2.19e9 expanded values, refused before any allocation of that size"""
+    with pytest.raises(dg.DohpError, match="32-bit"):
+        host_fs((101, 101, 101), 8, bs=3)
