@@ -196,3 +196,43 @@ def test_not_an_hdf5_file(L, tmp_path):
     v = ctypes.c_void_p()
     assert L.dViewerDHMOpen(str(bad).encode(), ctypes.c_int(0), ctypes.byref(v)) != 0
     assert b"not an HDF5 file" in L.dGetLastError()
+
+
+def test_damaged_files_are_refused(L, tmp_path):
+    """a flipped byte in the superblock or in an object header fails its checksum, a truncated file is refused; no
+    damaged file is read as data"""
+    path = tmp_path / "ok.dhm"
+    mesh, fs, jac = build_fs(L, (3, 3, 3), 2, 1)
+    u = np.random.default_rng(3).standard_normal(sizes(L, fs)[1])
+    v = ctypes.c_void_p()
+    dg.chk(L.dViewerDHMOpen(str(path).encode(), ctypes.c_int(1), ctypes.byref(v)))
+    dg.chk(L.dFSViewDHM(fs, b"f", v))
+    dg.chk(L.dViewerDHMSetTime(v, ctypes.c_double(0.0)))
+    dg.chk(L.dVecViewDHM(fs, b"u", dg.ptr(u), ctypes.c_int(0), v))
+    dg.chk(L.dViewerDestroy(ctypes.byref(v)))
+    raw = bytearray(path.read_bytes())
+
+    def refused(data, what):
+        bad = tmp_path / "bad.dhm"
+        bad.write_bytes(bytes(data))
+        w = ctypes.c_void_p()
+        if L.dViewerDHMOpen(str(bad).encode(), ctypes.c_int(0), ctypes.byref(w)) != 0:
+            assert what.encode() in L.dGetLastError(), L.dGetLastError()
+            return
+        m2, f2 = ctypes.c_void_p(), ctypes.c_void_p()
+        rc = L.dFSLoadDHM(w, b"f", jac, ctypes.byref(m2), ctypes.byref(f2))
+        L.dViewerDestroy(ctypes.byref(w))
+        assert rc != 0 and what.encode() in L.dGetLastError(), L.dGetLastError()
+
+    sb = bytearray(raw)
+    sb[20] ^= 0xFF  # inside the superblock's addresses
+    refused(sb, "superblock checksum")
+    heads = [i for i in range(len(raw) - 4) if raw[i:i + 4] == b"OHDR"]
+    assert len(heads) > 5
+    for h in heads[:3]:
+        oh = bytearray(raw)
+        oh[h + 12] ^= 0x55  # inside the header's messages
+        refused(oh, "checksum")
+    refused(raw[:len(raw) // 2], "")
+    L.dFSDestroy(ctypes.byref(fs))
+    L.dMeshDestroy(ctypes.byref(mesh))
