@@ -248,6 +248,13 @@ class Mat:
     def mult(self, x, y):
         chk(lib().dMatMult(self.h, ptr(x), ptr(y)))
 
+    def set_values_expanded(self, idxm, idxn, v, imode=ADD_VALUES):
+        """dFSMatSetValuesBlockedExpanded: a block of values in expanded indices (host arrays)"""
+        im, jn = np.ascontiguousarray(idxm, np.int32), np.ascontiguousarray(idxn, np.int32)
+        vv = np.ascontiguousarray(v, np.float64)
+        chk(lib().dFSMatSetValuesBlockedExpanded(self.fs.h, self.h, _i32(len(im)), ptr(im), _i32(len(jn)), ptr(jn), ptr(vv),
+                                                 ctypes.c_int(imode)))
+
 
 class KSP:
     def __init__(self, op, pmat=None, ksp_type=dKSP_CG, pc=dPC_CHEBYSHEV_Q1, cheb_degree=3, inner_prec=dPREC_FP64,

@@ -471,6 +471,92 @@ dErr dMatGetCSRHost(dMat J, dInt *rowptr, dInt *col, dScalar *val) {
   return 0;
 }
 
+}  // extern "C"
+
+namespace {
+// entries of a matrix set or added in the given order by one thread: the order a host loop over them would take, so
+// repeated entries end as PETSc's MatSetValues leaves them (INSERT: the last wins; ADD: summed in order)
+__global__ void k_set_entries(int64_t count, const int64_t *__restrict__ pos, const double *__restrict__ v, int add,
+                              double *__restrict__ val) {
+  if (blockIdx.x || threadIdx.x) return;
+  for (int64_t i = 0; i < count; i++) val[pos[i]] = add ? val[pos[i]] + v[i] : v[i];
+}
+}  // namespace
+
+extern "C" {
+
+// dFSMatSetValuesBlockedExpanded (src/fs/interface/fs.c:826-930): an m x n block of values in expanded (element
+// node) indices, v row-major [m bs][n bs] on the host, expanded through E into the explicit-dof matrix J (rows and
+// columns of Dirichlet nodes dropped, as in the preconditioning matrix): each value becomes
+// E[row][r] * (E[col][c] * v), columns expanded first as the reference does; every target must lie in J's pattern
+// (the Q1-embedded sparsity), else an error. The values change on J's stream; a KSP built on J sees them after
+// dKSPSetOperators, as after a PETSc MatAssembly.
+dErr dFSMatSetValuesBlockedExpanded(dFS fs, dMat J, dInt m, const dInt idxm[], dInt n, const dInt idxn[], const dScalar v[],
+                                    InsertMode imode) {
+  if (!fs || !J || !idxm || !idxn || !v) return set_error("null argument");
+  if (J->fs != fs) return set_error("the matrix belongs to another space");
+  if (imode != INSERT_VALUES && imode != ADD_VALUES) return set_error("InsertMode %d invalid", (int)imode);
+  if (m < 0 || n < 0) return set_error("negative block size");
+  const int bs = fs->bs;
+  if (J->nrows != fs->n * bs) return set_error("matrix rows %lld do not match the space (%lld)", (long long)J->nrows, (long long)fs->n * bs);
+  if (J->h_rowptr.empty()) {
+    J->h_rowptr.resize(J->nrows + 1);
+    J->h_col.resize(J->nnz);
+    CUCHK(cudaMemcpyAsync(J->h_rowptr.data(), J->d_rowptr, (J->nrows + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, fs->stream));
+    if (J->nnz) CUCHK(cudaMemcpyAsync(J->h_col.data(), J->d_col, J->nnz * sizeof(int32_t), cudaMemcpyDeviceToHost, fs->stream));
+    CUCHK(cudaStreamSynchronize(fs->stream));
+  }
+  // one expanded node's E row: (global node, weight) pairs
+  auto erow = [&](int32_t e, std::vector<std::pair<int32_t, double>> &out) -> dErr {
+    out.clear();
+    if (e < 0 || e >= fs->nexp) return set_error("expanded index %d outside [0, %lld)", e, (long long)fs->nexp);
+    if (fs->boolean_e) out.push_back({fs->emap[e], 1.0});
+    else
+      for (int32_t k = fs->eptr[e]; k < fs->eptr[e + 1]; k++) out.push_back({fs->ecol[k], fs->eval[k]});
+    return 0;
+  };
+  std::vector<int64_t> pos;
+  std::vector<double> val;
+  std::vector<std::pair<int32_t, double>> er, ec;
+  for (dInt i = 0; i < m; i++) {
+    DCHK(erow(idxm[i], er));
+    for (const auto &r : er) {
+      if (r.first >= fs->n) continue;  // a Dirichlet node: no row of the preconditioning matrix
+      for (int a = 0; a < bs; a++) {
+        const int64_t row = (int64_t)r.first * bs + a;
+        const int32_t *c0 = J->h_col.data() + J->h_rowptr[row], *c1 = J->h_col.data() + J->h_rowptr[row + 1];
+        for (dInt j = 0; j < n; j++) {
+          DCHK(erow(idxn[j], ec));
+          for (const auto &c : ec) {
+            if (c.first >= fs->n) continue;
+            for (int b = 0; b < bs; b++) {
+              const int32_t col = c.first * bs + b;
+              const int32_t *hit = std::find(c0, c1, col);
+              if (hit == c1) return set_error("entry (%lld, %d) is not in the matrix's sparsity pattern", (long long)row, col);
+              pos.push_back(hit - J->h_col.data());
+              val.push_back(r.second * (c.second * v[((int64_t)(i * bs + a) * n + j) * bs + b]));
+            }
+          }
+        }
+      }
+    }
+  }
+  if (pos.empty()) return 0;
+  int64_t *dpos;
+  double *dval;
+  CUCHK(cudaMallocAsync(&dpos, pos.size() * sizeof(int64_t), fs->stream));
+  CUCHK(cudaMallocAsync(&dval, val.size() * sizeof(double), fs->stream));
+  CUCHK(cudaMemcpyAsync(dpos, pos.data(), pos.size() * sizeof(int64_t), cudaMemcpyHostToDevice, fs->stream));
+  CUCHK(cudaMemcpyAsync(dval, val.data(), val.size() * sizeof(double), cudaMemcpyHostToDevice, fs->stream));
+  k_set_entries<<<1, 1, 0, fs->stream>>>((int64_t)pos.size(), dpos, dval, imode == ADD_VALUES, J->d_val);
+  CUCHK(cudaGetLastError());
+  CUCHK(cudaFreeAsync(dpos, fs->stream));
+  CUCHK(cudaFreeAsync(dval, fs->stream));
+  CUCHK(cudaStreamSynchronize(fs->stream));  // the host vectors above must outlive their copies
+  J->sell_valid = false;
+  return 0;
+}
+
 dErr dMatMult(dMat J, const dScalar *x, dScalar *y) {
   if (!J) return set_error("null matrix");
   return mat_mult(J, x, y, J->fs->stream);

@@ -165,6 +165,8 @@ struct _p_dMat {
   int32_t *d_sell_col = nullptr;
   double *d_sell_val = nullptr;
   bool sell_valid = false;
+  // host copy of the CSR pattern (dFSMatSetValuesBlockedExpanded locates its entries on the host)
+  std::vector<int32_t> h_rowptr, h_col;
 };
 
 dErr mat_sell(_p_dMat *J, cudaStream_t s);

@@ -398,6 +398,12 @@ dErr dFSAssembleQ1(dFS fs, dMat J, dOperatorKind kind, const dReal *param, const
 /* EllipJacobian (ellip.c:474-536): the Q1-embedded p-Laplacian Jacobian at the state g (device vector),
  * store at every SPARSE point from the state's gradient there; scalar uniform-order spaces */
 dErr dFSAssembleQ1PLaplace(dFS fs, dMat J, const dScalar *g, dReal p, dReal eps, int reference_quirk);
+/* dFSMatSetValuesBlockedExpanded (src/fs/interface/fs.c:826-930): an element block of values in expanded indices
+ * (host arrays; v row-major [m bs][n bs]) expanded through E into J's explicit-dof rows and columns (Dirichlet nodes
+ * dropped), INSERT_VALUES or ADD_VALUES; targets outside J's Q1-embedded pattern are an error. A KSP on J sees the new
+ * values after dKSPSetOperators. */
+dErr dFSMatSetValuesBlockedExpanded(dFS fs, dMat J, dInt m, const dInt idxm[], dInt n, const dInt idxn[], const dScalar v[],
+                                    InsertMode imode);
 dErr dMatGetCSR(dMat J, dInt *nrows, int64_t *nnz, const dInt **rowptr, const dInt **col, const dScalar **val);
 dErr dMatMult(dMat J, const dScalar *x, dScalar *y);
 /* host copies of the CSR arrays (rowptr nrows+1, col nnz, val nnz) */
