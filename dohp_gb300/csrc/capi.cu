@@ -64,72 +64,82 @@ __device__ void tmult(int D, const int P[3], const int Q[3], const double *const
 // contiguous (element b at b * np nodes, b * nq points) unless an element list with node / point offsets is
 // given (the elements of one order in a mixed-order space: elist[b] = e, ioff[e] / ooff[e] = the element's first
 // input / output node or point)
+// components [c0, c0 + Dk) of element b's values: value k of node (or point) i of a slice is global entry
+// (base + i) D + c0 + k (with Dk = D the contiguous block of the element); elements too large for all D components in
+// shared memory run one component per pass
 __global__ void k_efs_apply(EFSDev f, int64_t nelem, const int32_t *elist, const int32_t *ioff, const int32_t *ooff,
-                            const double *jinv, int D, const double *in, double *out, int amode, int imode) {
+                            const double *jinv, int D, int Dk, const double *in, double *out, int amode, int imode) {
   extern __shared__ double sm[];
   const int64_t b = blockIdx.x;
   if (b >= nelem) return;
   const int64_t e = elist ? elist[b] : b;
   const int P[3] = {f.P[0], f.P[1], f.P[2]}, Q[3] = {f.Q[0], f.Q[1], f.Q[2]};
-  const int np = P[0] * P[1] * P[2], nq = Q[0] * Q[1] * Q[2], mx = max(np, nq) * D;
+  const int np = P[0] * P[1] * P[2], nq = Q[0] * Q[1] * Q[2];
   const bool fwd = amode == dAPPLY_INTERP || amode == dAPPLY_GRAD;
   const int64_t ib = ioff ? (int64_t)ioff[e] : e * (fwd ? np : nq), ob = ooff ? (int64_t)ooff[e] : e * (fwd ? nq : np);
   const int64_t qb = fwd ? ob : ib;  // first quadrature point of the element
-  // generous scratch: each buffer holds max(P,Q)^3 * D
+  // generous scratch: each buffer holds max(P,Q)^3 * Dk
   const int m3 = max(max(P[0], Q[0]), max(max(P[1], Q[1]), max(P[2], Q[2])));
-  const int buf = m3 * m3 * m3 * D;
+  const int buf = m3 * m3 * m3 * Dk;
   double *sin = sm, *t1 = sm + buf, *t2 = sm + 2 * buf, *g = sm + 3 * buf;  // g: 3 gradient buffers
-  (void)mx;
   const bool add = imode == ADD_VALUES;
   const double *Jq = jinv ? jinv + qb * 9 : nullptr;
-  if (fwd) {
-    for (int t = threadIdx.x; t < np * D; t += blockDim.x) sin[t] = in[ib * D + t];
-    __syncthreads();
-    if (amode == dAPPLY_INTERP) {
-      double *o = out + ob * D;
-      const double *A[3] = {f.B[0], f.B[1], f.B[2]};
-      // write through shared then copy so that ADD semantics apply to global memory
-      tmult(D, P, Q, A, 0, sin, t1, t2, g, false);
-      for (int t = threadIdx.x; t < nq * D; t += blockDim.x) o[t] = add ? o[t] + g[t] : g[t];
-    } else {
-      for (int dir = 0; dir < 3; dir++) {
-        const double *A[3] = {dir == 0 ? f.D[0] : f.B[0], dir == 1 ? f.D[1] : f.B[1], dir == 2 ? f.D[2] : f.B[2]};
-        tmult(D, P, Q, A, 0, sin, t1, t2, g + dir * buf, false);
-      }
-      double *o = out + ob * D * 3;
-      for (int t = threadIdx.x; t < nq * D; t += blockDim.x) {
-        const int q = t / D;
-        double gr[3] = {g[t], g[buf + t], g[2 * buf + t]};
-        for (int c = 0; c < 3; c++) {
-          double v = Jq ? gr[0] * Jq[q * 9 + 0 * 3 + c] + gr[1] * Jq[q * 9 + 1 * 3 + c] + gr[2] * Jq[q * 9 + 2 * 3 + c] : gr[c];
-          o[t * 3 + c] = add ? o[t * 3 + c] + v : v;
+  auto gidx = [&](int64_t base, int t, int c0) { return (base + t / Dk) * D + c0 + t % Dk; };
+  for (int c0 = 0; c0 < D; c0 += Dk) {
+    if (fwd) {
+      for (int t = threadIdx.x; t < np * Dk; t += blockDim.x) sin[t] = in[gidx(ib, t, c0)];
+      __syncthreads();
+      if (amode == dAPPLY_INTERP) {
+        // write through shared then copy so that ADD semantics apply to global memory
+        const double *A[3] = {f.B[0], f.B[1], f.B[2]};
+        tmult(Dk, P, Q, A, 0, sin, t1, t2, g, false);
+        for (int t = threadIdx.x; t < nq * Dk; t += blockDim.x) {
+          double *o = out + gidx(ob, t, c0);
+          *o = add ? *o + g[t] : g[t];
+        }
+      } else {
+        for (int dir = 0; dir < 3; dir++) {
+          const double *A[3] = {dir == 0 ? f.D[0] : f.B[0], dir == 1 ? f.D[1] : f.B[1], dir == 2 ? f.D[2] : f.B[2]};
+          tmult(Dk, P, Q, A, 0, sin, t1, t2, g + dir * buf, false);
+        }
+        for (int t = threadIdx.x; t < nq * Dk; t += blockDim.x) {
+          const int q = t / Dk;
+          double *o = out + gidx(ob, t, c0) * 3;
+          double gr[3] = {g[t], g[buf + t], g[2 * buf + t]};
+          for (int c = 0; c < 3; c++) {
+            double v = Jq ? gr[0] * Jq[q * 9 + 0 * 3 + c] + gr[1] * Jq[q * 9 + 1 * 3 + c] + gr[2] * Jq[q * 9 + 2 * 3 + c] : gr[c];
+            o[c] = add ? o[c] + v : v;
+          }
         }
       }
-    }
-  } else {
-    if (amode == dAPPLY_INTERP_TRANSPOSE) {
-      for (int t = threadIdx.x; t < nq * D; t += blockDim.x) sin[t] = in[ib * D + t];
-      __syncthreads();
-      const double *A[3] = {f.B[0], f.B[1], f.B[2]};
-      tmult(D, Q, P, A, 1, sin, t1, t2, g, false);
-    } else {  // GRAD_TRANSPOSE: map with jinv^T then three transposed contractions accumulated
-      for (int t = threadIdx.x; t < nq * D; t += blockDim.x) {
-        const int q = t / D;
-        const double *v = in + (ib * D + t) * 3;
-        for (int dir = 0; dir < 3; dir++)
-          g[dir * buf + t] = Jq ? v[0] * Jq[q * 9 + dir * 3 + 0] + v[1] * Jq[q * 9 + dir * 3 + 1] + v[2] * Jq[q * 9 + dir * 3 + 2] : v[dir];
+    } else {
+      if (amode == dAPPLY_INTERP_TRANSPOSE) {
+        for (int t = threadIdx.x; t < nq * Dk; t += blockDim.x) sin[t] = in[gidx(ib, t, c0)];
+        __syncthreads();
+        const double *A[3] = {f.B[0], f.B[1], f.B[2]};
+        tmult(Dk, Q, P, A, 1, sin, t1, t2, g, false);
+      } else {  // GRAD_TRANSPOSE: map with jinv^T then three transposed contractions accumulated
+        for (int t = threadIdx.x; t < nq * Dk; t += blockDim.x) {
+          const int q = t / Dk;
+          const double *v = in + gidx(ib, t, c0) * 3;
+          for (int dir = 0; dir < 3; dir++)
+            g[dir * buf + t] = Jq ? v[0] * Jq[q * 9 + dir * 3 + 0] + v[1] * Jq[q * 9 + dir * 3 + 1] + v[2] * Jq[q * 9 + dir * 3 + 2] : v[dir];
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < np * Dk; t += blockDim.x) sin[t] = 0;
+        __syncthreads();
+        for (int dir = 0; dir < 3; dir++) {
+          const double *A[3] = {dir == 0 ? f.D[0] : f.B[0], dir == 1 ? f.D[1] : f.B[1], dir == 2 ? f.D[2] : f.B[2]};
+          tmult(Dk, Q, P, A, 1, g + dir * buf, t1, t2, sin, true);
+        }
       }
-      __syncthreads();
-      for (int t = threadIdx.x; t < np * D; t += blockDim.x) sin[t] = 0;
-      __syncthreads();
-      for (int dir = 0; dir < 3; dir++) {
-        const double *A[3] = {dir == 0 ? f.D[0] : f.B[0], dir == 1 ? f.D[1] : f.B[1], dir == 2 ? f.D[2] : f.B[2]};
-        tmult(D, Q, P, A, 1, g + dir * buf, t1, t2, sin, true);
+      const double *src = amode == dAPPLY_INTERP_TRANSPOSE ? g : sin;
+      for (int t = threadIdx.x; t < np * Dk; t += blockDim.x) {
+        double *o = out + gidx(ob, t, c0);
+        *o = add ? *o + src[t] : src[t];
       }
     }
-    double *o = out + ob * D;
-    const double *src = amode == dAPPLY_INTERP_TRANSPOSE ? g : sin;
-    for (int t = threadIdx.x; t < np * D; t += blockDim.x) o[t] = add ? o[t] + src[t] : src[t];
+    __syncthreads();  // the next slice reuses the buffers
   }
 }
 
@@ -159,10 +169,12 @@ dErr efs_apply_list(dEFS efs, int64_t nelem, const int32_t *elist, const int32_t
   }
   int m3 = 0;
   for (int d = 0; d < 3; d++) m3 = std::max(m3, std::max(f.P[d], f.Q[d]));
-  const size_t smem = 6ull * m3 * m3 * m3 * D * sizeof(double);
+  // all D components at once when they fit in shared memory, else one component per pass
+  const int Dk = 6ull * m3 * m3 * m3 * D * sizeof(double) <= 220 * 1024 ? D : 1;
+  const size_t smem = 6ull * m3 * m3 * m3 * Dk * sizeof(double);
   if (smem > 220 * 1024) return set_error("element too large for the batched apply (%zu bytes of shared memory)", smem);
   CUCHK(cudaFuncSetAttribute(k_efs_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_efs_apply<<<(unsigned)nelem, 256, smem, stream>>>(f, nelem, elist, ioff, ooff, jinv, D, in, out, (int)amode, (int)imode);
+  k_efs_apply<<<(unsigned)nelem, 256, smem, stream>>>(f, nelem, elist, ioff, ooff, jinv, D, Dk, in, out, (int)amode, (int)imode);
   CUCHK(cudaGetLastError());
   return 0;
 }

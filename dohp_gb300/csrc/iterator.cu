@@ -9,9 +9,10 @@
 // Start and NextPatch ends the loop, so the reference's while loop runs its body once. Arrays are element-natural
 // per element, elements back to back (element e's points start at the ruleset's point offset of e), and every
 // evaluation is one batched dEFSApply launch per group of elements that share their rule and the link's basis
-// orders (one launch per link on a uniform-order space). FAST rules on any space; on uniform-order spaces the
-// SPARSE rule (2 Gauss points in each GLL sub-interval, (2p)^3 points per element in tensor order: the p^3
-// patches of the reference's patch loop are the 2 x 2 x 2 blocks of it). The stash (AddStash / GetStash,
+// orders (one launch per link on a uniform-order space). FAST and SPARSE rules on any space, each element with the
+// rule of its own orders; the SPARSE rule has 2 Gauss points in each GLL sub-interval, (2p)^3 points per element in
+// tensor order: the p^3 patches of the reference's patch loop are the 2 x 2 x 2 blocks of it (patch bases on
+// uniform-order spaces). The stash (AddStash / GetStash,
 // fsrulesetit.c:779-798) is device memory: elembytes per element and nodebytes per point, for all elements.
 #include <stdarg.h>
 
@@ -240,8 +241,6 @@ dErr iterator_add_link(_p_dRulesetIterator *it, dFS fs, bool coords) {
   if (!fs->jac) return set_error("dRulesetIteratorAddFS: dFS was created without a dJacobi");
   if (fs->mesh != it->rset->fs->mesh) return set_error("dRulesetIteratorAddFS: the space lives on another mesh than the ruleset");
   if (it->started) return set_error("dRulesetIteratorAddFS: the iterator is in a traversal (Finish first)");
-  if (it->rset->method == dQUADRATURE_METHOD_SPARSE && !coords && !fs->uniform)
-    return set_error("SPARSE rules need uniform-order spaces");
   ItLink L;
   L.fs = fs;
   L.bs = coords ? 3 : fs->bs;
@@ -265,7 +264,6 @@ dErr dFSGetPreferredQuadratureRuleSet(dFS fs, dQuadratureMethod method, dRuleset
   if (!fs->jac) return set_error("dFS was created without a dJacobi");
   if (method != dQUADRATURE_METHOD_FAST && method != dQUADRATURE_METHOD_SPARSE)
     return set_error("dFSGetPreferredQuadratureRuleSet: FAST and SPARSE rules");
-  if (method == dQUADRATURE_METHOD_SPARSE && !fs->uniform) return set_error("SPARSE rulesets need a uniform-order space");
   _p_dRuleset *R = new _p_dRuleset();
   R->fs = fs;
   R->method = method;
@@ -569,6 +567,10 @@ dErr dRulesetIteratorGetPatchAssembly(dRulesetIterator it, dInt *P, const dInt *
     ItLink &L = it->links[i];
     if (L.coords) {
       err = set_error("dRulesetIteratorGetPatchAssembly: the coordinate link has no patch bases here (pass NULL for link 0)");
+      break;
+    }
+    if (!L.fs->uniform || !R->fs->uniform) {
+      err = set_error("dRulesetIteratorGetPatchAssembly: link %d: patch bases need uniform-order spaces", (int)i);
       break;
     }
     const int px = L.fs->p, py = px, pz = px;

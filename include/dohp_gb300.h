@@ -274,7 +274,7 @@ dErr dOperatorMultHost(dOperator op, const dScalar *x_host, dScalar *y_host);
  * repeat the per-link arguments for links 1.. exactly as in dohp. */
 typedef struct _p_dRuleset *dRuleset;
 /* dFSGetPreferredQuadratureRuleSet (include/dohpfs.h:97): the rules of the space's elements (order 2p per direction,
- * fsruleset.c:32-37) for FAST, or SPARSE on uniform-order spaces; over all regions of the mesh */
+ * fsruleset.c:32-37), FAST or SPARSE, each element with the rule of its own orders; over all regions of the mesh */
 dErr dFSGetPreferredQuadratureRuleSet(dFS fs, dQuadratureMethod method, dRuleset *rset);
 dErr dRulesetGetSize(dRuleset rset, dInt *size);
 /* total points and the host array of per-element point offsets [nelem+1] (owned by the ruleset) */
@@ -308,7 +308,8 @@ dErr dRulesetIteratorGetPatchApplied(dRulesetIterator it, dInt *Q, const dReal *
 /* dRulesetIteratorCommitPatchApplied (fsrulesetit.c:595-643): per link (v, dv) as returned by GetPatchApplied or NULL;
  * integrates v (INTERP_TRANSPOSE) and dv (GRAD_TRANSPOSE) into the link's expanded test vector (imode per element) */
 dErr dRulesetIteratorCommitPatchApplied(dRulesetIterator it, InsertMode imode, const dScalar *v, const dScalar *dv, ...);
-/* dRulesetIteratorGetPatchAssembly (fsrulesetit.c:657-701), SPARSE rulesets, after GetPatchApplied: per link (P, rowcol,
+/* dRulesetIteratorGetPatchAssembly (fsrulesetit.c:657-701), SPARSE rulesets on uniform-order spaces (an error on mixed
+ * orders), after GetPatchApplied: per link (P, rowcol,
  * interp, deriv), NULL for link 0: the Q1 sub-cell bases of every patch of every element (dEFSGetExplicitSparse,
  * efstopo.c:660-717, the inverse Jacobian read at the reference's patch-natural index): P = 8, device arrays rowcol
  * [nelem*p^3][8] (expanded node indices), interp [nelem*p^3][8][8], deriv [nelem*p^3][8][8][3], patches element-major in

@@ -1,6 +1,7 @@
 """Batched dRulesetIterator: a q-function written in torch between GetPatchApplied and CommitPatchApplied
 reproduces the fused operator applies and the oracle (src/fs/interface/fsrulesetit.c, the Start /
 GetPatchApplied / CommitPatchApplied / Finish cycle used by src/fs/tests/elast.c and src/fs/tests/ellip.c)."""
+import ctypes
 import os
 
 import numpy as np
@@ -114,9 +115,6 @@ def test_errors():
     fs = dg.FS((3, 3, 3), degree=2, seed=1)
     with pytest.raises(dg.DohpError):
         dg.RulesetIterator(fs, method=dg.SELF)
-    ed = np.random.default_rng(0).integers(2, 4, size=8).astype(np.int32)
-    with pytest.raises(dg.DohpError):  # SPARSE on mixed orders
-        dg.RulesetIterator(dg.FS((3, 3, 3), degree=2, seed=1, elem_degree=ed), method=dg.SPARSE)
     it = dg.RulesetIterator(fs)
     with pytest.raises(dg.DohpError):
         it.get()
@@ -207,30 +205,33 @@ def test_error_norms_of_an_exactly_represented_solution():
     assert ue[2] < 1e-15 and ge[2] < 1e-13 and ue[1] < 1e-15
 
 
-@pytest.mark.parametrize("p", [2, 3, 4])
-def test_sparse_rule_iterator(p):
+@pytest.mark.parametrize("p,bs", [(2, 1), (3, 1), (4, 1), (6, 3)])
+def test_sparse_rule_iterator(p, bs):
     """SPARSE rule (2 Gauss points per GLL sub-interval, (2p)^3 per element): the mesh volume on a perturbed mesh
-    (the trilinear det J is integrated exactly), and on an affine mesh the integrals of u^2 and |grad u|^2 of a
-    linear field agree with the FAST rule's (both rules are exact there); the stiffness energy identity holds"""
+    (the trilinear det J is integrated exactly), and on an affine mesh the integrals of |u|^2 and |grad u|^2 of a
+    linear field agree with the FAST rule's (both rules are exact there); the stiffness energy identity holds.
+    Degree 6 with three components: 12^3 points per element, applied one component at a time."""
     npts = (4, 3, 5)
-    fs = dg.FS(npts, degree=p, perturb=0.1, seed=p)
+    fs = dg.FS(npts, degree=p, perturb=0.1, seed=p, bs=bs)
     it = dg.RulesetIterator(fs, method=dg.SPARSE)
     it.start(None)
     a = it.get()
     assert a["jw"].numel() == fs.nelem * (2 * p) ** 3
     assert abs(float(a["jw"].sum()) - 1.0) < 1e-13
     o = po.FS(*npts, degree=p, perturb=0.0, seed=p, dirichlet_mask=0)
-    fs = dg.FS(npts, degree=p, perturb=0.0, seed=p, dirichlet=())
+    fs = dg.FS(npts, degree=p, perturb=0.0, seed=p, dirichlet=(), bs=bs)
     em, xs, ce = o.emap(), o.xstart(), o.coords_expanded()
     gll = po.lobatto(p + 1)[0]
-    f = lambda X: 0.3 * X[0] - 1.1 * X[1] + 0.7 * X[2] + 0.2
-    g = np.zeros(fs.n)
+    coef = np.array([[0.3, -1.1, 0.7, 0.2], [-0.4, 0.5, 0.9, -0.1], [1.3, 0.2, -0.6, 0.4]])[:bs]
+    f = lambda X: np.stack([c[0] * X[0] + c[1] * X[1] + c[2] * X[2] + c[3] for c in coef], -1)
+    g = np.zeros(fs.n * bs)
     P = p + 1
     for e in range(o.nelem):
         lo, hi = ce[e].min(0), ce[e].max(0)
         for loc in range(P ** 3):
             ijk = (loc // (P * P), (loc // P) % P, loc % P)
-            g[em[xs[e] + loc]] = f([lo[k] + (1 + gll[ijk[k]]) / 2 * (hi[k] - lo[k]) for k in range(3)])
+            node = em[xs[e] + loc]
+            g[node * bs:(node + 1) * bs] = f([lo[k] + (1 + gll[ijk[k]]) / 2 * (hi[k] - lo[k]) for k in range(3)])
     vals = {}
     for m in (dg.FAST, dg.SPARSE):
         it = dg.RulesetIterator(fs, method=m)
@@ -238,11 +239,59 @@ def test_sparse_rule_iterator(p):
         a = it.get()
         vals[m] = (float((a["jw"][:, None] * a["u"] ** 2).sum()), float((a["jw"][:, None, None] * a["du"] ** 2).sum()))
         if m == dg.SPARSE:
-            np.testing.assert_allclose(a["u"][:, 0].cpu().numpy(), f(a["x"].cpu().numpy().T), rtol=0, atol=1e-13)
+            np.testing.assert_allclose(a["u"].cpu().numpy(), f(a["x"].cpu().numpy().T), rtol=0, atol=1e-13)
             a["dv"].copy_(a["jw"][:, None, None] * a["du"])
             it.commit(dg.INSERT_VALUES, use_v=False, use_dv=True)
-            y = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
+            y = torch.zeros(fs.n * bs, dtype=torch.float64, device="cuda")
             it.finish(y)
             torch.cuda.synchronize()
             assert abs(g @ y.cpu().numpy() - vals[m][1]) < 1e-12 * abs(vals[m][1])
     np.testing.assert_allclose(vals[dg.SPARSE], vals[dg.FAST], rtol=1e-13)
+
+
+@pytest.mark.parametrize("bs", [1, 3])
+def test_sparse_rule_mixed_orders(bs):
+    """SPARSE rules on a mixed-order space (per-element degrees 1..6, each element with the SPARSE rule of its own
+    orders, as fsruleset.c:30-36 asks element by element): weights, values and gradients at every element's points
+    against the oracle's tensor contraction with that element's SPARSE points and basis, the mesh volume, and the
+    refusal of patch assembly (its patches are the sub-cells of one degree)"""
+    npts = (4, 3, 5)
+    ne = 3 * 2 * 4
+    ed = np.random.default_rng(7 + bs).integers(1, 7, size=ne).astype(np.int32)
+    fs = dg.FS(npts, degree=3, perturb=0.1, seed=3, bs=bs, elem_degree=ed, dirichlet=())
+    g = torch.as_tensor(np.random.default_rng(bs).uniform(-1, 1, fs.n * bs), device="cuda")
+    it = dg.RulesetIterator(fs, method=dg.SPARSE)
+    it.start(g)
+    a = it.get()
+    qe = (2 * ed.astype(np.int64)) ** 3
+    assert a["jw"].numel() == int(qe.sum())
+    assert abs(float(a["jw"].sum()) - 1.0) < 1e-13
+    xexp = torch.zeros(fs.nexp * bs, dtype=torch.float64, device="cuda")
+    fs.global_to_expanded(g, xexp)
+    torch.cuda.synchronize()
+    xexp = xexp.cpu().numpy()
+    _, xs = fs.emap()
+    u, du, dx, jw = (a[k].cpu().numpy() for k in ("u", "du", "dx", "jw"))
+    qoff = np.concatenate([[0], np.cumsum(qe)])
+    efs_of = {}
+    for e in range(ne):
+        p = int(ed[e])
+        if p not in efs_of:
+            efs = fs.jac.efs(p, method=dg.SPARSE)
+            assert efs.Q == [2 * p] * 3
+            x1, w1 = efs.points[:2 * p], efs.weights[:2 * p]
+            interp, deriv, _, _ = po.tensor_basis(p + 1, x1)
+            efs_of[p] = (interp, deriv, np.einsum("i,j,k->ijk", w1, w1, w1).ravel())
+        interp, deriv, w = efs_of[p]
+        q = slice(qoff[e], qoff[e + 1])
+        jinv = np.linalg.inv(dx[q])
+        np.testing.assert_allclose(jw[q], w * np.linalg.det(dx[q]), rtol=1e-13, atol=0)
+        xe = xexp[xs[e] * bs:(xs[e] + (p + 1) ** 3) * bs]
+        for amode, got in ((dg.dAPPLY_INTERP, u[q]), (dg.dAPPLY_GRAD, du[q])):
+            ref = po.efs_apply_hex([p + 1] * 3, [2 * p] * 3, [interp] * 3, [deriv] * 3, jinv.ravel(), bs, xe, amode)
+            assert np.linalg.norm(got.ravel() - ref) <= 1e-13 * np.linalg.norm(ref), (e, p, amode)
+    L = dg.lib()
+    P, rc, bi, bd = ctypes.c_int32(), ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    NULL = ctypes.c_void_p(0)
+    assert L.dRulesetIteratorGetPatchAssembly(it.h, NULL, NULL, NULL, NULL, ctypes.byref(P), ctypes.byref(rc), ctypes.byref(bi),
+                                              ctypes.byref(bd)) != 0

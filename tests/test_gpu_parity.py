@@ -180,14 +180,19 @@ def test_cg_chebyshev_q1_reaches_rtol():
 INTERP, INTERP_T, GRAD, GRAD_T = 40001, 40002, 40003, 40004
 
 
-@pytest.mark.parametrize("degree,D", [(1, 1), (3, 1), (4, 3), (7, 1), (8, 3)])
-def test_efs_apply_batched(degree, D):
+# (6, 3, 22) and (8, 3, 30): 12 and 16 points per direction, too many for all three components' buffers in shared
+# memory at once, so the kernel runs one component per pass
+@pytest.mark.parametrize("degree,D,order", [(1, 1, None), (3, 1, None), (4, 3, None), (7, 1, None), (8, 3, None),
+                                            (6, 3, 22), (8, 3, 30)])
+def test_efs_apply_batched(degree, D, order):
+    order = order or 2 * degree
     jac = dg.Jacobi()
-    efs = jac.efs(degree)
+    efs = jac.efs(degree, rule_order=[order] * 3)
     P, Q = efs.P, efs.Q
     nb, nq, ne = int(np.prod(P)), int(np.prod(Q)), 5
     rng = np.random.default_rng(degree)
-    x, _ = po.rule_1d(0, 0, 2 * degree)
+    x, _ = po.rule_1d(0, 0, order)
+    assert Q == [len(x)] * 3
     interp, deriv, _, _ = po.tensor_basis(degree + 1, x)
     jinv = rng.standard_normal((ne, nq, 9))
     for amode, nin, nout in [(INTERP, nb * D, nq * D), (GRAD, nb * D, nq * D * 3), (INTERP_T, nq * D, nb * D), (GRAD_T, nq * D * 3, nb * D)]:
