@@ -491,7 +491,8 @@ def secondary_newton(args):
 
 def multigrid_solves(fs, op, m, b):
     """the Q1 multigrid preconditioner on a lognormal problem (no network): CG with FP64 applies, and FGMRES with
-    FP32 inner applies; the V-cycle is FP64 in both. Set-up (hierarchy, eigenvalue estimates) is timed apart."""
+    FP32 inner applies; the V-cycle runs in the preconditioner's precision (FP64 under CG, FP32 inside the FGMRES).
+    Set-up (hierarchy, eigenvalue estimates) is timed apart."""
     import torch
     import dohp_gb300 as dg
     out = {}
@@ -537,26 +538,6 @@ def secondary_multigrid(args):
     b = torch.as_tensor(np.random.default_rng(5000).uniform(-1, 1, fs.n), device="cuda")
     out = {"workload": "lognormal-poisson-%d^3-p4, Q1 multigrid" % ne, "dofs": fs.n, "rtol": 1e-8}
     out.update(multigrid_solves(fs, op, m, b))
-    if "vertex" in nets:  # the network added to the multigrid preconditioner (trained on Chebyshev-Jacobi pairs)
-        ksp = dg.KSP(op, m, ksp_type=dg.dKSP_FGMRES, inner_prec=dg.dPREC_FP32, restart=30, pc=dg.dPC_MG_Q1)
-        ksp.set_learned(nets["vertex"])
-        x = torch.zeros(fs.n, dtype=torch.float64, device="cuda")
-        try:  # set-up outside the timed solve, as the multigrid legs
-            ksp.solve(b, x, rtol=1e-1, maxit=50)
-        except dg.DohpError:
-            pass
-        x.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        its, _ = ksp.solve(b, x, rtol=1e-8, maxit=2000)
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-        r = torch.empty_like(x)
-        op.mult(x, r)
-        applies, rejects, active = ksp.stats()
-        out["learned_multigrid_mixed"] = {"its": its, "wall_s": wall,
-                                          "true_rel_residual": float(torch.linalg.norm(b - r) / torch.linalg.norm(b)),
-                                          "correction_dropped": bool(rejects), "correction_active_at_end": active}
     return out
 
 

@@ -5,6 +5,7 @@
     python -m dohp_gb300.workloads unet-train --ne 64 --batch 16         # loss + gradient steps on the vertex lattice
     python -m dohp_gb300.workloads cg --ne 8                             # Poisson CG + Q1 Chebyshev(3)-Jacobi to 1e-8
     python -m dohp_gb300.workloads fgmres --ne 64 --precision fp32       # 2 restart cycles, lognormal Poisson
+    python -m dohp_gb300.workloads fgmres --ne 64 --precision fp32 --pc mg   # the same with the Q1 multigrid V-cycle
 
 Seeded random inputs and weights; each workload runs --reps passes after one warm-up pass and prints one JSON line
 with the mean time per pass (CUDA events)."""
@@ -26,6 +27,7 @@ def main(argv=None):
     ap.add_argument("--batch", type=int, default=1)
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--tensor-cores", type=int, default=-1, help="1 on, 0 off, -1 the lattice's default")
+    ap.add_argument("--pc", choices=["cheb", "mg"], default="cheb", help="fgmres workload: Q1 Chebyshev(3)-Jacobi or Q1 multigrid")
     a = ap.parse_args(argv)
     torch.cuda.set_device(0)
     fs = dg.FS((a.ne + 1,) * 3, degree=a.degree, perturb=0.1, seed=1)
@@ -89,8 +91,9 @@ def cg(fs, a):
 
 
 def fgmres(fs, a):
-    """FGMRES(30) with the Q1 Chebyshev(3)-Jacobi preconditioner and inner applies in --precision on the lognormal
-    Poisson problem (field seed 5000), two restart cycles (60 iterations) after one warm-up cycle: ms per iteration"""
+    """FGMRES(30) with the Q1 Chebyshev(3)-Jacobi preconditioner (or the Q1 multigrid V-cycle, --pc mg) and inner
+    applies in --precision on the lognormal Poisson problem (field seed 5000), two restart cycles (at most 60
+    iterations, fewer when rtol 1e-12 comes first) after one warm-up cycle: ms per iteration"""
     grf = dg.grf_create(64, 2.0, 0.1, 5000)
     kq = torch.empty(fs.nq, dtype=torch.float64, device="cuda")
     fs.lognormal(grf, kq)
@@ -99,7 +102,8 @@ def fgmres(fs, a):
     m = fs.matrix()
     m.assemble(grf=grf)
     prec = {"fp64": dg.dPREC_FP64, "fp32": dg.dPREC_FP32, "bf16": dg.dPREC_BF16, "ff": dg.dPREC_FF}[a.precision]
-    ksp = dg.KSP(op, m, ksp_type=dg.dKSP_FGMRES, inner_prec=prec, restart=30)
+    pc = dg.dPC_MG_Q1 if a.pc == "mg" else dg.dPC_CHEBYSHEV_Q1
+    ksp = dg.KSP(op, m, ksp_type=dg.dKSP_FGMRES, inner_prec=prec, restart=30, pc=pc)
     gen = torch.Generator(device="cuda").manual_seed(5)
     b = torch.rand(fs.n, dtype=torch.float64, device="cuda", generator=gen) * 2 - 1
     x = torch.zeros_like(b)
@@ -107,18 +111,18 @@ def fgmres(fs, a):
     def cycles(k):
         x.zero_()
         try:  # stops at maxit before the tolerance: reported as an error
-            ksp.solve(b, x, rtol=1e-12, maxit=30 * k)
+            return ksp.solve(b, x, rtol=1e-12, maxit=30 * k)[0]
         except dg.DohpError:
-            pass
+            return 30 * k
 
     cycles(1)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    cycles(2)
+    its = cycles(2)
     e1.record()
     torch.cuda.synchronize()
-    print(json.dumps({"workload": "fgmres", "elements": a.ne ** 3, "dofs": fs.n, "precision": a.precision,
-                      "ms_per_iteration": e0.elapsed_time(e1) / 60}))
+    print(json.dumps({"workload": "fgmres", "elements": a.ne ** 3, "dofs": fs.n, "precision": a.precision, "pc": a.pc,
+                      "iterations": its, "ms_per_iteration": e0.elapsed_time(e1) / its}))
 
 
 def run(step, a, info):

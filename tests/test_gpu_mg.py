@@ -75,6 +75,24 @@ def test_lognormal_fgmres():
     assert its_m <= its_c // 4, (its_m, its_c)
 
 
+def test_fp32_cycle_on_a_box_lattice():
+    """the FP32 V-cycle (the scalar fine-level stencil product on 32 x 8 node tiles, ragged at every edge of a
+    33 x 17 x 25 lattice) inside FGMRES with FP32 inner applies: the same convergence as the FP64 cycle"""
+    fs = dg.FS((9, 5, 7), degree=4, perturb=0.1, seed=4)
+    b = torch.as_tensor(np.random.default_rng(4).uniform(-1, 1, fs.n), device="cuda")
+    op, m = fs.operator(), fs.matrix()
+    m.assemble()
+    its = {}
+    for prec in (dg.dPREC_FP64, dg.dPREC_FP32):
+        ksp = dg.KSP(op, m, ksp_type=dg.dKSP_FGMRES, inner_prec=prec, restart=30, pc=dg.dPC_MG_Q1)
+        x = torch.zeros_like(b)
+        its[prec], _ = ksp.solve(b, x, rtol=1e-8, maxit=500)
+        r = torch.empty_like(x)
+        op.mult(x, r)
+        assert float(torch.linalg.norm(b - r) / torch.linalg.norm(b)) <= 1.01e-8
+    assert its[dg.dPREC_FP32] <= its[dg.dPREC_FP64] + 3, its
+
+
 def test_plaplace_newton_with_multigrid():
     fs = dg.FS((9, 9, 9), degree=4, perturb=0.1, seed=1)
     b = torch.as_tensor(np.random.default_rng(0).uniform(-1, 1, fs.n), device="cuda")
