@@ -104,7 +104,9 @@ void lagrange(int P, const double *nodes, double t, double *val, double *der) {
   }
 }
 
-int rule_1d(dQuadratureMethod method, int order, double *x, double *w) {
+// family: dGAUSS_LEGENDRE or dGAUSS_LOBATTO (FAST and SPARSE rules; SELF rules are Lobatto); -1 for another
+int rule_1d(dQuadratureMethod method, int order, double *x, double *w, int family) {
+  if (family != dGAUSS_LEGENDRE && family != dGAUSS_LOBATTO) return -1;
   if (method == dQUADRATURE_METHOD_SPARSE) {
     int size = order > 0 ? order : 1;
     if (size == 1) {
@@ -115,7 +117,8 @@ int rule_1d(dQuadratureMethod method, int order, double *x, double *w) {
     int nel = size / 2;
     double iv[64], un[64];
     lobatto_rule(nel + 1, iv, un);
-    const double g = 0.57735026918962573;
+    // two points per GLL sub-interval: the Gauss pair +-1/sqrt(3), or the Lobatto pair (the interval's ends)
+    const double g = family == dGAUSS_LEGENDRE ? 0.57735026918962573 : 1.0;
     for (int i = 0; i < nel; i++) {
       double h = iv[i + 1] - iv[i];
       x[2 * i] = iv[i] + (1 - g) * h / 2.;
@@ -125,6 +128,11 @@ int rule_1d(dQuadratureMethod method, int order, double *x, double *w) {
     return size;
   }
   if (method == dQUADRATURE_METHOD_FAST) {
+    if (family == dGAUSS_LOBATTO) {  // n Lobatto points integrate order 2n - 3 exactly
+      int size = 2 + order / 2;
+      lobatto_rule(size, x, w);
+      return size;
+    }
     int size = 1 + order / 2;
     gauss_rule(size, x, w);
     return size;

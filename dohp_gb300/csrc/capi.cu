@@ -143,12 +143,73 @@ __global__ void k_efs_apply(EFSDev f, int64_t nelem, const int32_t *elist, const
   }
 }
 
+// dEFSApply_Modal_All (src/jacobi/impls/modal/modaltopo.c:73-126) over nelem elements stored back to back: one
+// block per element, one thread per output value summing over the modes (INTERP, GRAD) or the points
+// (INTERP_TRANSPOSE) in the reference's order; tables interp [Q][P] and deriv [Q][P][3] in global memory (at most
+// 18 modes: small and cached). Values [P][D] (modes) and [Q][D] (points), gradients [Q][D][3].
+__global__ void k_modal_apply(int64_t nelem, int P, int Q, const double *interp, const double *deriv, int D,
+                              const double *in, double *out, int amode, int imode) {
+  const int64_t e = blockIdx.x;
+  if (e >= nelem) return;
+  const bool add = imode == ADD_VALUES;
+  if (amode == dAPPLY_INTERP) {
+    const double *u = in + e * P * D;
+    double *v = out + e * Q * D;
+    for (int t = threadIdx.x; t < Q * D; t += blockDim.x) {
+      const int i = t / D, c = t % D;
+      double s = 0;
+      for (int j = 0; j < P; j++) s += interp[i * P + j] * u[j * D + c];
+      v[t] = add ? v[t] + s : s;
+    }
+  } else if (amode == dAPPLY_INTERP_TRANSPOSE) {
+    const double *u = in + e * Q * D;
+    double *v = out + e * P * D;
+    for (int t = threadIdx.x; t < P * D; t += blockDim.x) {
+      const int j = t / D, c = t % D;
+      double s = 0;
+      for (int i = 0; i < Q; i++) s += interp[i * P + j] * u[i * D + c];
+      v[t] = add ? v[t] + s : s;
+    }
+  } else {  // dAPPLY_GRAD
+    const double *u = in + e * P * D;
+    double *v = out + e * Q * D * 3;
+    for (int t = threadIdx.x; t < Q * D * 3; t += blockDim.x) {
+      const int i = t / (3 * D), c = (t / 3) % D, d = t % 3;
+      double s = 0;
+      for (int j = 0; j < P; j++) s += deriv[(i * P + j) * 3 + d] * u[j * D + c];
+      v[t] = add ? v[t] + s : s;
+    }
+  }
+}
+
 }  // namespace
+
+// the modal element's batched apply (dEFSApplyBatched on a modal dEFS); jinv is not used, as the reference's
+dErr efs_apply_modal(dEFS efs, int64_t nelem, int D, const double *in, double *out, dApplyMode amode, InsertMode imode,
+                     cudaStream_t stream) {
+  if (amode != dAPPLY_INTERP && amode != dAPPLY_INTERP_TRANSPOSE && amode != dAPPLY_GRAD)
+    return set_error("modal dEFSApply: Apply-mode %d not implemented", (int)amode);
+  if (imode != INSERT_VALUES && imode != ADD_VALUES) return set_error("InsertMode %d invalid", (int)imode);
+  if (D < 1 || D > 4096) return set_error("dofs %d, must be in 1..4096", D);
+  if (nelem < 0) return set_error("nelem %lld negative", (long long)nelem);
+  if (nelem == 0) return 0;
+  if (!in || !out) return set_error("null vector");
+  if (!efs->d_tab) {
+    CUCHK(cudaMalloc(&efs->d_tab, efs->h_tab.size() * sizeof(double)));
+    CUCHK(cudaMemcpy(efs->d_tab, efs->h_tab.data(), efs->h_tab.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  const int P = efs->P[0], Q = efs->Q[0] * efs->Q[1] * efs->Q[2];
+  k_modal_apply<<<(unsigned)nelem, 128, 0, stream>>>(nelem, P, Q, efs->d_tab, efs->d_tab + (size_t)Q * P, D, in, out,
+                                                      (int)amode, (int)imode);
+  CUCHK(cudaGetLastError());
+  return 0;
+}
 
 // the batched apply over a list of elements with node / point offsets (dEFSApplyBatched: contiguous elements)
 dErr efs_apply_list(dEFS efs, int64_t nelem, const int32_t *elist, const int32_t *ioff, const int32_t *ooff, const double *jinv,
                     int D, const double *in, double *out, dApplyMode amode, InsertMode imode, cudaStream_t stream) {
   if (!efs) return set_error("null EFS");
+  if (efs->modal >= 0) return set_error("a modal element in a tensor element loop");
   if (amode < dAPPLY_INTERP || amode > dAPPLY_GRAD_TRANSPOSE) return set_error("invalid/unimplemented dApplyMode %d", (int)amode);
   if (imode != INSERT_VALUES && imode != ADD_VALUES) return set_error("InsertMode %d invalid", (int)imode);
   if (amode == dAPPLY_GRAD_TRANSPOSE && !jinv) return set_error("No Jinv, need a mapping");
@@ -205,9 +266,9 @@ dErr dJacobiGetEFSTensor(dJacobi jac, const dInt degree[3], dQuadratureMethod me
 
 }  // extern "C"
 
-dErr jacobi_efs(dJacobi jac, const dInt degree[3], dQuadratureMethod method, const dInt rule_order[3], dEFS *efs) {
+dErr jacobi_efs(dJacobi jac, const dInt degree[3], dQuadratureMethod method, const dInt rule_order[3], dEFS *efs, int family) {
   if (!jac || !efs) return set_error("null argument");
-  std::vector<int> key = {degree[0], degree[1], degree[2], (int)method, rule_order[0], rule_order[1], rule_order[2]};
+  std::vector<int> key = {degree[0], degree[1], degree[2], (int)method, rule_order[0], rule_order[1], rule_order[2], family};
   auto it = jac->efs.find(key);
   if (it != jac->efs.end()) {
     *efs = it->second;
@@ -223,7 +284,7 @@ dErr jacobi_efs(dJacobi jac, const dInt degree[3], dQuadratureMethod method, con
       return set_error("basis degree %d out of range", degree[d]);
     }
     b.P = degree[d] + 1;
-    b.Q = rule_1d(method, rule_order[d], b.x, b.w);
+    b.Q = rule_1d(method, rule_order[d], b.x, b.w, family);
     if (b.Q < 1 || b.Q > MAXQ) {
       delete f;
       return set_error("rule size %d out of range", b.Q);
@@ -238,7 +299,7 @@ dErr jacobi_efs(dJacobi jac, const dInt degree[3], dQuadratureMethod method, con
   }
   {
     const int ro[3] = {rule_order[0], rule_order[1], rule_order[2]};
-    dErr e = jacobi_rule(jac, method, ro, &f->rule);
+    dErr e = jacobi_rule(jac, method, ro, &f->rule, family);
     if (e) {
       delete f;
       return e;
@@ -255,6 +316,11 @@ extern "C" {
 dErr dEFSGetSizes(dEFS efs, dInt *dim, dInt *inodes, dInt *total) {
   if (!efs) return set_error("null EFS");
   if (dim) *dim = 3;
+  if (efs->modal >= 0) {  // dEFSGetSizes_Modal_All (modaltopo.c:62-71): every mode is interior
+    if (inodes) *inodes = efs->P[0];
+    if (total) *total = efs->P[0];
+    return 0;
+  }
   if (inodes) *inodes = std::max(0, efs->P[0] - 2) * std::max(0, efs->P[1] - 2) * std::max(0, efs->P[2] - 2);
   if (total) *total = efs->P[0] * efs->P[1] * efs->P[2];
   return 0;
@@ -262,6 +328,7 @@ dErr dEFSGetSizes(dEFS efs, dInt *dim, dInt *inodes, dInt *total) {
 
 dErr dEFSGetTensorNodes(dEFS efs, dInt P[3], dInt Q[3], dReal *basis_nodes, dReal *rule_points, dReal *rule_weights) {
   if (!efs) return set_error("null EFS");
+  if (efs->modal >= 0) return set_error("dEFSGetTensorNodes: a modal element has no tensor nodes");
   int op = 0, oq = 0;
   for (int d = 0; d < 3; d++) {
     if (P) P[d] = efs->P[d];
@@ -281,6 +348,7 @@ dErr dEFSGetTensorNodes(dEFS efs, dInt P[3], dInt Q[3], dReal *basis_nodes, dRea
 dErr dEFSApplyBatched(dEFS efs, dInt nelem, const dReal *jinv, dInt D, const dScalar *in, dScalar *out, dApplyMode amode,
                       InsertMode imode, void *stream) {
   Range range_("dEFSApply");
+  if (efs && efs->modal >= 0) return efs_apply_modal(efs, nelem, D, in, out, amode, imode, (cudaStream_t)stream);
   return efs_apply_list(efs, nelem, nullptr, nullptr, nullptr, jinv, D, in, out, amode, imode, (cudaStream_t)stream);
 }
 

@@ -206,6 +206,7 @@ extern "C" {
 
 dErr dFSCreate(dMesh mesh, dJacobi jac, dFS *fs) {
   if (!mesh || !fs) return set_error("dFSCreate: null argument");
+  if (jac && jac->modal) return set_error("dFSCreate: a dFS needs a tensor dJacobi (modal element spaces are discontinuous)");
   _p_dFS *f = new _p_dFS();
   f->mesh = mesh;
   f->jac = jac;
@@ -259,6 +260,7 @@ dErr dFSSetStream(dFS fs, void *stream) {
 dErr dFSBuildSpace(dFS fs) {
   if (!fs) return set_error("null dFS");
   if (fs->built) return 0;
+  if (fs->jac && fs->jac->modal) return set_error("dFSBuildSpace: a dFS needs a tensor dJacobi (modal element spaces are discontinuous)");
   DCHK(fs_build_space(fs));
   fs->built = true;
   return 0;

@@ -43,7 +43,8 @@ void gauss_rule(int n, double *x, double *w);
 void lobatto_rule(int n, double *x, double *w);
 // Lagrange basis on nodes[P] at t: values and derivatives
 void lagrange(int P, const double *nodes, double t, double *val, double *der);
-int rule_1d(dQuadratureMethod method, int order, double *x, double *w);  // Gauss family
+// 1-D rule of a method and order (tensorquad.c:51-118) in a point family (Gauss-Legendre unless given)
+int rule_1d(dQuadratureMethod method, int order, double *x, double *w, int family = dGAUSS_LEGENDRE);
 // 1-D tables for one basis degree p (P = p+1 GLL nodes) on a rule
 struct Basis1D {
   int P = 0, Q = 0;
@@ -59,6 +60,7 @@ int make_basis(int p, dQuadratureMethod method, Basis1D *b);
 
 struct _p_dEFS {
   int P[3], Q[3];
+  int modal = -1;  // >= 0: a modal (P-discontinuous) basis of this order, P[0] modes; h_tab = interp [nq][P], deriv [nq][P][3]
   dQuadratureMethod method;
   _p_dRule *rule = nullptr;  // the rule the basis is evaluated on (owned by the dJacobi's quadrature)
   dgb::Basis1D b[3];
@@ -67,12 +69,16 @@ struct _p_dEFS {
 };
 
 struct _p_dJacobi {
+  int modal = 0;  // dJacobiSetType: 0 tensor, 1 modal (what dJacobiGetEFS makes)
   std::map<std::vector<int>, _p_dEFS *> efs;
   _p_dQuadrature *quad[3] = {nullptr, nullptr, nullptr};  // per dQuadratureMethod, made on first request
 };
 void jacobi_free_quadratures(dJacobi jac);
-dErr jacobi_rule(dJacobi jac, dQuadratureMethod method, const int order[3], _p_dRule **out);
-dErr jacobi_efs(dJacobi jac, const dInt degree[3], dQuadratureMethod method, const dInt rule_order[3], dEFS *efs);
+// the dJacobi's rule / tensor element space of a method and orders in a point family (the dFS paths: Gauss-Legendre)
+dErr jacobi_rule(dJacobi jac, dQuadratureMethod method, const int order[3], _p_dRule **out, int family = dGAUSS_LEGENDRE);
+dErr jacobi_efs(dJacobi jac, const dInt degree[3], dQuadratureMethod method, const dInt rule_order[3], dEFS *efs,
+                int family = dGAUSS_LEGENDRE);
+int jacobi_quad_family(dJacobi jac, dQuadratureMethod method);  // the family dQuadratureTensorSetGaussFamily set
 
 struct _p_dMesh {
   int nx, ny, nz;

@@ -264,6 +264,9 @@ dErr dFSGetPreferredQuadratureRuleSet(dFS fs, dQuadratureMethod method, dRuleset
   if (!fs->jac) return set_error("dFS was created without a dJacobi");
   if (method != dQUADRATURE_METHOD_FAST && method != dQUADRATURE_METHOD_SPARSE)
     return set_error("dFSGetPreferredQuadratureRuleSet: FAST and SPARSE rules");
+  if (jacobi_quad_family(fs->jac, method) != dGAUSS_LEGENDRE)
+    return set_error("dFSGetPreferredQuadratureRuleSet: the element loops use Gauss-Legendre rules (the dJacobi's quadrature "
+                     "was set to another family)");
   _p_dRuleset *R = new _p_dRuleset();
   R->fs = fs;
   R->method = method;

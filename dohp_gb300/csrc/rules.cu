@@ -1,5 +1,6 @@
 // dJacobi quadrature, rules and explicit element bases on the host (src/jacobi/interface/jacobi.c,
 // quadrature.c; src/jacobi/quadrature/impls/tensor/tensorquad.c; src/jacobi/impls/tensor/efstopo.c:660-717),
+// the modal (P-discontinuous) element spaces of the modal dJacobi type (src/jacobi/impls/modal/modal.c),
 // plus the vector constructors of a dFS.
 //
 // A dQuadrature is owned by its dJacobi (one per method, made on first request, as dJacobiGetQuadrature caches
@@ -7,6 +8,7 @@
 // hex, owned by its dQuadrature and shared by every caller that asks for the same orders. Arrays of handles
 // returned by dQuadratureGetRules / dJacobiGetEFS are the caller's and are released with dFree, as in dohp.
 #include <stdlib.h>
+#include <string.h>
 
 #include <algorithm>
 #include <cmath>
@@ -19,6 +21,7 @@ using namespace dgb;
 
 struct _p_dRule {
   dQuadratureMethod method;
+  int family = dGAUSS_LEGENDRE;  // point family (dQuadratureTensorSetGaussFamily)
   int order[3];  // polynomial order integrated exactly, per direction
   int Q[3];
   double x[3][MAXQ], w[3][MAXQ];
@@ -29,10 +32,9 @@ struct _p_dRule {
 
 struct _p_dQuadrature {
   dQuadratureMethod method;
-  std::map<std::vector<int>, _p_dRule *> rules;
+  int family = dGAUSS_LEGENDRE;  // family of the rules made from now on
+  std::map<std::vector<int>, _p_dRule *> rules;  // key {family, order x, y, z}
 };
-
-dErr jacobi_efs(dJacobi jac, const dInt degree[3], dQuadratureMethod method, const dInt rule_order[3], dEFS *efs);
 
 void jacobi_free_quadratures(dJacobi jac) {
   for (auto &q : jac->quad) {
@@ -43,17 +45,22 @@ void jacobi_free_quadratures(dJacobi jac) {
   }
 }
 
-dErr quad_rule(_p_dQuadrature *q, const int order[3], _p_dRule **out);
+dErr quad_rule(_p_dQuadrature *q, const int order[3], int family, _p_dRule **out);
 
-// the rule of the given method and orders, owned by the dJacobi's quadrature (used for every dEFS's rule)
-dErr jacobi_rule(dJacobi jac, dQuadratureMethod method, const int order[3], _p_dRule **out) {
+// the rule of the given method, orders and family, owned by the dJacobi's quadrature (used for every dEFS's rule)
+dErr jacobi_rule(dJacobi jac, dQuadratureMethod method, const int order[3], _p_dRule **out, int family) {
   dQuadrature q;
   DCHK(dJacobiGetQuadrature(jac, method, &q));
-  return quad_rule(q, order, out);
+  return quad_rule(q, order, family, out);
 }
 
-dErr quad_rule(_p_dQuadrature *q, const int order[3], _p_dRule **out) {
-  std::vector<int> key = {order[0], order[1], order[2]};
+// the family a dJacobi's quadrature of a method makes rules in (Gauss-Legendre before one exists)
+int jacobi_quad_family(dJacobi jac, dQuadratureMethod method) {
+  return jac && method >= 0 && method < 3 && jac->quad[method] ? jac->quad[method]->family : (int)dGAUSS_LEGENDRE;
+}
+
+dErr quad_rule(_p_dQuadrature *q, const int order[3], int family, _p_dRule **out) {
+  std::vector<int> key = {family, order[0], order[1], order[2]};
   auto it = q->rules.find(key);
   if (it != q->rules.end()) {
     *out = it->second;
@@ -61,6 +68,7 @@ dErr quad_rule(_p_dQuadrature *q, const int order[3], _p_dRule **out) {
   }
   _p_dRule *r = new _p_dRule();
   r->method = q->method;
+  r->family = family;
   for (int d = 0; d < 3; d++) {
     if (order[d] < 0 || order[d] > 2 * MAXQ) {
       delete r;
@@ -68,7 +76,7 @@ dErr quad_rule(_p_dQuadrature *q, const int order[3], _p_dRule **out) {
     }
     r->order[d] = order[d];
     double x[64], w[64];
-    const int n = rule_1d(q->method, order[d], x, w);
+    const int n = rule_1d(q->method, order[d], x, w, family);
     if (n < 1 || n > MAXQ) {
       delete r;
       return set_error("rule of order %d has %d points (at most %d supported)", order[d], n, MAXQ);
@@ -100,7 +108,66 @@ double invert3_host(const double a[9], double b[9]) {
   return det;
 }
 
+// Modal (P-discontinuous) hexahedral bases of the modal dJacobi (src/jacobi/impls/modal/modal.c:15-240). Every
+// mode is a product of orthonormal Legendre polynomials sqrt(n + 1/2) P_n(t), one per direction; the modes of each
+// order are listed by their degrees per direction in the reference's order (its order-3 set has 18 modes: the
+// y^2 z and y z^2 products are not in it).
+constexpr int kModalCount[4] = {1, 4, 10, 18};  // ModalPCount (modal.c:15-42), region
+constexpr int kModalDegrees[18][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {2, 0, 0}, {0, 2, 0},
+                                      {0, 0, 2}, {1, 1, 0}, {0, 1, 1}, {1, 0, 1}, {3, 0, 0}, {0, 3, 0},
+                                      {0, 0, 3}, {2, 1, 0}, {1, 2, 0}, {2, 0, 1}, {1, 0, 2}, {1, 1, 1}};
+
+// sqrt(n + 1/2) P_n(t) and its derivative by Bonnet's recurrence (k+1) P_{k+1} = (2k+1) t P_k - k P_{k-1},
+// P'_{k+1} = P'_{k-1} + (2k+1) P_k
+void legendre_orthonormal(int n, double t, double *v, double *dv) {
+  double p0 = 1, p1 = t, d0 = 0, d1 = 1;
+  if (n == 0) p1 = 1, d1 = 0;
+  for (int k = 1; k < n; k++) {
+    const double p2 = ((2 * k + 1) * t * p1 - k * p0) / (k + 1), d2 = d0 + (2 * k + 1) * p1;
+    p0 = p1, p1 = p2, d0 = d1, d1 = d2;
+  }
+  const double c = std::sqrt(n + 0.5);
+  *v = c * p1;
+  *dv = c * d1;
+}
+
 }  // namespace
+
+// the modal element space of an order on a rule, cached in the dJacobi (key {-1, order, 0, method, rule orders,
+// family}: tensor keys start with a degree >= 1); tables interp [nq][P] and deriv [nq][P][3] at the rule's points
+dErr jacobi_efs_modal(dJacobi jac, int order, _p_dRule *rule, dEFS *efs) {
+  if (order < 0 || order > 3) return set_error("modal basis: order %d for type region (orders 0..3)", order);
+  std::vector<int> key = {-1, order, 0, (int)rule->method, rule->order[0], rule->order[1], rule->order[2], rule->family};
+  auto it = jac->efs.find(key);
+  if (it != jac->efs.end()) {
+    *efs = it->second;
+    return 0;
+  }
+  const int P = kModalCount[order], nq = rule->Q[0] * rule->Q[1] * rule->Q[2];
+  std::vector<double> pts(3 * (size_t)nq);
+  DCHK(dRuleGetNodeWeight(rule, pts.data(), nullptr));
+  _p_dEFS *f = new _p_dEFS();
+  f->modal = order;
+  f->method = rule->method;
+  f->rule = rule;
+  f->P[0] = P, f->P[1] = f->P[2] = 1;
+  for (int d = 0; d < 3; d++) f->Q[d] = rule->Q[d];
+  f->h_tab.assign((size_t)nq * P * 4, 0.0);
+  double *interp = f->h_tab.data(), *deriv = interp + (size_t)nq * P;
+  for (int q = 0; q < nq; q++)
+    for (int j = 0; j < P; j++) {
+      double v[3], dv[3];
+      for (int d = 0; d < 3; d++) legendre_orthonormal(kModalDegrees[j][d], pts[3 * q + d], &v[d], &dv[d]);
+      interp[(size_t)q * P + j] = v[0] * v[1] * v[2];
+      double *g = deriv + ((size_t)q * P + j) * 3;
+      g[0] = dv[0] * v[1] * v[2];
+      g[1] = v[0] * dv[1] * v[2];
+      g[2] = v[0] * v[1] * dv[2];
+    }
+  jac->efs[key] = f;
+  *efs = f;
+  return 0;
+}
 
 extern "C" {
 
@@ -132,13 +199,25 @@ dErr dQuadratureGetRules(dQuadrature quad, dInt n, const dEntTopology topo[], co
       return set_error("dQuadratureGetRules: topology %d not supported (hexahedra only)", (int)topo[i]);
     }
     const int o[3] = {dPolynomialOrder1D(order[i], 0), dPolynomialOrder1D(order[i], 1), dPolynomialOrder1D(order[i], 2)};
-    dErr e = quad_rule(quad, o, &arr[i]);
+    dErr e = quad_rule(quad, o, quad->family, &arr[i]);
     if (e) {
       free(arr);
       return e;
     }
   }
   *rules = arr;
+  return 0;
+}
+
+dErr dQuadratureTensorSetGaussFamily(dQuadrature quad, dGaussFamily family) {
+  if (!quad) return set_error("null quadrature");
+  static const char *names[] = {"gauss", "lobatto", "radau"};
+  if (family != dGAUSS_LEGENDRE && family != dGAUSS_LOBATTO) {
+    if (family == dGAUSS_RADAU)
+      return set_error("GaussFamily %s and dQuadratureMethod %d not supported", names[family], (int)quad->method);
+    return set_error("invalid GaussFamily %d", (int)family);
+  }
+  quad->family = family;
   return 0;
 }
 
@@ -240,14 +319,91 @@ dErr dJacobiGetEFS(dJacobi jac, dInt n, const dEntTopology topo[], const dPolyno
       free(arr);
       return set_error("dJacobiGetEFS: topology %d not supported (hexahedra only)", (int)topo[i]);
     }
-    const dInt deg[3] = {dPolynomialOrder1D(order[i], 0), dPolynomialOrder1D(order[i], 1), dPolynomialOrder1D(order[i], 2)};
-    dErr e = jacobi_efs(jac, deg, rules[i]->method, rules[i]->order, &arr[i]);
+    dErr e;
+    if (jac->modal) {  // dJacobiGetEFS_Modal (modal.c:343-370): the total order of the degree
+      e = jacobi_efs_modal(jac, dPolynomialOrderMax(order[i]), rules[i], &arr[i]);
+    } else {
+      const dInt deg[3] = {dPolynomialOrder1D(order[i], 0), dPolynomialOrder1D(order[i], 1), dPolynomialOrder1D(order[i], 2)};
+      e = jacobi_efs(jac, deg, rules[i]->method, rules[i]->order, &arr[i], rules[i]->family);
+    }
     if (e) {
       free(arr);
       return e;
     }
   }
   *efs = arr;
+  return 0;
+}
+
+dErr dJacobiSetType(dJacobi jac, const char *type) {
+  if (!jac || !type) return set_error("null argument");
+  if (!strcmp(type, dJACOBI_TENSOR)) jac->modal = 0;
+  else if (!strcmp(type, dJACOBI_MODAL)) jac->modal = 1;
+  else return set_error("Unable to find requested dJacobi type %s", type);
+  return 0;
+}
+
+dErr dJacobiGetType(dJacobi jac, const char **type) {
+  if (!jac || !type) return set_error("null argument");
+  *type = jac->modal ? dJACOBI_MODAL : dJACOBI_TENSOR;
+  return 0;
+}
+
+// the reference's dJacobiModalSetFamily looks its implementation up under a name the modal type does not compose
+// (modal.c:413-418 against 385), so it never reaches the check of dJacobiModalSetFamily_Modal (modal.c:273-281);
+// here the check applies on a modal dJacobi
+dErr dJacobiModalSetFamily(dJacobi jac, dJacobiModalFamily family) {
+  if (!jac) return set_error("null dJacobi");
+  if (!jac->modal) return 0;
+  if (family != dJACOBI_MODAL_P_DISCONTINUOUS) return set_error("dJacobiModalSetFamily: only P-discontinuous");
+  return 0;
+}
+
+// dEFSGetExplicit (jacobi.c:508-559): the basis and its (mapped) derivatives at the rule points; the reference's
+// generic path applies INTERP and GRAD to each unit vector, the same numbers as the products formed here
+dErr dEFSGetExplicit(dEFS efs, const dReal jinv[], dInt *Q, dInt *P, const dReal **basis, const dReal **deriv) {
+  if (!efs || !Q || !P || !basis || !deriv) return set_error("null argument");
+  const int nq = efs->Q[0] * efs->Q[1] * efs->Q[2], np = efs->P[0] * efs->P[1] * efs->P[2];
+  double *B = (double *)malloc(sizeof(double) * (size_t)std::max(nq * np, 1));
+  double *G = (double *)malloc(sizeof(double) * 3 * (size_t)std::max(nq * np, 1));
+  if (!B || !G) {
+    free(B);
+    free(G);
+    return set_error("out of host memory");
+  }
+  if (efs->modal >= 0) {  // dEFSApply_Modal_All ignores the mapping (modaltopo.c:73)
+    std::copy(efs->h_tab.begin(), efs->h_tab.begin() + (size_t)nq * np, B);
+    std::copy(efs->h_tab.begin() + (size_t)nq * np, efs->h_tab.begin() + (size_t)nq * np * 4, G);
+  } else {
+    const int *Pn = efs->P, *Qn = efs->Q;
+    for (int q = 0; q < nq; q++) {
+      const int a = q / (Qn[1] * Qn[2]), b = (q / Qn[2]) % Qn[1], c = q % Qn[2];
+      for (int k = 0; k < np; k++) {
+        const int ki = k / (Pn[1] * Pn[2]), kj = (k / Pn[2]) % Pn[1], kk = k % Pn[2];
+        const double Bx = efs->b[0].B[a * Pn[0] + ki], By = efs->b[1].B[b * Pn[1] + kj], Bz = efs->b[2].B[c * Pn[2] + kk];
+        const double Dx = efs->b[0].D[a * Pn[0] + ki], Dy = efs->b[1].D[b * Pn[1] + kj], Dz = efs->b[2].D[c * Pn[2] + kk];
+        const double r[3] = {Dx * By * Bz, Bx * Dy * Bz, Bx * By * Dz};
+        B[(size_t)q * np + k] = Bx * By * Bz;
+        double *g = G + ((size_t)q * np + k) * 3;
+        for (int e = 0; e < 3; e++)  // TensorRuleMapping (efstopo.c:557-590): sum_k r_k jinv[q][k][e]
+          g[e] = jinv ? r[0] * jinv[q * 9 + e] + r[1] * jinv[q * 9 + 3 + e] + r[2] * jinv[q * 9 + 6 + e] : r[e];
+      }
+    }
+  }
+  *Q = nq;
+  *P = np;
+  *basis = B;
+  *deriv = G;
+  return 0;
+}
+
+dErr dEFSRestoreExplicit(dEFS efs, const dReal jinv[], dInt *Q, dInt *P, const dReal **basis, const dReal **deriv) {
+  (void)jinv;
+  if (!efs || !Q || !P || !basis || !deriv) return set_error("null argument");
+  free((void *)*basis);
+  free((void *)*deriv);
+  *Q = *P = 0;
+  *basis = *deriv = nullptr;
   return 0;
 }
 
@@ -265,6 +421,7 @@ dErr dEFSGetRule(dEFS efs, dRule *rule) {
 dErr dEFSGetExplicitSparse(dEFS efs, dInt npatches, dInt Q, const dInt qidx[], const dReal cjinv[], dInt eoffset, dInt *P, dInt eidx[],
                            dReal interp[], dReal deriv[]) {
   if (!efs || !qidx || !P || !eidx || !interp || !deriv) return set_error("null argument");
+  if (efs->modal >= 0) return set_error("dEFSGetExplicitSparse: not available for a modal element");  // jacobi.c:606
   if (npatches <= 0 || Q <= 0) return set_error("dEFSGetExplicitSparse: npatches and Q must be positive");
   const int px = efs->P[0] - 1, py = efs->P[1] - 1, pz = efs->P[2] - 1;
   static const double s1 = 0.78867513459481287, s0 = 0.21132486540518713;

@@ -43,6 +43,17 @@ typedef enum { NOT_SET_VALUES = 0, INSERT_VALUES = 1, ADD_VALUES = 2 } InsertMod
 typedef enum { dFS_HOMOGENEOUS, dFS_INHOMOGENEOUS } dFSHomogeneousMode;
 /* include/dohpjacobi.h:141-148 */
 typedef enum { dQUADRATURE_METHOD_FAST, dQUADRATURE_METHOD_SPARSE, dQUADRATURE_METHOD_SELF } dQuadratureMethod;
+/* include/dohpjacobi.h:223: point family of the tensor quadrature's rules (dQuadratureTensorSetGaussFamily) */
+typedef enum { dGAUSS_LEGENDRE, dGAUSS_LOBATTO, dGAUSS_RADAU } dGaussFamily;
+/* include/dohpjacobi.h:134-136, 211-217: dJacobi types and the families of the modal type */
+#define dJACOBI_TENSOR "tensor"
+#define dJACOBI_MODAL "modal"
+typedef enum {
+  dJACOBI_MODAL_P_CONFORMING,
+  dJACOBI_MODAL_P_DISCONTINUOUS,
+  dJACOBI_MODAL_Q_CONFORMING,
+  dJACOBI_MODAL_Q_DISCONTINUOUS
+} dJacobiModalFamily;
 /* include/dohpfs.h:41-47: the reference's values (the low 16 bits hold a count of strongly enforced dofs, unused
  * here). DIRICHLET removes the set's nodes from the global space; WEAK puts its faces in the facet iterator. */
 typedef enum {
@@ -71,6 +82,11 @@ static inline dPolynomialOrder dPolynomialOrderCreate(dInt max, dInt x, dInt y, 
 static inline dInt dPolynomialOrder1D(dPolynomialOrder o, dInt dir) {
   const dInt d = dir == 0 ? o.s.x : dir == 1 ? o.s.y : dir == 2 ? o.s.z : 0;
   return d ? d : o.s.max;
+}
+/* include/dohpjacobi.h:79-83: the total order (max, or x + y + z when larger) */
+static inline dInt dPolynomialOrderMax(dPolynomialOrder o) {
+  const dInt xyz = (dInt)o.s.x + o.s.y + o.s.z;
+  return o.s.max > xyz ? (dInt)o.s.max : xyz;
 }
 
 typedef struct _p_dJacobi *dJacobi;
@@ -109,6 +125,15 @@ const char *dGetLastError(void);
 /* dJacobiCreate (src/jacobi/interface/jacobi.c) with the tensor (GLL nodal) type */
 dErr dJacobiCreate(dJacobi *jac);
 dErr dJacobiDestroy(dJacobi *jac);
+/* dJacobiSetType / dJacobiGetType (src/jacobi/interface/jacobi.c:42-70): dJACOBI_TENSOR (the default: GLL nodal
+ * tensor-product bases) or dJACOBI_MODAL (P-discontinuous modal bases of orders 0..3 on hexahedra,
+ * src/jacobi/impls/modal/modal.c); another name is an error. The type decides what dJacobiGetEFS makes; element
+ * spaces already made stay valid. A dFS needs the tensor type (its spaces are continuous). */
+dErr dJacobiSetType(dJacobi jac, const char *type);
+dErr dJacobiGetType(dJacobi jac, const char **type);
+/* dJacobiModalSetFamily (modal.c:273-281, 413-418): only dJACOBI_MODAL_P_DISCONTINUOUS is built; another family is
+ * an error on a modal dJacobi. On a tensor dJacobi the call does nothing, as the reference's PetscTryMethod. */
+dErr dJacobiModalSetFamily(dJacobi jac, dJacobiModalFamily family);
 /* release an array the library allocated for the caller (dQuadratureGetRules, dJacobiGetEFS), as dohp's dFree */
 dErr dFree(void *ptr);
 /* dJacobiGetQuadrature (include/dohpjacobi.h:170, src/jacobi/interface/jacobi.c:268-285): the dJacobi's quadrature
@@ -118,6 +143,12 @@ dErr dJacobiGetQuadrature(dJacobi jac, dQuadratureMethod method, dQuadrature *qu
  * order[i] exactly on the reference hex (tensorquad.c:51-118: FAST n = 1 + order/2 Gauss points, SPARSE two Gauss
  * points per GLL sub-interval, SELF Lobatto); the rules themselves are owned by the quadrature. Hexahedra only. */
 dErr dQuadratureGetRules(dQuadrature quad, dInt n, const dEntTopology topo[], const dPolynomialOrder order[], dRule **rules);
+/* dQuadratureTensorSetGaussFamily (tensorquad.c:446-462, rule sizes 51-118): the point family of the rules this
+ * quadrature makes from now on. FAST: Gauss-Legendre (default, 1 + order/2 points) or Gauss-Lobatto (2 + order/2
+ * points); SPARSE: two Gauss-Legendre or two Lobatto (end) points per GLL sub-interval; SELF rules are Lobatto for
+ * either family. Radau is an error. Rules made before the call keep their family. The rulesets of a dFS are
+ * Gauss-Legendre (dFSGetPreferredQuadratureRuleSet refuses a dJacobi whose quadrature was set otherwise). */
+dErr dQuadratureTensorSetGaussFamily(dQuadrature quad, dGaussFamily family);
 /* dRuleGetSize / dRuleGetNodeWeight / dRuleGetTensorNodeWeight (include/dohpjacobi.h:186-189): host arrays; nodes
  * [n][3] and weights [n] in tensor order (x slowest); the 1-D tables are owned by the rule */
 dErr dRuleGetSize(dRule rule, dInt *dim, dInt *nnodes);
@@ -142,16 +173,25 @@ dErr dEFSGetRule(dEFS efs, dRule *rule);
  * points per patch and the p_x p_y p_z GLL sub-cells as patches, the Q1 sub-cell bases of efstopo.c:660-717 (P = 8,
  * derivatives with respect to the unit sub-cell coordinate mapped by cjinv [pidx*8+q]), otherwise the element's own
  * basis at each patch point (P = nodes of the element, cjinv read at qidx[qidx[pidx*Q+q]] as jacobi.c:620-626 does).
- * cjinv NULL: reference coordinates.
+ * cjinv NULL: reference coordinates. A modal element has no sparse form (an error, as jacobi.c:606).
  * Outputs (host): eidx [npatches][P] = eoffset + element node, interp [npatches][Q][P], deriv [npatches][Q][P][3]. */
 dErr dEFSGetExplicitSparse(dEFS efs, dInt npatches, dInt Q, const dInt qidx[], const dReal cjinv[], dInt eoffset, dInt *P,
                            dInt eidx[], dReal interp[], dReal deriv[]);
-/* dEFSGetSizes (include/dohpjacobi.h:172): dim, interior nodes, total nodes */
+/* dEFSGetExplicit / dEFSRestoreExplicit (include/dohpjacobi.h:179-180, src/jacobi/interface/jacobi.c:508-576): the
+ * element basis at the rule points as host arrays *basis [Q][P] and *deriv [Q][P][3], the derivatives mapped by
+ * jinv [Q][3][3] (NULL: reference coordinates; a modal basis ignores jinv, as its apply does). Restore releases
+ * the arrays and zeroes the outputs. */
+dErr dEFSGetExplicit(dEFS efs, const dReal jinv[], dInt *Q, dInt *P, const dReal **basis, const dReal **deriv);
+dErr dEFSRestoreExplicit(dEFS efs, const dReal jinv[], dInt *Q, dInt *P, const dReal **basis, const dReal **deriv);
+/* dEFSGetSizes (include/dohpjacobi.h:172): dim, interior nodes, total nodes (a modal basis: its modes for both) */
 dErr dEFSGetSizes(dEFS efs, dInt *dim, dInt *inodes, dInt *total);
-/* dEFSGetTensorNodes / dRuleGetTensorNodeWeight: host copies of basis nodes, rule points, weights */
+/* dEFSGetTensorNodes / dRuleGetTensorNodeWeight: host copies of basis nodes, rule points, weights (a modal element:
+ * an error, it has no nodes) */
 dErr dEFSGetTensorNodes(dEFS efs, dInt P[3], dInt Q[3], dReal *basis_nodes, dReal *rule_points, dReal *rule_weights);
 /* dEFSApply (include/dohpjacobi.h:177, src/jacobi/impls/tensor/efstopo.c:368-423) for ONE element:
- * device pointers; jinv NULL means reference coordinates (efstopo.c:565-568). */
+ * device pointers; jinv NULL means reference coordinates (efstopo.c:565-568). On a modal element
+ * (src/jacobi/impls/modal/modaltopo.c:73-126): INTERP, INTERP_TRANSPOSE and GRAD (reference-coordinate
+ * derivatives, jinv unused), GRAD_TRANSPOSE is an error; values are [P][D] per element for modes. */
 dErr dEFSApply(dEFS efs, const dReal *jinv, dInt D, const dScalar *in, dScalar *out, dApplyMode amode, InsertMode imode);
 /* Batched dEFSApply over nelem elements stored back to back (element stride = the mode's in/out size),
  * jinv strided by 9*Q per element (or NULL). stream: cudaStream_t or NULL. */

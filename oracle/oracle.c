@@ -417,6 +417,89 @@ int or_explicit_sparse(const int P3[3], const int Q3[3], const double *interp[3]
 }
 
 /* ----------------------------------------------------------------------------------------------
+ * Modal (P-discontinuous) element bases of the modal dJacobi (src/jacobi/impls/modal/modal.c,
+ * modaltopo.c), hexahedra. The reference tabulates sympy-generated Gram-Schmidt polynomials; they are
+ * products of orthonormal Legendre polynomials Lh_n(t) = sqrt(n + 1/2) P_n(t), one factor per direction,
+ * evaluated here from the closed forms of P_0..P_3. The mode order is the reference's (table as reference,
+ * modal.c:141-238): its order-3 set has 18 modes, without the y^2 z and y z^2 products.
+ * -------------------------------------------------------------------------------------------- */
+static const int modal_hex_exp[18][3] = {
+  {0, 0, 0},                                                    /* order 0 */
+  {1, 0, 0}, {0, 1, 0}, {0, 0, 1},                              /* order 1 */
+  {2, 0, 0}, {0, 2, 0}, {0, 0, 2}, {1, 1, 0}, {0, 1, 1}, {1, 0, 1}, /* order 2 */
+  {3, 0, 0}, {0, 3, 0}, {0, 0, 3}, {2, 1, 0}, {1, 2, 0}, {2, 0, 1}, {1, 0, 2}, {1, 1, 1} /* order 3 */
+};
+
+/* ModalPCount (modal.c:15-42), region case */
+int or_modal_count(int order)
+{
+  static const int count[4] = {1, 4, 10, 18};
+  if (order < 0 || order > 3) return or_fail("Order %d for type region", order);
+  return count[order];
+}
+
+static void legendre_hat(int n, double t, double *v, double *d)
+{
+  double p, dp;
+  switch (n) {
+  case 0: p = 1; dp = 0; break;
+  case 1: p = t; dp = 1; break;
+  case 2: p = 1.5 * t * t - 0.5; dp = 3 * t; break;
+  default: p = 2.5 * t * t * t - 1.5 * t; dp = 7.5 * t * t - 1.5; break;
+  }
+  *v = sqrt(n + 0.5) * p;
+  *d = sqrt(n + 0.5) * dp;
+}
+
+/* dEFSModalSetUp (modal.c:45-240), hexahedra: interp [Q][P], deriv [Q][P][3] at the Q points rcoord [Q][3].
+ * Returns P, or -1 for an unsupported order. */
+int or_modal_basis(int order, int Q, const double *rcoord, double *interp, double *deriv)
+{
+  const int P = or_modal_count(order);
+  if (P < 0) return -1;
+  for (int i = 0; i < Q; i++) {
+    for (int j = 0; j < P; j++) {
+      double v[3], d[3];
+      for (int k = 0; k < 3; k++) legendre_hat(modal_hex_exp[j][k], rcoord[3 * i + k], &v[k], &d[k]);
+      interp[i * P + j] = v[0] * v[1] * v[2];
+      deriv[(i * P + j) * 3 + 0] = d[0] * v[1] * v[2];
+      deriv[(i * P + j) * 3 + 1] = v[0] * d[1] * v[2];
+      deriv[(i * P + j) * 3 + 2] = v[0] * v[1] * d[2];
+    }
+  }
+  return P;
+}
+
+/* dEFSApply_Modal_All (modaltopo.c:73-126): dense products with the tables; the mapping (jinv) is not used,
+ * GRAD gives reference-coordinate derivatives [Q][D][3]; GRAD_TRANSPOSE is not implemented (an error). */
+int or_modal_apply(int P, int Q, const double *interp, const double *deriv, int D, const double *in, double *out,
+                   int amode, int imode)
+{
+  switch (amode) {
+  case OR_INTERP:
+    if (imode == OR_INSERT) memset(out, 0, sizeof(double) * Q * D);
+    for (int i = 0; i < Q; i++)
+      for (int j = 0; j < P; j++)
+        for (int c = 0; c < D; c++) out[i * D + c] += interp[i * P + j] * in[j * D + c];
+    return 0;
+  case OR_INTERP_TRANSPOSE:
+    if (imode == OR_INSERT) memset(out, 0, sizeof(double) * P * D);
+    for (int i = 0; i < Q; i++)
+      for (int j = 0; j < P; j++)
+        for (int c = 0; c < D; c++) out[j * D + c] += interp[i * P + j] * in[i * D + c];
+    return 0;
+  case OR_GRAD:
+    if (imode == OR_INSERT) memset(out, 0, sizeof(double) * Q * D * 3);
+    for (int i = 0; i < Q; i++)
+      for (int j = 0; j < P; j++)
+        for (int c = 0; c < D; c++)
+          for (int e = 0; e < 3; e++) out[(i * D + c) * 3 + e] += deriv[(i * P + j) * 3 + e] * in[j * D + c];
+    return 0;
+  default: return or_fail("Apply-mode not implemented");
+  }
+}
+
+/* ----------------------------------------------------------------------------------------------
  * Structured block mesh: entity creation order of dMeshGenerateBlock (genblock.c:206-402),
  * adjacency in canonical side order (dMeshGetAdjacency, mesh.c:1074-1191) and orientation
  * permutations (dMeshAdjacencyPermutations_Private, mesh.c:1039-1072; dohpgeom.h:97-150).

@@ -46,6 +46,13 @@ int or_efs_apply_hex(const int P[3], const int Q[3], const double *interp[3], co
                      const double *jinv, int D, const double *in, double *out, int amode, int imode);
 /* dGeomInvert3 (include/dohpgeom.h:57-79) */
 void or_invert3(const double a[9], double b[9], double *det);
+/* Modal (P-discontinuous) hexahedral bases (src/jacobi/impls/modal/modal.c:15-240, modaltopo.c:73-126):
+ * mode count of an order (0..3), tables interp [Q][P] / deriv [Q][P][3] at rcoord [Q][3] (returns P),
+ * and the element apply (INTERP, INTERP_TRANSPOSE, GRAD; jinv unused, as the reference). */
+int or_modal_count(int order);
+int or_modal_basis(int order, int Q, const double *rcoord, double *interp, double *deriv);
+int or_modal_apply(int P, int Q, const double *interp, const double *deriv, int D, const double *in, double *out,
+                   int amode, int imode);
 /* dEFSGetExplicitSparse_Tensor_Hex (efstopo.c:660-717); cjinv indexed as the reference does. */
 int or_explicit_sparse_hex(int px, int py, int pz, int npatches, int Q, const int *qidx, const double *cjinv,
                            int eoffset, int *P, int *eidx, double *interp, double *deriv);

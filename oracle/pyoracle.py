@@ -51,6 +51,10 @@ def lib():
         L.or_explicit_sparse.argtypes = [_i32p, _i32p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                          _i32p, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _i32p,
                                          _f64p, _f64p]
+        L.or_modal_count.argtypes = [ctypes.c_int]
+        L.or_modal_basis.argtypes = [ctypes.c_int, ctypes.c_int, _f64p, _f64p, _f64p]
+        L.or_modal_apply.argtypes = [ctypes.c_int, ctypes.c_int, _f64p, _f64p, ctypes.c_int, _f64p, _f64p, ctypes.c_int,
+                                     ctypes.c_int]
         L.or_fs_create.restype = ctypes.c_void_p
         L.or_fs_create.argtypes = [ctypes.c_int] * 3 + [_f64p, ctypes.c_double, ctypes.c_uint64, ctypes.c_int,
                                    ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
@@ -185,6 +189,33 @@ def efs_apply_hex(P, Q, interp, deriv, jinv, D, x, amode, imode=1, out=None):
     jinv_c = None if jinv is None else np.ascontiguousarray(jinv, dtype=np.float64)
     rc = lib().or_efs_apply_hex(P, Q, ip, dp, None if jinv_c is None else jinv_c.ctypes.data, D,
                                 np.ascontiguousarray(x, dtype=np.float64), out, amode, imode)
+    if rc:
+        raise RuntimeError(lib().or_last_error().decode())
+    return out
+
+
+def modal_basis(order, rcoord):
+    """Modal (P-discontinuous) hexahedral basis of an order 0..3 at the points rcoord [Q][3]
+    (modal.c:45-240): interp [Q][P], deriv [Q][P][3]."""
+    rcoord = np.ascontiguousarray(rcoord, dtype=np.float64).reshape(-1, 3)
+    Q = len(rcoord)
+    P = lib().or_modal_count(order)
+    if P < 0:
+        raise RuntimeError(lib().or_last_error().decode())
+    interp = np.zeros(Q * P); deriv = np.zeros(Q * P * 3)
+    lib().or_modal_basis(order, Q, rcoord, interp, deriv)
+    return interp.reshape(Q, P), deriv.reshape(Q, P, 3)
+
+
+def modal_apply(interp, deriv, D, x, amode, imode=1, out=None):
+    """dEFSApply_Modal_All (modaltopo.c:73-126) for one element"""
+    Q, P = interp.shape
+    size = {40001: Q * D, 40002: P * D, 40003: Q * D * 3}.get(amode, 1)
+    if out is None:
+        out = np.zeros(size)
+    rc = lib().or_modal_apply(P, Q, np.ascontiguousarray(interp, dtype=np.float64),
+                              np.ascontiguousarray(deriv, dtype=np.float64), D,
+                              np.ascontiguousarray(x, dtype=np.float64), out, amode, imode)
     if rc:
         raise RuntimeError(lib().or_last_error().decode())
     return out

@@ -47,6 +47,23 @@ def explicit_bases(root, name, full_elems=(0, 1), head_rows=16):
     return out
 
 
+def modal_values(root, name):
+    """jacobi-2-modal-*: per element (modal orders 0..3) the values of the modes (weights 2, 3, 5, 7, ... as
+    ex2.c sets them) at the rule points, and the modes after the mass matrix (INTERP_TRANSPOSE of the weighted
+    values)."""
+    lines = read(root, f"src/jacobi/tests/refout/{name}.refout")
+    out, elem, cur = {}, -1, None
+    for ln in lines:
+        if ln.startswith("Values of"):
+            elem += 1
+            cur = out.setdefault(f"e{elem}_values", [])
+        elif ln.startswith("Modal values after"):
+            cur = out.setdefault(f"e{elem}_mass_applied", [])
+        else:
+            cur.extend(float(v) for v in ln.split(":", 1)[1].split())
+    return {k: np.array(v) for k, v in out.items()}
+
+
 def sparse_bases(root, name, max_patches=4):
     lines = read(root, f"src/jacobi/tests/refout/{name}.refout")
     tabs = {}
@@ -189,6 +206,10 @@ def main(root):
     fixtures = {
         "jacobi3_gauss": explicit_bases(root, "jacobi-3-tensor-gauss"),
         "jacobi3_lobatto": explicit_bases(root, "jacobi-3-tensor-lobatto"),
+        "jacobi3_modal_gauss": explicit_bases(root, "jacobi-3-modal-gauss", full_elems=(0, 1, 2, 3), head_rows=64),
+        "jacobi2_modal_fast_gauss": modal_values(root, "jacobi-2-modal-fast-gauss"),
+        "jacobi2_modal_fast_lobatto": modal_values(root, "jacobi-2-modal-fast-lobatto"),
+        "jacobi2_modal_sparse_gauss": modal_values(root, "jacobi-2-modal-sparse-gauss"),
         "jacobi3_sparsex_r4": sparse_bases(root, "jacobi-3-tensor-sparsex-r4"),
         "jacobi3_sparsex_r6": sparse_bases(root, "jacobi-3-tensor-sparsex-r6"),
         "jacobi4_fast": patches(root, "jacobi-4-tensor-fast"),

@@ -251,3 +251,60 @@ def test_sparse_rule_efs_golden():
         np.testing.assert_allclose(interp, g[f"P{P}_interp"], atol=6e-6)
         np.testing.assert_allclose(deriv, g[f"P{P}_deriv"], atol=6e-6)
         np.testing.assert_allclose(node, g[f"P{P}_node"], atol=6e-6)
+
+
+# ---------------------------------------------------------------- modal bases (jacobi-2-modal-*, jacobi-3-modal-gauss)
+# ex2.c's mode weights: the first primes, one per mode
+PRIMES = np.array([2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61, 67, 71], float)
+
+
+def tensor_points(method, family, rule_degree):
+    """rule points [Q][3] (x slowest) and weights of the tensor rule (dRuleGetNodeWeight order)"""
+    x, w = po.rule_1d(method, family, rule_degree)
+    pts = np.stack(np.meshgrid(x, x, x, indexing="ij"), axis=-1).reshape(-1, 3)
+    return pts, np.einsum("i,j,k->ijk", w, w, w).ravel()
+
+
+@pytest.mark.parametrize("name,method,family,rdeg", [("jacobi2_modal_fast_gauss", 0, 0, 6),
+                                                     ("jacobi2_modal_fast_lobatto", 0, 1, 4),
+                                                     ("jacobi2_modal_sparse_gauss", 1, 0, 6)])
+def test_modal_values_and_mass_golden(name, method, family, rdeg):
+    """jacobi-2-modal-* (src/jacobi/tests/ex2.c): modes of orders 0..3 weighted by the first primes, evaluated at the
+    rule points (INTERP) and brought back through the weighted INTERP_TRANSPOSE (the mass matrix: the identity where
+    the rule integrates the products exactly; the 4-point Lobatto rule does not for the cubic modes), to the 5
+    printed digits"""
+    g = gold(name)
+    pts, w = tensor_points(method, family, rdeg)
+    for order in range(4):
+        interp, deriv = po.modal_basis(order, pts)
+        P = interp.shape[1]
+        assert P == [1, 4, 10, 18][order]
+        vals = po.modal_apply(interp, deriv, 1, PRIMES[:P], INTERP)
+        ref = g[f"e{order}_values"]
+        np.testing.assert_allclose(vals, ref, rtol=5.1e-5, atol=1e-9 * np.abs(ref).max())
+        back = po.modal_apply(interp, deriv, 1, vals * w, INTERP_T)
+        ref = g[f"e{order}_mass_applied"]
+        np.testing.assert_allclose(back, ref, rtol=5.1e-5, atol=1e-9 * np.abs(ref).max())
+
+
+def test_modal_explicit_golden():
+    """jacobi-3-modal-gauss (src/jacobi/tests/ex3.c on the modal type, FAST Gauss rule of degree 6): interpolation
+    (Q, P), gradient (Q, 3P) and mass (P, P) matrices of the orders 0..3 to the 6 printed decimals; GRAD of each unit
+    mode is the gradient column block, as the reference's generic dEFSGetExplicit forms it"""
+    g = gold("jacobi3_modal_gauss")
+    pts, w = tensor_points(0, 0, 6)
+    for order in range(4):
+        interp, deriv = po.modal_basis(order, pts)
+        P = interp.shape[1]
+        grad = np.stack([po.modal_apply(interp, deriv, 1, np.eye(P)[j], GRAD).reshape(-1, 3) for j in range(P)], axis=1)
+        np.testing.assert_allclose(interp, g[f"e{order}_interpolation"], atol=6e-7)
+        np.testing.assert_allclose(grad.reshape(len(pts), 3 * P), g[f"e{order}_gradient"], atol=6e-7)
+        np.testing.assert_allclose(interp.T @ (w[:, None] * interp), g[f"e{order}_mass"], atol=6e-7)
+
+
+def test_modal_orders_and_modes_refused():
+    with pytest.raises(RuntimeError, match="Order 4"):
+        po.modal_basis(4, np.zeros((1, 3)))
+    interp, deriv = po.modal_basis(2, tensor_points(0, 0, 4)[0])
+    with pytest.raises(RuntimeError, match="Apply-mode not implemented"):
+        po.modal_apply(interp, deriv, 1, np.zeros(len(interp) * 3), GRAD_T)
