@@ -100,17 +100,47 @@ class EFS:
                                    ctypes.c_int(imode), _vp(stream)))
 
 
+class Mesh:
+    """A hexahedral mesh given by its entities (dMeshCreateFromConnectivity): vertex coordinates [nv][3], edges
+    [ne][2], quadrilaterals [nf][4] and hexahedra [nr][8] (ITAPS vertex order), each in creation order, as a dohp
+    caller builds one through iMesh. It has no boundary sets."""
+
+    def __init__(self, vtx, econn, fconn, hconn):
+        vtx = np.ascontiguousarray(vtx, np.float64).reshape(-1, 3)
+        conn = [np.ascontiguousarray(c, np.int32).ravel() for c in (econn, fconn, hconn)]
+        self.h = _vp()
+        chk(lib().dMeshCreateFromConnectivity(_i32(len(vtx)), ptr(vtx), _i32(len(conn[0]) // 2), ptr(conn[0]),
+                                              _i32(len(conn[1]) // 4), ptr(conn[1]), _i32(len(conn[2]) // 8), ptr(conn[2]),
+                                              ctypes.byref(self.h)))
+
+    def adjacency(self):
+        """dMeshGetAdjacency: toff [5], adjoff [nents+1], adjind, adjperm (copies)"""
+        toff = np.zeros(5, np.int32)
+        ao, ai, ap = [ctypes.POINTER(ctypes.c_int32)() for _ in range(3)]
+        chk(lib().dMeshGetAdjacency(self.h, ptr(toff), ctypes.byref(ao), ctypes.byref(ai), ctypes.byref(ap)))
+        adjoff = np.ctypeslib.as_array(ao, (int(toff[4]) + 1,)).copy()
+        na = int(adjoff[-1])
+        return toff, adjoff, np.ctypeslib.as_array(ai, (na,)).copy(), np.ctypeslib.as_array(ap, (na,)).copy()
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.dMeshDestroy(ctypes.byref(self.h))
+
+
 class FS:
-    """dFS on a seeded perturbed block mesh (dMeshGenerateBlock + dFSBuildSpace)."""
+    """dFS on a seeded perturbed block mesh (dMeshGenerateBlock + dFSBuildSpace), or on a given Mesh."""
 
     def __init__(self, npoints, degree=4, box=(0, 1, 0, 1, 0, 1), perturb=0.1, seed=1, bs=1,
-                 dirichlet=(100, 200, 300), elem_degree=None, stream=None, weak=(), mesh_of=None):
+                 dirichlet=(100, 200, 300), elem_degree=None, stream=None, weak=(), mesh_of=None, mesh=None):
         """mesh_of: another FS whose mesh this space shares (a second field on the same mesh, e.g. the pressure
-        of a Stokes pair); npoints, box, perturb and seed are then ignored"""
+        of a Stokes pair); mesh: a Mesh from connectivity (no boundary sets: pass dirichlet=()); npoints, box,
+        perturb and seed are then ignored"""
         L = lib()
         self.mesh = _vp()
-        self._mesh_owner = mesh_of
-        if mesh_of is not None:
+        self._mesh_owner = mesh_of if mesh is None else mesh
+        if mesh is not None:
+            self.mesh = mesh.h
+        elif mesh_of is not None:
             self.mesh = mesh_of.mesh
         else:
             chk(L.dMeshCreateBlock(ptr(np.asarray(npoints, np.int32)), ptr(np.asarray(box, np.float64)), _dbl(perturb),
@@ -167,6 +197,13 @@ class FS:
 
     def qpt_coords(self, xq):
         chk(lib().dFSGetQuadratureCoordinates(self.h, ptr(xq)))
+
+    def nodal_coordinates(self, expanded=True):
+        """dFSGetNodalCoordinatesExpanded [nexp][3] / dFSGetNodalCoordinatesGlobal [nc][3], host arrays"""
+        out = np.zeros(((self.nexp if expanded else self.nc), 3))
+        f = lib().dFSGetNodalCoordinatesExpanded if expanded else lib().dFSGetNodalCoordinatesGlobal
+        chk(f(self.h, ptr(out), ctypes.c_int(0)))
+        return out
 
     def lognormal(self, grf, kq):
         chk(lib().dFSEvaluateLognormal(self.h, ptr(np.ascontiguousarray(grf, np.float64)), ptr(kq)))

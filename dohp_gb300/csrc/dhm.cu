@@ -628,6 +628,7 @@ dErr dFSViewDHM(dFS fs, const char *name, dViewer v) {
   if (!fs->built) return set_error("dFS space not built");
   if (!*name || strlen(name) >= kStr - 16 || strchr(name, '/')) return set_error("DHM: FS name must be 1..%d characters without '/'", kStr - 17);
   _p_dMesh *m = fs->mesh;
+  if (!m->structured) return set_error("DHM: spaces on a mesh from connectivity are not written (block meshes only)");
   auto mit = v->meshname.find(m);  // one mesh group per dMesh
   if (mit == v->meshname.end()) mit = v->meshname.insert({m, "mesh" + std::to_string(v->meshname.size())}).first;
   const std::string mname = mit->second, mpath = "/dohp/mesh/" + mname + "/000";

@@ -87,6 +87,7 @@ struct _p_dMesh {
   std::vector<int64_t> econn, fconn, hconn;  // [ne][2], [nf][4], [nr][8]
   std::vector<signed char> fset;           // generator face set per entity (0..5) or -1
   std::vector<int32_t> adjoff, adjind, adjperm;
+  bool structured = true;  // a block (nx, ny, nz, lattice order); false: entities given by connectivity
 };
 
 struct _p_dFS {

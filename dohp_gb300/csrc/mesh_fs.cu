@@ -11,6 +11,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <array>
+#include <map>
 
 #include "internal.h"
 
@@ -219,6 +221,67 @@ dErr mesh_adjacency(_p_dMesh *m) {
           m->adjperm[a++] = perm;
         }
       }
+  m->adjoff[m->nents] = (int32_t)a;
+  return 0;
+}
+
+// dMeshGetAdjacency (mesh.c:1074-1191) for a mesh given by its entities: the same canonical sides and orientation
+// permutations as the block form above, each side's edge or face found by its vertices
+dErr mesh_adjacency_general(_p_dMesh *m) {
+  const int64_t E0 = m->nv, F0 = m->nv + m->ne, R0 = F0 + m->nf;
+  std::map<std::pair<int64_t, int64_t>, int64_t> edge_of;  // sorted vertex pair -> edge
+  for (int64_t e = 0; e < m->ne; e++) {
+    const int64_t a = m->econn[2 * e], b = m->econn[2 * e + 1];
+    if (a == b) return set_error("edge %lld has one vertex twice", (long long)e);
+    if (!edge_of.emplace(std::make_pair(std::min(a, b), std::max(a, b)), e).second)
+      return set_error("edge %lld repeats another edge", (long long)e);
+  }
+  std::map<std::array<int64_t, 4>, int64_t> face_of;  // sorted vertex quadruple -> face
+  for (int64_t f = 0; f < m->nf; f++) {
+    std::array<int64_t, 4> k = {m->fconn[4 * f], m->fconn[4 * f + 1], m->fconn[4 * f + 2], m->fconn[4 * f + 3]};
+    std::sort(k.begin(), k.end());
+    if (!face_of.emplace(k, f).second) return set_error("face %lld repeats another face", (long long)f);
+  }
+  m->adjoff.assign(m->nents + 1, 0);
+  m->adjind.assign(2 * m->ne + 4 * m->nf + 6 * m->nr, 0);
+  m->adjperm.assign(m->adjind.size(), 0);
+  int64_t a = 0;
+  for (int64_t e = 0; e < m->ne; e++) {
+    m->adjoff[E0 + e] = (int32_t)a;
+    m->adjind[a++] = (int32_t)m->econn[2 * e];
+    m->adjind[a++] = (int32_t)m->econn[2 * e + 1];
+  }
+  for (int64_t f = 0; f < m->nf; f++) {
+    m->adjoff[F0 + f] = (int32_t)a;
+    const int64_t *fv = &m->fconn[4 * f];
+    for (int s = 0; s < 4; s++) {
+      const int64_t v0 = fv[kQuadEdge[s][0]], v1 = fv[kQuadEdge[s][1]];
+      auto it = edge_of.find(std::make_pair(std::min(v0, v1), std::max(v0, v1)));
+      if (it == edge_of.end()) return set_error("no edge on side %d of face %lld", s, (long long)f);
+      m->adjind[a] = (int32_t)(E0 + it->second);
+      m->adjperm[a++] = m->econn[2 * it->second] == v0 ? 0 : 1;
+    }
+  }
+  for (int64_t r = 0; r < m->nr; r++) {
+    m->adjoff[R0 + r] = (int32_t)a;
+    const int64_t *rv = &m->hconn[8 * r];
+    for (int s = 0; s < 6; s++) {
+      std::array<int64_t, 4> k = {rv[kHexFace[s][0]], rv[kHexFace[s][1]], rv[kHexFace[s][2]], rv[kHexFace[s][3]]};
+      std::sort(k.begin(), k.end());
+      auto it = face_of.find(k);
+      if (it == face_of.end()) return set_error("no face on side %d of region %lld", s, (long long)r);
+      const int64_t *fv = &m->fconn[4 * it->second];
+      int perm = -1;
+      for (int t = 0; t < 8 && perm < 0; t++) {
+        bool match = true;
+        for (int c = 0; c < 4; c++) match = match && fv[kQuadPerm[t][c]] == rv[kHexFace[s][c]];
+        if (match) perm = t;
+      }
+      if (perm < 0) return set_error("face %lld is not a rotation or reflection of side %d of region %lld", (long long)it->second, s, (long long)r);
+      m->adjind[a] = (int32_t)(F0 + it->second);
+      m->adjperm[a++] = perm;
+    }
+  }
   m->adjoff[m->nents] = (int32_t)a;
   return 0;
 }
@@ -457,6 +520,8 @@ dErr fs_build_space(_p_dFS *fs) {
     maxdeg = *std::max_element(fs->elem_degree_in.begin(), fs->elem_degree_in.end());
   }
   if (maxdeg < 1 || maxdeg > MAXP - 1) return set_error("degree %d out of range [1,%d]", maxdeg, MAXP - 1);
+  if (!m->structured && (fs->dirichlet_mask || fs->weak_mask))
+    return set_error("boundary sets are those of the block generator: a mesh from connectivity has none");
   // isotropic degree tag then min-rule propagation (tables as tensor.c:201-204)
   std::vector<Ord> deg(m->nents);
   for (int64_t v = 0; v < m->nv; v++) deg[v] = {0, 0, 0};
@@ -588,6 +653,43 @@ dErr dMeshCreateBlock(const dInt npoints[3], const dReal box[6], dReal perturb, 
   return 0;
 }
 
+dErr dMeshCreateFromConnectivity(dInt nv, const dReal *vtx, dInt ne, const dInt *econn, dInt nf, const dInt *fconn, dInt nr,
+                                 const dInt *hconn, dMesh *mesh) {
+  if (!mesh || !vtx || (ne && !econn) || (nf && !fconn) || !hconn) return set_error("dMeshCreateFromConnectivity: null argument");
+  *mesh = nullptr;
+  if (nv < 8 || ne < 12 || nf < 6 || nr < 1) return set_error("dMeshCreateFromConnectivity: a hexahedral mesh needs its vertices, edges, faces and regions");
+  const struct { dInt n, k; const dInt *c; } lists[3] = {{ne, 2, econn}, {nf, 4, fconn}, {nr, 8, hconn}};
+  for (const auto &l : lists)
+    for (int64_t i = 0; i < (int64_t)l.n * l.k; i++)
+      if (l.c[i] < 0 || l.c[i] >= nv) return set_error("dMeshCreateFromConnectivity: vertex %d out of range [0,%d)", l.c[i], nv);
+  _p_dMesh *m = new _p_dMesh();
+  m->structured = false;
+  m->nx = m->ny = m->nz = 0;
+  m->nv = nv, m->ne = ne, m->nf = nf, m->nr = nr;
+  m->nents = (int64_t)nv + ne + nf + nr;
+  m->vx.assign(vtx, vtx + 3 * (size_t)nv);
+  m->econn.assign(econn, econn + 2 * (size_t)ne);
+  m->fconn.assign(fconn, fconn + 4 * (size_t)nf);
+  m->hconn.assign(hconn, hconn + 8 * (size_t)nr);
+  m->fset.assign(m->nents, -1);  // no boundary sets
+  dErr e = mesh_adjacency_general(m);
+  if (e) {
+    delete m;
+    return e;
+  }
+  *mesh = m;
+  return 0;
+}
+
+dErr dMeshGetAdjacency(dMesh m, dInt toff[5], const dInt **adjoff, const dInt **adjind, const dInt **adjperm) {
+  if (!m) return set_error("null mesh");
+  if (toff) toff[0] = 0, toff[1] = (dInt)m->nv, toff[2] = (dInt)(m->nv + m->ne), toff[3] = (dInt)(m->nv + m->ne + m->nf), toff[4] = (dInt)m->nents;
+  if (adjoff) *adjoff = m->adjoff.data();
+  if (adjind) *adjind = m->adjind.data();
+  if (adjperm) *adjperm = m->adjperm.data();
+  return 0;
+}
+
 dErr dMeshDestroy(dMesh *mesh) {
   if (mesh && *mesh) {
     delete *mesh;
@@ -599,6 +701,119 @@ dErr dMeshDestroy(dMesh *mesh) {
 dErr dMeshGetNumEnts(dMesh m, dInt counts[4]) {
   if (!m) return set_error("null mesh");
   counts[0] = (dInt)m->nv, counts[1] = (dInt)m->ne, counts[2] = (dInt)m->nf, counts[3] = (dInt)m->nr;
+  return 0;
+}
+
+}  // extern "C"
+
+namespace {
+
+// the coordinates of every expanded node: the element's trilinear map (its 8 vertices in tensor order, as the
+// coordinate space holds them, fsgeom.c:151) at its GLL nodes, [nexp][3] (dFSGetNodalCoordinatesExpanded,
+// fsgeom.c:17-58, which applies the coordinate space's INTERP on the Lobatto nodes of each element's degree)
+void nodal_coordinates_expanded(const _p_dFS *fs, std::vector<double> &out) {
+  static const int kConn[8] = {0, 4, 3, 7, 1, 5, 2, 6};
+  const _p_dMesh *m = fs->mesh;
+  out.assign(3 * (size_t)fs->nexp, 0.0);
+  for (int64_t r = 0; r < fs->nelem; r++) {
+    const int P[3] = {fs->edeg[3 * r] + 1, fs->edeg[3 * r + 1] + 1, fs->edeg[3 * r + 2] + 1};
+    double node[3][MAXP], w[MAXP];
+    for (int d = 0; d < 3; d++) lobatto_rule(P[d], node[d], w);
+    double X[8][3];
+    for (int v = 0; v < 8; v++)
+      for (int c = 0; c < 3; c++) X[v][c] = m->vx[3 * m->hconn[8 * r + kConn[v]] + c];
+    int64_t row = fs->xstart[r];
+    for (int a = 0; a < P[0]; a++)
+      for (int b = 0; b < P[1]; b++)
+        for (int cc = 0; cc < P[2]; cc++, row++) {
+          const double t[3] = {node[0][a], node[1][b], node[2][cc]};
+          double L[3][2];
+          for (int d = 0; d < 3; d++) L[d][0] = 0.5 * (1 - t[d]), L[d][1] = 0.5 * (1 + t[d]);
+          for (int c = 0; c < 3; c++) {
+            double s = 0;
+            for (int v = 0; v < 8; v++) s += L[0][v >> 2] * L[1][(v >> 1) & 1] * L[2][v & 1] * X[v][c];
+            out[3 * row + c] = s;
+          }
+        }
+  }
+}
+
+dErr copy_out(const std::vector<double> &h, dReal *coords, int on_device) {
+  if (on_device) CUCHK(cudaMemcpy(coords, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+  else std::copy(h.begin(), h.end(), coords);
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+dErr dFSGetNodalCoordinatesExpanded(dFS fs, dReal *coords, int on_device) {
+  if (!fs || !coords) return set_error("null argument");
+  if (!fs->built) return set_error("dFS space not built");
+  std::vector<double> h;
+  nodal_coordinates_expanded(fs, h);
+  return copy_out(h, coords, on_device);
+}
+
+// dFSGetNodalCoordinatesGlobal (fsgeom.c:72-107): every closure node's coordinates, the mean over its expanded
+// copies (E^T of the expanded coordinates over E^T of ones); rows of E that interpolate (hp constraints) are not
+// nodes of the closure and are skipped
+dErr dFSGetNodalCoordinatesGlobal(dFS fs, dReal *coords, int on_device) {
+  if (!fs || !coords) return set_error("null argument");
+  if (!fs->built) return set_error("dFS space not built");
+  std::vector<double> x, g(3 * (size_t)fs->nc, 0.0), count(fs->nc, 0.0);
+  nodal_coordinates_expanded(fs, x);
+  for (int64_t row = 0; row < fs->nexp; row++) {
+    const int32_t c = fs->emap[row];
+    if (c < 0) continue;
+    count[c] += 1;
+    for (int d = 0; d < 3; d++) g[3 * (size_t)c + d] += x[3 * row + d];
+  }
+  for (int64_t c = 0; c < fs->nc; c++)
+    for (int d = 0; d < 3; d++) g[3 * c + d] /= count[c];
+  return copy_out(g, coords, on_device);
+}
+
+// dFSGetSubElementMeshSize_Cont (cont.c:387-415): px py pz hexahedral sub-cells per element, the closure nodes as
+// vertices, 8 vertices per sub-cell
+dErr dFSGetSubElementMeshSize(dFS fs, dInt *nelems, dInt *nverts, dInt *nconn) {
+  if (!fs || !nelems || !nverts || !nconn) return set_error("null argument");
+  if (!fs->built) return set_error("dFS space not built");
+  int64_t nsub = 0;
+  for (int64_t r = 0; r < fs->nelem; r++) nsub += (int64_t)fs->edeg[3 * r] * fs->edeg[3 * r + 1] * fs->edeg[3 * r + 2];
+  if (8 * nsub > INT32_MAX) return set_error("sub-element mesh too large for 32-bit sizes");
+  *nelems = (dInt)nsub;
+  *nverts = (dInt)fs->nc;
+  *nconn = (dInt)(8 * nsub);
+  return 0;
+}
+
+// dFSGetSubElementMesh_Cont (cont.c:417-470): the sub-cells of each element in its SPARSE patch order (x-major), each
+// as 8 closure nodes in ITAPS hexahedron order (the tensor corners {0,4,6,2,1,5,7,3}); E must be Boolean there
+dErr dFSGetSubElementMesh(dFS fs, dInt nelems, dInt nconn, dEntTopology topo[], dInt off[], dInt ind[]) {
+  if (!fs || !topo || !off || !ind) return set_error("null argument");
+  dInt ns, nv, nc;
+  DCHK(dFSGetSubElementMeshSize(fs, &ns, &nv, &nc));
+  if (nelems < ns || nconn < nc) return set_error("Insufficient preallocation for the sub-element mesh (%d, %d needed)", ns, nc);
+  static const int kItapsToTensor[8] = {0, 4, 6, 2, 1, 5, 7, 3};
+  int64_t sub = 0, subc = 0;
+  for (int64_t r = 0; r < fs->nelem; r++) {
+    const int px = fs->edeg[3 * r], py = fs->edeg[3 * r + 1], pz = fs->edeg[3 * r + 2];
+    for (int i = 0; i < px; i++)
+      for (int j = 0; j < py; j++)
+        for (int k = 0; k < pz; k++, sub++) {
+          topo[sub] = dTOPO_HEX;
+          off[sub] = (dInt)subc;
+          for (int v = 0; v < 8; v++, subc++) {
+            const int t = kItapsToTensor[v], bi = t >> 2, bj = (t >> 1) & 1, bk = t & 1;
+            const int64_t row = fs->xstart[r] + ((int64_t)(i + bi) * (py + 1) + j + bj) * (pz + 1) + k + bk;
+            if (fs->emap[row] < 0) return set_error("Element assembly matrix is not boolean (row %lld)", (long long)row);
+            ind[subc] = fs->emap[row];
+          }
+        }
+  }
+  off[sub] = (dInt)subc;
   return 0;
 }
 

@@ -567,6 +567,7 @@ static dErr level_alloc(MGLevel &l, int bs) {
 // (M p + 1)-per-direction lattice L0; also used by the learned correction on the GLL lattice
 dErr fs_gll_lattice(_p_dFS *fs, std::vector<int32_t> &lat, int L0[3]) {
   if (!fs->uniform) return set_error("the GLL lattice needs a uniform-order space");
+  if (!fs->mesh->structured) return set_error("the GLL lattice needs a block mesh");
   const _p_dMesh *mesh = fs->mesh;
   const int p = fs->p, P = p + 1, My = mesh->ny - 1, Mz = mesh->nz - 1;
   L0[0] = (mesh->nx - 1) * p + 1, L0[1] = My * p + 1, L0[2] = Mz * p + 1;
@@ -607,6 +608,7 @@ dErr mg_build(_p_dMat *J, int degree, bool fp32, void **out) {
   const int bs = J->bs;
   if (bs != 1 && bs != 3) return set_error("Q1 multigrid: block size %d", bs);
   if (!fs->uniform) return set_error("Q1 multigrid needs a uniform-order space");
+  if (!fs->mesh->structured) return set_error("Q1 multigrid needs a block mesh (its GLL lattice)");
   const _p_dMesh *mesh = fs->mesh;
   const int p = fs->p, Mx = mesh->nx - 1, My = mesh->ny - 1, Mz = mesh->nz - 1;
   const int L0[3] = {Mx * p + 1, My * p + 1, Mz * p + 1};

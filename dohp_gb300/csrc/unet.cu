@@ -1082,6 +1082,7 @@ dErr dLearnedCreateOnGrid(dFS fs, dLearnedGrid grid, dInt crop, uint64_t seed, d
   Dims d0;
   std::vector<int32_t> vdof, Pp, Pc;
   std::vector<double> Pv, vxyz;
+  if (!mesh->structured) return set_error("learned correction needs a block mesh (its vertex or GLL lattice)");
   if (grid == dLEARNED_GRID_VERTEX) {
     d0 = {mesh->nx, mesh->ny, mesh->nz};
     if (std::min({d0.x, d0.y, d0.z}) < 5) return set_error("learned correction needs at least 4 elements per direction");

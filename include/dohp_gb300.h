@@ -203,6 +203,19 @@ dErr dEFSApplyBatched(dEFS efs, dInt nelem, const dReal *jinv, dInt D, const dSc
  * box = {x0,x1,y0,y1,z0,z1}, followed by a seeded perturbation of interior vertices by
  * U[-perturb h, perturb h] per coordinate (splitmix64(seed), vertex order) in place of dMeshMorph. */
 dErr dMeshCreateBlock(const dInt npoints[3], const dReal box[6], dReal perturb, uint64_t seed, dMesh *mesh);
+/* A hexahedral mesh given by its entities, as a dohp caller builds one through iMesh (src/fs/tests/ex1.c:48-104,
+ * cunit.c:76-136, fsex4.c:11-47): vertex coordinates vtx [nv][3], edges econn [ne][2], quadrilaterals fconn [nf][4] and
+ * hexahedra hconn [nr][8] (ITAPS vertex order), each in creation order; entities are numbered vertices, edges, faces,
+ * regions (dMeshGetAdjacency's toff). Every side of a hexahedron and of a face must be given. Adjacency and
+ * orientations as dMeshGetAdjacency (src/fs/mesh/interface/mesh.c:1039-1191). Such a mesh has no boundary sets: a
+ * dFS on it has no Dirichlet or weak sets (registering one is an error at dFSBuildSpace), and the block-lattice
+ * parts (Q1 multigrid, learned correction, DHM output) refuse it. */
+dErr dMeshCreateFromConnectivity(dInt nv, const dReal *vtx, dInt ne, const dInt *econn, dInt nf, const dInt *fconn, dInt nr,
+                                 const dInt *hconn, dMesh *mesh);
+/* dMeshGetAdjacency (mesh.c:1074-1191, include/dohpmesh.h dMeshAdjacency): toff = the first entity of each type
+ * (vertex, edge, face, region, end); adjoff [nents+1], adjind (edges: their 2 vertices; faces: 4 edges; regions:
+ * 6 faces, canonical side order), adjperm (orientation of each side). Arrays owned by the mesh. */
+dErr dMeshGetAdjacency(dMesh mesh, dInt toff[5], const dInt **adjoff, const dInt **adjind, const dInt **adjperm);
 dErr dMeshDestroy(dMesh *mesh);
 dErr dMeshGetNumEnts(dMesh mesh, dInt counts[4]); /* vertices, edges, faces, regions */
 
@@ -323,6 +336,18 @@ dErr dRulesetDestroy(dRuleset *rset);
 /* dFSGetCoordinateFS (src/fs/interface/fsgeom.c:176-204): the Q1, block size 3 space of vertex coordinates on the same mesh,
  * owned by fs; its expanded vector is dFSGetGeometryVectorExpanded's [nelem][8][3] */
 dErr dFSGetCoordinateFS(dFS fs, dFS *cfs);
+/* dFSGetNodalCoordinatesExpanded (src/fs/interface/fsgeom.c:17-58): the coordinates of every expanded node (each
+ * element's trilinear map at its GLL nodes), coords [nexp][3]; dFSGetNodalCoordinatesGlobal (fsgeom.c:72-107): every
+ * closure node's coordinates (the mean of its expanded copies), coords [nc][3]. coords is a device pointer when
+ * on_device, else host memory. After dFSBuildSpace. */
+dErr dFSGetNodalCoordinatesExpanded(dFS fs, dReal *coords, int on_device);
+dErr dFSGetNodalCoordinatesGlobal(dFS fs, dReal *coords, int on_device);
+/* dFSGetSubElementMeshSize / dFSGetSubElementMesh (src/fs/interface/fsgeom.c:257-285, cont.c:387-470): the Q1
+ * sub-cell mesh of the space for visualization: p_x p_y p_z hexahedra per element (SPARSE patch order), their
+ * vertices the closure nodes (nverts = nc), off [nelems+1], ind [nconn] in ITAPS hexahedron vertex order, topo all
+ * dTOPO_HEX. Host arrays; needs a Boolean E (no hp constraint rows). */
+dErr dFSGetSubElementMeshSize(dFS fs, dInt *nelems, dInt *nverts, dInt *nconn);
+dErr dFSGetSubElementMesh(dFS fs, dInt nelems, dInt nconn, dEntTopology topo[], dInt off[], dInt ind[]);
 /* dRulesetCreateIterator (fsrulesetit.c:129-150): link 0 = cfs (coordinates) */
 dErr dRulesetCreateIterator(dRuleset rset, dFS cfs, dRulesetIterator *it);
 /* dRulesetIteratorAddFS (fsrulesetit.c:161-181): one more field link (same mesh, any degrees on FAST rules) */

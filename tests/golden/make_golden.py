@@ -64,6 +64,100 @@ def modal_values(root, name):
     return {k: np.array(v) for k, v in out.items()}
 
 
+def c_arrays(root, rel, names):
+    """integer / real array initialisers {..} of the named C arrays in a reference source file (test input data)"""
+    src = "\n".join(read(root, rel))
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    out = {}
+    for name in names:
+        m = re.search(r"\b" + re.escape(name) + r"\s*\[[^\]]*\]\s*=\s*\{(.*?)\}\s*[;,]", src, re.S)
+        assert m, (rel, name)
+        out[name] = np.array([float(v) for v in NUM.findall(m.group(1))])
+    return out
+
+
+def hex_meshes(root):
+    """The hand-built MOAB meshes of the fs tests (vertices, edges, faces, hexahedra in creation order) and the
+    adjacency ex1.c verifies by hand (verifyAdjacencies, src/fs/tests/ex1.c:106-138); the affine deformation of
+    cunit.c"""
+    a = c_arrays(root, "src/fs/tests/ex1.c", ["vtx_affine", "vtx_parametric", "rconn", "fconn", "econn", "toff", "adjoff",
+                                              "adjind", "adjperm"])
+    out = {"ex1_" + k: v for k, v in a.items()}
+    b = c_arrays(root, "src/fs/tests/cunit.c", ["vtx_base", "rconn", "fconn", "econn"])
+    out.update({"cunit_" + k: v for k, v in b.items()})
+    src = "\n".join(read(root, "src/fs/tests/cunit.c"))
+    m = re.search(r"tmpctx\s*=\s*\{\.A\s*=\s*\{(.*?)\}\s*,\s*\.b\s*=\s*\{(.*?)\}\s*\}", src, re.S)
+    out["cunit_affine_A"] = np.array([float(v) for v in NUM.findall(m.group(1))]).reshape(3, 3)
+    out["cunit_affine_b"] = np.array([float(v) for v in NUM.findall(m.group(2))])
+    c = c_arrays(root, "src/fs/tests/fsex4.c", ["vtx", "econn", "fconn", "rconn"])
+    out.update({"fsex4_" + k: v for k, v in c.items()})
+    return out
+
+
+def cunit(root, name):
+    """cunit-*: the expanded vector of closure indices + 1000, the expanded (Q1) coordinates and the coordinates of the
+    expanded nodes (degree 2 on the two-hex mesh)"""
+    lines = read(root, f"src/fs/tests/refout/{name}.refout")
+    out, key = {}, None
+    for ln in lines:
+        if ln.startswith("Expanded vector"):
+            key = "expanded"
+        elif ln.startswith("Expanded coordinate vector"):
+            key = "cexp"
+        elif ln.startswith("Nodal coordinates in expanded space"):
+            key = "nce"
+        elif ln.startswith("Comparison of"):
+            key = None
+        elif key == "expanded" and re.fullmatch(r"\s*\d+(\.\d+)?\s*", ln):
+            out.setdefault(key, []).append(float(ln))
+        elif key in ("cexp", "nce") and ln.startswith("[0]"):
+            out.setdefault(key, []).append([float(v) for v in ln.split(":", 1)[1].split()])
+    return {k: np.array(v) for k, v in out.items()}
+
+
+def submesh(root, name):
+    """fsex4-submesh-*: sub-element offsets and connectivity, closure node coordinates (before any read back)"""
+    lines = read(root, f"src/fs/tests/refout/{name}.refout")
+    out, key = {}, None
+    for ln in lines:
+        if ln.startswith("Offsets for"):
+            if "off" in out:
+                break  # the read-back copy repeats the same tables
+            key = "off"
+        elif ln.startswith("Connectivity"):
+            key = "conn"
+        elif ln.startswith("Coordinates"):
+            key = "coords"
+        elif ln.startswith("[0] DHM") or ln.startswith("Loaded"):
+            break
+        elif key in ("off", "conn") and re.match(r"\s*\d+:", ln):
+            out.setdefault(key, []).extend(int(v) for v in ln.split(":", 1)[1].split())
+        elif key == "coords" and re.fullmatch(r"\s*-?[\d.e+-]+\s*", ln):
+            out.setdefault(key, []).append(float(ln))
+    return {k: np.array(v) for k, v in out.items()}
+
+
+def projection(root, name):
+    """fs-mf-projection-* / fs-mf-op-proj-*: sizes, the sums of ex1.c's useFS, the SNES function norms and the
+    projection residual norms"""
+    lines = read(root, f"src/fs/tests/refout/{name}.refout")
+    out = {"snes": []}
+    for ln in lines:
+        m = re.match(r"expanded size (\d+), global size (\d+)", ln)
+        if m:
+            out["sizes"] = [int(m.group(1)), int(m.group(2))]
+        m = re.match(r"\|x\| = (\S+), \|g\| = (\S+), \|y\| = (\S+)", ln)
+        if m:
+            out["sums"] = [float(m.group(k)) for k in (1, 2, 3)]
+        m = re.match(r"\s*\d+ SNES Function norm (< 1.e-11|\S+)", ln)
+        if m:
+            out["snes"].append(0.0 if m.group(1).startswith("<") else float(m.group(1)))
+        m = re.match(r"(Algebraic|Pointwise|Gradient) .*\|x\|_1 (\S+)\s+\|x\|_2 (\S+)\s+\|x\|_inf (\S+)", ln)
+        if m:
+            out[m.group(1).lower()] = [float(m.group(k)) for k in (2, 3, 4)]
+    return {k: np.array(v) for k, v in out.items()}
+
+
 def sparse_bases(root, name, max_patches=4):
     lines = read(root, f"src/jacobi/tests/refout/{name}.refout")
     tabs = {}
@@ -210,6 +304,16 @@ def main(root):
         "jacobi2_modal_fast_gauss": modal_values(root, "jacobi-2-modal-fast-gauss"),
         "jacobi2_modal_fast_lobatto": modal_values(root, "jacobi-2-modal-fast-lobatto"),
         "jacobi2_modal_sparse_gauss": modal_values(root, "jacobi-2-modal-sparse-gauss"),
+        "hex_meshes": hex_meshes(root),
+        "cunit_identity_0": cunit(root, "cunit-identity-0"),
+        "cunit_affine_0": cunit(root, "cunit-affine-0"),
+        "fsex4_submesh_p1": submesh(root, "fsex4-submesh-p1"),
+        "fsex4_submesh_p2": submesh(root, "fsex4-submesh-p2-read"),
+        "fs_mf_projection_v1": projection(root, "fs-mf-projection-v1"),
+        "fs_mf_projection_v3": projection(root, "fs-mf-projection-v3"),
+        "fs_mf_projection_v3_sparse": projection(root, "fs-mf-projection-v3-sparse"),
+        "fs_mf_op_proj_0": projection(root, "fs-mf-op-proj-0"),
+        "fs_mf_op_proj_1": projection(root, "fs-mf-op-proj-1"),
         "jacobi3_sparsex_r4": sparse_bases(root, "jacobi-3-tensor-sparsex-r4"),
         "jacobi3_sparsex_r6": sparse_bases(root, "jacobi-3-tensor-sparsex-r6"),
         "jacobi4_fast": patches(root, "jacobi-4-tensor-fast"),
