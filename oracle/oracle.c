@@ -1397,6 +1397,19 @@ static void qfunction(int kind, int D, const double *qd, const double *param, do
     const double etaw = pow(eps * eps + gamma, (pe - 2) / 2) * w;
     v[0] = 0;
     for (int i = 0; i < 3; i++) dv[i] = etaw * du[i];
+  } else if (kind == 7) { /* EllipPointwiseFunction (ellip.c:355-367) with the Bratu term, param = {p, eps, lambda}:
+                           v = -w lambda e^u, Dv = w eta Du (forcing added by the caller) */
+    const double pe = param[0], eps = param[1], lam = param[2];
+    const double gamma = 0.5 * (du[0] * du[0] + du[1] * du[1] + du[2] * du[2]);
+    const double etaw = pow(eps * eps + gamma, (pe - 2) / 2) * w;
+    v[0] = lam != 0 ? -w * lam * exp(u[0]) : 0; /* lambda_exp_u of EllipPointwiseComputeStore (ellip.c:341) */
+    for (int i = 0; i < 3; i++) dv[i] = etaw * du[i];
+  } else if (kind == 8) { /* EllipPointwiseJacobian (ellip.c:370-377) with the store [eta, sqrt(-eta') Du, lambda e^u]:
+                           v = -w lambda e^u u, Dv = w (eta Du - (s . Du) s) */
+    const double eta = qd[0], *s = qd + 1;
+    const double dotw = (s[0] * du[0] + s[1] * du[1] + s[2] * du[2]) * w, etaw = eta * w;
+    v[0] = -w * qd[4] * u[0];
+    for (int i = 0; i < 3; i++) dv[i] = etaw * du[i] - dotw * s[i];
   } else if (kind == 3) { /* mass: the right-hand side b = int v f_h of src/fs/tests/ex1.c:399-430 */
     v[0] = w * u[0];
     dv[0] = dv[1] = dv[2] = 0;
@@ -1461,6 +1474,7 @@ static int operator_eval(const or_fs *m, int kind, const double *qdata, const do
         if (kind == 0 && qdata) qd = qdata + qoff[r] + q;
         if (kind == 1) qd = qdata + 4 * (int64_t)(qoff[r] + q);
         if (kind == 5) qd = qdata + 9 * (int64_t)(qoff[r] + q);
+        if (kind == 8) qd = qdata + 5 * (int64_t)(qoff[r] + q);
         qfunction(kind, D, qd, param, jw[q], u + q * D, du + q * 3 * D, v + q * D, dv + q * 3 * D);
         if (fq) /* body force: the coefficient of v is -w f (ellip.c:362, elast.c:261) */
           for (int c = 0; c < D; c++) v[q * D + c] += -jw[q] * fq[(int64_t)(qoff[r] + q) * D + c];
@@ -1484,7 +1498,8 @@ int or_operator_apply(const or_fs *m, int kind, const double *qdata, const doubl
 int or_operator_function(const or_fs *m, int kind, const double *param, const double *g, const double *dcache,
                          const double *fq, double *y, int nthreads)
 {
-  if (kind != 4 && kind != 6) return or_fail("or_operator_function: kind 4 (St. Venant-Kirchhoff) or 6 (p-Laplacian)");
+  if (kind != 4 && kind != 6 && kind != 7)
+    return or_fail("or_operator_function: kind 4 (St. Venant-Kirchhoff), 6 or 7 (p-Laplacian, 7 with the Bratu term)");
   return operator_eval(m, kind, NULL, param, g, dcache, fq, y, nthreads);
 }
 

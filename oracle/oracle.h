@@ -105,6 +105,9 @@ void or_fs_expanded_to_global(const or_fs *fs, const double *x, double *g, int a
  * kind 4: St. Venant-Kirchhoff function at the state g (ElastPointwiseFunction, elast.c:256-266, no body force)
  * kind 5: St. Venant-Kirchhoff Jacobian at the stashed deformation gradients qdata [nq][9] (elast.c:268-280)
  * kind 6: p-Laplacian function, param = {p, eps} (EllipPointwiseFunction, ellip.c:355-367, lambda = 0, no forcing)
+ * kind 7: the same with the Bratu term, param = {p, eps, lambda}: v = -w lambda e^u (ellip.c:341, 363)
+ * kind 8: p-Laplacian Jacobian with the Bratu term at the store qdata [nq][5] = {eta, sqrt(-eta') Du, lambda e^u}
+ *         (EllipPointwiseJacobian, ellip.c:370-377)
  * nthreads: OpenMP threads over element ranges (the reference runs one MPI rank per core). */
 int or_operator_apply(const or_fs *fs, int kind, const double *qdata, const double *param,
                       const double *g, double *y, int nthreads);

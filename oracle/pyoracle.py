@@ -319,7 +319,8 @@ class FS:
         return xq.reshape(nq, 3)
 
     def function(self, g, kind, param, dcache=None, fq=None, nthreads=1):
-        """or_operator_function: EllipFunction (kind 6, param (p, eps)) or ElastFunction (kind 4, param (lambda, mu))
+        """or_operator_function: EllipFunction (kind 6, param (p, eps); kind 7 with the Bratu term, param (p, eps, lambda))
+        or ElastFunction (kind 4, param (lambda, mu))
         with the Dirichlet values dcache and the body force fq at qpt_coords()"""
         y = np.zeros(self.n * self.bs)
         keep = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (dcache, fq)]

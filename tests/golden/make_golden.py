@@ -327,6 +327,7 @@ def main(root):
         "ellip_e0_b1_p16": solver_log(root, "ellip-e0-b1-p16"),
         "ellip_e0_b3_p16": solver_log(root, "ellip-e0-b3-p16"),
         "ellip_e0_b3_p14": solver_log(root, "ellip-e0-b3-p14-sse"),
+        "ellip_e0_b3_p17_lam1": solver_log(root, "ellip-e0-b3-p17-lam1-sse"),
         "elast_e0_b3_g01": solver_log(root, "elast-e0-b3-g01"),
         "ellip_morph": solver_log(root, "ellip-morph"),
         "ellip_morph_qfast": solver_log(root, "ellip-morph-qfast"),

@@ -6,6 +6,9 @@ walls (sets 100, 200, 300).
 
   ellip-e0-b{1,3}-p16, -b3-p14: u = cos(a x) exp(b y) sin(c z), (a, b, c) = (1.6, 1.7, 1.8) (ellip.c:42-57), the
     p-Laplacian with eps = 1 (ellip.c:153-161) at p = 1.6 / 1.4, degree 1 or 3;
+  ellip-e0-b3-p17-lam1-sse: the same solution with (a, b, c) = (1, 1, 1) (ellip.c:199), p = 1.7, degree 3 and the
+    Bratu term lambda e^u with lambda = 1 (ellip.c:341, 363, 375), which the forcing does not include (the discrete
+    solution then differs from the exact one by about 0.4);
   elast-e0-b3-g01: ElastExact_0 (elastexact.py:74-79), (a, b, c) = (0.98, 1.01, 1.01), E = 1, nu = 0.3
     (elast.c:91-96, 99-110), degree 3.
 
@@ -56,6 +59,7 @@ CASES = {  # name: (degree, bs, function kind, param, exact)
     "ellip_e0_b1_p16": (1, 1, 6, (1.6, 1.0), lambda: ellip_exact(1.6, 1.7, 1.8, 1.6, 1.0)),
     "ellip_e0_b3_p16": (3, 1, 6, (1.6, 1.0), lambda: ellip_exact(1.6, 1.7, 1.8, 1.6, 1.0)),
     "ellip_e0_b3_p14": (3, 1, 6, (1.4, 1.0), lambda: ellip_exact(1.6, 1.7, 1.8, 1.4, 1.0)),
+    "ellip_e0_b3_p17_lam1": (3, 1, 7, (1.7, 1.0, 1.0), lambda: ellip_exact(1.0, 1.0, 1.0, 1.7, 1.0)),
     "elast_e0_b3_g01": (3, 3, 4, (LAM, MU), lambda: elast_exact(0.98, 1.01, 1.01, LAM, MU)),
 }
 
@@ -81,29 +85,43 @@ class Problem:
     def qdata(self, x):
         """the Jacobian's store at the state x with the Dirichlet values: [eta, sqrt(-eta') Du] of
         EllipPointwiseComputeStore (ellip.c:333-342), or the deformation gradient I + Du (elast.c:224-225)"""
-        _, du, _ = self.fs.eval_points(x, self.dc)
-        if self.kind == 6:
-            pe, eps = self.param
+        u, du, _ = self.fs.eval_points(x, self.dc)
+        if self.kind in (6, 7):
+            pe, eps = self.param[:2]
             g = du[:, 0, :]
             espg = eps ** 2 + 0.5 * (g ** 2).sum(1)
             eta = espg ** ((pe - 2) / 2)
-            return np.concatenate([eta[:, None], np.sqrt(-(pe - 2) / 2 * eta / espg)[:, None] * g], 1).ravel()
+            st = [eta[:, None], np.sqrt(-(pe - 2) / 2 * eta / espg)[:, None] * g]
+            if self.kind == 7:  # lambda e^u, the Bratu term's Jacobian coefficient (ellip.c:341)
+                st.append(self.param[2] * np.exp(u[:, :1]))
+            return np.concatenate(st, 1).ravel()
         return (np.eye(3)[None] + du).reshape(-1)
 
-    def solve(self):
+    def jacobian(self, x):
         n = self.s.size
-        qd = self.qdata(self.s)
+        qd = self.qdata(x)
+        kind = {6: 1, 7: 8, 4: 5}[self.kind]
         J = np.zeros((n, n))
         e = np.zeros(n)
         for j in range(n):
             e[j] = 1
-            J[:, j] = self.fs.apply(e, kind=1 if self.kind == 6 else 5, qdata=qd, param=self.param)
+            J[:, j] = self.fs.apply(e, kind=kind, qdata=qd, param=self.param)
             e[j] = 0
-        lu = sl.lu_factor(J)
+        return J
+
+    def solve(self):
+        """chord iteration from the interpolant of the exact solution with the Jacobian there; with the Bratu term the
+        discrete solution is far from that interpolant, so Newton steps (Jacobian at the iterate) come first"""
+        n = self.s.size
         x = self.s.copy()
+        F0 = max(1.0, np.linalg.norm(self.F(np.zeros(n))))
+        newton = 6 if self.kind == 7 else 0
+        for _ in range(newton):
+            x = x - np.linalg.solve(self.jacobian(x), self.F(x))
+        lu = sl.lu_factor(self.jacobian(x))
         for _ in range(40):
             Fx = self.F(x)
-            if np.linalg.norm(Fx) < 1e-12 * max(1.0, np.linalg.norm(self.F(np.zeros(n)))):
+            if np.linalg.norm(Fx) < 1e-12 * F0:
                 break
             x = x - sl.lu_solve(lu, Fx)
         return x
