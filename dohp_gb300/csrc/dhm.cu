@@ -628,7 +628,6 @@ dErr dFSViewDHM(dFS fs, const char *name, dViewer v) {
   if (!fs->built) return set_error("dFS space not built");
   if (!*name || strlen(name) >= kStr - 16 || strchr(name, '/')) return set_error("DHM: FS name must be 1..%d characters without '/'", kStr - 17);
   _p_dMesh *m = fs->mesh;
-  if (!m->structured) return set_error("DHM: spaces on a mesh from connectivity are not written (block meshes only)");
   auto mit = v->meshname.find(m);  // one mesh group per dMesh
   if (mit == v->meshname.end()) mit = v->meshname.insert({m, "mesh" + std::to_string(v->meshname.size())}).first;
   const std::string mname = mit->second, mpath = "/dohp/mesh/" + mname + "/000";
@@ -636,10 +635,16 @@ dErr dFSViewDHM(dFS fs, const char *name, dViewer v) {
   auto mg = ensure_group(ensure_group(meshroot, mname), "000");
   if (mg->links.empty()) {  // the mesh itself (the reference writes a MOAB file and its name here)
     std::vector<int64_t> hex(m->hconn.begin(), m->hconn.end());
-    const int32_t np[3] = {m->nx, m->ny, m->nz};
     mg->links.push_back({"vertices", dataset(t_f64(), {(uint64_t)m->nv, 3}, bytes_of(m->vx.data(), m->vx.size()))});
     mg->links.push_back({"hexes", dataset(t_int(8), {(uint64_t)m->nr, 8}, bytes_of(hex.data(), hex.size()))});
-    mg->links.push_back({"npoints", dataset(t_int(4), {3}, bytes_of(np, 3))});
+    if (m->structured) {  // a block: its extents give the entity order back
+      const int32_t np[3] = {m->nx, m->ny, m->nz};
+      mg->links.push_back({"npoints", dataset(t_int(4), {3}, bytes_of(np, 3))});
+    } else {  // a mesh from connectivity: its edges and faces in their order
+      std::vector<int64_t> ed(m->econn.begin(), m->econn.end()), fa(m->fconn.begin(), m->fconn.end());
+      mg->links.push_back({"edges", dataset(t_int(8), {(uint64_t)m->ne, 2}, bytes_of(ed.data(), ed.size()))});
+      mg->links.push_back({"faces", dataset(t_int(8), {(uint64_t)m->nf, 4}, bytes_of(fa.data(), fa.size()))});
+    }
   }
   // per-FS tags (the reference's degree and boundary-status tags of the MOAB mesh)
   const std::string deg_name = std::string(name) + "_degree", bst_name = std::string(name) + "_bstatus";
@@ -739,20 +744,36 @@ dErr dFSLoadDHM(dViewer v, const char *name, dJacobi jac, dMesh *mesh, dFS *fs) 
   FSRec r;
   memcpy(&r, rec->data.data(), sizeof r);
   auto mg = lookup(v->root, std::string(r.mesh, strnlen(r.mesh, kStr)));
-  auto vx = child(mg, "vertices"), np = child(mg, "npoints");
+  auto vx = child(mg, "vertices"), np = child(mg, "npoints"), hx = child(mg, "hexes");
+  auto eds = child(mg, "edges"), fas = child(mg, "faces");
   auto deg = child(mg, std::string(r.degree, strnlen(r.degree, kStr))), bst = child(mg, std::string(r.bstatus, strnlen(r.bstatus, kStr)));
-  if (!vx || !np || !deg || !bst) return set_error("DHM: incomplete mesh record for FS \"%s\"", name);
-  int32_t npts[3], masks[2];
-  memcpy(npts, np->data.data(), sizeof npts);
+  if (!vx || !hx || !(np || (eds && fas)) || !deg || !bst) return set_error("DHM: incomplete mesh record for FS \"%s\"", name);
+  int32_t masks[2];
   memcpy(masks, bst->data.data(), sizeof masks);
-  const dReal box[6] = {0, 1, 0, 1, 0, 1};
-  DCHK(dMeshCreateBlock(npts, box, 0.0, 0, mesh));
-  _p_dMesh *m = *mesh;
-  if (vx->data.size() != m->vx.size() * sizeof(double)) {
-    dMeshDestroy(mesh);
-    return set_error("DHM: vertex count of the file does not match its block extents");
+  if (np) {
+    int32_t npts[3];
+    memcpy(npts, np->data.data(), sizeof npts);
+    const dReal box[6] = {0, 1, 0, 1, 0, 1};
+    DCHK(dMeshCreateBlock(npts, box, 0.0, 0, mesh));
+    _p_dMesh *m = *mesh;
+    if (vx->data.size() != m->vx.size() * sizeof(double)) {
+      dMeshDestroy(mesh);
+      return set_error("DHM: vertex count of the file does not match its block extents");
+    }
+    memcpy(m->vx.data(), vx->data.data(), vx->data.size());
+  } else {  // a mesh from connectivity: entities in the order written
+    auto ints = [](const std::shared_ptr<Node> &d, std::vector<dInt> &out) {
+      const int64_t *p = (const int64_t *)d->data.data();
+      out.resize(d->data.size() / sizeof(int64_t));
+      for (size_t i = 0; i < out.size(); i++) out[i] = (dInt)p[i];
+    };
+    std::vector<dInt> e2, f4, h8;
+    ints(eds, e2), ints(fas, f4), ints(hx, h8);
+    DCHK(dMeshCreateFromConnectivity((dInt)(vx->data.size() / (3 * sizeof(double))), (const double *)vx->data.data(),
+                                     (dInt)(e2.size() / 2), e2.data(), (dInt)(f4.size() / 4), f4.data(), (dInt)(h8.size() / 8),
+                                     h8.data(), mesh));
   }
-  memcpy(m->vx.data(), vx->data.data(), vx->data.size());
+  _p_dMesh *m = *mesh;
   dErr e = dFSCreate(m, jac, fs);
   const int32_t *dg = (const int32_t *)deg->data.data();
   const int64_t ne = (int64_t)deg->dims[0];

@@ -209,7 +209,7 @@ dErr dMeshCreateBlock(const dInt npoints[3], const dReal box[6], dReal perturb, 
  * regions (dMeshGetAdjacency's toff). Every side of a hexahedron and of a face must be given. Adjacency and
  * orientations as dMeshGetAdjacency (src/fs/mesh/interface/mesh.c:1039-1191). Such a mesh has no boundary sets: a
  * dFS on it has no Dirichlet or weak sets (registering one is an error at dFSBuildSpace), and the block-lattice
- * parts (Q1 multigrid, learned correction, DHM output) refuse it. */
+ * parts (Q1 multigrid, learned correction) refuse it. DHM files hold its entities (dFSLoadDHM rebuilds it). */
 dErr dMeshCreateFromConnectivity(dInt nv, const dReal *vtx, dInt ne, const dInt *econn, dInt nf, const dInt *fconn, dInt nr,
                                  const dInt *hconn, dMesh *mesh);
 /* dMeshGetAdjacency (mesh.c:1074-1191, include/dohpmesh.h dMeshAdjacency): toff = the first entity of each type

@@ -116,24 +116,30 @@ def cunit(root, name):
 
 
 def submesh(root, name):
-    """fsex4-submesh-*: sub-element offsets and connectivity, closure node coordinates (before any read back)"""
+    """fsex4-submesh-*: sub-element offsets and connectivity, closure node coordinates; with -read_back the same
+    printed again from the space read back from the DHM file (suffix _read), the file's step time and, with
+    -read_back_vec, the vector read back"""
     lines = read(root, f"src/fs/tests/refout/{name}.refout")
-    out, key = {}, None
+    out, key, sfx = {}, None, ""
     for ln in lines:
+        m = re.match(r"\[0\] step 0\s+time (\S+)", ln)
+        if m:
+            out["time"] = [float(m.group(1))]
         if ln.startswith("Offsets for"):
-            if "off" in out:
-                break  # the read-back copy repeats the same tables
+            sfx = "_read" if "off" in out else ""
             key = "off"
         elif ln.startswith("Connectivity"):
             key = "conn"
         elif ln.startswith("Coordinates"):
             key = "coords"
-        elif ln.startswith("[0] DHM") or ln.startswith("Loaded"):
-            break
+        elif ln.startswith("Loaded vector"):
+            key, sfx = "loaded", ""
+        elif ln.startswith("[0]"):
+            key = None
         elif key in ("off", "conn") and re.match(r"\s*\d+:", ln):
-            out.setdefault(key, []).extend(int(v) for v in ln.split(":", 1)[1].split())
-        elif key == "coords" and re.fullmatch(r"\s*-?[\d.e+-]+\s*", ln):
-            out.setdefault(key, []).append(float(ln))
+            out.setdefault(key + sfx, []).extend(int(v) for v in ln.split(":", 1)[1].split())
+        elif key in ("coords", "loaded") and re.fullmatch(r"\s*-?[\d.e+-]+\s*", ln):
+            out.setdefault(key + sfx, []).append(float(ln))
     return {k: np.array(v) for k, v in out.items()}
 
 
@@ -308,6 +314,7 @@ def main(root):
         "cunit_identity_0": cunit(root, "cunit-identity-0"),
         "cunit_affine_0": cunit(root, "cunit-affine-0"),
         "fsex4_submesh_p1": submesh(root, "fsex4-submesh-p1"),
+        "fsex4_submesh_p1_read": submesh(root, "fsex4-submesh-p1-read"),
         "fsex4_submesh_p2": submesh(root, "fsex4-submesh-p2-read"),
         "fs_mf_projection_v1": projection(root, "fs-mf-projection-v1"),
         "fs_mf_projection_v3": projection(root, "fs-mf-projection-v3"),

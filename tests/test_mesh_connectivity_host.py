@@ -157,3 +157,45 @@ def test_connectivity_errors(L):
     assert L.dFSBuildSpace(h) != 0
     assert b"a mesh from connectivity has none" in L.dGetLastError()
     L.dFSDestroy(ctypes.byref(h))
+
+
+@pytest.mark.parametrize("degree,name", [(1, "fsex4_submesh_p1_read"), (2, "fsex4_submesh_p2")])
+def test_fsex4_read_back(L, tmp_path, degree, name):
+    """fsex4-submesh-p1-read / -p2-read: the space and its vector 0.1 i (FSEx4FillVec, fsex4.c:85-97) written to a
+    DHM file at time 0.1 and read back (dFSLoadDHM rebuilds the mesh from the entities written): one step at time
+    0.1, the same sub-element mesh and closure coordinates, and the vector"""
+    g = gold(name)
+    fs = HostFS(L, mesh_of("fsex4_"), degree)
+    x = 0.1 * np.arange(fs.nc)
+    path = str(tmp_path / "fsex4.dhm").encode()
+    v = ctypes.c_void_p()
+    dg.chk(L.dViewerDHMOpen(path, ctypes.c_int(1), ctypes.byref(v)))
+    dg.chk(L.dViewerDHMSetTime(v, ctypes.c_double(0.1)))
+    dg.chk(L.dFSViewDHM(fs.h, b"dFS_0", v))
+    dg.chk(L.dVecViewDHM(fs.h, b"Vec_global_0", dg.ptr(x), ctypes.c_int(0), v))
+    dg.chk(L.dViewerDestroy(ctypes.byref(v)))
+    dg.chk(L.dViewerDHMOpen(path, ctypes.c_int(0), ctypes.byref(v)))
+    ns = ctypes.c_int32()
+    dg.chk(L.dViewerDHMGetSteps(v, ctypes.byref(ns), None))
+    times = np.zeros(ns.value)
+    dg.chk(L.dViewerDHMGetSteps(v, ctypes.byref(ns), dg.ptr(times)))
+    np.testing.assert_array_equal(times, g["time"])
+    mesh2, h2 = ctypes.c_void_p(), ctypes.c_void_p()
+    dg.chk(L.dFSLoadDHM(v, b"dFS_0", None, ctypes.byref(mesh2), ctypes.byref(h2)))
+    back = HostFS.__new__(HostFS)
+    back.L, back._mesh, back.h = L, None, h2
+    sz = [ctypes.c_int32() for _ in range(5)]
+    dg.chk(L.dFSGetSizes(h2, *[ctypes.byref(s) for s in sz]))
+    back.n, back.nc, back.nexp, back.bs, back.nelem = [s.value for s in sz]
+    nverts, topo, off, ind = back.submesh()
+    np.testing.assert_array_equal(off, g["off_read"])
+    np.testing.assert_array_equal(ind, g["conn_read"])
+    np.testing.assert_allclose(back.nodal(expanded=False).ravel(), g["coords_read"], rtol=5e-6, atol=1e-12)
+    got = np.zeros(back.nc)
+    dg.chk(L.dVecLoadDHM(v, b"Vec_global_0", h2, dg.ptr(got), ctypes.c_int(0)))
+    np.testing.assert_array_equal(got, x)
+    if "loaded" in g:
+        np.testing.assert_allclose(got, g["loaded"], rtol=1e-12, atol=1e-15)
+    dg.chk(L.dViewerDestroy(ctypes.byref(v)))
+    del back
+    L.dMeshDestroy(ctypes.byref(mesh2))
