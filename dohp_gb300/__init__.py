@@ -89,10 +89,10 @@ class EFS:
     def __init__(self, h, jac):
         self.h, self._jac = h, jac
         P = np.zeros(3, np.int32); Q = np.zeros(3, np.int32)
-        chk(lib().dEFSGetTensorNodes(h, ptr(P), ptr(Q), None, None, None))
+        chk(lib().dEFSGetTensorTables(h, ptr(P), ptr(Q), None, None, None))
         self.P, self.Q = P.tolist(), Q.tolist()
         nodes = np.zeros(P.sum()); pts = np.zeros(Q.sum()); wts = np.zeros(Q.sum())
-        chk(lib().dEFSGetTensorNodes(h, ptr(P), ptr(Q), ptr(nodes), ptr(pts), ptr(wts)))
+        chk(lib().dEFSGetTensorTables(h, ptr(P), ptr(Q), ptr(nodes), ptr(pts), ptr(wts)))
         self.nodes, self.points, self.weights = nodes, pts, wts
 
     def apply(self, nelem, jinv, D, x, y, amode, imode=INSERT_VALUES, stream=None):

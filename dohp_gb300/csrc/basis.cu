@@ -150,8 +150,7 @@ int make_basis(int p, dQuadratureMethod method, Basis1D *b) {
   b->P = p + 1;
   b->Q = rule_1d(method, 2 * p, b->x, b->w);
   if (b->Q < 1 || b->Q > MAXQ) return set_error("rule size %d out of range", b->Q);
-  double wn[MAXP];
-  lobatto_rule(b->P, b->node, wn);
+  lobatto_rule(b->P, b->node, b->nodew);
   for (int i = 0; i < b->Q; i++) {
     lagrange(b->P, b->node, b->x[i], b->B + i * b->P, b->D + i * b->P);
     const double cn[2] = {-1.0, 1.0};

@@ -289,8 +289,7 @@ dErr jacobi_efs(dJacobi jac, const dInt degree[3], dQuadratureMethod method, con
       delete f;
       return set_error("rule size %d out of range", b.Q);
     }
-    double wn[MAXP];
-    lobatto_rule(b.P, b.node, wn);
+    lobatto_rule(b.P, b.node, b.nodew);
     for (int i = 0; i < b.Q; i++) lagrange(b.P, b.node, b.x[i], b.B + i * b.P, b.D + i * b.P);
     f->P[d] = b.P;
     f->Q[d] = b.Q;
@@ -326,9 +325,25 @@ dErr dEFSGetSizes(dEFS efs, dInt *dim, dInt *inodes, dInt *total) {
   return 0;
 }
 
-dErr dEFSGetTensorNodes(dEFS efs, dInt P[3], dInt Q[3], dReal *basis_nodes, dReal *rule_points, dReal *rule_weights) {
+// dEFSGetTensorNodes_Tensor_Hex (efstopo.c:260-290): pointers to the element's own 1-D tables
+dErr dEFSGetTensorNodes(dEFS efs, dInt *dim, dInt tsize[3], dReal *nodes[3], dReal *weight[3], const dReal *mscale[3],
+                        const dReal *lscale[3]) {
   if (!efs) return set_error("null EFS");
   if (efs->modal >= 0) return set_error("dEFSGetTensorNodes: a modal element has no tensor nodes");
+  if (mscale || lscale)
+    return set_error("dEFSGetTensorNodes: the Q1 mass / Laplacian scalings (mscale, lscale) are not provided; pass NULL");
+  if (dim) *dim = 3;
+  for (int d = 0; d < 3; d++) {
+    if (tsize) tsize[d] = efs->P[d];
+    if (nodes) nodes[d] = efs->b[d].node;
+    if (weight) weight[d] = efs->b[d].nodew;
+  }
+  return 0;
+}
+
+dErr dEFSGetTensorTables(dEFS efs, dInt P[3], dInt Q[3], dReal *basis_nodes, dReal *rule_points, dReal *rule_weights) {
+  if (!efs) return set_error("null EFS");
+  if (efs->modal >= 0) return set_error("dEFSGetTensorTables: a modal element has no tensor nodes");
   int op = 0, oq = 0;
   for (int d = 0; d < 3; d++) {
     if (P) P[d] = efs->P[d];

@@ -48,7 +48,7 @@ int rule_1d(dQuadratureMethod method, int order, double *x, double *w, int famil
 // 1-D tables for one basis degree p (P = p+1 GLL nodes) on a rule
 struct Basis1D {
   int P = 0, Q = 0;
-  double node[MAXP], x[MAXQ], w[MAXQ];
+  double node[MAXP], nodew[MAXP], x[MAXQ], w[MAXQ];  // GLL nodes and their weights; rule points and weights
   double B[MAXQ * MAXP];   // interp [Q][P]
   double D[MAXQ * MAXP];   // deriv [Q][P]
   double Dq[MAXQ * MAXQ];  // collocation derivative at the rule points [Q][Q] (FAST: Q == P)

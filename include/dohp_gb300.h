@@ -185,9 +185,15 @@ dErr dEFSGetExplicit(dEFS efs, const dReal jinv[], dInt *Q, dInt *P, const dReal
 dErr dEFSRestoreExplicit(dEFS efs, const dReal jinv[], dInt *Q, dInt *P, const dReal **basis, const dReal **deriv);
 /* dEFSGetSizes (include/dohpjacobi.h:172): dim, interior nodes, total nodes (a modal basis: its modes for both) */
 dErr dEFSGetSizes(dEFS efs, dInt *dim, dInt *inodes, dInt *total);
-/* dEFSGetTensorNodes / dRuleGetTensorNodeWeight: host copies of basis nodes, rule points, weights (a modal element:
- * an error, it has no nodes) */
-dErr dEFSGetTensorNodes(dEFS efs, dInt P[3], dInt Q[3], dReal *basis_nodes, dReal *rule_points, dReal *rule_weights);
+/* dEFSGetTensorNodes (include/dohpjacobi.h:174, src/jacobi/interface/jacobi.c:447-455, efstopo.c:260-290): dim (3),
+ * the nodes per direction tsize[3], and pointers (owned by the element space) to its GLL nodes and their weights per
+ * direction. mscale / lscale (the reference's tabulated Q1 mass and Laplacian scalings, which no reference caller
+ * reads) are not provided: pass NULL (else an error). A modal element: an error, it has no nodes. */
+dErr dEFSGetTensorNodes(dEFS efs, dInt *dim, dInt tsize[3], dReal *nodes[3], dReal *weight[3], const dReal *mscale[3],
+                        const dReal *lscale[3]);
+/* host copies of the basis nodes, rule points and rule weights, concatenated over the three directions (no reference
+ * counterpart: the rule's side of dEFSGetTensorNodes and dRuleGetTensorNodeWeight in one call) */
+dErr dEFSGetTensorTables(dEFS efs, dInt P[3], dInt Q[3], dReal *basis_nodes, dReal *rule_points, dReal *rule_weights);
 /* dEFSApply (include/dohpjacobi.h:177, src/jacobi/impls/tensor/efstopo.c:368-423) for ONE element:
  * device pointers; jinv NULL means reference coordinates (efstopo.c:565-568). On a modal element
  * (src/jacobi/impls/modal/modaltopo.c:73-126): INTERP, INTERP_TRANSPOSE and GRAD (reference-coordinate

@@ -229,7 +229,8 @@ def test_type_and_family_errors(L, jac):
     assert L.dJacobiGetEFS(jac, ctypes.c_int32(1), dg.ptr(topo), dg.ptr(ords), rl, ctypes.byref(arr)) != 0
     assert b"order 4" in L.dGetLastError()
     (m,) = get_efs(L, jac, [order(2)], [r])
-    assert L.dEFSGetTensorNodes(m, None, None, None, None, None) != 0
+    assert L.dEFSGetTensorNodes(m, None, None, None, None, None, None) != 0
+    assert L.dEFSGetTensorTables(m, None, None, None, None, None) != 0
     eidx, bi, bd, Pn = np.zeros(64, np.int32), np.zeros(512), np.zeros(1536), ctypes.c_int32()
     qidx = np.arange(8, dtype=np.int32)
     assert L.dEFSGetExplicitSparse(m, ctypes.c_int32(1), ctypes.c_int32(8), dg.ptr(qidx), None,
@@ -250,3 +251,21 @@ def test_type_and_family_errors(L, jac):
     assert b"tensor dJacobi" in L.dGetLastError()
     L.dFSDestroy(ctypes.byref(fs))
     L.dMeshDestroy(ctypes.byref(mesh))
+
+
+def test_tensor_nodes_with_the_reference_signature(L, jac):
+    """dEFSGetTensorNodes (jacobi.c:447-455, efstopo.c:260-290): dim, nodes per direction and the element's own GLL
+    nodes and weights per direction (jacobi/tests/ex1.c:138 reads them this way)"""
+    (r,) = get_rules(L, quad(L, jac, FAST), [order(0, 4, 6, 8)])
+    (efs,) = get_efs(L, jac, [order(0, 2, 3, 4)], [r])
+    dim, tsize = ctypes.c_int32(), (ctypes.c_int32 * 3)()
+    nodes, weights = (ctypes.POINTER(ctypes.c_double) * 3)(), (ctypes.POINTER(ctypes.c_double) * 3)()
+    dg.chk(L.dEFSGetTensorNodes(efs, ctypes.byref(dim), tsize, nodes, weights, None, None))
+    assert dim.value == 3 and list(tsize) == [3, 4, 5]
+    for d, P in enumerate(tsize):
+        x, w = po.lobatto(P)
+        np.testing.assert_allclose(np.ctypeslib.as_array(nodes[d], (P,)), x, rtol=0, atol=1e-15)
+        np.testing.assert_allclose(np.ctypeslib.as_array(weights[d], (P,)), w, rtol=1e-14)
+    ms = (ctypes.POINTER(ctypes.c_double) * 3)()
+    assert L.dEFSGetTensorNodes(efs, None, None, None, None, ms, None) != 0
+    assert b"pass NULL" in L.dGetLastError()
