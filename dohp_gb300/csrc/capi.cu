@@ -184,7 +184,8 @@ __global__ void k_modal_apply(int64_t nelem, int P, int Q, const double *interp,
 
 }  // namespace
 
-// the modal element's batched apply (dEFSApplyBatched on a modal dEFS); jinv is not used, as the reference's
+// the modal element's batched apply (dEFSApplyBatched on a modal dEFS); jinv is not used, as in the reference's
+// modal apply
 dErr efs_apply_modal(dEFS efs, int64_t nelem, int D, const double *in, double *out, dApplyMode amode, InsertMode imode,
                      cudaStream_t stream) {
   if (amode != dAPPLY_INTERP && amode != dAPPLY_INTERP_TRANSPOSE && amode != dAPPLY_GRAD)

@@ -197,7 +197,7 @@ dErr dEFSGetTensorTables(dEFS efs, dInt P[3], dInt Q[3], dReal *basis_nodes, dRe
 /* dEFSApply (include/dohpjacobi.h:177, src/jacobi/impls/tensor/efstopo.c:368-423) for ONE element:
  * device pointers; jinv NULL means reference coordinates (efstopo.c:565-568). On a modal element
  * (src/jacobi/impls/modal/modaltopo.c:73-126): INTERP, INTERP_TRANSPOSE and GRAD (reference-coordinate
- * derivatives, jinv unused), GRAD_TRANSPOSE is an error; values are [P][D] per element for modes. */
+ * derivatives, jinv unused), GRAD_TRANSPOSE is an error; values are [P][D] per element for modes, D <= 4096. */
 dErr dEFSApply(dEFS efs, const dReal *jinv, dInt D, const dScalar *in, dScalar *out, dApplyMode amode, InsertMode imode);
 /* Batched dEFSApply over nelem elements stored back to back (element stride = the mode's in/out size),
  * jinv strided by 9*Q per element (or NULL). stream: cudaStream_t or NULL. */
