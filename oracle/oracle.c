@@ -1013,6 +1013,8 @@ static void expanded_coords(or_fs *m)
       for (int d = 0; d < 3; d++) m->xexp[(r * 8 + i) * 3 + d] = m->vx[3 * m->hconn[8 * r + connidx[i]] + d];
 }
 
+static or_fs *fs_build(or_fs *m, int degree, const int *elem_degree, int dirichlet_mask);
+
 or_fs *or_fs_create(int nx, int ny, int nz, const double box[6], double perturb, uint64_t seed,
                     int degree, const int *elem_degree, int bs, int dirichlet_mask)
 {
@@ -1021,7 +1023,15 @@ or_fs *or_fs_create(int nx, int ny, int nz, const double box[6], double perturb,
   m->nx = nx; m->ny = ny; m->nz = nz; m->bs = bs;
   m->hp = elem_degree != NULL;
   for (int p = 1; p < 16; p++) { double w[16]; or_lobatto(p + 1, m->gll[p], w); }
-  if (build_mesh(m, box, perturb, seed) || build_adjacency(m) || propagate_degree(m, degree, elem_degree)) { or_fs_destroy(m); return NULL; }
+  if (build_mesh(m, box, perturb, seed) || build_adjacency(m)) { or_fs_destroy(m); return NULL; }
+  return fs_build(m, degree, elem_degree, dirichlet_mask);
+}
+
+/* The space on a mesh with its adjacency (dFSBuildSpace: cont.c:93-385, fsbuild.c:55-146): degree propagation,
+ * explicit / Dirichlet partition with natural ordering, E, expanded coordinates. Frees m on error. */
+static or_fs *fs_build(or_fs *m, int degree, const int *elem_degree, int dirichlet_mask)
+{
+  if (propagate_degree(m, degree, elem_degree)) { or_fs_destroy(m); return NULL; }
   /* boundary face sets 0..3 -> 100 (walls), 5 -> 200 (top), 4 -> 300 (bottom) (genblock.c:409-421) */
   const int set_of_face[6] = {0, 0, 0, 0, 2, 1};
   m->ordered = malloc(sizeof(int32_t) * m->nents);
@@ -1096,6 +1106,95 @@ void or_fs_set_vertex_coords(or_fs *m, const double *vx)
 {
   memcpy(m->vx, vx, sizeof(double) * 3 * m->nv);
   expanded_coords(m);
+}
+
+/* dMeshGetAdjacency (mesh.c:1074-1191) for a mesh given by its entities: each canonical side of a face (CN_QL) is the
+ * edge with the same two vertices, each side of a hexahedron (CN_HQ) the face with the same four, and the orientation
+ * is the rotation / reflection that carries one onto the other (a search over all entities: small meshes only). */
+static int build_adjacency_search(or_fs *m)
+{
+  static const int hq_perm[8][4] = {{0, 1, 2, 3}, {3, 0, 1, 2}, {2, 3, 0, 1}, {1, 2, 3, 0}, {0, 3, 2, 1}, {1, 0, 3, 2}, {2, 1, 0, 3}, {3, 2, 1, 0}};
+  const int64_t E0 = m->nv, F0 = m->nv + m->ne, R0 = m->nv + m->ne + m->nf;
+  const int64_t nadj = 2 * m->ne + 4 * m->nf + 6 * m->nr;
+  m->adjoff = malloc(sizeof(int32_t) * (m->nents + 1));
+  m->adjind = malloc(sizeof(int32_t) * nadj);
+  m->adjperm = malloc(sizeof(int32_t) * nadj);
+  int64_t a = 0;
+  for (int64_t v = 0; v < m->nv; v++) m->adjoff[v] = 0;
+  for (int64_t e = 0; e < m->ne; e++) {
+    m->adjoff[E0 + e] = (int32_t)a;
+    for (int s = 0; s < 2; s++) { m->adjind[a] = (int32_t)m->econn[2 * e + s]; m->adjperm[a] = 0; a++; }
+  }
+  for (int64_t f = 0; f < m->nf; f++) {
+    m->adjoff[F0 + f] = (int32_t)a;
+    const int64_t *fv = m->fconn + 4 * f;
+    for (int s = 0; s < 4; s++) {
+      const int64_t v0 = fv[CN_QL[s][0]], v1 = fv[CN_QL[s][1]];
+      int64_t found = -1;
+      int perm = 0;
+      for (int64_t e = 0; e < m->ne && found < 0; e++) {
+        const int64_t *ev = m->econn + 2 * e;
+        if (ev[0] == v0 && ev[1] == v1) found = e, perm = 0;
+        else if (ev[0] == v1 && ev[1] == v0) found = e, perm = 1;
+      }
+      if (found < 0) return or_fail("Edges cannot be matched (face %lld side %d)", (long long)f, s);
+      m->adjind[a] = (int32_t)(E0 + found);
+      m->adjperm[a] = perm;
+      a++;
+    }
+  }
+  for (int64_t r = 0; r < m->nr; r++) {
+    m->adjoff[R0 + r] = (int32_t)a;
+    const int64_t *rv = m->hconn + 8 * r;
+    for (int s = 0; s < 6; s++) {
+      int64_t found = -1;
+      int perm = -1;
+      for (int64_t f = 0; f < m->nf && found < 0; f++) {
+        const int64_t *fv = m->fconn + 4 * f;
+        for (int p = 0; p < 8; p++) {
+          int same = 1;
+          for (int c = 0; c < 4; c++) same = same && fv[hq_perm[p][c]] == rv[CN_HQ[s][c]];
+          if (same) { found = f; perm = p; break; }
+        }
+      }
+      if (found < 0) return or_fail("Face (Quad) cannot be matched to region (Hex) %lld side %d", (long long)r, s);
+      m->adjind[a] = (int32_t)(F0 + found);
+      m->adjperm[a] = perm;
+      a++;
+    }
+  }
+  m->adjoff[m->nents] = (int32_t)a;
+  return 0;
+}
+
+or_fs *or_fs_create_conn(int nv, const double *vtx, int ne, const int *econn, int nf, const int *fconn, int nr,
+                         const int *hconn, int degree, const int *elem_degree, int bs)
+{
+  or_fs *m = calloc(1, sizeof(or_fs));
+  m->bs = bs;
+  m->hp = elem_degree != NULL;
+  for (int p = 1; p < 16; p++) { double w[16]; or_lobatto(p + 1, m->gll[p], w); }
+  m->nv = nv; m->ne = ne; m->nf = nf; m->nr = nr;
+  m->nents = m->nv + m->ne + m->nf + m->nr;
+  m->vx = malloc(sizeof(double) * 3 * nv);
+  memcpy(m->vx, vtx, sizeof(double) * 3 * nv);
+  m->econn = malloc(sizeof(int64_t) * 2 * ne);
+  m->fconn = malloc(sizeof(int64_t) * 4 * nf);
+  m->hconn = malloc(sizeof(int64_t) * 8 * nr);
+  for (int64_t i = 0; i < 2 * (int64_t)ne; i++) m->econn[i] = econn[i];
+  for (int64_t i = 0; i < 4 * (int64_t)nf; i++) m->fconn[i] = fconn[i];
+  for (int64_t i = 0; i < 8 * (int64_t)nr; i++) m->hconn[i] = hconn[i];
+  m->fset = malloc(m->nents);
+  memset(m->fset, -1, m->nents); /* no boundary sets */
+  if (build_adjacency_search(m)) { or_fs_destroy(m); return NULL; }
+  return fs_build(m, degree, elem_degree, 0);
+}
+
+const int32_t *or_fs_adjacency(const or_fs *m, const int32_t **adjind, const int32_t **adjperm)
+{
+  if (adjind) *adjind = m->adjind;
+  if (adjperm) *adjperm = m->adjperm;
+  return m->adjoff;
 }
 
 void or_fs_destroy(or_fs *m)

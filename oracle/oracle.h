@@ -74,6 +74,13 @@ typedef struct or_fs or_fs;
 or_fs *or_fs_create(int nx, int ny, int nz, const double box[6], double perturb, uint64_t seed,
                     int degree, const int *elem_degree, int bs, int dirichlet_mask);
 void or_fs_destroy(or_fs *fs);
+/* The same space on a mesh given by its entities (vertices [nv][3], edges [ne][2], quadrilaterals [nf][4], hexahedra
+ * [nr][8] in ITAPS order, each in creation order; the hand-built meshes of src/fs/tests/ex1.c, cunit.c, fsex4.c):
+ * adjacency by vertex matching, no boundary sets. */
+or_fs *or_fs_create_conn(int nv, const double *vtx, int ne, const int *econn, int nf, const int *fconn, int nr,
+                         const int *hconn, int degree, const int *elem_degree, int bs);
+/* adjoff [nents+1]; adjind / adjperm as dMeshGetAdjacency (mesh.c:1074-1191) */
+const int32_t *or_fs_adjacency(const or_fs *fs, const int32_t **adjind, const int32_t **adjperm);
 const char *or_last_error(void);
 /* sizes: [0]=nelem [1]=n explicit nodes [2]=nc closure nodes [3]=nexp expanded nodes [4]=bs
  *        [5]=nverts [6]=nedges [7]=nfaces */

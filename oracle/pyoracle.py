@@ -59,6 +59,11 @@ def lib():
         L.or_fs_create.argtypes = [ctypes.c_int] * 3 + [_f64p, ctypes.c_double, ctypes.c_uint64, ctypes.c_int,
                                    ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         L.or_fs_destroy.argtypes = [ctypes.c_void_p]
+        L.or_fs_create_conn.restype = ctypes.c_void_p
+        L.or_fs_create_conn.argtypes = [ctypes.c_int, _f64p, ctypes.c_int, _i32p, ctypes.c_int, _i32p, ctypes.c_int, _i32p,
+                                        ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+        L.or_fs_adjacency.restype = ctypes.POINTER(ctypes.c_int32)
+        L.or_fs_adjacency.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.or_last_error.restype = ctypes.c_char_p
         L.or_fs_sizes.argtypes = [ctypes.c_void_p, _i64p]
         for name in ("or_fs_emap", "or_fs_xstart", "or_fs_elem_degree"):
@@ -243,15 +248,22 @@ class FS:
     """Oracle function space on a structured block mesh (see oracle.h or_fs_create)."""
 
     def __init__(self, nx, ny, nz, degree=4, box=(0, 1, 0, 1, 0, 1), perturb=0.1, seed=1, bs=1,
-                 dirichlet_mask=7, elem_degree=None):
+                 dirichlet_mask=7, elem_degree=None, conn=None):
+        """conn: (vtx [nv][3], econn [ne][2], fconn [nf][4], hconn [nr][8]) for a mesh given by its entities
+        (or_fs_create_conn, no boundary sets); nx, ny, nz, box, perturb, seed and dirichlet_mask are then unused"""
         L = lib()
         ed = None
         self._ed = None
         if elem_degree is not None:
             self._ed = np.ascontiguousarray(elem_degree, dtype=np.int32)
             ed = self._ed.ctypes.data
-        self.h = L.or_fs_create(nx, ny, nz, np.asarray(box, dtype=np.float64), perturb, seed, degree, ed, bs,
-                                dirichlet_mask)
+        if conn is not None:
+            v = np.ascontiguousarray(conn[0], np.float64).reshape(-1, 3)
+            e, f, r = [np.ascontiguousarray(c, np.int32).ravel() for c in conn[1:]]
+            self.h = L.or_fs_create_conn(len(v), v, len(e) // 2, e, len(f) // 4, f, len(r) // 8, r, degree, ed, bs)
+        else:
+            self.h = L.or_fs_create(nx, ny, nz, np.asarray(box, dtype=np.float64), perturb, seed, degree, ed, bs,
+                                    dirichlet_mask)
         if not self.h:
             raise RuntimeError("oracle fs: " + L.or_last_error().decode())
         s = np.zeros(8, dtype=np.int64)
@@ -266,6 +278,14 @@ class FS:
 
     def emap(self):
         return np.ctypeslib.as_array(lib().or_fs_emap(self.h), shape=(self.nexp,)).copy()
+
+    def adjacency(self):
+        """(adjoff, adjind, adjperm) as dMeshGetAdjacency"""
+        ai, ap = ctypes.POINTER(ctypes.c_int32)(), ctypes.POINTER(ctypes.c_int32)()
+        ao = lib().or_fs_adjacency(self.h, ctypes.byref(ai), ctypes.byref(ap))
+        adjoff = np.ctypeslib.as_array(ao, shape=(self.nents + 1,)).copy()
+        na = int(adjoff[-1])
+        return adjoff, np.ctypeslib.as_array(ai, shape=(na,)).copy(), np.ctypeslib.as_array(ap, shape=(na,)).copy()
 
     def ecsr(self):
         p = ctypes.POINTER(ctypes.c_int64)(); c = ctypes.POINTER(ctypes.c_int32)(); v = ctypes.POINTER(ctypes.c_double)()
