@@ -2,13 +2,15 @@
 hand-built two-hex mesh (dMeshCreateFromConnectivity), through the product's device expand / restrict and batched
 dRulesetIterator, against the printed numbers: useFS's sums, the first SNES function norm (the projection residual at
 zero) and, after solving the projection, the pointwise value and gradient residual norms (ProjResidualNorms,
-ex1.c:484-530)."""
+ex1.c:484-530); fs-mf-projection-v3 prints the same numbers as -v1. The operator apply on the hand-built meshes of
+ex1.c and fsex4.c against the oracle's (its own mesh from the same entities) at 1e-12."""
 import os
 
 import numpy as np
 import pytest
 
 import dohp_gb300 as dg
+import pyoracle as po
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -104,3 +106,35 @@ def test_ex1_projection(name, degree, method, freq):
     gw = [(gr * jw).sum().item(), torch.sqrt((gr ** 2 * jw).sum()).item(), gr.max().item()]
     np.testing.assert_allclose(pw, g["pointwise"], rtol=6e-3)
     np.testing.assert_allclose(gw, g["gradient"], rtol=6e-3)
+
+
+@pytest.mark.parametrize("prefix,vtx", [("ex1_", "ex1_vtx_parametric"), ("fsex4_", "fsex4_vtx")])
+def test_operator_apply_against_the_oracle(prefix, vtx):
+    """EllipShellMatMult / ElastShellMatMult on meshes given by their entities (no boundary sets): diffusion at
+    degrees 1, 3, 6, 8 and with per-element degrees 2..8 (the hp form), linear elasticity at degree 3, each against
+    the oracle's apply of the same input at 1e-12"""
+    hm = gold("hex_meshes")
+    conn = (hm[vtx], hm[prefix + "econn"], hm[prefix + "fconn"], hm[prefix + "rconn"])
+    mesh = dg.Mesh(*conn)
+    rng = np.random.default_rng(5)
+    nr = len(conn[3]) // 8
+
+    def check(fs, o, op, kind=0, param=None):
+        x = rng.uniform(-1, 1, fs.n * fs.bs)
+        y = torch.zeros(fs.n * fs.bs, dtype=torch.float64, device="cuda")
+        op.mult(torch.as_tensor(x, device="cuda"), y)
+        torch.cuda.synchronize()
+        ref = o.apply(x, kind=kind, param=param)
+        err = np.linalg.norm(y.cpu().numpy() - ref) / np.linalg.norm(ref)
+        assert err < 1e-12, err
+
+    for degree in (1, 3, 6, 8):
+        fs = dg.FS(None, degree=degree, dirichlet=(), mesh=mesh)
+        check(fs, po.FS(0, 0, 0, degree=degree, conn=conn), fs.operator())
+    ed = rng.integers(2, 9, size=nr).astype(np.int32)
+    fs = dg.FS(None, degree=8, dirichlet=(), mesh=mesh, elem_degree=ed)
+    check(fs, po.FS(0, 0, 0, degree=8, elem_degree=ed, conn=conn), fs.operator())
+    E0, NU = 1.0, 0.3
+    fs = dg.FS(None, degree=3, bs=3, dirichlet=(), mesh=mesh)
+    check(fs, po.FS(0, 0, 0, degree=3, bs=3, conn=conn), fs.operator(dg.dOP_ELASTICITY, param=(E0, NU)), kind=2,
+          param=np.array([E0 * NU / ((1 + NU) * (1 - 2 * NU)), E0 / (2 * (1 + NU))]))
