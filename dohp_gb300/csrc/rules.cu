@@ -22,6 +22,10 @@ using namespace dgb;
 struct _p_dRule {
   dQuadratureMethod method;
   int family = dGAUSS_LEGENDRE;  // point family (dQuadratureTensorSetGaussFamily)
+  // facet rules (dQuadratureGetFacetRules): side 0..5 of the hex, else -1; the 2-D rule's points (X, Y, 0) are mapped
+  // by xi = R (X, Y, 0) + t (the reference's transformed rules, tensorquad.c:224-242)
+  int facet = -1;
+  double R[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}}, t[3] = {0, 0, 0};
   int order[3];  // polynomial order integrated exactly, per direction
   int Q[3];
   double x[3][MAXQ], w[3][MAXQ];
@@ -84,6 +88,54 @@ dErr quad_rule(_p_dQuadrature *q, const int order[3], int family, _p_dRule **out
     r->Q[d] = n;
     std::copy(x, x + n, r->x[d]);
     std::copy(w, w + n, r->w[d]);
+  }
+  q->rules[key] = r;
+  *out = r;
+  return 0;
+}
+
+// the facet rule of a side and per-direction orders: a tensor rule on [-1,1]^2 (its third direction one point of
+// weight 1 at 0), mapped by the side's rotation and translation (dQuadratureGetFacetRules_Tensor_Private,
+// tensorquad.c:309-355: rotations and translations as the reference tabulates them; table as reference). The face
+// rule's two orders are formed as the reference does, from the rows of the rotation (a direction's degree where
+// the row is nonzero); for isotropic orders, the ones its callers pass, that is the order itself.
+dErr quad_facet_rule(_p_dQuadrature *q, int facet, const int order[3], int family, _p_dRule **out) {
+  static const double kR[6][3][3] = {{{1, 0, 0}, {0, 0, -1}, {0, 1, 0}},  {{0, 0, 1}, {1, 0, 0}, {0, 1, 0}},
+                                     {{-1, 0, 0}, {0, 0, 1}, {0, 1, 0}},  {{0, 0, -1}, {-1, 0, 0}, {0, 1, 0}},
+                                     {{0, 1, 0}, {1, 0, 0}, {0, 0, -1}},  {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}}};
+  static const double kT[6][3] = {{0, -1, 0}, {1, 0, 0}, {0, 1, 0}, {-1, 0, 0}, {0, 0, -1}, {0, 0, 1}};
+  if (facet < 0 || facet > 5) return set_error("facet %d of a hexahedron out of range 0..5", facet);
+  int rot[2];
+  for (int i = 0; i < 2; i++) {
+    rot[i] = 0;
+    for (int j = 0; j < 3; j++) rot[i] += kR[facet][i][j] != 0 ? order[j] : 0;
+  }
+  std::vector<int> key = {family, rot[0], rot[1], 0, 100 + facet};
+  auto it = q->rules.find(key);
+  if (it != q->rules.end()) {
+    *out = it->second;
+    return 0;
+  }
+  _p_dRule *r = new _p_dRule();
+  r->method = q->method;
+  r->family = family;
+  r->facet = facet;
+  for (int d = 0; d < 2; d++) {
+    double x[64], w[64];
+    const int n = rule_1d(q->method, rot[d], x, w, family);
+    if (n < 1 || n > MAXQ) {
+      delete r;
+      return set_error("facet rule of order %d has %d points (at most %d supported)", rot[d], n, MAXQ);
+    }
+    r->order[d] = rot[d];
+    r->Q[d] = n;
+    std::copy(x, x + n, r->x[d]);
+    std::copy(w, w + n, r->w[d]);
+  }
+  r->order[2] = 0, r->Q[2] = 1, r->x[2][0] = 0, r->w[2][0] = 1;
+  for (int i = 0; i < 3; i++) {
+    r->t[i] = kT[facet][i];
+    for (int j = 0; j < 3; j++) r->R[i][j] = kR[facet][i][j];
   }
   q->rules[key] = r;
   *out = r;
@@ -221,15 +273,36 @@ dErr dQuadratureTensorSetGaussFamily(dQuadrature quad, dGaussFamily family) {
   return 0;
 }
 
+dErr dQuadratureGetFacetRules(dQuadrature quad, dInt n, const dEntTopology topo[], const dInt facet[], const dPolynomialOrder order[],
+                              dRule **rules) {
+  if (!quad || !rules || (n > 0 && (!topo || !facet || !order))) return set_error("null argument");
+  *rules = nullptr;
+  dRule *arr = (dRule *)malloc(sizeof(dRule) * (size_t)std::max<dInt>(n, 1));
+  if (!arr) return set_error("out of host memory");
+  for (dInt i = 0; i < n; i++) {
+    dErr e = 0;
+    if (topo[i] != dTOPO_HEX) e = set_error("dQuadratureGetFacetRules: unsupported topology %d (hexahedra only)", (int)topo[i]);
+    const int o[3] = {dPolynomialOrder1D(order[i], 0), dPolynomialOrder1D(order[i], 1), dPolynomialOrder1D(order[i], 2)};
+    if (!e) e = quad_facet_rule(quad, facet[i], o, quad->family, &arr[i]);
+    if (e) {
+      free(arr);
+      return e;
+    }
+  }
+  *rules = arr;
+  return 0;
+}
+
 dErr dRuleGetSize(dRule rule, dInt *dim, dInt *nnodes) {
   if (!rule) return set_error("null rule");
-  if (dim) *dim = 3;
+  if (dim) *dim = rule->facet >= 0 ? 2 : 3;
   if (nnodes) *nnodes = rule->Q[0] * rule->Q[1] * rule->Q[2];
   return 0;
 }
 
 dErr dRuleGetTensorNodeWeight(dRule rule, dInt *dim, dInt nnodes[3], const dReal *coord[3], const dReal *weight[3]) {
   if (!rule) return set_error("null rule");
+  if (rule->facet >= 0) return set_error("dRuleGetTensorNodeWeight: a facet rule has no tensor form in the element's directions");
   if (dim) *dim = 3;
   for (int d = 0; d < 3; d++) {
     if (nnodes) nnodes[d] = rule->Q[d];
@@ -246,7 +319,13 @@ dErr dRuleGetNodeWeight(dRule rule, dReal *coord, dReal *weight) {
     for (int j = 0; j < Q[1]; j++)
       for (int k = 0; k < Q[2]; k++) {
         const int q = (i * Q[1] + j) * Q[2] + k;
-        if (coord) coord[3 * q] = rule->x[0][i], coord[3 * q + 1] = rule->x[1][j], coord[3 * q + 2] = rule->x[2][k];
+        const double X[3] = {rule->x[0][i], rule->x[1][j], rule->x[2][k]};
+        if (coord) {
+          if (rule->facet >= 0)  // dRuleGetNodeWeight_Transformed (tensorquad.c:224-242)
+            for (int c = 0; c < 3; c++) coord[3 * q + c] = rule->R[c][0] * X[0] + rule->R[c][1] * X[1] + rule->R[c][2] * X[2] + rule->t[c];
+          else
+            coord[3 * q] = X[0], coord[3 * q + 1] = X[1], coord[3 * q + 2] = X[2];
+        }
         if (weight) weight[q] = rule->w[0][i] * rule->w[1][j] * rule->w[2][k];
       }
   return 0;
@@ -322,6 +401,8 @@ dErr dJacobiGetEFS(dJacobi jac, dInt n, const dEntTopology topo[], const dPolyno
     dErr e;
     if (jac->modal) {  // dJacobiGetEFS_Modal (modal.c:343-370): the total order of the degree
       e = jacobi_efs_modal(jac, dPolynomialOrderMax(order[i]), rules[i], &arr[i]);
+    } else if (rules[i]->facet >= 0) {
+      e = set_error("dJacobiGetEFS: tensor element spaces on facet rules are not built (dFacetIterator evaluates faces)");
     } else {
       const dInt deg[3] = {dPolynomialOrder1D(order[i], 0), dPolynomialOrder1D(order[i], 1), dPolynomialOrder1D(order[i], 2)};
       e = jacobi_efs(jac, deg, rules[i]->method, rules[i]->order, &arr[i], rules[i]->family);

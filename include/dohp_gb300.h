@@ -406,6 +406,14 @@ dErr dRulesetIteratorErrorNorms(dRulesetIterator it, const dScalar *exact_u, con
  * 0: y=-1, 1: x=+1, 2: y=+1, 3: x=-1, 4: z=-1, 5: z=+1; R_side's third column is the outward normal.
  * nodes [n][3], weights [n]; room for 81 nodes covers orders up to 16 (FAST). Host only. */
 dErr dFSGetFacetRule(dInt side, dQuadratureMethod method, dInt order, dInt *nnodes, dReal *nodes, dReal *weights);
+/* dQuadratureGetFacetRules (include/dohpjacobi.h:210, tensorquad.c:309-355) with the reference's arguments: *rules = a
+ * new array (dFree) of n facet rules, facet[i] the side of the hex topo[i] (hexahedra only) in the order above, owned by
+ * the quadrature: dRuleGetSize gives dim 2 and the face's points, dRuleGetNodeWeight the points on the side in
+ * reference coordinates (as dFSGetFacetRule) with their face weights, dRuleGetPatches one patch (FAST) or the 2 x 2
+ * blocks (SPARSE). The face orders come from the rows of the side's rotation as in the reference (the same for
+ * isotropic orders). dRuleGetTensorNodeWeight and tensor element spaces (dJacobiGetEFS) are refused on them. */
+dErr dQuadratureGetFacetRules(dQuadrature quad, dInt n, const dEntTopology topo[], const dInt facet[], const dPolynomialOrder order[],
+                              dRule **rules);
 /* Batched facet iterator over the faces of the sets registered with dFSBSTATUS_WEAK (the reference's weakFace set,
  * src/fs/interface/fsbuild.c:87-90), the boundary analogue of the dRulesetIterator: FAST rules (p+1 Gauss points
  * per face direction, order 2p as the volume rule), facets in (element, side) order, points X-major per facet.

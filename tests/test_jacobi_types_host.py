@@ -269,3 +269,42 @@ def test_tensor_nodes_with_the_reference_signature(L, jac):
     ms = (ctypes.POINTER(ctypes.c_double) * 3)()
     assert L.dEFSGetTensorNodes(efs, None, None, None, None, ms, None) != 0
     assert b"pass NULL" in L.dGetLastError()
+
+
+def test_facet_rules_with_the_reference_arguments(L, jac):
+    """dQuadratureGetFacetRules (tensorquad.c:309-355): for every side of the hex and isotropic orders, the facet rule's
+    points and weights are those of dFSGetFacetRule and of the oracle's restatement; dim 2; cached per (side, orders);
+    tensor element spaces and tensor node queries are refused on facet rules; a side out of range is an error"""
+    q = quad(L, jac, FAST)
+    for order_ in (2, 4, 6):
+        sides = np.arange(6, dtype=np.int32)
+        topo, ords = np.full(6, HEX, np.int32), np.full(6, order(order_), np.int32)
+        arr = ctypes.POINTER(ctypes.c_void_p)()
+        dg.chk(L.dQuadratureGetFacetRules(q, ctypes.c_int32(6), dg.ptr(topo), dg.ptr(sides), dg.ptr(ords), ctypes.byref(arr)))
+        rules = [ctypes.c_void_p(arr[i]) for i in range(6)]
+        dg.chk(L.dFree(arr))
+        for side, r in enumerate(rules):
+            dim, nn = ctypes.c_int32(), ctypes.c_int32()
+            dg.chk(L.dRuleGetSize(r, ctypes.byref(dim), ctypes.byref(nn)))
+            assert dim.value == 2 and nn.value == (1 + order_ // 2) ** 2
+            pts, w = node_weight(L, r)
+            n_ref, w_ref = dg.facet_rule(side, order_)
+            np.testing.assert_array_equal(pts, n_ref.reshape(-1, 3))
+            np.testing.assert_array_equal(w, w_ref)
+            no, wo = po.facet_rule(side, order_)
+            np.testing.assert_allclose(pts, no.reshape(-1, 3), rtol=0, atol=1e-15)
+            np.testing.assert_allclose(w, wo, rtol=1e-14)
+            npch, psz = ctypes.c_int32(), ctypes.c_int32()
+            dg.chk(L.dRuleGetPatches(r, ctypes.byref(npch), ctypes.byref(psz), None, None))
+            assert (npch.value, psz.value) == (1, nn.value)
+        again = ctypes.POINTER(ctypes.c_void_p)()
+        dg.chk(L.dQuadratureGetFacetRules(q, ctypes.c_int32(6), dg.ptr(topo), dg.ptr(sides), dg.ptr(ords), ctypes.byref(again)))
+        assert [again[i] for i in range(6)] == [r.value for r in rules]
+        dg.chk(L.dFree(again))
+    assert L.dRuleGetTensorNodeWeight(rules[0], None, None, None, None) != 0
+    rl = (ctypes.c_void_p * 1)(rules[0].value)
+    topo1, ord1 = np.array([HEX], np.int32), np.array([order(2)], np.int32)
+    assert L.dJacobiGetEFS(jac, ctypes.c_int32(1), dg.ptr(topo1), dg.ptr(ord1), rl, ctypes.byref(arr)) != 0
+    assert b"facet rules" in L.dGetLastError()
+    bad = np.array([6], np.int32)
+    assert L.dQuadratureGetFacetRules(q, ctypes.c_int32(1), dg.ptr(topo1), dg.ptr(bad), dg.ptr(ord1), ctypes.byref(arr)) != 0
