@@ -416,6 +416,41 @@ dErr dJacobiGetEFS(dJacobi jac, dInt n, const dEntTopology topo[], const dPolyno
   return 0;
 }
 
+// dJacobiGetNodeCount (jacobi.c:254-264): interior and expanded node counts per entity. Tensor type
+// (dJacobiGetNodeCount_Tensor, tensor.c:249-281): interior prod max(0, p_d - 1), expanded prod (p_d + 1) over the
+// entity's directions (hexahedron 3, quadrilateral 2, line 1, point: 1 and 1). Modal type (modal.c:297-310): the
+// modes of the total order, both counts (ModalPCount; regions only, as this library's modal spaces).
+dErr dJacobiGetNodeCount(dJacobi jac, dInt count, const dEntTopology top[], const dPolynomialOrder deg[], dInt inode[], dInt xnode[]) {
+  if (!jac || (count > 0 && (!top || !deg))) return set_error("null argument");
+  for (dInt i = 0; i < count; i++) {
+    if (jac->modal) {
+      const int o = dPolynomialOrderMax(deg[i]);
+      if (top[i] != dTOPO_HEX) return set_error("dJacobiGetNodeCount: modal bases on topology %d not built (hexahedra only)", (int)top[i]);
+      if (o < 0 || o > 3) return set_error("Order %d for type region", o);
+      if (inode) inode[i] = kModalCount[o];
+      if (xnode) xnode[i] = kModalCount[o];
+      continue;
+    }
+    int dims;
+    switch (top[i]) {
+      case dTOPO_HEX: dims = 3; break;
+      case dTOPO_QUAD: dims = 2; break;
+      case dTOPO_LINE: dims = 1; break;
+      case dTOPO_POINT: dims = 0; break;
+      default: return set_error("Topology %d not supported", (int)top[i]);
+    }
+    int ic = 1, xc = 1;
+    for (int d = 0; d < dims; d++) {
+      const int p = dPolynomialOrder1D(deg[i], d);
+      ic *= std::max(0, p - 1);
+      xc *= p + 1;
+    }
+    if (inode) inode[i] = ic;
+    if (xnode) xnode[i] = xc;
+  }
+  return 0;
+}
+
 dErr dJacobiSetType(dJacobi jac, const char *type) {
   if (!jac || !type) return set_error("null argument");
   if (!strcmp(type, dJACOBI_TENSOR)) jac->modal = 0;

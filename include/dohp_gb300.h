@@ -134,6 +134,11 @@ dErr dJacobiGetType(dJacobi jac, const char **type);
 /* dJacobiModalSetFamily (modal.c:273-281, 413-418): only dJACOBI_MODAL_P_DISCONTINUOUS is built; another family is
  * an error on a modal dJacobi. On a tensor dJacobi the call does nothing, as the reference's PetscTryMethod. */
 dErr dJacobiModalSetFamily(dJacobi jac, dJacobiModalFamily family);
+/* dJacobiGetNodeCount (include/dohpjacobi.h:183, src/jacobi/interface/jacobi.c:254-264): per entity of topology top[i]
+ * and degree deg[i], its interior nodes inode[i] and expanded nodes xnode[i] (either may be NULL). Tensor type:
+ * prod max(0, p_d - 1) and prod (p_d + 1) over the entity's directions (tensor.c:249-281); modal type: the modes of
+ * the total order for both (hexahedra). */
+dErr dJacobiGetNodeCount(dJacobi jac, dInt count, const dEntTopology top[], const dPolynomialOrder deg[], dInt inode[], dInt xnode[]);
 /* release an array the library allocated for the caller (dQuadratureGetRules, dJacobiGetEFS), as dohp's dFree */
 dErr dFree(void *ptr);
 /* dJacobiGetQuadrature (include/dohpjacobi.h:170, src/jacobi/interface/jacobi.c:268-285): the dJacobi's quadrature

@@ -308,3 +308,26 @@ def test_facet_rules_with_the_reference_arguments(L, jac):
     assert b"facet rules" in L.dGetLastError()
     bad = np.array([6], np.int32)
     assert L.dQuadratureGetFacetRules(q, ctypes.c_int32(1), dg.ptr(topo1), dg.ptr(bad), dg.ptr(ord1), ctypes.byref(arr)) != 0
+
+
+def test_node_counts(L, jac):
+    """dJacobiGetNodeCount (tensor.c:249-281, modal.c:297-310): interior and expanded nodes per entity; against the sizes
+    of the element spaces the dJacobi makes and of a built space's closure"""
+    topo = np.array([HEX, HEX, 4, 1, 0], np.int32)  # hexahedron, quadrilateral, line, point
+    deg = np.array([order(0, 2, 3, 4), order(5), order(0, 3, 2, 2), order(4), order(4)], np.int32)
+    ino, xno = np.zeros(5, np.int32), np.zeros(5, np.int32)
+    dg.chk(L.dJacobiGetNodeCount(jac, ctypes.c_int32(5), dg.ptr(topo), dg.ptr(deg), dg.ptr(ino), dg.ptr(xno)))
+    np.testing.assert_array_equal(ino, [1 * 2 * 3, 4 ** 3, 2 * 1, 3, 1])
+    np.testing.assert_array_equal(xno, [3 * 4 * 5, 6 ** 3, 4 * 3, 5, 1])
+    (r,) = get_rules(L, quad(L, jac, FAST), [order(10)])
+    (efs,) = get_efs(L, jac, [order(5)], [r])
+    dim, inodes, total = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    dg.chk(L.dEFSGetSizes(efs, ctypes.byref(dim), ctypes.byref(inodes), ctypes.byref(total)))
+    assert (inodes.value, total.value) == (ino[1], xno[1])
+    bad, deg1 = np.array([6], np.int32), deg[:1].copy()
+    assert L.dJacobiGetNodeCount(jac, ctypes.c_int32(1), dg.ptr(bad), dg.ptr(deg1), None, None) != 0
+    set_type(L, jac, "modal")
+    mdeg, mtopo = np.array([order(i) for i in range(4)], np.int32), np.full(4, HEX, np.int32)
+    dg.chk(L.dJacobiGetNodeCount(jac, ctypes.c_int32(4), dg.ptr(mtopo), dg.ptr(mdeg), dg.ptr(ino), dg.ptr(xno)))
+    np.testing.assert_array_equal(ino[:4], [1, 4, 10, 18])
+    np.testing.assert_array_equal(xno[:4], [1, 4, 10, 18])
